@@ -1,0 +1,186 @@
+/*
+ * pythia_gpu.h — C ABI of the GB300 (sm_103a) execution path for Pythia's
+ * data-parallel operators: radix/range partitioning, hash-join build and
+ * probe, group-by aggregate_sum / aggregate_count, the page sort and the
+ * MPSM sort-merge join.
+ *
+ * Plain C: pointers, sizes and status codes only; nothing here throws.
+ * Relations are arrays of fixed-width row-major tuples exactly as Pythia's
+ * Page/TupleBuffer holds them (util/buffer.h:134-337) with the column layout
+ * of Schema (schema.h:148-350: packed, offsets = running sum of widths;
+ * int 4 B, long/dec/date 8 B). All data pointers are DEVICE pointers unless a
+ * function's name ends in _host. A `stream` is a cudaStream_t (NULL = the
+ * legacy default stream).
+ *
+ * Each entry point names the reference interface it replaces.
+ */
+#ifndef PYTHIA_GPU_H
+#define PYTHIA_GPU_H
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (Operator::ResultCode Error, operators/operators.h:89-93,
+ *      is the caller's mapping of every non-zero value) ---- */
+#define PG_OK               0
+#define PG_ERR_ARG          1  /* invalid argument or unsupported layout          */
+#define PG_ERR_OOM          2  /* device allocation failed                        */
+#define PG_ERR_CUDA         3  /* a CUDA runtime call failed                      */
+#define PG_ERR_TIMEOUT      4  /* a bounded device-side wait gave up               */
+#define PG_ERR_TABLE_FULL   5  /* hash table probe sequence exhausted             */
+#define PG_ERR_OUTPUT_FULL  6  /* output capacity too small; *n_out = rows needed */
+#define PG_ERR_UNSUPPORTED  7  /* configuration this build does not implement     */
+
+typedef struct pg_ctx pg_ctx;
+typedef struct pg_hashtable pg_hashtable;
+typedef void* pg_stream;
+
+/* ---- hash function descriptor: the plan's `hash` node as
+ *      TupleHasher::create reads it (hash.cpp:99-234) ---- */
+enum {
+	PG_FN_BYTES = 0, PG_FN_MODULO = 1, PG_FN_RANGE = 2, PG_FN_EXACTRANGE = 3,
+	PG_FN_PARAMMODULO = 4, PG_FN_KNUTH = 5, PG_FN_TPCHORDERKEY = 6,
+	PG_FN_WILLIS = 7, PG_FN_ALWAYSZERO = 8, PG_FN_TPCHQ1MAGIC = 9
+};
+typedef struct {
+	int32_t fn;          /* PG_FN_*                                   */
+	uint32_t buckets;    /* "buckets"                                 */
+	int64_t min, max;    /* "range" = [min, max] (range, exactrange)  */
+	uint32_t skipbits;   /* "skipbits" (parammodulo, knuth)           */
+	uint32_t offset;     /* "offset"   (parammodulo)                  */
+} pg_hashcfg;
+
+/* A relation: n tuples of `width` bytes; the key column at key_off,
+ * key_bytes = 4 (int) or 8 (long/date), or 0 where no key applies. */
+typedef struct {
+	const void* data;
+	uint64_t n;
+	uint32_t width;
+	uint32_t key_off;
+	uint32_t key_bytes;
+} pg_rel;
+
+/* One output column of a join projection ("B$i" / "P$i",
+ * createProjectionVector, operators/join.cpp:141-182): side 0 = build,
+ * 1 = probe; byte offset and width of the column in that side's tuple. */
+typedef struct {
+	uint32_t side;
+	uint32_t off;
+	uint32_t bytes;
+} pg_col;
+
+/* Join outcome. n_out counts output rows whether or not they were written. */
+typedef struct {
+	uint64_t n_out;
+	int64_t sum;        /* wrapping int64 sum of output column sum_col  */
+} pg_join_result;
+
+enum { PG_JOIN_MATERIALIZE = 1, PG_JOIN_COUNT = 2, PG_JOIN_SUM = 4 };
+
+/* ---------------------------------------------------------------------- */
+/* Context, memory, streams (replace numaallocate_*, util/numaallocate.h:35-37,
+ * and the per-operator thread/barrier plumbing of MergeOp)                */
+/* ---------------------------------------------------------------------- */
+int pg_init(int device, uint64_t reserved_bytes, pg_ctx** ctx);
+int pg_shutdown(pg_ctx* ctx);
+const char* pg_last_error(pg_ctx* ctx);
+int pg_device_status(pg_ctx* ctx);             /* sticky device error word  */
+int pg_stream_create(pg_ctx* ctx, pg_stream* stream);
+int pg_stream_destroy(pg_ctx* ctx, pg_stream stream);
+int pg_sync(pg_ctx* ctx, pg_stream stream);
+int pg_buffer_alloc(pg_ctx* ctx, uint64_t bytes, void** dptr);
+int pg_buffer_free(pg_ctx* ctx, void* dptr);
+int pg_host_alloc(pg_ctx* ctx, uint64_t bytes, void** hptr);   /* pinned */
+int pg_host_free(pg_ctx* ctx, void* hptr);
+int pg_h2d(pg_ctx* ctx, pg_stream stream, void* dst, const void* src, uint64_t bytes);
+int pg_d2h(pg_ctx* ctx, pg_stream stream, void* dst, const void* src, uint64_t bytes);
+int pg_memset(pg_ctx* ctx, pg_stream stream, void* dst, int value, uint64_t bytes);
+/* Number of kernels this library has launched (process-wide). */
+uint64_t pg_kernel_launches(void);
+
+/* ---------------------------------------------------------------------- */
+/* Tuple hashing: TupleHasher::hash over a column (hash.h:85-124) with the
+ * bucket functions of hash.h:150-479. out[i] = bucket of tuple i.        */
+/* ---------------------------------------------------------------------- */
+int pg_hash_buckets(pg_ctx* ctx, const pg_hashcfg* cfg, uint32_t* nbuckets);
+int pg_hash_tuples(pg_ctx* ctx, pg_stream stream, const pg_rel* in,
+		const pg_hashcfg* cfg, uint32_t* out);
+
+/* ---------------------------------------------------------------------- */
+/* Partition: PartitionOp::scanStart histogram / prefix / scatter
+ * (operators/partition.cpp:166-359). Stable: within a partition tuples keep
+ * input order, as the reference's per-thread prefix sums make them when
+ * threads read consecutive slices. offsets (device, nbuckets+1 uint64)
+ * receive partition starts, offsets[nbuckets] = n. Any hash function with
+ * at most 4096 buckets; every tuple must hash below buckets().          */
+/* ---------------------------------------------------------------------- */
+int pg_partition(pg_ctx* ctx, pg_stream stream, const pg_rel* in,
+		const pg_hashcfg* cfg, void* out, uint64_t* offsets);
+
+/* Optional per-partition sort ("sort" = "yes", partition.cpp:83-95, 339-353):
+ * sorts each partition of `data` in place by its key column. */
+int pg_partition_sort(pg_ctx* ctx, pg_stream stream, const pg_rel* data,
+		const uint64_t* offsets_host, uint32_t nbuckets, void* scratch_out);
+
+/* ---------------------------------------------------------------------- */
+/* Hash join build/probe: HashJoinOp::buildFromPage + scanStart (build,
+ * operators/join.cpp:396-464, 641-667) and HashJoinOp::getNext
+ * (probe, join.cpp:503-562) with constructOutputTuple (join.cpp:475-501).
+ * Equi-join on R.key = S.key; duplicates on either side give every pair.
+ * `proj` lists the output columns in order. Output rows are packed to the
+ * sum of the projected widths; their order is unspecified.               */
+/* ---------------------------------------------------------------------- */
+int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
+		const pg_col* proj, int nproj, pg_hashtable** ht);
+int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
+		const pg_rel* S, const pg_col* proj, int nproj,
+		void* out, uint64_t out_capacity, int flags, int sum_col,
+		pg_join_result* res);
+int pg_hashtable_free(pg_ctx* ctx, pg_hashtable* ht);
+/* Whole operator through HOST buffers (the call a Page-draining operator
+ * makes): copies in, builds, probes, copies out. Chunked so copies overlap
+ * the probe. out_host may be NULL with flags lacking PG_JOIN_MATERIALIZE. */
+int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* R_host, const pg_rel* S_host,
+		const pg_col* proj, int nproj, void* out_host, uint64_t out_capacity,
+		int flags, int sum_col, pg_join_result* res);
+
+/* ---------------------------------------------------------------------- */
+/* Group-by: GenericAggregate::remember + AggregateSum / AggregateCount fold
+ * (operators/genericaggregate.cpp:240-487, aggregatesum.cpp:53-107,
+ * aggregatecount.cpp:37-52). Key: in->key_bytes 4 or 8, or 0 for no GROUP BY
+ * (the "alwayszero" plan). Output rows: (key, agg) packed; agg is int32 for
+ * an int sum (wrapping, as the reference's CtInt +=), int64 for a long sum or
+ * a count, double for a dec sum. Integer results are exact; dec sums use
+ * error-compensated FP64 accumulation. groups_hint sizes the table (0: n).  */
+/* ---------------------------------------------------------------------- */
+enum { PG_VAL_INT = 0, PG_VAL_LONG = 1, PG_VAL_DEC = 2 };
+enum { PG_AGG_SUM = 0, PG_AGG_COUNT = 1 };
+int pg_groupby(pg_ctx* ctx, pg_stream stream, const pg_rel* in,
+		uint32_t val_off, int val_type, int agg, uint64_t groups_hint,
+		void* out, uint64_t out_capacity, uint64_t* ngroups);
+
+/* ---------------------------------------------------------------------- */
+/* Page sort: TupleBuffer::sort<KeyT> / sortAllInPage (util/buffer.inl:135-292,
+ * operators/join.cpp:893-912) and the bitonic block sort
+ * (util/bitonicsort.cpp:371-443): bitonic sort of `tile`-tuple pages in
+ * shared memory, then merge-path merges. Ascending signed key; ties in
+ * unspecified order. `out` may not alias `in`.                            */
+/* ---------------------------------------------------------------------- */
+int pg_sort_pages(pg_ctx* ctx, pg_stream stream, const pg_rel* in, void* out);
+
+/* ---------------------------------------------------------------------- */
+/* MPSM / sort-merge join: SortMergeJoinOp::BufferAndSort + OldMPSMJoinOp /
+ * MPSMJoinOp merge (operators/join.cpp:945-1371, 1383-1538). Same output
+ * contract as pg_hashjoin_probe.                                          */
+/* ---------------------------------------------------------------------- */
+int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, const pg_rel* S,
+		const pg_col* proj, int nproj, void* out, uint64_t out_capacity,
+		int flags, int sum_col, pg_join_result* res);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,305 @@
+// Group-by aggregation (aggregate_sum, aggregate_count) on sm_103a.
+//
+// Replaces GenericAggregate::remember + fold (operators/genericaggregate.cpp:
+// 240-282; aggregatesum.cpp:53-107; aggregatecount.cpp:37-52) and the getNext
+// emission of groups (genericaggregate.cpp:419-487). The reference keeps a
+// chained table per thread (ThreadLocal) or one locked table (Global); a
+// second aggregate over a merge combines thread partials.
+//
+// Here one open-addressing table per operator holds every group: the key word
+// is claimed with atomicCAS, accumulators are updated with atomics. Integer
+// sums and counts are exact (wrapping like the reference's CtInt/CtLong +=).
+// Double sums are error-compensated without locks: every atomicAdd(hi, v)
+// returns the old value, from which the exact rounding error of that one
+// addition follows by Knuth's TwoSum; errors accumulate in a second word `lo`
+// and the result is hi + lo. This is the compensated-summation accuracy class
+// (Kahan/Neumaier): error ~ eps*|S| + n*eps^2*sum|x|, independent of the order
+// in which threads arrive. Lanes of a warp that carry the same key are
+// combined first (warp match), which cuts atomics on skewed keys; with few
+// groups each CTA aggregates into a shared-memory table and merges once.
+#include "pg_internal.cuh"
+#include <algorithm>
+
+#define GB_THREADS 256
+#define GB_SMEM_SLOTS 4096
+
+struct GbTable {
+	unsigned long long* keys;   // [cap + 1]; slot cap is the group whose key is the empty marker
+	unsigned long long* acc;    // [cap + 1]: count, long sum, int sum (low 32 bits) or dec hi
+	double* lo;                 // [cap + 1]: dec compensation
+	int* sentinel_used;
+	uint32_t log2cap;
+};
+
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e)
+{
+	s = a + b;
+	double bb = s - a;
+	e = (a - (s - bb)) + (b - bb);
+}
+
+// Adds v into (hi, lo) with one atomic on hi and one on lo when the addition
+// rounded.
+__device__ __forceinline__ void atomic_comp_add(double* hi, double* lo, double v, double c)
+{
+	double old = atomicAdd(hi, v);
+	double s, e;
+	two_sum(old, v, s, e);
+	e += c;
+	if (e != 0.0) atomicAdd(lo, e);
+}
+
+template <int VT, int AGG>
+__device__ __forceinline__ void fold_slot(unsigned long long* acc, double* lo, uint64_t slot,
+		unsigned long long ival, double dv, double dc)
+{
+	if (AGG == PG_AGG_COUNT) atomicAdd(&acc[slot], ival);
+	else if (VT == PG_VAL_LONG) atomicAdd(&acc[slot], ival);
+	else if (VT == PG_VAL_INT) atomicAdd(reinterpret_cast<unsigned int*>(&acc[slot]), (unsigned int) ival);
+	else atomic_comp_add(reinterpret_cast<double*>(&acc[slot]), &lo[slot], dv, dc);
+}
+
+// Finds or claims the slot of key k. Returns cap (the side slot) for the
+// empty-marker key, or UINT64_MAX when the table is full.
+__device__ __forceinline__ uint64_t gb_slot(unsigned long long* keys, uint32_t log2cap, int64_t k,
+		int* sentinel_used)
+{
+	const uint64_t cap = 1ull << log2cap, mask = cap - 1;
+	if (k == PG_EMPTY_KEY) { if (!*sentinel_used) atomicExch(sentinel_used, 1); return cap; }
+	uint64_t s = pg_mix64((uint64_t) k) >> (64 - log2cap);
+	for (uint64_t probe = 0; probe < cap; ++probe) {
+		unsigned long long cur = keys[s];
+		if (cur == (unsigned long long) k) return s;
+		if (cur == (unsigned long long) PG_EMPTY_KEY) {
+			unsigned long long old = atomicCAS(&keys[s], (unsigned long long) PG_EMPTY_KEY, (unsigned long long) k);
+			if (old == (unsigned long long) PG_EMPTY_KEY || old == (unsigned long long) k) return s;
+		}
+		s = (s + 1) & mask;
+	}
+	return UINT64_MAX;
+}
+
+// Combines the values of lanes in `peers` (same key) at the leader lane, in
+// lane order. Integers add exactly; doubles are summed with TwoSum carries.
+template <int VT, int AGG>
+__device__ __forceinline__ void warp_combine(uint32_t peers, int lane, unsigned long long& ival,
+		double& dv, double& dc)
+{
+	if (AGG == PG_AGG_COUNT || VT != PG_VAL_DEC) {
+		unsigned long long tot = 0;
+		uint32_t m = peers;
+		while (m) {
+			int src = __ffs(m) - 1; m &= m - 1;
+			unsigned long long x = __shfl_sync(peers, ival, src);
+			tot += x;
+		}
+		ival = tot;
+	} else {
+		double s = 0.0, c = 0.0;
+		uint32_t m = peers;
+		while (m) {
+			int src = __ffs(m) - 1; m &= m - 1;
+			double x = __shfl_sync(peers, dv, src);
+			double e;
+			two_sum(s, x, s, e);
+			c += e;
+		}
+		dv = s; dc = c;
+	}
+}
+
+template <int VT, int AGG, bool HASKEY, bool SMEM>
+__global__ void __launch_bounds__(GB_THREADS)
+k_gb_insert(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes,
+		uint32_t voff, GbTable t, uint32_t smem_log2, int* __restrict__ status)
+{
+	extern __shared__ __align__(16) unsigned char sm[];
+	unsigned long long* skeys = reinterpret_cast<unsigned long long*>(sm);
+	unsigned long long* sacc = skeys + (SMEM ? (1u << smem_log2) + 1 : 0);
+	double* slo = reinterpret_cast<double*>(sacc + (SMEM ? (1u << smem_log2) + 1 : 0));
+	__shared__ int s_sentinel;
+	const int lane = threadIdx.x & 31;
+	if (SMEM) {
+		const uint32_t sc = (1u << smem_log2) + 1;
+		for (uint32_t i = threadIdx.x; i < sc; i += blockDim.x) {
+			skeys[i] = (unsigned long long) PG_EMPTY_KEY; sacc[i] = 0; slo[i] = 0.0;
+		}
+		if (threadIdx.x == 0) s_sentinel = 0;
+		__syncthreads();
+	}
+	bool full = false;
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	const uint64_t n_round = pg_div_up(n, 32) * 32;
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n_round; i += stride) {
+		bool valid = i < n;
+		int64_t k = 0;
+		unsigned long long ival = 0;
+		double dv = 0.0, dc = 0.0;
+		if (valid) {
+			const char* r = in + i * W;
+			if (HASKEY) k = pg_load_key(r + koff, kbytes);
+			if (AGG == PG_AGG_COUNT) ival = 1;
+			else if (VT == PG_VAL_INT) ival = (unsigned long long) (long long) *reinterpret_cast<const int32_t*>(r + voff);
+			else if (VT == PG_VAL_LONG) ival = (unsigned long long) pg_load_key(r + voff, 8);
+			else dv = __longlong_as_double(pg_load_key(r + voff, 8));
+		}
+		// Lanes with the same key fold together first.
+		uint32_t active = __ballot_sync(0xffffffffu, valid);
+		if (!valid) continue;
+		uint32_t peers = HASKEY ? __match_any_sync(active, (unsigned long long) k) : active;
+		warp_combine<VT, AGG>(peers, lane, ival, dv, dc);
+		if (lane != __ffs(peers) - 1) continue;
+		if (SMEM) {
+			uint64_t s = HASKEY ? gb_slot(skeys, smem_log2, k, &s_sentinel) : 0;
+			if (s == UINT64_MAX) { full = true; continue; }
+			fold_slot<VT, AGG>(sacc, slo, s, ival, dv, dc);
+		} else {
+			uint64_t s = HASKEY ? gb_slot(t.keys, t.log2cap, k, t.sentinel_used) : 0;
+			if (s == UINT64_MAX) { full = true; continue; }
+			fold_slot<VT, AGG>(t.acc, t.lo, s, ival, dv, dc);
+		}
+	}
+	if (full) pg_set_status(status, PG_ERR_TABLE_FULL);
+	if (SMEM) {
+		// Merge this CTA's partial groups into the global table.
+		__syncthreads();
+		const uint32_t sc = 1u << smem_log2;
+		for (uint32_t i = threadIdx.x; i <= sc; i += blockDim.x) {
+			bool used = HASKEY ? ((i < sc) ? skeys[i] != (unsigned long long) PG_EMPTY_KEY : s_sentinel != 0)
+			                   : i == 0;
+			if (!used) continue;
+			int64_t k = (i < sc) ? (int64_t) skeys[i] : PG_EMPTY_KEY;
+			uint64_t s = HASKEY ? gb_slot(t.keys, t.log2cap, k, t.sentinel_used) : 0;
+			if (s == UINT64_MAX) { pg_set_status(status, PG_ERR_TABLE_FULL); continue; }
+			if (VT == PG_VAL_DEC && AGG == PG_AGG_SUM)
+				atomic_comp_add(reinterpret_cast<double*>(&t.acc[s]), &t.lo[s],
+						__longlong_as_double((long long) sacc[i]), slo[i]);
+			else fold_slot<VT, AGG>(t.acc, t.lo, s, sacc[i], 0.0, 0.0);
+		}
+	}
+}
+
+template <int VT, int AGG, bool HASKEY>
+__global__ void k_gb_emit(GbTable t, uint32_t kbytes, char* __restrict__ out, uint64_t cap_rows,
+		unsigned long long* __restrict__ cursor, uint64_t nonkey_rows)
+{
+	const uint64_t cap = 1ull << t.log2cap;
+	const uint32_t aw = (AGG == PG_AGG_SUM && VT == PG_VAL_INT) ? 4 : 8;
+	const uint32_t ow = (HASKEY ? kbytes : 0) + aw;
+	const uint64_t limit = HASKEY ? cap + 1 : 1;
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < pg_div_up(limit, 32) * 32;
+			i += (uint64_t) gridDim.x * blockDim.x) {
+		bool used = false;
+		if (i < limit) {
+			if (!HASKEY) used = nonkey_rows > 0;
+			else if (i < cap) used = t.keys[i] != (unsigned long long) PG_EMPTY_KEY;
+			else used = *t.sentinel_used != 0;
+		}
+		uint32_t ball = __ballot_sync(0xffffffffu, used);
+		if (!ball) continue;
+		int lane = threadIdx.x & 31;
+		unsigned long long base = 0;
+		if (lane == __ffs(ball) - 1) base = atomicAdd(cursor, (unsigned long long) __popc(ball));
+		base = __shfl_sync(0xffffffffu, base, __ffs(ball) - 1);
+		if (!used) continue;
+		uint64_t pos = base + __popc(ball & ((1u << lane) - 1));
+		if (pos >= cap_rows) continue;
+		char* o = out + pos * ow;
+		if (HASKEY) {
+			int64_t k = i < cap ? (int64_t) t.keys[i] : PG_EMPTY_KEY;
+			if (kbytes == 4) *reinterpret_cast<int32_t*>(o) = (int32_t) k;
+			else { reinterpret_cast<uint32_t*>(o)[0] = (uint32_t) k; reinterpret_cast<uint32_t*>(o)[1] = (uint32_t) ((uint64_t) k >> 32); }
+			o += kbytes;
+		}
+		if (aw == 4) *reinterpret_cast<uint32_t*>(o) = (uint32_t) t.acc[i];
+		else {
+			unsigned long long a = t.acc[i];
+			if (VT == PG_VAL_DEC && AGG == PG_AGG_SUM) {
+				double r = __longlong_as_double((long long) a) + t.lo[i];
+				a = (unsigned long long) __double_as_longlong(r);
+			}
+			reinterpret_cast<uint32_t*>(o)[0] = (uint32_t) a;
+			reinterpret_cast<uint32_t*>(o)[1] = (uint32_t) (a >> 32);
+		}
+	}
+}
+
+template <int VT, int AGG>
+static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, uint64_t hint,
+		void* out, uint64_t out_cap, uint64_t* ngroups)
+{
+	const bool haskey = in->key_bytes != 0;
+	uint64_t groups = haskey ? std::max<uint64_t>(1, std::min<uint64_t>(hint ? hint : in->n, in->n ? in->n : 1)) : 1;
+	for (int attempt = 0; attempt < 6; ++attempt) {
+		uint32_t lg = 10;
+		while ((1ull << lg) < 2 * groups) ++lg;
+		const uint64_t cap = 1ull << lg;
+		GbTable t;
+		t.log2cap = lg;
+		char* mem = nullptr;
+		int rc;
+		size_t bytes = (cap + 1) * 24 + 64;
+		if ((rc = pg_alloc_async(ctx, s, (void**) &mem, bytes))) return rc;
+		t.keys = reinterpret_cast<unsigned long long*>(mem);
+		t.acc = t.keys + cap + 1;
+		t.lo = reinterpret_cast<double*>(t.acc + cap + 1);
+		t.sentinel_used = reinterpret_cast<int*>(t.lo + cap + 1);
+		unsigned long long* cursor = reinterpret_cast<unsigned long long*>(t.sentinel_used + 2);
+		PG_CUDA(ctx, cudaMemsetAsync(t.keys, 0xFF, (cap + 1) * 8, s));
+		PG_CUDA(ctx, cudaMemsetAsync(t.acc, 0, (cap + 1) * 16 + 64, s));
+		const bool smem = groups <= GB_SMEM_SLOTS / 2;
+		uint32_t slg = 1;
+		while ((1u << slg) < 2 * groups) ++slg;
+		if (!haskey) slg = 0;
+		const size_t smem_bytes = smem ? ((size_t) (1u << slg) + 1) * 24 : 0;
+		int blocks = (int) std::min<uint64_t>(pg_div_up(std::max<uint64_t>(in->n, 1), GB_THREADS),
+				(uint64_t) ctx->sm_count * (smem ? 4 : 8));
+		if (in->n) {
+			#define GB_LAUNCH(HK, SM) k_gb_insert<VT, AGG, HK, SM><<<blocks, GB_THREADS, smem_bytes, s>>>( \
+					(const char*) in->data, in->n, in->width, in->key_off, in->key_bytes, voff, t, slg, ctx->d_status)
+			if (haskey && smem) GB_LAUNCH(true, true);
+			else if (haskey) GB_LAUNCH(true, false);
+			else GB_LAUNCH(false, true);
+			#undef GB_LAUNCH
+			PG_LAUNCHED(ctx);
+		}
+		rc = pg_check_status(ctx, s, "pg_groupby");
+		if (rc == PG_ERR_TABLE_FULL) { pg_free_async(ctx, s, mem); groups *= 4; continue; }
+		if (rc) { pg_free_async(ctx, s, mem); return rc; }
+		int eblocks = (int) std::min<uint64_t>(pg_div_up(cap + 1, 256), (uint64_t) ctx->sm_count * 8);
+		if (haskey) k_gb_emit<VT, AGG, true><<<eblocks, 256, 0, s>>>(t, in->key_bytes, (char*) out, out_cap, cursor, 0);
+		else k_gb_emit<VT, AGG, false><<<1, 32, 0, s>>>(t, 0, (char*) out, out_cap, cursor, in->n);
+		PG_LAUNCHED(ctx);
+		unsigned long long ng = 0;
+		PG_CUDA(ctx, cudaMemcpyAsync(&ng, cursor, 8, cudaMemcpyDeviceToHost, s));
+		PG_CUDA(ctx, cudaStreamSynchronize(s));
+		pg_free_async(ctx, s, mem);
+		*ngroups = ng;
+		if (ng > out_cap) return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_groupby: output capacity too small");
+		return PG_OK;
+	}
+	return pg_fail(ctx, PG_ERR_TABLE_FULL, "pg_groupby: group table kept overflowing");
+}
+
+extern "C" int pg_groupby(pg_ctx* ctx, pg_stream stream, const pg_rel* in,
+		uint32_t val_off, int val_type, int agg, uint64_t groups_hint,
+		void* out, uint64_t out_capacity, uint64_t* ngroups)
+{
+	if (!ctx || !in || !ngroups) return pg_fail(ctx, PG_ERR_ARG, "pg_groupby: null argument");
+	if (in->n && !in->data) return pg_fail(ctx, PG_ERR_ARG, "pg_groupby: null data");
+	if (in->width == 0 || (in->width & 3)) return pg_fail(ctx, PG_ERR_UNSUPPORTED, "pg_groupby: tuple width must be a multiple of 4");
+	if (in->key_bytes != 0 && ((in->key_bytes != 4 && in->key_bytes != 8) || (in->key_off & 3) ||
+			in->key_off + in->key_bytes > in->width))
+		return pg_fail(ctx, PG_ERR_ARG, "pg_groupby: key must be a 4-byte-aligned int or long column, or absent");
+	if (agg != PG_AGG_SUM && agg != PG_AGG_COUNT) return pg_fail(ctx, PG_ERR_ARG, "pg_groupby: bad aggregate");
+	if (agg == PG_AGG_SUM) {
+		uint32_t vb = val_type == PG_VAL_INT ? 4 : 8;
+		if (val_type < 0 || val_type > 2 || (val_off & 3) || val_off + vb > in->width)
+			return pg_fail(ctx, PG_ERR_ARG, "pg_groupby: bad sum column");
+	}
+	cudaStream_t s = (cudaStream_t) stream;
+	if (agg == PG_AGG_COUNT) return gb_run<PG_VAL_LONG, PG_AGG_COUNT>(ctx, s, in, val_off, groups_hint, out, out_capacity, ngroups);
+	if (val_type == PG_VAL_INT) return gb_run<PG_VAL_INT, PG_AGG_SUM>(ctx, s, in, val_off, groups_hint, out, out_capacity, ngroups);
+	if (val_type == PG_VAL_LONG) return gb_run<PG_VAL_LONG, PG_AGG_SUM>(ctx, s, in, val_off, groups_hint, out, out_capacity, ngroups);
+	return gb_run<PG_VAL_DEC, PG_AGG_SUM>(ctx, s, in, val_off, groups_hint, out, out_capacity, ngroups);
+}

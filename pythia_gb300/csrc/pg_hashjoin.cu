@@ -1,0 +1,751 @@
+// Hash join build and probe on sm_103a.
+//
+// Replaces HashJoinOp (operators/join.cpp:273-675) and its chained-bucket
+// HashTable (util/hashtable.{h,cpp}). The reference hashes the build key into
+// a bucket, takes the bucket's spinlock, appends the sbuild tuple (key +
+// build-projected columns, join.cpp:641-667), and later walks the chain per
+// probe tuple (join.cpp:503-562), emitting constructOutputTuple
+// (join.cpp:475-501) for every key match.
+//
+// Here the table is open addressing with linear probing over 16-byte slots
+// {int64 key, uint64 value}: inserts claim a slot with one 64-bit atomicCAS on
+// the key word; the value is the build-projected columns packed into 8 bytes
+// when they fit, else the build row index (the output then gathers from R).
+// Keys equal to the empty marker live in a small side list. Duplicate build
+// keys are legal (each occupies its own slot); the build records whether any
+// occurred, and the probe takes a single-pass path when keys are unique
+// (PK-FK joins) and a count-then-write path otherwise.
+//
+// Probe (unique keys): each CTA takes tiles of 2048 probe tuples, loads them
+// with streaming (evict-first) 16-byte loads, probes the table with
+// evict-last loads so the table stays in L2, ranks matches with warp ballots
+// in tile order, reserves one output range per tile with a single atomicAdd,
+// and writes coalesced rows. With PG_JOIN_COUNT/SUM the matches are folded
+// into a count and a wrapping int64 sum instead (aggregate_count /
+// aggregate_sum over the join, aggregatecount.cpp:37-52,
+// aggregatesum.cpp:81-107).
+#include "pg_internal.cuh"
+#include <algorithm>
+#include <vector>
+
+#define HJ_THREADS 256
+#define HJ_ITEMS 8
+#define HJ_TILE (HJ_THREADS * HJ_ITEMS)
+#define HJ_MAX_COLS 16
+#define HJ_SIDE_CAP0 1024
+
+struct HjCols {                 // projected columns, in projection order
+	int n;
+	int ow_words;               // output width in 4-byte words
+	uint8_t side[HJ_MAX_COLS];  // 0 build, 1 probe
+	uint16_t src[HJ_MAX_COLS];  // word offset: probe tuple, packed build value, or build tuple
+	uint8_t words[HJ_MAX_COLS];
+};
+
+struct HjBuildCols {            // build-projected columns packed into the value
+	int n;
+	uint16_t roff[HJ_MAX_COLS]; // word offset in the build tuple
+	uint8_t words[HJ_MAX_COLS];
+};
+
+struct pg_hashtable {
+	unsigned long long* slots;  // 2 * capacity words
+	uint64_t capacity;
+	uint32_t log2cap;
+	uint64_t nbuild;
+	bool unique;
+	bool inline_val;            // value = packed build columns, else row index
+	HjBuildCols bcols;
+	const char* R;              // build tuples (row-index mode gathers from here)
+	uint32_t wR;
+	uint32_t bkey_bytes;
+	unsigned long long* side;   // values of build tuples whose key is the empty marker
+	uint32_t side_cap;
+	uint32_t nside;
+	pg_col proj[HJ_MAX_COLS];
+	int nproj;
+	cudaStream_t stream;        // stream the table was built on
+};
+
+__device__ __forceinline__ uint64_t hj_slot0(int64_t k, uint32_t log2cap)
+{
+	return pg_mix64((uint64_t) k) >> (64 - log2cap);
+}
+
+__device__ __forceinline__ uint32_t hj_word(const char* tuple, uint32_t w)
+{
+	return reinterpret_cast<const uint32_t*>(tuple)[w];
+}
+
+__global__ void k_ht_build(const char* __restrict__ R, uint64_t n, uint32_t W, uint32_t koff,
+		uint32_t kbytes, HjBuildCols bc, bool inline_val, unsigned long long* __restrict__ slots,
+		uint32_t log2cap, unsigned long long* __restrict__ side, uint32_t side_cap,
+		unsigned int* __restrict__ side_count, int* __restrict__ flags, int* __restrict__ status)
+{
+	const uint64_t mask = (1ull << log2cap) - 1;
+	bool dup = false;
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+			i += (uint64_t) gridDim.x * blockDim.x) {
+		const char* t = R + i * W;
+		int64_t k = pg_load_key(t + koff, kbytes);
+		uint64_t v;
+		if (inline_val) {
+			uint32_t w[2] = {0, 0};
+			int o = 0;
+			for (int c = 0; c < bc.n; ++c)
+				for (int j = 0; j < bc.words[c]; ++j) w[o++] = hj_word(t, bc.roff[c] + j);
+			v = ((uint64_t) w[1] << 32) | w[0];
+		} else {
+			v = i;
+		}
+		if (k == PG_EMPTY_KEY) {
+			unsigned int idx = atomicAdd(side_count, 1u);
+			if (idx < side_cap) side[idx] = v; else atomicOr(flags, 2);
+			continue;
+		}
+		uint64_t s = hj_slot0(k, log2cap);
+		uint64_t probe = 0;
+		for (; probe <= mask; ++probe) {
+			unsigned long long old = atomicCAS(&slots[2 * s], (unsigned long long) PG_EMPTY_KEY,
+					(unsigned long long) k);
+			if (old == (unsigned long long) PG_EMPTY_KEY) { slots[2 * s + 1] = v; break; }
+			if ((long long) old == k) dup = true;
+			s = (s + 1) & mask;
+		}
+		if (probe > mask) pg_set_status(status, PG_ERR_TABLE_FULL);
+	}
+	if (__any_sync(__activemask(), dup) && dup) atomicOr(flags, 1);
+}
+
+// Value of output word `w` for a match: from the probe tuple or from the build
+// side (packed value, or the build tuple when values are row indices).
+__device__ __forceinline__ uint32_t hj_out_word(const HjCols& pc, int c, int j, const char* ptup,
+		uint64_t val, bool inline_val, const char* R, uint32_t wR)
+{
+	if (pc.side[c]) return hj_word(ptup, pc.src[c] + j);
+	if (inline_val) {
+		uint32_t idx = pc.src[c] + j;
+		return idx == 0 ? (uint32_t) val : (uint32_t) (val >> 32);
+	}
+	return hj_word(R + val * wR, pc.src[c] + j);
+}
+
+// ---------------------------------------------------------------------------
+// Unique-key probe: one pass, tile-ordered output, one atomicAdd per tile.
+// FAST16: probe tuples are 16 bytes and output rows 16 bytes (4 words).
+// ---------------------------------------------------------------------------
+template <bool MATERIALIZE, bool FAST16>
+__global__ void __launch_bounds__(HJ_THREADS)
+k_probe_unique(const char* __restrict__ S, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes,
+		const unsigned long long* __restrict__ slots, uint32_t log2cap,
+		const unsigned long long* __restrict__ side, uint32_t nside,
+		HjCols pc, char* __restrict__ out, uint64_t out_cap,
+		unsigned long long* __restrict__ cursor, unsigned long long* __restrict__ agg,
+		int sum_col, int* __restrict__ status)
+{
+	__shared__ uint32_t wcnt[HJ_ITEMS][HJ_THREADS / 32];
+	__shared__ unsigned long long tile_base;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const uint64_t mask = (1ull << log2cap) - 1;
+	const uint64_t ntiles = pg_div_up(n, HJ_TILE);
+	unsigned long long cnt_acc = 0, sum_acc = 0;
+
+	for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+		const uint64_t base = tile * HJ_TILE;
+		uint4 tup[HJ_ITEMS];
+		int64_t key[HJ_ITEMS];
+		uint64_t val[HJ_ITEMS];
+		bool hit[HJ_ITEMS];
+		// Load probe tuples (streaming) and their first table slot (L2-resident).
+		#pragma unroll
+		for (int j = 0; j < HJ_ITEMS; ++j) {
+			uint64_t r = base + (uint64_t) j * HJ_THREADS + tid;
+			hit[j] = false;
+			key[j] = 0;
+			if (r < n) {
+				if (FAST16) {
+					tup[j] = pg_ld_stream16(S + r * 16);
+					key[j] = (int64_t) (((uint64_t) tup[j].y << 32) | tup[j].x);
+					if (koff == 8) key[j] = (int64_t) (((uint64_t) tup[j].w << 32) | tup[j].z);
+				} else {
+					key[j] = pg_load_key(S + r * W + koff, kbytes);
+				}
+			}
+		}
+		uint4 sl[HJ_ITEMS];
+		#pragma unroll
+		for (int j = 0; j < HJ_ITEMS; ++j) {
+			uint64_t r = base + (uint64_t) j * HJ_THREADS + tid;
+			if (r < n && key[j] != PG_EMPTY_KEY)
+				sl[j] = pg_ld_table16(slots + 2 * hj_slot0(key[j], log2cap));
+		}
+		#pragma unroll
+		for (int j = 0; j < HJ_ITEMS; ++j) {
+			uint64_t r = base + (uint64_t) j * HJ_THREADS + tid;
+			if (r >= n) continue;
+			if (key[j] == PG_EMPTY_KEY) {
+				if (nside) { hit[j] = true; val[j] = side[0]; }
+				continue;
+			}
+			uint64_t s = hj_slot0(key[j], log2cap);
+			uint4 v = sl[j];
+			for (uint64_t probe = 0;; ++probe) {
+				int64_t sk = (int64_t) (((uint64_t) v.y << 32) | v.x);
+				if (sk == key[j]) { hit[j] = true; val[j] = ((uint64_t) v.w << 32) | v.z; break; }
+				if (sk == PG_EMPTY_KEY || probe > mask) break;
+				s = (s + 1) & mask;
+				v = pg_ld_table16(slots + 2 * s);
+			}
+		}
+		if (MATERIALIZE) {
+			// Tile-order ranks: item-major, then warp, then lane.
+			uint32_t ball[HJ_ITEMS];
+			#pragma unroll
+			for (int j = 0; j < HJ_ITEMS; ++j) {
+				ball[j] = __ballot_sync(0xffffffffu, hit[j]);
+				if (lane == 0) wcnt[j][warp] = __popc(ball[j]);
+			}
+			__syncthreads();
+			if (tid == 0) {
+				uint32_t run = 0;
+				for (int j = 0; j < HJ_ITEMS; ++j)
+					for (int w = 0; w < HJ_THREADS / 32; ++w) { uint32_t c = wcnt[j][w]; wcnt[j][w] = run; run += c; }
+				tile_base = atomicAdd(cursor, (unsigned long long) run);
+			}
+			__syncthreads();
+			const unsigned long long tb = tile_base;
+			#pragma unroll
+			for (int j = 0; j < HJ_ITEMS; ++j) {
+				if (!hit[j]) continue;
+				uint64_t pos = tb + wcnt[j][warp] + __popc(ball[j] & ((1u << lane) - 1));
+				if (pos >= out_cap) continue;
+				if (FAST16) {
+					uint32_t w4[4];
+					int o = 0;
+					for (int c = 0; c < pc.n; ++c)
+						for (int q = 0; q < pc.words[c]; ++q) {
+							uint32_t src = pc.src[c] + q, x;
+							if (pc.side[c]) x = src == 0 ? tup[j].x : src == 1 ? tup[j].y : src == 2 ? tup[j].z : tup[j].w;
+							else x = src == 0 ? (uint32_t) val[j] : (uint32_t) (val[j] >> 32);
+							w4[o++] = x;
+						}
+					pg_st_stream16(out + pos * 16, make_uint4(w4[0], w4[1], w4[2], w4[3]));
+				} else {
+					uint32_t* o = reinterpret_cast<uint32_t*>(out + pos * (uint64_t) pc.ow_words * 4);
+					const char* pt = S + (base + (uint64_t) j * HJ_THREADS + tid) * W;
+					int wo = 0;
+					for (int c = 0; c < pc.n; ++c)
+						for (int q = 0; q < pc.words[c]; ++q)
+							o[wo++] = hj_out_word(pc, c, q, pt, val[j], true, nullptr, 0);
+				}
+			}
+			__syncthreads();
+		} else {
+			#pragma unroll
+			for (int j = 0; j < HJ_ITEMS; ++j) {
+				if (!hit[j]) continue;
+				cnt_acc++;
+				if (sum_col >= 0) {
+					const char* pt = S + (base + (uint64_t) j * HJ_THREADS + tid) * W;
+					uint32_t lo = hj_out_word(pc, sum_col, 0, pt, val[j], true, nullptr, 0);
+					if (pc.words[sum_col] == 2) {
+						uint32_t hi = hj_out_word(pc, sum_col, 1, pt, val[j], true, nullptr, 0);
+						sum_acc += ((unsigned long long) hi << 32) | lo;
+					} else {
+						sum_acc += (unsigned long long) (long long) (int32_t) lo;
+					}
+				}
+			}
+		}
+	}
+	if (!MATERIALIZE) {
+		#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			cnt_acc += __shfl_down_sync(0xffffffffu, cnt_acc, o);
+			sum_acc += __shfl_down_sync(0xffffffffu, sum_acc, o);
+		}
+		if (lane == 0) { atomicAdd(&agg[0], cnt_acc); atomicAdd(&agg[1], sum_acc); }
+	}
+}
+
+// ---------------------------------------------------------------------------
+// General probe (duplicate build keys and/or row-index values): pass 1 counts
+// matches per tile (and folds count/sum), pass 2 writes at scanned offsets.
+// ---------------------------------------------------------------------------
+template <bool WRITE>
+__global__ void __launch_bounds__(HJ_THREADS)
+k_probe_general(const char* __restrict__ S, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes,
+		const unsigned long long* __restrict__ slots, uint32_t log2cap,
+		const unsigned long long* __restrict__ side, uint32_t nside,
+		HjCols pc, bool inline_val, const char* __restrict__ R, uint32_t wR,
+		uint64_t* __restrict__ tile_counts, char* __restrict__ out,
+		unsigned long long* __restrict__ agg, int sum_col, int* __restrict__ status)
+{
+	__shared__ unsigned long long wtot[HJ_THREADS / 32];
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const uint64_t mask = (1ull << log2cap) - 1;
+	const uint64_t ntiles = pg_div_up(n, HJ_TILE);
+	unsigned long long cnt_acc = 0, sum_acc = 0;
+	const uint64_t ow = (uint64_t) pc.ow_words * 4;
+
+	for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+		const uint64_t base = tile * HJ_TILE;
+		unsigned long long run = WRITE ? tile_counts[tile] : 0;
+		#pragma unroll 1
+		for (int j = 0; j < HJ_ITEMS; ++j) {
+			uint64_t r = base + (uint64_t) j * HJ_THREADS + tid;
+			const char* pt = S + r * W;
+			uint32_t c = 0;
+			int64_t k = 0;
+			if (r < n) {
+				k = pg_load_key(pt + koff, kbytes);
+				if (k == PG_EMPTY_KEY) c = nside;
+				else {
+					uint64_t s = hj_slot0(k, log2cap);
+					for (uint64_t probe = 0; probe <= mask; ++probe) {
+						uint4 v = pg_ld_table16(slots + 2 * s);
+						int64_t sk = (int64_t) (((uint64_t) v.y << 32) | v.x);
+						if (sk == PG_EMPTY_KEY) break;
+						if (sk == k) {
+							if (!WRITE && sum_col >= 0) {
+								uint64_t val = ((uint64_t) v.w << 32) | v.z;
+								uint32_t lo = hj_out_word(pc, sum_col, 0, pt, val, inline_val, R, wR);
+								if (pc.words[sum_col] == 2) {
+									uint32_t hi = hj_out_word(pc, sum_col, 1, pt, val, inline_val, R, wR);
+									sum_acc += ((unsigned long long) hi << 32) | lo;
+								} else sum_acc += (unsigned long long) (long long) (int32_t) lo;
+							}
+							++c;
+						}
+						s = (s + 1) & mask;
+					}
+				}
+			}
+			if (!WRITE && sum_col >= 0 && k == PG_EMPTY_KEY && r < n) {
+				for (uint32_t q = 0; q < nside; ++q) {
+					uint64_t val = side[q];
+					uint32_t lo = hj_out_word(pc, sum_col, 0, pt, val, inline_val, R, wR);
+					if (pc.words[sum_col] == 2) {
+						uint32_t hi = hj_out_word(pc, sum_col, 1, pt, val, inline_val, R, wR);
+						sum_acc += ((unsigned long long) hi << 32) | lo;
+					} else sum_acc += (unsigned long long) (long long) (int32_t) lo;
+				}
+			}
+			cnt_acc += c;
+			if (WRITE) {
+				// Exclusive block scan of c in (item, warp, lane) order.
+				unsigned long long x = c;
+				#pragma unroll
+				for (int o = 1; o < 32; o <<= 1) {
+					unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+					if (lane >= o) x += y;
+				}
+				if (lane == 31) wtot[warp] = x;
+				__syncthreads();
+				unsigned long long before = 0, total = 0;
+				for (int w = 0; w < HJ_THREADS / 32; ++w) { if (w < warp) before += wtot[w]; total += wtot[w]; }
+				unsigned long long pos = run + before + x - c;
+				run += total;
+				__syncthreads();
+				if (c && r < n) {
+					auto emit = [&](uint64_t val) {
+						uint32_t* o = reinterpret_cast<uint32_t*>(out + pos * ow);
+						int wo = 0;
+						for (int cc = 0; cc < pc.n; ++cc)
+							for (int q = 0; q < pc.words[cc]; ++q)
+								o[wo++] = hj_out_word(pc, cc, q, pt, val, inline_val, R, wR);
+						++pos;
+					};
+					if (k == PG_EMPTY_KEY) {
+						for (uint32_t q = 0; q < nside; ++q) emit(side[q]);
+					} else {
+						uint64_t s = hj_slot0(k, log2cap);
+						for (uint64_t probe = 0; probe <= mask; ++probe) {
+							uint4 v = pg_ld_table16(slots + 2 * s);
+							int64_t sk = (int64_t) (((uint64_t) v.y << 32) | v.x);
+							if (sk == PG_EMPTY_KEY) break;
+							if (sk == k) emit(((uint64_t) v.w << 32) | v.z);
+							s = (s + 1) & mask;
+						}
+					}
+				}
+			}
+		}
+	}
+	if (!WRITE) {
+		// The host launches one CTA per tile, so the CTA total is the tile's.
+		#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			cnt_acc += __shfl_down_sync(0xffffffffu, cnt_acc, o);
+			sum_acc += __shfl_down_sync(0xffffffffu, sum_acc, o);
+		}
+		if (lane == 0) wtot[warp] = cnt_acc;
+		__syncthreads();
+		if (tid == 0) {
+			unsigned long long t = 0;
+			for (int w = 0; w < HJ_THREADS / 32; ++w) t += wtot[w];
+			tile_counts[blockIdx.x] = t;
+		}
+		if (lane == 0) { atomicAdd(&agg[0], cnt_acc); atomicAdd(&agg[1], sum_acc); }
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+static int hj_validate_rel(pg_ctx* ctx, const pg_rel* r, const char* who)
+{
+	if (!r) return pg_fail(ctx, PG_ERR_ARG, std::string(who) + ": null relation");
+	if (r->n && !r->data) return pg_fail(ctx, PG_ERR_ARG, std::string(who) + ": null data");
+	if (r->width == 0 || (r->width & 3))
+		return pg_fail(ctx, PG_ERR_UNSUPPORTED, std::string(who) + ": tuple width must be a multiple of 4 bytes");
+	if ((r->key_bytes != 4 && r->key_bytes != 8) || (r->key_off & 3) || r->key_off + r->key_bytes > r->width)
+		return pg_fail(ctx, PG_ERR_ARG, std::string(who) + ": key must be a 4-byte-aligned int or long column");
+	if (r->n && (reinterpret_cast<uintptr_t>(r->data) & 15))
+		return pg_fail(ctx, PG_ERR_ARG, std::string(who) + ": data must be 16-byte aligned");
+	return PG_OK;
+}
+
+static int hj_validate_proj(pg_ctx* ctx, const pg_col* proj, int nproj, uint32_t wR, uint32_t wS)
+{
+	if (nproj < 0 || nproj > HJ_MAX_COLS || (nproj && !proj))
+		return pg_fail(ctx, PG_ERR_ARG, "join: 0..16 projected columns");
+	for (int i = 0; i < nproj; ++i) {
+		const pg_col& c = proj[i];
+		uint32_t w = c.side ? wS : wR;
+		if (c.side > 1 || (c.bytes != 4 && c.bytes != 8) || (c.off & 3) || c.off + c.bytes > w)
+			return pg_fail(ctx, PG_ERR_UNSUPPORTED, "join: projected columns must be 4- or 8-byte, 4-byte aligned, inside the tuple");
+	}
+	return PG_OK;
+}
+
+extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
+		const pg_col* proj, int nproj, pg_hashtable** out)
+{
+	if (!ctx || !out) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_build: null argument");
+	int rc;
+	if ((rc = hj_validate_rel(ctx, R, "pg_hashjoin_build"))) return rc;
+	if ((rc = hj_validate_proj(ctx, proj, nproj, R->width, 1u << 30))) return rc;
+	cudaStream_t s = (cudaStream_t) stream;
+	pg_hashtable* ht = new pg_hashtable();
+	ht->nbuild = R->n; ht->R = (const char*) R->data; ht->wR = R->width; ht->bkey_bytes = R->key_bytes;
+	ht->nproj = nproj;
+	ht->stream = s;
+	for (int i = 0; i < nproj; ++i) ht->proj[i] = proj[i];
+	uint32_t bbytes = 0;
+	ht->bcols.n = 0;
+	for (int i = 0; i < nproj; ++i)
+		if (proj[i].side == 0) {
+			ht->bcols.roff[ht->bcols.n] = (uint16_t) (proj[i].off / 4);
+			ht->bcols.words[ht->bcols.n] = (uint8_t) (proj[i].bytes / 4);
+			ht->bcols.n++;
+			bbytes += proj[i].bytes;
+		}
+	ht->inline_val = bbytes <= 8;
+	uint64_t want = std::max<uint64_t>(1024, 2 * R->n);
+	uint32_t lg = 10;
+	while ((1ull << lg) < want) ++lg;
+	ht->log2cap = lg; ht->capacity = 1ull << lg;
+	ht->side_cap = HJ_SIDE_CAP0;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &ht->slots, ht->capacity * 16))) { delete ht; return rc; }
+	if ((rc = pg_alloc_async(ctx, s, (void**) &ht->side, ht->side_cap * 8 + 64))) { delete ht; return rc; }
+	// side buffer tail: [side_count u32][flags i32]
+	unsigned int* side_count = reinterpret_cast<unsigned int*>(ht->side + ht->side_cap);
+	int* flags = reinterpret_cast<int*>(side_count + 1);
+	for (int attempt = 0; attempt < 2; ++attempt) {
+		PG_CUDA(ctx, cudaMemsetAsync(ht->slots, 0xFF, ht->capacity * 16, s));
+		PG_CUDA(ctx, cudaMemsetAsync(side_count, 0, 8, s));
+		if (R->n) {
+			int blocks = (int) std::min<uint64_t>(pg_div_up(R->n, 256), (uint64_t) ctx->sm_count * 16);
+			k_ht_build<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off, R->key_bytes,
+					ht->bcols, ht->inline_val, ht->slots, ht->log2cap, ht->side, ht->side_cap,
+					side_count, flags, ctx->d_status);
+			PG_LAUNCHED(ctx);
+		}
+		unsigned int hdr[2];
+		PG_CUDA(ctx, cudaMemcpyAsync(hdr, side_count, 8, cudaMemcpyDeviceToHost, s));
+		if ((rc = pg_check_status(ctx, s, "pg_hashjoin_build"))) { pg_hashtable_free(ctx, ht); return rc; }
+		ht->nside = hdr[0];
+		ht->unique = (hdr[1] & 1) == 0 && ht->nside <= 1;
+		if (!(hdr[1] & 2)) break;
+		// More empty-marker keys than the side list holds: grow it and rebuild.
+		pg_free_async(ctx, s, ht->side);
+		ht->side_cap = hdr[0];
+		if ((rc = pg_alloc_async(ctx, s, (void**) &ht->side, ht->side_cap * 8 + 64))) { delete ht; return rc; }
+		side_count = reinterpret_cast<unsigned int*>(ht->side + ht->side_cap);
+		flags = reinterpret_cast<int*>(side_count + 1);
+	}
+	*out = ht;
+	return PG_OK;
+}
+
+extern "C" int pg_hashtable_free(pg_ctx* ctx, pg_hashtable* ht)
+{
+	if (!ht) return PG_OK;
+	// Probes finish before they return (they read their counts back), so
+	// only work still queued on the build stream can use the table.
+	cudaStreamSynchronize(ht->stream);
+	pg_free_async(ctx, ht->stream, ht->slots);
+	pg_free_async(ctx, ht->stream, ht->side);
+	delete ht;
+	return PG_OK;
+}
+
+static int hj_make_cols(pg_ctx* ctx, const pg_hashtable* ht, const pg_col* proj, int nproj, HjCols* pc)
+{
+	if (nproj != ht->nproj) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe: projection differs from the build's");
+	pc->n = nproj;
+	int ow = 0, boff = 0;
+	for (int i = 0; i < nproj; ++i) {
+		if (proj[i].side != ht->proj[i].side || (proj[i].side == 0 &&
+				(proj[i].off != ht->proj[i].off || proj[i].bytes != ht->proj[i].bytes)))
+			return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe: projection differs from the build's");
+		pc->side[i] = (uint8_t) proj[i].side;
+		pc->words[i] = (uint8_t) (proj[i].bytes / 4);
+		if (proj[i].side) pc->src[i] = (uint16_t) (proj[i].off / 4);
+		else if (ht->inline_val) { pc->src[i] = (uint16_t) boff; boff += proj[i].bytes / 4; }
+		else pc->src[i] = (uint16_t) (proj[i].off / 4);
+		ow += pc->words[i];
+	}
+	pc->ow_words = ow;
+	return PG_OK;
+}
+
+extern "C" int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
+		const pg_rel* S, const pg_col* proj, int nproj,
+		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res)
+{
+	if (!ctx || !ht || !res) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe: null argument");
+	int rc;
+	if ((rc = hj_validate_rel(ctx, S, "pg_hashjoin_probe"))) return rc;
+	if ((rc = hj_validate_proj(ctx, proj, nproj, ht->wR, S->width))) return rc;
+	HjCols pc;
+	if ((rc = hj_make_cols(ctx, ht, proj, nproj, &pc))) return rc;
+	const bool materialize = (flags & PG_JOIN_MATERIALIZE) != 0;
+	if (sum_col >= nproj) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe: sum_col out of range");
+	if (!(flags & PG_JOIN_SUM)) sum_col = -1;
+	if (materialize && out_capacity && !out) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe: null output");
+	cudaStream_t s = (cudaStream_t) stream;
+	res->n_out = 0; res->sum = 0;
+	if (S->n == 0) return PG_OK;
+	unsigned long long* acc = nullptr;   // [cursor, count, sum, spare]
+	if ((rc = pg_alloc_async(ctx, s, (void**) &acc, 64))) return rc;
+	PG_CUDA(ctx, cudaMemsetAsync(acc, 0, 64, s));
+	const uint64_t ntiles = pg_div_up(S->n, HJ_TILE);
+	const int grid_persist = (int) std::min<uint64_t>(ntiles, (uint64_t) ctx->sm_count * 8);
+	const bool fast16 = S->width == 16 && (S->key_off == 0 || S->key_off == 8) && S->key_bytes == 8 && pc.ow_words == 4;
+	unsigned long long host_acc[4] = {0, 0, 0, 0};
+
+	if (ht->unique && ht->inline_val) {
+		if (materialize) {
+			if (fast16)
+				k_probe_unique<true, true><<<grid_persist, HJ_THREADS, 0, s>>>((const char*) S->data, S->n, S->width,
+						S->key_off, S->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, (char*) out,
+						out_capacity, acc, acc + 1, sum_col, ctx->d_status);
+			else
+				k_probe_unique<true, false><<<grid_persist, HJ_THREADS, 0, s>>>((const char*) S->data, S->n, S->width,
+						S->key_off, S->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, (char*) out,
+						out_capacity, acc, acc + 1, sum_col, ctx->d_status);
+			PG_LAUNCHED(ctx);
+			PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
+			if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
+			res->n_out = host_acc[0];
+			if (sum_col >= 0 || (flags & PG_JOIN_COUNT)) {
+				// Fold count/sum over what was written (second, cheap pass).
+				k_probe_unique<false, false><<<grid_persist, HJ_THREADS, 0, s>>>((const char*) S->data, S->n, S->width,
+						S->key_off, S->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, nullptr, 0,
+						acc, acc + 1, sum_col, ctx->d_status);
+				PG_LAUNCHED(ctx);
+				PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
+				if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
+				res->sum = (int64_t) host_acc[2];
+			}
+		} else {
+			k_probe_unique<false, false><<<grid_persist, HJ_THREADS, 0, s>>>((const char*) S->data, S->n, S->width,
+					S->key_off, S->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, nullptr, 0,
+					acc, acc + 1, sum_col, ctx->d_status);
+			PG_LAUNCHED(ctx);
+			PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
+			if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
+			res->n_out = host_acc[1];
+			res->sum = (int64_t) host_acc[2];
+		}
+		pg_free_async(ctx, s, acc);
+		if (materialize && res->n_out > out_capacity)
+			return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_hashjoin_probe: output capacity too small");
+		return PG_OK;
+	}
+
+	// General path: one CTA per tile for the count pass, scan, write pass.
+	uint64_t* tile_counts = nullptr;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &tile_counts, (ntiles + 1) * 8))) return rc;
+	k_probe_general<false><<<(unsigned) ntiles, HJ_THREADS, 0, s>>>((const char*) S->data, S->n, S->width,
+			S->key_off, S->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, ht->inline_val,
+			ht->R, ht->wR, tile_counts, nullptr, acc + 1, sum_col, ctx->d_status);
+	PG_LAUNCHED(ctx);
+	if ((rc = pg_scan_u64(ctx, s, tile_counts, ntiles, (uint64_t*) acc))) return rc;
+	PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
+	if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
+	res->n_out = host_acc[0];
+	res->sum = (int64_t) host_acc[2];
+	if (materialize) {
+		if (res->n_out > out_capacity) {
+			pg_free_async(ctx, s, tile_counts); pg_free_async(ctx, s, acc);
+			return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_hashjoin_probe: output capacity too small");
+		}
+		k_probe_general<true><<<(unsigned) ntiles, HJ_THREADS, 0, s>>>((const char*) S->data, S->n, S->width,
+				S->key_off, S->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, ht->inline_val,
+				ht->R, ht->wR, tile_counts, (char*) out, acc + 1, -1, ctx->d_status);
+		PG_LAUNCHED(ctx);
+		if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
+	}
+	pg_free_async(ctx, s, tile_counts);
+	pg_free_async(ctx, s, acc);
+	return PG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Whole join through host buffers: build from R, then stream S through the
+// device in chunks on three streams so that the host->device copy of chunk
+// i+1, the probe of chunk i and the device->host copy of chunk i-1 overlap.
+// ---------------------------------------------------------------------------
+#define HJH_CHUNK (8ull << 20)
+
+extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
+		const pg_col* proj, int nproj, void* out_host, uint64_t out_capacity,
+		int flags, int sum_col, pg_join_result* res)
+{
+	if (!ctx || !Rh || !Sh || !res) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_host: null argument");
+	int rc;
+	if ((rc = hj_validate_proj(ctx, proj, nproj, Rh->width, Sh->width))) return rc;
+	const bool materialize = (flags & PG_JOIN_MATERIALIZE) != 0;
+	if (materialize && out_capacity && !out_host) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_host: null output");
+	uint32_t ow = 0;
+	for (int i = 0; i < nproj; ++i) ow += proj[i].bytes;
+	res->n_out = 0; res->sum = 0;
+	cudaStream_t sin, scomp, sout;
+	PG_CUDA(ctx, cudaStreamCreateWithFlags(&sin, cudaStreamNonBlocking));
+	PG_CUDA(ctx, cudaStreamCreateWithFlags(&scomp, cudaStreamNonBlocking));
+	PG_CUDA(ctx, cudaStreamCreateWithFlags(&sout, cudaStreamNonBlocking));
+	char *dR = nullptr, *dS[2] = {nullptr, nullptr}, *dO[2] = {nullptr, nullptr};
+	unsigned long long* acc = nullptr;        // per chunk slot: [cursor, count, sum, pad] x 2
+	unsigned long long* hacc = nullptr;       // pinned copy of acc
+	pg_hashtable* ht = nullptr;
+	cudaEvent_t ev_in[2], ev_comp[2], ev_out[2];
+	for (int i = 0; i < 2; ++i) {
+		cudaEventCreateWithFlags(&ev_in[i], cudaEventDisableTiming);
+		cudaEventCreateWithFlags(&ev_comp[i], cudaEventDisableTiming);
+		cudaEventCreateWithFlags(&ev_out[i], cudaEventDisableTiming);
+	}
+	auto cleanup = [&]() {
+		cudaStreamSynchronize(sin); cudaStreamSynchronize(scomp); cudaStreamSynchronize(sout);
+		if (ht) pg_hashtable_free(ctx, ht);
+		cudaFree(dR); cudaFree(dS[0]); cudaFree(dS[1]); cudaFree(dO[0]); cudaFree(dO[1]); cudaFree(acc);
+		if (hacc) cudaFreeHost(hacc);
+		for (int i = 0; i < 2; ++i) { cudaEventDestroy(ev_in[i]); cudaEventDestroy(ev_comp[i]); cudaEventDestroy(ev_out[i]); }
+		cudaStreamDestroy(sin); cudaStreamDestroy(scomp); cudaStreamDestroy(sout);
+	};
+#define HJH_TRY(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { int r_ = pg_cuda_fail(ctx, e_, #call); cleanup(); return r_; } } while (0)
+	const uint64_t nR = Rh->n, nS = Sh->n;
+	HJH_TRY(cudaMalloc(&dR, std::max<uint64_t>(16, nR * Rh->width)));
+	HJH_TRY(cudaMemcpyAsync(dR, Rh->data, nR * Rh->width, cudaMemcpyHostToDevice, scomp));
+	pg_rel R = *Rh; R.data = dR;
+	if ((rc = pg_hashjoin_build(ctx, scomp, &R, proj, nproj, &ht))) { cleanup(); return rc; }
+	HjCols pc;
+	if ((rc = hj_make_cols(ctx, ht, proj, nproj, &pc))) { cleanup(); return rc; }
+	if (!(flags & PG_JOIN_SUM)) sum_col = -1;
+	const uint64_t CH = std::min<uint64_t>(HJH_CHUNK, std::max<uint64_t>(nS, 1));
+	const bool pipelined = ht->unique && ht->inline_val;
+	if (!pipelined) {
+		// Duplicate keys: sizes are unknown until counted; one device pass.
+		char* dSall = nullptr;
+		HJH_TRY(cudaMalloc(&dSall, std::max<uint64_t>(16, nS * Sh->width)));
+		dS[0] = dSall;
+		HJH_TRY(cudaMemcpyAsync(dSall, Sh->data, nS * Sh->width, cudaMemcpyHostToDevice, scomp));
+		pg_rel S = *Sh; S.data = dSall;
+		char* dOut = nullptr;
+		pg_join_result r0;
+		if ((rc = pg_hashjoin_probe(ctx, scomp, ht, &S, proj, nproj, nullptr, 0, flags & ~PG_JOIN_MATERIALIZE, sum_col, &r0))) { cleanup(); return rc; }
+		if (materialize && r0.n_out) {
+			if (r0.n_out > out_capacity) { cleanup(); res->n_out = r0.n_out; return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_hashjoin_host: output capacity too small"); }
+			HJH_TRY(cudaMalloc(&dOut, r0.n_out * ow));
+			dO[0] = dOut;
+			if ((rc = pg_hashjoin_probe(ctx, scomp, ht, &S, proj, nproj, dOut, r0.n_out, PG_JOIN_MATERIALIZE, -1, &r0))) { cleanup(); return rc; }
+			HJH_TRY(cudaMemcpyAsync(out_host, dOut, r0.n_out * ow, cudaMemcpyDeviceToHost, scomp));
+			HJH_TRY(cudaStreamSynchronize(scomp));
+		}
+		*res = r0;
+		cleanup();
+		return PG_OK;
+	}
+	for (int i = 0; i < 2; ++i) {
+		HJH_TRY(cudaMalloc(&dS[i], CH * Sh->width));
+		if (materialize) HJH_TRY(cudaMalloc(&dO[i], CH * ow));
+	}
+	HJH_TRY(cudaMalloc(&acc, 2 * 4 * sizeof(unsigned long long)));
+	HJH_TRY(cudaMallocHost(&hacc, 2 * 4 * sizeof(unsigned long long)));
+	HJH_TRY(cudaStreamSynchronize(scomp));
+	const uint64_t nchunks = pg_div_up(nS, CH);
+	const bool fast16 = Sh->width == 16 && (Sh->key_off == 0 || Sh->key_off == 8) && Sh->key_bytes == 8 && pc.ow_words == 4;
+	const int grid = (int) std::min<uint64_t>(pg_div_up(CH, HJ_TILE), (uint64_t) ctx->sm_count * 8);
+	uint64_t written = 0;
+	unsigned long long count = 0, sum = 0;
+	auto issue = [&](uint64_t c) -> int {
+		const int b = (int) (c & 1);
+		const uint64_t r0 = c * CH, rows = std::min<uint64_t>(CH, nS - r0);
+		if (c >= 2) HJH_TRY(cudaStreamWaitEvent(sin, ev_comp[b], 0));     // input buffer free
+		HJH_TRY(cudaMemcpyAsync(dS[b], (const char*) Sh->data + r0 * Sh->width, rows * Sh->width,
+				cudaMemcpyHostToDevice, sin));
+		HJH_TRY(cudaEventRecord(ev_in[b], sin));
+		HJH_TRY(cudaStreamWaitEvent(scomp, ev_in[b], 0));
+		if (c >= 2) HJH_TRY(cudaStreamWaitEvent(scomp, ev_out[b], 0));   // output buffer free
+		HJH_TRY(cudaMemsetAsync(acc + 4 * b, 0, 32, scomp));
+		if (materialize) {
+			if (fast16)
+				k_probe_unique<true, true><<<grid, HJ_THREADS, 0, scomp>>>(dS[b], rows, Sh->width, Sh->key_off,
+						Sh->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, dO[b], CH,
+						acc + 4 * b, acc + 4 * b + 1, -1, ctx->d_status);
+			else
+				k_probe_unique<true, false><<<grid, HJ_THREADS, 0, scomp>>>(dS[b], rows, Sh->width, Sh->key_off,
+						Sh->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, dO[b], CH,
+						acc + 4 * b, acc + 4 * b + 1, -1, ctx->d_status);
+			g_kernel_launches.fetch_add(1);
+		}
+		if (!materialize || sum_col >= 0 || (flags & PG_JOIN_COUNT)) {
+			k_probe_unique<false, false><<<grid, HJ_THREADS, 0, scomp>>>(dS[b], rows, Sh->width, Sh->key_off,
+					Sh->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, nullptr, 0,
+					acc + 4 * b, acc + 4 * b + 1, sum_col, ctx->d_status);
+			g_kernel_launches.fetch_add(1);
+		}
+		HJH_TRY(cudaGetLastError());
+		HJH_TRY(cudaMemcpyAsync(hacc + 4 * b, acc + 4 * b, 32, cudaMemcpyDeviceToHost, scomp));
+		HJH_TRY(cudaEventRecord(ev_comp[b], scomp));
+		return PG_OK;
+	};
+	if (nchunks && (rc = issue(0))) return rc;
+	for (uint64_t c = 0; c < nchunks; ++c) {
+		const int b = (int) (c & 1);
+		if (c + 1 < nchunks && (rc = issue(c + 1))) return rc;
+		HJH_TRY(cudaEventSynchronize(ev_comp[b]));
+		const unsigned long long rows_out = hacc[4 * b];
+		count += materialize ? rows_out : hacc[4 * b + 1];
+		if (!materialize || sum_col >= 0 || (flags & PG_JOIN_COUNT)) sum += hacc[4 * b + 2];
+		if (materialize && rows_out) {
+			if (written + rows_out > out_capacity) { written += rows_out; continue; }
+			HJH_TRY(cudaStreamWaitEvent(sout, ev_comp[b], 0));
+			HJH_TRY(cudaMemcpyAsync((char*) out_host + written * ow, dO[b], rows_out * ow, cudaMemcpyDeviceToHost, sout));
+			written += rows_out;
+		}
+		HJH_TRY(cudaEventRecord(ev_out[b], sout));
+	}
+	HJH_TRY(cudaStreamSynchronize(sout));
+	if ((rc = pg_check_status(ctx, scomp, "pg_hashjoin_host"))) { cleanup(); return rc; }
+	if (materialize && (flags & PG_JOIN_COUNT) == 0 && sum_col < 0) count = written;
+	res->n_out = materialize ? written : count;
+	res->sum = (int64_t) sum;
+	cleanup();
+#undef HJH_TRY
+	if (materialize && written > out_capacity)
+		return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_hashjoin_host: output capacity too small");
+	return PG_OK;
+}

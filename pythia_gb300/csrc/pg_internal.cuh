@@ -1,0 +1,229 @@
+// Internal definitions shared by the sm_103a kernels of libpythia_gpu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <mutex>
+#include <atomic>
+#include "../../include/pythia_gpu.h"
+
+// ---------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------
+struct pg_ctx {
+	int device;
+	int sm_count;
+	cudaMemPool_t pool;
+	int* d_status;          // sticky device error word (PG_ERR_*), 0 = fine
+	unsigned long long* d_scratch64;  // small per-context device scratch (counters)
+	std::mutex mu;
+	std::string last_error;
+};
+
+extern std::atomic<uint64_t> g_kernel_launches;
+
+int pg_fail(pg_ctx* ctx, int code, const std::string& msg);
+int pg_cuda_fail(pg_ctx* ctx, cudaError_t e, const char* what);
+
+#define PG_CUDA(ctx, call)                                                   \
+	do {                                                                     \
+		cudaError_t e_ = (call);                                             \
+		if (e_ != cudaSuccess) return pg_cuda_fail((ctx), e_, #call);        \
+	} while (0)
+
+// Records a kernel launch and checks its configuration error.
+#define PG_LAUNCHED(ctx)                                                     \
+	do {                                                                     \
+		g_kernel_launches.fetch_add(1, std::memory_order_relaxed);           \
+		cudaError_t e_ = cudaGetLastError();                                 \
+		if (e_ != cudaSuccess) return pg_cuda_fail((ctx), e_, "kernel launch"); \
+	} while (0)
+
+// Stream-ordered scratch from the context's pool.
+int pg_alloc_async(pg_ctx* ctx, cudaStream_t s, void** p, size_t bytes);
+void pg_free_async(pg_ctx* ctx, cudaStream_t s, void* p);
+// Reads the sticky status after synchronising `s`; returns its PG_ERR_* code.
+int pg_check_status(pg_ctx* ctx, cudaStream_t s, const char* what);
+
+// ---------------------------------------------------------------------------
+// Bucket functions (hash.h:51-479) in the form their constructors leave them.
+// ---------------------------------------------------------------------------
+struct pg_hashfn {
+	int32_t fn;
+	int64_t k;            // HashFunction::_k as each subclass uses it
+	int64_t min, max;
+	int64_t bucketrange;
+	uint32_t skipbits;
+	uint32_t nbuckets;
+};
+
+int pg_hashfn_derive(const pg_hashcfg* c, pg_hashfn* f);
+
+// Key columns are 4-byte aligned (column offsets and tuple widths are
+// multiples of 4); an 8-byte key may straddle an 8-byte boundary.
+__device__ __forceinline__ int64_t pg_load_key(const char* p, uint32_t bytes)
+{
+	if (bytes == 4) return (int64_t) *reinterpret_cast<const int32_t*>(p);
+	if ((reinterpret_cast<uintptr_t>(p) & 7) == 0) return *reinterpret_cast<const int64_t*>(p);
+	const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
+	return (int64_t) (((uint64_t) q[1] << 32) | q[0]);
+}
+
+// Bucket of one field value; mirrors the reference's arithmetic exactly,
+// including its unsigned-int truncations.
+__device__ __forceinline__ uint32_t pg_hash_field(const pg_hashfn& f, const char* p, uint32_t size)
+{
+	switch (f.fn) {
+	case PG_FN_BYTES: {
+		uint64_t h = 14695981039346656037ull;
+		for (uint32_t i = 0; i < size; ++i) {
+			h ^= (uint64_t) (int64_t) (signed char) p[i];
+			h += (h << 1) + (h << 4) + (h << 5) + (h << 7) + (h << 8) + (h << 40);
+		}
+		return (uint32_t) (((h >> f.k) ^ h) & ((1ull << f.k) - 1));
+	}
+	case PG_FN_TPCHQ1MAGIC: {
+		uint32_t v = *reinterpret_cast<const uint32_t*>(p);
+		return (((v >> 4) | (v >> 16)) & 0x1u) | ((v >> 1) & 0x2u);
+	}
+	case PG_FN_ALWAYSZERO: return 0;
+	default: break;
+	}
+	int64_t v = pg_load_key(p, size);
+	switch (f.fn) {
+	case PG_FN_MODULO: return (uint32_t) (v & f.k);
+	case PG_FN_RANGE: {
+		int64_t val = (int64_t) ((uint64_t) (v - f.min) << f.k);
+		return (uint32_t) (val / (f.max - f.min + 1));
+	}
+	case PG_FN_EXACTRANGE: return (uint32_t) ((v - f.min) / f.bucketrange);
+	case PG_FN_PARAMMODULO: return (uint32_t) (((v - f.min) & f.k) >> f.skipbits);
+	case PG_FN_KNUTH:
+		return (uint32_t) ((((uint64_t) v * 2654435761ull) & (uint64_t) f.k) >> f.skipbits);
+	case PG_FN_TPCHORDERKEY: return (uint32_t) ((((v >> 2) & ~7LL) | (v & 7)) & f.k);
+	case PG_FN_WILLIS: {
+		uint64_t l = (uint64_t) v;
+		l = ~l + (l << 21);
+		l = (uint64_t) ((int64_t) l ^ ((int64_t) l >> 24));
+		l = l + (l << 3) + (l << 8);
+		l = (uint64_t) ((int64_t) l ^ ((int64_t) l >> 14));
+		l = l + (l << 2) + (l << 4);
+		l = (uint64_t) ((int64_t) l ^ ((int64_t) l >> 28));
+		l = l + (l << 31);
+		int64_t s = (int64_t) l;
+		s = (s > 0) ? s : (int64_t) (0 - (uint64_t) s);
+		return (uint32_t) (s & f.k);
+	}
+	default: return 0;
+	}
+}
+
+// 64-bit finaliser of MurmurHash3 (Appleby): slot placement for the
+// open-addressing tables. Bijective, so distinct keys never collide in full.
+__device__ __forceinline__ uint64_t pg_mix64(uint64_t k)
+{
+	k ^= k >> 33; k *= 0xff51afd7ed558ccdull;
+	k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull;
+	k ^= k >> 33;
+	return k;
+}
+
+// Empty-slot marker of the open-addressing tables (all one bits, so a table
+// clears with one memset). A real key equal to it takes a separate path.
+#define PG_EMPTY_KEY ((long long) -1)
+
+// Bounded spin budget for device-side waits.
+#define PG_SPIN_LIMIT (1u << 26)
+
+__device__ __forceinline__ void pg_set_status(int* status, int code)
+{
+	atomicCAS(status, 0, code);
+}
+
+// ---------------------------------------------------------------------------
+// PTX helpers: mbarrier + bulk (TMA) copies global -> shared
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t pg_smem_addr(const void* p)
+{
+	return (uint32_t) __cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void pg_mbar_init(uint64_t* bar, uint32_t count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(pg_smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void pg_fence_mbar_init()
+{
+	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void pg_mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+			:: "r"(pg_smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+// One-dimensional bulk copy (cp.async.bulk) of `bytes` (multiple of 16,
+// both addresses 16-byte aligned) completing on `bar`.
+__device__ __forceinline__ void pg_bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+			:: "r"(pg_smem_addr(dst)), "l"(src), "r"(bytes), "r"(pg_smem_addr(bar)) : "memory");
+}
+
+// Bounded wait for phase `parity` of `bar`. Returns false when it gave up.
+__device__ __forceinline__ bool pg_mbar_wait(uint64_t* bar, uint32_t parity)
+{
+	uint32_t a = pg_smem_addr(bar);
+	for (uint32_t it = 0; it < PG_SPIN_LIMIT; ++it) {
+		uint32_t done;
+		asm volatile("{\n\t.reg .pred p;\n\t"
+				"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+				"selp.u32 %0, 1, 0, p;\n\t}"
+				: "=r"(done) : "r"(a), "r"(parity) : "memory");
+		if (done) return true;
+	}
+	return false;
+}
+
+// L2 cache policies (createpolicy): streams are evict-first so that the
+// randomly accessed tables, loaded evict-last, stay resident in L2.
+__device__ __forceinline__ uint64_t pg_policy_evict_first()
+{
+	uint64_t p;
+	asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+	return p;
+}
+
+__device__ __forceinline__ uint64_t pg_policy_evict_last()
+{
+	uint64_t p;
+	asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+	return p;
+}
+
+__device__ __forceinline__ uint4 pg_ld_hint16(const void* p, uint64_t pol)
+{
+	uint4 v;
+	asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+			: "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p), "l"(pol));
+	return v;
+}
+
+__device__ __forceinline__ void pg_st_hint16(void* p, uint4 v, uint64_t pol)
+{
+	asm volatile("st.global.L1::no_allocate.L2::cache_hint.v4.u32 [%0], {%1,%2,%3,%4}, %5;"
+			:: "l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol) : "memory");
+}
+
+__device__ __forceinline__ uint4 pg_ld_stream16(const void* p) { return pg_ld_hint16(p, pg_policy_evict_first()); }
+__device__ __forceinline__ uint4 pg_ld_table16(const void* p) { return pg_ld_hint16(p, pg_policy_evict_last()); }
+__device__ __forceinline__ void pg_st_stream16(void* p, uint4 v) { pg_st_hint16(p, v, pg_policy_evict_first()); }
+
+__host__ __device__ __forceinline__ uint64_t pg_div_up(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
+__host__ __device__ __forceinline__ uint64_t pg_min64(uint64_t a, uint64_t b) { return a < b ? a : b; }
+__host__ __device__ __forceinline__ uint32_t pg_min32(uint32_t a, uint32_t b) { return a < b ? a : b; }
+
+// Exclusive scan of n uint64 values in place on the device (multi-block).
+int pg_scan_u64(pg_ctx* ctx, cudaStream_t s, uint64_t* data, uint64_t n, uint64_t* total_dev);

@@ -1,0 +1,246 @@
+// MPSM / sort-merge join on sm_103a.
+//
+// Replaces SortMergeJoinOp::BufferAndSort (operators/join.cpp:945-996) and
+// the merge loops of OldMPSMJoinOp / MPSMJoinOp (join.cpp:1245-1371,
+// 1516-1538; PresortedPrepartitionedMergeJoinOp::getNext, join.cpp:1929-1968),
+// which sort per-thread runs of both inputs and merge each build run against
+// the probe runs, buffering the build tuples of the current key
+// (mostfreqbuildkeyoccurances) and emitting the cartesian product of equal-key
+// groups.
+//
+// GPU plan: sort both relations (bitonic tile sort + merge-path merges,
+// pg_sort.cu), cut each sorted relation into equal-key runs (head flags +
+// scan), match build runs to probe runs by binary search over the sorted
+// probe run keys, scan the per-run output counts |R_k|*|S_k|, and either fold
+// count and sum (no output materialised; a build column sums as
+// |S_k| * sum_R_k, a probe column as |R_k| * sum_S_k, wrapping int64 like the
+// reference's CtLong +=) or write every pair, each thread producing a
+// contiguous slice of output positions (load-balanced over skewed groups).
+// The reference's per-key buffer limit does not exist here: any multiplicity
+// is joined.
+#include "pg_internal.cuh"
+#include "pg_sort.cuh"
+#include <algorithm>
+
+#define MJ_MAX_COLS 16
+
+struct MjCols {
+	int n, ow_words;
+	uint8_t side[MJ_MAX_COLS];
+	uint16_t off[MJ_MAX_COLS];    // byte offset in the side's tuple
+	uint8_t words[MJ_MAX_COLS];
+};
+
+struct MjSide {
+	const pg_rec* rec;   // sorted records
+	const char* rows;    // original tuples
+	uint32_t W, koff;
+	int mode;            // pg_sort_mode
+	const uint64_t* run_start;  // [nruns + 1]
+	uint64_t nruns;
+};
+
+// Word w of column (off, words) of the tuple behind record r.
+__device__ __forceinline__ uint32_t mj_word(const MjSide& sd, const pg_rec& r, uint32_t off, uint32_t w)
+{
+	if (sd.mode == 2) return reinterpret_cast<const uint32_t*>(sd.rows + r.val * sd.W + off)[w];
+	// 16-byte tuple: the key half and the other half.
+	uint32_t byte = off + 4 * w;
+	bool in_key = (byte >= sd.koff && byte < sd.koff + 8);
+	unsigned long long half = in_key ? (unsigned long long) r.key : r.val;
+	uint32_t rel = in_key ? byte - sd.koff : (byte >= 8 ? byte - 8 : byte);
+	return rel == 0 ? (uint32_t) half : (uint32_t) (half >> 32);
+}
+
+__device__ __forceinline__ unsigned long long mj_col64(const MjSide& sd, const pg_rec& r, uint32_t off, uint32_t words)
+{
+	uint32_t lo = mj_word(sd, r, off, 0);
+	if (words == 2) return ((unsigned long long) mj_word(sd, r, off, 1) << 32) | lo;
+	return (unsigned long long) (long long) (int32_t) lo;
+}
+
+__global__ void k_run_heads(const pg_rec* __restrict__ rec, uint64_t n, uint64_t* __restrict__ head)
+{
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+			i += (uint64_t) gridDim.x * blockDim.x)
+		head[i] = (i == 0 || rec[i].key != rec[i - 1].key) ? 1 : 0;
+}
+
+// After an exclusive scan, head[i] is the run id of a head element.
+__global__ void k_run_starts(const pg_rec* __restrict__ rec, uint64_t n, const uint64_t* __restrict__ rid,
+		uint64_t* __restrict__ start)
+{
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+			i += (uint64_t) gridDim.x * blockDim.x)
+		if (i == 0 || rec[i].key != rec[i - 1].key) start[rid[i]] = i;
+}
+
+// For every build run: matching probe run (or none), output count, and the
+// folded count/sum contribution.
+__global__ void k_match_runs(MjSide R, MjSide S, MjCols pc, int sum_col,
+		uint64_t* __restrict__ counts, uint64_t* __restrict__ match, unsigned long long* __restrict__ agg)
+{
+	unsigned long long sum_acc = 0;
+	for (uint64_t u = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; u < R.nruns;
+			u += (uint64_t) gridDim.x * blockDim.x) {
+		const uint64_t r0 = R.run_start[u], r1 = R.run_start[u + 1];
+		const long long k = R.rec[r0].key;
+		uint64_t lo = 0, hi = S.nruns;
+		while (lo < hi) {
+			uint64_t mid = (lo + hi) >> 1;
+			if (S.rec[S.run_start[mid]].key < k) lo = mid + 1; else hi = mid;
+		}
+		uint64_t c = 0;
+		match[u] = UINT64_MAX;
+		if (lo < S.nruns && S.rec[S.run_start[lo]].key == k) {
+			const uint64_t s0 = S.run_start[lo], s1 = S.run_start[lo + 1];
+			c = (r1 - r0) * (s1 - s0);
+			match[u] = lo;
+			if (sum_col >= 0) {
+				unsigned long long part = 0;
+				if (pc.side[sum_col] == 0) {
+					for (uint64_t i = r0; i < r1; ++i) part += mj_col64(R, R.rec[i], pc.off[sum_col], pc.words[sum_col]);
+					sum_acc += part * (unsigned long long) (s1 - s0);
+				} else {
+					for (uint64_t i = s0; i < s1; ++i) part += mj_col64(S, S.rec[i], pc.off[sum_col], pc.words[sum_col]);
+					sum_acc += part * (unsigned long long) (r1 - r0);
+				}
+			}
+		}
+		counts[u] = c;
+	}
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) sum_acc += __shfl_down_sync(0xffffffffu, sum_acc, o);
+	if ((threadIdx.x & 31) == 0 && sum_acc) atomicAdd(agg, sum_acc);
+}
+
+#define MJ_PER_THREAD 8
+
+// Writes output rows [t*8, t*8+8): pair (u, v) of position p is found by a
+// binary search over the scanned counts; within a pair, position q maps to
+// probe tuple q / |R_u| and build tuple q % |R_u|.
+__global__ void k_mj_write(MjSide R, MjSide S, MjCols pc, const uint64_t* __restrict__ offs,
+		const uint64_t* __restrict__ match, uint64_t nout, char* __restrict__ out)
+{
+	const uint64_t ow = (uint64_t) pc.ow_words * 4;
+	for (uint64_t t = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; t * MJ_PER_THREAD < nout;
+			t += (uint64_t) gridDim.x * blockDim.x) {
+		uint64_t p = t * MJ_PER_THREAD;
+		const uint64_t pend = pg_min64(nout, p + MJ_PER_THREAD);
+		// upper_bound(offs, p) - 1 over runs with offsets
+		uint64_t lo = 0, hi = R.nruns;
+		while (lo < hi) {
+			uint64_t mid = (lo + hi) >> 1;
+			if (offs[mid] <= p) lo = mid + 1; else hi = mid;
+		}
+		uint64_t u = lo - 1;
+		while (p < pend) {
+			while (offs[u + 1] <= p) ++u;           // skip empty runs
+			const uint64_t v = match[u];
+			const uint64_t r0 = R.run_start[u], nr = R.run_start[u + 1] - r0;
+			const uint64_t s0 = S.run_start[v];
+			uint64_t q = p - offs[u];
+			const uint64_t stop = pg_min64(pend, offs[u + 1]);
+			for (; p < stop; ++p, ++q) {
+				const pg_rec& br = R.rec[r0 + q % nr];
+				const pg_rec& pr = S.rec[s0 + q / nr];
+				uint32_t* o = reinterpret_cast<uint32_t*>(out + p * ow);
+				int wo = 0;
+				for (int c = 0; c < pc.n; ++c)
+					for (int w = 0; w < pc.words[c]; ++w)
+						o[wo++] = pc.side[c] ? mj_word(S, pr, pc.off[c], w) : mj_word(R, br, pc.off[c], w);
+			}
+		}
+	}
+}
+
+static int mj_runs(pg_ctx* ctx, cudaStream_t s, const pg_rec* rec, uint64_t n, uint64_t** starts, uint64_t* nruns)
+{
+	int rc;
+	uint64_t* head = nullptr;
+	uint64_t* total = nullptr;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &head, (n + 1) * 8))) return rc;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &total, 8))) return rc;
+	int blocks = (int) std::min<uint64_t>(pg_div_up(std::max<uint64_t>(n, 1), 256), (uint64_t) ctx->sm_count * 16);
+	if (n) { k_run_heads<<<blocks, 256, 0, s>>>(rec, n, head); PG_LAUNCHED(ctx); }
+	if ((rc = pg_scan_u64(ctx, s, head, n, total))) return rc;
+	uint64_t nr = 0;
+	PG_CUDA(ctx, cudaMemcpyAsync(&nr, total, 8, cudaMemcpyDeviceToHost, s));
+	PG_CUDA(ctx, cudaStreamSynchronize(s));
+	uint64_t* st = nullptr;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &st, (nr + 1) * 8))) return rc;
+	if (n) { k_run_starts<<<blocks, 256, 0, s>>>(rec, n, head, st); PG_LAUNCHED(ctx); }
+	PG_CUDA(ctx, cudaMemcpyAsync(st + nr, &n, 8, cudaMemcpyHostToDevice, s));
+	pg_free_async(ctx, s, head);
+	pg_free_async(ctx, s, total);
+	*starts = st; *nruns = nr;
+	return PG_OK;
+}
+
+extern "C" int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, const pg_rel* S,
+		const pg_col* proj, int nproj, void* out, uint64_t out_capacity,
+		int flags, int sum_col, pg_join_result* res)
+{
+	if (!ctx || !R || !S || !res) return pg_fail(ctx, PG_ERR_ARG, "pg_mpsm_join: null argument");
+	for (const pg_rel* r : {R, S}) {
+		if (r->n && !r->data) return pg_fail(ctx, PG_ERR_ARG, "pg_mpsm_join: null data");
+		if (r->width == 0 || (r->width & 3) || (r->key_bytes != 4 && r->key_bytes != 8) ||
+				(r->key_off & 3) || r->key_off + r->key_bytes > r->width)
+			return pg_fail(ctx, PG_ERR_UNSUPPORTED, "pg_mpsm_join: 4-byte-aligned tuples with an int or long key");
+	}
+	if (nproj < 0 || nproj > MJ_MAX_COLS) return pg_fail(ctx, PG_ERR_ARG, "pg_mpsm_join: 0..16 columns");
+	MjCols pc; pc.n = nproj; pc.ow_words = 0;
+	for (int i = 0; i < nproj; ++i) {
+		const pg_col& c = proj[i];
+		uint32_t w = c.side ? S->width : R->width;
+		if (c.side > 1 || (c.bytes != 4 && c.bytes != 8) || (c.off & 3) || c.off + c.bytes > w)
+			return pg_fail(ctx, PG_ERR_UNSUPPORTED, "pg_mpsm_join: projected columns must be 4/8 bytes, aligned");
+		pc.side[i] = (uint8_t) c.side; pc.off[i] = (uint16_t) c.off; pc.words[i] = (uint8_t) (c.bytes / 4);
+		pc.ow_words += c.bytes / 4;
+	}
+	if (sum_col >= nproj) return pg_fail(ctx, PG_ERR_ARG, "pg_mpsm_join: sum_col out of range");
+	if (!(flags & PG_JOIN_SUM)) sum_col = -1;
+	const bool materialize = (flags & PG_JOIN_MATERIALIZE) != 0;
+	res->n_out = 0; res->sum = 0;
+	if (R->n == 0 || S->n == 0) return PG_OK;
+	cudaStream_t s = (cudaStream_t) stream;
+	int rc;
+	pg_rec *rr = nullptr, *sr = nullptr;
+	if ((rc = pg_sort_records(ctx, s, R, &rr))) return rc;
+	if ((rc = pg_sort_records(ctx, s, S, &sr))) return rc;
+	MjSide RS{rr, (const char*) R->data, R->width, R->key_off, pg_sort_mode(R), nullptr, 0};
+	MjSide SS{sr, (const char*) S->data, S->width, S->key_off, pg_sort_mode(S), nullptr, 0};
+	uint64_t *rst = nullptr, *sst = nullptr;
+	if ((rc = mj_runs(ctx, s, rr, R->n, &rst, &RS.nruns))) return rc;
+	if ((rc = mj_runs(ctx, s, sr, S->n, &sst, &SS.nruns))) return rc;
+	RS.run_start = rst; SS.run_start = sst;
+	uint64_t *counts = nullptr, *match = nullptr;
+	unsigned long long* acc = nullptr;  // [total, sum]
+	if ((rc = pg_alloc_async(ctx, s, (void**) &counts, (RS.nruns + 1) * 8))) return rc;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &match, (RS.nruns + 1) * 8))) return rc;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &acc, 16))) return rc;
+	PG_CUDA(ctx, cudaMemsetAsync(acc, 0, 16, s));
+	int blocks = (int) std::min<uint64_t>(pg_div_up(RS.nruns, 256), (uint64_t) ctx->sm_count * 16);
+	k_match_runs<<<blocks, 256, 0, s>>>(RS, SS, pc, sum_col, counts, match, acc + 1);
+	PG_LAUNCHED(ctx);
+	if ((rc = pg_scan_u64(ctx, s, counts, RS.nruns, (uint64_t*) acc))) return rc;
+	unsigned long long h[2];
+	PG_CUDA(ctx, cudaMemcpyAsync(h, acc, 16, cudaMemcpyDeviceToHost, s));
+	if ((rc = pg_check_status(ctx, s, "pg_mpsm_join"))) return rc;
+	res->n_out = h[0];
+	res->sum = (int64_t) h[1];
+	if (materialize && res->n_out) {
+		if (res->n_out > out_capacity) {
+			rc = pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_mpsm_join: output capacity too small");
+		} else {
+			PG_CUDA(ctx, cudaMemcpyAsync(counts + RS.nruns, &res->n_out, 8, cudaMemcpyHostToDevice, s));
+			int wb = (int) std::min<uint64_t>(pg_div_up(pg_div_up(res->n_out, MJ_PER_THREAD), 256), (uint64_t) ctx->sm_count * 16);
+			k_mj_write<<<wb, 256, 0, s>>>(RS, SS, pc, counts, match, res->n_out, (char*) out);
+			PG_LAUNCHED(ctx);
+			rc = pg_check_status(ctx, s, "pg_mpsm_join");
+		}
+	}
+	for (void* p : {(void*) rr, (void*) sr, (void*) rst, (void*) sst, (void*) counts, (void*) match, (void*) acc})
+		pg_free_async(ctx, s, p);
+	return rc;
+}

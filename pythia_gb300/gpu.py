@@ -1,0 +1,289 @@
+"""ctypes binding of the C ABI in include/pythia_gpu.h (libpythia_gpu.so).
+
+This is the same binding a Python caller of the Pythia GPU operators would
+write; tests and the benchmark drive every kernel through it. There is no CPU
+fallback: a missing library or device raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+PG_OK, PG_ERR_ARG, PG_ERR_OOM, PG_ERR_CUDA, PG_ERR_TIMEOUT = 0, 1, 2, 3, 4
+PG_ERR_TABLE_FULL, PG_ERR_OUTPUT_FULL, PG_ERR_UNSUPPORTED = 5, 6, 7
+JOIN_MATERIALIZE, JOIN_COUNT, JOIN_SUM = 1, 2, 4
+FN = {"bytes": 0, "modulo": 1, "range": 2, "exactrange": 3, "parammodulo": 4,
+      "knuth": 5, "tpchorderkey": 6, "willis": 7, "alwayszero": 8, "tpchq1magic": 9}
+VAL = {"int": 0, "long": 1, "dec": 2}
+AGG = {"sum": 0, "count": 1}
+
+
+class PgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"pythia_gpu error {code}: {msg}")
+        self.code = code
+
+
+class Rel(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("n", ctypes.c_uint64), ("width", ctypes.c_uint32),
+                ("key_off", ctypes.c_uint32), ("key_bytes", ctypes.c_uint32)]
+
+
+class HashCfg(ctypes.Structure):
+    _fields_ = [("fn", ctypes.c_int32), ("buckets", ctypes.c_uint32), ("min", ctypes.c_int64),
+                ("max", ctypes.c_int64), ("skipbits", ctypes.c_uint32), ("offset", ctypes.c_uint32)]
+
+
+class Col(ctypes.Structure):
+    _fields_ = [("side", ctypes.c_uint32), ("off", ctypes.c_uint32), ("bytes", ctypes.c_uint32)]
+
+
+class JoinResult(ctypes.Structure):
+    _fields_ = [("n_out", ctypes.c_uint64), ("sum", ctypes.c_int64)]
+
+
+SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_stream_create",
+           "pg_stream_destroy", "pg_sync", "pg_buffer_alloc", "pg_buffer_free", "pg_host_alloc",
+           "pg_host_free", "pg_h2d", "pg_d2h", "pg_memset", "pg_kernel_launches",
+           "pg_hash_buckets", "pg_hash_tuples", "pg_partition", "pg_partition_sort",
+           "pg_hashjoin_build", "pg_hashjoin_probe", "pg_hashtable_free", "pg_hashjoin_host",
+           "pg_groupby", "pg_sort_pages", "pg_mpsm_join"]
+
+
+def lib_path():
+    return os.path.join(_PKG, "libpythia_gpu.so")
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        p = lib_path()
+        if not os.path.exists(p):
+            raise RuntimeError(f"{p} is missing: run __graft_entry__.build() first")
+        L = ctypes.CDLL(p)
+        vp, u64, u32, ci, P = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int, ctypes.POINTER
+        sig = {
+            "pg_init": ([ci, u64, P(vp)], ci),
+            "pg_shutdown": ([vp], ci),
+            "pg_last_error": ([vp], ctypes.c_char_p),
+            "pg_device_status": ([vp], ci),
+            "pg_stream_create": ([vp, P(vp)], ci),
+            "pg_stream_destroy": ([vp, vp], ci),
+            "pg_sync": ([vp, vp], ci),
+            "pg_buffer_alloc": ([vp, u64, P(vp)], ci),
+            "pg_buffer_free": ([vp, vp], ci),
+            "pg_host_alloc": ([vp, u64, P(vp)], ci),
+            "pg_host_free": ([vp, vp], ci),
+            "pg_h2d": ([vp, vp, vp, vp, u64], ci),
+            "pg_d2h": ([vp, vp, vp, vp, u64], ci),
+            "pg_memset": ([vp, vp, vp, ci, u64], ci),
+            "pg_kernel_launches": ([], u64),
+            "pg_hash_buckets": ([vp, P(HashCfg), P(u32)], ci),
+            "pg_hash_tuples": ([vp, vp, P(Rel), P(HashCfg), vp], ci),
+            "pg_partition": ([vp, vp, P(Rel), P(HashCfg), vp, vp], ci),
+            "pg_partition_sort": ([vp, vp, P(Rel), vp, u32, vp], ci),
+            "pg_hashjoin_build": ([vp, vp, P(Rel), P(Col), ci, P(vp)], ci),
+            "pg_hashjoin_probe": ([vp, vp, vp, P(Rel), P(Col), ci, vp, u64, ci, ci, P(JoinResult)], ci),
+            "pg_hashtable_free": ([vp, vp], ci),
+            "pg_hashjoin_host": ([vp, P(Rel), P(Rel), P(Col), ci, vp, u64, ci, ci, P(JoinResult)], ci),
+            "pg_groupby": ([vp, vp, P(Rel), u32, ci, ci, u64, vp, u64, P(u64)], ci),
+            "pg_sort_pages": ([vp, vp, P(Rel), vp], ci),
+            "pg_mpsm_join": ([vp, vp, P(Rel), P(Rel), P(Col), ci, vp, u64, ci, ci, P(JoinResult)], ci),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes, f.restype = args, res
+        _LIB = L
+    return _LIB
+
+
+def hashcfg(fn, buckets=1, min=0, max=0, skipbits=0, offset=0):
+    return HashCfg(FN[fn] if isinstance(fn, str) else fn, buckets, min, max, skipbits, offset)
+
+
+def cols(spec):
+    """spec: [(side, byte offset, bytes)], side "B"/"P" (build/probe)."""
+    arr = (Col * max(1, len(spec)))()
+    for i, (s, o, b) in enumerate(spec):
+        arr[i] = Col(0 if s in ("B", 0) else 1, o, b)
+    return arr, len(spec)
+
+
+class DeviceBuffer:
+    def __init__(self, ctx, nbytes):
+        self.ctx, self.nbytes = ctx, int(nbytes)
+        p = ctypes.c_void_p()
+        ctx._check(lib().pg_buffer_alloc(ctx.h, max(16, self.nbytes), ctypes.byref(p)))
+        self.ptr = p.value
+
+    def free(self):
+        if self.ptr:
+            lib().pg_buffer_free(self.ctx.h, self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    """One pg_ctx on one device, with one stream."""
+
+    def __init__(self, device=0, reserve=0):
+        h = ctypes.c_void_p()
+        rc = lib().pg_init(device, reserve, ctypes.byref(h))
+        if rc:
+            raise PgError(rc, lib().pg_last_error(None).decode())
+        self.h = h.value
+        s = ctypes.c_void_p()
+        self._check(lib().pg_stream_create(self.h, ctypes.byref(s)))
+        self.stream = s.value
+
+    def _check(self, rc):
+        if rc:
+            raise PgError(rc, (lib().pg_last_error(self.h) or b"").decode())
+        return rc
+
+    def close(self):
+        if self.h:
+            lib().pg_stream_destroy(self.h, self.stream)
+            lib().pg_shutdown(self.h)
+            self.h = None
+
+    # ---- memory ----
+    def alloc(self, nbytes):
+        return DeviceBuffer(self, nbytes)
+
+    def upload(self, a):
+        a = np.ascontiguousarray(a)
+        b = DeviceBuffer(self, a.nbytes)
+        self._check(lib().pg_h2d(self.h, self.stream, b.ptr, a.ctypes.data, a.nbytes))
+        self.sync()
+        return b
+
+    def download(self, buf, nbytes, dtype=np.uint8):
+        out = np.empty(nbytes, dtype=np.uint8)
+        if nbytes:
+            self._check(lib().pg_d2h(self.h, self.stream, out.ctypes.data, buf.ptr, nbytes))
+            self.sync()
+        return out.view(dtype)
+
+    def sync(self):
+        self._check(lib().pg_sync(self.h, self.stream))
+
+    @staticmethod
+    def rel(buf, n, width, key_off=0, key_bytes=8):
+        return Rel(buf.ptr if buf is not None else None, n, width, key_off, key_bytes)
+
+    # ---- operators on numpy inputs (upload, run, download) ----
+    def hash_tuples(self, rows, cfg, key_off=0, key_bytes=8):
+        a = np.ascontiguousarray(rows)
+        n, w = a.shape[0], a.strides[0] if a.ndim > 1 else a.itemsize
+        d = self.upload(a)
+        o = self.alloc(4 * max(n, 1))
+        r = self.rel(d, n, w, key_off, key_bytes)
+        self._check(lib().pg_hash_tuples(self.h, self.stream, ctypes.byref(r), ctypes.byref(cfg), o.ptr))
+        return self.download(o, 4 * n, np.uint32)
+
+    def nbuckets(self, cfg):
+        nb = ctypes.c_uint32()
+        self._check(lib().pg_hash_buckets(self.h, ctypes.byref(cfg), ctypes.byref(nb)))
+        return nb.value
+
+    def partition(self, rows, cfg, key_off=0, key_bytes=8):
+        a = np.ascontiguousarray(rows)
+        n, w = a.shape[0], a.strides[0]
+        nb = self.nbuckets(cfg)
+        d = self.upload(a)
+        o = self.alloc(a.nbytes)
+        offs = self.alloc(8 * (nb + 1))
+        r = self.rel(d, n, w, key_off, key_bytes)
+        self._check(lib().pg_partition(self.h, self.stream, ctypes.byref(r), ctypes.byref(cfg),
+                                       o.ptr, offs.ptr))
+        out = self.download(o, a.nbytes).view(a.dtype).reshape(a.shape)
+        return out, self.download(offs, 8 * (nb + 1), np.uint64)
+
+    def hashjoin(self, R, S, proj=(("P", 8, 8), ("B", 8, 8)), bkey=(0, 8), pkey=(0, 8),
+                 flags=JOIN_MATERIALIZE, sum_col=-1, out_cap=None):
+        Ra, Sa = np.ascontiguousarray(R), np.ascontiguousarray(S)
+        dR, dS = self.upload(Ra), self.upload(Sa)
+        rR = self.rel(dR, Ra.shape[0], Ra.strides[0] if Ra.shape[0] else Ra.itemsize * Ra.shape[1], *bkey)
+        rS = self.rel(dS, Sa.shape[0], Sa.strides[0] if Sa.shape[0] else Sa.itemsize * Sa.shape[1], *pkey)
+        c, nc = cols(proj)
+        ow = sum(b for _, _, b in proj)
+        ht = ctypes.c_void_p()
+        self._check(lib().pg_hashjoin_build(self.h, self.stream, ctypes.byref(rR), c, nc, ctypes.byref(ht)))
+        try:
+            res = JoinResult()
+            if flags & JOIN_MATERIALIZE:
+                cap = Sa.shape[0] if out_cap is None else out_cap
+                o = self.alloc(max(cap, 1) * ow)
+                rc = lib().pg_hashjoin_probe(self.h, self.stream, ht.value, ctypes.byref(rS), c, nc,
+                                             o.ptr, cap, flags, sum_col, ctypes.byref(res))
+                if rc == PG_ERR_OUTPUT_FULL and out_cap is None:
+                    cap = res.n_out
+                    o = self.alloc(max(cap, 1) * ow)
+                    rc = lib().pg_hashjoin_probe(self.h, self.stream, ht.value, ctypes.byref(rS), c, nc,
+                                                 o.ptr, cap, flags, sum_col, ctypes.byref(res))
+                self._check(rc)
+                out = self.download(o, res.n_out * ow).reshape(-1, ow) if ow else None
+            else:
+                self._check(lib().pg_hashjoin_probe(self.h, self.stream, ht.value, ctypes.byref(rS), c, nc,
+                                                    None, 0, flags, sum_col, ctypes.byref(res)))
+                out = None
+        finally:
+            lib().pg_hashtable_free(self.h, ht.value)
+        return out, res.n_out, res.sum
+
+    def groupby(self, rows, key=(0, 8), val=(8, "long"), agg="sum", groups_hint=0, has_key=True):
+        a = np.ascontiguousarray(rows)
+        n, w = a.shape[0], a.strides[0]
+        d = self.upload(a)
+        vtype = VAL[val[1]]
+        aw = 4 if (agg == "sum" and vtype == 0) else 8
+        kb = key[1] if has_key else 0
+        ow = kb + aw
+        cap = max(n, 1)
+        o = self.alloc(cap * ow)
+        ng = ctypes.c_uint64()
+        r = self.rel(d, n, w, key[0] if has_key else 0, kb)
+        self._check(lib().pg_groupby(self.h, self.stream, ctypes.byref(r), val[0], vtype, AGG[agg],
+                                     groups_hint, o.ptr, cap, ctypes.byref(ng)))
+        return self.download(o, ng.value * ow).reshape(-1, ow)
+
+    def sort(self, rows, key=(0, 8)):
+        a = np.ascontiguousarray(rows)
+        n, w = a.shape[0], a.strides[0]
+        d = self.upload(a)
+        o = self.alloc(a.nbytes)
+        r = self.rel(d, n, w, *key)
+        self._check(lib().pg_sort_pages(self.h, self.stream, ctypes.byref(r), o.ptr))
+        return self.download(o, a.nbytes).view(a.dtype).reshape(a.shape)
+
+    def mpsm(self, R, S, proj=(("P", 8, 8), ("B", 8, 8)), bkey=(0, 8), pkey=(0, 8),
+             flags=JOIN_MATERIALIZE, sum_col=-1):
+        Ra, Sa = np.ascontiguousarray(R), np.ascontiguousarray(S)
+        dR, dS = self.upload(Ra), self.upload(Sa)
+        rR = self.rel(dR, Ra.shape[0], Ra.strides[0] if Ra.shape[0] else Ra.itemsize * Ra.shape[1], *bkey)
+        rS = self.rel(dS, Sa.shape[0], Sa.strides[0] if Sa.shape[0] else Sa.itemsize * Sa.shape[1], *pkey)
+        c, nc = cols(proj)
+        ow = sum(b for _, _, b in proj)
+        res = JoinResult()
+        rc = lib().pg_mpsm_join(self.h, self.stream, ctypes.byref(rR), ctypes.byref(rS), c, nc, None, 0,
+                                flags & ~JOIN_MATERIALIZE, sum_col, ctypes.byref(res))
+        self._check(rc)
+        if not flags & JOIN_MATERIALIZE:
+            return None, res.n_out, res.sum
+        o = self.alloc(max(res.n_out, 1) * ow)
+        self._check(lib().pg_mpsm_join(self.h, self.stream, ctypes.byref(rR), ctypes.byref(rS), c, nc,
+                                       o.ptr, res.n_out, flags, sum_col, ctypes.byref(res)))
+        return self.download(o, res.n_out * ow).reshape(-1, ow), res.n_out, res.sum
+
+
+def kernel_launches():
+    return lib().pg_kernel_launches()

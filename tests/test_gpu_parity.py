@@ -1,0 +1,358 @@
+"""GPU parity: every operator through the C ABI against the oracle.
+
+Integer work (hash buckets, partitions, join rows, counts, integer sums, sort
+keys) must match bit for bit; unordered outputs (joins, group-by) compare as
+sorted multisets. Double sums: relative error <= 1e-12 against the exactly
+rounded sum (the tolerance the operator contract states).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from pythia_gb300 import datagen as dg
+from pythia_gb300 import gpu
+from tests.golden import inputs as gin
+
+pytestmark = pytest.mark.gpu
+DEC_RTOL = 1e-12
+
+
+def canon(a):
+    return orc.canonical(np.ascontiguousarray(a))
+
+
+# ---------------------------------------------------------------- hashing
+HASHES = [("bytes", {}), ("modulo", {}), ("range", {"min": -1000, "max": 1000}),
+          ("exactrange", {"min": -1000, "max": 1000}), ("parammodulo", {"skipbits": 3, "offset": 7}),
+          ("knuth", {"skipbits": 2, "offset": 5}), ("tpchorderkey", {}), ("willis", {}),
+          ("alwayszero", {}), ("tpchq1magic", {})]
+
+
+@pytest.mark.parametrize("fn,extra", HASHES)
+@pytest.mark.parametrize("buckets", [1, 7, 100, 4096])
+def test_hash_functions(ctx, fn, extra, buckets):
+    rows = gin.make({"gen": "formula", "name": "signed_keys", "n": 5000})
+    cfg_g = gpu.hashcfg(fn, buckets, **extra)
+    cfg_o = orc.hashcfg(fn, buckets, **extra)
+    assert ctx.nbuckets(cfg_g) == orc.hashfn(cfg_o).nbuckets
+    for off, size in ((0, 8), (8, 8)):
+        got = ctx.hash_tuples(rows, cfg_g, off, size)
+        want = orc.hash_column(cfg_o, rows, off, size)
+        assert np.array_equal(got, want), fn
+
+
+def test_hash_int32_keys(ctx):
+    rows = gin.make({"gen": "formula", "name": "int_pairs", "n": 4096})
+    for fn in ("modulo", "bytes", "knuth", "willis", "parammodulo"):
+        got = ctx.hash_tuples(rows, gpu.hashcfg(fn, 256), 4, 4)
+        want = orc.hash_column(orc.hashcfg(fn, 256), rows, 4, 4)
+        assert np.array_equal(got, want), fn
+
+
+# ---------------------------------------------------------------- partition
+def _part_check(ctx, rows, cfg_g, cfg_o, key=(0, 8)):
+    got, goffs = ctx.partition(rows, cfg_g, *key)
+    want, woffs = orc.partition(rows, cfg_o, key)
+    assert np.array_equal(goffs, woffs)
+    assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), "partition output (stable order) differs"
+
+
+@pytest.mark.parametrize("T", [1, 3, 7, 15, 127])
+def test_partition_exactrange(ctx, T):
+    rows = dg.uniform_keys(100_000, 50_000, dg.seed_for(20 + T))
+    _part_check(ctx, rows, gpu.hashcfg("exactrange", T, 0, 49_999), orc.hashcfg("exactrange", T, 0, 49_999))
+
+
+@pytest.mark.parametrize("bits", [4, 6, 8, 10, 12])
+def test_partition_radix(ctx, bits):
+    rows = dg.uniform_keys(300_001, 1 << 40, dg.seed_for(30 + bits))
+    cfg = dict(buckets=1 << bits, skipbits=3)
+    _part_check(ctx, rows, gpu.hashcfg("parammodulo", **cfg), orc.hashcfg("parammodulo", **cfg))
+
+
+def test_partition_zipf_skew(ctx):
+    rows = dg.zipf_keys(200_000, 10_000, 1.0, dg.seed_for(40))
+    _part_check(ctx, rows, gpu.hashcfg("exactrange", 5, 0, 9999), orc.hashcfg("exactrange", 5, 0, 9999))
+
+
+def test_partition_widths(ctx):
+    # 20-byte tuples (int, long, long) keyed on the long at offset 4, and
+    # 8-byte (int, int) tuples keyed on an int.
+    base = dg.uniform_keys(50_003, 1000, dg.seed_for(41))
+    t20 = np.zeros((base.shape[0], 5), dtype=np.int32)
+    t20[:, 0] = np.arange(base.shape[0])
+    t20[:, 1:5] = base.view(np.int32)
+    _part_check(ctx, t20, gpu.hashcfg("exactrange", 9, 0, 999), orc.hashcfg("exactrange", 9, 0, 999), key=(4, 8))
+    t8 = gin.make({"gen": "formula", "name": "int_pairs", "n": 70_000})
+    _part_check(ctx, t8, gpu.hashcfg("modulo", 64), orc.hashcfg("modulo", 64), key=(0, 4))
+
+
+def test_partition_edge_sizes(ctx):
+    for n in (0, 1, 2047, 2048, 2049, 4096):
+        rows = dg.uniform_keys(n, 100, dg.seed_for(42))
+        _part_check(ctx, rows, gpu.hashcfg("modulo", 16), orc.hashcfg("modulo", 16))
+
+
+def test_partition_out_of_range_is_an_error(ctx):
+    rows = dg.uniform_keys(1000, 100, dg.seed_for(43))
+    with pytest.raises(gpu.PgError):
+        ctx.partition(rows, gpu.hashcfg("exactrange", 4, 0, 49))   # keys up to 99 exceed the range
+
+
+# ---------------------------------------------------------------- hash join
+def _join_check(ctx, R, S, proj=(("P", 8, 8), ("B", 8, 8)), bkey=(0, 8), pkey=(0, 8), buckets=1024):
+    got, n, _ = ctx.hashjoin(R, S, proj=proj, bkey=bkey, pkey=pkey)
+    want, wn, _ = orc.hashjoin(R, S, proj=proj, bkey=bkey, pkey=pkey, hash=orc.hashcfg("modulo", buckets))
+    assert n == wn
+    assert np.array_equal(canon(got), canon(want))
+    sc = len(proj) - 1
+    _, n2, s2 = ctx.hashjoin(R, S, proj=proj, bkey=bkey, pkey=pkey, flags=gpu.JOIN_COUNT | gpu.JOIN_SUM, sum_col=sc)
+    _, wn2, ws2 = orc.hashjoin(R, S, proj=proj, bkey=bkey, pkey=pkey, materialise=False, sum_col=sc,
+                               hash=orc.hashcfg("modulo", buckets))
+    assert (n2, s2) == (wn2, ws2)
+    return n
+
+
+def test_join_pkfk_uniform(ctx):
+    R = dg.build_relation(50_000, dg.seed_for(1))
+    S = dg.probe_uniform(400_000, R, dg.seed_for(2))
+    assert _join_check(ctx, R, S) == 400_000
+
+
+def test_join_pkfk_zipf(ctx):
+    R = dg.build_relation(30_000, dg.seed_for(11))
+    S = dg.probe_zipf(300_000, 1.0, R, dg.seed_for(12))
+    _join_check(ctx, R, S)
+
+
+def test_join_many_to_many(ctx):
+    R = dg.uniform_keys(5000, 700, dg.seed_for(5))
+    S = dg.uniform_keys(9000, 900, dg.seed_for(6))
+    _join_check(ctx, R, S)
+
+
+def test_join_projection_orders(ctx):
+    R = dg.build_relation(3000, dg.seed_for(7))
+    S = dg.probe_uniform(9000, R, dg.seed_for(8))
+    _join_check(ctx, R, S, proj=(("B", 0, 8), ("P", 8, 8), ("B", 8, 8)))   # 24-byte rows
+    _join_check(ctx, R, S, proj=(("B", 8, 8), ("P", 8, 8)))
+    _join_check(ctx, R, S, proj=(("P", 0, 8), ("P", 8, 8), ("B", 8, 4), ("B", 12, 4)))
+    _join_check(ctx, R, S, proj=(("B", 0, 8), ("B", 8, 8), ("P", 8, 8)))   # 16 B of build columns: row-index path
+
+
+def test_join_edge_cases(ctx):
+    R = dg.build_relation(1000, dg.seed_for(9))
+    empty = np.zeros((0, 2), dtype=np.int64)
+    assert _join_check(ctx, R, empty) == 0
+    assert _join_check(ctx, empty, R) == 0
+    big = gin.make({"gen": "formula", "name": "big_keys", "n": 5000})
+    assert _join_check(ctx, R, big) == 0
+    one = R[:1].copy()
+    assert _join_check(ctx, one, one) == 1
+
+
+def test_join_empty_marker_key(ctx):
+    # -1 is the tables' empty marker; a real key -1 must still join.
+    R = dg.build_relation(2000, dg.seed_for(13))
+    R[17, 0] = -1
+    S = dg.probe_uniform(10_000, R, dg.seed_for(14))
+    S[::97, 0] = -1
+    _join_check(ctx, R, S)
+    R2 = R.copy()
+    R2[18, 0] = -1                           # two build tuples with key -1
+    _join_check(ctx, R2, S)
+
+
+def test_join_negative_and_int32_keys(ctx):
+    R = gin.make({"gen": "formula", "name": "signed_keys", "n": 3000})
+    S = gin.make({"gen": "formula", "name": "signed_keys", "n": 3000})
+    _join_check(ctx, R, S)
+    I = gin.make({"gen": "formula", "name": "int_pairs", "n": 4000})
+    I[:, 0] %= 500
+    _join_check(ctx, I, I, proj=(("P", 4, 4), ("B", 4, 4)), bkey=(0, 4), pkey=(0, 4))
+
+
+def test_join_wide_tuples(ctx):
+    base = dg.build_relation(4000, dg.seed_for(15))
+    R = np.zeros((4000, 5), dtype=np.int32)
+    R[:, 1:] = base.view(np.int32)
+    sb = dg.probe_uniform(12000, base, dg.seed_for(16))
+    S = np.zeros((12000, 5), dtype=np.int32)
+    S[:, 0] = np.arange(12000)
+    S[:, 1:] = sb.view(np.int32)
+    _join_check(ctx, R, S, proj=(("P", 0, 4), ("P", 12, 8), ("B", 12, 8)), bkey=(4, 8), pkey=(4, 8))
+
+
+def test_join_reference_unit_test(ctx):
+    # unit_tests/queryhashjoin.cpp: build (i, i), probe (i, i+0.1), i = 1..20.
+    R = gin.make({"gen": "formula", "name": "i_i", "n": 20})
+    S = gin.make({"gen": "formula", "name": "i_i_plus_0.1", "n": 20})
+    got, n, _ = ctx.hashjoin(R, S, proj=(("B", 8, 8), ("P", 8, 8)))
+    assert n == 20
+    rows = got.view(np.int64).reshape(-1, 2)
+    assert sorted(rows[:, 0].tolist()) == list(range(1, 21))
+    assert np.allclose(rows[:, 1].view(np.float64), rows[:, 0] + 0.1)
+
+
+# ---------------------------------------------------------------- group-by
+def _gb_int_check(ctx, rows, agg, vtype, key=(0, 8), hint=0, has_key=True):
+    got = ctx.groupby(rows, key=key, val=(8 if vtype != "int" else 4, vtype), agg=agg,
+                      groups_hint=hint, has_key=has_key)
+    want = orc.groupby(rows, key=key, val=(8 if vtype != "int" else 4, vtype), agg=agg,
+                       hash=orc.hashcfg("modulo", 1024), has_key=has_key)
+    assert np.array_equal(canon(got), canon(want))
+
+
+@pytest.mark.parametrize("groups", [1, 10, 1000, 200_000])
+def test_groupby_long_sum_and_count(ctx, groups):
+    rows = dg.uniform_keys(500_000, groups, dg.seed_for(50))
+    rows[:, 1] -= 1 << 30    # negative values too
+    for agg in ("sum", "count"):
+        _gb_int_check(ctx, rows, agg, "long")
+        _gb_int_check(ctx, rows, agg, "long", hint=groups)
+
+
+def test_groupby_int_sum_wraps(ctx):
+    rows = gin.make({"gen": "formula", "name": "int_big", "n": 100_000})
+    got = ctx.groupby(rows, key=(0, 4), val=(4, "int"), agg="sum")
+    want = orc.groupby(rows, key=(0, 4), val=(4, "int"), agg="sum")
+    assert np.array_equal(canon(got), canon(want))
+
+
+def test_groupby_no_group_by(ctx):
+    rows = dg.uniform_keys(123_457, 1000, dg.seed_for(51))
+    _gb_int_check(ctx, rows, "count", "long", has_key=False)
+    _gb_int_check(ctx, rows, "sum", "long", has_key=False)
+    assert ctx.groupby(rows[:0], agg="count", has_key=False).shape[0] == 0
+
+
+def test_groupby_empty_marker_key(ctx):
+    rows = dg.uniform_keys(20_000, 300, dg.seed_for(52))
+    rows[::7, 0] = -1
+    _gb_int_check(ctx, rows, "sum", "long")
+    _gb_int_check(ctx, rows, "count", "long", hint=10_000)
+
+
+def _gb_dec_check(ctx, rows, hint=0):
+    got = ctx.groupby(rows, val=(8, "dec"), agg="sum", groups_hint=hint)
+    exact = orc.groupby_exact(rows)
+    g = got.view(np.int64).reshape(-1, 2)
+    e = exact.view(np.int64).reshape(-1, 2)
+    g = g[np.argsort(g[:, 0], kind="stable")]
+    assert np.array_equal(g[:, 0], e[:, 0])
+    gv, ev = g[:, 1].view(np.float64), e[:, 1].view(np.float64)
+    rel = np.abs(gv - ev) / np.maximum(np.abs(ev), 1e-300)
+    assert rel.max() <= DEC_RTOL, rel.max()
+
+
+@pytest.mark.parametrize("groups", [1, 300, 100_000])
+def test_groupby_dec_compensated(ctx, groups):
+    rows = dg.groupby_rows(1_000_000, groups, 1e4, dg.seed_for(53))
+    _gb_dec_check(ctx, rows)
+    _gb_dec_check(ctx, rows, hint=groups)
+
+
+def test_groupby_dec_ill_conditioned(ctx):
+    # Large values that cancel plus many small ones: naive summation loses the
+    # small ones entirely; compensated summation keeps them.
+    n = 200_000
+    rows = np.zeros((n, 2), dtype=np.int64)
+    rows[:, 0] = np.arange(n) % 10
+    v = np.full(n, 1e-3)
+    v[0:20:2] = 1e16
+    v[1:20:2] = -1e16
+    rows[:, 1] = v.view(np.int64)
+    _gb_dec_check(ctx, rows)
+
+
+def test_groupby_dec_zipf(ctx):
+    rows = gin.make({"gen": "groupby_zipf", "n": 300_000, "groups": 20_000, "rel": 54})
+    _gb_dec_check(ctx, rows)
+
+
+def test_groupby_reference_unit_test(ctx):
+    # unit_tests/queryaggsum.cpp: group i holds 1..i; sum must be i(i+1)/2.
+    rows = gin.make({"gen": "formula", "name": "agg_1_to_i", "n": 20})
+    got = ctx.groupby(rows, val=(8, "dec"), agg="sum").view(np.int64).reshape(-1, 2)
+    d = {int(k): float(v) for k, v in zip(got[:, 0], got[:, 1].view(np.float64))}
+    assert d == {i: i * (i + 1) / 2 for i in range(1, 21)}
+
+
+# ---------------------------------------------------------------- sort
+def _sort_check(ctx, rows, key=(0, 8)):
+    got = ctx.sort(rows, key)
+    want = orc.sort(rows, key)
+    kb = key[1]
+    gk = got.view(np.uint8).reshape(got.shape[0], -1)[:, key[0]:key[0] + kb].copy().view(np.int64 if kb == 8 else np.int32)
+    wk = want.view(np.uint8).reshape(want.shape[0], -1)[:, key[0]:key[0] + kb].copy().view(np.int64 if kb == 8 else np.int32)
+    assert np.array_equal(gk, wk)
+    assert np.array_equal(canon(got), canon(want))
+
+
+@pytest.mark.parametrize("n", [0, 1, 100, 4095, 4096, 4097, 8192, 100_000, 1_000_003])
+def test_sort_sizes(ctx, n):
+    _sort_check(ctx, dg.uniform_keys(n, 1 << 40, dg.seed_for(60)))
+
+
+def test_sort_duplicates_and_negatives(ctx):
+    _sort_check(ctx, dg.uniform_keys(300_000, 50, dg.seed_for(61)))
+    _sort_check(ctx, gin.make({"gen": "formula", "name": "signed_keys", "n": 50_000}))
+    a = dg.uniform_keys(10_000, 10, dg.seed_for(62))
+    a[:, 0] = np.iinfo(np.int64).max - a[:, 0]
+    a[::3, 0] = np.iinfo(np.int64).min
+    _sort_check(ctx, a)
+
+
+def test_sort_layouts(ctx):
+    a = dg.uniform_keys(70_000, 1 << 30, dg.seed_for(63))
+    _sort_check(ctx, a, key=(8, 8))                  # key in the second column
+    t8 = gin.make({"gen": "formula", "name": "int_pairs", "n": 50_000})
+    _sort_check(ctx, t8, key=(4, 4))                 # int key
+    t20 = np.zeros((30_000, 5), dtype=np.int32)
+    t20[:, 0] = np.arange(30_000)
+    t20[:, 1:] = dg.uniform_keys(30_000, 999, dg.seed_for(64)).view(np.int32)
+    _sort_check(ctx, t20, key=(4, 8))
+
+
+# ---------------------------------------------------------------- MPSM
+def _mpsm_check(ctx, R, S, proj=(("P", 8, 8), ("B", 8, 8)), bkey=(0, 8), pkey=(0, 8)):
+    got, n, _ = ctx.mpsm(R, S, proj=proj, bkey=bkey, pkey=pkey)
+    want, wn, _ = orc.mergejoin(R, S, proj=proj, bkey=bkey, pkey=pkey)
+    assert n == wn
+    assert np.array_equal(canon(got), canon(want))
+    for sc in range(len(proj)):
+        _, n2, s2 = ctx.mpsm(R, S, proj=proj, bkey=bkey, pkey=pkey, flags=gpu.JOIN_COUNT | gpu.JOIN_SUM, sum_col=sc)
+        _, wn2, ws2 = orc.mergejoin(R, S, proj=proj, bkey=bkey, pkey=pkey, materialise=False, sum_col=sc)
+        assert (n2, s2) == (wn2, ws2)
+    return n
+
+
+def test_mpsm_reference_unit_tests(ctx):
+    f = lambda name, n: gin.make({"gen": "formula", "name": name, "n": n})  # noqa: E731
+    assert _mpsm_check(ctx, f("i_i", 2000), f("i_i", 2000)) == 2000
+    assert _mpsm_check(ctx, f("i_i", 2000), f("fk_i_and_3", 2000)) == 5000
+    assert _mpsm_check(ctx, f("ones", 200), f("ones", 200)) == 40_000
+
+
+def test_mpsm_duplicates(ctx):
+    R = dg.uniform_keys(50_000, 12_500, dg.seed_for(70))
+    S = dg.uniform_keys(50_000, 12_500, dg.seed_for(71))
+    _mpsm_check(ctx, R, S)
+
+
+def test_mpsm_skew_and_edges(ctx):
+    R = dg.zipf_keys(20_000, 2000, 1.0, dg.seed_for(72))
+    S = dg.zipf_keys(20_000, 2000, 1.0, dg.seed_for(73))
+    _mpsm_check(ctx, R, S)
+    empty = np.zeros((0, 2), dtype=np.int64)
+    assert _mpsm_check(ctx, R, empty) == 0
+    neg = gin.make({"gen": "formula", "name": "signed_keys", "n": 6000})
+    _mpsm_check(ctx, neg, neg, proj=(("B", 0, 8), ("P", 8, 8), ("B", 8, 8)))
+
+
+def test_mpsm_matches_hashjoin(ctx):
+    R = dg.uniform_keys(40_000, 10_000, dg.seed_for(74))
+    S = dg.uniform_keys(40_000, 10_000, dg.seed_for(75))
+    a, n1, _ = ctx.mpsm(R, S)
+    b, n2, _ = ctx.hashjoin(R, S)
+    assert n1 == n2 and np.array_equal(canon(a), canon(b))
