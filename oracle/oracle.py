@@ -88,7 +88,8 @@ def hashfn(cfg):
 
 def _rows(a):
     a = np.ascontiguousarray(a)
-    return a, a.ctypes.data, a.shape[0], a.strides[0] if a.ndim > 1 else a.itemsize
+    w = int(a.itemsize * int(np.prod(a.shape[1:]))) if a.ndim > 1 else int(a.itemsize)
+    return a, a.ctypes.data, a.shape[0], w
 
 
 def hash_column(cfg, rows, off=0, size=8, width=None):

@@ -183,7 +183,7 @@ class Context:
     # ---- operators on numpy inputs (upload, run, download) ----
     def hash_tuples(self, rows, cfg, key_off=0, key_bytes=8):
         a = np.ascontiguousarray(rows)
-        n, w = a.shape[0], a.strides[0] if a.ndim > 1 else a.itemsize
+        n, w = a.shape[0], row_width(a)
         d = self.upload(a)
         o = self.alloc(4 * max(n, 1))
         r = self.rel(d, n, w, key_off, key_bytes)
@@ -197,7 +197,7 @@ class Context:
 
     def partition(self, rows, cfg, key_off=0, key_bytes=8):
         a = np.ascontiguousarray(rows)
-        n, w = a.shape[0], a.strides[0]
+        n, w = a.shape[0], row_width(a)
         nb = self.nbuckets(cfg)
         d = self.upload(a)
         o = self.alloc(a.nbytes)
@@ -212,8 +212,8 @@ class Context:
                  flags=JOIN_MATERIALIZE, sum_col=-1, out_cap=None):
         Ra, Sa = np.ascontiguousarray(R), np.ascontiguousarray(S)
         dR, dS = self.upload(Ra), self.upload(Sa)
-        rR = self.rel(dR, Ra.shape[0], Ra.strides[0] if Ra.shape[0] else Ra.itemsize * Ra.shape[1], *bkey)
-        rS = self.rel(dS, Sa.shape[0], Sa.strides[0] if Sa.shape[0] else Sa.itemsize * Sa.shape[1], *pkey)
+        rR = self.rel(dR, Ra.shape[0], row_width(Ra), *bkey)
+        rS = self.rel(dS, Sa.shape[0], row_width(Sa), *pkey)
         c, nc = cols(proj)
         ow = sum(b for _, _, b in proj)
         ht = ctypes.c_void_p()
@@ -242,7 +242,7 @@ class Context:
 
     def groupby(self, rows, key=(0, 8), val=(8, "long"), agg="sum", groups_hint=0, has_key=True):
         a = np.ascontiguousarray(rows)
-        n, w = a.shape[0], a.strides[0]
+        n, w = a.shape[0], row_width(a)
         d = self.upload(a)
         vtype = VAL[val[1]]
         aw = 4 if (agg == "sum" and vtype == 0) else 8
@@ -258,7 +258,7 @@ class Context:
 
     def sort(self, rows, key=(0, 8)):
         a = np.ascontiguousarray(rows)
-        n, w = a.shape[0], a.strides[0]
+        n, w = a.shape[0], row_width(a)
         d = self.upload(a)
         o = self.alloc(a.nbytes)
         r = self.rel(d, n, w, *key)
@@ -269,8 +269,8 @@ class Context:
              flags=JOIN_MATERIALIZE, sum_col=-1):
         Ra, Sa = np.ascontiguousarray(R), np.ascontiguousarray(S)
         dR, dS = self.upload(Ra), self.upload(Sa)
-        rR = self.rel(dR, Ra.shape[0], Ra.strides[0] if Ra.shape[0] else Ra.itemsize * Ra.shape[1], *bkey)
-        rS = self.rel(dS, Sa.shape[0], Sa.strides[0] if Sa.shape[0] else Sa.itemsize * Sa.shape[1], *pkey)
+        rR = self.rel(dR, Ra.shape[0], row_width(Ra), *bkey)
+        rS = self.rel(dS, Sa.shape[0], row_width(Sa), *pkey)
         c, nc = cols(proj)
         ow = sum(b for _, _, b in proj)
         res = JoinResult()
@@ -283,6 +283,11 @@ class Context:
         self._check(lib().pg_mpsm_join(self.h, self.stream, ctypes.byref(rR), ctypes.byref(rS), c, nc,
                                        o.ptr, res.n_out, flags, sum_col, ctypes.byref(res)))
         return self.download(o, res.n_out * ow).reshape(-1, ow), res.n_out, res.sum
+
+
+def row_width(a):
+    """Bytes per tuple of a row-major (n, ...) array, also when n == 0."""
+    return int(a.itemsize * int(np.prod(a.shape[1:]))) if a.ndim > 1 else int(a.itemsize)
 
 
 def kernel_launches():
