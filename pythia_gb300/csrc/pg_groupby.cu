@@ -255,11 +255,13 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 		int blocks = (int) std::min<uint64_t>(pg_div_up(std::max<uint64_t>(in->n, 1), GB_THREADS),
 				(uint64_t) ctx->sm_count * (smem ? 4 : 8));
 		if (in->n) {
-			#define GB_LAUNCH(HK, SM) k_gb_insert<VT, AGG, HK, SM><<<blocks, GB_THREADS, smem_bytes, s>>>( \
+			#define GB_LAUNCH(HK, SM) cudaFuncSetAttribute(k_gb_insert<VT, AGG, HK, SM>, \
+					cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_bytes); \
+					k_gb_insert<VT, AGG, HK, SM><<<blocks, GB_THREADS, smem_bytes, s>>>( \
 					(const char*) in->data, in->n, in->width, in->key_off, in->key_bytes, voff, t, slg, ctx->d_status)
-			if (haskey && smem) GB_LAUNCH(true, true);
-			else if (haskey) GB_LAUNCH(true, false);
-			else GB_LAUNCH(false, true);
+			if (haskey && smem) { GB_LAUNCH(true, true); }
+			else if (haskey) { GB_LAUNCH(true, false); }
+			else { GB_LAUNCH(false, true); }
 			#undef GB_LAUNCH
 			PG_LAUNCHED(ctx);
 		}

@@ -67,9 +67,11 @@ struct pg_hashtable {
 	cudaStream_t stream;        // stream the table was built on
 };
 
+// First slot of key k's probe sequence: always even, so the sequence starts
+// at a 32-byte bucket of two slots that one 256-bit load fetches.
 __device__ __forceinline__ uint64_t hj_slot0(int64_t k, uint32_t log2cap)
 {
-	return pg_mix64((uint64_t) k) >> (64 - log2cap);
+	return (pg_mix64((uint64_t) k) >> (65 - log2cap)) << 1;
 }
 
 __device__ __forceinline__ uint32_t hj_word(const char* tuple, uint32_t w)
@@ -259,6 +261,175 @@ k_probe_unique(const char* __restrict__ S, uint64_t n, uint32_t W, uint32_t koff
 		}
 	}
 	if (!MATERIALIZE) {
+		#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			cnt_acc += __shfl_down_sync(0xffffffffu, cnt_acc, o);
+			sum_acc += __shfl_down_sync(0xffffffffu, sum_acc, o);
+		}
+		if (lane == 0) { atomicAdd(&agg[0], cnt_acc); atomicAdd(&agg[1], sum_acc); }
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Unique-key probe of 16-byte tuples, Blackwell path. Per CTA, persistent over
+// tiles of 2048 probe tuples:
+//   * tiles arrive in shared memory by bulk copy (cp.async.bulk + mbarrier),
+//     the next tile prefetched while the current one is probed;
+//   * each thread resolves 8 keys; every key's first 32-byte bucket (two
+//     slots) is fetched with one 256-bit evict-last load, all 8 issued before
+//     any is inspected, and keys that need a further bucket advance together
+//     in rounds, so dependent loads overlap;
+//   * matches are ranked in tile order with warp ballots, assembled as output
+//     rows in shared memory and written with one bulk store per tile to a
+//     range reserved by a single atomicAdd (only the issuing thread waits on
+//     it).
+// ---------------------------------------------------------------------------
+#define HJT_TILE 1024
+#define HJT_THREADS 256
+#define HJT_ITEMS (HJT_TILE / HJT_THREADS)
+
+__device__ __forceinline__ uint32_t hj_pick(const uint4& t, uint64_t v, uint32_t i)
+{
+	uint32_t r = t.x;
+	r = i == 1 ? t.y : r;
+	r = i == 2 ? t.z : r;
+	r = i == 3 ? t.w : r;
+	r = i == 4 ? (uint32_t) v : r;
+	r = i == 5 ? (uint32_t) (v >> 32) : r;
+	return r;
+}
+
+template <bool MATERIALIZE>
+__global__ void __launch_bounds__(HJT_THREADS, 3)
+k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff,
+		const unsigned long long* __restrict__ slots, uint32_t log2cap,
+		const unsigned long long* __restrict__ side, uint32_t nside,
+		uint32_t wsel, uint32_t sum_w0, uint32_t sum_words, char* __restrict__ out, uint64_t out_cap,
+		unsigned long long* __restrict__ cursor, unsigned long long* __restrict__ agg,
+		int sum_col, int* __restrict__ status)
+{
+	extern __shared__ __align__(128) unsigned char sm[];
+	uint4* const tin0 = reinterpret_cast<uint4*>(sm);
+	uint4* const tout = reinterpret_cast<uint4*>(sm + 2 * HJT_TILE * 16);
+	__shared__ __align__(8) uint64_t bar[2];
+	__shared__ uint32_t wcnt[HJT_ITEMS][HJT_THREADS / 32];
+	__shared__ uint32_t tile_total;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const uint64_t mask = (1ull << log2cap) - 1;
+	const uint64_t ntiles = pg_div_up(n, HJT_TILE);
+	const uint64_t pol = pg_policy_evict_last();
+	unsigned long long cnt_acc = 0, sum_acc = 0;
+	// Output word i is source word (wsel >> 4i) & 15 of (probe tuple words
+	// 0-3, packed build value words 4-5).
+	const uint32_t w0 = wsel & 15, w1 = (wsel >> 4) & 15, w2 = (wsel >> 8) & 15, w3 = (wsel >> 12) & 15;
+	if (tid == 0) { pg_mbar_init(&bar[0], 1); pg_mbar_init(&bar[1], 1); pg_fence_mbar_init(); }
+	__syncthreads();
+	uint64_t tile = blockIdx.x;
+	if (tile >= ntiles) return;
+	auto issue = [&](uint64_t t, int b) {
+		const uint32_t rows = (uint32_t) pg_min64(HJT_TILE, n - t * HJT_TILE);
+		pg_mbar_expect_tx(&bar[b], rows * 16);
+		pg_bulk_g2s(tin0 + b * HJT_TILE, S + t * (uint64_t) HJT_TILE * 16, rows * 16, &bar[b]);
+	};
+	if (tid == 0) issue(tile, 0);
+	uint32_t phases = 0;     // bit b: parity expected next on bar[b]
+	for (int it = 0; tile < ntiles; tile += gridDim.x, ++it) {
+		const int b = it & 1;
+		const uint4* const tb = tin0 + b * HJT_TILE;
+		const uint64_t base = tile * HJT_TILE;
+		const uint32_t rows = (uint32_t) pg_min64(HJT_TILE, n - base);
+		const bool ok = pg_mbar_wait(&bar[b], (phases >> b) & 1);
+		if (__syncthreads_or(!ok)) { if (tid == 0) pg_set_status(status, PG_ERR_TIMEOUT); break; }
+		phases ^= 1u << b;
+		// Prefetch the next tile into the other buffer (its previous contents
+		// were consumed before the last __syncthreads of the previous tile).
+		if (tid == 0 && tile + gridDim.x < ntiles) issue(tile + gridDim.x, b ^ 1);
+
+		int64_t key[HJT_ITEMS];
+		uint64_t slot[HJT_ITEMS];
+		uint64_t val[HJT_ITEMS];
+		bool hit[HJT_ITEMS], open[HJT_ITEMS];
+		#pragma unroll
+		for (int j = 0; j < HJT_ITEMS; ++j) {
+			const uint32_t p = j * HJT_THREADS + tid;
+			hit[j] = false; open[j] = false; val[j] = 0;
+			key[j] = 0;
+			if (p < rows) {
+				const uint4 t = tb[p];
+				key[j] = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
+				if (key[j] == PG_EMPTY_KEY) { if (nside) { hit[j] = true; val[j] = side[0]; } }
+				else { open[j] = true; slot[j] = hj_slot0(key[j], log2cap); }
+			}
+		}
+		// Rounds of bucket loads: all open keys issue, then all inspect.
+		for (uint32_t round = 0; round <= (mask >> 1); ++round) {
+			pg_u64x4 bk[HJT_ITEMS];
+			bool any = false;
+			#pragma unroll
+			for (int j = 0; j < HJT_ITEMS; ++j)
+				if (open[j]) { bk[j] = pg_ld_bucket32(slots + 2 * slot[j], pol); any = true; }
+			if (!any) break;
+			#pragma unroll
+			for (int j = 0; j < HJT_ITEMS; ++j) {
+				if (!open[j]) continue;
+				if ((long long) bk[j].a == key[j]) { hit[j] = true; val[j] = bk[j].b; open[j] = false; }
+				else if (bk[j].a == (unsigned long long) PG_EMPTY_KEY) open[j] = false;
+				else if ((long long) bk[j].c == key[j]) { hit[j] = true; val[j] = bk[j].d; open[j] = false; }
+				else if (bk[j].c == (unsigned long long) PG_EMPTY_KEY) open[j] = false;
+				else slot[j] = (slot[j] + 2) & mask;
+			}
+		}
+		if (MATERIALIZE) {
+			uint32_t ball[HJT_ITEMS];
+			#pragma unroll
+			for (int j = 0; j < HJT_ITEMS; ++j) {
+				ball[j] = __ballot_sync(0xffffffffu, hit[j]);
+				if (lane == 0) wcnt[j][warp] = __popc(ball[j]);
+			}
+			// The output buffer is free once the previous tile's bulk store
+			// has read it.
+			if (tid == 0) pg_bulk_wait_read();
+			__syncthreads();
+			if (tid == 0) {
+				uint32_t run = 0;
+				for (int j = 0; j < HJT_ITEMS; ++j)
+					for (int w = 0; w < HJT_THREADS / 32; ++w) { uint32_t c = wcnt[j][w]; wcnt[j][w] = run; run += c; }
+				tile_total = run;
+			}
+			__syncthreads();
+			#pragma unroll
+			for (int j = 0; j < HJT_ITEMS; ++j) {
+				if (!hit[j]) continue;
+				const uint32_t pos = wcnt[j][warp] + __popc(ball[j] & ((1u << lane) - 1));
+				const uint4 t = tb[j * HJT_THREADS + tid];
+				tout[pos] = make_uint4(hj_pick(t, val[j], w0), hj_pick(t, val[j], w1),
+						hj_pick(t, val[j], w2), hj_pick(t, val[j], w3));
+			}
+			pg_fence_proxy_async_smem();
+			__syncthreads();
+			if (tid == 0 && tile_total) {
+				const unsigned long long at = atomicAdd(cursor, (unsigned long long) tile_total);
+				if (at + tile_total <= out_cap) pg_bulk_s2g(out + at * 16, tout, tile_total * 16);
+			}
+		} else {
+			#pragma unroll
+			for (int j = 0; j < HJT_ITEMS; ++j) {
+				if (!hit[j]) continue;
+				cnt_acc++;
+				if (sum_col >= 0) {
+					const uint4 t = tb[j * HJT_THREADS + tid];
+					const uint32_t lo = hj_pick(t, val[j], (wsel >> (4 * sum_w0)) & 15);
+					if (sum_words == 2)
+						sum_acc += ((unsigned long long) hj_pick(t, val[j], (wsel >> (4 * sum_w0 + 4)) & 15) << 32) | lo;
+					else sum_acc += (unsigned long long) (long long) (int32_t) lo;
+				}
+			}
+			__syncthreads();   // tile buffer b is refilled by the prefetch two tiles on
+		}
+	}
+	if (MATERIALIZE) {
+		if (tid == 0) pg_bulk_wait_all();
+	} else {
 		#pragma unroll
 		for (int o = 16; o > 0; o >>= 1) {
 			cnt_acc += __shfl_down_sync(0xffffffffu, cnt_acc, o);
@@ -511,6 +682,47 @@ static int hj_make_cols(pg_ctx* ctx, const pg_hashtable* ht, const pg_col* proj,
 	return PG_OK;
 }
 
+// Launches the unique-key probe over n tuples at S (device) into `out`;
+// counts/sums accumulate in acc[1..2], the output cursor is acc[0].
+static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht, const char* S,
+		uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes, const HjCols& pc, char* out,
+		uint64_t cap, unsigned long long* acc, bool materialize, int sum_col)
+{
+	const uint64_t ntiles = pg_div_up(n, HJ_TILE);
+	const bool fast16 = W == 16 && (koff == 0 || koff == 8) && kbytes == 8 && pc.ow_words == 4 &&
+		(reinterpret_cast<uintptr_t>(S) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+	if (fast16) {
+		const int smem = 3 * HJT_TILE * 16;
+		uint32_t wsel = 0, o = 0, sum_w0 = 0, sum_words = 0;
+		for (int c = 0; c < pc.n; ++c) {
+			if (c == sum_col) { sum_w0 = o; sum_words = pc.words[c]; }
+			for (int q = 0; q < pc.words[c]; ++q, ++o)
+				wsel |= (pc.side[c] ? (pc.src[c] + q) : (4u + pc.src[c] + q)) << (4 * o);
+		}
+		const int grid = (int) std::min<uint64_t>(pg_div_up(n, HJT_TILE), (uint64_t) ctx->sm_count * 3);
+		if (materialize) {
+			PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+			k_probe16_tma<true><<<grid, HJT_THREADS, smem, s>>>(S, n, koff, ht->slots, ht->log2cap, ht->side,
+					ht->nside, wsel, 0, 0, out, cap, acc, acc + 1, -1, ctx->d_status);
+		} else {
+			PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+			k_probe16_tma<false><<<grid, HJT_THREADS, smem, s>>>(S, n, koff, ht->slots, ht->log2cap, ht->side,
+					ht->nside, wsel, sum_w0, sum_words, nullptr, 0, acc, acc + 1, sum_col, ctx->d_status);
+		}
+		PG_LAUNCHED(ctx);
+		return PG_OK;
+	}
+	const int grid = (int) std::min<uint64_t>(ntiles, (uint64_t) ctx->sm_count * 8);
+	if (materialize)
+		k_probe_unique<true, false><<<grid, HJ_THREADS, 0, s>>>(S, n, W, koff, kbytes, ht->slots, ht->log2cap,
+				ht->side, ht->nside, pc, out, cap, acc, acc + 1, -1, ctx->d_status);
+	else
+		k_probe_unique<false, false><<<grid, HJ_THREADS, 0, s>>>(S, n, W, koff, kbytes, ht->slots, ht->log2cap,
+				ht->side, ht->nside, pc, nullptr, 0, acc, acc + 1, sum_col, ctx->d_status);
+	PG_LAUNCHED(ctx);
+	return PG_OK;
+}
+
 extern "C" int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 		const pg_rel* S, const pg_col* proj, int nproj,
 		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res)
@@ -532,39 +744,27 @@ extern "C" int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht
 	if ((rc = pg_alloc_async(ctx, s, (void**) &acc, 64))) return rc;
 	PG_CUDA(ctx, cudaMemsetAsync(acc, 0, 64, s));
 	const uint64_t ntiles = pg_div_up(S->n, HJ_TILE);
-	const int grid_persist = (int) std::min<uint64_t>(ntiles, (uint64_t) ctx->sm_count * 8);
-	const bool fast16 = S->width == 16 && (S->key_off == 0 || S->key_off == 8) && S->key_bytes == 8 && pc.ow_words == 4;
 	unsigned long long host_acc[4] = {0, 0, 0, 0};
 
 	if (ht->unique && ht->inline_val) {
+		const char* Sd = (const char*) S->data;
 		if (materialize) {
-			if (fast16)
-				k_probe_unique<true, true><<<grid_persist, HJ_THREADS, 0, s>>>((const char*) S->data, S->n, S->width,
-						S->key_off, S->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, (char*) out,
-						out_capacity, acc, acc + 1, sum_col, ctx->d_status);
-			else
-				k_probe_unique<true, false><<<grid_persist, HJ_THREADS, 0, s>>>((const char*) S->data, S->n, S->width,
-						S->key_off, S->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, (char*) out,
-						out_capacity, acc, acc + 1, sum_col, ctx->d_status);
-			PG_LAUNCHED(ctx);
+			if ((rc = hj_launch_unique(ctx, s, ht, Sd, S->n, S->width, S->key_off, S->key_bytes, pc,
+					(char*) out, out_capacity, acc, true, -1))) return rc;
 			PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
 			if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
 			res->n_out = host_acc[0];
 			if (sum_col >= 0 || (flags & PG_JOIN_COUNT)) {
-				// Fold count/sum over what was written (second, cheap pass).
-				k_probe_unique<false, false><<<grid_persist, HJ_THREADS, 0, s>>>((const char*) S->data, S->n, S->width,
-						S->key_off, S->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, nullptr, 0,
-						acc, acc + 1, sum_col, ctx->d_status);
-				PG_LAUNCHED(ctx);
+				// Fold count/sum with a second, non-materialising pass.
+				if ((rc = hj_launch_unique(ctx, s, ht, Sd, S->n, S->width, S->key_off, S->key_bytes, pc,
+						nullptr, 0, acc, false, sum_col))) return rc;
 				PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
 				if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
 				res->sum = (int64_t) host_acc[2];
 			}
 		} else {
-			k_probe_unique<false, false><<<grid_persist, HJ_THREADS, 0, s>>>((const char*) S->data, S->n, S->width,
-					S->key_off, S->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, nullptr, 0,
-					acc, acc + 1, sum_col, ctx->d_status);
-			PG_LAUNCHED(ctx);
+			if ((rc = hj_launch_unique(ctx, s, ht, Sd, S->n, S->width, S->key_off, S->key_bytes, pc,
+					nullptr, 0, acc, false, sum_col))) return rc;
 			PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
 			if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
 			res->n_out = host_acc[1];
@@ -686,8 +886,6 @@ extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
 	HJH_TRY(cudaMallocHost(&hacc, 2 * 4 * sizeof(unsigned long long)));
 	HJH_TRY(cudaStreamSynchronize(scomp));
 	const uint64_t nchunks = pg_div_up(nS, CH);
-	const bool fast16 = Sh->width == 16 && (Sh->key_off == 0 || Sh->key_off == 8) && Sh->key_bytes == 8 && pc.ow_words == 4;
-	const int grid = (int) std::min<uint64_t>(pg_div_up(CH, HJ_TILE), (uint64_t) ctx->sm_count * 8);
 	uint64_t written = 0;
 	unsigned long long count = 0, sum = 0;
 	auto issue = [&](uint64_t c) -> int {
@@ -700,23 +898,11 @@ extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
 		HJH_TRY(cudaStreamWaitEvent(scomp, ev_in[b], 0));
 		if (c >= 2) HJH_TRY(cudaStreamWaitEvent(scomp, ev_out[b], 0));   // output buffer free
 		HJH_TRY(cudaMemsetAsync(acc + 4 * b, 0, 32, scomp));
-		if (materialize) {
-			if (fast16)
-				k_probe_unique<true, true><<<grid, HJ_THREADS, 0, scomp>>>(dS[b], rows, Sh->width, Sh->key_off,
-						Sh->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, dO[b], CH,
-						acc + 4 * b, acc + 4 * b + 1, -1, ctx->d_status);
-			else
-				k_probe_unique<true, false><<<grid, HJ_THREADS, 0, scomp>>>(dS[b], rows, Sh->width, Sh->key_off,
-						Sh->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, dO[b], CH,
-						acc + 4 * b, acc + 4 * b + 1, -1, ctx->d_status);
-			g_kernel_launches.fetch_add(1);
-		}
-		if (!materialize || sum_col >= 0 || (flags & PG_JOIN_COUNT)) {
-			k_probe_unique<false, false><<<grid, HJ_THREADS, 0, scomp>>>(dS[b], rows, Sh->width, Sh->key_off,
-					Sh->key_bytes, ht->slots, ht->log2cap, ht->side, ht->nside, pc, nullptr, 0,
-					acc + 4 * b, acc + 4 * b + 1, sum_col, ctx->d_status);
-			g_kernel_launches.fetch_add(1);
-		}
+		if (materialize && hj_launch_unique(ctx, scomp, ht, dS[b], rows, Sh->width, Sh->key_off, Sh->key_bytes,
+				pc, dO[b], CH, acc + 4 * b, true, -1)) { cleanup(); return PG_ERR_CUDA; }
+		if ((!materialize || sum_col >= 0 || (flags & PG_JOIN_COUNT)) &&
+				hj_launch_unique(ctx, scomp, ht, dS[b], rows, Sh->width, Sh->key_off, Sh->key_bytes,
+				pc, nullptr, 0, acc + 4 * b, false, sum_col)) { cleanup(); return PG_ERR_CUDA; }
 		HJH_TRY(cudaGetLastError());
 		HJH_TRY(cudaMemcpyAsync(hacc + 4 * b, acc + 4 * b, 32, cudaMemcpyDeviceToHost, scomp));
 		HJH_TRY(cudaEventRecord(ev_comp[b], scomp));

@@ -221,6 +221,35 @@ __device__ __forceinline__ uint4 pg_ld_stream16(const void* p) { return pg_ld_hi
 __device__ __forceinline__ uint4 pg_ld_table16(const void* p) { return pg_ld_hint16(p, pg_policy_evict_last()); }
 __device__ __forceinline__ void pg_st_stream16(void* p, uint4 v) { pg_st_hint16(p, v, pg_policy_evict_first()); }
 
+// 32-byte (256-bit) load of one table bucket, kept in L2 (evict-last).
+struct pg_u64x4 { unsigned long long a, b, c, d; };
+__device__ __forceinline__ pg_u64x4 pg_ld_bucket32(const void* p, uint64_t pol)
+{
+	pg_u64x4 v;
+	asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u64 {%0,%1,%2,%3}, [%4], %5;"
+			: "=l"(v.a), "=l"(v.b), "=l"(v.c), "=l"(v.d) : "l"(p), "l"(pol));
+	return v;
+}
+
+// Bulk (TMA) store shared -> global; `bytes` a multiple of 16, both ends
+// 16-byte aligned. Writers fence their shared stores to the async proxy first.
+__device__ __forceinline__ void pg_fence_proxy_async_smem()
+{
+	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void pg_bulk_s2g(void* dst, const void* src, uint32_t bytes)
+{
+	asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+			:: "l"(dst), "r"(pg_smem_addr(src)), "r"(bytes) : "memory");
+	asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+// Waits until every committed bulk store has finished reading shared memory.
+__device__ __forceinline__ void pg_bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// Waits until every committed bulk store has completed.
+__device__ __forceinline__ void pg_bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 __host__ __device__ __forceinline__ uint64_t pg_div_up(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
 __host__ __device__ __forceinline__ uint64_t pg_min64(uint64_t a, uint64_t b) { return a < b ? a : b; }
 __host__ __device__ __forceinline__ uint32_t pg_min32(uint32_t a, uint32_t b) { return a < b ? a : b; }
