@@ -65,7 +65,26 @@ struct pg_hashtable {
 	pg_col proj[HJ_MAX_COLS];
 	int nproj;
 	cudaStream_t stream;        // stream the table was built on
+	// Dense layout (unique keys spanning at most twice |R| values): value and
+	// presence bit indexed by key - dmin instead of hashed slots.
+	bool dense;
+	unsigned long long* dense_val;
+	uint32_t* dense_bits;
+	long long dmin;
+	unsigned long long drange;
 };
+
+struct HjProbeTable {
+	const unsigned long long* slots;   // hashed: 2 words per slot
+	uint32_t log2cap;
+	const unsigned long long* side;    // values of build keys equal to the empty marker
+	uint32_t nside;
+	const unsigned long long* dense_val;   // dense: value per key - dmin
+	const uint32_t* dense_bits;            // dense: presence bit per key - dmin
+	long long dmin;
+	unsigned long long drange;
+};
+
 
 // First slot of key k's probe sequence: always even, so the sequence starts
 // at a 32-byte bucket of two slots that one 256-bit load fetches.
@@ -119,6 +138,52 @@ __global__ void k_ht_build(const char* __restrict__ R, uint64_t n, uint32_t W, u
 	if (__any_sync(__activemask(), dup) && dup) atomicOr(flags, 1);
 }
 
+// Key range of the build side (signed keys mapped to ordered unsigned words).
+__global__ void k_key_minmax(const char* __restrict__ R, uint64_t n, uint32_t W, uint32_t koff,
+		uint32_t kbytes, unsigned long long* __restrict__ mm)
+{
+	unsigned long long lo = ~0ull, hi = 0;
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+			i += (uint64_t) gridDim.x * blockDim.x) {
+		const unsigned long long u = (unsigned long long) pg_load_key(R + i * W + koff, kbytes) ^ (1ull << 63);
+		lo = u < lo ? u : lo;
+		hi = u > hi ? u : hi;
+	}
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		unsigned long long a = __shfl_down_sync(0xffffffffu, lo, o), b = __shfl_down_sync(0xffffffffu, hi, o);
+		lo = a < lo ? a : lo;
+		hi = b > hi ? b : hi;
+	}
+	if ((threadIdx.x & 31) == 0) { atomicMin(&mm[0], lo); atomicMax(&mm[1], hi); }
+}
+
+// Dense table: presence bit and value at key - dmin. A bit found already set
+// means a duplicate key; the host then builds the hashed table instead.
+__global__ void k_dense_build(const char* __restrict__ R, uint64_t n, uint32_t W, uint32_t koff,
+		uint32_t kbytes, HjBuildCols bc, bool inline_val, long long dmin,
+		unsigned long long* __restrict__ dval, uint32_t* __restrict__ dbits, int* __restrict__ flags)
+{
+	bool dup = false;
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+			i += (uint64_t) gridDim.x * blockDim.x) {
+		const char* t = R + i * W;
+		const unsigned long long d = (unsigned long long) pg_load_key(t + koff, kbytes) - (unsigned long long) dmin;
+		uint64_t v = i;
+		if (inline_val) {
+			uint32_t w[2] = {0, 0};
+			int o = 0;
+			for (int c = 0; c < bc.n; ++c)
+				for (int j = 0; j < bc.words[c]; ++j) w[o++] = hj_word(t, bc.roff[c] + j);
+			v = ((uint64_t) w[1] << 32) | w[0];
+		}
+		const uint32_t bit = 1u << (d & 31);
+		if (atomicOr(&dbits[d >> 5], bit) & bit) dup = true;
+		dval[d] = v;
+	}
+	if (dup) atomicOr(flags, 1);
+}
+
 // Value of output word `w` for a match: from the probe tuple or from the build
 // side (packed value, or the build tuple when values are row indices).
 __device__ __forceinline__ uint32_t hj_out_word(const HjCols& pc, int c, int j, const char* ptup,
@@ -136,11 +201,37 @@ __device__ __forceinline__ uint32_t hj_out_word(const HjCols& pc, int c, int j, 
 // Unique-key probe: one pass, tile-ordered output, one atomicAdd per tile.
 // FAST16: probe tuples are 16 bytes and output rows 16 bytes (4 words).
 // ---------------------------------------------------------------------------
+// Single lookup in a unique-key table (hashed or dense). Returns whether key
+// k is present and its value.
+__device__ __forceinline__ bool hj_lookup_unique(const HjProbeTable& tb, bool dense, int64_t k, uint64_t& val)
+{
+	if (dense) {
+		const unsigned long long d = (unsigned long long) k - (unsigned long long) tb.dmin;
+		if (d >= tb.drange || !((tb.dense_bits[d >> 5] >> (d & 31)) & 1)) return false;
+		val = tb.dense_val[d];
+		return true;
+	}
+	if (k == PG_EMPTY_KEY) {
+		if (!tb.nside) return false;
+		val = tb.side[0];
+		return true;
+	}
+	const uint64_t mask = (1ull << tb.log2cap) - 1;
+	uint64_t s = hj_slot0(k, tb.log2cap);
+	for (uint64_t probe = 0; probe <= mask; ++probe) {
+		const uint4 v = pg_ld_table16(tb.slots + 2 * s);
+		const int64_t sk = (int64_t) (((uint64_t) v.y << 32) | v.x);
+		if (sk == k) { val = ((uint64_t) v.w << 32) | v.z; return true; }
+		if (sk == PG_EMPTY_KEY) return false;
+		s = (s + 1) & mask;
+	}
+	return false;
+}
+
 template <bool MATERIALIZE, bool FAST16>
 __global__ void __launch_bounds__(HJ_THREADS)
 k_probe_unique(const char* __restrict__ S, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes,
-		const unsigned long long* __restrict__ slots, uint32_t log2cap,
-		const unsigned long long* __restrict__ side, uint32_t nside,
+		const HjProbeTable tb, bool dense,
 		HjCols pc, char* __restrict__ out, uint64_t out_cap,
 		unsigned long long* __restrict__ cursor, unsigned long long* __restrict__ agg,
 		int sum_col, int* __restrict__ status)
@@ -148,7 +239,6 @@ k_probe_unique(const char* __restrict__ S, uint64_t n, uint32_t W, uint32_t koff
 	__shared__ uint32_t wcnt[HJ_ITEMS][HJ_THREADS / 32];
 	__shared__ unsigned long long tile_base;
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-	const uint64_t mask = (1ull << log2cap) - 1;
 	const uint64_t ntiles = pg_div_up(n, HJ_TILE);
 	unsigned long long cnt_acc = 0, sum_acc = 0;
 
@@ -174,30 +264,10 @@ k_probe_unique(const char* __restrict__ S, uint64_t n, uint32_t W, uint32_t koff
 				}
 			}
 		}
-		uint4 sl[HJ_ITEMS];
 		#pragma unroll
 		for (int j = 0; j < HJ_ITEMS; ++j) {
 			uint64_t r = base + (uint64_t) j * HJ_THREADS + tid;
-			if (r < n && key[j] != PG_EMPTY_KEY)
-				sl[j] = pg_ld_table16(slots + 2 * hj_slot0(key[j], log2cap));
-		}
-		#pragma unroll
-		for (int j = 0; j < HJ_ITEMS; ++j) {
-			uint64_t r = base + (uint64_t) j * HJ_THREADS + tid;
-			if (r >= n) continue;
-			if (key[j] == PG_EMPTY_KEY) {
-				if (nside) { hit[j] = true; val[j] = side[0]; }
-				continue;
-			}
-			uint64_t s = hj_slot0(key[j], log2cap);
-			uint4 v = sl[j];
-			for (uint64_t probe = 0;; ++probe) {
-				int64_t sk = (int64_t) (((uint64_t) v.y << 32) | v.x);
-				if (sk == key[j]) { hit[j] = true; val[j] = ((uint64_t) v.w << 32) | v.z; break; }
-				if (sk == PG_EMPTY_KEY || probe > mask) break;
-				s = (s + 1) & mask;
-				v = pg_ld_table16(slots + 2 * s);
-			}
+			if (r < n) hit[j] = hj_lookup_unique(tb, dense, key[j], val[j]);
 		}
 		if (MATERIALIZE) {
 			// Tile-order ranks: item-major, then warp, then lane.
@@ -272,21 +342,24 @@ k_probe_unique(const char* __restrict__ S, uint64_t n, uint32_t W, uint32_t koff
 
 // ---------------------------------------------------------------------------
 // Unique-key probe of 16-byte tuples, Blackwell path. Per CTA, persistent over
-// tiles of 2048 probe tuples:
-//   * tiles arrive in shared memory by bulk copy (cp.async.bulk + mbarrier),
-//     the next tile prefetched while the current one is probed;
-//   * each thread resolves 8 keys; every key's first 32-byte bucket (two
-//     slots) is fetched with one 256-bit evict-last load, all 8 issued before
-//     any is inspected, and keys that need a further bucket advance together
-//     in rounds, so dependent loads overlap;
-//   * matches are ranked in tile order with warp ballots, assembled as output
-//     rows in shared memory and written with one bulk store per tile to a
-//     range reserved by a single atomicAdd (only the issuing thread waits on
-//     it).
+// tiles of 1024 probe tuples:
+//   * tiles arrive in shared memory by bulk copy (cp.async.bulk + mbarrier,
+//     L2 evict-first), the next tile prefetched while the current one is
+//     probed;
+//   * each thread resolves 4 keys. Hashed tables: every key's first 32-byte
+//     bucket (two slots) is fetched with one 256-bit evict-last load, all
+//     issued before any is inspected, and keys needing a further bucket
+//     advance together in rounds. Dense tables: one bitmap word and one
+//     8-byte value per key, both issued at once;
+//   * matches are ranked in tile order (warp ballots + per-warp prefix),
+//     assembled as output rows in shared memory, and written with one bulk
+//     store per tile (evict-first) into a range reserved by a single
+//     atomicAdd that only the issuing thread waits on.
 // ---------------------------------------------------------------------------
 #define HJT_TILE 1024
 #define HJT_THREADS 256
 #define HJT_ITEMS (HJT_TILE / HJT_THREADS)
+#define HJT_WARPS (HJT_THREADS / 32)
 
 __device__ __forceinline__ uint32_t hj_pick(const uint4& t, uint64_t v, uint32_t i)
 {
@@ -299,11 +372,9 @@ __device__ __forceinline__ uint32_t hj_pick(const uint4& t, uint64_t v, uint32_t
 	return r;
 }
 
-template <bool MATERIALIZE>
+template <bool MATERIALIZE, bool DENSE>
 __global__ void __launch_bounds__(HJT_THREADS, 3)
-k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff,
-		const unsigned long long* __restrict__ slots, uint32_t log2cap,
-		const unsigned long long* __restrict__ side, uint32_t nside,
+k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb,
 		uint32_t wsel, uint32_t sum_w0, uint32_t sum_words, char* __restrict__ out, uint64_t out_cap,
 		unsigned long long* __restrict__ cursor, unsigned long long* __restrict__ agg,
 		int sum_col, int* __restrict__ status)
@@ -312,12 +383,12 @@ k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff,
 	uint4* const tin0 = reinterpret_cast<uint4*>(sm);
 	uint4* const tout = reinterpret_cast<uint4*>(sm + 2 * HJT_TILE * 16);
 	__shared__ __align__(8) uint64_t bar[2];
-	__shared__ uint32_t wcnt[HJT_ITEMS][HJT_THREADS / 32];
-	__shared__ uint32_t tile_total;
+	__shared__ uint32_t wsum[HJT_WARPS];
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-	const uint64_t mask = (1ull << log2cap) - 1;
+	const uint64_t mask = (1ull << tb.log2cap) - 1;
 	const uint64_t ntiles = pg_div_up(n, HJT_TILE);
-	const uint64_t pol = pg_policy_evict_last();
+	const uint64_t keep = pg_policy_evict_last();
+	const uint64_t stream = pg_policy_evict_first();
 	unsigned long long cnt_acc = 0, sum_acc = 0;
 	// Output word i is source word (wsel >> 4i) & 15 of (probe tuple words
 	// 0-3, packed build value words 4-5).
@@ -329,87 +400,108 @@ k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff,
 	auto issue = [&](uint64_t t, int b) {
 		const uint32_t rows = (uint32_t) pg_min64(HJT_TILE, n - t * HJT_TILE);
 		pg_mbar_expect_tx(&bar[b], rows * 16);
-		pg_bulk_g2s(tin0 + b * HJT_TILE, S + t * (uint64_t) HJT_TILE * 16, rows * 16, &bar[b]);
+		pg_bulk_g2s_hint(tin0 + b * HJT_TILE, S + t * (uint64_t) HJT_TILE * 16, rows * 16, &bar[b], stream);
 	};
 	if (tid == 0) issue(tile, 0);
 	uint32_t phases = 0;     // bit b: parity expected next on bar[b]
 	for (int it = 0; tile < ntiles; tile += gridDim.x, ++it) {
 		const int b = it & 1;
-		const uint4* const tb = tin0 + b * HJT_TILE;
+		const uint4* const tp = tin0 + b * HJT_TILE;
 		const uint64_t base = tile * HJT_TILE;
 		const uint32_t rows = (uint32_t) pg_min64(HJT_TILE, n - base);
-		const bool ok = pg_mbar_wait(&bar[b], (phases >> b) & 1);
-		if (__syncthreads_or(!ok)) { if (tid == 0) pg_set_status(status, PG_ERR_TIMEOUT); break; }
+		// A wait that gives up leaves the tile's contents unspecified; every
+		// later access stays in bounds and the host sees the status.
+		if (!pg_mbar_wait(&bar[b], (phases >> b) & 1)) pg_set_status(status, PG_ERR_TIMEOUT);
 		phases ^= 1u << b;
-		// Prefetch the next tile into the other buffer (its previous contents
-		// were consumed before the last __syncthreads of the previous tile).
+		// Prefetch the next tile into the other buffer; its previous contents
+		// were last read before the final barrier of the previous tile.
 		if (tid == 0 && tile + gridDim.x < ntiles) issue(tile + gridDim.x, b ^ 1);
 
 		int64_t key[HJT_ITEMS];
-		uint64_t slot[HJT_ITEMS];
 		uint64_t val[HJT_ITEMS];
-		bool hit[HJT_ITEMS], open[HJT_ITEMS];
-		#pragma unroll
-		for (int j = 0; j < HJT_ITEMS; ++j) {
-			const uint32_t p = j * HJT_THREADS + tid;
-			hit[j] = false; open[j] = false; val[j] = 0;
-			key[j] = 0;
-			if (p < rows) {
-				const uint4 t = tb[p];
-				key[j] = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
-				if (key[j] == PG_EMPTY_KEY) { if (nside) { hit[j] = true; val[j] = side[0]; } }
-				else { open[j] = true; slot[j] = hj_slot0(key[j], log2cap); }
-			}
-		}
-		// Rounds of bucket loads: all open keys issue, then all inspect.
-		for (uint32_t round = 0; round <= (mask >> 1); ++round) {
-			pg_u64x4 bk[HJT_ITEMS];
-			bool any = false;
-			#pragma unroll
-			for (int j = 0; j < HJT_ITEMS; ++j)
-				if (open[j]) { bk[j] = pg_ld_bucket32(slots + 2 * slot[j], pol); any = true; }
-			if (!any) break;
+		bool hit[HJT_ITEMS];
+		if (DENSE) {
+			uint32_t bits[HJT_ITEMS];
 			#pragma unroll
 			for (int j = 0; j < HJT_ITEMS; ++j) {
-				if (!open[j]) continue;
-				if ((long long) bk[j].a == key[j]) { hit[j] = true; val[j] = bk[j].b; open[j] = false; }
-				else if (bk[j].a == (unsigned long long) PG_EMPTY_KEY) open[j] = false;
-				else if ((long long) bk[j].c == key[j]) { hit[j] = true; val[j] = bk[j].d; open[j] = false; }
-				else if (bk[j].c == (unsigned long long) PG_EMPTY_KEY) open[j] = false;
-				else slot[j] = (slot[j] + 2) & mask;
+				const uint32_t p = j * HJT_THREADS + tid;
+				hit[j] = false; val[j] = 0; bits[j] = 0;
+				if (p < rows) {
+					const uint4 t = tp[p];
+					key[j] = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
+					const unsigned long long d = (unsigned long long) key[j] - (unsigned long long) tb.dmin;
+					if (d < tb.drange) {
+						bits[j] = __ldg(tb.dense_bits + (d >> 5)) >> (d & 31);
+						asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u64 %0, [%1], %2;"
+								: "=l"(val[j]) : "l"(tb.dense_val + d), "l"(keep));
+						hit[j] = true;
+					}
+				}
+			}
+			#pragma unroll
+			for (int j = 0; j < HJT_ITEMS; ++j) hit[j] = hit[j] && (bits[j] & 1);
+		} else {
+			uint64_t slot[HJT_ITEMS];
+			bool open[HJT_ITEMS];
+			#pragma unroll
+			for (int j = 0; j < HJT_ITEMS; ++j) {
+				const uint32_t p = j * HJT_THREADS + tid;
+				hit[j] = false; open[j] = false; val[j] = 0;
+				key[j] = 0;
+				if (p < rows) {
+					const uint4 t = tp[p];
+					key[j] = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
+					if (key[j] == PG_EMPTY_KEY) { if (tb.nside) { hit[j] = true; val[j] = tb.side[0]; } }
+					else { open[j] = true; slot[j] = hj_slot0(key[j], tb.log2cap); }
+				}
+			}
+			// Rounds of bucket loads: all open keys issue, then all inspect.
+			for (uint32_t round = 0; round <= (mask >> 1); ++round) {
+				pg_u64x4 bk[HJT_ITEMS];
+				bool any = false;
+				#pragma unroll
+				for (int j = 0; j < HJT_ITEMS; ++j)
+					if (open[j]) { bk[j] = pg_ld_bucket32(tb.slots + 2 * slot[j], keep); any = true; }
+				if (!any) break;
+				#pragma unroll
+				for (int j = 0; j < HJT_ITEMS; ++j) {
+					if (!open[j]) continue;
+					if ((long long) bk[j].a == key[j]) { hit[j] = true; val[j] = bk[j].b; open[j] = false; }
+					else if (bk[j].a == (unsigned long long) PG_EMPTY_KEY) open[j] = false;
+					else if ((long long) bk[j].c == key[j]) { hit[j] = true; val[j] = bk[j].d; open[j] = false; }
+					else if (bk[j].c == (unsigned long long) PG_EMPTY_KEY) open[j] = false;
+					else slot[j] = (slot[j] + 2) & mask;
+				}
 			}
 		}
 		if (MATERIALIZE) {
-			uint32_t ball[HJT_ITEMS];
+			// Row order in the tile: warp, then item, then lane.
+			uint32_t ball[HJT_ITEMS], mine = 0;
 			#pragma unroll
-			for (int j = 0; j < HJT_ITEMS; ++j) {
-				ball[j] = __ballot_sync(0xffffffffu, hit[j]);
-				if (lane == 0) wcnt[j][warp] = __popc(ball[j]);
-			}
+			for (int j = 0; j < HJT_ITEMS; ++j) { ball[j] = __ballot_sync(0xffffffffu, hit[j]); mine += __popc(ball[j]); }
+			if (lane == 0) wsum[warp] = mine;
 			// The output buffer is free once the previous tile's bulk store
 			// has read it.
 			if (tid == 0) pg_bulk_wait_read();
 			__syncthreads();
-			if (tid == 0) {
-				uint32_t run = 0;
-				for (int j = 0; j < HJT_ITEMS; ++j)
-					for (int w = 0; w < HJT_THREADS / 32; ++w) { uint32_t c = wcnt[j][w]; wcnt[j][w] = run; run += c; }
-				tile_total = run;
-			}
-			__syncthreads();
+			uint32_t pos = 0, total = 0;
+			#pragma unroll
+			for (int w = 0; w < HJT_WARPS; ++w) { uint32_t c = wsum[w]; pos += w < warp ? c : 0; total += c; }
 			#pragma unroll
 			for (int j = 0; j < HJT_ITEMS; ++j) {
-				if (!hit[j]) continue;
-				const uint32_t pos = wcnt[j][warp] + __popc(ball[j] & ((1u << lane) - 1));
-				const uint4 t = tb[j * HJT_THREADS + tid];
-				tout[pos] = make_uint4(hj_pick(t, val[j], w0), hj_pick(t, val[j], w1),
-						hj_pick(t, val[j], w2), hj_pick(t, val[j], w3));
+				if (hit[j]) {
+					const uint4 t = tp[j * HJT_THREADS + tid];
+					tout[pos + __popc(ball[j] & ((1u << lane) - 1))] =
+						make_uint4(hj_pick(t, val[j], w0), hj_pick(t, val[j], w1),
+								hj_pick(t, val[j], w2), hj_pick(t, val[j], w3));
+				}
+				pos += __popc(ball[j]);
 			}
 			pg_fence_proxy_async_smem();
 			__syncthreads();
-			if (tid == 0 && tile_total) {
-				const unsigned long long at = atomicAdd(cursor, (unsigned long long) tile_total);
-				if (at + tile_total <= out_cap) pg_bulk_s2g(out + at * 16, tout, tile_total * 16);
+			if (tid == 0 && total) {
+				const unsigned long long at = atomicAdd(cursor, (unsigned long long) total);
+				if (at + total <= out_cap) pg_bulk_s2g_hint(out + at * 16, tout, total * 16, stream);
 			}
 		} else {
 			#pragma unroll
@@ -417,14 +509,14 @@ k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff,
 				if (!hit[j]) continue;
 				cnt_acc++;
 				if (sum_col >= 0) {
-					const uint4 t = tb[j * HJT_THREADS + tid];
+					const uint4 t = tp[j * HJT_THREADS + tid];
 					const uint32_t lo = hj_pick(t, val[j], (wsel >> (4 * sum_w0)) & 15);
 					if (sum_words == 2)
 						sum_acc += ((unsigned long long) hj_pick(t, val[j], (wsel >> (4 * sum_w0 + 4)) & 15) << 32) | lo;
 					else sum_acc += (unsigned long long) (long long) (int32_t) lo;
 				}
 			}
-			__syncthreads();   // tile buffer b is refilled by the prefetch two tiles on
+			__syncthreads();   // tile buffer b is refilled by the next prefetch
 		}
 	}
 	if (MATERIALIZE) {
@@ -613,6 +705,48 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 			bbytes += proj[i].bytes;
 		}
 	ht->inline_val = bbytes <= 8;
+	ht->dense = false; ht->dense_val = nullptr; ht->dense_bits = nullptr;
+	if (R->n) {
+		// Dense key domain (unique keys spanning at most 2|R| values, e.g. a
+		// surrogate primary key 1..N): index by key - min, no hashing.
+		unsigned long long* mm = nullptr;
+		if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 32))) { delete ht; return rc; }
+		unsigned long long init[4] = {~0ull, 0, 0, 0};
+		PG_CUDA(ctx, cudaMemcpyAsync(mm, init, 32, cudaMemcpyHostToDevice, s));
+		int blocks = (int) std::min<uint64_t>(pg_div_up(R->n, 256), (uint64_t) ctx->sm_count * 8);
+		k_key_minmax<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off, R->key_bytes, mm);
+		PG_LAUNCHED(ctx);
+		unsigned long long h[2];
+		PG_CUDA(ctx, cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, s));
+		PG_CUDA(ctx, cudaStreamSynchronize(s));
+		const long long kmin = (long long) (h[0] ^ (1ull << 63)), kmax = (long long) (h[1] ^ (1ull << 63));
+		const unsigned long long range = (unsigned long long) kmax - (unsigned long long) kmin + 1;
+		if (range != 0 && range <= std::max<uint64_t>(2 * R->n, 64) && range < (1ull << 34)) {
+			const uint64_t words = pg_div_up(range, 32);
+			if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense_val, range * 8))) { delete ht; return rc; }
+			if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense_bits, words * 4))) { delete ht; return rc; }
+			PG_CUDA(ctx, cudaMemsetAsync(ht->dense_bits, 0, words * 4, s));
+			PG_CUDA(ctx, cudaMemsetAsync(mm, 0, 32, s));
+			k_dense_build<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off,
+					R->key_bytes, ht->bcols, ht->inline_val, kmin, ht->dense_val, ht->dense_bits,
+					reinterpret_cast<int*>(mm));
+			PG_LAUNCHED(ctx);
+			int dupflag = 0;
+			PG_CUDA(ctx, cudaMemcpyAsync(&dupflag, mm, 4, cudaMemcpyDeviceToHost, s));
+			PG_CUDA(ctx, cudaStreamSynchronize(s));
+			if (!dupflag) {
+				ht->dense = true; ht->unique = true; ht->dmin = kmin; ht->drange = range;
+				ht->slots = nullptr; ht->side = nullptr; ht->nside = 0; ht->log2cap = 1; ht->capacity = 0;
+				pg_free_async(ctx, s, mm);
+				*out = ht;
+				return PG_OK;
+			}
+			pg_free_async(ctx, s, ht->dense_val);
+			pg_free_async(ctx, s, ht->dense_bits);
+			ht->dense_val = nullptr; ht->dense_bits = nullptr;
+		}
+		pg_free_async(ctx, s, mm);
+	}
 	uint64_t want = std::max<uint64_t>(1024, 2 * R->n);
 	uint32_t lg = 10;
 	while ((1ull << lg) < want) ++lg;
@@ -658,6 +792,8 @@ extern "C" int pg_hashtable_free(pg_ctx* ctx, pg_hashtable* ht)
 	cudaStreamSynchronize(ht->stream);
 	pg_free_async(ctx, ht->stream, ht->slots);
 	pg_free_async(ctx, ht->stream, ht->side);
+	pg_free_async(ctx, ht->stream, ht->dense_val);
+	pg_free_async(ctx, ht->stream, ht->dense_bits);
 	delete ht;
 	return PG_OK;
 }
@@ -689,6 +825,9 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 		uint64_t cap, unsigned long long* acc, bool materialize, int sum_col)
 {
 	const uint64_t ntiles = pg_div_up(n, HJ_TILE);
+	HjProbeTable tb;
+	tb.slots = ht->slots; tb.log2cap = ht->log2cap; tb.side = ht->side; tb.nside = ht->nside;
+	tb.dense_val = ht->dense_val; tb.dense_bits = ht->dense_bits; tb.dmin = ht->dmin; tb.drange = ht->drange;
 	const bool fast16 = W == 16 && (koff == 0 || koff == 8) && kbytes == 8 && pc.ow_words == 4 &&
 		(reinterpret_cast<uintptr_t>(S) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
 	if (fast16) {
@@ -700,25 +839,23 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 				wsel |= (pc.side[c] ? (pc.src[c] + q) : (4u + pc.src[c] + q)) << (4 * o);
 		}
 		const int grid = (int) std::min<uint64_t>(pg_div_up(n, HJT_TILE), (uint64_t) ctx->sm_count * 3);
-		if (materialize) {
-			PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-			k_probe16_tma<true><<<grid, HJT_THREADS, smem, s>>>(S, n, koff, ht->slots, ht->log2cap, ht->side,
-					ht->nside, wsel, 0, 0, out, cap, acc, acc + 1, -1, ctx->d_status);
-		} else {
-			PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-			k_probe16_tma<false><<<grid, HJT_THREADS, smem, s>>>(S, n, koff, ht->slots, ht->log2cap, ht->side,
-					ht->nside, wsel, sum_w0, sum_words, nullptr, 0, acc, acc + 1, sum_col, ctx->d_status);
-		}
+#define HJT_LAUNCH(M, D) do { \
+			PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_tma<M, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
+			k_probe16_tma<M, D><<<grid, HJT_THREADS, smem, s>>>(S, n, koff, tb, wsel, sum_w0, sum_words, \
+					M ? out : nullptr, M ? cap : 0, acc, acc + 1, M ? -1 : sum_col, ctx->d_status); } while (0)
+		if (materialize) { if (ht->dense) HJT_LAUNCH(true, true); else HJT_LAUNCH(true, false); }
+		else { if (ht->dense) HJT_LAUNCH(false, true); else HJT_LAUNCH(false, false); }
+#undef HJT_LAUNCH
 		PG_LAUNCHED(ctx);
 		return PG_OK;
 	}
 	const int grid = (int) std::min<uint64_t>(ntiles, (uint64_t) ctx->sm_count * 8);
 	if (materialize)
-		k_probe_unique<true, false><<<grid, HJ_THREADS, 0, s>>>(S, n, W, koff, kbytes, ht->slots, ht->log2cap,
-				ht->side, ht->nside, pc, out, cap, acc, acc + 1, -1, ctx->d_status);
+		k_probe_unique<true, false><<<grid, HJ_THREADS, 0, s>>>(S, n, W, koff, kbytes, tb, ht->dense,
+				pc, out, cap, acc, acc + 1, -1, ctx->d_status);
 	else
-		k_probe_unique<false, false><<<grid, HJ_THREADS, 0, s>>>(S, n, W, koff, kbytes, ht->slots, ht->log2cap,
-				ht->side, ht->nside, pc, nullptr, 0, acc, acc + 1, sum_col, ctx->d_status);
+		k_probe_unique<false, false><<<grid, HJ_THREADS, 0, s>>>(S, n, W, koff, kbytes, tb, ht->dense,
+				pc, nullptr, 0, acc, acc + 1, sum_col, ctx->d_status);
 	PG_LAUNCHED(ctx);
 	return PG_OK;
 }

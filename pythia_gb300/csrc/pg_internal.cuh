@@ -172,6 +172,15 @@ __device__ __forceinline__ void pg_bulk_g2s(void* dst, const void* src, uint32_t
 			:: "r"(pg_smem_addr(dst)), "l"(src), "r"(bytes), "r"(pg_smem_addr(bar)) : "memory");
 }
 
+// Bulk copy global -> shared with an L2 eviction policy (streams: evict-first).
+__device__ __forceinline__ void pg_bulk_g2s_hint(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+		uint64_t pol)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+			" [%0], [%1], %2, [%3], %4;"
+			:: "r"(pg_smem_addr(dst)), "l"(src), "r"(bytes), "r"(pg_smem_addr(bar)), "l"(pol) : "memory");
+}
+
 // Bounded wait for phase `parity` of `bar`. Returns false when it gave up.
 __device__ __forceinline__ bool pg_mbar_wait(uint64_t* bar, uint32_t parity)
 {
@@ -242,6 +251,13 @@ __device__ __forceinline__ void pg_bulk_s2g(void* dst, const void* src, uint32_t
 {
 	asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
 			:: "l"(dst), "r"(pg_smem_addr(src)), "r"(bytes) : "memory");
+	asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void pg_bulk_s2g_hint(void* dst, const void* src, uint32_t bytes, uint64_t pol)
+{
+	asm volatile("cp.async.bulk.global.shared::cta.bulk_group.L2::cache_hint [%0], [%1], %2, %3;"
+			:: "l"(dst), "r"(pg_smem_addr(src)), "r"(bytes), "l"(pol) : "memory");
 	asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
 

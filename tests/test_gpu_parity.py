@@ -125,6 +125,19 @@ def test_join_pkfk_zipf(ctx):
     _join_check(ctx, R, S)
 
 
+def test_join_sparse_unique_keys(ctx):
+    # Unique keys spread over a wide domain take the hashed table (dense
+    # tables need the keys within twice |R| consecutive values).
+    R = dg.build_relation(60_000, dg.seed_for(17))
+    R[:, 0] = R[:, 0] * 7919 - (1 << 40)
+    S = dg.probe_uniform(500_000, R, dg.seed_for(18))
+    S[::1000, 0] += 3                      # some misses
+    R[5, 0] = -1                           # a unique key equal to the empty marker
+    S[::777, 0] = -1
+    _join_check(ctx, R, S)
+    _join_check(ctx, R, S, proj=(("B", 8, 8), ("P", 0, 8)))
+
+
 def test_join_many_to_many(ctx):
     R = dg.uniform_keys(5000, 700, dg.seed_for(5))
     S = dg.uniform_keys(9000, 900, dg.seed_for(6))
