@@ -532,6 +532,166 @@ k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPro
 }
 
 // ---------------------------------------------------------------------------
+// Unique-key probe of 16-byte tuples without block barriers: every warp runs
+// on its own. Warp w of the grid owns chunks w, w + W, w + 2W, ... of 256
+// probe tuples; each chunk arrives in the warp's own shared-memory stage by a
+// bulk copy (3 stages in flight per warp, L2 evict-first). With unique build
+// keys a probe tuple yields at most one row, so chunk c writes its rows to
+// output rows [256c, 256c + matches) in probe order: no atomics and no
+// block-wide ranking. When every probe tuple matches (PK-FK) the output is
+// already dense; otherwise per-chunk counts drive a compaction pass.
+// ---------------------------------------------------------------------------
+#define PW_WARPS 4
+#define PW_CHUNK 256
+#define PW_STAGES 3
+
+template <bool MATERIALIZE, bool DENSE>
+__global__ void __launch_bounds__(PW_WARPS * 32)
+k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb,
+		uint32_t wsel, uint32_t sum_w0, uint32_t sum_words, char* __restrict__ out,
+		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg,
+		int sum_col, int* __restrict__ status)
+{
+	constexpr int ITEMS = PW_CHUNK / 32;             // tuples per lane per chunk
+	constexpr int GROUP = DENSE ? ITEMS : 4;         // lookups issued together (registers)
+	extern __shared__ __align__(128) unsigned char sm[];
+	__shared__ __align__(8) uint64_t bars[PW_WARPS][PW_STAGES];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	uint4* const st0 = reinterpret_cast<uint4*>(sm) + (size_t) warp * PW_STAGES * PW_CHUNK;
+	uint64_t* const bar = bars[warp];
+	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
+	const uint64_t W = (uint64_t) gridDim.x * PW_WARPS;
+	const uint64_t first = (uint64_t) blockIdx.x * PW_WARPS + warp;
+	const uint64_t mask = (1ull << tb.log2cap) - 1;
+	const uint64_t keep = pg_policy_evict_last();
+	const uint64_t stream = pg_policy_evict_first();
+	const uint32_t w0 = wsel & 15, w1 = (wsel >> 4) & 15, w2 = (wsel >> 8) & 15, w3 = (wsel >> 12) & 15;
+	unsigned long long cnt_acc = 0, sum_acc = 0;
+	if (first >= nchunks) return;
+	auto issue = [&](uint64_t c, int stg) {
+		const uint32_t rows = (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK);
+		pg_mbar_expect_tx(&bar[stg], rows * 16);
+		pg_bulk_g2s_hint(st0 + stg * PW_CHUNK, S + c * (uint64_t) PW_CHUNK * 16, rows * 16, &bar[stg], stream);
+	};
+	if (lane == 0) {
+		for (int i = 0; i < PW_STAGES; ++i) pg_mbar_init(&bar[i], 1);
+		pg_fence_mbar_init();
+		for (int i = 0; i < PW_STAGES; ++i)
+			if (first + i * W < nchunks) issue(first + i * W, i);
+	}
+	__syncwarp();
+	for (uint64_t k = 0, c = first; c < nchunks; ++k, c += W) {
+		const int stg = (int) (k % PW_STAGES);
+		const uint32_t parity = (uint32_t) ((k / PW_STAGES) & 1);
+		// A wait that gives up leaves the chunk unspecified; all accesses stay
+		// in bounds and the host reads the status.
+		if (!pg_mbar_wait(&bar[stg], parity)) pg_set_status(status, PG_ERR_TIMEOUT);
+		const uint4* const tp = st0 + stg * PW_CHUNK;
+		const uint32_t rows = (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK);
+		uint32_t rank = 0;
+		#pragma unroll
+		for (int g = 0; g < ITEMS; g += GROUP) {
+			int64_t key[GROUP];
+			uint64_t val[GROUP];
+			bool hit[GROUP];
+			if (DENSE) {
+				uint32_t bits[GROUP];
+				#pragma unroll
+				for (int j = 0; j < GROUP; ++j) {
+					const uint32_t p = (g + j) * 32 + lane;
+					hit[j] = false; val[j] = 0; bits[j] = 0;
+					if (p < rows) {
+						const uint4 t = tp[p];
+						key[j] = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
+						const unsigned long long d = (unsigned long long) key[j] - (unsigned long long) tb.dmin;
+						if (d < tb.drange) {
+							bits[j] = __ldg(tb.dense_bits + (d >> 5)) >> (d & 31);
+							asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u64 %0, [%1], %2;"
+									: "=l"(val[j]) : "l"(tb.dense_val + d), "l"(keep));
+							hit[j] = true;
+						}
+					}
+				}
+				#pragma unroll
+				for (int j = 0; j < GROUP; ++j) hit[j] = hit[j] && (bits[j] & 1);
+			} else {
+				uint64_t slot[GROUP];
+				bool open[GROUP];
+				#pragma unroll
+				for (int j = 0; j < GROUP; ++j) {
+					const uint32_t p = (g + j) * 32 + lane;
+					hit[j] = false; open[j] = false; val[j] = 0; key[j] = 0;
+					if (p < rows) {
+						const uint4 t = tp[p];
+						key[j] = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
+						if (key[j] == PG_EMPTY_KEY) { if (tb.nside) { hit[j] = true; val[j] = tb.side[0]; } }
+						else { open[j] = true; slot[j] = hj_slot0(key[j], tb.log2cap); }
+					}
+				}
+				for (uint32_t round = 0; round <= (mask >> 1); ++round) {
+					pg_u64x4 bk[GROUP];
+					bool any = false;
+					#pragma unroll
+					for (int j = 0; j < GROUP; ++j)
+						if (open[j]) { bk[j] = pg_ld_bucket32(tb.slots + 2 * slot[j], keep); any = true; }
+					if (!any) break;
+					#pragma unroll
+					for (int j = 0; j < GROUP; ++j) {
+						if (!open[j]) continue;
+						if ((long long) bk[j].a == key[j]) { hit[j] = true; val[j] = bk[j].b; open[j] = false; }
+						else if (bk[j].a == (unsigned long long) PG_EMPTY_KEY) open[j] = false;
+						else if ((long long) bk[j].c == key[j]) { hit[j] = true; val[j] = bk[j].d; open[j] = false; }
+						else if (bk[j].c == (unsigned long long) PG_EMPTY_KEY) open[j] = false;
+						else slot[j] = (slot[j] + 2) & mask;
+					}
+				}
+			}
+			#pragma unroll
+			for (int j = 0; j < GROUP; ++j) {
+				const uint32_t ball = __ballot_sync(0xffffffffu, hit[j]);
+				if (hit[j]) {
+					const uint4 t = tp[(g + j) * 32 + lane];
+					if (MATERIALIZE) {
+						const uint64_t row = c * PW_CHUNK + rank + __popc(ball & ((1u << lane) - 1));
+						pg_st_hint16(out + row * 16, make_uint4(hj_pick(t, val[j], w0), hj_pick(t, val[j], w1),
+								hj_pick(t, val[j], w2), hj_pick(t, val[j], w3)), stream);
+					} else if (sum_col >= 0) {
+						const uint32_t lo = hj_pick(t, val[j], (wsel >> (4 * sum_w0)) & 15);
+						if (sum_words == 2)
+							sum_acc += ((unsigned long long) hj_pick(t, val[j], (wsel >> (4 * sum_w0 + 4)) & 15) << 32) | lo;
+						else sum_acc += (unsigned long long) (long long) (int32_t) lo;
+					}
+				}
+				rank += __popc(ball);
+			}
+		}
+		cnt_acc += rank;
+		if (MATERIALIZE && lane == 0) chunk_counts[c] = rank;
+		// Every lane has finished reading this stage: refill it.
+		__syncwarp();
+		if (lane == 0 && c + PW_STAGES * W < nchunks) issue(c + PW_STAGES * W, stg);
+	}
+	if (!MATERIALIZE) {
+		#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) sum_acc += __shfl_down_sync(0xffffffffu, sum_acc, o);
+	}
+	if (lane == 0) { atomicAdd(&agg[0], cnt_acc); if (!MATERIALIZE) atomicAdd(&agg[1], sum_acc); }
+}
+
+// Closes the gaps of a positional probe output: chunk c's rows move from
+// [256c, 256c + count) to [offs[c], offs[c] + count) of `dst`.
+__global__ void k_compact_chunks(const uint4* __restrict__ src, const uint64_t* __restrict__ counts,
+		const uint64_t* __restrict__ offs, uint64_t nchunks, uint4* __restrict__ dst, uint64_t cap)
+{
+	for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+		const uint32_t cnt = (uint32_t) counts[c];
+		const uint64_t o = offs[c];
+		for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x)
+			if (o + i < cap) dst[o + i] = src[c * PW_CHUNK + i];
+	}
+}
+
+// ---------------------------------------------------------------------------
 // General probe (duplicate build keys and/or row-index values): pass 1 counts
 // matches per tile (and folds count/sum), pass 2 writes at scanned offsets.
 // ---------------------------------------------------------------------------
@@ -706,9 +866,10 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 		}
 	ht->inline_val = bbytes <= 8;
 	ht->dense = false; ht->dense_val = nullptr; ht->dense_bits = nullptr;
-	if (R->n) {
+	if (R->n && ht->inline_val) {
 		// Dense key domain (unique keys spanning at most 2|R| values, e.g. a
-		// surrogate primary key 1..N): index by key - min, no hashing.
+		// surrogate primary key 1..N): index by key - min, no hashing. Only
+		// for packed values: the unique-key probe kernels read them inline.
 		unsigned long long* mm = nullptr;
 		if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 32))) { delete ht; return rc; }
 		unsigned long long init[4] = {~0ull, 0, 0, 0};
@@ -820,10 +981,15 @@ static int hj_make_cols(pg_ctx* ctx, const pg_hashtable* ht, const pg_col* proj,
 
 // Launches the unique-key probe over n tuples at S (device) into `out`;
 // counts/sums accumulate in acc[1..2], the output cursor is acc[0].
+// With `counts` (device, one word per 256-tuple chunk) and cap >= n, 16-byte
+// probes use the warp-independent kernel and write rows positionally; the
+// caller then compacts when fewer than n rows matched (*positional = true).
 static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht, const char* S,
 		uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes, const HjCols& pc, char* out,
-		uint64_t cap, unsigned long long* acc, bool materialize, int sum_col)
+		uint64_t cap, unsigned long long* acc, bool materialize, int sum_col,
+		uint64_t* counts = nullptr, bool* positional = nullptr)
 {
+	if (positional) *positional = false;
 	const uint64_t ntiles = pg_div_up(n, HJ_TILE);
 	HjProbeTable tb;
 	tb.slots = ht->slots; tb.log2cap = ht->log2cap; tb.side = ht->side; tb.nside = ht->nside;
@@ -837,6 +1003,21 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 			if (c == sum_col) { sum_w0 = o; sum_words = pc.words[c]; }
 			for (int q = 0; q < pc.words[c]; ++q, ++o)
 				wsel |= (pc.side[c] ? (pc.src[c] + q) : (4u + pc.src[c] + q)) << (4 * o);
+		}
+		if (!materialize || (counts && cap >= n)) {
+			const int psmem = PW_WARPS * PW_STAGES * PW_CHUNK * 16;
+			const int pgrid = (int) std::min<uint64_t>(pg_div_up(pg_div_up(n, PW_CHUNK), PW_WARPS),
+					(uint64_t) ctx->sm_count * 4);
+#define PW_LAUNCH(M, D) do { \
+			PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_warp<M, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, psmem)); \
+			k_probe16_warp<M, D><<<pgrid, PW_WARPS * 32, psmem, s>>>(S, n, koff, tb, wsel, sum_w0, sum_words, \
+					M ? out : nullptr, M ? counts : nullptr, M ? acc : acc + 1, M ? -1 : sum_col, ctx->d_status); } while (0)
+			if (materialize) { if (ht->dense) PW_LAUNCH(true, true); else PW_LAUNCH(true, false); }
+			else { if (ht->dense) PW_LAUNCH(false, true); else PW_LAUNCH(false, false); }
+#undef PW_LAUNCH
+			PG_LAUNCHED(ctx);
+			if (positional) *positional = materialize;
+			return PG_OK;
 		}
 		const int grid = (int) std::min<uint64_t>(pg_div_up(n, HJT_TILE), (uint64_t) ctx->sm_count * 3);
 #define HJT_LAUNCH(M, D) do { \
@@ -857,6 +1038,28 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 		k_probe_unique<false, false><<<grid, HJ_THREADS, 0, s>>>(S, n, W, koff, kbytes, tb, ht->dense,
 				pc, nullptr, 0, acc, acc + 1, sum_col, ctx->d_status);
 	PG_LAUNCHED(ctx);
+	return PG_OK;
+}
+
+// Compacts a positional probe output of n tuples with `total` matches in place
+// (through a scratch copy): chunk counts are scanned into offsets first.
+static int hj_compact(pg_ctx* ctx, cudaStream_t s, char* out, uint64_t n, uint64_t* counts, uint64_t total)
+{
+	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
+	int rc;
+	uint64_t* offs = nullptr;
+	char* tmp = nullptr;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &offs, nchunks * 8))) return rc;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &tmp, std::max<uint64_t>(total, 1) * 16))) return rc;
+	PG_CUDA(ctx, cudaMemcpyAsync(offs, counts, nchunks * 8, cudaMemcpyDeviceToDevice, s));
+	if ((rc = pg_scan_u64(ctx, s, offs, nchunks, nullptr))) return rc;
+	const int grid = (int) std::min<uint64_t>(nchunks, (uint64_t) ctx->sm_count * 16);
+	k_compact_chunks<<<grid, 256, 0, s>>>(reinterpret_cast<const uint4*>(out), counts, offs, nchunks,
+			reinterpret_cast<uint4*>(tmp), total);
+	PG_LAUNCHED(ctx);
+	if (total) PG_CUDA(ctx, cudaMemcpyAsync(out, tmp, total * 16, cudaMemcpyDeviceToDevice, s));
+	pg_free_async(ctx, s, offs);
+	pg_free_async(ctx, s, tmp);
 	return PG_OK;
 }
 
@@ -886,11 +1089,19 @@ extern "C" int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht
 	if (ht->unique && ht->inline_val) {
 		const char* Sd = (const char*) S->data;
 		if (materialize) {
+			uint64_t* counts = nullptr;
+			bool positional = false;
+			if ((rc = pg_alloc_async(ctx, s, (void**) &counts, pg_div_up(S->n, PW_CHUNK) * 8))) return rc;
 			if ((rc = hj_launch_unique(ctx, s, ht, Sd, S->n, S->width, S->key_off, S->key_bytes, pc,
-					(char*) out, out_capacity, acc, true, -1))) return rc;
+					(char*) out, out_capacity, acc, true, -1, counts, &positional))) return rc;
 			PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
 			if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
 			res->n_out = host_acc[0];
+			if (positional && res->n_out < S->n) {
+				if ((rc = hj_compact(ctx, s, (char*) out, S->n, counts, res->n_out))) return rc;
+				if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
+			}
+			pg_free_async(ctx, s, counts);
 			if (sum_col >= 0 || (flags & PG_JOIN_COUNT)) {
 				// Fold count/sum with a second, non-materialising pass.
 				if ((rc = hj_launch_unique(ctx, s, ht, Sd, S->n, S->width, S->key_off, S->key_bytes, pc,
@@ -914,6 +1125,8 @@ extern "C" int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht
 	}
 
 	// General path: one CTA per tile for the count pass, scan, write pass.
+	// It walks hashed slots, which a dense table does not have.
+	if (ht->dense) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe: dense table on the general path");
 	uint64_t* tile_counts = nullptr;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &tile_counts, (ntiles + 1) * 8))) return rc;
 	k_probe_general<false><<<(unsigned) ntiles, HJ_THREADS, 0, s>>>((const char*) S->data, S->n, S->width,
@@ -965,6 +1178,8 @@ extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
 	PG_CUDA(ctx, cudaStreamCreateWithFlags(&scomp, cudaStreamNonBlocking));
 	PG_CUDA(ctx, cudaStreamCreateWithFlags(&sout, cudaStreamNonBlocking));
 	char *dR = nullptr, *dS[2] = {nullptr, nullptr}, *dO[2] = {nullptr, nullptr};
+	uint64_t* dC[2] = {nullptr, nullptr};     // per-chunk match counts of a positional probe
+	bool posit[2] = {false, false};
 	unsigned long long* acc = nullptr;        // per chunk slot: [cursor, count, sum, pad] x 2
 	unsigned long long* hacc = nullptr;       // pinned copy of acc
 	pg_hashtable* ht = nullptr;
@@ -978,6 +1193,7 @@ extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
 		cudaStreamSynchronize(sin); cudaStreamSynchronize(scomp); cudaStreamSynchronize(sout);
 		if (ht) pg_hashtable_free(ctx, ht);
 		cudaFree(dR); cudaFree(dS[0]); cudaFree(dS[1]); cudaFree(dO[0]); cudaFree(dO[1]); cudaFree(acc);
+		cudaFree(dC[0]); cudaFree(dC[1]);
 		if (hacc) cudaFreeHost(hacc);
 		for (int i = 0; i < 2; ++i) { cudaEventDestroy(ev_in[i]); cudaEventDestroy(ev_comp[i]); cudaEventDestroy(ev_out[i]); }
 		cudaStreamDestroy(sin); cudaStreamDestroy(scomp); cudaStreamDestroy(sout);
@@ -1018,6 +1234,7 @@ extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
 	for (int i = 0; i < 2; ++i) {
 		HJH_TRY(cudaMalloc(&dS[i], CH * Sh->width));
 		if (materialize) HJH_TRY(cudaMalloc(&dO[i], CH * ow));
+		HJH_TRY(cudaMalloc(&dC[i], pg_div_up(CH, PW_CHUNK) * 8));
 	}
 	HJH_TRY(cudaMalloc(&acc, 2 * 4 * sizeof(unsigned long long)));
 	HJH_TRY(cudaMallocHost(&hacc, 2 * 4 * sizeof(unsigned long long)));
@@ -1036,7 +1253,7 @@ extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
 		if (c >= 2) HJH_TRY(cudaStreamWaitEvent(scomp, ev_out[b], 0));   // output buffer free
 		HJH_TRY(cudaMemsetAsync(acc + 4 * b, 0, 32, scomp));
 		if (materialize && hj_launch_unique(ctx, scomp, ht, dS[b], rows, Sh->width, Sh->key_off, Sh->key_bytes,
-				pc, dO[b], CH, acc + 4 * b, true, -1)) { cleanup(); return PG_ERR_CUDA; }
+				pc, dO[b], CH, acc + 4 * b, true, -1, dC[b], &posit[b])) { cleanup(); return PG_ERR_CUDA; }
 		if ((!materialize || sum_col >= 0 || (flags & PG_JOIN_COUNT)) &&
 				hj_launch_unique(ctx, scomp, ht, dS[b], rows, Sh->width, Sh->key_off, Sh->key_bytes,
 				pc, nullptr, 0, acc + 4 * b, false, sum_col)) { cleanup(); return PG_ERR_CUDA; }
@@ -1055,6 +1272,12 @@ extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
 		if (!materialize || sum_col >= 0 || (flags & PG_JOIN_COUNT)) sum += hacc[4 * b + 2];
 		if (materialize && rows_out) {
 			if (written + rows_out > out_capacity) { written += rows_out; continue; }
+			const uint64_t rows_in = std::min<uint64_t>(CH, nS - c * CH);
+			if (posit[b] && rows_out < rows_in) {
+				// Some probe tuples missed: close the gaps before copying out.
+				if ((rc = hj_compact(ctx, scomp, dO[b], rows_in, dC[b], rows_out))) { cleanup(); return rc; }
+				HJH_TRY(cudaEventRecord(ev_comp[b], scomp));
+			}
 			HJH_TRY(cudaStreamWaitEvent(sout, ev_comp[b], 0));
 			HJH_TRY(cudaMemcpyAsync((char*) out_host + written * ow, dO[b], rows_out * ow, cudaMemcpyDeviceToHost, sout));
 			written += rows_out;
