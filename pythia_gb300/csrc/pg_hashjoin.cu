@@ -72,6 +72,12 @@ struct pg_hashtable {
 	uint32_t* dense_bits;
 	long long dmin;
 	unsigned long long drange;
+	// Narrow dense layout: 4-byte entries holding value - vmin (frame of
+	// reference), all ones for an absent key; used when the packed build
+	// values span fewer than 2^32 - 1 values. Halves the table (a 16M-key
+	// table is 64 MB, which stays in L2) and needs no presence bitmap.
+	uint32_t* dense32;
+	unsigned long long vmin;
 };
 
 struct HjProbeTable {
@@ -81,6 +87,8 @@ struct HjProbeTable {
 	uint32_t nside;
 	const unsigned long long* dense_val;   // dense: value per key - dmin
 	const uint32_t* dense_bits;            // dense: presence bit per key - dmin
+	const uint32_t* dense32;               // narrow dense: value - vmin, or all ones
+	unsigned long long vmin;
 	long long dmin;
 	unsigned long long drange;
 };
@@ -138,24 +146,61 @@ __global__ void k_ht_build(const char* __restrict__ R, uint64_t n, uint32_t W, u
 	if (__any_sync(__activemask(), dup) && dup) atomicOr(flags, 1);
 }
 
-// Key range of the build side (signed keys mapped to ordered unsigned words).
-__global__ void k_key_minmax(const char* __restrict__ R, uint64_t n, uint32_t W, uint32_t koff,
-		uint32_t kbytes, unsigned long long* __restrict__ mm)
+// Key range of the build side (signed keys mapped to ordered unsigned words)
+// and the range of the packed build values (unsigned): mm = {kmin, kmax, vmin, vmax}.
+__device__ __forceinline__ uint64_t hj_pack_value(const char* t, const HjBuildCols& bc)
 {
-	unsigned long long lo = ~0ull, hi = 0;
+	uint32_t w[2] = {0, 0};
+	int o = 0;
+	for (int c = 0; c < bc.n; ++c)
+		for (int j = 0; j < bc.words[c]; ++j) w[o++] = reinterpret_cast<const uint32_t*>(t)[bc.roff[c] + j];
+	return ((uint64_t) w[1] << 32) | w[0];
+}
+
+__global__ void k_key_minmax(const char* __restrict__ R, uint64_t n, uint32_t W, uint32_t koff,
+		uint32_t kbytes, HjBuildCols bc, unsigned long long* __restrict__ mm)
+{
+	unsigned long long lo = ~0ull, hi = 0, vlo = ~0ull, vhi = 0;
 	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
 			i += (uint64_t) gridDim.x * blockDim.x) {
-		const unsigned long long u = (unsigned long long) pg_load_key(R + i * W + koff, kbytes) ^ (1ull << 63);
+		const char* t = R + i * W;
+		const unsigned long long u = (unsigned long long) pg_load_key(t + koff, kbytes) ^ (1ull << 63);
+		const unsigned long long v = hj_pack_value(t, bc);
 		lo = u < lo ? u : lo;
 		hi = u > hi ? u : hi;
+		vlo = v < vlo ? v : vlo;
+		vhi = v > vhi ? v : vhi;
 	}
 	#pragma unroll
 	for (int o = 16; o > 0; o >>= 1) {
 		unsigned long long a = __shfl_down_sync(0xffffffffu, lo, o), b = __shfl_down_sync(0xffffffffu, hi, o);
+		unsigned long long c = __shfl_down_sync(0xffffffffu, vlo, o), d = __shfl_down_sync(0xffffffffu, vhi, o);
 		lo = a < lo ? a : lo;
 		hi = b > hi ? b : hi;
+		vlo = c < vlo ? c : vlo;
+		vhi = d > vhi ? d : vhi;
 	}
-	if ((threadIdx.x & 31) == 0) { atomicMin(&mm[0], lo); atomicMax(&mm[1], hi); }
+	if ((threadIdx.x & 31) == 0) {
+		atomicMin(&mm[0], lo); atomicMax(&mm[1], hi);
+		atomicMin(&mm[2], vlo); atomicMax(&mm[3], vhi);
+	}
+}
+
+// Narrow dense table: entry key - dmin holds value - vmin; an entry that was
+// not all ones before the exchange means a duplicate key.
+__global__ void k_dense32_build(const char* __restrict__ R, uint64_t n, uint32_t W, uint32_t koff,
+		uint32_t kbytes, HjBuildCols bc, long long dmin, unsigned long long vmin,
+		uint32_t* __restrict__ table, int* __restrict__ flags)
+{
+	bool dup = false;
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+			i += (uint64_t) gridDim.x * blockDim.x) {
+		const char* t = R + i * W;
+		const unsigned long long d = (unsigned long long) pg_load_key(t + koff, kbytes) - (unsigned long long) dmin;
+		const uint32_t e = (uint32_t) (hj_pack_value(t, bc) - vmin);
+		if (atomicExch(&table[d], e) != 0xFFFFFFFFu) dup = true;
+	}
+	if (dup) atomicOr(flags, 1);
 }
 
 // Dense table: presence bit and value at key - dmin. A bit found already set
@@ -207,7 +252,13 @@ __device__ __forceinline__ bool hj_lookup_unique(const HjProbeTable& tb, bool de
 {
 	if (dense) {
 		const unsigned long long d = (unsigned long long) k - (unsigned long long) tb.dmin;
-		if (d >= tb.drange || !((tb.dense_bits[d >> 5] >> (d & 31)) & 1)) return false;
+		if (d >= tb.drange) return false;
+		if (tb.dense32) {
+			const uint32_t e = tb.dense32[d];
+			val = tb.vmin + e;
+			return e != 0xFFFFFFFFu;
+		}
+		if (!((tb.dense_bits[d >> 5] >> (d & 31)) & 1)) return false;
 		val = tb.dense_val[d];
 		return true;
 	}
@@ -372,7 +423,7 @@ __device__ __forceinline__ uint32_t hj_pick(const uint4& t, uint64_t v, uint32_t
 	return r;
 }
 
-template <bool MATERIALIZE, bool DENSE>
+template <bool MATERIALIZE, int MODE>
 __global__ void __launch_bounds__(HJT_THREADS, 3)
 k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb,
 		uint32_t wsel, uint32_t sum_w0, uint32_t sum_words, char* __restrict__ out, uint64_t out_cap,
@@ -420,7 +471,7 @@ k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPro
 		int64_t key[HJT_ITEMS];
 		uint64_t val[HJT_ITEMS];
 		bool hit[HJT_ITEMS];
-		if (DENSE) {
+		if (MODE != 0) {
 			uint32_t bits[HJT_ITEMS];
 			#pragma unroll
 			for (int j = 0; j < HJT_ITEMS; ++j) {
@@ -431,9 +482,17 @@ k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPro
 					key[j] = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
 					const unsigned long long d = (unsigned long long) key[j] - (unsigned long long) tb.dmin;
 					if (d < tb.drange) {
-						bits[j] = __ldg(tb.dense_bits + (d >> 5)) >> (d & 31);
-						asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u64 %0, [%1], %2;"
-								: "=l"(val[j]) : "l"(tb.dense_val + d), "l"(keep));
+						if (MODE == 2) {
+							uint32_t e;
+							asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;"
+									: "=r"(e) : "l"(tb.dense32 + d), "l"(keep));
+							bits[j] = e != 0xFFFFFFFFu;
+							val[j] = tb.vmin + e;
+						} else {
+							bits[j] = __ldg(tb.dense_bits + (d >> 5)) >> (d & 31);
+							asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u64 %0, [%1], %2;"
+									: "=l"(val[j]) : "l"(tb.dense_val + d), "l"(keep));
+						}
 						hit[j] = true;
 					}
 				}
@@ -533,27 +592,27 @@ k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPro
 
 // ---------------------------------------------------------------------------
 // Unique-key probe of 16-byte tuples without block barriers: every warp runs
-// on its own. Warp w of the grid owns chunks w, w + W, w + 2W, ... of 256
+// on its own. Warp w of the grid owns chunks w, w + W, w + 2W, ... of 128
 // probe tuples; each chunk arrives in the warp's own shared-memory stage by a
-// bulk copy (3 stages in flight per warp, L2 evict-first). With unique build
+// bulk copy (2 stages in flight per warp, L2 evict-first). With unique build
 // keys a probe tuple yields at most one row, so chunk c writes its rows to
-// output rows [256c, 256c + matches) in probe order: no atomics and no
+// output rows [128c, 128c + matches) in probe order: no atomics and no
 // block-wide ranking. When every probe tuple matches (PK-FK) the output is
 // already dense; otherwise per-chunk counts drive a compaction pass.
 // ---------------------------------------------------------------------------
-#define PW_WARPS 4
-#define PW_CHUNK 256
-#define PW_STAGES 3
+#define PW_WARPS 8
+#define PW_CHUNK 128
+#define PW_STAGES 2
 
-template <bool MATERIALIZE, bool DENSE>
-__global__ void __launch_bounds__(PW_WARPS * 32)
+template <bool MATERIALIZE, int MODE>
+__global__ void __launch_bounds__(PW_WARPS * 32, MODE != 0 ? 4 : 2)
 k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb,
 		uint32_t wsel, uint32_t sum_w0, uint32_t sum_words, char* __restrict__ out,
 		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg,
 		int sum_col, int* __restrict__ status)
 {
 	constexpr int ITEMS = PW_CHUNK / 32;             // tuples per lane per chunk
-	constexpr int GROUP = DENSE ? ITEMS : 4;         // lookups issued together (registers)
+	constexpr int GROUP = MODE != 0 ? ITEMS : 4;     // lookups issued together (registers)
 	extern __shared__ __align__(128) unsigned char sm[];
 	__shared__ __align__(8) uint64_t bars[PW_WARPS][PW_STAGES];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -594,7 +653,7 @@ k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 			int64_t key[GROUP];
 			uint64_t val[GROUP];
 			bool hit[GROUP];
-			if (DENSE) {
+			if (MODE != 0) {
 				uint32_t bits[GROUP];
 				#pragma unroll
 				for (int j = 0; j < GROUP; ++j) {
@@ -605,9 +664,17 @@ k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 						key[j] = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
 						const unsigned long long d = (unsigned long long) key[j] - (unsigned long long) tb.dmin;
 						if (d < tb.drange) {
-							bits[j] = __ldg(tb.dense_bits + (d >> 5)) >> (d & 31);
-							asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u64 %0, [%1], %2;"
-									: "=l"(val[j]) : "l"(tb.dense_val + d), "l"(keep));
+							if (MODE == 2) {
+								uint32_t e;
+								asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;"
+										: "=r"(e) : "l"(tb.dense32 + d), "l"(keep));
+								bits[j] = e != 0xFFFFFFFFu;
+								val[j] = tb.vmin + e;
+							} else {
+								bits[j] = __ldg(tb.dense_bits + (d >> 5)) >> (d & 31);
+								asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u64 %0, [%1], %2;"
+										: "=l"(val[j]) : "l"(tb.dense_val + d), "l"(keep));
+							}
 							hit[j] = true;
 						}
 					}
@@ -679,7 +746,7 @@ k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 }
 
 // Closes the gaps of a positional probe output: chunk c's rows move from
-// [256c, 256c + count) to [offs[c], offs[c] + count) of `dst`.
+// [128c, 128c + count) to [offs[c], offs[c] + count) of `dst`.
 __global__ void k_compact_chunks(const uint4* __restrict__ src, const uint64_t* __restrict__ counts,
 		const uint64_t* __restrict__ offs, uint64_t nchunks, uint4* __restrict__ dst, uint64_t cap)
 {
@@ -865,38 +932,47 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 			bbytes += proj[i].bytes;
 		}
 	ht->inline_val = bbytes <= 8;
-	ht->dense = false; ht->dense_val = nullptr; ht->dense_bits = nullptr;
+	ht->dense = false; ht->dense_val = nullptr; ht->dense_bits = nullptr; ht->dense32 = nullptr; ht->vmin = 0;
 	if (R->n && ht->inline_val) {
 		// Dense key domain (unique keys spanning at most 2|R| values, e.g. a
 		// surrogate primary key 1..N): index by key - min, no hashing. Only
 		// for packed values: the unique-key probe kernels read them inline.
 		unsigned long long* mm = nullptr;
-		if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 32))) { delete ht; return rc; }
-		unsigned long long init[4] = {~0ull, 0, 0, 0};
+		if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 64))) { delete ht; return rc; }
+		unsigned long long init[4] = {~0ull, 0, ~0ull, 0};
 		PG_CUDA(ctx, cudaMemcpyAsync(mm, init, 32, cudaMemcpyHostToDevice, s));
 		int blocks = (int) std::min<uint64_t>(pg_div_up(R->n, 256), (uint64_t) ctx->sm_count * 8);
-		k_key_minmax<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off, R->key_bytes, mm);
+		k_key_minmax<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off, R->key_bytes,
+				ht->bcols, mm);
 		PG_LAUNCHED(ctx);
-		unsigned long long h[2];
-		PG_CUDA(ctx, cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, s));
+		unsigned long long h[4];
+		PG_CUDA(ctx, cudaMemcpyAsync(h, mm, 32, cudaMemcpyDeviceToHost, s));
 		PG_CUDA(ctx, cudaStreamSynchronize(s));
 		const long long kmin = (long long) (h[0] ^ (1ull << 63)), kmax = (long long) (h[1] ^ (1ull << 63));
 		const unsigned long long range = (unsigned long long) kmax - (unsigned long long) kmin + 1;
+		const bool narrow = h[3] - h[2] < 0xFFFFFFFFull;
 		if (range != 0 && range <= std::max<uint64_t>(2 * R->n, 64) && range < (1ull << 34)) {
-			const uint64_t words = pg_div_up(range, 32);
-			if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense_val, range * 8))) { delete ht; return rc; }
-			if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense_bits, words * 4))) { delete ht; return rc; }
-			PG_CUDA(ctx, cudaMemsetAsync(ht->dense_bits, 0, words * 4, s));
-			PG_CUDA(ctx, cudaMemsetAsync(mm, 0, 32, s));
-			k_dense_build<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off,
-					R->key_bytes, ht->bcols, ht->inline_val, kmin, ht->dense_val, ht->dense_bits,
-					reinterpret_cast<int*>(mm));
+			int* dupflag_dev = reinterpret_cast<int*>(mm + 4);
+			PG_CUDA(ctx, cudaMemsetAsync(dupflag_dev, 0, 8, s));
+			if (narrow) {
+				if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense32, range * 4))) { delete ht; return rc; }
+				PG_CUDA(ctx, cudaMemsetAsync(ht->dense32, 0xFF, range * 4, s));
+				k_dense32_build<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off,
+						R->key_bytes, ht->bcols, kmin, h[2], ht->dense32, dupflag_dev);
+			} else {
+				const uint64_t words = pg_div_up(range, 32);
+				if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense_val, range * 8))) { delete ht; return rc; }
+				if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense_bits, words * 4))) { delete ht; return rc; }
+				PG_CUDA(ctx, cudaMemsetAsync(ht->dense_bits, 0, words * 4, s));
+				k_dense_build<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off,
+						R->key_bytes, ht->bcols, ht->inline_val, kmin, ht->dense_val, ht->dense_bits, dupflag_dev);
+			}
 			PG_LAUNCHED(ctx);
 			int dupflag = 0;
-			PG_CUDA(ctx, cudaMemcpyAsync(&dupflag, mm, 4, cudaMemcpyDeviceToHost, s));
+			PG_CUDA(ctx, cudaMemcpyAsync(&dupflag, dupflag_dev, 4, cudaMemcpyDeviceToHost, s));
 			PG_CUDA(ctx, cudaStreamSynchronize(s));
 			if (!dupflag) {
-				ht->dense = true; ht->unique = true; ht->dmin = kmin; ht->drange = range;
+				ht->dense = true; ht->unique = true; ht->dmin = kmin; ht->drange = range; ht->vmin = h[2];
 				ht->slots = nullptr; ht->side = nullptr; ht->nside = 0; ht->log2cap = 1; ht->capacity = 0;
 				pg_free_async(ctx, s, mm);
 				*out = ht;
@@ -904,7 +980,8 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 			}
 			pg_free_async(ctx, s, ht->dense_val);
 			pg_free_async(ctx, s, ht->dense_bits);
-			ht->dense_val = nullptr; ht->dense_bits = nullptr;
+			pg_free_async(ctx, s, ht->dense32);
+			ht->dense_val = nullptr; ht->dense_bits = nullptr; ht->dense32 = nullptr;
 		}
 		pg_free_async(ctx, s, mm);
 	}
@@ -955,6 +1032,7 @@ extern "C" int pg_hashtable_free(pg_ctx* ctx, pg_hashtable* ht)
 	pg_free_async(ctx, ht->stream, ht->side);
 	pg_free_async(ctx, ht->stream, ht->dense_val);
 	pg_free_async(ctx, ht->stream, ht->dense_bits);
+	pg_free_async(ctx, ht->stream, ht->dense32);
 	delete ht;
 	return PG_OK;
 }
@@ -994,6 +1072,8 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 	HjProbeTable tb;
 	tb.slots = ht->slots; tb.log2cap = ht->log2cap; tb.side = ht->side; tb.nside = ht->nside;
 	tb.dense_val = ht->dense_val; tb.dense_bits = ht->dense_bits; tb.dmin = ht->dmin; tb.drange = ht->drange;
+	tb.dense32 = ht->dense32; tb.vmin = ht->vmin;
+	const int mode = ht->dense ? (ht->dense32 ? 2 : 1) : 0;
 	const bool fast16 = W == 16 && (koff == 0 || koff == 8) && kbytes == 8 && pc.ow_words == 4 &&
 		(reinterpret_cast<uintptr_t>(S) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
 	if (fast16) {
@@ -1012,8 +1092,8 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 			PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_warp<M, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, psmem)); \
 			k_probe16_warp<M, D><<<pgrid, PW_WARPS * 32, psmem, s>>>(S, n, koff, tb, wsel, sum_w0, sum_words, \
 					M ? out : nullptr, M ? counts : nullptr, M ? acc : acc + 1, M ? -1 : sum_col, ctx->d_status); } while (0)
-			if (materialize) { if (ht->dense) PW_LAUNCH(true, true); else PW_LAUNCH(true, false); }
-			else { if (ht->dense) PW_LAUNCH(false, true); else PW_LAUNCH(false, false); }
+			if (materialize) { if (mode == 2) PW_LAUNCH(true, 2); else if (mode == 1) PW_LAUNCH(true, 1); else PW_LAUNCH(true, 0); }
+			else { if (mode == 2) PW_LAUNCH(false, 2); else if (mode == 1) PW_LAUNCH(false, 1); else PW_LAUNCH(false, 0); }
 #undef PW_LAUNCH
 			PG_LAUNCHED(ctx);
 			if (positional) *positional = materialize;
@@ -1024,8 +1104,8 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 			PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_tma<M, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
 			k_probe16_tma<M, D><<<grid, HJT_THREADS, smem, s>>>(S, n, koff, tb, wsel, sum_w0, sum_words, \
 					M ? out : nullptr, M ? cap : 0, acc, acc + 1, M ? -1 : sum_col, ctx->d_status); } while (0)
-		if (materialize) { if (ht->dense) HJT_LAUNCH(true, true); else HJT_LAUNCH(true, false); }
-		else { if (ht->dense) HJT_LAUNCH(false, true); else HJT_LAUNCH(false, false); }
+		if (materialize) { if (mode == 2) HJT_LAUNCH(true, 2); else if (mode == 1) HJT_LAUNCH(true, 1); else HJT_LAUNCH(true, 0); }
+		else { if (mode == 2) HJT_LAUNCH(false, 2); else if (mode == 1) HJT_LAUNCH(false, 1); else HJT_LAUNCH(false, 0); }
 #undef HJT_LAUNCH
 		PG_LAUNCHED(ctx);
 		return PG_OK;

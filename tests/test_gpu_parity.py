@@ -138,6 +138,18 @@ def test_join_sparse_unique_keys(ctx):
     _join_check(ctx, R, S, proj=(("B", 8, 8), ("P", 0, 8)))
 
 
+def test_join_dense_keys_wide_values(ctx):
+    # Dense keys whose build values span more than 2^32 values take the wide
+    # dense layout (8-byte values + presence bits) instead of 4-byte entries.
+    R = dg.build_relation(40_000, dg.seed_for(19))
+    R[:, 1] = dg.raw_words(dg.seed_for(19), 1, 40_000).view(np.int64)
+    S = dg.probe_uniform(300_000, R, dg.seed_for(20))
+    S[::5, 0] += 100_000                      # misses beyond the key range
+    _join_check(ctx, R, S)
+    R[::3, 0] += 20_000                       # holes inside the key range
+    _join_check(ctx, R, S)
+
+
 def test_join_many_to_many(ctx):
     R = dg.uniform_keys(5000, 700, dg.seed_for(5))
     S = dg.uniform_keys(9000, 900, dg.seed_for(6))
