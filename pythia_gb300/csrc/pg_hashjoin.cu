@@ -605,7 +605,7 @@ k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPro
 #define PW_STAGES 2
 
 template <bool MATERIALIZE, int MODE>
-__global__ void __launch_bounds__(PW_WARPS * 32, MODE != 0 ? 4 : 2)
+__global__ void __launch_bounds__(PW_WARPS * 32, MODE != 0 ? 5 : 2)
 k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb,
 		uint32_t wsel, uint32_t sum_w0, uint32_t sum_words, char* __restrict__ out,
 		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg,
@@ -1086,8 +1086,10 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 		}
 		if (!materialize || (counts && cap >= n)) {
 			const int psmem = PW_WARPS * PW_STAGES * PW_CHUNK * 16;
+			// Dense-table kernels fit five 8-warp CTAs per SM (registers and
+			// shared memory both allow it); hashed ones two.
 			const int pgrid = (int) std::min<uint64_t>(pg_div_up(pg_div_up(n, PW_CHUNK), PW_WARPS),
-					(uint64_t) ctx->sm_count * 4);
+					(uint64_t) ctx->sm_count * (mode != 0 ? 5 : 2));
 #define PW_LAUNCH(M, D) do { \
 			PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_warp<M, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, psmem)); \
 			k_probe16_warp<M, D><<<pgrid, PW_WARPS * 32, psmem, s>>>(S, n, koff, tb, wsel, sum_w0, sum_words, \
