@@ -147,6 +147,22 @@ int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* R_host, const pg_rel* S_host,
 		const pg_col* proj, int nproj, void* out_host, uint64_t out_capacity,
 		int flags, int sum_col, pg_join_result* res);
 
+/* Join count/sum that allocates nothing. No counterpart in the reference: an
+ * addition for callers that may not allocate device memory while a query runs
+ * (a host that owns the device's memory through its own pool, a sandbox with a
+ * fixed budget, a latency-critical path that must not reach the allocator).
+ * Computes pg_hashjoin_build + pg_hashjoin_probe(PG_JOIN_COUNT | PG_JOIN_SUM):
+ * res->n_out = join rows, res->sum = wrapping sum of output column sum_col
+ * (-1: none). The hash table lives in one fixed 16 MiB device array that the
+ * library declares; the build side may hold at most 524288 tuples (PG_ERR_ARG
+ * beyond), and build-side projected columns at most 8 bytes in total. The
+ * first call on a device looks the array up and should precede any stream
+ * capture. Calls share the array (each clears it first), so calls that overlap
+ * on the GPU race. Synchronous: returns after the result is on the host. */
+int pg_hashjoin_agg_noalloc(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
+		const pg_rel* S, const pg_col* proj, int nproj, int sum_col,
+		pg_join_result* res);
+
 /* ---------------------------------------------------------------------- */
 /* Group-by: GenericAggregate::remember + AggregateSum / AggregateCount fold
  * (operators/genericaggregate.cpp:240-487, aggregatesum.cpp:53-107,

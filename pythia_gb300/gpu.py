@@ -50,7 +50,7 @@ SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_st
            "pg_host_free", "pg_h2d", "pg_d2h", "pg_memset", "pg_kernel_launches",
            "pg_hash_buckets", "pg_hash_tuples", "pg_partition", "pg_partition_sort",
            "pg_hashjoin_build", "pg_hashjoin_probe", "pg_hashtable_free", "pg_hashjoin_host",
-           "pg_groupby", "pg_sort_pages", "pg_mpsm_join"]
+           "pg_groupby", "pg_sort_pages", "pg_mpsm_join", "pg_hashjoin_agg_noalloc"]
 
 
 def lib_path():
@@ -92,6 +92,7 @@ def lib():
             "pg_groupby": ([vp, vp, P(Rel), u32, ci, ci, u64, vp, u64, P(u64)], ci),
             "pg_sort_pages": ([vp, vp, P(Rel), vp], ci),
             "pg_mpsm_join": ([vp, vp, P(Rel), P(Rel), P(Col), ci, vp, u64, ci, ci, P(JoinResult)], ci),
+            "pg_hashjoin_agg_noalloc": ([vp, vp, P(Rel), P(Rel), P(Col), ci, ci, P(JoinResult)], ci),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
