@@ -101,6 +101,21 @@ int pg_memset(pg_ctx* ctx, pg_stream stream, void* dst, int value, uint64_t byte
 /* Number of kernels this library has launched (process-wide). */
 uint64_t pg_kernel_launches(void);
 
+/* Launch-shape knobs of a context, set by the autotuner (pythia_gb300/autotune.py).
+ * No reference counterpart: they replace the reference's compile-time and plan
+ * constants that size per-thread work (buffsize, tuplesperbucket, thread counts).
+ * Value 0 restores the built-in choice. Results never depend on them. */
+enum {
+	PG_TUNE_PROBE_CTAS_PER_SM = 0,   /* resident 8-warp CTAs per SM of the 16-byte probe (1..5) */
+	PG_TUNE_PROBE_VARIANT = 1,       /* 1: warp-independent positional, 2: tiled with bulk stores */
+	PG_TUNE_DENSE = 2,               /* 1: allow dense tables (default), 2: always hash */
+	PG_TUNE_PARTITION_TILE = 3,      /* partition tile bytes (8192..65536) */
+	PG_TUNE_GROUPBY_SMEM_GROUPS = 4, /* largest group count aggregated in shared memory first */
+	PG_TUNE_COUNT = 8
+};
+int pg_tune_set(pg_ctx* ctx, int knob, int64_t value);
+int64_t pg_tune_get(pg_ctx* ctx, int knob);
+
 /* ---------------------------------------------------------------------- */
 /* Tuple hashing: TupleHasher::hash over a column (hash.h:85-124) with the
  * bucket functions of hash.h:150-479. out[i] = bucket of tuple i.        */

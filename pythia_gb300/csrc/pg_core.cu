@@ -26,6 +26,20 @@ int pg_cuda_fail(pg_ctx* ctx, cudaError_t e, const char* what)
 
 extern "C" uint64_t pg_kernel_launches(void) { return g_kernel_launches.load(); }
 
+extern "C" int pg_tune_set(pg_ctx* ctx, int knob, int64_t value)
+{
+	if (!ctx || knob < 0 || knob >= PG_TUNE_COUNT || value < 0)
+		return pg_fail(ctx, PG_ERR_ARG, "pg_tune_set: unknown knob or negative value");
+	ctx->tune[knob] = value;
+	return PG_OK;
+}
+
+extern "C" int64_t pg_tune_get(pg_ctx* ctx, int knob)
+{
+	if (!ctx || knob < 0 || knob >= PG_TUNE_COUNT) return -1;
+	return ctx->tune[knob];
+}
+
 extern "C" int pg_init(int device, uint64_t reserved_bytes, pg_ctx** out)
 {
 	if (!out) return pg_fail(nullptr, PG_ERR_ARG, "pg_init: null ctx pointer");
@@ -36,6 +50,7 @@ extern "C" int pg_init(int device, uint64_t reserved_bytes, pg_ctx** out)
 	if (device < 0 || device >= ndev) return pg_fail(nullptr, PG_ERR_ARG, "pg_init: bad device");
 	pg_ctx* ctx = new pg_ctx();
 	ctx->device = device;
+	for (int i = 0; i < PG_TUNE_COUNT; ++i) ctx->tune[i] = 0;
 	if ((e = cudaSetDevice(device)) != cudaSuccess) { delete ctx; return pg_cuda_fail(nullptr, e, "cudaSetDevice"); }
 	cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
 	cudaDeviceGetDefaultMemPool(&ctx->pool, device);

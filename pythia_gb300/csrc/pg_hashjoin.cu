@@ -605,7 +605,7 @@ k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPro
 #define PW_STAGES 2
 
 template <bool MATERIALIZE, int MODE>
-__global__ void __launch_bounds__(PW_WARPS * 32, MODE != 0 ? 5 : 2)
+__global__ void __launch_bounds__(PW_WARPS * 32, MODE != 0 ? 4 : 2)
 k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb,
 		uint32_t wsel, uint32_t sum_w0, uint32_t sum_words, char* __restrict__ out,
 		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg,
@@ -933,7 +933,7 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 		}
 	ht->inline_val = bbytes <= 8;
 	ht->dense = false; ht->dense_val = nullptr; ht->dense_bits = nullptr; ht->dense32 = nullptr; ht->vmin = 0;
-	if (R->n && ht->inline_val) {
+	if (R->n && ht->inline_val && ctx->tune[PG_TUNE_DENSE] != 2) {
 		// Dense key domain (unique keys spanning at most 2|R| values, e.g. a
 		// surrogate primary key 1..N): index by key - min, no hashing. Only
 		// for packed values: the unique-key probe kernels read them inline.
@@ -1084,12 +1084,16 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 			for (int q = 0; q < pc.words[c]; ++q, ++o)
 				wsel |= (pc.side[c] ? (pc.src[c] + q) : (4u + pc.src[c] + q)) << (4 * o);
 		}
-		if (!materialize || (counts && cap >= n)) {
+		const bool tiled = ctx->tune[PG_TUNE_PROBE_VARIANT] == 2;
+		if (!materialize || (counts && cap >= n && !tiled)) {
 			const int psmem = PW_WARPS * PW_STAGES * PW_CHUNK * 16;
-			// Dense-table kernels fit five 8-warp CTAs per SM (registers and
-			// shared memory both allow it); hashed ones two.
+			// Persistent grid: CTAs per SM from the tuning table, else 4 for
+			// dense tables (more resident warps evict table lines from L2
+			// faster than they hide latency) and 2 for hashed ones.
+			const int64_t per_sm = ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] > 0
+				? std::min<int64_t>(5, ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM]) : (mode != 0 ? 4 : 2);
 			const int pgrid = (int) std::min<uint64_t>(pg_div_up(pg_div_up(n, PW_CHUNK), PW_WARPS),
-					(uint64_t) ctx->sm_count * (mode != 0 ? 5 : 2));
+					(uint64_t) ctx->sm_count * per_sm);
 #define PW_LAUNCH(M, D) do { \
 			PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_warp<M, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, psmem)); \
 			k_probe16_warp<M, D><<<pgrid, PW_WARPS * 32, psmem, s>>>(S, n, koff, tb, wsel, sum_w0, sum_words, \

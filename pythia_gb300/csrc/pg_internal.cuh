@@ -13,6 +13,7 @@
 struct pg_ctx {
 	int device;
 	int sm_count;
+	int64_t tune[PG_TUNE_COUNT];   // launch-shape knobs, PG_TUNE_* (0 = built-in choice)
 	cudaMemPool_t pool;
 	int* d_status;          // sticky device error word (PG_ERR_*), 0 = fine
 	unsigned long long* d_scratch64;  // small per-context device scratch (counters)

@@ -50,7 +50,10 @@ SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_st
            "pg_host_free", "pg_h2d", "pg_d2h", "pg_memset", "pg_kernel_launches",
            "pg_hash_buckets", "pg_hash_tuples", "pg_partition", "pg_partition_sort",
            "pg_hashjoin_build", "pg_hashjoin_probe", "pg_hashtable_free", "pg_hashjoin_host",
-           "pg_groupby", "pg_sort_pages", "pg_mpsm_join", "pg_hashjoin_agg_noalloc"]
+           "pg_groupby", "pg_sort_pages", "pg_mpsm_join", "pg_hashjoin_agg_noalloc",
+           "pg_tune_set", "pg_tune_get"]
+TUNE = {"probe_ctas_per_sm": 0, "probe_variant": 1, "dense": 2, "partition_tile": 3,
+        "groupby_smem_groups": 4}
 
 
 def lib_path():
@@ -93,6 +96,8 @@ def lib():
             "pg_sort_pages": ([vp, vp, P(Rel), vp], ci),
             "pg_mpsm_join": ([vp, vp, P(Rel), P(Rel), P(Col), ci, vp, u64, ci, ci, P(JoinResult)], ci),
             "pg_hashjoin_agg_noalloc": ([vp, vp, P(Rel), P(Rel), P(Col), ci, ci, P(JoinResult)], ci),
+            "pg_tune_set": ([vp, ci, ctypes.c_int64], ci),
+            "pg_tune_get": ([vp, ci], ctypes.c_int64),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -176,6 +181,11 @@ class Context:
 
     def sync(self):
         self._check(lib().pg_sync(self.h, self.stream))
+
+    def tune(self, **knobs):
+        """Sets launch-shape knobs (see PG_TUNE_* in include/pythia_gpu.h)."""
+        for k, v in knobs.items():
+            self._check(lib().pg_tune_set(self.h, TUNE[k], int(v)))
 
     @staticmethod
     def rel(buf, n, width, key_off=0, key_bytes=8):
