@@ -348,6 +348,205 @@ def run_gpu(args, ws, rank, local):
     ctx.close()
 
 
+# ---------------------------------------------------------------------------
+# Other operators of the path (bench.py --op ...): one JSON line each, same
+# keys as the headline. Sizes are the configurations' full sizes.
+# ---------------------------------------------------------------------------
+OPS = {
+    "partition": dict(n=1 << 28, metric="partition tuples/s (256M int64 tuples, 256-way radix, stable)",
+                      workload="radix partition of 256M 16-byte tuples on the low 8 key bits (parammodulo)"),
+    "groupby": dict(n=1 << 28, metric="group-by rows/s (256M rows, 1M groups, compensated FP64 sum)",
+                    workload="aggregate_sum over (long key U[0,1M), dec value U[0,1e4)), 256M rows"),
+    "sort": dict(n=1 << 26, metric="page sort tuples/s (64M int64-keyed 16-byte tuples)",
+                 workload="page sort of 64M (long key U[0,16M), long payload) tuples"),
+    "mpsm": dict(n=1 << 26, metric="MPSM join tuples/s (64M x 64M, keys U[0,16M), fused count+sum)",
+                 workload="sort-merge join of two 64M-tuple relations, keys U[0,16M) (~4 duplicates per side)"),
+}
+
+
+def _pinned_array(ctx, L, n, cols=2):
+    p = ctypes.c_void_p()
+    ctx._check(L.pg_host_alloc(ctx.h, n * 8 * cols, ctypes.byref(p)))
+    return p.value, np.ctypeslib.as_array((ctypes.c_int64 * (n * cols)).from_address(p.value)).reshape(n, cols)
+
+
+def _op_inputs(op, n, threads):
+    from pythia_gb300 import datagen as dg
+    if op == "partition":
+        return [dg.uniform_keys(n, 1 << 40, dg.seed_for(111), threads=threads)]
+    if op == "groupby":
+        return [dg.groupby_rows(n, 1 << 20, 1e4, dg.seed_for(112), threads=threads)]
+    if op == "sort":
+        return [dg.uniform_keys(n, 1 << 24, dg.seed_for(113), threads=threads)]
+    return [dg.uniform_keys(n, 1 << 24, dg.seed_for(114), threads=threads),
+            dg.uniform_keys(n, 1 << 24, dg.seed_for(115), threads=threads)]
+
+
+def _op_parity(op, ins, out, extra):
+    """Size-independent checks at full size (integer ones exact)."""
+    if op == "partition":
+        keys = ins[0][:, 0]
+        hist = np.bincount((keys & 255).astype(np.int64), minlength=256).astype(np.uint64)
+        offs = extra
+        ok = np.array_equal(np.diff(offs), hist)
+        o = out.reshape(-1, 2)
+        for b in (0, 17, 255):
+            part = o[int(offs[b]):int(offs[b + 1]), 0]
+            ok &= bool(np.all((part & 255) == b))
+        ok &= int(o.astype(np.uint64).sum(dtype=np.uint64)) == int(ins[0].astype(np.uint64).sum(dtype=np.uint64))
+        return {"offsets_equal_histogram": bool(ok)}
+    if op == "groupby":
+        rows = ins[0]
+        from oracle import oracle as orc
+        g = out.view(np.int64).reshape(-1, 2)
+        ngroups_ok = g.shape[0] == int((np.bincount(rows[:, 0], minlength=1 << 20) > 0).sum())
+        total = orc.fsum(rows[:, 1].view(np.float64))
+        got_total = orc.fsum(g[:, 1].view(np.float64))
+        rng = np.random.default_rng(7)
+        pick = rng.choice(1 << 20, 16, replace=False)
+        sel = np.isin(rows[:, 0], pick)
+        sub = rows[sel]
+        d = {int(k): float(v) for k, v in zip(g[:, 0], g[:, 1].view(np.float64))}
+        worst = 0.0
+        for k in pick:
+            ex = orc.fsum(sub[sub[:, 0] == k, 1].view(np.float64))
+            worst = max(worst, abs(d[int(k)] - ex) / abs(ex))
+        return {"groups_ok": bool(ngroups_ok), "total_rel_err": abs(got_total - total) / total,
+                "sampled_group_max_rel_err": worst, "tolerance": 1e-12,
+                "ok": bool(ngroups_ok and worst <= 1e-12)}
+    if op == "sort":
+        o = out.reshape(-1, 2)
+        ok = bool(np.all(np.diff(o[:, 0]) >= 0))
+        ok &= int(o.astype(np.uint64).sum(dtype=np.uint64)) == int(ins[0].astype(np.uint64).sum(dtype=np.uint64))
+        return {"sorted_and_same_multiset_checksum": ok}
+    R, S = ins
+    cr = np.bincount(R[:, 0], minlength=1 << 24).astype(np.int64)
+    cs = np.bincount(S[:, 0], minlength=1 << 24).astype(np.int64)
+    pr = np.bincount(R[:, 0], weights=R[:, 1].astype(np.float64), minlength=1 << 24).astype(np.int64)
+    count = int((cr * cs).sum())
+    sum_build = int((pr * cs).astype(np.uint64).sum(dtype=np.uint64).astype(np.int64))
+    return {"count_ok": extra[0] == count, "build_payload_sum_ok": extra[1] == sum_build,
+            "count": count}
+
+
+def run_op(args, ws, rank, local, op):
+    import torch
+    from pythia_gb300 import gpu
+    torch.cuda.set_device(local)
+    spec = OPS[op]
+    n = spec["n"] >> args.scale_down
+    threads = host_threads()
+    ctx = gpu.Context(local)
+    L = gpu.lib()
+    ins = _op_inputs(op, n, threads)
+    d_in = [ctx.upload(a) for a in ins]
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    c, nc = gpu.cols((("P", 8, 8), ("B", 8, 8)))
+    out_bytes = {"partition": n * 16, "groupby": (1 << 20) * 16 + 16, "sort": n * 16, "mpsm": 16}[op]
+    d_out = ctx.alloc(out_bytes)
+    offs = ctx.alloc(8 * 257)
+    ng = ctypes.c_uint64()
+    res = gpu.JoinResult()
+    rel = [gpu.Rel(d.ptr, n, 16, 0, 8) for d in d_in]
+
+    def step():
+        if op == "partition":
+            cfg = gpu.hashcfg("parammodulo", 256)
+            ctx._check(L.pg_partition(ctx.h, ctx.stream, ctypes.byref(rel[0]), ctypes.byref(cfg), d_out.ptr, offs.ptr))
+        elif op == "groupby":
+            ctx._check(L.pg_groupby(ctx.h, ctx.stream, ctypes.byref(rel[0]), 8, 2, 0, 1 << 20, d_out.ptr,
+                                    1 << 20, ctypes.byref(ng)))
+        elif op == "sort":
+            ctx._check(L.pg_sort_pages(ctx.h, ctx.stream, ctypes.byref(rel[0]), d_out.ptr))
+        else:
+            ctx._check(L.pg_mpsm_join(ctx.h, ctx.stream, ctypes.byref(rel[0]), ctypes.byref(rel[1]), c, nc,
+                                      None, 0, gpu.JOIN_COUNT | gpu.JOIN_SUM, 1, ctypes.byref(res)))
+
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+    k0 = gpu.kernel_launches()
+    clocks = Clocks(local)
+    barrier(ws)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    clk = clocks.stop()
+    launches = gpu.kernel_launches() - k0
+    ms = max_over_ranks(ws, e0.elapsed_time(e1) / args.steps)
+    units = 2 * n if op == "mpsm" else n
+    value = ws * units / (ms / 1e3)
+    alg = {"partition": 32 * n, "groupby": 16 * n + 16 * (1 << 20), "sort": 32 * n, "mpsm": 16 * 2 * n}[op]
+    peak, peak_kind = measured_peak()
+    achieved = alg / (ms / 1e3) / 1e9
+    # Parity at full size.
+    if op == "partition":
+        out = ctx.download(d_out, n * 16).view(np.int64)
+        parity = _op_parity(op, ins, out, ctx.download(offs, 8 * 257, np.uint64))
+    elif op == "groupby":
+        parity = _op_parity(op, ins, ctx.download(d_out, ng.value * 16), None)
+    elif op == "sort":
+        parity = _op_parity(op, ins, ctx.download(d_out, n * 16).view(np.int64), None)
+    else:
+        parity = _op_parity(op, ins, None, (res.n_out, res.sum))
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_op_sample(op, ins, threads)
+    if rank == 0:
+        line = {"metric": spec["metric"], "value": value, "unit": "tuples/s", "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "int64" if op != "groupby" else "f64",
+                "data": "synthetic (seeded generator, resident in HBM)",
+                "config": {"workload": spec["workload"], "op": op, "tuples": n,
+                           "l2": "inputs larger than L2; no flush"},
+                "parity": parity,
+                "roofline": {"bound": "hbm", "kernel": f"pg_{op} (whole operator)", "achieved": achieved,
+                             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                             "peak_source": peak_kind, "algorithmic_bytes": alg},
+                "gpu_launches": int(launches), "clocks": clk}
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def cpu_op_sample(op, ins, threads):
+    """Times the oracle port of the reference operator on a bounded sample and
+    scales linearly in tuples (n log n for the sort) to the full size."""
+    from oracle import oracle as orc
+    n = ins[0].shape[0]
+    m = min(n, 1 << 24)
+    a = np.ascontiguousarray(ins[0][:m])
+    t0 = time.perf_counter()
+    if op == "partition":
+        orc.partition(a, orc.hashcfg("parammodulo", 256), threads=threads)
+        scale, kind = n / m, "linear"
+    elif op == "groupby":
+        orc.groupby(a, val=(8, "dec"), agg="sum", hash=orc.hashcfg("modulo", 1 << 20), threads=threads)
+        scale, kind = n / m, "linear"
+    elif op == "sort":
+        m = min(n, 1 << 22)
+        a = np.ascontiguousarray(ins[0][:m])
+        t0 = time.perf_counter()
+        orc.sort(a)
+        scale, kind = (n * np.log2(n)) / (m * np.log2(m)), "n log n"
+    else:
+        m = min(n, 1 << 22)
+        R = np.ascontiguousarray(ins[0][:m]); S = np.ascontiguousarray(ins[1][:m])
+        R[:, 0] >>= 4; S[:, 0] >>= 4      # same ~4 duplicates per key at 1/16 of the size
+        t0 = time.perf_counter()
+        orc.mergejoin(R, S, materialise=False, sum_col=1, threads=threads)
+        scale, kind = n / m, "linear"
+    t = (time.perf_counter() - t0) * scale
+    units = 2 * n if op == "mpsm" else n
+    return {"value": units / t, "unit": "tuples/s", "cores": threads if op != "sort" else 1,
+            "kind": "port", "sample": f"{m} tuples (oracle port), time scaled {kind} to {n}"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -359,6 +558,8 @@ def main():
     ap.add_argument("--key-domain", default="dense", choices=["dense", "sparse"],
                     help="dense: keys 1..|R| (direct-mapped table); sparse: the same keys "
                          "multiplied by an odd constant (hashed table)")
+    ap.add_argument("--op", default="hashjoin", choices=["hashjoin"] + sorted(OPS))
+    ap.add_argument("--scale-down", type=int, default=0, help="divide --op sizes by 2^k")
     ap.add_argument("--build-log2", type=int, default=24)
     ap.add_argument("--probe-log2", type=int, default=28)
     args = ap.parse_args()
@@ -367,6 +568,8 @@ def main():
     ws, rank, local = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, ws, rank)
+    elif args.op != "hashjoin":
+        run_op(args, ws, rank, local, args.op)
     else:
         run_gpu(args, ws, rank, local)
     if ws > 1:
