@@ -179,6 +179,97 @@ k_gb_insert(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, 
 	}
 }
 
+// Global-table insert with four independent rows per thread per iteration:
+// their key loads, slot reads and accumulator atomics are issued together, so
+// the chains of dependent L2 round trips overlap instead of running one row
+// at a time.
+#define GB_ILP 4
+template <int VT, int AGG>
+__global__ void __launch_bounds__(GB_THREADS)
+k_gb_insert_ilp(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes,
+		uint32_t voff, GbTable t, int* __restrict__ status)
+{
+	const int lane = threadIdx.x & 31;
+	const uint64_t cap = 1ull << t.log2cap, mask = cap - 1;
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	const uint64_t step = stride * GB_ILP;
+	bool full = false;
+	for (uint64_t base = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; base < pg_div_up(n, 32) * 32;
+			base += step) {
+		int64_t k[GB_ILP];
+		unsigned long long iv[GB_ILP];
+		double dv[GB_ILP], dc[GB_ILP];
+		bool lead[GB_ILP];
+		#pragma unroll
+		for (int j = 0; j < GB_ILP; ++j) {
+			const uint64_t i = base + j * stride;
+			const bool valid = i < n;
+			k[j] = 0; iv[j] = 0; dv[j] = 0.0; dc[j] = 0.0; lead[j] = false;
+			if (valid) {
+				const char* r = in + i * W;
+				k[j] = pg_load_key(r + koff, kbytes);
+				if (AGG == PG_AGG_COUNT) iv[j] = 1;
+				else if (VT == PG_VAL_INT) iv[j] = (unsigned long long) (long long) *reinterpret_cast<const int32_t*>(r + voff);
+				else if (VT == PG_VAL_LONG) iv[j] = (unsigned long long) pg_load_key(r + voff, 8);
+				else dv[j] = __longlong_as_double(pg_load_key(r + voff, 8));
+			}
+			const uint32_t active = __ballot_sync(0xffffffffu, valid);
+			if (valid) {
+				const uint32_t peers = __match_any_sync(active, (unsigned long long) k[j]);
+				warp_combine<VT, AGG>(peers, lane, iv[j], dv[j], dc[j]);
+				lead[j] = lane == __ffs(peers) - 1;
+			}
+		}
+		uint64_t slot[GB_ILP];
+		unsigned long long cur[GB_ILP];
+		#pragma unroll
+		for (int j = 0; j < GB_ILP; ++j) {
+			if (!lead[j]) continue;
+			if (k[j] == PG_EMPTY_KEY) { slot[j] = cap; cur[j] = 0; continue; }
+			slot[j] = pg_mix64((uint64_t) k[j]) >> (64 - t.log2cap);
+			cur[j] = t.keys[slot[j]];
+		}
+		#pragma unroll
+		for (int j = 0; j < GB_ILP; ++j) {
+			if (!lead[j]) continue;
+			if (slot[j] == cap) { if (!*t.sentinel_used) atomicExch(t.sentinel_used, 1); continue; }
+			uint64_t probe = 0;
+			for (; probe < cap; ++probe) {
+				if (cur[j] == (unsigned long long) k[j]) break;
+				if (cur[j] == (unsigned long long) PG_EMPTY_KEY) {
+					const unsigned long long old = atomicCAS(&t.keys[slot[j]], (unsigned long long) PG_EMPTY_KEY,
+							(unsigned long long) k[j]);
+					if (old == (unsigned long long) PG_EMPTY_KEY || old == (unsigned long long) k[j]) break;
+					cur[j] = old;
+					continue;
+				}
+				slot[j] = (slot[j] + 1) & mask;
+				cur[j] = t.keys[slot[j]];
+			}
+			if (probe == cap) { full = true; lead[j] = false; }
+		}
+		if (VT == PG_VAL_DEC && AGG == PG_AGG_SUM) {
+			double old[GB_ILP];
+			#pragma unroll
+			for (int j = 0; j < GB_ILP; ++j)
+				if (lead[j]) old[j] = atomicAdd(reinterpret_cast<double*>(&t.acc[slot[j]]), dv[j]);
+			#pragma unroll
+			for (int j = 0; j < GB_ILP; ++j) {
+				if (!lead[j]) continue;
+				double sres, e;
+				two_sum(old[j], dv[j], sres, e);
+				e += dc[j];
+				if (e != 0.0) atomicAdd(&t.lo[slot[j]], e);
+			}
+		} else {
+			#pragma unroll
+			for (int j = 0; j < GB_ILP; ++j)
+				if (lead[j]) fold_slot<VT, AGG>(t.acc, t.lo, slot[j], iv[j], 0.0, 0.0);
+		}
+	}
+	if (full) pg_set_status(status, PG_ERR_TABLE_FULL);
+}
+
 template <int VT, int AGG, bool HASKEY>
 __global__ void k_gb_emit(GbTable t, uint32_t kbytes, char* __restrict__ out, uint64_t cap_rows,
 		unsigned long long* __restrict__ cursor, uint64_t nonkey_rows)
@@ -260,7 +351,10 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 					k_gb_insert<VT, AGG, HK, SM><<<blocks, GB_THREADS, smem_bytes, s>>>( \
 					(const char*) in->data, in->n, in->width, in->key_off, in->key_bytes, voff, t, slg, ctx->d_status)
 			if (haskey && smem) { GB_LAUNCH(true, true); }
-			else if (haskey) { GB_LAUNCH(true, false); }
+			else if (haskey) {
+				k_gb_insert_ilp<VT, AGG><<<blocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n,
+						in->width, in->key_off, in->key_bytes, voff, t, ctx->d_status);
+			}
 			else { GB_LAUNCH(false, true); }
 			#undef GB_LAUNCH
 			PG_LAUNCHED(ctx);

@@ -59,6 +59,10 @@ struct pg_hashfn {
 };
 
 int pg_hashfn_derive(const pg_hashcfg* c, pg_hashfn* f);
+// Stable partition by a derived bucket function (pg_partition.cu); offsets may
+// be null. Queues work on `s` without synchronising.
+int pg_partition_fn(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, const pg_hashfn& f,
+		void* out, uint64_t* offsets);
 
 // Key columns are 4-byte aligned (column offsets and tuple widths are
 // multiples of 4); an 8-byte key may straddle an 8-byte boundary.

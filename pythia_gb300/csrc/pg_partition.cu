@@ -260,6 +260,16 @@ extern "C" int pg_partition(pg_ctx* ctx, pg_stream stream, const pg_rel* in,
 	if (!ctx || !in || !cfg || !offsets) return pg_fail(ctx, PG_ERR_ARG, "pg_partition: null argument");
 	pg_hashfn f;
 	if (pg_hashfn_derive(cfg, &f)) return pg_fail(ctx, PG_ERR_ARG, "pg_partition: invalid hash configuration");
+	int rc = pg_partition_fn(ctx, (cudaStream_t) stream, in, f, out, offsets);
+	if (rc) return rc;
+	return pg_check_status(ctx, (cudaStream_t) stream, "pg_partition");
+}
+
+// Partition by an already derived bucket function; offsets may be null. Does
+// not synchronise (the radix sort chains passes on the stream).
+int pg_partition_fn(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, const pg_hashfn& f,
+		void* out, uint64_t* offsets)
+{
 	const uint32_t B = f.nbuckets, W = in->width;
 	if (B == 0 || B > PART_MAX_BUCKETS)
 		return pg_fail(ctx, PG_ERR_UNSUPPORTED, "pg_partition: at most 4096 buckets in one pass");
@@ -268,14 +278,14 @@ extern "C" int pg_partition(pg_ctx* ctx, pg_stream stream, const pg_rel* in,
 	if (in->key_off + in->key_bytes > W || (in->key_bytes != 4 && in->key_bytes != 8))
 		return pg_fail(ctx, PG_ERR_ARG, "pg_partition: key must be a 4- or 8-byte column inside the tuple");
 	if (in->n >= (1ull << 32)) return pg_fail(ctx, PG_ERR_UNSUPPORTED, "pg_partition: at most 2^32-1 tuples");
-	cudaStream_t s = (cudaStream_t) stream;
 	const uint64_t n = in->n;
 	if (n == 0) {
-		PG_CUDA(ctx, cudaMemsetAsync(offsets, 0, (B + 1) * sizeof(uint64_t), s));
+		if (offsets) PG_CUDA(ctx, cudaMemsetAsync(offsets, 0, (B + 1) * sizeof(uint64_t), s));
 		return PG_OK;
 	}
 	const int NW = B <= 1024 ? 8 : 4;
-	uint32_t tile = PART_TILE_BYTES / W;
+	const int64_t tb = ctx->tune[PG_TUNE_PARTITION_TILE];
+	uint32_t tile = (uint32_t) (tb > 0 ? std::min<int64_t>(65536, std::max<int64_t>(8192, tb)) : PART_TILE_BYTES) / W;
 	tile = std::max<uint32_t>(NW * 32, tile / (NW * 32) * (NW * 32));
 	const uint64_t ntiles = pg_div_up(n, tile);
 	const size_t smem = part_smem_bytes(tile, W, B, NW);
@@ -305,9 +315,11 @@ extern "C" int pg_partition(pg_ctx* ctx, pg_stream stream, const pg_rel* in,
 	PG_LAUNCHED(ctx);
 	// offsets[b] = first slot of bucket b = scanned count of (b, CTA 0).
 	// Strided copy: counts[b*G] for b < B, then n.
-	PG_CUDA(ctx, cudaMemcpy2DAsync(offsets, sizeof(uint64_t), counts, G * sizeof(uint64_t),
-			sizeof(uint64_t), B, cudaMemcpyDeviceToDevice, s));
-	PG_CUDA(ctx, cudaMemcpyAsync(offsets + B, &in->n, sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+	if (offsets) {
+		PG_CUDA(ctx, cudaMemcpy2DAsync(offsets, sizeof(uint64_t), counts, G * sizeof(uint64_t),
+				sizeof(uint64_t), B, cudaMemcpyDeviceToDevice, s));
+		PG_CUDA(ctx, cudaMemcpyAsync(offsets + B, &in->n, sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+	}
 	pg_free_async(ctx, s, counts);
-	return pg_check_status(ctx, s, "pg_partition");
+	return PG_OK;
 }

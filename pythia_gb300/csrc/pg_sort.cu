@@ -10,7 +10,8 @@
 // merge passes, each CTA producing 2048 outputs of a run pair located by a
 // merge-path binary search (Odeh et al., "Merge Path", 2012).
 //
-// Tuples travel as 16-byte records {int64 key, uint64 val}. A 16-byte tuple
+// Keys spanning at most 2^32 values take an LSD radix path instead (see
+// radix_sort below). Tuples travel as 16-byte records {int64 key, uint64 val}. A 16-byte tuple
 // with an 8-byte key is its own record (the key half first); any other layout
 // sorts (widened key, row index) records and gathers rows at the end. Ties are
 // left in unspecified order, as std::sort leaves them. Unlike the reference's
@@ -163,6 +164,98 @@ __global__ void k_records_to_tuples(const pg_rec* __restrict__ rec, uint64_t n, 
 	}
 }
 
+// ---------------------------------------------------------------------------
+// LSD radix path: when the keys span at most 2^32 values, ceil(bits/8) stable
+// 256-way partitions on successive 8-bit digits of (key - min) sort the
+// tuples (pg_partition.cu; each pass reads and writes the relation once). This
+// is ParameterizedModuloValueHasher::generate's multi-pass radix split
+// (hash.cpp:237-267) driven to completion. Ties keep input order.
+// ---------------------------------------------------------------------------
+__global__ void k_sort_minmax(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff,
+		uint32_t kbytes, unsigned long long* __restrict__ mm)
+{
+	unsigned long long lo = ~0ull, hi = 0;
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+			i += (uint64_t) gridDim.x * blockDim.x) {
+		const unsigned long long u = (unsigned long long) pg_load_key(in + i * W + koff, kbytes) ^ (1ull << 63);
+		lo = u < lo ? u : lo;
+		hi = u > hi ? u : hi;
+	}
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		const unsigned long long a = __shfl_down_sync(0xffffffffu, lo, o), b = __shfl_down_sync(0xffffffffu, hi, o);
+		lo = a < lo ? a : lo;
+		hi = b > hi ? b : hi;
+	}
+	if ((threadIdx.x & 31) == 0) { atomicMin(&mm[0], lo); atomicMax(&mm[1], hi); }
+}
+
+// (key, other half) or (key, row index) records for layouts other than a
+// 16-byte tuple keyed at offset 0.
+__global__ void k_make_records(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff,
+		uint32_t kbytes, int mode, pg_rec* __restrict__ out)
+{
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
+			i += (uint64_t) gridDim.x * blockDim.x) {
+		pg_rec r;
+		if (mode == 1) {
+			const pg_rec t = reinterpret_cast<const pg_rec*>(in)[i];
+			r.key = (long long) t.val; r.val = (unsigned long long) t.key;
+		} else {
+			r.key = pg_load_key(in + i * W + koff, kbytes);
+			r.val = i;
+		}
+		out[i] = r;
+	}
+}
+
+// Sorts `in` into `out` by radix passes when the key span allows; returns
+// PG_OK with *done = false (nothing queued) when it does not. `tmp` holds n
+// tuples of scratch.
+static int radix_sort(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, void* out, void* tmp, bool* done)
+{
+	*done = false;
+	const uint64_t n = in->n;
+	if (n == 0 || n >= (1ull << 32)) return PG_OK;
+	int rc;
+	unsigned long long* mm = nullptr;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 16))) return rc;
+	const unsigned long long init[2] = {~0ull, 0ull};
+	PG_CUDA(ctx, cudaMemcpyAsync(mm, init, 16, cudaMemcpyHostToDevice, s));
+	const int blocks = (int) std::min<uint64_t>(pg_div_up(n, 256), (uint64_t) ctx->sm_count * 8);
+	k_sort_minmax<<<blocks, 256, 0, s>>>((const char*) in->data, n, in->width, in->key_off, in->key_bytes, mm);
+	PG_LAUNCHED(ctx);
+	unsigned long long h[2];
+	PG_CUDA(ctx, cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, s));
+	PG_CUDA(ctx, cudaStreamSynchronize(s));
+	pg_free_async(ctx, s, mm);
+	const unsigned long long span = h[1] - h[0];
+	const int bits = span == 0 ? 0 : 64 - __builtin_clzll(span);
+	if (bits > 32) return PG_OK;
+	const long long kmin = (long long) (h[0] ^ (1ull << 63));
+	if (bits == 0) {   // one key value: already sorted
+		PG_CUDA(ctx, cudaMemcpyAsync(out, in->data, n * in->width, cudaMemcpyDeviceToDevice, s));
+		*done = true;
+		return PG_OK;
+	}
+	const int passes = (bits + 7) / 8;
+	pg_rel cur = *in;
+	for (int p = 0; p < passes; ++p) {
+		pg_hashfn f;
+		f.fn = PG_FN_PARAMMODULO;
+		f.skipbits = 8 * p;
+		f.k = (int64_t) 255 << f.skipbits;
+		f.min = kmin;
+		f.max = 0; f.bucketrange = 0;
+		f.nbuckets = 256;
+		void* dst = ((passes - 1 - p) % 2 == 0) ? out : tmp;
+		if ((rc = pg_partition_fn(ctx, s, &cur, f, dst, nullptr))) return rc;
+		cur.data = dst;
+	}
+	*done = true;
+	return PG_OK;
+}
+
 int pg_sort_mode(const pg_rel* r)
 {
 	if (r->width == 16 && r->key_bytes == 8 && r->key_off == 0) return 0;
@@ -180,6 +273,27 @@ int pg_sort_records(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, pg_rec** recs
 	pg_rec *a = nullptr, *b = nullptr;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &a, n * sizeof(pg_rec)))) return rc;
 	if (n == 0) { *recs = a; return PG_OK; }
+	{
+		// Radix path: sort 16-byte records (the tuples themselves when the
+		// layout is a 16-byte tuple keyed at 0).
+		pg_rec* src = nullptr;
+		pg_rel r = *in;
+		if (mode != 0) {
+			if ((rc = pg_alloc_async(ctx, s, (void**) &src, n * sizeof(pg_rec)))) return rc;
+			const int blocks = (int) std::min<uint64_t>(pg_div_up(n, 256), (uint64_t) ctx->sm_count * 16);
+			k_make_records<<<blocks, 256, 0, s>>>((const char*) in->data, n, in->width, in->key_off,
+					in->key_bytes, mode, src);
+			PG_LAUNCHED(ctx);
+			r.data = src; r.width = 16; r.key_off = 0; r.key_bytes = 8;
+		}
+		if ((rc = pg_alloc_async(ctx, s, (void**) &b, n * sizeof(pg_rec)))) return rc;
+		bool done = false;
+		if ((rc = radix_sort(ctx, s, &r, a, b, &done))) return rc;
+		pg_free_async(ctx, s, b);
+		b = nullptr;
+		if (src) pg_free_async(ctx, s, src);
+		if (done) { *recs = a; return PG_OK; }
+	}
 	const uint64_t tiles = pg_div_up(n, TS_TILE);
 	const size_t smem = TS_TILE * (sizeof(pg_rec) + 8 + 2);
 	PG_CUDA(ctx, cudaFuncSetAttribute(k_tile_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
@@ -213,6 +327,15 @@ extern "C" int pg_sort_pages(pg_ctx* ctx, pg_stream stream, const pg_rel* in, vo
 	if (in->n == 0) return PG_OK;
 	pg_rec* recs = nullptr;
 	int rc;
+	{
+		void* tmp = nullptr;
+		if ((rc = pg_alloc_async(ctx, s, &tmp, in->n * in->width))) return rc;
+		bool done = false;
+		rc = radix_sort(ctx, s, in, out, tmp, &done);
+		pg_free_async(ctx, s, tmp);
+		if (rc) return rc;
+		if (done) return pg_check_status(ctx, s, "pg_sort_pages");
+	}
 	if ((rc = pg_sort_records(ctx, s, in, &recs))) return rc;
 	const int mode = pg_sort_mode(in);
 	int blocks = (int) std::min<uint64_t>(pg_div_up(in->n, 256), (uint64_t) ctx->sm_count * 16);
