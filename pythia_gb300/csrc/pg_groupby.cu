@@ -270,6 +270,129 @@ k_gb_insert_ilp(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t ko
 	if (full) pg_set_status(status, PG_ERR_TABLE_FULL);
 }
 
+// ---------------------------------------------------------------------------
+// High-cardinality path: rows are first radix-partitioned on the top bits of
+// the key mix (PG_FN_MIXRADIX) so that each partition holds about 1K groups;
+// then one CTA per partition aggregates it in a shared-memory table with the
+// same compensated atomics, on shared instead of L2 atomics, and writes its
+// groups out. A partition whose groups overflow the shared table sends the
+// excess keys to the global table (emitted afterwards).
+// ---------------------------------------------------------------------------
+#define GBP_LOG2 12
+#define GBP_SLOTS (1u << GBP_LOG2)
+#define GBP_THREADS 512
+
+// Slot of key k in a per-partition table: low bits of the mix (the top bits
+// are the partition number).
+__device__ __forceinline__ uint32_t gbp_slot(unsigned long long* keys, int64_t k, int* sentinel)
+{
+	if (k == PG_EMPTY_KEY) { if (!*sentinel) atomicExch(sentinel, 1); return GBP_SLOTS; }
+	uint32_t s = (uint32_t) (pg_mix64((uint64_t) k) & (GBP_SLOTS - 1));
+	for (uint32_t probe = 0; probe < GBP_SLOTS; ++probe) {
+		const unsigned long long cur = keys[s];
+		if (cur == (unsigned long long) k) return s;
+		if (cur == (unsigned long long) PG_EMPTY_KEY) {
+			const unsigned long long old = atomicCAS(&keys[s], (unsigned long long) PG_EMPTY_KEY, (unsigned long long) k);
+			if (old == (unsigned long long) PG_EMPTY_KEY || old == (unsigned long long) k) return s;
+		}
+		s = (s + 1) & (GBP_SLOTS - 1);
+	}
+	return UINT32_MAX;
+}
+
+template <int VT, int AGG>
+__device__ __forceinline__ void gb_write_row(char* o, uint32_t kbytes, int64_t k, unsigned long long a, double lo)
+{
+	if (kbytes == 4) *reinterpret_cast<int32_t*>(o) = (int32_t) k;
+	else { reinterpret_cast<uint32_t*>(o)[0] = (uint32_t) k; reinterpret_cast<uint32_t*>(o)[1] = (uint32_t) ((uint64_t) k >> 32); }
+	o += kbytes;
+	if (AGG == PG_AGG_SUM && VT == PG_VAL_INT) { *reinterpret_cast<uint32_t*>(o) = (uint32_t) a; return; }
+	if (VT == PG_VAL_DEC && AGG == PG_AGG_SUM)
+		a = (unsigned long long) __double_as_longlong(__longlong_as_double((long long) a) + lo);
+	reinterpret_cast<uint32_t*>(o)[0] = (uint32_t) a;
+	reinterpret_cast<uint32_t*>(o)[1] = (uint32_t) (a >> 32);
+}
+
+template <int VT, int AGG>
+__global__ void __launch_bounds__(GBP_THREADS)
+k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, uint32_t P, uint32_t W,
+		uint32_t koff, uint32_t kbytes, uint32_t voff, GbTable t, char* __restrict__ out, uint64_t out_cap,
+		unsigned long long* __restrict__ cursor, int* __restrict__ overflow, int* __restrict__ status)
+{
+	extern __shared__ __align__(16) unsigned char sm[];
+	unsigned long long* skeys = reinterpret_cast<unsigned long long*>(sm);        // [SLOTS + 1]
+	unsigned long long* sacc = skeys + GBP_SLOTS + 1;                              // [SLOTS + 1]
+	double* slo = reinterpret_cast<double*>(sacc + GBP_SLOTS + 1);                 // [SLOTS + 1]
+	__shared__ int s_sent;
+	__shared__ uint32_t wtot[GBP_THREADS / 32];
+	__shared__ unsigned long long s_base;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const uint32_t ow = kbytes + ((AGG == PG_AGG_SUM && VT == PG_VAL_INT) ? 4 : 8);
+	for (uint32_t part = blockIdx.x; part < P; part += gridDim.x) {
+		for (uint32_t i = tid; i <= GBP_SLOTS; i += blockDim.x) {
+			skeys[i] = (unsigned long long) PG_EMPTY_KEY; sacc[i] = 0; slo[i] = 0.0;
+		}
+		if (tid == 0) s_sent = 0;
+		__syncthreads();
+		const uint64_t lo = offs[part], hi = offs[part + 1];
+		bool spilled = false;
+		for (uint64_t i = lo + tid; i < lo + pg_div_up(hi - lo, 32) * 32; i += blockDim.x) {
+			const bool valid = i < hi;
+			int64_t k = 0;
+			unsigned long long iv = 0;
+			double dv = 0.0, dc = 0.0;
+			if (valid) {
+				const char* r = rows + i * W;
+				k = pg_load_key(r + koff, kbytes);
+				if (AGG == PG_AGG_COUNT) iv = 1;
+				else if (VT == PG_VAL_INT) iv = (unsigned long long) (long long) *reinterpret_cast<const int32_t*>(r + voff);
+				else if (VT == PG_VAL_LONG) iv = (unsigned long long) pg_load_key(r + voff, 8);
+				else dv = __longlong_as_double(pg_load_key(r + voff, 8));
+			}
+			const uint32_t active = __ballot_sync(0xffffffffu, valid);
+			if (!valid) continue;
+			const uint32_t peers = __match_any_sync(active, (unsigned long long) k);
+			warp_combine<VT, AGG>(peers, lane, iv, dv, dc);
+			if (lane != __ffs(peers) - 1) continue;
+			const uint32_t s = gbp_slot(skeys, k, &s_sent);
+			if (s != UINT32_MAX) { fold_slot<VT, AGG>(sacc, slo, s, iv, dv, dc); continue; }
+			// Shared table full: this key lives in the global table.
+			const uint64_t g = gb_slot(t.keys, t.log2cap, k, t.sentinel_used);
+			if (g == UINT64_MAX) { pg_set_status(status, PG_ERR_TABLE_FULL); continue; }
+			fold_slot<VT, AGG>(t.acc, t.lo, g, iv, dv, dc);
+			spilled = true;
+		}
+		if (spilled) atomicExch(overflow, 1);
+		__syncthreads();
+		// Emit: count used slots per thread, scan, reserve, write.
+		uint32_t mine = 0;
+		for (uint32_t i = tid; i <= GBP_SLOTS; i += blockDim.x)
+			mine += (i < GBP_SLOTS) ? (skeys[i] != (unsigned long long) PG_EMPTY_KEY) : (s_sent != 0);
+		uint32_t x = mine;
+		#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+			if (lane >= o) x += y;
+		}
+		if (lane == 31) wtot[warp] = x;
+		__syncthreads();
+		uint32_t before = 0, total = 0;
+		for (int w = 0; w < GBP_THREADS / 32; ++w) { const uint32_t c = wtot[w]; before += w < warp ? c : 0; total += c; }
+		if (tid == 0) s_base = total ? atomicAdd(cursor, (unsigned long long) total) : 0;
+		__syncthreads();
+		uint64_t pos = s_base + before + x - mine;
+		for (uint32_t i = tid; i <= GBP_SLOTS; i += blockDim.x) {
+			const bool used = (i < GBP_SLOTS) ? (skeys[i] != (unsigned long long) PG_EMPTY_KEY) : (s_sent != 0);
+			if (!used) continue;
+			if (pos < out_cap)
+				gb_write_row<VT, AGG>(out + pos * ow, kbytes, i < GBP_SLOTS ? (int64_t) skeys[i] : PG_EMPTY_KEY,
+						sacc[i], slo[i]);
+			++pos;
+		}
+		__syncthreads();
+	}
+}
+
 template <int VT, int AGG, bool HASKEY>
 __global__ void k_gb_emit(GbTable t, uint32_t kbytes, char* __restrict__ out, uint64_t cap_rows,
 		unsigned long long* __restrict__ cursor, uint64_t nonkey_rows)
@@ -339,6 +462,46 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 		PG_CUDA(ctx, cudaMemsetAsync(t.keys, 0xFF, (cap + 1) * 8, s));
 		PG_CUDA(ctx, cudaMemsetAsync(t.acc, 0, (cap + 1) * 16 + 64, s));
 		const bool smem = groups <= GB_SMEM_SLOTS / 2;
+		if (haskey && !smem && in->n >= 4 * groups && in->n < (1ull << 32) && in->width <= 1024) {
+			// High cardinality: partition by key hash, aggregate per partition.
+			uint32_t lp = 1;
+			while ((1ull << lp) < groups / 1024 && lp < 12) ++lp;
+			const uint32_t P = 1u << lp;
+			char* prow = nullptr;
+			uint64_t* poffs = nullptr;
+			int* oflag = reinterpret_cast<int*>(cursor + 1);
+			if ((rc = pg_alloc_async(ctx, s, (void**) &prow, in->n * in->width))) return rc;
+			if ((rc = pg_alloc_async(ctx, s, (void**) &poffs, (P + 1) * 8))) return rc;
+			pg_hashfn f;
+			f.fn = PG_FN_MIXRADIX; f.k = 0; f.min = 0; f.max = 0; f.bucketrange = 0;
+			f.skipbits = 64 - lp; f.nbuckets = P;
+			if ((rc = pg_partition_fn(ctx, s, in, f, prow, poffs))) return rc;
+			const size_t psm = (size_t) (GBP_SLOTS + 1) * 24;
+			PG_CUDA(ctx, cudaFuncSetAttribute(k_gb_part_agg<VT, AGG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) psm));
+			const int pblocks = (int) std::min<uint64_t>(P, (uint64_t) ctx->sm_count * 2);
+			k_gb_part_agg<VT, AGG><<<pblocks, GBP_THREADS, psm, s>>>(prow, poffs, P, in->width, in->key_off,
+					in->key_bytes, voff, t, (char*) out, out_cap, cursor, oflag, ctx->d_status);
+			PG_LAUNCHED(ctx);
+			int hflag = 0;
+			PG_CUDA(ctx, cudaMemcpyAsync(&hflag, oflag, 4, cudaMemcpyDeviceToHost, s));
+			rc = pg_check_status(ctx, s, "pg_groupby");
+			pg_free_async(ctx, s, prow);
+			pg_free_async(ctx, s, poffs);
+			if (rc == PG_ERR_TABLE_FULL) { pg_free_async(ctx, s, mem); groups *= 4; continue; }
+			if (rc) { pg_free_async(ctx, s, mem); return rc; }
+			if (hflag) {   // groups that overflowed a partition's table
+				int eblocks = (int) std::min<uint64_t>(pg_div_up(cap + 1, 256), (uint64_t) ctx->sm_count * 8);
+				k_gb_emit<VT, AGG, true><<<eblocks, 256, 0, s>>>(t, in->key_bytes, (char*) out, out_cap, cursor, 0);
+				PG_LAUNCHED(ctx);
+			}
+			unsigned long long ng = 0;
+			PG_CUDA(ctx, cudaMemcpyAsync(&ng, cursor, 8, cudaMemcpyDeviceToHost, s));
+			PG_CUDA(ctx, cudaStreamSynchronize(s));
+			pg_free_async(ctx, s, mem);
+			*ngroups = ng;
+			if (ng > out_cap) return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_groupby: output capacity too small");
+			return PG_OK;
+		}
 		uint32_t slg = 1;
 		while ((1u << slg) < 2 * groups) ++slg;
 		if (!haskey) slg = 0;

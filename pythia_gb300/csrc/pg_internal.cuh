@@ -64,6 +64,13 @@ int pg_hashfn_derive(const pg_hashcfg* c, pg_hashfn* f);
 int pg_partition_fn(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, const pg_hashfn& f,
 		void* out, uint64_t* offsets);
 
+// Internal bucket function (not a plan option): the top log2(buckets) bits of
+// the 64-bit key mix, skipbits = 64 - log2(buckets). Spreads any key domain
+// evenly, for partitions that feed per-partition tables.
+#define PG_FN_MIXRADIX 64
+
+__device__ __forceinline__ uint64_t pg_mix64(uint64_t k);
+
 // Key columns are 4-byte aligned (column offsets and tuple widths are
 // multiples of 4); an 8-byte key may straddle an 8-byte boundary.
 __device__ __forceinline__ int64_t pg_load_key(const char* p, uint32_t bytes)
@@ -87,6 +94,8 @@ __device__ __forceinline__ uint32_t pg_hash_field(const pg_hashfn& f, const char
 		}
 		return (uint32_t) (((h >> f.k) ^ h) & ((1ull << f.k) - 1));
 	}
+	case PG_FN_MIXRADIX:
+		return (uint32_t) (pg_mix64((uint64_t) pg_load_key(p, size)) >> f.skipbits);
 	case PG_FN_TPCHQ1MAGIC: {
 		uint32_t v = *reinterpret_cast<const uint32_t*>(p);
 		return (((v >> 4) | (v >> 16)) & 0x1u) | ((v >> 1) & 0x2u);

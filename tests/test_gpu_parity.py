@@ -228,7 +228,7 @@ def _gb_int_check(ctx, rows, agg, vtype, key=(0, 8), hint=0, has_key=True):
     assert np.array_equal(canon(got), canon(want))
 
 
-@pytest.mark.parametrize("groups", [1, 10, 1000, 200_000])
+@pytest.mark.parametrize("groups", [1, 10, 1000, 20_000, 200_000])
 def test_groupby_long_sum_and_count(ctx, groups):
     rows = dg.uniform_keys(500_000, groups, dg.seed_for(50))
     rows[:, 1] -= 1 << 30    # negative values too
@@ -293,6 +293,16 @@ def test_groupby_dec_ill_conditioned(ctx):
 def test_groupby_dec_zipf(ctx):
     rows = gin.make({"gen": "groupby_zipf", "n": 300_000, "groups": 20_000, "rel": 54})
     _gb_dec_check(ctx, rows)
+    _gb_dec_check(ctx, rows, hint=20_000)     # partitioned path with skewed partitions
+
+
+def test_groupby_partition_overflow(ctx):
+    # A hint far below the real group count: partitions overflow their shared
+    # tables into the global one, and the global table itself regrows.
+    rows = dg.uniform_keys(400_000, 90_000, dg.seed_for(55))
+    got = ctx.groupby(rows, val=(8, "long"), agg="sum", groups_hint=5000)
+    want = orc.groupby(rows, val=(8, "long"), agg="sum", hash=orc.hashcfg("modulo", 1024))
+    assert np.array_equal(canon(got), canon(want))
 
 
 def test_groupby_reference_unit_test(ctx):
