@@ -547,6 +547,183 @@ def cpu_op_sample(op, ins, threads):
             "kind": "port", "sample": f"{m} tuples (oracle port), time scaled {kind} to {n}"}
 
 
+# ---------------------------------------------------------------------------
+# Batched uneven joins (bench.py --op batch): 10,000 join + aggregate_count
+# instances, |R_i| log-uniform in [1K, 4M] unique keys, |S_i| = 8|R_i| FK.
+# ---------------------------------------------------------------------------
+BATCH_N = 10_000
+BATCH_POOL = 1 << 22
+
+
+def batch_sizes(n):
+    from pythia_gb300 import datagen as dg
+    u = dg.raw_words(dg.seed_for(120), 0, n).astype(np.float64) * (1.0 / 2.0 ** 64)
+    lo, hi = np.log(1000.0), np.log(float(BATCH_POOL))
+    return np.clip(np.rint(np.exp(lo + u * (hi - lo))).astype(np.int64), 1000, BATCH_POOL)
+
+
+def fk_host(R, seed, n):
+    """Host replica of pg_generate_fk (k_generate_fk), for the CPU sample."""
+    M = (1 << 64) - 1
+    j = np.arange(1, n + 1, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed) + j * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+        nR = np.uint64(R.shape[0])
+        # multiply-high of z * nR (nR < 2^32): split z into 32-bit halves
+        zh, zl = z >> np.uint64(32), z & np.uint64(0xFFFFFFFF)
+        idx = (zh * nR + ((zl * nR) >> np.uint64(32))) >> np.uint64(32)
+        pay = ((z * np.uint64(0xD1B54A32D192ED03)) >> np.uint64(33)).astype(np.int64)
+    del M
+    out = np.empty((n, 2), dtype=np.int64)
+    out[:, 0] = R[idx.astype(np.int64), 0]
+    out[:, 1] = pay
+    return out
+
+
+def run_batch(args, ws, rank, local):
+    import torch
+    from pythia_gb300 import autotune, datagen as dg, gpu
+    torch.cuda.set_device(local)
+    threads = host_threads()
+    ctx = gpu.Context(local)
+    L = gpu.lib()
+    n_inst = BATCH_N >> args.scale_down
+    sizes = batch_sizes(n_inst)
+    pool = dg.build_relation(BATCH_POOL, dg.seed_for(121), threads=threads)
+    d_pool = ctx.upload(pool)
+    wave_cap = (1 << 30) >> args.scale_down          # probe tuples per wave
+    waves, cur, tot = [], [], 0
+    for i, r in enumerate(sizes):
+        if cur and tot + 8 * r > wave_cap:
+            waves.append(cur); cur, tot = [], 0
+        cur.append(i); tot += 8 * r
+    if cur:
+        waves.append(cur)
+    d_S = ctx.alloc(16 * max(sum(8 * int(sizes[i]) for i in w) for w in waves))
+    gpu_name = torch.cuda.get_device_name(local)
+
+    def gen_wave(w):
+        items, off = [], 0
+        for i in w:
+            r = int(sizes[i]); s = 8 * r
+            Sp = d_S.ptr + 16 * off
+            ctx._check(L.pg_generate_fk(ctx.h, ctx.stream, d_pool.ptr, r, dg.seed_for(1000 + i), Sp, s))
+            items.append((i, (d_pool.ptr, r, Sp, s)))
+            off += s
+        ctx.sync()
+        return items
+
+    # Autotune per size class on the first wave (cached per GPU).
+    cached = autotune.load(gpu_name) or {}
+    shapes = cached.get("batch")
+    sweep = None
+    items0 = gen_wave(waves[0])
+    if shapes is None or args.retune:
+        by_cls = {}
+        for i, it in items0:
+            by_cls.setdefault(autotune.size_class(int(sizes[i])), []).append(it)
+        shapes, sweep = autotune.tune_batch(ctx, by_cls, repeats=2)
+        cached["batch"] = shapes
+        autotune.save(gpu_name, cached)
+    default = autotune.BATCH_SHAPES[0]
+
+    counts = np.zeros(n_inst, dtype=np.uint64)
+    loop_counts = np.zeros(n_inst, dtype=np.uint64)
+    t_batch = 0.0
+    t_loop = 0.0
+    launches = 0
+    c, nc = gpu.cols((("P", 8, 8), ("B", 8, 8)))
+    for wi, w in enumerate(waves):
+        items = items0 if wi == 0 else gen_wave(w)
+        by_cls = {}
+        for i, it in items:
+            by_cls.setdefault(autotune.size_class(int(sizes[i])), []).append((i, it))
+        batches = []
+        for cls, lst in by_cls.items():
+            b = autotune.prepare(ctx, [it for _, it in lst], shapes.get(cls, default))
+            batches.append((b, [i for i, _ in lst]))
+        for b, _ in batches:
+            autotune.run(ctx, b)           # warm-up replay
+        ctx.sync()
+        k0 = gpu.kernel_launches()
+        best = float("inf")
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            for b, _ in batches:
+                autotune.run(ctx, b)
+            best = min(best, time.perf_counter() - t0)
+        launches += (gpu.kernel_launches() - k0) // max(1, args.steps)
+        t_batch += best
+        for b, idx in batches:
+            cc = np.zeros(len(idx), dtype=np.uint64)
+            autotune.run(ctx, b, cc)
+            counts[idx] = cc
+            autotune.free(ctx, b)
+        # The same instances through the plain entry points, one by one.
+        t0 = time.perf_counter()
+        for i, (Rp, r, Sp, s) in items:
+            rR = gpu.Rel(Rp, r, 16, 0, 8)
+            rS = gpu.Rel(Sp, s, 16, 0, 8)
+            ht = ctypes.c_void_p()
+            ctx._check(L.pg_hashjoin_build(ctx.h, ctx.stream, ctypes.byref(rR), c, nc, ctypes.byref(ht)))
+            res = gpu.JoinResult()
+            ctx._check(L.pg_hashjoin_probe(ctx.h, ctx.stream, ht.value, ctypes.byref(rS), c, nc, None, 0,
+                                           gpu.JOIN_COUNT, -1, ctypes.byref(res)))
+            L.pg_hashtable_free(ctx.h, ht.value)
+            loop_counts[i] = res.n_out
+        t_loop += time.perf_counter() - t0
+    want = (8 * sizes).astype(np.uint64)
+    parity = {"counts_equal_probe_sizes": bool(np.array_equal(counts, want)),
+              "batched_equals_loop": bool(np.array_equal(counts, loop_counts))}
+    alg = int(16 * (sizes.sum() + 8 * sizes.sum()))
+    value = n_inst / t_batch
+    peak, peak_kind = measured_peak()
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as orc
+        pick = [i for i in range(n_inst) if sizes[i] <= 65536][:40]
+        t0 = time.perf_counter()
+        tuples = 0
+        for i in pick:
+            r = int(sizes[i])
+            S = fk_host(pool[:r], dg.seed_for(1000 + i), 8 * r)
+            _, n_out, _ = orc.hashjoin(pool[:r], S, hash=orc.hashcfg("modulo", r), tuplesperbucket=4,
+                                       threads=threads, materialise=False)
+            assert n_out == 8 * r
+            tuples += 9 * r
+        t = time.perf_counter() - t0
+        total_tuples = int(9 * sizes.sum())
+        cpu = {"value": n_inst / (t * total_tuples / tuples), "unit": "instances/s", "cores": threads,
+               "kind": "port", "sample": f"{len(pick)} instances with |R| <= 64K (oracle port, join + count), "
+                                        f"time scaled by tuples to all {n_inst}"}
+    if rank == 0:
+        line = {"metric": "batched join+count instances/s (10,000 uneven PK-FK instances)", "value": value,
+                "unit": "instances/s", "n_gpus": ws, "steps": args.steps, "warmup": 1,
+                "ms_per_step": t_batch * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "int64", "data": "synthetic (build pool + device FK generator)",
+                "config": {"workload": f"{n_inst} instances, |R| log-uniform [1K, 4M], |S| = 8|R|, "
+                                       f"join + aggregate_count", "waves": len(waves),
+                           "total_build": int(sizes.sum()), "total_probe": int(8 * sizes.sum()),
+                           "shapes": shapes},
+                "loop_baseline": {"value": n_inst / t_loop, "unit": "instances/s", "ms": t_loop * 1e3,
+                                  "what": "pg_hashjoin_build + pg_hashjoin_probe(COUNT) per instance"},
+                "speedup_vs_loop": t_loop / t_batch,
+                "parity": parity,
+                "roofline": {"bound": "hbm", "kernel": "k_batch_build + k_batch_probe_count",
+                             "achieved": alg / t_batch / 1e9, "peak": peak, "unit": "GB/s",
+                             "frac": alg / t_batch / 1e9 / peak, "traffic": None, "peak_source": peak_kind},
+                "gpu_launches": int(launches)}
+        if sweep:
+            line["autotune"] = sweep
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -558,7 +735,8 @@ def main():
     ap.add_argument("--key-domain", default="dense", choices=["dense", "sparse"],
                     help="dense: keys 1..|R| (direct-mapped table); sparse: the same keys "
                          "multiplied by an odd constant (hashed table)")
-    ap.add_argument("--op", default="hashjoin", choices=["hashjoin"] + sorted(OPS))
+    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "batch"] + sorted(OPS))
+    ap.add_argument("--retune", action="store_true", help="rerun the autotuner for --op batch")
     ap.add_argument("--scale-down", type=int, default=0, help="divide --op sizes by 2^k")
     ap.add_argument("--build-log2", type=int, default=24)
     ap.add_argument("--probe-log2", type=int, default=28)
@@ -568,6 +746,8 @@ def main():
     ws, rank, local = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, ws, rank)
+    elif args.op == "batch":
+        run_batch(args, ws, rank, local)
     elif args.op != "hashjoin":
         run_op(args, ws, rank, local, args.op)
     else:

@@ -111,6 +111,7 @@ enum {
 	PG_TUNE_DENSE = 2,               /* 1: allow dense tables (default), 2: always hash */
 	PG_TUNE_PARTITION_TILE = 3,      /* partition tile bytes (8192..65536) */
 	PG_TUNE_GROUPBY_SMEM_GROUPS = 4, /* largest group count aggregated in shared memory first */
+	PG_TUNE_RADIX_BITS = 5,          /* radix sort digit: 4..12 bits (partition fan-out 2^bits) */
 	PG_TUNE_COUNT = 8
 };
 int pg_tune_set(pg_ctx* ctx, int knob, int64_t value);
@@ -210,6 +211,36 @@ int pg_sort_pages(pg_ctx* ctx, pg_stream stream, const pg_rel* in, void* out);
 int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, const pg_rel* S,
 		const pg_col* proj, int nproj, void* out, uint64_t out_capacity,
 		int flags, int sum_col, pg_join_result* res);
+
+/* ---------------------------------------------------------------------- */
+/* Batched uneven joins: many independent join + aggregate_count instances
+ * (one HashJoinOp plan per instance under MergeOp in the reference,
+ * operators/join.cpp:273-675, aggregatecount.cpp:37-52) run by one build and
+ * one probe launch over instance-aligned tiles, optionally replayed as a CUDA
+ * graph. Relations are 16-byte (long key, long payload) tuples keyed at 0;
+ * counts[i] = number of join rows of instance i.                          */
+/* ---------------------------------------------------------------------- */
+typedef struct {
+	const void* R; uint64_t nR;      /* build relation (device)  */
+	const void* S; uint64_t nS;      /* probe relation (device)  */
+} pg_batch_item;
+typedef struct {
+	int32_t threads;       /* 128, 256 or 512 threads per CTA                */
+	int32_t items;         /* probe keys in flight per thread: 1, 2, 4, 8    */
+	uint32_t tile;         /* tuples per tile                                */
+	int32_t ctas_per_sm;   /* persistent CTAs per SM                         */
+	int32_t load_inverse;  /* table slots per build tuple (2: load 1/2)      */
+	int32_t use_graph;     /* capture clear+build+probe as a CUDA graph      */
+} pg_batch_shape;
+typedef struct pg_batch pg_batch;
+int pg_batch_prepare(pg_ctx* ctx, pg_stream stream, const pg_batch_item* items, uint32_t n,
+		const pg_batch_shape* shape, pg_batch** batch);
+int pg_batch_run(pg_ctx* ctx, pg_batch* batch, uint64_t* counts_host);
+int pg_batch_free(pg_ctx* ctx, pg_batch* batch);
+/* Synthetic foreign keys for benchmarks: S[j] = (R[h(seed, j) mod nR].key,
+ * h'(seed, j)), 16-byte tuples, h a SplitMix64 counter hash. */
+int pg_generate_fk(pg_ctx* ctx, pg_stream stream, const void* R, uint64_t nR, uint64_t seed,
+		void* S, uint64_t nS);
 
 #ifdef __cplusplus
 }

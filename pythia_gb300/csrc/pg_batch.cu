@@ -1,0 +1,295 @@
+// Batched uneven joins on sm_103a.
+//
+// Many independent join + aggregate_count instances (the reference would run
+// one HashJoinOp plan per instance under a MergeOp, operators/join.cpp:
+// 273-675 with aggregatecount.cpp:37-52 above it) are executed by one build
+// launch and one probe launch per size class instead of two launches, a host
+// synchronisation and scratch allocations per instance. Work is cut into
+// tiles that never straddle instances; each persistent CTA walks the tile
+// list, so a 1K-tuple instance and a 32M-tuple instance share the machine
+// without per-instance launch overhead. The sequence (table clear, build,
+// probe, count copy-out) can be captured once as a CUDA graph and replayed.
+//
+// Every instance gets its own open-addressing table region (16-byte slots,
+// linear probing from an even slot, 32-byte bucket loads on probe) sized by
+// the class's load factor. Launch shape (threads per CTA, tile size, CTAs per
+// SM) and load factor come from pg_batch_shape, which the autotuner chooses
+// per size class.
+#include "pg_internal.cuh"
+#include <algorithm>
+#include <vector>
+
+struct BatchInst {
+	const char* R; const char* S;
+	uint64_t nR, nS;
+	uint64_t table_off;     // first slot of the instance's table
+	uint32_t log2cap;
+	uint32_t pad;
+};
+
+struct BatchTile {           // [begin, end) of one side of instance `inst`
+	uint32_t inst;
+	uint32_t pad;
+	uint64_t begin, end;
+};
+
+__device__ __forceinline__ uint64_t bt_slot0(int64_t k, uint32_t log2cap)
+{
+	return (pg_mix64((uint64_t) k) >> (65 - log2cap)) << 1;
+}
+
+__global__ void k_batch_build(const BatchInst* __restrict__ inst, const BatchTile* __restrict__ tiles,
+		uint64_t ntiles, unsigned long long* __restrict__ slots, int* __restrict__ status)
+{
+	for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+		const BatchTile tl = tiles[t];
+		const BatchInst in = inst[tl.inst];
+		unsigned long long* tab = slots + 2 * in.table_off;
+		const uint64_t mask = (1ull << in.log2cap) - 1;
+		for (uint64_t i = tl.begin + threadIdx.x; i < tl.end; i += blockDim.x) {
+			const uint4 tup = reinterpret_cast<const uint4*>(in.R)[i];
+			const long long k = (long long) (((uint64_t) tup.y << 32) | tup.x);
+			const unsigned long long v = ((unsigned long long) tup.w << 32) | tup.z;
+			uint64_t s = bt_slot0(k, in.log2cap), probe = 0;
+			for (; probe <= mask; ++probe) {
+				const unsigned long long old = atomicCAS(&tab[2 * s], (unsigned long long) PG_EMPTY_KEY,
+						(unsigned long long) k);
+				if (old == (unsigned long long) PG_EMPTY_KEY) { tab[2 * s + 1] = v; break; }
+				s = (s + 1) & mask;
+			}
+			if (probe > mask) pg_set_status(status, PG_ERR_TABLE_FULL);
+		}
+	}
+}
+
+// Counts, per instance, the probe tuples' matches (duplicates included: the
+// probe walks its whole sequence). One atomicAdd per tile and CTA.
+template <int ITEMS>
+__global__ void k_batch_probe_count(const BatchInst* __restrict__ inst, const BatchTile* __restrict__ tiles,
+		uint64_t ntiles, const unsigned long long* __restrict__ slots, unsigned long long* __restrict__ counts)
+{
+	__shared__ unsigned long long wsum[32];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+	const uint64_t keep = pg_policy_evict_last();
+	for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+		const BatchTile tl = tiles[t];
+		const BatchInst in = inst[tl.inst];
+		const unsigned long long* tab = slots + 2 * in.table_off;
+		const uint64_t mask = (1ull << in.log2cap) - 1;
+		unsigned long long c = 0;
+		for (uint64_t base = tl.begin; base < tl.end; base += (uint64_t) blockDim.x * ITEMS) {
+			long long key[ITEMS];
+			uint64_t slot[ITEMS];
+			bool open[ITEMS];
+			#pragma unroll
+			for (int j = 0; j < ITEMS; ++j) {
+				const uint64_t i = base + (uint64_t) j * blockDim.x + threadIdx.x;
+				open[j] = i < tl.end;
+				key[j] = open[j] ? reinterpret_cast<const long long*>(in.S)[2 * i] : 0;
+				slot[j] = bt_slot0(key[j], in.log2cap);
+			}
+			for (uint64_t round = 0; round <= (mask >> 1); ++round) {
+				pg_u64x4 bk[ITEMS];
+				bool any = false;
+				#pragma unroll
+				for (int j = 0; j < ITEMS; ++j)
+					if (open[j]) { bk[j] = pg_ld_bucket32(tab + 2 * slot[j], keep); any = true; }
+				if (!any) break;
+				#pragma unroll
+				for (int j = 0; j < ITEMS; ++j) {
+					if (!open[j]) continue;
+					if ((long long) bk[j].a == key[j]) ++c;
+					if (bk[j].a == (unsigned long long) PG_EMPTY_KEY) { open[j] = false; continue; }
+					if ((long long) bk[j].c == key[j]) ++c;
+					if (bk[j].c == (unsigned long long) PG_EMPTY_KEY) { open[j] = false; continue; }
+					slot[j] = (slot[j] + 2) & mask;
+				}
+			}
+		}
+		#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+		if (lane == 0) wsum[warp] = c;
+		__syncthreads();
+		if (threadIdx.x == 0) {
+			unsigned long long tot = 0;
+			for (int w = 0; w < nwarps; ++w) tot += wsum[w];
+			if (tot) atomicAdd(&counts[tl.inst], tot);
+		}
+		__syncthreads();
+	}
+}
+
+// Keys equal to the empty marker never occur in the batch workloads' build
+// sides; the host rejects them instead of carrying a side list per instance.
+__global__ void k_batch_check_keys(const BatchInst* __restrict__ inst, uint32_t ninst, int* __restrict__ status)
+{
+	for (uint32_t b = blockIdx.x; b < ninst; b += gridDim.x) {
+		const BatchInst in = inst[b];
+		for (uint64_t i = threadIdx.x; i < in.nR; i += blockDim.x)
+			if (reinterpret_cast<const long long*>(in.R)[2 * i] == PG_EMPTY_KEY) pg_set_status(status, PG_ERR_UNSUPPORTED);
+	}
+}
+
+// Synthetic foreign keys: S[j].key = R[h(seed, j) mod nR].key, payload from
+// the same counter hash (SplitMix64 finaliser; multiply-high reduction).
+__global__ void k_generate_fk(const char* __restrict__ R, uint64_t nR, uint64_t seed, char* __restrict__ S, uint64_t nS)
+{
+	for (uint64_t j = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; j < nS;
+			j += (uint64_t) gridDim.x * blockDim.x) {
+		uint64_t z = seed + (j + 1) * 0x9E3779B97F4A7C15ull;
+		z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+		z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+		z ^= z >> 31;
+		const uint64_t idx = __umul64hi(z, nR);
+		const long long key = reinterpret_cast<const long long*>(R)[2 * idx];
+		reinterpret_cast<long long*>(S)[2 * j] = key;
+		reinterpret_cast<long long*>(S)[2 * j + 1] = (long long) ((z * 0xD1B54A32D192ED03ull) >> 33);
+	}
+}
+
+extern "C" int pg_generate_fk(pg_ctx* ctx, pg_stream stream, const void* R, uint64_t nR, uint64_t seed,
+		void* S, uint64_t nS)
+{
+	if (!ctx || (nS && (!R || !S || nR == 0))) return pg_fail(ctx, PG_ERR_ARG, "pg_generate_fk: bad argument");
+	if (nS == 0) return PG_OK;
+	const int blocks = (int) std::min<uint64_t>(pg_div_up(nS, 256), (uint64_t) ctx->sm_count * 16);
+	k_generate_fk<<<blocks, 256, 0, (cudaStream_t) stream>>>((const char*) R, nR, seed, (char*) S, nS);
+	PG_LAUNCHED(ctx);
+	return PG_OK;
+}
+
+// Prepared batch: device descriptors, tile lists and tables; replayable.
+struct pg_batch {
+	pg_ctx* ctx;
+	cudaStream_t stream;
+	uint32_t ninst;
+	BatchInst* d_inst;
+	BatchTile* d_btiles;
+	BatchTile* d_ptiles;
+	uint64_t nbtiles, nptiles;
+	unsigned long long* d_slots;
+	uint64_t nslots;
+	unsigned long long* d_counts;
+	pg_batch_shape shape;
+	cudaGraphExec_t graph;
+	bool has_graph;
+};
+
+static int batch_launch(pg_batch* b, cudaStream_t s)
+{
+	pg_ctx* ctx = b->ctx;
+	PG_CUDA(ctx, cudaMemsetAsync(b->d_slots, 0xFF, b->nslots * 16, s));
+	PG_CUDA(ctx, cudaMemsetAsync(b->d_counts, 0, b->ninst * 8, s));
+	const int per_sm = b->shape.ctas_per_sm > 0 ? b->shape.ctas_per_sm : 4;
+	const int threads = b->shape.threads > 0 ? b->shape.threads : 256;
+	if (b->nbtiles) {
+		const int grid = (int) std::min<uint64_t>(b->nbtiles, (uint64_t) ctx->sm_count * per_sm);
+		k_batch_build<<<grid, threads, 0, s>>>(b->d_inst, b->d_btiles, b->nbtiles, b->d_slots, ctx->d_status);
+		PG_LAUNCHED(ctx);
+	}
+	if (b->nptiles) {
+		const int grid = (int) std::min<uint64_t>(b->nptiles, (uint64_t) ctx->sm_count * per_sm);
+		switch (b->shape.items) {
+		case 1: k_batch_probe_count<1><<<grid, threads, 0, s>>>(b->d_inst, b->d_ptiles, b->nptiles, b->d_slots, b->d_counts); break;
+		case 2: k_batch_probe_count<2><<<grid, threads, 0, s>>>(b->d_inst, b->d_ptiles, b->nptiles, b->d_slots, b->d_counts); break;
+		case 8: k_batch_probe_count<8><<<grid, threads, 0, s>>>(b->d_inst, b->d_ptiles, b->nptiles, b->d_slots, b->d_counts); break;
+		default: k_batch_probe_count<4><<<grid, threads, 0, s>>>(b->d_inst, b->d_ptiles, b->nptiles, b->d_slots, b->d_counts); break;
+		}
+		PG_LAUNCHED(ctx);
+	}
+	return PG_OK;
+}
+
+extern "C" int pg_batch_prepare(pg_ctx* ctx, pg_stream stream, const pg_batch_item* items, uint32_t n,
+		const pg_batch_shape* shape, pg_batch** out)
+{
+	if (!ctx || !out || (n && !items)) return pg_fail(ctx, PG_ERR_ARG, "pg_batch_prepare: null argument");
+	pg_batch_shape sh = {256, 4, 4096, 4, 2, 0};
+	if (shape) sh = *shape;
+	if (sh.threads != 128 && sh.threads != 256 && sh.threads != 512) sh.threads = 256;
+	if (sh.items != 1 && sh.items != 2 && sh.items != 4 && sh.items != 8) sh.items = 4;
+	if (sh.tile < 256) sh.tile = 4096;
+	if (sh.load_inverse < 2) sh.load_inverse = 2;
+	cudaStream_t s = (cudaStream_t) stream;
+	std::vector<BatchInst> inst(n);
+	std::vector<BatchTile> bt, pt;
+	uint64_t slots = 0;
+	for (uint32_t i = 0; i < n; ++i) {
+		const pg_batch_item& it = items[i];
+		if ((it.nR && !it.R) || (it.nS && !it.S))
+			return pg_fail(ctx, PG_ERR_ARG, "pg_batch_prepare: null relation");
+		if (((reinterpret_cast<uintptr_t>(it.R) | reinterpret_cast<uintptr_t>(it.S)) & 15))
+			return pg_fail(ctx, PG_ERR_ARG, "pg_batch_prepare: relations must be 16-byte aligned");
+		uint32_t lg = 6;
+		while ((1ull << lg) < (uint64_t) sh.load_inverse * it.nR) ++lg;
+		inst[i] = BatchInst{(const char*) it.R, (const char*) it.S, it.nR, it.nS, slots, lg, 0};
+		slots += 1ull << lg;
+		for (uint64_t b = 0; b < it.nR; b += sh.tile) bt.push_back(BatchTile{i, 0, b, std::min<uint64_t>(it.nR, b + sh.tile)});
+		for (uint64_t b = 0; b < it.nS; b += sh.tile) pt.push_back(BatchTile{i, 0, b, std::min<uint64_t>(it.nS, b + sh.tile)});
+	}
+	pg_batch* bb = new pg_batch();
+	bb->ctx = ctx; bb->stream = s; bb->ninst = n; bb->shape = sh;
+	bb->nbtiles = bt.size(); bb->nptiles = pt.size(); bb->nslots = std::max<uint64_t>(slots, 1);
+	bb->has_graph = false;
+	int rc = PG_OK;
+	cudaError_t e;
+	if ((e = cudaMalloc(&bb->d_inst, std::max<size_t>(1, n) * sizeof(BatchInst))) ||
+			(e = cudaMalloc(&bb->d_btiles, std::max<size_t>(1, bt.size()) * sizeof(BatchTile))) ||
+			(e = cudaMalloc(&bb->d_ptiles, std::max<size_t>(1, pt.size()) * sizeof(BatchTile))) ||
+			(e = cudaMalloc(&bb->d_slots, bb->nslots * 16)) ||
+			(e = cudaMalloc(&bb->d_counts, std::max<size_t>(1, n) * 8))) {
+		rc = pg_cuda_fail(ctx, e, "pg_batch_prepare: cudaMalloc");
+		pg_batch_free(ctx, bb);
+		return rc;
+	}
+	if (n) PG_CUDA(ctx, cudaMemcpyAsync(bb->d_inst, inst.data(), n * sizeof(BatchInst), cudaMemcpyHostToDevice, s));
+	if (!bt.empty()) PG_CUDA(ctx, cudaMemcpyAsync(bb->d_btiles, bt.data(), bt.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, s));
+	if (!pt.empty()) PG_CUDA(ctx, cudaMemcpyAsync(bb->d_ptiles, pt.data(), pt.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, s));
+	if (n) {
+		k_batch_check_keys<<<(int) std::min<uint32_t>(n, ctx->sm_count * 8), 256, 0, s>>>(bb->d_inst, n, ctx->d_status);
+		PG_LAUNCHED(ctx);
+	}
+	if ((rc = pg_check_status(ctx, s, "pg_batch_prepare"))) {
+		pg_batch_free(ctx, bb);
+		return pg_fail(ctx, rc, "pg_batch_prepare: a build key equals -1 (not supported in batches)");
+	}
+	if (sh.use_graph) {
+		// Capture clear + build + probe once; pg_batch_run replays it.
+		cudaGraph_t g;
+		if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal))) { pg_batch_free(ctx, bb); return pg_cuda_fail(ctx, e, "cudaStreamBeginCapture"); }
+		rc = batch_launch(bb, s);
+		e = cudaStreamEndCapture(s, &g);
+		if (rc || e) { pg_batch_free(ctx, bb); return rc ? rc : pg_cuda_fail(ctx, e, "cudaStreamEndCapture"); }
+		e = cudaGraphInstantiate(&bb->graph, g, 0);
+		cudaGraphDestroy(g);
+		if (e) { pg_batch_free(ctx, bb); return pg_cuda_fail(ctx, e, "cudaGraphInstantiate"); }
+		bb->has_graph = true;
+	}
+	*out = bb;
+	return PG_OK;
+}
+
+extern "C" int pg_batch_run(pg_ctx* ctx, pg_batch* b, uint64_t* counts_host)
+{
+	if (!ctx || !b) return pg_fail(ctx, PG_ERR_ARG, "pg_batch_run: null argument");
+	int rc;
+	if (b->has_graph) {
+		PG_CUDA(ctx, cudaGraphLaunch(b->graph, b->stream));
+		g_kernel_launches.fetch_add((b->nbtiles ? 1 : 0) + (b->nptiles ? 1 : 0));
+	} else if ((rc = batch_launch(b, b->stream))) return rc;
+	if (counts_host && b->ninst)
+		PG_CUDA(ctx, cudaMemcpyAsync(counts_host, b->d_counts, b->ninst * 8, cudaMemcpyDeviceToHost, b->stream));
+	return pg_check_status(ctx, b->stream, "pg_batch_run");
+}
+
+extern "C" int pg_batch_free(pg_ctx* ctx, pg_batch* b)
+{
+	if (!b) return PG_OK;
+	cudaStreamSynchronize(b->stream);
+	if (b->has_graph) cudaGraphExecDestroy(b->graph);
+	cudaFree(b->d_inst); cudaFree(b->d_btiles); cudaFree(b->d_ptiles);
+	cudaFree(b->d_slots); cudaFree(b->d_counts);
+	delete b;
+	(void) ctx;
+	return PG_OK;
+}

@@ -165,8 +165,9 @@ __global__ void k_records_to_tuples(const pg_rec* __restrict__ rec, uint64_t n, 
 }
 
 // ---------------------------------------------------------------------------
-// LSD radix path: when the keys span at most 2^32 values, ceil(bits/8) stable
-// 256-way partitions on successive 8-bit digits of (key - min) sort the
+// LSD radix path: when the keys span at most 2^32 values, ceil(bits/d) stable
+// 2^d-way partitions on successive d-bit digits of (key - min) (d = 8, or the
+// PG_TUNE_RADIX_BITS knob, 4..12) sort the
 // tuples (pg_partition.cu; each pass reads and writes the relation once). This
 // is ParameterizedModuloValueHasher::generate's multi-pass radix split
 // (hash.cpp:237-267) driven to completion. Ties keep input order.
@@ -238,16 +239,18 @@ static int radix_sort(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, void* out, 
 		*done = true;
 		return PG_OK;
 	}
-	const int passes = (bits + 7) / 8;
+	const int64_t tb = ctx->tune[PG_TUNE_RADIX_BITS];
+	const int digit = tb >= 4 && tb <= 12 ? (int) tb : 8;
+	const int passes = (bits + digit - 1) / digit;
 	pg_rel cur = *in;
 	for (int p = 0; p < passes; ++p) {
 		pg_hashfn f;
 		f.fn = PG_FN_PARAMMODULO;
-		f.skipbits = 8 * p;
-		f.k = (int64_t) 255 << f.skipbits;
+		f.skipbits = digit * p;
+		f.k = (int64_t) ((1u << digit) - 1) << f.skipbits;
 		f.min = kmin;
 		f.max = 0; f.bucketrange = 0;
-		f.nbuckets = 256;
+		f.nbuckets = 1u << digit;
 		void* dst = ((passes - 1 - p) % 2 == 0) ? out : tmp;
 		if ((rc = pg_partition_fn(ctx, s, &cur, f, dst, nullptr))) return rc;
 		cur.data = dst;

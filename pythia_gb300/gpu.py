@@ -45,15 +45,27 @@ class JoinResult(ctypes.Structure):
     _fields_ = [("n_out", ctypes.c_uint64), ("sum", ctypes.c_int64)]
 
 
+class BatchItem(ctypes.Structure):
+    _fields_ = [("R", ctypes.c_void_p), ("nR", ctypes.c_uint64), ("S", ctypes.c_void_p),
+                ("nS", ctypes.c_uint64)]
+
+
+class BatchShape(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int32), ("items", ctypes.c_int32), ("tile", ctypes.c_uint32),
+                ("ctas_per_sm", ctypes.c_int32), ("load_inverse", ctypes.c_int32),
+                ("use_graph", ctypes.c_int32)]
+
+
 SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_stream_create",
            "pg_stream_destroy", "pg_sync", "pg_buffer_alloc", "pg_buffer_free", "pg_host_alloc",
            "pg_host_free", "pg_h2d", "pg_d2h", "pg_memset", "pg_kernel_launches",
            "pg_hash_buckets", "pg_hash_tuples", "pg_partition", "pg_partition_sort",
            "pg_hashjoin_build", "pg_hashjoin_probe", "pg_hashtable_free", "pg_hashjoin_host",
            "pg_groupby", "pg_sort_pages", "pg_mpsm_join", "pg_hashjoin_agg_noalloc",
-           "pg_tune_set", "pg_tune_get"]
+           "pg_tune_set", "pg_tune_get", "pg_batch_prepare", "pg_batch_run", "pg_batch_free",
+           "pg_generate_fk"]
 TUNE = {"probe_ctas_per_sm": 0, "probe_variant": 1, "dense": 2, "partition_tile": 3,
-        "groupby_smem_groups": 4}
+        "groupby_smem_groups": 4, "radix_bits": 5}
 
 
 def lib_path():
@@ -98,6 +110,10 @@ def lib():
             "pg_hashjoin_agg_noalloc": ([vp, vp, P(Rel), P(Rel), P(Col), ci, ci, P(JoinResult)], ci),
             "pg_tune_set": ([vp, ci, ctypes.c_int64], ci),
             "pg_tune_get": ([vp, ci], ctypes.c_int64),
+            "pg_batch_prepare": ([vp, vp, P(BatchItem), u32, P(BatchShape), P(vp)], ci),
+            "pg_batch_run": ([vp, vp, vp], ci),
+            "pg_batch_free": ([vp, vp], ci),
+            "pg_generate_fk": ([vp, vp, vp, u64, u64, vp, u64], ci),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

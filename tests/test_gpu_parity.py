@@ -394,3 +394,46 @@ def test_mpsm_matches_hashjoin(ctx):
     a, n1, _ = ctx.mpsm(R, S)
     b, n2, _ = ctx.hashjoin(R, S)
     assert n1 == n2 and np.array_equal(canon(a), canon(b))
+
+
+# ---------------------------------------------------------------- batches
+def test_batch_join_count_matches_oracle(ctx):
+    from pythia_gb300 import autotune
+    rng = np.random.default_rng(3)
+    sizes = np.concatenate([rng.integers(1, 3000, 40), [1, 4096, 20_000]])
+    rels, items, want = [], [], []
+    for i, r in enumerate(sizes):
+        R = dg.build_relation(int(r), dg.seed_for(300 + i))
+        if i % 3 == 0:
+            R[:, 0] = R[:, 0] * 1_000_003            # sparse keys
+        S = dg.probe_uniform(int(8 * r), R, dg.seed_for(600 + i))
+        S[::11, 0] += 5_000_000                       # some misses
+        if i % 5 == 0:
+            R[: max(1, int(r) // 4), 0] = R[0, 0]     # duplicate build keys
+        dR, dS = ctx.upload(R), ctx.upload(S)
+        rels += [dR, dS]
+        items.append((dR.ptr, R.shape[0], dS.ptr, S.shape[0]))
+        _, n, _ = orc.hashjoin(R, S, materialise=False, hash=orc.hashcfg("modulo", 1024))
+        want.append(n)
+    items.append((rels[0].ptr, 0, rels[1].ptr, 0))    # an empty instance
+    want.append(0)
+    for shape in (autotune.BATCH_SHAPES[0], autotune.BATCH_SHAPES[3],
+                  dict(autotune.BATCH_SHAPES[8], use_graph=0)):
+        b = autotune.prepare(ctx, items, shape)
+        try:
+            for _ in range(2):                         # replays give the same counts
+                counts = np.zeros(len(items), dtype=np.uint64)
+                autotune.run(ctx, b, counts)
+                assert counts.tolist() == want
+        finally:
+            autotune.free(ctx, b)
+
+
+def test_generate_fk_matches_host_replica(ctx):
+    import bench
+    R = dg.build_relation(5000, dg.seed_for(700))
+    dR = ctx.upload(R)
+    dS = ctx.alloc(16 * 40_000)
+    ctx._check(gpu.lib().pg_generate_fk(ctx.h, ctx.stream, dR.ptr, 5000, 12345, dS.ptr, 40_000))
+    got = ctx.download(dS, 16 * 40_000).view(np.int64).reshape(-1, 2)
+    assert np.array_equal(got, bench.fk_host(R, 12345, 40_000))
