@@ -38,6 +38,7 @@ sys.path.insert(0, ROOT)
 NR = 1 << 24            # overridable with --build-log2 / --probe-log2 (smaller configs)
 NS = 1 << 28
 TUPLE = 16
+PROBE_DRAM_BYTES_PER_TUPLE = (1.094478e9 + 0.517657e9) / (1 << 25)
 METRIC = "join tuples/s (16M build x 256M probe, PK-FK, int64 keys, materialised)"
 WORKLOAD = "radix-scale PK-FK hash join: |R|=16M unique int64 keys, |S|=256M uniform FK, 16-byte tuples, output (P$1,B$1)"
 
@@ -318,10 +319,9 @@ def run_gpu(args, ws, rank, local):
                "detail": info}
 
     if rank == 0:
-        traffic = None
-        tp = os.path.join(ROOT, "profiles", "probe_traffic.json")
-        if os.path.exists(tp):
-            traffic = json.load(open(tp)).get("bytes_per_launch")
+        # DRAM bytes per probe tuple measured by ncu on the same 64 MB table
+        # (profiles/hashjoin_probe_16Mx256M.md); traffic scales with |S|.
+        traffic = PROBE_DRAM_BYTES_PER_TUPLE * NS if args.key_domain == "dense" else None
         line = {"metric": METRIC, "value": value, "unit": "tuples/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
@@ -334,7 +334,7 @@ def run_gpu(args, ws, rank, local):
                 "e2e": {"value": ws * (NR + NS) / (e2e / 1e3), "unit": "tuples/s",
                         "h2d_bytes_per_step": (NR + NS) * TUPLE, "d2h_bytes_per_step": NS * TUPLE,
                         "ms_per_step": e2e},
-                "roofline": {"bound": "hbm", "kernel": "k_probe_unique (materialise)",
+                "roofline": {"bound": "hbm", "kernel": "k_probe16_warp (materialise)",
                              "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
                              "peak_source": peak_kind, "probe_ms": probe,
