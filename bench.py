@@ -724,6 +724,73 @@ def run_batch(args, ws, rank, local):
     ctx.close()
 
 
+# ---------------------------------------------------------------------------
+# Serving (bench.py --op serve): join + group-by plans on resident tables,
+# continuous batching vs one at a time.
+# ---------------------------------------------------------------------------
+def run_serve(args, ws, rank, local):
+    import torch
+    from pythia_gb300 import datagen as dg, gpu, serving
+    torch.cuda.set_device(local)
+    ctx = gpu.Context(local)
+    ntab = 24 >> min(args.scale_down, 3)
+    u = dg.raw_words(dg.seed_for(130), 0, ntab).astype(np.float64) * (1.0 / 2.0 ** 64)
+    lo, hi = np.log(10_000.0), np.log(float((64 << 20) >> args.scale_down))
+    sizes = np.rint(np.exp(lo + u * (hi - lo))).astype(np.int64)
+    t0 = time.perf_counter()
+    cat = serving.Catalog(ctx, sizes, threads=host_threads())
+    build_s = time.perf_counter() - t0
+    nq = 200 >> min(args.scale_down, 2)
+    rng_t = dg.raw_words(dg.seed_for(131), 0, nq) % np.uint64(ntab)
+    rng_z = dg.raw_words(dg.seed_for(131), 1, nq) & np.uint64(1)
+
+    def queries(arrivals):
+        return [serving.Query(i, int(rng_t[i]), 0.8 if rng_z[i] else 0.0, float(arrivals[i])) for i in range(nq)]
+
+    budget = 150 << 30
+    one = serving.Server(ctx, cat, 1, budget)
+    many = serving.Server(ctx, cat, args.slots, budget)
+    one.run(queries(np.zeros(nq))[: min(nq, 8)])       # warm-up
+    many.run(queries(np.zeros(nq))[: min(nq, 8)])
+    sat_one = serving.summarize(one.run(queries(np.zeros(nq))))
+    qs_many = many.run(queries(np.zeros(nq)))
+    sat_many = serving.summarize(qs_many)
+    # Same results alone (one slot) and in the mix.
+    qs_one = one.run(queries(np.zeros(nq)))
+    same = True
+    worst = 0.0
+    for a, b in zip(qs_one, qs_many):
+        ka, va, na = a.result
+        kb, vb, nb = b.result
+        same &= bool(na == nb and np.array_equal(ka, kb))
+        if len(va):
+            worst = max(worst, float(np.max(np.abs(va - vb) / np.maximum(np.abs(va), 1e-300))))
+    sweep = []
+    for frac in (0.5, 0.9, 2.0):
+        lam = frac * sat_one["queries_per_s"]
+        arr = serving.poisson_arrivals(nq, lam, dg.seed_for(132))
+        r1 = serving.summarize(one.run(queries(arr)))
+        r2 = serving.summarize(many.run(queries(arr)))
+        sweep.append({"rate_qps": lam, "one_at_a_time": r1, "continuous_batching": r2})
+    one.close(); many.close(); cat.close()
+    if rank == 0:
+        line = {"metric": "served join+group-by queries/s (continuous batching) and p50/p99 latency",
+                "value": sat_many["queries_per_s"], "unit": "queries/s", "n_gpus": ws, "steps": 1, "warmup": 1,
+                "ms_per_step": sat_many["makespan_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic resident catalog (device generator)",
+                "config": {"workload": f"{nq} plans: hash join on a resident table (|R| log-uniform "
+                                       f"[10K, 64M], {ntab} tables), |S| = 10|R| uniform or Zipf 0.8, then "
+                                       f"aggregate_sum over |R|/100 groups", "slots": args.slots,
+                           "hbm_budget_bytes": budget, "resident_bytes": cat.resident_bytes,
+                           "catalog_build_s": build_s},
+                "saturation": {"one_at_a_time": sat_one, "continuous_batching": sat_many,
+                               "throughput_ratio": sat_many["queries_per_s"] / sat_one["queries_per_s"]},
+                "poisson_sweep": sweep,
+                "parity": {"same_results_alone_and_mixed": same, "max_rel_diff": worst, "tolerance": 1e-12}}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -735,7 +802,8 @@ def main():
     ap.add_argument("--key-domain", default="dense", choices=["dense", "sparse"],
                     help="dense: keys 1..|R| (direct-mapped table); sparse: the same keys "
                          "multiplied by an odd constant (hashed table)")
-    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "batch"] + sorted(OPS))
+    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "batch", "serve"] + sorted(OPS))
+    ap.add_argument("--slots", type=int, default=8, help="worker slots for --op serve")
     ap.add_argument("--retune", action="store_true", help="rerun the autotuner for --op batch")
     ap.add_argument("--scale-down", type=int, default=0, help="divide --op sizes by 2^k")
     ap.add_argument("--build-log2", type=int, default=24)
@@ -748,6 +816,8 @@ def main():
         run_reference(args, ws, rank)
     elif args.op == "batch":
         run_batch(args, ws, rank, local)
+    elif args.op == "serve":
+        run_serve(args, ws, rank, local)
     elif args.op != "hashjoin":
         run_op(args, ws, rank, local, args.op)
     else:

@@ -93,6 +93,10 @@ int pg_stream_destroy(pg_ctx* ctx, pg_stream stream);
 int pg_sync(pg_ctx* ctx, pg_stream stream);
 int pg_buffer_alloc(pg_ctx* ctx, uint64_t bytes, void** dptr);
 int pg_buffer_free(pg_ctx* ctx, void* dptr);
+/* Stream-ordered device buffers from the context's pool: no device-wide
+ * synchronisation, so queries on other streams keep running. */
+int pg_buffer_alloc_async(pg_ctx* ctx, pg_stream stream, uint64_t bytes, void** dptr);
+int pg_buffer_free_async(pg_ctx* ctx, pg_stream stream, void* dptr);
 int pg_host_alloc(pg_ctx* ctx, uint64_t bytes, void** hptr);   /* pinned */
 int pg_host_free(pg_ctx* ctx, void* hptr);
 int pg_h2d(pg_ctx* ctx, pg_stream stream, void* dst, const void* src, uint64_t bytes);
@@ -241,6 +245,11 @@ int pg_batch_free(pg_ctx* ctx, pg_batch* batch);
  * h'(seed, j)), 16-byte tuples, h a SplitMix64 counter hash. */
 int pg_generate_fk(pg_ctx* ctx, pg_stream stream, const void* R, uint64_t nR, uint64_t seed,
 		void* S, uint64_t nS);
+/* As pg_generate_fk with Zipf(s) ranks over R's rows (rejection-inversion,
+ * Hormann-Derflinger 1996; s = 0 is uniform) and a dec payload uniform in
+ * [0, vmax): S[j] = (R[rank - 1].key, value). */
+int pg_generate_zipf_fk(pg_ctx* ctx, pg_stream stream, const void* R, uint64_t nR, double s,
+		uint64_t seed, void* S, uint64_t nS, double vmax);
 
 #ifdef __cplusplus
 }

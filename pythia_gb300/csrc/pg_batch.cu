@@ -293,3 +293,67 @@ extern "C" int pg_batch_free(pg_ctx* ctx, pg_batch* b)
 	(void) ctx;
 	return PG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Zipf foreign keys on the device (rejection-inversion, Hormann & Derflinger
+// 1996): rank k in [1, n] with P(k) ~ k^-s, drawn from a counter hash of
+// (seed, j, attempt); s = 0 draws ranks uniformly. Dec payload uniform in
+// [0, vmax).
+// ---------------------------------------------------------------------------
+struct ZipfParams { double s, hx1, hn, sx; uint64_t n; };
+
+__host__ __device__ static inline double zf_h2(double t) { return fabs(t) > 1e-8 ? expm1(t) / t : 1.0 + t * 0.5 * (1.0 + t / 3.0); }
+__host__ __device__ static inline double zf_h1(double t) { return fabs(t) > 1e-8 ? log1p(t) / t : 1.0 - t * (0.5 - t / 3.0); }
+__host__ __device__ static inline double zf_H(double s, double x) { const double lx = log(x); return zf_h2((1.0 - s) * lx) * lx; }
+__host__ __device__ static inline double zf_Hinv(double s, double u) { return exp(zf_h1((1.0 - s) * u) * u); }
+__host__ __device__ static inline double zf_h(double s, double x) { return exp(-s * log(x)); }
+
+__device__ __forceinline__ uint64_t zf_hash(uint64_t seed, uint64_t j, uint64_t a)
+{
+	uint64_t z = seed + (j + 1) * 0x9E3779B97F4A7C15ull + a * 0xD1B54A32D192ED03ull;
+	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+	z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+	return z ^ (z >> 31);
+}
+
+__global__ void k_generate_zipf_fk(const char* __restrict__ R, ZipfParams zp, uint64_t seed,
+		char* __restrict__ S, uint64_t nS, double vmax)
+{
+	for (uint64_t j = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; j < nS;
+			j += (uint64_t) gridDim.x * blockDim.x) {
+		uint64_t k = 1;
+		if (zp.s == 0.0) {
+			k = __umul64hi(zf_hash(seed, j, 0), zp.n) + 1;
+		} else {
+			for (uint64_t a = 0; a < 64; ++a) {
+				const double u01 = (double) (zf_hash(seed, j, a) >> 11) * 0x1.0p-53;
+				const double u = zp.hn + u01 * (zp.hx1 - zp.hn);
+				const double x = zf_Hinv(zp.s, u);
+				double kd = floor(x + 0.5);
+				kd = kd < 1.0 ? 1.0 : (kd > (double) zp.n ? (double) zp.n : kd);
+				k = (uint64_t) kd;
+				if (kd - x <= zp.sx || u >= zf_H(zp.s, kd + 0.5) - zf_h(zp.s, kd)) break;
+			}
+		}
+		const long long key = reinterpret_cast<const long long*>(R)[2 * (k - 1)];
+		const double v = (double) (zf_hash(seed ^ 0x5A5A5A5Aull, j, 99) >> 11) * 0x1.0p-53 * vmax;
+		reinterpret_cast<long long*>(S)[2 * j] = key;
+		reinterpret_cast<double*>(S)[2 * j + 1] = v;
+	}
+}
+
+extern "C" int pg_generate_zipf_fk(pg_ctx* ctx, pg_stream stream, const void* R, uint64_t nR, double s,
+		uint64_t seed, void* S, uint64_t nS, double vmax)
+{
+	if (!ctx || (nS && (!R || !S || nR == 0)) || s < 0.0) return pg_fail(ctx, PG_ERR_ARG, "pg_generate_zipf_fk: bad argument");
+	if (nS == 0) return PG_OK;
+	ZipfParams zp;
+	zp.s = s; zp.n = nR;
+	zp.hx1 = zf_H(s, 1.5) - 1.0;
+	zp.hn = zf_H(s, (double) nR + 0.5);
+	zp.sx = 2.0 - zf_Hinv(s, zf_H(s, 2.5) - zf_h(s, 2.0));
+	const int blocks = (int) std::min<uint64_t>(pg_div_up(nS, 256), (uint64_t) ctx->sm_count * 16);
+	k_generate_zipf_fk<<<blocks, 256, 0, (cudaStream_t) stream>>>((const char*) R, zp, seed, (char*) S, nS, vmax);
+	PG_LAUNCHED(ctx);
+	return PG_OK;
+}

@@ -147,6 +147,19 @@ extern "C" int pg_buffer_free(pg_ctx* ctx, void* p)
 	return PG_OK;
 }
 
+extern "C" int pg_buffer_alloc_async(pg_ctx* ctx, pg_stream s, uint64_t bytes, void** p)
+{
+	if (!ctx || !p) return PG_ERR_ARG;
+	return pg_alloc_async(ctx, (cudaStream_t) s, p, bytes);
+}
+
+extern "C" int pg_buffer_free_async(pg_ctx* ctx, pg_stream s, void* p)
+{
+	if (!ctx) return PG_ERR_ARG;
+	pg_free_async(ctx, (cudaStream_t) s, p);
+	return PG_OK;
+}
+
 extern "C" int pg_host_alloc(pg_ctx* ctx, uint64_t bytes, void** p)
 {
 	if (!ctx || !p) return PG_ERR_ARG;

@@ -63,7 +63,7 @@ SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_st
            "pg_hashjoin_build", "pg_hashjoin_probe", "pg_hashtable_free", "pg_hashjoin_host",
            "pg_groupby", "pg_sort_pages", "pg_mpsm_join", "pg_hashjoin_agg_noalloc",
            "pg_tune_set", "pg_tune_get", "pg_batch_prepare", "pg_batch_run", "pg_batch_free",
-           "pg_generate_fk"]
+           "pg_generate_fk", "pg_buffer_alloc_async", "pg_buffer_free_async", "pg_generate_zipf_fk"]
 TUNE = {"probe_ctas_per_sm": 0, "probe_variant": 1, "dense": 2, "partition_tile": 3,
         "groupby_smem_groups": 4, "radix_bits": 5}
 
@@ -114,6 +114,9 @@ def lib():
             "pg_batch_run": ([vp, vp, vp], ci),
             "pg_batch_free": ([vp, vp], ci),
             "pg_generate_fk": ([vp, vp, vp, u64, u64, vp, u64], ci),
+            "pg_generate_zipf_fk": ([vp, vp, vp, u64, ctypes.c_double, u64, vp, u64, ctypes.c_double], ci),
+            "pg_buffer_alloc_async": ([vp, vp, u64, P(vp)], ci),
+            "pg_buffer_free_async": ([vp, vp, vp], ci),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
