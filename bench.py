@@ -202,12 +202,21 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def make_ctx(args, local):
+    """GPU context with the --tune knobs applied (name=value,...)."""
+    from pythia_gb300 import gpu
+    ctx = gpu.Context(local)
+    if args.tune:
+        ctx.tune(**{k: int(v) for k, v in (kv.split("=") for kv in args.tune.split(","))})
+    return ctx
+
+
 def run_gpu(args, ws, rank, local):
     import torch
     from pythia_gb300 import gpu
     torch.cuda.set_device(local)
     threads = host_threads()
-    ctx = gpu.Context(local)
+    ctx = make_ctx(args, local)
     L = gpu.lib()
     # Pinned host relations (also the e2e sources) and output.
     def pinned(nbytes):
@@ -436,7 +445,7 @@ def run_op(args, ws, rank, local, op):
     spec = OPS[op]
     n = spec["n"] >> args.scale_down
     threads = host_threads()
-    ctx = gpu.Context(local)
+    ctx = make_ctx(args, local)
     L = gpu.lib()
     ins = _op_inputs(op, n, threads)
     d_in = [ctx.upload(a) for a in ins]
@@ -588,7 +597,7 @@ def run_batch(args, ws, rank, local):
     from pythia_gb300 import autotune, datagen as dg, gpu
     torch.cuda.set_device(local)
     threads = host_threads()
-    ctx = gpu.Context(local)
+    ctx = make_ctx(args, local)
     L = gpu.lib()
     n_inst = BATCH_N >> args.scale_down
     sizes = batch_sizes(n_inst)
@@ -732,7 +741,7 @@ def run_serve(args, ws, rank, local):
     import torch
     from pythia_gb300 import datagen as dg, gpu, serving
     torch.cuda.set_device(local)
-    ctx = gpu.Context(local)
+    ctx = make_ctx(args, local)
     ntab = 24 >> min(args.scale_down, 3)
     u = dg.raw_words(dg.seed_for(130), 0, ntab).astype(np.float64) * (1.0 / 2.0 ** 64)
     lo, hi = np.log(10_000.0), np.log(float((64 << 20) >> args.scale_down))
@@ -806,6 +815,7 @@ def main():
     ap.add_argument("--slots", type=int, default=8, help="worker slots for --op serve")
     ap.add_argument("--retune", action="store_true", help="rerun the autotuner for --op batch")
     ap.add_argument("--scale-down", type=int, default=0, help="divide --op sizes by 2^k")
+    ap.add_argument("--tune", default="", help="tuning knobs, e.g. probe_items=8,l2_persist=1")
     ap.add_argument("--build-log2", type=int, default=24)
     ap.add_argument("--probe-log2", type=int, default=28)
     args = ap.parse_args()

@@ -116,7 +116,12 @@ enum {
 	PG_TUNE_PARTITION_TILE = 3,      /* partition tile bytes (8192..65536) */
 	PG_TUNE_GROUPBY_SMEM_GROUPS = 4, /* largest group count aggregated in shared memory first */
 	PG_TUNE_RADIX_BITS = 5,          /* radix sort digit: 4..12 bits (partition fan-out 2^bits) */
-	PG_TUNE_COUNT = 8
+	PG_TUNE_PROBE_ITEMS = 6,         /* dense-table lookups in flight per lane of the 16-byte probe: 4 or 8 */
+	PG_TUNE_PROBE_CACHE = 7,         /* 16-byte probe L2 policies: bits 0-1 table loads (0 evict-last,
+	                                    1 normal, 2 unchanged, 3 first), bit 2 probe reads and bit 3
+	                                    output stores normal instead of evict-first */
+	PG_TUNE_PROBE_PASSES = 8,        /* dense-table probe passes: 1, 2 (half the table each), 0 by size */
+	PG_TUNE_COUNT = 12
 };
 int pg_tune_set(pg_ctx* ctx, int knob, int64_t value);
 int64_t pg_tune_get(pg_ctx* ctx, int knob);

@@ -91,6 +91,9 @@ struct HjProbeTable {
 	unsigned long long vmin;
 	long long dmin;
 	unsigned long long drange;
+	uint32_t cache;                        // L2 policy knob: bits 0-1 table loads (0 evict-last,
+	                                       // 1 normal, 2 unchanged, 3 first); bit 2 probe reads,
+	                                       // bit 3 output stores normal instead of evict-first
 };
 
 
@@ -592,45 +595,58 @@ k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPro
 
 // ---------------------------------------------------------------------------
 // Unique-key probe of 16-byte tuples without block barriers: every warp runs
-// on its own. Warp w of the grid owns chunks w, w + W, w + 2W, ... of 128
-// probe tuples; each chunk arrives in the warp's own shared-memory stage by a
-// bulk copy (2 stages in flight per warp, L2 evict-first). With unique build
-// keys a probe tuple yields at most one row, so chunk c writes its rows to
-// output rows [128c, 128c + matches) in probe order: no atomics and no
+// on its own. Warp w of the grid owns blocks w, w + W, w + 2W, ... of
+// 32 * ITEMS probe tuples; each block arrives in the warp's own shared-memory
+// stage by a bulk copy (2 stages in flight per warp, L2 evict-first), and
+// every lane has ITEMS table lookups in flight at once. With unique build keys
+// a probe tuple yields at most one row, so the 128-tuple chunk c writes its
+// rows to output rows [128c, 128c + matches) in probe order: no atomics and no
 // block-wide ranking. When every probe tuple matches (PK-FK) the output is
 // already dense; otherwise per-chunk counts drive a compaction pass.
+// Dense tables larger than L2 holds next to the streams are probed in two
+// passes over the probe relation, each looking up only keys whose table index
+// d lies in [dlo, dhi) (half the table, which stays in L2): run 0 writes a
+// chunk's rows at its front and counts them in the low word of the chunk's
+// count, run 1 writes them backwards from the chunk's end and counts them in
+// the high word; run -1 is the single pass over the whole table.
 // ---------------------------------------------------------------------------
 #define PW_WARPS 8
 #define PW_CHUNK 128
 #define PW_STAGES 2
 
-template <bool MATERIALIZE, int MODE>
-__global__ void __launch_bounds__(PW_WARPS * 32, MODE != 0 ? 4 : 2)
+template <bool MATERIALIZE, int MODE, int ITEMS>
+__global__ void __launch_bounds__(PW_WARPS * 32, MODE != 0 ? (ITEMS > 4 ? 3 : 4) : 2)
 k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb,
 		uint32_t wsel, uint32_t sum_w0, uint32_t sum_words, char* __restrict__ out,
 		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg,
-		int sum_col, int* __restrict__ status)
+		int sum_col, int* __restrict__ status, uint64_t dlo, uint64_t dhi, int run)
 {
-	constexpr int ITEMS = PW_CHUNK / 32;             // tuples per lane per chunk
+	static_assert(ITEMS % 4 == 0, "a block is whole 128-tuple chunks");
+	constexpr int BLK = 32 * ITEMS;                  // tuples per warp block
+	constexpr int SUB = ITEMS / 4;                   // 128-tuple chunks per block
 	constexpr int GROUP = MODE != 0 ? ITEMS : 4;     // lookups issued together (registers)
 	extern __shared__ __align__(128) unsigned char sm[];
 	__shared__ __align__(8) uint64_t bars[PW_WARPS][PW_STAGES];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	uint4* const st0 = reinterpret_cast<uint4*>(sm) + (size_t) warp * PW_STAGES * PW_CHUNK;
+	uint4* const st0 = reinterpret_cast<uint4*>(sm) + (size_t) warp * PW_STAGES * BLK;
 	uint64_t* const bar = bars[warp];
-	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
+	const uint64_t nchunks = pg_div_up(n, BLK);
+	const uint64_t nchunks128 = pg_div_up(n, PW_CHUNK);
 	const uint64_t W = (uint64_t) gridDim.x * PW_WARPS;
 	const uint64_t first = (uint64_t) blockIdx.x * PW_WARPS + warp;
 	const uint64_t mask = (1ull << tb.log2cap) - 1;
-	const uint64_t keep = pg_policy_evict_last();
-	const uint64_t stream = pg_policy_evict_first();
+	const uint32_t tp_ = tb.cache & 3;
+	const uint64_t keep = tp_ == 0 ? pg_policy_evict_last() : tp_ == 1 ? pg_policy_evict_normal()
+		: tp_ == 2 ? pg_policy_evict_unchanged() : pg_policy_evict_first();
+	const uint64_t instream = (tb.cache & 4) ? pg_policy_evict_normal() : pg_policy_evict_first();
+	const uint64_t stream = (tb.cache & 8) ? pg_policy_evict_normal() : pg_policy_evict_first();
 	const uint32_t w0 = wsel & 15, w1 = (wsel >> 4) & 15, w2 = (wsel >> 8) & 15, w3 = (wsel >> 12) & 15;
 	unsigned long long cnt_acc = 0, sum_acc = 0;
 	if (first >= nchunks) return;
 	auto issue = [&](uint64_t c, int stg) {
-		const uint32_t rows = (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK);
+		const uint32_t rows = (uint32_t) pg_min64(BLK, n - c * BLK);
 		pg_mbar_expect_tx(&bar[stg], rows * 16);
-		pg_bulk_g2s_hint(st0 + stg * PW_CHUNK, S + c * (uint64_t) PW_CHUNK * 16, rows * 16, &bar[stg], stream);
+		pg_bulk_g2s_hint(st0 + stg * BLK, S + c * (uint64_t) BLK * 16, rows * 16, &bar[stg], instream);
 	};
 	if (lane == 0) {
 		for (int i = 0; i < PW_STAGES; ++i) pg_mbar_init(&bar[i], 1);
@@ -645,9 +661,11 @@ k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 		// A wait that gives up leaves the chunk unspecified; all accesses stay
 		// in bounds and the host reads the status.
 		if (!pg_mbar_wait(&bar[stg], parity)) pg_set_status(status, PG_ERR_TIMEOUT);
-		const uint4* const tp = st0 + stg * PW_CHUNK;
-		const uint32_t rows = (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK);
-		uint32_t rank = 0;
+		const uint4* const tp = st0 + stg * BLK;
+		const uint32_t rows = (uint32_t) pg_min64(BLK, n - c * BLK);
+		uint32_t rank[SUB];
+		#pragma unroll
+		for (int q = 0; q < SUB; ++q) rank[q] = 0;
 		#pragma unroll
 		for (int g = 0; g < ITEMS; g += GROUP) {
 			int64_t key[GROUP];
@@ -663,7 +681,7 @@ k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 						const uint4 t = tp[p];
 						key[j] = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
 						const unsigned long long d = (unsigned long long) key[j] - (unsigned long long) tb.dmin;
-						if (d < tb.drange) {
+						if (d >= dlo && d < dhi) {
 							if (MODE == 2) {
 								uint32_t e;
 								asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;"
@@ -715,11 +733,14 @@ k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 			}
 			#pragma unroll
 			for (int j = 0; j < GROUP; ++j) {
+				const int q = (g + j) / 4;               // 128-tuple chunk within the block
 				const uint32_t ball = __ballot_sync(0xffffffffu, hit[j]);
 				if (hit[j]) {
 					const uint4 t = tp[(g + j) * 32 + lane];
 					if (MATERIALIZE) {
-						const uint64_t row = c * PW_CHUNK + rank + __popc(ball & ((1u << lane) - 1));
+						const uint32_t r = rank[q] + __popc(ball & ((1u << lane) - 1));
+						const uint64_t c0 = c * BLK + q * PW_CHUNK;
+						const uint64_t row = run == 1 ? c0 + pg_min64(PW_CHUNK, n - c0) - 1 - r : c0 + r;
 						pg_st_hint16(out + row * 16, make_uint4(hj_pick(t, val[j], w0), hj_pick(t, val[j], w1),
 								hj_pick(t, val[j], w2), hj_pick(t, val[j], w3)), stream);
 					} else if (sum_col >= 0) {
@@ -729,11 +750,17 @@ k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 						else sum_acc += (unsigned long long) (long long) (int32_t) lo;
 					}
 				}
-				rank += __popc(ball);
+				rank[q] += __popc(ball);
 			}
 		}
-		cnt_acc += rank;
-		if (MATERIALIZE && lane == 0) chunk_counts[c] = rank;
+		#pragma unroll
+		for (int q = 0; q < SUB; ++q) {
+			cnt_acc += rank[q];
+			if (MATERIALIZE && lane == 0 && c * SUB + q < nchunks128) {
+				if (run < 0) chunk_counts[c * SUB + q] = rank[q];
+				else reinterpret_cast<uint32_t*>(chunk_counts)[2 * (c * SUB + q) + run] = rank[q];
+			}
+		}
 		// Every lane has finished reading this stage: refill it.
 		__syncwarp();
 		if (lane == 0 && c + PW_STAGES * W < nchunks) issue(c + PW_STAGES * W, stg);
@@ -745,16 +772,40 @@ k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 	if (lane == 0) { atomicAdd(&agg[0], cnt_acc); if (!MATERIALIZE) atomicAdd(&agg[1], sum_acc); }
 }
 
-// Closes the gaps of a positional probe output: chunk c's rows move from
-// [128c, 128c + count) to [offs[c], offs[c] + count) of `dst`.
+// Positional probe output: the 128-tuple chunk c (rows_c = min(128, n - 128c)
+// probe tuples) holds lo = counts[c] & 0xffffffff rows at its front,
+// [128c, 128c + lo), and hi = counts[c] >> 32 rows at its back,
+// [128c + rows_c - hi, 128c + rows_c). k_chunk_totals turns the counts into
+// lo + hi; k_compact_chunks moves both runs of chunk c to
+// [offs[c], offs[c] + lo + hi) of `dst`.
+// Front and back run lengths of chunk c, clamped to the chunk's rows.
+__device__ __forceinline__ void hj_chunk_runs(uint64_t cnt, uint64_t n, uint64_t c, uint32_t& lo, uint32_t& hi,
+		uint32_t& rows)
+{
+	rows = (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK);
+	lo = pg_min32((uint32_t) cnt, rows);
+	hi = pg_min32((uint32_t) (cnt >> 32), rows - lo);
+}
+
+__global__ void k_chunk_totals(const uint64_t* __restrict__ counts, uint64_t* __restrict__ tot, uint64_t nchunks,
+		uint64_t n)
+{
+	for (uint64_t c = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; c < nchunks; c += (uint64_t) gridDim.x * blockDim.x) {
+		uint32_t lo, hi, rows;
+		hj_chunk_runs(counts[c], n, c, lo, hi, rows);
+		tot[c] = lo + hi;
+	}
+}
+
 __global__ void k_compact_chunks(const uint4* __restrict__ src, const uint64_t* __restrict__ counts,
-		const uint64_t* __restrict__ offs, uint64_t nchunks, uint4* __restrict__ dst, uint64_t cap)
+		const uint64_t* __restrict__ offs, uint64_t nchunks, uint64_t n, uint4* __restrict__ dst, uint64_t cap)
 {
 	for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-		const uint32_t cnt = (uint32_t) counts[c];
+		uint32_t lo, hi, rows;
+		hj_chunk_runs(counts[c], n, c, lo, hi, rows);
 		const uint64_t o = offs[c];
-		for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x)
-			if (o + i < cap) dst[o + i] = src[c * PW_CHUNK + i];
+		for (uint32_t i = threadIdx.x; i < lo + hi; i += blockDim.x)
+			if (o + i < cap) dst[o + i] = src[c * PW_CHUNK + (i < lo ? i : rows - hi + (i - lo))];
 	}
 }
 
@@ -1057,6 +1108,9 @@ static int hj_make_cols(pg_ctx* ctx, const pg_hashtable* ht, const pg_col* proj,
 	return PG_OK;
 }
 
+#define HJ_TWO_PASS_MIN_BYTES (56ull << 20)   // dense tables above this probe in two passes
+#define HJ_TWO_PASS_MAX_BYTES (112ull << 20)  // ... up to this (half must fit in L2)
+
 // Launches the unique-key probe over n tuples at S (device) into `out`;
 // counts/sums accumulate in acc[1..2], the output cursor is acc[0].
 // With `counts` (device, one word per 256-tuple chunk) and cap >= n, 16-byte
@@ -1073,6 +1127,7 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 	tb.slots = ht->slots; tb.log2cap = ht->log2cap; tb.side = ht->side; tb.nside = ht->nside;
 	tb.dense_val = ht->dense_val; tb.dense_bits = ht->dense_bits; tb.dmin = ht->dmin; tb.drange = ht->drange;
 	tb.dense32 = ht->dense32; tb.vmin = ht->vmin;
+	tb.cache = (uint32_t) (ctx->tune[PG_TUNE_PROBE_CACHE] & 15);
 	const int mode = ht->dense ? (ht->dense32 ? 2 : 1) : 0;
 	const bool fast16 = W == 16 && (koff == 0 || koff == 8) && kbytes == 8 && pc.ow_words == 4 &&
 		(reinterpret_cast<uintptr_t>(S) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
@@ -1086,22 +1141,47 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 		}
 		const bool tiled = ctx->tune[PG_TUNE_PROBE_VARIANT] == 2;
 		if (!materialize || (counts && cap >= n && !tiled)) {
-			const int psmem = PW_WARPS * PW_STAGES * PW_CHUNK * 16;
-			// Persistent grid: CTAs per SM from the tuning table, else 4 for
-			// dense tables (more resident warps evict table lines from L2
-			// faster than they hide latency) and 2 for hashed ones.
+			// Lookups in flight per lane: 8 for dense tables when asked, else 4.
+			const int items = (mode != 0 && ctx->tune[PG_TUNE_PROBE_ITEMS] == 8) ? 8 : 4;
+			const int psmem = PW_WARPS * PW_STAGES * 32 * items * 16;
+			// Persistent grid: CTAs per SM from the tuning table, else as many
+			// as the shared memory holds for dense tables (4 at 4 items, 3 at
+			// 8: more resident warps evict table lines from L2 faster than
+			// they hide latency) and 2 for hashed ones.
 			const int64_t per_sm = ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] > 0
-				? std::min<int64_t>(5, ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM]) : (mode != 0 ? 4 : 2);
-			const int pgrid = (int) std::min<uint64_t>(pg_div_up(pg_div_up(n, PW_CHUNK), PW_WARPS),
+				? std::min<int64_t>(items > 4 ? 3 : 5, ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM])
+				: (mode != 0 ? (items > 4 ? 3 : 4) : 2);
+			const int pgrid = (int) std::min<uint64_t>(pg_div_up(pg_div_up(n, 32 * items), PW_WARPS),
 					(uint64_t) ctx->sm_count * per_sm);
-#define PW_LAUNCH(M, D) do { \
-			PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_warp<M, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, psmem)); \
-			k_probe16_warp<M, D><<<pgrid, PW_WARPS * 32, psmem, s>>>(S, n, koff, tb, wsel, sum_w0, sum_words, \
-					M ? out : nullptr, M ? counts : nullptr, M ? acc : acc + 1, M ? -1 : sum_col, ctx->d_status); } while (0)
-			if (materialize) { if (mode == 2) PW_LAUNCH(true, 2); else if (mode == 1) PW_LAUNCH(true, 1); else PW_LAUNCH(true, 0); }
-			else { if (mode == 2) PW_LAUNCH(false, 2); else if (mode == 1) PW_LAUNCH(false, 1); else PW_LAUNCH(false, 0); }
+			// Two passes over half the table each when the dense table is
+			// larger than L2 keeps next to the streams (knob: 1 one pass,
+			// 2 two passes, 0 by table size).
+			const uint64_t tbytes = mode == 2 ? ht->drange * 4 : ht->drange * 8;
+			const int64_t pk = ctx->tune[PG_TUNE_PROBE_PASSES];
+			const int passes = mode == 0 || pk == 1 ? 1
+				: (pk == 2 || (tbytes > HJ_TWO_PASS_MIN_BYTES && tbytes <= HJ_TWO_PASS_MAX_BYTES)) ? 2 : 1;
+			const uint64_t dr = mode == 0 ? 0 : ht->drange;
+			for (int pass = 0; pass < passes; ++pass) {
+				const int run = passes == 1 ? -1 : pass;
+				const uint64_t dlo = passes == 1 ? 0 : (pass == 0 ? 0 : dr / 2);
+				const uint64_t dhi = passes == 1 ? dr : (pass == 0 ? dr / 2 : dr);
+#define PW_LAUNCH(M, D, I) do { \
+				PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_warp<M, D, I>, cudaFuncAttributeMaxDynamicSharedMemorySize, psmem)); \
+				k_probe16_warp<M, D, I><<<pgrid, PW_WARPS * 32, psmem, s>>>(S, n, koff, tb, wsel, sum_w0, sum_words, \
+						M ? out : nullptr, M ? counts : nullptr, M ? acc : acc + 1, M ? -1 : sum_col, ctx->d_status, \
+						dlo, dhi, run); } while (0)
+				if (materialize) {
+					if (mode == 2) { if (items == 8) PW_LAUNCH(true, 2, 8); else PW_LAUNCH(true, 2, 4); }
+					else if (mode == 1) { if (items == 8) PW_LAUNCH(true, 1, 8); else PW_LAUNCH(true, 1, 4); }
+					else PW_LAUNCH(true, 0, 4);
+				} else {
+					if (mode == 2) { if (items == 8) PW_LAUNCH(false, 2, 8); else PW_LAUNCH(false, 2, 4); }
+					else if (mode == 1) { if (items == 8) PW_LAUNCH(false, 1, 8); else PW_LAUNCH(false, 1, 4); }
+					else PW_LAUNCH(false, 0, 4);
+				}
 #undef PW_LAUNCH
-			PG_LAUNCHED(ctx);
+				PG_LAUNCHED(ctx);
+			}
 			if (positional) *positional = materialize;
 			return PG_OK;
 		}
@@ -1137,10 +1217,12 @@ static int hj_compact(pg_ctx* ctx, cudaStream_t s, char* out, uint64_t n, uint64
 	char* tmp = nullptr;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &offs, nchunks * 8))) return rc;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &tmp, std::max<uint64_t>(total, 1) * 16))) return rc;
-	PG_CUDA(ctx, cudaMemcpyAsync(offs, counts, nchunks * 8, cudaMemcpyDeviceToDevice, s));
+	k_chunk_totals<<<(int) std::min<uint64_t>(pg_div_up(nchunks, 256), (uint64_t) ctx->sm_count * 8), 256, 0, s>>>(
+			counts, offs, nchunks, n);
+	PG_LAUNCHED(ctx);
 	if ((rc = pg_scan_u64(ctx, s, offs, nchunks, nullptr))) return rc;
 	const int grid = (int) std::min<uint64_t>(nchunks, (uint64_t) ctx->sm_count * 16);
-	k_compact_chunks<<<grid, 256, 0, s>>>(reinterpret_cast<const uint4*>(out), counts, offs, nchunks,
+	k_compact_chunks<<<grid, 256, 0, s>>>(reinterpret_cast<const uint4*>(out), counts, offs, nchunks, n,
 			reinterpret_cast<uint4*>(tmp), total);
 	PG_LAUNCHED(ctx);
 	if (total) PG_CUDA(ctx, cudaMemcpyAsync(out, tmp, total * 16, cudaMemcpyDeviceToDevice, s));

@@ -219,6 +219,20 @@ __device__ __forceinline__ uint64_t pg_policy_evict_first()
 	return p;
 }
 
+__device__ __forceinline__ uint64_t pg_policy_evict_normal()
+{
+	uint64_t p;
+	asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+	return p;
+}
+
+__device__ __forceinline__ uint64_t pg_policy_evict_unchanged()
+{
+	uint64_t p;
+	asm volatile("createpolicy.fractional.L2::evict_unchanged.b64 %0, 1.0;" : "=l"(p));
+	return p;
+}
+
 __device__ __forceinline__ uint64_t pg_policy_evict_last()
 {
 	uint64_t p;

@@ -150,6 +150,25 @@ def test_join_dense_keys_wide_values(ctx):
     _join_check(ctx, R, S)
 
 
+@pytest.mark.parametrize("knobs", [dict(probe_items=8), dict(probe_cache=1), dict(probe_cache=14), dict(probe_passes=2), dict(probe_passes=2, probe_items=8), dict(probe_passes=1)])
+def test_join_probe_launch_shapes(ctx, knobs):
+    # Lookups in flight per lane and the L2 persisting window change speed,
+    # never rows: narrow and wide dense tables, with misses (compaction) and
+    # a ragged tail (n not a multiple of the 256-tuple block).
+    R = dg.build_relation(70_001, dg.seed_for(23))
+    S = dg.probe_uniform(555_555, R, dg.seed_for(24))
+    S[::97, 0] += 200_000
+    Rw = R.copy()
+    Rw[:, 1] = dg.raw_words(dg.seed_for(23), 1, 70_001).view(np.int64)
+    try:
+        ctx.tune(**knobs)
+        _join_check(ctx, R, S)
+        _join_check(ctx, Rw, S)
+        _join_check(ctx, R, S[:1000])
+    finally:
+        ctx.tune(probe_items=0, probe_cache=0, probe_passes=0)
+
+
 def test_join_many_to_many(ctx):
     R = dg.uniform_keys(5000, 700, dg.seed_for(5))
     S = dg.uniform_keys(9000, 900, dg.seed_for(6))
