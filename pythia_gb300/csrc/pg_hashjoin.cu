@@ -772,6 +772,125 @@ k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 	if (lane == 0) { atomicAdd(&agg[0], cnt_acc); if (!MATERIALIZE) atomicAdd(&agg[1], sum_acc); }
 }
 
+// ---------------------------------------------------------------------------
+// Dense-table probe of 16-byte tuples straight from global memory into
+// registers: the same warp-owned 128-tuple chunks, positional output and
+// two-pass runs as k_probe16_warp, but each lane loads its four tuples with
+// 16-byte loads (a warp instruction covers 512 contiguous bytes) and the next
+// chunk's loads are issued before the current chunk's table lookups, so a
+// warp keeps eight tuple loads and four lookups in flight without shared
+// memory or barriers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 hj_ld_stream(const char* p, uint64_t pol)
+{
+	uint4 v;
+	asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+			: "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p), "l"(pol));
+	return v;
+}
+
+__device__ __forceinline__ void hj_st_stream(char* p, uint4 v, uint64_t pol)
+{
+	asm volatile("st.global.L1::no_allocate.L2::cache_hint.v4.u32 [%0], {%1,%2,%3,%4}, %5;"
+			:: "l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol));
+}
+
+template <bool MATERIALIZE, int MODE, bool PF>
+__global__ void __launch_bounds__(PW_WARPS * 32, PF ? 4 : 5)
+k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb,
+		uint32_t wsel, uint32_t sum_w0, uint32_t sum_words, char* __restrict__ out,
+		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg,
+		int sum_col, uint64_t dlo, uint64_t dhi, int run)
+{
+	static_assert(MODE == 1 || MODE == 2, "dense tables only");
+	constexpr int ITEMS = PW_CHUNK / 32;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
+	const uint64_t W = (uint64_t) gridDim.x * PW_WARPS;
+	const uint64_t first = (uint64_t) blockIdx.x * PW_WARPS + warp;
+	const uint32_t tp_ = tb.cache & 3;
+	const uint64_t keep = tp_ == 0 ? pg_policy_evict_last() : tp_ == 1 ? pg_policy_evict_normal()
+		: tp_ == 2 ? pg_policy_evict_unchanged() : pg_policy_evict_first();
+	const uint64_t instream = (tb.cache & 4) ? pg_policy_evict_normal() : pg_policy_evict_first();
+	const uint64_t stream = (tb.cache & 8) ? pg_policy_evict_normal() : pg_policy_evict_first();
+	const uint32_t w0 = wsel & 15, w1 = (wsel >> 4) & 15, w2 = (wsel >> 8) & 15, w3 = (wsel >> 12) & 15;
+	unsigned long long cnt_acc = 0, sum_acc = 0;
+	if (first >= nchunks) return;
+	uint4 cur[ITEMS], nxt[ITEMS];
+	auto load = [&](uint64_t c, uint4 (&t)[ITEMS]) {
+		const uint32_t rows = (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK);
+		#pragma unroll
+		for (int j = 0; j < ITEMS; ++j) {
+			const uint32_t p = j * 32 + lane;
+			t[j] = p < rows ? hj_ld_stream(S + (c * PW_CHUNK + p) * 16, instream) : make_uint4(0, 0, 0, 0);
+		}
+	};
+	if (PF) load(first, cur);
+	for (uint64_t c = first; c < nchunks; c += W) {
+		if (PF) { if (c + W < nchunks) load(c + W, nxt); }
+		else load(c, cur);
+		const uint32_t rows = (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK);
+		// Narrow tables keep the 4-byte entry (all ones: absent); wide ones
+		// the 8-byte value and the presence bit.
+		uint32_t e32[ITEMS], pres[ITEMS];
+		uint64_t v64[ITEMS];
+		#pragma unroll
+		for (int j = 0; j < ITEMS; ++j) {
+			const uint32_t p = j * 32 + lane;
+			e32[j] = 0xFFFFFFFFu; pres[j] = 0; v64[j] = 0;
+			const uint4 t = cur[j];
+			const int64_t key = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
+			const unsigned long long d = (unsigned long long) key - (unsigned long long) tb.dmin;
+			if (p < rows && d >= dlo && d < dhi) {
+				if (MODE == 2) {
+					asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;"
+							: "=r"(e32[j]) : "l"(tb.dense32 + d), "l"(keep));
+				} else {
+					pres[j] = __ldg(tb.dense_bits + (d >> 5)) >> (d & 31);
+					asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u64 %0, [%1], %2;"
+							: "=l"(v64[j]) : "l"(tb.dense_val + d), "l"(keep));
+				}
+			}
+		}
+		uint32_t rank = 0;
+		#pragma unroll
+		for (int j = 0; j < ITEMS; ++j) {
+			const bool h = MODE == 2 ? e32[j] != 0xFFFFFFFFu : (pres[j] & 1) != 0;
+			const uint32_t ball = __ballot_sync(0xffffffffu, h);
+			if (h) {
+				const uint64_t v = MODE == 2 ? tb.vmin + e32[j] : v64[j];
+				const uint4 t = cur[j];
+				if (MATERIALIZE) {
+					const uint32_t r = rank + __popc(ball & ((1u << lane) - 1));
+					const uint64_t row = run == 1 ? c * PW_CHUNK + rows - 1 - r : c * PW_CHUNK + r;
+					hj_st_stream(out + row * 16, make_uint4(hj_pick(t, v, w0), hj_pick(t, v, w1),
+							hj_pick(t, v, w2), hj_pick(t, v, w3)), stream);
+				} else if (sum_col >= 0) {
+					const uint32_t lo = hj_pick(t, v, (wsel >> (4 * sum_w0)) & 15);
+					if (sum_words == 2)
+						sum_acc += ((unsigned long long) hj_pick(t, v, (wsel >> (4 * sum_w0 + 4)) & 15) << 32) | lo;
+					else sum_acc += (unsigned long long) (long long) (int32_t) lo;
+				}
+			}
+			rank += __popc(ball);
+		}
+		cnt_acc += rank;
+		if (MATERIALIZE && lane == 0) {
+			if (run < 0) chunk_counts[c] = rank;
+			else reinterpret_cast<uint32_t*>(chunk_counts)[2 * c + run] = rank;
+		}
+		if (PF) {
+			#pragma unroll
+			for (int j = 0; j < ITEMS; ++j) cur[j] = nxt[j];
+		}
+	}
+	if (!MATERIALIZE) {
+		#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) sum_acc += __shfl_down_sync(0xffffffffu, sum_acc, o);
+	}
+	if (lane == 0) { atomicAdd(&agg[0], cnt_acc); if (!MATERIALIZE) atomicAdd(&agg[1], sum_acc); }
+}
+
 // Positional probe output: the 128-tuple chunk c (rows_c = min(128, n - 128c)
 // probe tuples) holds lo = counts[c] & 0xffffffff rows at its front,
 // [128c, 128c + lo), and hi = counts[c] >> 32 rows at its back,
@@ -1158,13 +1277,39 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 			// 2 two passes, 0 by table size).
 			const uint64_t tbytes = mode == 2 ? ht->drange * 4 : ht->drange * 8;
 			const int64_t pk = ctx->tune[PG_TUNE_PROBE_PASSES];
+			// Dense tables take the register-loading probe unless the knob asks
+			// for the staged one (1) or the non-prefetching one (4).
+			const int64_t var = ctx->tune[PG_TUNE_PROBE_VARIANT];
+			const bool direct = mode != 0 && (var == 0 || var == 3 || var == 4);
 			const int passes = mode == 0 || pk == 1 ? 1
-				: (pk == 2 || (tbytes > HJ_TWO_PASS_MIN_BYTES && tbytes <= HJ_TWO_PASS_MAX_BYTES)) ? 2 : 1;
+				: (pk == 2 || (!direct && tbytes > HJ_TWO_PASS_MIN_BYTES && tbytes <= HJ_TWO_PASS_MAX_BYTES)) ? 2 : 1;
 			const uint64_t dr = mode == 0 ? 0 : ht->drange;
 			for (int pass = 0; pass < passes; ++pass) {
 				const int run = passes == 1 ? -1 : pass;
 				const uint64_t dlo = passes == 1 ? 0 : (pass == 0 ? 0 : dr / 2);
 				const uint64_t dhi = passes == 1 ? dr : (pass == 0 ? dr / 2 : dr);
+				if (direct) {
+					// Grids of several waves (4 CTAs of 8 warps resident per SM):
+					// 24 CTAs per SM with prefetch, 80 without, measured best on
+					// the 16M x 256M join; each warp adds its count once.
+					const uint64_t wchunks = pg_div_up(pg_div_up(n, PW_CHUNK), PW_WARPS);
+					const bool pf = var != 4;
+					const int64_t want = ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] > 0
+						? std::min<int64_t>(1 << 14, ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM]) : (pf ? 24 : 80);
+					const int dgrid = (int) std::min<uint64_t>(wchunks, (uint64_t) ctx->sm_count * want);
+#define PD_LAUNCH(M, D, P) k_probe16_direct<M, D, P><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, wsel, sum_w0, \
+						sum_words, M ? out : nullptr, M ? counts : nullptr, M ? acc : acc + 1, M ? -1 : sum_col, dlo, dhi, run)
+					if (materialize) {
+						if (mode == 2) { if (pf) PD_LAUNCH(true, 2, true); else PD_LAUNCH(true, 2, false); }
+						else { if (pf) PD_LAUNCH(true, 1, true); else PD_LAUNCH(true, 1, false); }
+					} else {
+						if (mode == 2) { if (pf) PD_LAUNCH(false, 2, true); else PD_LAUNCH(false, 2, false); }
+						else { if (pf) PD_LAUNCH(false, 1, true); else PD_LAUNCH(false, 1, false); }
+					}
+#undef PD_LAUNCH
+					PG_LAUNCHED(ctx);
+					continue;
+				}
 #define PW_LAUNCH(M, D, I) do { \
 				PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_warp<M, D, I>, cudaFuncAttributeMaxDynamicSharedMemorySize, psmem)); \
 				k_probe16_warp<M, D, I><<<pgrid, PW_WARPS * 32, psmem, s>>>(S, n, koff, tb, wsel, sum_w0, sum_words, \

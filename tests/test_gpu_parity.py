@@ -150,11 +150,15 @@ def test_join_dense_keys_wide_values(ctx):
     _join_check(ctx, R, S)
 
 
-@pytest.mark.parametrize("knobs", [dict(probe_items=8), dict(probe_cache=1), dict(probe_cache=14), dict(probe_passes=2), dict(probe_passes=2, probe_items=8), dict(probe_passes=1)])
+@pytest.mark.parametrize("knobs", [dict(probe_variant=1), dict(probe_variant=1, probe_items=8),
+                                   dict(probe_variant=1, probe_passes=2, probe_items=8), dict(probe_cache=1),
+                                   dict(probe_cache=14), dict(probe_passes=2), dict(probe_variant=4),
+                                   dict(probe_variant=4, probe_passes=2, probe_ctas_per_sm=5),
+                                   dict(probe_variant=2)])
 def test_join_probe_launch_shapes(ctx, knobs):
-    # Lookups in flight per lane and the L2 persisting window change speed,
-    # never rows: narrow and wide dense tables, with misses (compaction) and
-    # a ragged tail (n not a multiple of the 256-tuple block).
+    # Probe kernel variants, lookups in flight, L2 policies, passes and grid
+    # shapes change speed, never rows: narrow and wide dense tables, with
+    # misses (compaction) and a ragged tail (n not a multiple of 256).
     R = dg.build_relation(70_001, dg.seed_for(23))
     S = dg.probe_uniform(555_555, R, dg.seed_for(24))
     S[::97, 0] += 200_000
@@ -166,7 +170,7 @@ def test_join_probe_launch_shapes(ctx, knobs):
         _join_check(ctx, Rw, S)
         _join_check(ctx, R, S[:1000])
     finally:
-        ctx.tune(probe_items=0, probe_cache=0, probe_passes=0)
+        ctx.tune(probe_items=0, probe_cache=0, probe_passes=0, probe_variant=0, probe_ctas_per_sm=0)
 
 
 def test_join_many_to_many(ctx):
