@@ -343,7 +343,7 @@ def run_gpu(args, ws, rank, local):
                 "e2e": {"value": ws * (NR + NS) / (e2e / 1e3), "unit": "tuples/s",
                         "h2d_bytes_per_step": (NR + NS) * TUPLE, "d2h_bytes_per_step": NS * TUPLE,
                         "ms_per_step": e2e},
-                "roofline": {"bound": "hbm", "kernel": "k_probe16_warp (materialise)",
+                "roofline": {"bound": "hbm", "kernel": "k_probe16_direct (materialise)",
                              "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
                              "peak_source": peak_kind, "probe_ms": probe,

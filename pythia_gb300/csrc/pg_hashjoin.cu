@@ -206,6 +206,91 @@ __global__ void k_dense32_build(const char* __restrict__ R, uint64_t n, uint32_t
 	if (dup) atomicOr(flags, 1);
 }
 
+// 16-byte build tuples (8-byte key at word 0 or 2, 16-byte aligned): one
+// vector load per tuple, four tuples in flight per thread.
+__device__ __forceinline__ uint32_t hj_word4(const uint4& t, uint32_t i)
+{
+	return i == 0 ? t.x : i == 1 ? t.y : i == 2 ? t.z : t.w;
+}
+
+__device__ __forceinline__ uint64_t hj_pack_value16(const uint4& t, const HjBuildCols& bc)
+{
+	uint32_t w[2] = {0, 0};
+	int o = 0;
+	for (int c = 0; c < bc.n; ++c)
+		for (int j = 0; j < bc.words[c]; ++j) w[o++] = hj_word4(t, bc.roff[c] + j);
+	return ((uint64_t) w[1] << 32) | w[0];
+}
+
+__global__ void k_key_minmax16(const uint4* __restrict__ R, uint64_t n, uint32_t kw, HjBuildCols bc,
+		unsigned long long* __restrict__ mm)
+{
+	unsigned long long lo = ~0ull, hi = 0, vlo = ~0ull, vhi = 0;
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	for (uint64_t i0 = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+		uint4 t[4];
+		#pragma unroll
+		for (int u = 0; u < 4; ++u) if (i0 + u * stride < n) t[u] = __ldg(R + i0 + u * stride);
+		#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			if (i0 + u * stride >= n) break;
+			const unsigned long long key = ((unsigned long long) hj_word4(t[u], kw + 1) << 32) | hj_word4(t[u], kw);
+			const unsigned long long k = key ^ (1ull << 63);
+			const unsigned long long v = hj_pack_value16(t[u], bc);
+			lo = k < lo ? k : lo; hi = k > hi ? k : hi;
+			vlo = v < vlo ? v : vlo; vhi = v > vhi ? v : vhi;
+		}
+	}
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		unsigned long long a = __shfl_down_sync(0xffffffffu, lo, o), b = __shfl_down_sync(0xffffffffu, hi, o);
+		unsigned long long c = __shfl_down_sync(0xffffffffu, vlo, o), d = __shfl_down_sync(0xffffffffu, vhi, o);
+		lo = a < lo ? a : lo; hi = b > hi ? b : hi;
+		vlo = c < vlo ? c : vlo; vhi = d > vhi ? d : vhi;
+	}
+	if ((threadIdx.x & 31) == 0) {
+		atomicMin(&mm[0], lo); atomicMax(&mm[1], hi);
+		atomicMin(&mm[2], vlo); atomicMax(&mm[3], vhi);
+	}
+}
+
+// Narrow dense table from 16-byte tuples with plain stores; duplicates are
+// found afterwards by counting present entries (k_dense32_count < n).
+__global__ void k_dense32_store16(const uint4* __restrict__ R, uint64_t n, uint32_t kw, HjBuildCols bc,
+		long long dmin, unsigned long long vmin, uint32_t* __restrict__ table)
+{
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	for (uint64_t i0 = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+		uint4 t[4];
+		#pragma unroll
+		for (int u = 0; u < 4; ++u) if (i0 + u * stride < n) t[u] = __ldg(R + i0 + u * stride);
+		#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			if (i0 + u * stride >= n) break;
+			const unsigned long long key = ((unsigned long long) hj_word4(t[u], kw + 1) << 32) | hj_word4(t[u], kw);
+			table[key - (unsigned long long) dmin] = (uint32_t) (hj_pack_value16(t[u], bc) - vmin);
+		}
+	}
+}
+
+// Present entries (not all ones) of a narrow dense table of `range` entries.
+__global__ void k_dense32_count(const uint32_t* __restrict__ table, uint64_t range, unsigned long long* __restrict__ cnt)
+{
+	unsigned long long c = 0;
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	const uint64_t n4 = range / 4;
+	const uint4* t4 = reinterpret_cast<const uint4*>(table);
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n4; i += stride) {
+		const uint4 v = t4[i];
+		c += (v.x != 0xFFFFFFFFu) + (v.y != 0xFFFFFFFFu) + (v.z != 0xFFFFFFFFu) + (v.w != 0xFFFFFFFFu);
+	}
+	for (uint64_t i = 4 * n4 + blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < range; i += stride)
+		c += table[i] != 0xFFFFFFFFu;
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+	if ((threadIdx.x & 31) == 0 && c) atomicAdd(cnt, c);
+}
+
 // Dense table: presence bit and value at key - dmin. A bit found already set
 // means a duplicate key; the host then builds the hashed table instead.
 __global__ void k_dense_build(const char* __restrict__ R, uint64_t n, uint32_t W, uint32_t koff,
@@ -1112,8 +1197,16 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 		unsigned long long init[4] = {~0ull, 0, ~0ull, 0};
 		PG_CUDA(ctx, cudaMemcpyAsync(mm, init, 32, cudaMemcpyHostToDevice, s));
 		int blocks = (int) std::min<uint64_t>(pg_div_up(R->n, 256), (uint64_t) ctx->sm_count * 8);
-		k_key_minmax<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off, R->key_bytes,
-				ht->bcols, mm);
+		bool vec16 = R->width == 16 && (R->key_off == 0 || R->key_off == 8) && R->key_bytes == 8 &&
+			(reinterpret_cast<uintptr_t>(R->data) & 15) == 0;
+		for (int c = 0; c < ht->bcols.n; ++c) vec16 = vec16 && ht->bcols.roff[c] + ht->bcols.words[c] <= 4;
+		const uint32_t kw = R->key_off / 4;
+		const int vblocks = (int) std::min<uint64_t>(pg_div_up(R->n, 4 * 256), (uint64_t) ctx->sm_count * 8);
+		if (vec16)
+			k_key_minmax16<<<vblocks, 256, 0, s>>>((const uint4*) R->data, R->n, kw, ht->bcols, mm);
+		else
+			k_key_minmax<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off, R->key_bytes,
+					ht->bcols, mm);
 		PG_LAUNCHED(ctx);
 		unsigned long long h[4];
 		PG_CUDA(ctx, cudaMemcpyAsync(h, mm, 32, cudaMemcpyDeviceToHost, s));
@@ -1123,12 +1216,24 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 		const bool narrow = h[3] - h[2] < 0xFFFFFFFFull;
 		if (range != 0 && range <= std::max<uint64_t>(2 * R->n, 64) && range < (1ull << 34)) {
 			int* dupflag_dev = reinterpret_cast<int*>(mm + 4);
-			PG_CUDA(ctx, cudaMemsetAsync(dupflag_dev, 0, 8, s));
+			unsigned long long* present = mm + 5;
+			PG_CUDA(ctx, cudaMemsetAsync(dupflag_dev, 0, 16, s));
+			bool counted = false;
 			if (narrow) {
 				if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense32, range * 4))) { delete ht; return rc; }
 				PG_CUDA(ctx, cudaMemsetAsync(ht->dense32, 0xFF, range * 4, s));
-				k_dense32_build<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off,
-						R->key_bytes, ht->bcols, kmin, h[2], ht->dense32, dupflag_dev);
+				if (vec16) {
+					// Plain stores; a duplicate key leaves fewer than |R| entries.
+					k_dense32_store16<<<vblocks, 256, 0, s>>>((const uint4*) R->data, R->n, kw, ht->bcols, kmin, h[2],
+							ht->dense32);
+					PG_LAUNCHED(ctx);
+					k_dense32_count<<<(int) std::min<uint64_t>(pg_div_up(range, 4 * 256), (uint64_t) ctx->sm_count * 8),
+							256, 0, s>>>(ht->dense32, range, present);
+					counted = true;
+				} else {
+					k_dense32_build<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off,
+							R->key_bytes, ht->bcols, kmin, h[2], ht->dense32, dupflag_dev);
+				}
 			} else {
 				const uint64_t words = pg_div_up(range, 32);
 				if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense_val, range * 8))) { delete ht; return rc; }
@@ -1138,10 +1243,11 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 						R->key_bytes, ht->bcols, ht->inline_val, kmin, ht->dense_val, ht->dense_bits, dupflag_dev);
 			}
 			PG_LAUNCHED(ctx);
-			int dupflag = 0;
-			PG_CUDA(ctx, cudaMemcpyAsync(&dupflag, dupflag_dev, 4, cudaMemcpyDeviceToHost, s));
+			unsigned long long dh[2] = {0, 0};    // [dup flag word, present entries]
+			PG_CUDA(ctx, cudaMemcpyAsync(dh, dupflag_dev, 16, cudaMemcpyDeviceToHost, s));
 			PG_CUDA(ctx, cudaStreamSynchronize(s));
-			if (!dupflag) {
+			const bool dup = counted ? dh[1] != R->n : (dh[0] & 0xFFFFFFFFull) != 0;
+			if (!dup) {
 				ht->dense = true; ht->unique = true; ht->dmin = kmin; ht->drange = range; ht->vmin = h[2];
 				ht->slots = nullptr; ht->side = nullptr; ht->nside = 0; ht->log2cap = 1; ht->capacity = 0;
 				pg_free_async(ctx, s, mm);

@@ -173,6 +173,16 @@ def test_join_probe_launch_shapes(ctx, knobs):
         ctx.tune(probe_items=0, probe_cache=0, probe_passes=0, probe_variant=0, probe_ctas_per_sm=0)
 
 
+def test_join_dense_keys_with_repeated_rows(ctx):
+    # A dense key domain whose build side repeats whole rows (same key and
+    # payload) must still join every copy: the dense build detects repeats by
+    # counting present entries and falls back to the hashed table.
+    R = dg.build_relation(20_000, dg.seed_for(25))
+    R = np.concatenate([R, R[:3], R[100:101]])
+    S = dg.probe_uniform(200_000, R[:20_000], dg.seed_for(26))
+    _join_check(ctx, R, S)
+
+
 def test_join_many_to_many(ctx):
     R = dg.uniform_keys(5000, 700, dg.seed_for(5))
     S = dg.uniform_keys(9000, 900, dg.seed_for(6))
