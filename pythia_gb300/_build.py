@@ -14,7 +14,7 @@ import subprocess
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
-HOST = os.path.join(PKG, "host")
+GPUOPS = os.path.join(PKG, "gpuops")
 BUILD = os.path.join(PKG, "_build")
 GENCODE = "arch=compute_103a,code=sm_103a"
 
@@ -85,19 +85,19 @@ def build_datagen():
 
 
 def build_host():
-    """C++ operator layer (Gpu*Op classes) linked against libpythia_gpu.so."""
-    if not os.path.isdir(HOST):
-        return None
-    srcs = sorted(os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".cpp"))
-    if not srcs:
-        return None
+    """C++ operator layer (Gpu*Op classes, gpuops/) on the mirror of the
+    engine's operator interface, with the plan runner, linked against
+    libpythia_gpu.so. C++98 like the engine, so the same operator source also
+    compiles against the engine's own headers (oracle/Makefile.ref)."""
+    srcs = [os.path.join(GPUOPS, "mirror", "pythia_mirror.cpp"), os.path.join(GPUOPS, "gpuops.cpp"),
+            os.path.join(GPUOPS, "harness.cpp")]
     lib = os.path.join(PKG, "libpythia_gpuops.so")
-    deps = srcs + [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")]
+    deps = srcs + [os.path.join(GPUOPS, "gpuops.h"), os.path.join(GPUOPS, "mirror", "pythia_mirror.h")]
     deps += _headers() + [os.path.join(PKG, "libpythia_gpu.so")]
     if _stale(lib, deps):
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall",
-              "-I" + os.path.join(ROOT, "include"), "-I" + HOST] + srcs +
-             ["-L" + PKG, "-lpythia_gpu", "-Wl,-rpath,$ORIGIN", "-lpthread", "-o", lib])
+        _run(["g++", "-O2", "-std=gnu++98", "-fPIC", "-shared", "-pthread", "-Wall", "-Wno-unused-parameter",
+              "-I" + os.path.join(ROOT, "include"), "-I" + GPUOPS] + srcs +
+             ["-L" + PKG, "-lpythia_gpu", "-Wl,-rpath,$ORIGIN", "-o", lib])
     return lib
 
 
@@ -117,9 +117,9 @@ def build_oracle():
 
 def build_all(verbose=False):
     build_datagen()
-    build_oracle()
     build_gpu(verbose=verbose)
     build_host()
+    build_oracle()      # after libpythia_gpu: the reference build links the operators against it
 
 
 if __name__ == "__main__":

@@ -1,0 +1,87 @@
+"""Pythia plans with GPU operators, run through the C++ operator layer.
+
+The plan is libconfig text as the engine reads it: `buffsize`, `treeroot`
+naming the root node, one top-level group per node with its `type` and keys,
+`input` (single-input) or `build` / `probe` (dual-input) naming children. GPU
+operator types: gpuhashjoin, gpumpsmjoin, gpupartition, gpuaggregate_sum,
+gpuaggregate_count (libpythia_gpuops, pythia_gb300/gpuops/). Leaves are
+`memscan` nodes over relations registered from numpy arrays: thread t of T
+reads rows [t n / T, (t + 1) n / T).
+
+    plans.register("R", R)                 # (n, width) uint8 / int64 rows
+    out, per_thread = plans.run(PLAN, threads=4)
+
+`run` returns every thread's output tuples in thread order as one
+(rows, tuple_size) uint8 array and the per-thread row counts. An operator
+that returns Error (a GPU failure, or no GPU at all: there is no CPU path)
+raises PlanError with code 1; a plan the operators refuse raises code 2.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_LIB = None
+_KEEP = {}          # registered arrays stay alive while plans may read them
+
+
+class PlanError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"plan failed ({code}): {msg}")
+        self.code = code
+
+
+def lib_path():
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "libpythia_gpuops.so")
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: build it with __graft_entry__.build()")
+        L = ctypes.CDLL(path)
+        L.pgo_register.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_uint]
+        L.pgo_register.restype = ctypes.c_int
+        L.pgo_run.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                              ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint),
+                              ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_char_p, ctypes.c_int]
+        L.pgo_run.restype = ctypes.c_int
+        L.pgo_free.argtypes = [ctypes.c_void_p]
+        L.pgo_free.restype = None
+        _LIB = L
+    return _LIB
+
+
+def register(name, rows):
+    """Makes `rows` (a C-contiguous 2-D array, one row per tuple) readable by
+    memscan nodes with `relation = name`."""
+    a = np.ascontiguousarray(rows)
+    if a.ndim != 2:
+        raise ValueError("rows must be 2-D")
+    width = a.shape[1] * a.itemsize
+    _KEEP[name] = a
+    if lib().pgo_register(name.encode(), a.ctypes.data if a.size else None, a.shape[0], width):
+        raise ValueError("pgo_register refused the relation")
+
+
+def run(plan, threads=1):
+    out = ctypes.c_void_p()
+    nbytes = ctypes.c_ulonglong()
+    tsize = ctypes.c_uint()
+    per = (ctypes.c_ulonglong * threads)()
+    err = ctypes.create_string_buffer(1024)
+    rc = lib().pgo_run(plan.encode(), threads, ctypes.byref(out), ctypes.byref(nbytes), ctypes.byref(tsize),
+                       per, err, len(err))
+    try:
+        if rc:
+            raise PlanError(rc, err.value.decode(errors="replace"))
+        w = tsize.value
+        buf = np.frombuffer(ctypes.string_at(out.value, nbytes.value), dtype=np.uint8).copy() \
+            if nbytes.value else np.zeros(0, np.uint8)
+        rows = buf.reshape(-1, w) if w else buf.reshape(0, 0)
+        return rows, [int(per[t]) // max(w, 1) for t in range(threads)]
+    finally:
+        if out.value:
+            lib().pgo_free(out)
