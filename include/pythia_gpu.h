@@ -123,6 +123,9 @@ enum {
 	                                    1 normal, 2 unchanged, 3 first), bit 2 probe reads and bit 3
 	                                    output stores normal instead of evict-first */
 	PG_TUNE_PROBE_PASSES = 8,        /* dense-table probe passes: 1, 2 (half the table each), 0 by size */
+	PG_TUNE_GROUPBY_PATH = 9,        /* group-by: 0 by key range and size, 1 hashed global table, 2 partitioned,
+	                                    3 hashed global without warp combining, 4 partitioned without warp
+	                                    combining, 6 dense when the key range allows */
 	PG_TUNE_COUNT = 12
 };
 int pg_tune_set(pg_ctx* ctx, int knob, int64_t value);

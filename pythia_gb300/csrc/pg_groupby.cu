@@ -38,15 +38,35 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
 	e = (a - (s - bb)) + (b - bb);
 }
 
-// Adds v into (hi, lo) with one atomic on hi and one on lo when the addition
-// rounded.
+// Exact rounding error of s = a + b by Dekker's Fast2Sum (3 FP64 adds: the
+// larger operand first). The magnitudes are ordered by an integer compare of
+// the bit patterns, and the zero test below is an integer test too: on this
+// GPU the FP64 pipe is narrow and the dominant cost of a compensated
+// aggregation, so only the three additions use it.
+__device__ __forceinline__ void fast_two_sum(double a, double b, double& s, double& e)
+{
+	const unsigned long long ma = (unsigned long long) __double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFull;
+	const unsigned long long mb = (unsigned long long) __double_as_longlong(b) & 0x7FFFFFFFFFFFFFFFull;
+	const double big = ma >= mb ? a : b, small = ma >= mb ? b : a;
+	s = a + b;
+	e = small - (s - big);
+}
+
+__device__ __forceinline__ bool nonzero(double x)
+{
+	return ((unsigned long long) __double_as_longlong(x) << 1) != 0;
+}
+
+// Adds v (+ compensation c) into (hi, lo): one atomic on hi, whose old value
+// gives the rounding error of this addition exactly, and one on lo when that
+// error (plus c) is not zero.
 __device__ __forceinline__ void atomic_comp_add(double* hi, double* lo, double v, double c)
 {
 	double old = atomicAdd(hi, v);
 	double s, e;
-	two_sum(old, v, s, e);
-	e += c;
-	if (e != 0.0) atomicAdd(lo, e);
+	fast_two_sum(old, v, s, e);
+	if (nonzero(c)) e += c;
+	if (nonzero(e)) atomicAdd(lo, e);
 }
 
 template <int VT, int AGG>
@@ -183,8 +203,7 @@ k_gb_insert(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, 
 // their key loads, slot reads and accumulator atomics are issued together, so
 // the chains of dependent L2 round trips overlap instead of running one row
 // at a time.
-#define GB_ILP 4
-template <int VT, int AGG>
+template <int VT, int AGG, bool MATCH, int GB_ILP>
 __global__ void __launch_bounds__(GB_THREADS)
 k_gb_insert_ilp(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes,
 		uint32_t voff, GbTable t, int* __restrict__ status)
@@ -213,11 +232,15 @@ k_gb_insert_ilp(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t ko
 				else if (VT == PG_VAL_LONG) iv[j] = (unsigned long long) pg_load_key(r + voff, 8);
 				else dv[j] = __longlong_as_double(pg_load_key(r + voff, 8));
 			}
-			const uint32_t active = __ballot_sync(0xffffffffu, valid);
-			if (valid) {
-				const uint32_t peers = __match_any_sync(active, (unsigned long long) k[j]);
-				warp_combine<VT, AGG>(peers, lane, iv[j], dv[j], dc[j]);
-				lead[j] = lane == __ffs(peers) - 1;
+			if (MATCH) {
+				const uint32_t active = __ballot_sync(0xffffffffu, valid);
+				if (valid) {
+					const uint32_t peers = __match_any_sync(active, (unsigned long long) k[j]);
+					warp_combine<VT, AGG>(peers, lane, iv[j], dv[j], dc[j]);
+					lead[j] = lane == __ffs(peers) - 1;
+				}
+			} else {
+				lead[j] = valid;
 			}
 		}
 		uint64_t slot[GB_ILP];
@@ -257,9 +280,9 @@ k_gb_insert_ilp(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t ko
 			for (int j = 0; j < GB_ILP; ++j) {
 				if (!lead[j]) continue;
 				double sres, e;
-				two_sum(old[j], dv[j], sres, e);
-				e += dc[j];
-				if (e != 0.0) atomicAdd(&t.lo[slot[j]], e);
+				fast_two_sum(old[j], dv[j], sres, e);
+				if (MATCH && nonzero(dc[j])) e += dc[j];
+				if (nonzero(e)) atomicAdd(&t.lo[slot[j]], e);
 			}
 		} else {
 			#pragma unroll
@@ -313,7 +336,7 @@ __device__ __forceinline__ void gb_write_row(char* o, uint32_t kbytes, int64_t k
 	reinterpret_cast<uint32_t*>(o)[1] = (uint32_t) (a >> 32);
 }
 
-template <int VT, int AGG>
+template <int VT, int AGG, bool MATCH>
 __global__ void __launch_bounds__(GBP_THREADS)
 k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, uint32_t P, uint32_t W,
 		uint32_t koff, uint32_t kbytes, uint32_t voff, GbTable t, char* __restrict__ out, uint64_t out_cap,
@@ -349,11 +372,15 @@ k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, 
 				else if (VT == PG_VAL_LONG) iv = (unsigned long long) pg_load_key(r + voff, 8);
 				else dv = __longlong_as_double(pg_load_key(r + voff, 8));
 			}
-			const uint32_t active = __ballot_sync(0xffffffffu, valid);
-			if (!valid) continue;
-			const uint32_t peers = __match_any_sync(active, (unsigned long long) k);
-			warp_combine<VT, AGG>(peers, lane, iv, dv, dc);
-			if (lane != __ffs(peers) - 1) continue;
+			if (MATCH) {
+				const uint32_t active = __ballot_sync(0xffffffffu, valid);
+				if (!valid) continue;
+				const uint32_t peers = __match_any_sync(active, (unsigned long long) k);
+				warp_combine<VT, AGG>(peers, lane, iv, dv, dc);
+				if (lane != __ffs(peers) - 1) continue;
+			} else if (!valid) {
+				continue;
+			}
 			const uint32_t s = gbp_slot(skeys, k, &s_sent);
 			if (s != UINT32_MAX) { fold_slot<VT, AGG>(sacc, slo, s, iv, dv, dc); continue; }
 			// Shared table full: this key lives in the global table.
@@ -438,11 +465,205 @@ __global__ void k_gb_emit(GbTable t, uint32_t kbytes, char* __restrict__ out, ui
 	}
 }
 
+// ---------------------------------------------------------------------------
+// Dense key domain (keys span at most a few times the group count, e.g.
+// group numbers 0..G-1 or surrogate keys): a min/max pass, then the slot of a
+// row is key - kmin. No probing and no key words: a row costs its compensated
+// atomic (or one integer reduction) and, for sums, a byte store marking the
+// group present.
+// ---------------------------------------------------------------------------
+template <bool VEC16>
+__global__ void k_gb_key_minmax(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff,
+		uint32_t kbytes, unsigned long long* __restrict__ mm)
+{
+	unsigned long long lo = ~0ull, hi = 0;
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += stride) {
+		int64_t k;
+		if (VEC16) {
+			const uint4 t = __ldg(reinterpret_cast<const uint4*>(in) + i);
+			k = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
+		} else {
+			k = pg_load_key(in + i * W + koff, kbytes);
+		}
+		const unsigned long long u = (unsigned long long) k ^ (1ull << 63);
+		lo = u < lo ? u : lo;
+		hi = u > hi ? u : hi;
+	}
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		const unsigned long long a = __shfl_down_sync(0xffffffffu, lo, o), b = __shfl_down_sync(0xffffffffu, hi, o);
+		lo = a < lo ? a : lo;
+		hi = b > hi ? b : hi;
+	}
+	if ((threadIdx.x & 31) == 0) { atomicMin(&mm[0], lo); atomicMax(&mm[1], hi); }
+}
+
+#define GBD_ILP 4
+template <int VT, int AGG, bool VEC16>
+__global__ void __launch_bounds__(GB_THREADS)
+k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes, uint32_t voff,
+		long long kmin, unsigned long long* __restrict__ acc, double* __restrict__ lo,
+		unsigned char* __restrict__ present)
+{
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	for (uint64_t base = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; base < n; base += stride * GBD_ILP) {
+		uint64_t d[GBD_ILP];
+		unsigned long long iv[GBD_ILP];
+		double dv[GBD_ILP];
+		bool ok[GBD_ILP];
+		#pragma unroll
+		for (int j = 0; j < GBD_ILP; ++j) {
+			const uint64_t i = base + j * stride;
+			ok[j] = i < n;
+			d[j] = 0; iv[j] = 0; dv[j] = 0.0;
+			if (!ok[j]) continue;
+			int64_t k;
+			uint64_t vbits;
+			if (VEC16) {
+				const uint4 t = __ldg(reinterpret_cast<const uint4*>(in) + i);
+				k = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
+				vbits = voff == 0 ? (((uint64_t) t.y << 32) | t.x) : voff == 8 ? (((uint64_t) t.w << 32) | t.z)
+					: voff == 4 ? t.y : t.w;
+				if (VT == PG_VAL_INT) vbits = (uint64_t) (int64_t) (int32_t) (voff == 0 ? t.x : voff == 4 ? t.y : voff == 8 ? t.z : t.w);
+			} else {
+				const char* r = in + i * W;
+				k = pg_load_key(r + koff, kbytes);
+				vbits = VT == PG_VAL_INT ? (uint64_t) (int64_t) *reinterpret_cast<const int32_t*>(r + voff)
+					: (uint64_t) pg_load_key(r + voff, 8);
+			}
+			d[j] = (uint64_t) k - (uint64_t) kmin;
+			if (AGG == PG_AGG_COUNT) iv[j] = 1;
+			else if (VT == PG_VAL_DEC) dv[j] = __longlong_as_double((long long) vbits);
+			else iv[j] = vbits;
+		}
+		if (AGG == PG_AGG_SUM && VT == PG_VAL_DEC) {
+			double old[GBD_ILP];
+			#pragma unroll
+			for (int j = 0; j < GBD_ILP; ++j)
+				if (ok[j]) old[j] = atomicAdd(reinterpret_cast<double*>(&acc[d[j]]), dv[j]);
+			#pragma unroll
+			for (int j = 0; j < GBD_ILP; ++j) {
+				if (!ok[j]) continue;
+				double sres, e;
+				fast_two_sum(old[j], dv[j], sres, e);
+				if (nonzero(e)) atomicAdd(&lo[d[j]], e);
+				present[d[j]] = 1;
+			}
+		} else {
+			#pragma unroll
+			for (int j = 0; j < GBD_ILP; ++j) {
+				if (!ok[j]) continue;
+				if (VT == PG_VAL_INT && AGG == PG_AGG_SUM)
+					atomicAdd(reinterpret_cast<unsigned int*>(&acc[d[j]]), (unsigned int) iv[j]);
+				else atomicAdd(&acc[d[j]], iv[j]);
+				if (AGG == PG_AGG_SUM) present[d[j]] = 1;
+			}
+		}
+	}
+}
+
+template <int VT, int AGG>
+__global__ void k_gb_dense_emit(const unsigned long long* __restrict__ acc, const double* __restrict__ lo,
+		const unsigned char* __restrict__ present, uint64_t range, long long kmin, uint32_t kbytes,
+		char* __restrict__ out, uint64_t cap_rows, unsigned long long* __restrict__ cursor)
+{
+	const uint32_t aw = (AGG == PG_AGG_SUM && VT == PG_VAL_INT) ? 4 : 8;
+	const uint32_t ow = kbytes + aw;
+	const int lane = threadIdx.x & 31;
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < pg_div_up(range, 32) * 32;
+			i += (uint64_t) gridDim.x * blockDim.x) {
+		const bool used = i < range && (AGG == PG_AGG_COUNT ? acc[i] != 0 : present[i] != 0);
+		const uint32_t ball = __ballot_sync(0xffffffffu, used);
+		if (!ball) continue;
+		unsigned long long base = 0;
+		if (lane == 0) base = atomicAdd(cursor, (unsigned long long) __popc(ball));
+		base = __shfl_sync(0xffffffffu, base, 0);
+		if (!used) continue;
+		const uint64_t pos = base + __popc(ball & ((1u << lane) - 1));
+		if (pos >= cap_rows) continue;
+		char* o = out + pos * ow;
+		const int64_t k = (int64_t) ((uint64_t) kmin + i);
+		if (kbytes == 4) *reinterpret_cast<int32_t*>(o) = (int32_t) k;
+		else { reinterpret_cast<uint32_t*>(o)[0] = (uint32_t) k; reinterpret_cast<uint32_t*>(o)[1] = (uint32_t) ((uint64_t) k >> 32); }
+		o += kbytes;
+		if (aw == 4) *reinterpret_cast<uint32_t*>(o) = (uint32_t) acc[i];
+		else {
+			unsigned long long a = acc[i];
+			if (VT == PG_VAL_DEC && AGG == PG_AGG_SUM)
+				a = (unsigned long long) __double_as_longlong(__longlong_as_double((long long) a) + lo[i]);
+			reinterpret_cast<uint32_t*>(o)[0] = (uint32_t) a;
+			reinterpret_cast<uint32_t*>(o)[1] = (uint32_t) (a >> 32);
+		}
+	}
+}
+
+// Runs the dense path when the key range allows it; *done = false leaves the
+// work to the hashed paths.
+template <int VT, int AGG>
+static int gb_dense(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, uint64_t hint,
+		void* out, uint64_t out_cap, uint64_t* ngroups, bool* done)
+{
+	*done = false;
+	int rc;
+	const bool vec16 = in->width == 16 && (in->key_off == 0 || in->key_off == 8) && in->key_bytes == 8 &&
+		(reinterpret_cast<uintptr_t>(in->data) & 15) == 0 &&
+		(AGG == PG_AGG_COUNT || (VT == PG_VAL_INT ? (voff & 3) == 0 : (voff == 0 || voff == 8)));
+	unsigned long long* mm = nullptr;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 32))) return rc;
+	const unsigned long long init[2] = {~0ull, 0ull};
+	PG_CUDA(ctx, cudaMemcpyAsync(mm, init, 16, cudaMemcpyHostToDevice, s));
+	const int blocks = (int) std::min<uint64_t>(pg_div_up(in->n, 256), (uint64_t) ctx->sm_count * 8);
+	if (vec16) k_gb_key_minmax<true><<<blocks, 256, 0, s>>>((const char*) in->data, in->n, in->width, in->key_off, in->key_bytes, mm);
+	else k_gb_key_minmax<false><<<blocks, 256, 0, s>>>((const char*) in->data, in->n, in->width, in->key_off, in->key_bytes, mm);
+	PG_LAUNCHED(ctx);
+	unsigned long long h[2];
+	PG_CUDA(ctx, cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, s));
+	PG_CUDA(ctx, cudaStreamSynchronize(s));
+	pg_free_async(ctx, s, mm);
+	const long long kmin = (long long) (h[0] ^ (1ull << 63)), kmax = (long long) (h[1] ^ (1ull << 63));
+	const uint64_t range = (uint64_t) kmax - (uint64_t) kmin + 1;
+	const uint64_t limit = std::max<uint64_t>(4 * std::max<uint64_t>(hint, 1), std::min<uint64_t>(2 * in->n, 1ull << 22));
+	if (range == 0 || range > limit || range > (1ull << 28)) return PG_OK;
+	char* mem = nullptr;
+	const size_t bytes = range * 17 + 64;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &mem, bytes))) return rc;
+	unsigned long long* acc = reinterpret_cast<unsigned long long*>(mem);
+	double* lo = reinterpret_cast<double*>(acc + range);
+	unsigned long long* cursor = reinterpret_cast<unsigned long long*>(lo + range);
+	unsigned char* present = reinterpret_cast<unsigned char*>(cursor + 1);
+	PG_CUDA(ctx, cudaMemsetAsync(mem, 0, bytes, s));
+	const int gblocks = (int) std::min<uint64_t>(pg_div_up(in->n, (uint64_t) GB_THREADS * GBD_ILP), (uint64_t) ctx->sm_count * 8);
+	if (vec16) k_gb_dense<VT, AGG, true><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, in->width,
+			in->key_off, in->key_bytes, voff, kmin, acc, lo, present);
+	else k_gb_dense<VT, AGG, false><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, in->width,
+			in->key_off, in->key_bytes, voff, kmin, acc, lo, present);
+	PG_LAUNCHED(ctx);
+	const int eblocks = (int) std::min<uint64_t>(pg_div_up(range, 256), (uint64_t) ctx->sm_count * 8);
+	k_gb_dense_emit<VT, AGG><<<eblocks, 256, 0, s>>>(acc, lo, present, range, kmin, in->key_bytes, (char*) out,
+			out_cap, cursor);
+	PG_LAUNCHED(ctx);
+	unsigned long long ng = 0;
+	PG_CUDA(ctx, cudaMemcpyAsync(&ng, cursor, 8, cudaMemcpyDeviceToHost, s));
+	PG_CUDA(ctx, cudaStreamSynchronize(s));
+	pg_free_async(ctx, s, mem);
+	*ngroups = ng;
+	*done = true;
+	if (ng > out_cap) return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_groupby: output capacity too small");
+	return pg_check_status(ctx, s, "pg_groupby");
+}
+
 template <int VT, int AGG>
 static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, uint64_t hint,
 		void* out, uint64_t out_cap, uint64_t* ngroups)
 {
 	const bool haskey = in->key_bytes != 0;
+	const int64_t gpath = ctx->tune[PG_TUNE_GROUPBY_PATH];
+	if (haskey && in->n && (gpath == 0 || gpath == 6)) {
+		bool done = false;
+		int rc = gb_dense<VT, AGG>(ctx, s, in, voff, hint, out, out_cap, ngroups, &done);
+		if (rc || done) return rc;
+	}
 	uint64_t groups = haskey ? std::max<uint64_t>(1, std::min<uint64_t>(hint ? hint : in->n, in->n ? in->n : 1)) : 1;
 	for (int attempt = 0; attempt < 6; ++attempt) {
 		uint32_t lg = 10;
@@ -462,7 +683,11 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 		PG_CUDA(ctx, cudaMemsetAsync(t.keys, 0xFF, (cap + 1) * 8, s));
 		PG_CUDA(ctx, cudaMemsetAsync(t.acc, 0, (cap + 1) * 16 + 64, s));
 		const bool smem = groups <= GB_SMEM_SLOTS / 2;
-		if (haskey && !smem && in->n >= 4 * groups && in->n < (1ull << 32) && in->width <= 1024) {
+		// Path knob: 0 by size, 1 global table (warp-combined), 2 partitioned,
+		// 3 global table without the warp combine.
+		const int64_t path = ctx->tune[PG_TUNE_GROUPBY_PATH];
+		const bool part_ok = haskey && !smem && in->n < (1ull << 32) && in->width <= 1024;
+		if (part_ok && (path == 2 || path == 4 || (path == 0 && in->n >= 4 * groups))) {
 			// High cardinality: partition by key hash, aggregate per partition.
 			uint32_t lp = 1;
 			while ((1ull << lp) < groups / 1024 && lp < 12) ++lp;
@@ -477,10 +702,16 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 			f.skipbits = 64 - lp; f.nbuckets = P;
 			if ((rc = pg_partition_fn(ctx, s, in, f, prow, poffs))) return rc;
 			const size_t psm = (size_t) (GBP_SLOTS + 1) * 24;
-			PG_CUDA(ctx, cudaFuncSetAttribute(k_gb_part_agg<VT, AGG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) psm));
 			const int pblocks = (int) std::min<uint64_t>(P, (uint64_t) ctx->sm_count * 2);
-			k_gb_part_agg<VT, AGG><<<pblocks, GBP_THREADS, psm, s>>>(prow, poffs, P, in->width, in->key_off,
-					in->key_bytes, voff, t, (char*) out, out_cap, cursor, oflag, ctx->d_status);
+			if (path == 4) {
+				PG_CUDA(ctx, cudaFuncSetAttribute(k_gb_part_agg<VT, AGG, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) psm));
+				k_gb_part_agg<VT, AGG, false><<<pblocks, GBP_THREADS, psm, s>>>(prow, poffs, P, in->width, in->key_off,
+						in->key_bytes, voff, t, (char*) out, out_cap, cursor, oflag, ctx->d_status);
+			} else {
+				PG_CUDA(ctx, cudaFuncSetAttribute(k_gb_part_agg<VT, AGG, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) psm));
+				k_gb_part_agg<VT, AGG, true><<<pblocks, GBP_THREADS, psm, s>>>(prow, poffs, P, in->width, in->key_off,
+						in->key_bytes, voff, t, (char*) out, out_cap, cursor, oflag, ctx->d_status);
+			}
 			PG_LAUNCHED(ctx);
 			int hflag = 0;
 			PG_CUDA(ctx, cudaMemcpyAsync(&hflag, oflag, 4, cudaMemcpyDeviceToHost, s));
@@ -514,8 +745,16 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 					k_gb_insert<VT, AGG, HK, SM><<<blocks, GB_THREADS, smem_bytes, s>>>( \
 					(const char*) in->data, in->n, in->width, in->key_off, in->key_bytes, voff, t, slg, ctx->d_status)
 			if (haskey && smem) { GB_LAUNCH(true, true); }
+			else if (haskey && (path == 3 || path == 5)) {
+				if (path == 5)
+					k_gb_insert_ilp<VT, AGG, false, 8><<<blocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n,
+							in->width, in->key_off, in->key_bytes, voff, t, ctx->d_status);
+				else
+					k_gb_insert_ilp<VT, AGG, false, 4><<<blocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n,
+							in->width, in->key_off, in->key_bytes, voff, t, ctx->d_status);
+			}
 			else if (haskey) {
-				k_gb_insert_ilp<VT, AGG><<<blocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n,
+				k_gb_insert_ilp<VT, AGG, true, 4><<<blocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n,
 						in->width, in->key_off, in->key_bytes, voff, t, ctx->d_status);
 			}
 			else { GB_LAUNCH(false, true); }

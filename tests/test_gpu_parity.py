@@ -262,7 +262,8 @@ def _gb_int_check(ctx, rows, agg, vtype, key=(0, 8), hint=0, has_key=True):
 
 
 @pytest.mark.parametrize("groups", [1, 10, 1000, 20_000, 200_000])
-def test_groupby_long_sum_and_count(ctx, groups):
+def test_groupby_long_sum_and_count(gbctx, groups):
+    ctx = gbctx
     rows = dg.uniform_keys(500_000, groups, dg.seed_for(50))
     rows[:, 1] -= 1 << 30    # negative values too
     for agg in ("sum", "count"):
@@ -270,7 +271,8 @@ def test_groupby_long_sum_and_count(ctx, groups):
         _gb_int_check(ctx, rows, agg, "long", hint=groups)
 
 
-def test_groupby_int_sum_wraps(ctx):
+def test_groupby_int_sum_wraps(gbctx):
+    ctx = gbctx
     rows = gin.make({"gen": "formula", "name": "int_big", "n": 100_000})
     got = ctx.groupby(rows, key=(0, 4), val=(4, "int"), agg="sum")
     want = orc.groupby(rows, key=(0, 4), val=(4, "int"), agg="sum")
@@ -284,11 +286,25 @@ def test_groupby_no_group_by(ctx):
     assert ctx.groupby(rows[:0], agg="count", has_key=False).shape[0] == 0
 
 
-def test_groupby_empty_marker_key(ctx):
+def test_groupby_empty_marker_key(gbctx):
+    ctx = gbctx
     rows = dg.uniform_keys(20_000, 300, dg.seed_for(52))
     rows[::7, 0] = -1
     _gb_int_check(ctx, rows, "sum", "long")
     _gb_int_check(ctx, rows, "count", "long", hint=10_000)
+
+
+# Every group-by path: 0 chooses (dense direct-indexed table for compact key
+# ranges), 3 hashed global table, 4 partitioned, 1 and 2 the same with warp
+# combining of equal keys.
+GB_PATHS = [0, 1, 2, 3, 4]
+
+
+@pytest.fixture(params=GB_PATHS)
+def gbctx(ctx, request):
+    ctx.tune(groupby_path=request.param)
+    yield ctx
+    ctx.tune(groupby_path=0)
 
 
 def _gb_dec_check(ctx, rows, hint=0):
@@ -304,13 +320,15 @@ def _gb_dec_check(ctx, rows, hint=0):
 
 
 @pytest.mark.parametrize("groups", [1, 300, 100_000])
-def test_groupby_dec_compensated(ctx, groups):
+def test_groupby_dec_compensated(gbctx, groups):
+    ctx = gbctx
     rows = dg.groupby_rows(1_000_000, groups, 1e4, dg.seed_for(53))
     _gb_dec_check(ctx, rows)
     _gb_dec_check(ctx, rows, hint=groups)
 
 
-def test_groupby_dec_ill_conditioned(ctx):
+def test_groupby_dec_ill_conditioned(gbctx):
+    ctx = gbctx
     # Large values that cancel plus many small ones: naive summation loses the
     # small ones entirely; compensated summation keeps them.
     n = 200_000
@@ -323,13 +341,15 @@ def test_groupby_dec_ill_conditioned(ctx):
     _gb_dec_check(ctx, rows)
 
 
-def test_groupby_dec_zipf(ctx):
+def test_groupby_dec_zipf(gbctx):
+    ctx = gbctx
     rows = gin.make({"gen": "groupby_zipf", "n": 300_000, "groups": 20_000, "rel": 54})
     _gb_dec_check(ctx, rows)
     _gb_dec_check(ctx, rows, hint=20_000)     # partitioned path with skewed partitions
 
 
-def test_groupby_partition_overflow(ctx):
+def test_groupby_partition_overflow(gbctx):
+    ctx = gbctx
     # A hint far below the real group count: partitions overflow their shared
     # tables into the global one, and the global table itself regrows.
     rows = dg.uniform_keys(400_000, 90_000, dg.seed_for(55))
@@ -338,7 +358,8 @@ def test_groupby_partition_overflow(ctx):
     assert np.array_equal(canon(got), canon(want))
 
 
-def test_groupby_reference_unit_test(ctx):
+def test_groupby_reference_unit_test(gbctx):
+    ctx = gbctx
     # unit_tests/queryaggsum.cpp: group i holds 1..i; sum must be i(i+1)/2.
     rows = gin.make({"gen": "formula", "name": "agg_1_to_i", "n": 20})
     got = ctx.groupby(rows, val=(8, "dec"), agg="sum").view(np.int64).reshape(-1, 2)
