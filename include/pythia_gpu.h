@@ -89,6 +89,10 @@ int pg_shutdown(pg_ctx* ctx);
 const char* pg_last_error(pg_ctx* ctx);
 int pg_device_status(pg_ctx* ctx);             /* sticky device error word  */
 int pg_stream_create(pg_ctx* ctx, pg_stream* stream);
+/* A stream whose kernels the block scheduler prefers to those of ordinary
+ * streams (highest CUDA stream priority): short requests run ahead of long
+ * ones sharing the GPU. */
+int pg_stream_create_urgent(pg_ctx* ctx, pg_stream* stream);
 int pg_stream_destroy(pg_ctx* ctx, pg_stream stream);
 int pg_sync(pg_ctx* ctx, pg_stream stream);
 int pg_buffer_alloc(pg_ctx* ctx, uint64_t bytes, void** dptr);
@@ -207,6 +211,18 @@ enum { PG_AGG_SUM = 0, PG_AGG_COUNT = 1 };
 int pg_groupby(pg_ctx* ctx, pg_stream stream, const pg_rel* in,
 		uint32_t val_off, int val_type, int agg, uint64_t groups_hint,
 		void* out, uint64_t out_capacity, uint64_t* ngroups);
+
+/* Join then group-by without writing the join rows: a HashJoinOp whose output
+ * feeds AggregateSum / AggregateCount grouped on the build-side column
+ * (join.cpp:503-562 + genericaggregate.cpp:240-282). `ht` must have been built
+ * with exactly one build-side projected column (the group key, 4 or 8 bytes);
+ * the probe column at val_off (val_type) is summed, or matches are counted.
+ * Output rows as pg_groupby: (group, agg), order unspecified; dec sums
+ * compensated. Needs a narrow dense table whose group values span a compact
+ * range and 16-byte probe tuples; otherwise PG_ERR_UNSUPPORTED, and the caller
+ * probes (materialised) and groups in two steps.                          */
+int pg_hashjoin_groupby(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht, const pg_rel* S,
+		uint32_t val_off, int val_type, int agg, void* out, uint64_t out_capacity, uint64_t* ngroups);
 
 /* ---------------------------------------------------------------------- */
 /* Page sort: TupleBuffer::sort<KeyT> / sortAllInPage (util/buffer.inl:135-292,

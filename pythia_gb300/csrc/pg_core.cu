@@ -119,6 +119,17 @@ extern "C" int pg_stream_create(pg_ctx* ctx, pg_stream* s)
 	return PG_OK;
 }
 
+extern "C" int pg_stream_create_urgent(pg_ctx* ctx, pg_stream* s)
+{
+	if (!ctx || !s) return PG_ERR_ARG;
+	int least = 0, greatest = 0;
+	PG_CUDA(ctx, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+	cudaStream_t st;
+	PG_CUDA(ctx, cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, greatest));
+	*s = st;
+	return PG_OK;
+}
+
 extern "C" int pg_stream_destroy(pg_ctx* ctx, pg_stream s)
 {
 	if (!ctx) return PG_ERR_ARG;

@@ -38,25 +38,6 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
 	e = (a - (s - bb)) + (b - bb);
 }
 
-// Exact rounding error of s = a + b by Dekker's Fast2Sum (3 FP64 adds: the
-// larger operand first). The magnitudes are ordered by an integer compare of
-// the bit patterns, and the zero test below is an integer test too: on this
-// GPU the FP64 pipe is narrow and the dominant cost of a compensated
-// aggregation, so only the three additions use it.
-__device__ __forceinline__ void fast_two_sum(double a, double b, double& s, double& e)
-{
-	const unsigned long long ma = (unsigned long long) __double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFull;
-	const unsigned long long mb = (unsigned long long) __double_as_longlong(b) & 0x7FFFFFFFFFFFFFFFull;
-	const double big = ma >= mb ? a : b, small = ma >= mb ? b : a;
-	s = a + b;
-	e = small - (s - big);
-}
-
-__device__ __forceinline__ bool nonzero(double x)
-{
-	return ((unsigned long long) __double_as_longlong(x) << 1) != 0;
-}
-
 // Adds v (+ compensation c) into (hi, lo): one atomic on hi, whose old value
 // gives the rounding error of this addition exactly, and one on lo when that
 // error (plus c) is not zero.
@@ -800,4 +781,24 @@ extern "C" int pg_groupby(pg_ctx* ctx, pg_stream stream, const pg_rel* in,
 	if (val_type == PG_VAL_INT) return gb_run<PG_VAL_INT, PG_AGG_SUM>(ctx, s, in, val_off, groups_hint, out, out_capacity, ngroups);
 	if (val_type == PG_VAL_LONG) return gb_run<PG_VAL_LONG, PG_AGG_SUM>(ctx, s, in, val_off, groups_hint, out, out_capacity, ngroups);
 	return gb_run<PG_VAL_DEC, PG_AGG_SUM>(ctx, s, in, val_off, groups_hint, out, out_capacity, ngroups);
+}
+
+// Emits the present groups of a dense group table (acc/lo/present over
+// `range` slots, group key = kmin + slot) as (key, agg) rows of kbytes + agg
+// bytes, appending at *cursor. Used by pg_hashjoin_groupby.
+int pg_dense_groups_emit(pg_ctx* ctx, cudaStream_t s, const unsigned long long* acc, const double* lo,
+		const unsigned char* present, uint64_t range, long long kmin, uint32_t kbytes, int val_type, int agg,
+		void* out, uint64_t out_cap, unsigned long long* cursor)
+{
+	const int eblocks = (int) std::min<uint64_t>(pg_div_up(range, 256), (uint64_t) ctx->sm_count * 8);
+	if (agg == PG_AGG_COUNT)
+		k_gb_dense_emit<PG_VAL_LONG, PG_AGG_COUNT><<<eblocks, 256, 0, s>>>(acc, lo, present, range, kmin, kbytes, (char*) out, out_cap, cursor);
+	else if (val_type == PG_VAL_INT)
+		k_gb_dense_emit<PG_VAL_INT, PG_AGG_SUM><<<eblocks, 256, 0, s>>>(acc, lo, present, range, kmin, kbytes, (char*) out, out_cap, cursor);
+	else if (val_type == PG_VAL_LONG)
+		k_gb_dense_emit<PG_VAL_LONG, PG_AGG_SUM><<<eblocks, 256, 0, s>>>(acc, lo, present, range, kmin, kbytes, (char*) out, out_cap, cursor);
+	else
+		k_gb_dense_emit<PG_VAL_DEC, PG_AGG_SUM><<<eblocks, 256, 0, s>>>(acc, lo, present, range, kmin, kbytes, (char*) out, out_cap, cursor);
+	PG_LAUNCHED(ctx);
+	return PG_OK;
 }

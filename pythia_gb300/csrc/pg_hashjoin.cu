@@ -78,6 +78,7 @@ struct pg_hashtable {
 	// table is 64 MB, which stays in L2) and needs no presence bitmap.
 	uint32_t* dense32;
 	unsigned long long vmin;
+	unsigned long long vmax;    // largest packed value (dense tables)
 };
 
 struct HjProbeTable {
@@ -1248,7 +1249,7 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 			PG_CUDA(ctx, cudaStreamSynchronize(s));
 			const bool dup = counted ? dh[1] != R->n : (dh[0] & 0xFFFFFFFFull) != 0;
 			if (!dup) {
-				ht->dense = true; ht->unique = true; ht->dmin = kmin; ht->drange = range; ht->vmin = h[2];
+				ht->dense = true; ht->unique = true; ht->dmin = kmin; ht->drange = range; ht->vmin = h[2]; ht->vmax = h[3];
 				ht->slots = nullptr; ht->side = nullptr; ht->nside = 0; ht->log2cap = 1; ht->capacity = 0;
 				pg_free_async(ctx, s, mm);
 				*out = ht;
@@ -1712,5 +1713,138 @@ extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
 #undef HJH_TRY
 	if (materialize && written > out_capacity)
 		return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_hashjoin_host: output capacity too small");
+	return PG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Join then group-by in one pass (a HashJoinOp feeding AggregateSum /
+// AggregateCount: join.cpp:503-562 with genericaggregate.cpp:240-282). The
+// group key is the table's value (the one projected build column); a narrow
+// dense table stores value - vmin, which is the row's group slot directly. The
+// probe-side value is folded into a dense group table with the compensated
+// atomics of the group-by (one atomic on hi whose old value gives the exact
+// rounding error, one on lo), so the join rows are never written.
+// ---------------------------------------------------------------------------
+template <int VT, int AGG>
+__global__ void __launch_bounds__(PW_WARPS * 32, 4)
+k_probe16_groupby(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb, uint32_t voff,
+		unsigned long long* __restrict__ acc, double* __restrict__ lo, unsigned char* __restrict__ present)
+{
+	constexpr int ITEMS = PW_CHUNK / 32;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
+	const uint64_t W = (uint64_t) gridDim.x * PW_WARPS;
+	const uint64_t first = (uint64_t) blockIdx.x * PW_WARPS + warp;
+	const uint64_t keep = pg_policy_evict_last();
+	const uint64_t instream = pg_policy_evict_first();
+	if (first >= nchunks) return;
+	uint4 cur[ITEMS], nxt[ITEMS];
+	auto load = [&](uint64_t c, uint4 (&t)[ITEMS]) {
+		const uint32_t rows = (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK);
+		#pragma unroll
+		for (int j = 0; j < ITEMS; ++j) {
+			const uint32_t p = j * 32 + lane;
+			t[j] = p < rows ? hj_ld_stream(S + (c * PW_CHUNK + p) * 16, instream) : make_uint4(0, 0, 0, 0);
+		}
+	};
+	load(first, cur);
+	for (uint64_t c = first; c < nchunks; c += W) {
+		if (c + W < nchunks) load(c + W, nxt);
+		const uint32_t rows = (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK);
+		uint32_t e[ITEMS];
+		#pragma unroll
+		for (int j = 0; j < ITEMS; ++j) {
+			const uint4 t = cur[j];
+			const int64_t key = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
+			const unsigned long long d = (unsigned long long) key - (unsigned long long) tb.dmin;
+			e[j] = 0xFFFFFFFFu;
+			if (j * 32 + lane < rows && d < tb.drange)
+				asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;"
+						: "=r"(e[j]) : "l"(tb.dense32 + d), "l"(keep));
+		}
+		if (AGG == PG_AGG_SUM && VT == PG_VAL_DEC) {
+			double v[ITEMS], old[ITEMS];
+			#pragma unroll
+			for (int j = 0; j < ITEMS; ++j) {
+				const uint4 t = cur[j];
+				v[j] = __longlong_as_double((long long) (voff == 0 ? (((uint64_t) t.y << 32) | t.x) : (((uint64_t) t.w << 32) | t.z)));
+				if (e[j] != 0xFFFFFFFFu) old[j] = atomicAdd(reinterpret_cast<double*>(&acc[e[j]]), v[j]);
+			}
+			#pragma unroll
+			for (int j = 0; j < ITEMS; ++j) {
+				if (e[j] == 0xFFFFFFFFu) continue;
+				double sres, err;
+				fast_two_sum(old[j], v[j], sres, err);
+				if (nonzero(err)) atomicAdd(&lo[e[j]], err);
+				present[e[j]] = 1;
+			}
+		} else {
+			#pragma unroll
+			for (int j = 0; j < ITEMS; ++j) {
+				if (e[j] == 0xFFFFFFFFu) continue;
+				const uint4 t = cur[j];
+				if (AGG == PG_AGG_COUNT) { atomicAdd(&acc[e[j]], 1ull); continue; }
+				const uint32_t w = voff / 4;
+				const uint32_t w0 = w == 0 ? t.x : w == 1 ? t.y : w == 2 ? t.z : t.w;
+				if (VT == PG_VAL_INT) atomicAdd(reinterpret_cast<unsigned int*>(&acc[e[j]]), w0);
+				else atomicAdd(&acc[e[j]], ((unsigned long long) (w == 0 ? t.y : t.w) << 32) | w0);
+				present[e[j]] = 1;
+			}
+		}
+		#pragma unroll
+		for (int j = 0; j < ITEMS; ++j) cur[j] = nxt[j];
+	}
+}
+
+extern "C" int pg_hashjoin_groupby(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht, const pg_rel* S,
+		uint32_t val_off, int val_type, int agg, void* out, uint64_t out_capacity, uint64_t* ngroups)
+{
+	if (!ctx || !ht || !S || !ngroups) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_groupby: null argument");
+	int rc;
+	if ((rc = hj_validate_rel(ctx, S, "pg_hashjoin_groupby"))) return rc;
+	if (agg != PG_AGG_SUM && agg != PG_AGG_COUNT) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_groupby: bad aggregate");
+	if (agg == PG_AGG_SUM && (val_type < 0 || val_type > 2 || (val_type == PG_VAL_INT ? (val_off & 3) : (val_off & 7)) ||
+			val_off + (val_type == PG_VAL_INT ? 4 : 8) > S->width))
+		return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_groupby: bad value column");
+	*ngroups = 0;
+	const uint64_t vrange = ht->dense32 ? ht->vmax - ht->vmin + 1 : 0;
+	uint32_t gbytes = 0;
+	for (int c = 0; c < ht->bcols.n; ++c) gbytes += 4 * ht->bcols.words[c];
+	if (!ht->dense32 || ht->bcols.n != 1 || (gbytes != 4 && gbytes != 8) || vrange == 0 ||
+			vrange > std::max<uint64_t>(4 * ht->nbuild, 1 << 20) || vrange > (1ull << 28) ||
+			S->width != 16 || (S->key_off != 0 && S->key_off != 8) || S->key_bytes != 8 ||
+			(reinterpret_cast<uintptr_t>(S->data) & 15) != 0)
+		return pg_fail(ctx, PG_ERR_UNSUPPORTED, "pg_hashjoin_groupby: needs a narrow dense table with one build "
+				"column of compact range and 16-byte probe tuples");
+	cudaStream_t s = (cudaStream_t) stream;
+	char* mem = nullptr;
+	const size_t bytes = vrange * 17 + 64;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &mem, bytes))) return rc;
+	unsigned long long* acc = reinterpret_cast<unsigned long long*>(mem);
+	double* lo = reinterpret_cast<double*>(acc + vrange);
+	unsigned long long* cursor = reinterpret_cast<unsigned long long*>(lo + vrange);
+	unsigned char* present = reinterpret_cast<unsigned char*>(cursor + 1);
+	PG_CUDA(ctx, cudaMemsetAsync(mem, 0, bytes, s));
+	if (S->n) {
+		HjProbeTable tb = {};
+		tb.dense32 = ht->dense32; tb.vmin = ht->vmin; tb.dmin = ht->dmin; tb.drange = ht->drange;
+		const int grid = (int) std::min<uint64_t>(pg_div_up(pg_div_up(S->n, PW_CHUNK), PW_WARPS), (uint64_t) ctx->sm_count * 24);
+#define PG_LAUNCH(VT, AGG) k_probe16_groupby<VT, AGG><<<grid, PW_WARPS * 32, 0, s>>>((const char*) S->data, S->n, \
+				S->key_off, tb, val_off, acc, lo, present)
+		if (agg == PG_AGG_COUNT) PG_LAUNCH(PG_VAL_LONG, PG_AGG_COUNT);
+		else if (val_type == PG_VAL_INT) PG_LAUNCH(PG_VAL_INT, PG_AGG_SUM);
+		else if (val_type == PG_VAL_LONG) PG_LAUNCH(PG_VAL_LONG, PG_AGG_SUM);
+		else PG_LAUNCH(PG_VAL_DEC, PG_AGG_SUM);
+#undef PG_LAUNCH
+		PG_LAUNCHED(ctx);
+	}
+	if ((rc = pg_dense_groups_emit(ctx, s, acc, lo, present, vrange, (long long) ht->vmin, gbytes, val_type, agg,
+			out, out_capacity, cursor))) return rc;
+	unsigned long long ng = 0;
+	PG_CUDA(ctx, cudaMemcpyAsync(&ng, cursor, 8, cudaMemcpyDeviceToHost, s));
+	if ((rc = pg_check_status(ctx, s, "pg_hashjoin_groupby"))) return rc;
+	pg_free_async(ctx, s, mem);
+	*ngroups = ng;
+	if (ng > out_capacity) return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_hashjoin_groupby: output capacity too small");
 	return PG_OK;
 }

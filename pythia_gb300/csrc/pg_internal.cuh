@@ -300,3 +300,27 @@ __host__ __device__ __forceinline__ uint32_t pg_min32(uint32_t a, uint32_t b) { 
 
 // Exclusive scan of n uint64 values in place on the device (multi-block).
 int pg_scan_u64(pg_ctx* ctx, cudaStream_t s, uint64_t* data, uint64_t n, uint64_t* total_dev);
+
+// Exact rounding error of s = a + b by Dekker's Fast2Sum (3 FP64 adds: the
+// larger operand first). The magnitudes are ordered by an integer compare of
+// the bit patterns, and the zero test is an integer test too: on this GPU the
+// FP64 pipe is narrow and the dominant cost of a compensated aggregation, so
+// only the three additions use it.
+__device__ __forceinline__ void fast_two_sum(double a, double b, double& s, double& e)
+{
+	const unsigned long long ma = (unsigned long long) __double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFull;
+	const unsigned long long mb = (unsigned long long) __double_as_longlong(b) & 0x7FFFFFFFFFFFFFFFull;
+	const double big = ma >= mb ? a : b, small = ma >= mb ? b : a;
+	s = a + b;
+	e = small - (s - big);
+}
+
+__device__ __forceinline__ bool nonzero(double x)
+{
+	return ((unsigned long long) __double_as_longlong(x) << 1) != 0;
+}
+
+// Dense group table emission (pg_groupby.cu).
+int pg_dense_groups_emit(pg_ctx* ctx, cudaStream_t s, const unsigned long long* acc, const double* lo,
+		const unsigned char* present, uint64_t range, long long kmin, uint32_t kbytes, int val_type, int agg,
+		void* out, uint64_t out_cap, unsigned long long* cursor);

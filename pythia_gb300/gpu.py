@@ -63,7 +63,8 @@ SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_st
            "pg_hashjoin_build", "pg_hashjoin_probe", "pg_hashtable_free", "pg_hashjoin_host",
            "pg_groupby", "pg_sort_pages", "pg_mpsm_join", "pg_hashjoin_agg_noalloc",
            "pg_tune_set", "pg_tune_get", "pg_batch_prepare", "pg_batch_run", "pg_batch_free",
-           "pg_generate_fk", "pg_buffer_alloc_async", "pg_buffer_free_async", "pg_generate_zipf_fk"]
+           "pg_generate_fk", "pg_buffer_alloc_async", "pg_buffer_free_async", "pg_generate_zipf_fk",
+           "pg_hashjoin_groupby", "pg_stream_create_urgent"]
 TUNE = {"probe_ctas_per_sm": 0, "probe_variant": 1, "dense": 2, "partition_tile": 3,
         "groupby_smem_groups": 4, "radix_bits": 5, "probe_items": 6, "probe_cache": 7, "probe_passes": 8, "groupby_path": 9}
 
@@ -117,6 +118,8 @@ def lib():
             "pg_generate_zipf_fk": ([vp, vp, vp, u64, ctypes.c_double, u64, vp, u64, ctypes.c_double], ci),
             "pg_buffer_alloc_async": ([vp, vp, u64, P(vp)], ci),
             "pg_buffer_free_async": ([vp, vp, vp], ci),
+            "pg_hashjoin_groupby": ([vp, vp, vp, P(Rel), u32, ci, ci, vp, u64, P(u64)], ci),
+            "pg_stream_create_urgent": ([vp, P(vp)], ci),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -269,6 +272,29 @@ class Context:
         finally:
             lib().pg_hashtable_free(self.h, ht.value)
         return out, res.n_out, res.sum
+
+    def hashjoin_groupby(self, R, S, group=(8, 8), val=(8, "dec"), agg="sum", bkey=(0, 8), pkey=(0, 8)):
+        """Join R and S on their keys and aggregate the probe column `val`
+        grouped by the build column `group` in one pass (pg_hashjoin_groupby).
+        Returns (group, agg) rows."""
+        Ra, Sa = np.ascontiguousarray(R), np.ascontiguousarray(S)
+        dR, dS = self.upload(Ra), self.upload(Sa)
+        rR = self.rel(dR, Ra.shape[0], row_width(Ra), *bkey)
+        rS = self.rel(dS, Sa.shape[0], row_width(Sa), *pkey)
+        c, nc = cols((("B", group[0], group[1]), ("P", val[0], 4 if val[1] == "int" else 8)))
+        ht = ctypes.c_void_p()
+        self._check(lib().pg_hashjoin_build(self.h, self.stream, ctypes.byref(rR), c, nc, ctypes.byref(ht)))
+        try:
+            vtype = VAL[val[1]]
+            ow = group[1] + (4 if (agg == "sum" and vtype == 0) else 8)
+            cap = max(Ra.shape[0], 1)
+            o = self.alloc(cap * ow)
+            ng = ctypes.c_uint64()
+            self._check(lib().pg_hashjoin_groupby(self.h, self.stream, ht.value, ctypes.byref(rS), val[0], vtype,
+                                                  AGG[agg], o.ptr, cap, ctypes.byref(ng)))
+            return self.download(o, ng.value * ow).reshape(-1, ow)
+        finally:
+            lib().pg_hashtable_free(self.h, ht.value)
 
     def groupby(self, rows, key=(0, 8), val=(8, "long"), agg="sum", groups_hint=0, has_key=True):
         a = np.ascontiguousarray(rows)

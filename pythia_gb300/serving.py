@@ -20,7 +20,6 @@ group key.
 Host-side failures (an exception in one query's execution) are recorded for
 that query and the loop continues.
 """
-import collections
 import ctypes
 import threading
 import time
@@ -91,55 +90,92 @@ def footprint(cat, q):
     return 32 * ns + 64 * t.groups + (1 << 20)
 
 
-def execute(ctx, stream, cat, q):
-    """Runs one query on `stream`; returns (group keys, sums) sorted by key."""
+def execute(ctx, stream, cat, q, fused=True):
+    """Runs one query on `stream`; returns (group keys, sums, join rows) with
+    groups in unspecified order. The plan runs as one pass (probe folding
+    straight into the group table, pg_hashjoin_groupby) when the table allows
+    it, else as a materialised probe followed by a group-by."""
     if q.fail:
         raise RuntimeError(f"query {q.qid}: injected host failure")
     L = gpu.lib()
     t = cat.tables[q.table]
     ns = cat.probe_factor * t.n
     c, nc = cat._cols
-    w1, w2 = ctypes.c_void_p(), ctypes.c_void_p()
-    ctx._check(L.pg_buffer_alloc_async(ctx.h, stream, 16 * ns, ctypes.byref(w1)))
+    rS = gpu.Rel(t.pools[q.zipf].ptr, ns, 16, 0, 8)
+    w2 = ctypes.c_void_p()
     ctx._check(L.pg_buffer_alloc_async(ctx.h, stream, 16 * (t.groups + 1), ctypes.byref(w2)))
+    w1 = ctypes.c_void_p()
     try:
-        rS = gpu.Rel(t.pools[q.zipf].ptr, ns, 16, 0, 8)
-        res = gpu.JoinResult()
-        ctx._check(L.pg_hashjoin_probe(ctx.h, stream, t.ht, ctypes.byref(rS), c, nc, w1.value, ns,
-                                       gpu.JOIN_MATERIALIZE, -1, ctypes.byref(res)))
-        rJ = gpu.Rel(w1.value, res.n_out, 16, 0, 8)
         ng = ctypes.c_uint64()
-        ctx._check(L.pg_groupby(ctx.h, stream, ctypes.byref(rJ), 8, gpu.VAL["dec"], gpu.AGG["sum"],
-                                t.groups, w2.value, t.groups + 1, ctypes.byref(ng)))
+        rc = L.pg_hashjoin_groupby(ctx.h, stream, t.ht, ctypes.byref(rS), 8, gpu.VAL["dec"], gpu.AGG["sum"],
+                                   w2.value, t.groups + 1, ctypes.byref(ng)) if fused else gpu.PG_ERR_UNSUPPORTED
+        if rc == gpu.PG_ERR_UNSUPPORTED:
+            ctx._check(L.pg_buffer_alloc_async(ctx.h, stream, 16 * ns, ctypes.byref(w1)))
+            res = gpu.JoinResult()
+            ctx._check(L.pg_hashjoin_probe(ctx.h, stream, t.ht, ctypes.byref(rS), c, nc, w1.value, ns,
+                                           gpu.JOIN_MATERIALIZE, -1, ctypes.byref(res)))
+            rJ = gpu.Rel(w1.value, res.n_out, 16, 0, 8)
+            ctx._check(L.pg_groupby(ctx.h, stream, ctypes.byref(rJ), 8, gpu.VAL["dec"], gpu.AGG["sum"],
+                                    t.groups, w2.value, t.groups + 1, ctypes.byref(ng)))
+        else:
+            ctx._check(rc)
         out = np.empty(ng.value * 2, dtype=np.int64)
         if ng.value:
             ctx._check(L.pg_d2h(ctx.h, stream, out.ctypes.data, w2.value, 16 * ng.value))
-            ctx._check(L.pg_sync(ctx.h, stream))
+        ctx._check(L.pg_sync(ctx.h, stream))
     finally:
-        L.pg_buffer_free_async(ctx.h, stream, w1.value)
+        if w1.value:
+            L.pg_buffer_free_async(ctx.h, stream, w1.value)
         L.pg_buffer_free_async(ctx.h, stream, w2.value)
     rows = out.reshape(-1, 2)
-    order = np.argsort(rows[:, 0], kind="stable")
-    return rows[order, 0].copy(), rows[order, 1].view(np.float64).copy(), int(res.n_out)
+    return rows[:, 0], rows[:, 1].view(np.float64)
+
+
+def canonical(result):
+    """A query result sorted by group key (results are unordered)."""
+    keys, sums = result
+    order = np.argsort(keys, kind="stable")
+    return keys[order], sums[order]
+
+
+def work(cat, q):
+    """Estimated work of a query: tuples it reads (probe + build)."""
+    t = cat.tables[q.table]
+    return (cat.probe_factor + 1) * t.n
 
 
 class Server:
-    def __init__(self, ctx, cat, slots, budget_bytes):
+    """Worker slots over one GPU context.
+
+    policy "fifo": a free slot takes the first pending query (arrival order)
+    whose footprint fits. policy "short-first": it takes the fitting query of
+    least estimated work, except that a query pending longer than `max_wait`
+    seconds goes first (no starvation); queries below `urgent_below` tuples
+    run on high-priority streams, so their kernels are scheduled ahead of the
+    long queries' kernels already on the GPU."""
+
+    def __init__(self, ctx, cat, slots, budget_bytes, policy="fifo", max_wait=0.25, urgent_below=32 << 20):
         self.ctx, self.cat, self.slots, self.budget = ctx, cat, slots, budget_bytes
-        self.streams = []
+        self.policy, self.max_wait, self.urgent_below = policy, max_wait, urgent_below
+        self.streams, self.urgent = [], []
+        L = gpu.lib()
         for _ in range(slots):
             s = ctypes.c_void_p()
-            ctx._check(gpu.lib().pg_stream_create(ctx.h, ctypes.byref(s)))
+            ctx._check(L.pg_stream_create(ctx.h, ctypes.byref(s)))
             self.streams.append(s.value)
+            u = ctypes.c_void_p()
+            ctx._check(L.pg_stream_create_urgent(ctx.h, ctypes.byref(u)))
+            self.urgent.append(u.value)
 
     def close(self):
-        for s in self.streams:
+        for s in self.streams + self.urgent:
             gpu.lib().pg_stream_destroy(self.ctx.h, s)
+        self.streams, self.urgent = [], []
 
     def run(self, queries):
         """Serves `queries` (arrival = seconds after start). Returns them with
         start/end times (seconds after start), results or errors."""
-        pending = collections.deque()
+        pending = []
         cv = threading.Condition()
         state = {"used": 0, "arrived": 0, "t0": time.perf_counter()}
         n = len(queries)
@@ -157,17 +193,27 @@ class Server:
                     state["arrived"] += 1
                     cv.notify_all()
 
+        def fits(q):
+            fp = footprint(self.cat, q)
+            return (state["used"] + fp <= self.budget or state["used"] == 0), fp
+
         def take():
-            # First pending query whose footprint fits; None when none fits.
-            for i, q in enumerate(pending):
-                fp = footprint(self.cat, q)
-                if state["used"] + fp <= self.budget or state["used"] == 0:
-                    del pending[i]
+            # The next query to admit, or None when none fits.
+            order = range(len(pending))
+            if self.policy == "short-first" and pending:
+                t = now()
+                overdue = [i for i in order if t - pending[i].arrival > self.max_wait]
+                order = overdue + sorted((i for i in order if i not in set(overdue)),
+                                         key=lambda i: work(self.cat, pending[i]))
+            for i in order:
+                ok, fp = fits(pending[i])
+                if ok:
+                    q = pending.pop(i)
                     state["used"] += fp
                     return q, fp
             return None, 0
 
-        def worker(stream):
+        def worker(slot):
             while True:
                 with cv:
                     while True:
@@ -177,6 +223,8 @@ class Server:
                         if state["arrived"] == n and not pending:
                             return
                         cv.wait(0.05)
+                urgent = self.policy == "short-first" and work(self.cat, q) < self.urgent_below
+                stream = self.urgent[slot] if urgent else self.streams[slot]
                 q.start = now()
                 try:
                     q.result = execute(self.ctx, stream, self.cat, q)
@@ -187,7 +235,7 @@ class Server:
                     state["used"] -= fp
                     cv.notify_all()
 
-        threads = [threading.Thread(target=worker, args=(s,), daemon=True) for s in self.streams]
+        threads = [threading.Thread(target=worker, args=(k,), daemon=True) for k in range(self.slots)]
         disp = threading.Thread(target=dispatcher, daemon=True)
         state["t0"] = time.perf_counter()
         disp.start()

@@ -358,6 +358,44 @@ def test_groupby_partition_overflow(gbctx):
     assert np.array_equal(canon(got), canon(want))
 
 
+def _fused_rows(n_build, groups, n_probe, seed):
+    R = dg.build_relation(n_build, dg.seed_for(seed))
+    R[:, 1] = dg.raw_words(dg.seed_for(seed), 3, n_build) % np.uint64(groups)
+    S = dg.probe_uniform(n_probe, R, dg.seed_for(seed + 1))
+    S[:, 1] = (dg.raw_words(dg.seed_for(seed + 1), 4, n_probe) >> np.uint64(11)).astype(np.float64).view(np.int64)
+    return R, S
+
+
+@pytest.mark.parametrize("n_build,groups", [(1000, 7), (60_000, 600), (200_000, 50_000)])
+def test_hashjoin_groupby_fused(ctx, n_build, groups):
+    # Join then aggregate in one pass == materialised join, then exact group-by.
+    R, S = _fused_rows(n_build, groups, 8 * n_build, 90 + groups % 7)
+    S[::53, 0] += 10 * n_build                     # probe misses
+    joined, n, _ = orc.hashjoin(R, S, proj=(("B", 8, 8), ("P", 8, 8)), hash=orc.hashcfg("modulo", 1 << 12))
+    exact = canon(orc.groupby_exact(joined.view(np.int64).reshape(-1, 2)))
+    got = canon(ctx.hashjoin_groupby(R, S, val=(8, "dec")))
+    assert np.array_equal(got[:, :8], exact[:, :8])
+    g, e = got[:, 8:].copy().view(np.float64).ravel(), exact[:, 8:].copy().view(np.float64).ravel()
+    assert np.all(np.abs(g - e) <= DEC_RTOL * np.abs(e))
+    # Count and long sum on the same plan.
+    Sl = S.copy(); Sl[:, 1] = dg.raw_words(dg.seed_for(7), 5, S.shape[0]).view(np.int64) >> 20
+    jl, _, _ = orc.hashjoin(R, Sl, proj=(("B", 8, 8), ("P", 8, 8)), hash=orc.hashcfg("modulo", 1 << 12))
+    for agg in ("sum", "count"):
+        want = orc.groupby(jl.view(np.int64).reshape(-1, 2), val=(8, "long"), agg=agg)
+        assert np.array_equal(canon(ctx.hashjoin_groupby(R, Sl, val=(8, "long"), agg=agg)), canon(want))
+
+
+def test_hashjoin_groupby_unsupported_layouts(ctx):
+    # A hashed (sparse-key) table cannot take the one-pass plan: the caller is
+    # told so and falls back to probe + group-by.
+    R, S = _fused_rows(5000, 50, 20_000, 97)
+    R[:, 0] *= 7919
+    S[:, 0] *= 7919
+    with pytest.raises(gpu.PgError) as e:
+        ctx.hashjoin_groupby(R, S)
+    assert e.value.code == gpu.PG_ERR_UNSUPPORTED
+
+
 def test_groupby_reference_unit_test(gbctx):
     ctx = gbctx
     # unit_tests/queryaggsum.cpp: group i holds 1..i; sum must be i(i+1)/2.

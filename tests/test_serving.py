@@ -25,9 +25,9 @@ def _queries(n, fail_at=None):
 
 
 def _same(a, b):
-    ka, va, na = a
-    kb, vb, nb = b
-    assert na == nb and np.array_equal(ka, kb)
+    ka, va = serving.canonical(a)
+    kb, vb = serving.canonical(b)
+    assert np.array_equal(ka, kb)
     assert np.all(np.abs(va - vb) <= RTOL * np.abs(vb))
 
 
@@ -73,8 +73,32 @@ def test_results_match_oracle(ctx, catalog):
         S = ctx.download(t.pools[q.zipf], 16 * ns).view(np.int64).reshape(-1, 2)
         joined, n, _ = orc.hashjoin(R, S, proj=(("B", 8, 8), ("P", 8, 8)), hash=orc.hashcfg("modulo", 1 << 16))
         exact = orc.groupby_exact(joined.view(np.int64).reshape(-1, 2)).view(np.int64).reshape(-1, 2)
-        keys, sums, n_out = q.result
-        assert n_out == n
+        keys, sums = serving.canonical(q.result)
         assert np.array_equal(keys, exact[:, 0])
         ev = exact[:, 1].view(np.float64)
         assert np.all(np.abs(sums - ev) <= RTOL * np.abs(ev))
+
+
+def test_one_pass_plan_matches_two_step_plan(ctx, catalog):
+    # The fused join+group-by and the materialised probe + group-by give the
+    # same groups and sums (within the dec tolerance).
+    stream = ctx.stream
+    for table in range(len(catalog.tables)):
+        for z in (0.0, 0.8):
+            q = serving.Query(0, table, z)
+            _same(serving.execute(ctx, stream, catalog, q, fused=True),
+                  serving.execute(ctx, stream, catalog, q, fused=False))
+
+
+def test_short_first_policy_serves_everything_with_same_results(ctx, catalog):
+    fifo = serving.Server(ctx, catalog, slots=1, budget_bytes=150 << 30)
+    short = serving.Server(ctx, catalog, slots=4, budget_bytes=150 << 30, policy="short-first",
+                           max_wait=0.01, urgent_below=1 << 22)
+    try:
+        qa = fifo.run(_queries(24))
+        qb = short.run(_queries(24))
+    finally:
+        fifo.close(); short.close()
+    assert all(q.error is None and q.end is not None for q in qb)
+    for a, b in zip(qa, qb):
+        _same(a.result, b.result)
