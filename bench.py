@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 NR = 1 << 24            # overridable with --build-log2 / --probe-log2 (smaller configs)
 NS = 1 << 28
 TUPLE = 16
-PROBE_DRAM_BYTES_PER_TUPLE = (1.094478e9 + 0.517657e9) / (1 << 25)
+PROBE_DRAM_BYTES_PER_TUPLE = (1.153772e9 + 0.516699e9) / (1 << 25)
 METRIC = "join tuples/s (16M build x 256M probe, PK-FK, int64 keys, materialised)"
 WORKLOAD = "radix-scale PK-FK hash join: |R|=16M unique int64 keys, |S|=256M uniform FK, 16-byte tuples, output (P$1,B$1)"
 

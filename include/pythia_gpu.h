@@ -267,6 +267,13 @@ int pg_batch_prepare(pg_ctx* ctx, pg_stream stream, const pg_batch_item* items, 
 		const pg_batch_shape* shape, pg_batch** batch);
 int pg_batch_run(pg_ctx* ctx, pg_batch* batch, uint64_t* counts_host);
 int pg_batch_free(pg_ctx* ctx, pg_batch* batch);
+/* Launch-shape autotuner over batches (no reference counterpart: the reference
+ * has no tunables at this level): prepares, warms and times each of the
+ * n_shapes candidate shapes on these instances (CUDA events, best of
+ * `repeats`), returns the fastest index in *best and each shape's time in
+ * ms_out[] (n_shapes entries, may be NULL). */
+int pg_autotune_batch(pg_ctx* ctx, pg_stream stream, const pg_batch_item* items, uint32_t n,
+		const pg_batch_shape* shapes, uint32_t n_shapes, int repeats, uint32_t* best, double* ms_out);
 /* Synthetic foreign keys for benchmarks: S[j] = (R[h(seed, j) mod nR].key,
  * h'(seed, j)), 16-byte tuples, h a SplitMix64 counter hash. */
 int pg_generate_fk(pg_ctx* ctx, pg_stream stream, const void* R, uint64_t nR, uint64_t seed,

@@ -14,7 +14,7 @@ GPU name, so later runs reuse them.
 import ctypes
 import json
 import os
-import time
+import time  # noqa: F401  (time_batch)
 
 from pythia_gb300 import gpu
 
@@ -73,25 +73,25 @@ def time_batch(ctx, b, repeats=3):
 
 
 def tune_batch(ctx, items_by_class, shapes=BATCH_SHAPES, repeats=3, log=None):
-    """items_by_class: {class: [(R_ptr, nR, S_ptr, nS), ...]}. Returns the
-    fastest shape per class and the sweep table."""
+    """items_by_class: {class: [(R_ptr, nR, S_ptr, nS), ...]}. Times every
+    shape per class in the library (pg_autotune_batch, CUDA events) and
+    returns the fastest shape per class and the sweep table."""
     best, table = {}, {}
+    arr_shapes = (gpu.BatchShape * len(shapes))(*[shape_struct(sh) for sh in shapes])
     for cls, items in items_by_class.items():
         if not items:
             continue
-        rows = []
-        for sh in shapes:
-            b = prepare(ctx, items, sh)
-            try:
-                t = time_batch(ctx, b, repeats)
-            finally:
-                free(ctx, b)
-            rows.append((t, sh))
-            if log:
-                log(f"{cls} {sh} {t * 1e3:.3f} ms")
-        rows.sort(key=lambda r: r[0])
-        best[cls] = rows[0][1]
-        table[cls] = [{"ms": r[0] * 1e3, **r[1]} for r in rows]
+        arr = (gpu.BatchItem * len(items))(*[gpu.BatchItem(R, nR, S, nS) for (R, nR, S, nS) in items])
+        pick = ctypes.c_uint32()
+        ms = (ctypes.c_double * len(shapes))()
+        ctx._check(gpu.lib().pg_autotune_batch(ctx.h, ctx.stream, arr, len(items), arr_shapes, len(shapes),
+                                               repeats, ctypes.byref(pick), ms))
+        rows = sorted(((ms[k], shapes[k]) for k in range(len(shapes))), key=lambda r: r[0])
+        if log:
+            for t, sh in rows:
+                log(f"{cls} {sh} {t:.3f} ms")
+        best[cls] = shapes[pick.value]
+        table[cls] = [{"ms": t, **sh} for t, sh in rows]
     return best, table
 
 

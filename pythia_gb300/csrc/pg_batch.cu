@@ -295,6 +295,46 @@ extern "C" int pg_batch_free(pg_ctx* ctx, pg_batch* b)
 }
 
 // ---------------------------------------------------------------------------
+// Launch-shape autotuner: every candidate shape is prepared on the caller's
+// instances, replayed once to warm up, then timed `repeats` times with CUDA
+// events on the batch's stream; the fastest shape wins. Shapes change speed,
+// never counts, so the sweep needs no checking beyond the status word.
+// ---------------------------------------------------------------------------
+extern "C" int pg_autotune_batch(pg_ctx* ctx, pg_stream stream, const pg_batch_item* items, uint32_t n,
+		const pg_batch_shape* shapes, uint32_t n_shapes, int repeats, uint32_t* best, double* ms_out)
+{
+	if (!ctx || !shapes || !n_shapes || !best || (n && !items) || repeats < 1)
+		return pg_fail(ctx, PG_ERR_ARG, "pg_autotune_batch: bad argument");
+	cudaEvent_t e0, e1;
+	PG_CUDA(ctx, cudaEventCreate(&e0));
+	PG_CUDA(ctx, cudaEventCreate(&e1));
+	double best_ms = 1e300;
+	*best = 0;
+	int rc = PG_OK;
+	for (uint32_t k = 0; k < n_shapes && rc == PG_OK; ++k) {
+		pg_batch* b = nullptr;
+		if ((rc = pg_batch_prepare(ctx, stream, items, n, &shapes[k], &b))) break;
+		double mine = 1e300;
+		rc = pg_batch_run(ctx, b, nullptr);
+		for (int r = 0; r < repeats && rc == PG_OK; ++r) {
+			cudaEventRecord(e0, b->stream);
+			if ((rc = pg_batch_run(ctx, b, nullptr))) break;
+			cudaEventRecord(e1, b->stream);
+			if (cudaEventSynchronize(e1) != cudaSuccess) { rc = pg_cuda_fail(ctx, cudaGetLastError(), "pg_autotune_batch"); break; }
+			float ms = 0.f;
+			cudaEventElapsedTime(&ms, e0, e1);
+			mine = std::min(mine, (double) ms);
+		}
+		pg_batch_free(ctx, b);
+		if (ms_out) ms_out[k] = mine;
+		if (rc == PG_OK && mine < best_ms) { best_ms = mine; *best = k; }
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	return rc;
+}
+
+// ---------------------------------------------------------------------------
 // Zipf foreign keys on the device (rejection-inversion, Hormann & Derflinger
 // 1996): rank k in [1, n] with P(k) ~ k^-s, drawn from a counter hash of
 // (seed, j, attempt); s = 0 draws ranks uniformly. Dec payload uniform in

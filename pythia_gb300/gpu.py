@@ -64,7 +64,7 @@ SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_st
            "pg_groupby", "pg_sort_pages", "pg_mpsm_join", "pg_hashjoin_agg_noalloc",
            "pg_tune_set", "pg_tune_get", "pg_batch_prepare", "pg_batch_run", "pg_batch_free",
            "pg_generate_fk", "pg_buffer_alloc_async", "pg_buffer_free_async", "pg_generate_zipf_fk",
-           "pg_hashjoin_groupby", "pg_stream_create_urgent"]
+           "pg_hashjoin_groupby", "pg_stream_create_urgent", "pg_autotune_batch"]
 TUNE = {"probe_ctas_per_sm": 0, "probe_variant": 1, "dense": 2, "partition_tile": 3,
         "groupby_smem_groups": 4, "radix_bits": 5, "probe_items": 6, "probe_cache": 7, "probe_passes": 8, "groupby_path": 9}
 
@@ -120,6 +120,7 @@ def lib():
             "pg_buffer_free_async": ([vp, vp, vp], ci),
             "pg_hashjoin_groupby": ([vp, vp, vp, P(Rel), u32, ci, ci, vp, u64, P(u64)], ci),
             "pg_stream_create_urgent": ([vp, P(vp)], ci),
+            "pg_autotune_batch": ([vp, vp, P(BatchItem), u32, P(BatchShape), u32, ci, P(u32), P(ctypes.c_double)], ci),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

@@ -519,6 +519,20 @@ def test_batch_join_count_matches_oracle(ctx):
                 assert counts.tolist() == want
         finally:
             autotune.free(ctx, b)
+    # The library autotuner times every candidate and picks one of them; the
+    # pick gives the same counts.
+    shapes = autotune.BATCH_SHAPES[:4]
+    best, table = autotune.tune_batch(ctx, {"mixed": items}, shapes=shapes, repeats=2)
+    assert best["mixed"] in shapes and len(table["mixed"]) == 4
+    assert all(r["ms"] > 0 for r in table["mixed"])
+    assert table["mixed"][0]["ms"] == min(r["ms"] for r in table["mixed"])
+    b = autotune.prepare(ctx, items, best["mixed"])
+    try:
+        counts = np.zeros(len(items), dtype=np.uint64)
+        autotune.run(ctx, b, counts)
+        assert counts.tolist() == want
+    finally:
+        autotune.free(ctx, b)
 
 
 def test_generate_fk_matches_host_replica(ctx):
