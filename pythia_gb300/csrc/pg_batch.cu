@@ -10,11 +10,15 @@
 // without per-instance launch overhead. The sequence (table clear, build,
 // probe, count copy-out) can be captured once as a CUDA graph and replayed.
 //
-// Every instance gets its own open-addressing table region (16-byte slots,
-// linear probing from an even slot, 32-byte bucket loads on probe) sized by
-// the class's load factor. Launch shape (threads per CTA, tile size, CTAs per
-// SM) and load factor come from pg_batch_shape, which the autotuner chooses
-// per size class.
+// An instance whose build keys are unique and whose key range needs no more
+// bytes as a bitmap than its hash table would (range / 8 <= 16 * slots) gets a
+// presence bitmap: the probe of a count-only PK-FK join then reads one bit
+// per probe tuple, and the bitmaps of a wave stay in L2. Other instances get
+// their own open-addressing table region (16-byte slots, linear probing from
+// an even slot, 32-byte bucket loads on probe) sized by the class's load
+// factor. Launch shape (threads per CTA, tile size, CTAs per SM) and load
+// factor come from pg_batch_shape, which the autotuner chooses per size
+// class.
 #include "pg_internal.cuh"
 #include <algorithm>
 #include <vector>
@@ -22,9 +26,11 @@
 struct BatchInst {
 	const char* R; const char* S;
 	uint64_t nR, nS;
-	uint64_t table_off;     // first slot of the instance's table
+	uint64_t table_off;     // hashed: first slot of the instance's table; bitmap: first word
 	uint32_t log2cap;
-	uint32_t pad;
+	uint32_t mode;          // 0 hashed table, 1 presence bitmap over keys [kmin, kmin + range)
+	long long kmin;
+	uint64_t range;
 };
 
 struct BatchTile {           // [begin, end) of one side of instance `inst`
@@ -38,12 +44,33 @@ __device__ __forceinline__ uint64_t bt_slot0(int64_t k, uint32_t log2cap)
 	return (pg_mix64((uint64_t) k) >> (65 - log2cap)) << 1;
 }
 
+// Build. Bitmap instances set their keys' bits; a bit found set already (a
+// repeated key) or a key outside the range marks the instance in `dup` (the
+// prepare-time trial) or fails the batch (a replay whose build side changed
+// since prepare: PG_ERR_ARG).
 __global__ void k_batch_build(const BatchInst* __restrict__ inst, const BatchTile* __restrict__ tiles,
-		uint64_t ntiles, unsigned long long* __restrict__ slots, int* __restrict__ status)
+		uint64_t ntiles, unsigned long long* __restrict__ slots, uint32_t* __restrict__ bits,
+		int* __restrict__ dup, bool trial, int* __restrict__ status)
 {
 	for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
 		const BatchTile tl = tiles[t];
 		const BatchInst in = inst[tl.inst];
+		if (in.mode == 1) {
+			bool bad = false;
+			for (uint64_t i = tl.begin + threadIdx.x; i < tl.end; i += blockDim.x) {
+				const long long k = reinterpret_cast<const long long*>(in.R)[2 * i];
+				const unsigned long long d = (unsigned long long) k - (unsigned long long) in.kmin;
+				if (d >= in.range) { bad = true; continue; }
+				const uint32_t bit = 1u << (d & 31);
+				if (atomicOr(&bits[in.table_off + (d >> 5)], bit) & bit) bad = true;
+			}
+			if (bad) {
+				if (trial) dup[tl.inst] = 1;
+				else pg_set_status(status, PG_ERR_ARG);
+			}
+			continue;
+		}
+		if (trial) continue;        // the trial builds bitmaps only (no slots exist yet)
 		unsigned long long* tab = slots + 2 * in.table_off;
 		const uint64_t mask = (1ull << in.log2cap) - 1;
 		for (uint64_t i = tl.begin + threadIdx.x; i < tl.end; i += blockDim.x) {
@@ -66,7 +93,8 @@ __global__ void k_batch_build(const BatchInst* __restrict__ inst, const BatchTil
 // probe walks its whole sequence). One atomicAdd per tile and CTA.
 template <int ITEMS>
 __global__ void k_batch_probe_count(const BatchInst* __restrict__ inst, const BatchTile* __restrict__ tiles,
-		uint64_t ntiles, const unsigned long long* __restrict__ slots, unsigned long long* __restrict__ counts)
+		uint64_t ntiles, const unsigned long long* __restrict__ slots, const uint32_t* __restrict__ bits,
+		unsigned long long* __restrict__ counts)
 {
 	__shared__ unsigned long long wsum[32];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -77,6 +105,23 @@ __global__ void k_batch_probe_count(const BatchInst* __restrict__ inst, const Ba
 		const unsigned long long* tab = slots + 2 * in.table_off;
 		const uint64_t mask = (1ull << in.log2cap) - 1;
 		unsigned long long c = 0;
+		if (in.mode == 1) {
+			// Presence bitmap: one bit per probe tuple.
+			for (uint64_t base = tl.begin; base < tl.end; base += (uint64_t) blockDim.x * ITEMS) {
+				uint32_t w[ITEMS];
+				uint64_t d[ITEMS];
+				#pragma unroll
+				for (int j = 0; j < ITEMS; ++j) {
+					const uint64_t i = base + (uint64_t) j * blockDim.x + threadIdx.x;
+					d[j] = ~0ull; w[j] = 0;
+					if (i < tl.end)
+						d[j] = (unsigned long long) reinterpret_cast<const long long*>(in.S)[2 * i] - (unsigned long long) in.kmin;
+					if (d[j] < in.range) w[j] = __ldg(bits + in.table_off + (d[j] >> 5));
+				}
+				#pragma unroll
+				for (int j = 0; j < ITEMS; ++j) c += d[j] < in.range ? (w[j] >> (d[j] & 31)) & 1 : 0;
+			}
+		} else
 		for (uint64_t base = tl.begin; base < tl.end; base += (uint64_t) blockDim.x * ITEMS) {
 			long long key[ITEMS];
 			uint64_t slot[ITEMS];
@@ -116,6 +161,29 @@ __global__ void k_batch_probe_count(const BatchInst* __restrict__ inst, const Ba
 			if (tot) atomicAdd(&counts[tl.inst], tot);
 		}
 		__syncthreads();
+	}
+}
+
+// Per-instance key minimum and maximum (sign-flipped for unsigned atomics).
+__global__ void k_batch_minmax(const BatchInst* __restrict__ inst, const BatchTile* __restrict__ tiles,
+		uint64_t ntiles, unsigned long long* __restrict__ mm)
+{
+	for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+		const BatchTile tl = tiles[t];
+		const BatchInst in = inst[tl.inst];
+		unsigned long long lo = ~0ull, hi = 0;
+		for (uint64_t i = tl.begin + threadIdx.x; i < tl.end; i += blockDim.x) {
+			const unsigned long long u = (unsigned long long) reinterpret_cast<const long long*>(in.R)[2 * i] ^ (1ull << 63);
+			lo = u < lo ? u : lo;
+			hi = u > hi ? u : hi;
+		}
+		#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			const unsigned long long a = __shfl_down_sync(0xffffffffu, lo, o), b = __shfl_down_sync(0xffffffffu, hi, o);
+			lo = a < lo ? a : lo;
+			hi = b > hi ? b : hi;
+		}
+		if ((threadIdx.x & 31) == 0) { atomicMin(&mm[2 * tl.inst], lo); atomicMax(&mm[2 * tl.inst + 1], hi); }
 	}
 }
 
@@ -169,6 +237,9 @@ struct pg_batch {
 	uint64_t nbtiles, nptiles;
 	unsigned long long* d_slots;
 	uint64_t nslots;
+	uint32_t* d_bits;           // presence bitmaps of bitmap instances
+	uint64_t nbits_words;
+	int* d_dup;                 // per instance: repeated key seen in the prepare trial
 	unsigned long long* d_counts;
 	pg_batch_shape shape;
 	cudaGraphExec_t graph;
@@ -179,21 +250,23 @@ static int batch_launch(pg_batch* b, cudaStream_t s)
 {
 	pg_ctx* ctx = b->ctx;
 	PG_CUDA(ctx, cudaMemsetAsync(b->d_slots, 0xFF, b->nslots * 16, s));
+	PG_CUDA(ctx, cudaMemsetAsync(b->d_bits, 0, b->nbits_words * 4, s));
 	PG_CUDA(ctx, cudaMemsetAsync(b->d_counts, 0, b->ninst * 8, s));
 	const int per_sm = b->shape.ctas_per_sm > 0 ? b->shape.ctas_per_sm : 4;
 	const int threads = b->shape.threads > 0 ? b->shape.threads : 256;
 	if (b->nbtiles) {
 		const int grid = (int) std::min<uint64_t>(b->nbtiles, (uint64_t) ctx->sm_count * per_sm);
-		k_batch_build<<<grid, threads, 0, s>>>(b->d_inst, b->d_btiles, b->nbtiles, b->d_slots, ctx->d_status);
+		k_batch_build<<<grid, threads, 0, s>>>(b->d_inst, b->d_btiles, b->nbtiles, b->d_slots, b->d_bits, b->d_dup,
+				false, ctx->d_status);
 		PG_LAUNCHED(ctx);
 	}
 	if (b->nptiles) {
 		const int grid = (int) std::min<uint64_t>(b->nptiles, (uint64_t) ctx->sm_count * per_sm);
 		switch (b->shape.items) {
-		case 1: k_batch_probe_count<1><<<grid, threads, 0, s>>>(b->d_inst, b->d_ptiles, b->nptiles, b->d_slots, b->d_counts); break;
-		case 2: k_batch_probe_count<2><<<grid, threads, 0, s>>>(b->d_inst, b->d_ptiles, b->nptiles, b->d_slots, b->d_counts); break;
-		case 8: k_batch_probe_count<8><<<grid, threads, 0, s>>>(b->d_inst, b->d_ptiles, b->nptiles, b->d_slots, b->d_counts); break;
-		default: k_batch_probe_count<4><<<grid, threads, 0, s>>>(b->d_inst, b->d_ptiles, b->nptiles, b->d_slots, b->d_counts); break;
+		case 1: k_batch_probe_count<1><<<grid, threads, 0, s>>>(b->d_inst, b->d_ptiles, b->nptiles, b->d_slots, b->d_bits, b->d_counts); break;
+		case 2: k_batch_probe_count<2><<<grid, threads, 0, s>>>(b->d_inst, b->d_ptiles, b->nptiles, b->d_slots, b->d_bits, b->d_counts); break;
+		case 8: k_batch_probe_count<8><<<grid, threads, 0, s>>>(b->d_inst, b->d_ptiles, b->nptiles, b->d_slots, b->d_bits, b->d_counts); break;
+		default: k_batch_probe_count<4><<<grid, threads, 0, s>>>(b->d_inst, b->d_ptiles, b->nptiles, b->d_slots, b->d_bits, b->d_counts); break;
 		}
 		PG_LAUNCHED(ctx);
 	}
@@ -222,7 +295,7 @@ extern "C" int pg_batch_prepare(pg_ctx* ctx, pg_stream stream, const pg_batch_it
 			return pg_fail(ctx, PG_ERR_ARG, "pg_batch_prepare: relations must be 16-byte aligned");
 		uint32_t lg = 6;
 		while ((1ull << lg) < (uint64_t) sh.load_inverse * it.nR) ++lg;
-		inst[i] = BatchInst{(const char*) it.R, (const char*) it.S, it.nR, it.nS, slots, lg, 0};
+		inst[i] = BatchInst{(const char*) it.R, (const char*) it.S, it.nR, it.nS, slots, lg, 0, 0, 0};
 		slots += 1ull << lg;
 		for (uint64_t b = 0; b < it.nR; b += sh.tile) bt.push_back(BatchTile{i, 0, b, std::min<uint64_t>(it.nR, b + sh.tile)});
 		for (uint64_t b = 0; b < it.nS; b += sh.tile) pt.push_back(BatchTile{i, 0, b, std::min<uint64_t>(it.nS, b + sh.tile)});
@@ -231,13 +304,73 @@ extern "C" int pg_batch_prepare(pg_ctx* ctx, pg_stream stream, const pg_batch_it
 	bb->ctx = ctx; bb->stream = s; bb->ninst = n; bb->shape = sh;
 	bb->nbtiles = bt.size(); bb->nptiles = pt.size(); bb->nslots = std::max<uint64_t>(slots, 1);
 	bb->has_graph = false;
+	bb->nbits_words = 1;
 	int rc = PG_OK;
 	cudaError_t e;
 	if ((e = cudaMalloc(&bb->d_inst, std::max<size_t>(1, n) * sizeof(BatchInst))) ||
 			(e = cudaMalloc(&bb->d_btiles, std::max<size_t>(1, bt.size()) * sizeof(BatchTile))) ||
 			(e = cudaMalloc(&bb->d_ptiles, std::max<size_t>(1, pt.size()) * sizeof(BatchTile))) ||
-			(e = cudaMalloc(&bb->d_slots, bb->nslots * 16)) ||
-			(e = cudaMalloc(&bb->d_counts, std::max<size_t>(1, n) * 8))) {
+			(e = cudaMalloc(&bb->d_counts, std::max<size_t>(1, n) * 8)) ||
+			(e = cudaMalloc(&bb->d_dup, std::max<size_t>(1, n) * sizeof(int)))) {
+		rc = pg_cuda_fail(ctx, e, "pg_batch_prepare: cudaMalloc");
+		pg_batch_free(ctx, bb);
+		return rc;
+	}
+	// Layout choice: per-instance key ranges (one pass over the build sides);
+	// instances whose bitmap is no larger than their hash table try the
+	// bitmap, and a trial build drops those with repeated keys back to the
+	// hash table.
+	if (n && !bt.empty()) {
+		unsigned long long* mm = nullptr;
+		if ((e = cudaMalloc(&mm, 16 * (size_t) n))) { pg_batch_free(ctx, bb); return pg_cuda_fail(ctx, e, "pg_batch_prepare: cudaMalloc"); }
+		std::vector<unsigned long long> init(2 * (size_t) n);
+		for (uint32_t i = 0; i < n; ++i) { init[2 * i] = ~0ull; init[2 * i + 1] = 0; }
+		PG_CUDA(ctx, cudaMemcpyAsync(mm, init.data(), 16 * (size_t) n, cudaMemcpyHostToDevice, s));
+		PG_CUDA(ctx, cudaMemcpyAsync(bb->d_inst, inst.data(), n * sizeof(BatchInst), cudaMemcpyHostToDevice, s));
+		PG_CUDA(ctx, cudaMemcpyAsync(bb->d_btiles, bt.data(), bt.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, s));
+		k_batch_minmax<<<(int) std::min<uint64_t>(bt.size(), (uint64_t) ctx->sm_count * 8), 256, 0, s>>>(
+				bb->d_inst, bb->d_btiles, bt.size(), mm);
+		PG_LAUNCHED(ctx);
+		PG_CUDA(ctx, cudaMemcpyAsync(init.data(), mm, 16 * (size_t) n, cudaMemcpyDeviceToHost, s));
+		PG_CUDA(ctx, cudaStreamSynchronize(s));
+		cudaFree(mm);
+		uint64_t words = 0;
+		for (uint32_t i = 0; i < n; ++i) {
+			if (inst[i].nR == 0) continue;
+			const long long kmin = (long long) (init[2 * i] ^ (1ull << 63));
+			const long long kmax = (long long) (init[2 * i + 1] ^ (1ull << 63));
+			const uint64_t range = (uint64_t) kmax - (uint64_t) kmin + 1;
+			if (range == 0 || range > (1ull << 32) || range / 8 > (1ull << inst[i].log2cap) * 16) continue;
+			inst[i].mode = 1; inst[i].kmin = kmin; inst[i].range = range; inst[i].table_off = words;
+			words += pg_div_up(range, 32);
+		}
+		bb->nbits_words = std::max<uint64_t>(words, 1);
+		if ((e = cudaMalloc(&bb->d_bits, bb->nbits_words * 4))) { pg_batch_free(ctx, bb); return pg_cuda_fail(ctx, e, "pg_batch_prepare: cudaMalloc"); }
+		if (words) {
+			PG_CUDA(ctx, cudaMemcpyAsync(bb->d_inst, inst.data(), n * sizeof(BatchInst), cudaMemcpyHostToDevice, s));
+			PG_CUDA(ctx, cudaMemsetAsync(bb->d_bits, 0, bb->nbits_words * 4, s));
+			PG_CUDA(ctx, cudaMemsetAsync(bb->d_dup, 0, n * sizeof(int), s));
+			k_batch_build<<<(int) std::min<uint64_t>(bt.size(), (uint64_t) ctx->sm_count * 8), 256, 0, s>>>(
+					bb->d_inst, bb->d_btiles, bt.size(), nullptr, bb->d_bits, bb->d_dup, true, ctx->d_status);
+			PG_LAUNCHED(ctx);
+			std::vector<int> dup(n);
+			PG_CUDA(ctx, cudaMemcpyAsync(dup.data(), bb->d_dup, n * sizeof(int), cudaMemcpyDeviceToHost, s));
+			PG_CUDA(ctx, cudaStreamSynchronize(s));
+			for (uint32_t i = 0; i < n; ++i)
+				if (dup[i] && inst[i].mode == 1) { inst[i].mode = 0; inst[i].kmin = 0; inst[i].range = 0; }
+		}
+	} else if ((e = cudaMalloc(&bb->d_bits, 4))) {
+		pg_batch_free(ctx, bb); return pg_cuda_fail(ctx, e, "pg_batch_prepare: cudaMalloc");
+	}
+	// Hash-table slots for the instances left on the hashed layout.
+	slots = 0;
+	for (uint32_t i = 0; i < n; ++i) {
+		if (inst[i].mode == 1) continue;
+		inst[i].table_off = slots;
+		slots += 1ull << inst[i].log2cap;
+	}
+	bb->nslots = std::max<uint64_t>(slots, 1);
+	if ((e = cudaMalloc(&bb->d_slots, bb->nslots * 16))) {
 		rc = pg_cuda_fail(ctx, e, "pg_batch_prepare: cudaMalloc");
 		pg_batch_free(ctx, bb);
 		return rc;
@@ -288,7 +421,7 @@ extern "C" int pg_batch_free(pg_ctx* ctx, pg_batch* b)
 	cudaStreamSynchronize(b->stream);
 	if (b->has_graph) cudaGraphExecDestroy(b->graph);
 	cudaFree(b->d_inst); cudaFree(b->d_btiles); cudaFree(b->d_ptiles);
-	cudaFree(b->d_slots); cudaFree(b->d_counts);
+	cudaFree(b->d_slots); cudaFree(b->d_counts); cudaFree(b->d_bits); cudaFree(b->d_dup);
 	delete b;
 	(void) ctx;
 	return PG_OK;

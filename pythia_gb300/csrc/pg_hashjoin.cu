@@ -881,7 +881,9 @@ __device__ __forceinline__ void hj_st_stream(char* p, uint4 v, uint64_t pol)
 			:: "l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol));
 }
 
-template <bool MATERIALIZE, int MODE, bool PF>
+// STD: the output row is (probe words 2-3, value) = the (P$1, B$1) projection
+// of 16-byte tuples, picked without the general word selector.
+template <bool MATERIALIZE, int MODE, bool PF, bool STD = false>
 __global__ void __launch_bounds__(PW_WARPS * 32, PF ? 4 : 5)
 k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb,
 		uint32_t wsel, uint32_t sum_w0, uint32_t sum_words, char* __restrict__ out,
@@ -949,8 +951,11 @@ k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const Hj
 				if (MATERIALIZE) {
 					const uint32_t r = rank + __popc(ball & ((1u << lane) - 1));
 					const uint64_t row = run == 1 ? c * PW_CHUNK + rows - 1 - r : c * PW_CHUNK + r;
-					hj_st_stream(out + row * 16, make_uint4(hj_pick(t, v, w0), hj_pick(t, v, w1),
-							hj_pick(t, v, w2), hj_pick(t, v, w3)), stream);
+					if (STD)
+						hj_st_stream(out + row * 16, make_uint4(t.z, t.w, (uint32_t) v, (uint32_t) (v >> 32)), stream);
+					else
+						hj_st_stream(out + row * 16, make_uint4(hj_pick(t, v, w0), hj_pick(t, v, w1),
+								hj_pick(t, v, w2), hj_pick(t, v, w3)), stream);
 				} else if (sum_col >= 0) {
 					const uint32_t lo = hj_pick(t, v, (wsel >> (4 * sum_w0)) & 15);
 					if (sum_words == 2)
@@ -1406,7 +1411,10 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 					const int dgrid = (int) std::min<uint64_t>(wchunks, (uint64_t) ctx->sm_count * want);
 #define PD_LAUNCH(M, D, P) k_probe16_direct<M, D, P><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, wsel, sum_w0, \
 						sum_words, M ? out : nullptr, M ? counts : nullptr, M ? acc : acc + 1, M ? -1 : sum_col, dlo, dhi, run)
-					if (materialize) {
+					if (materialize && mode == 2 && pf && wsel == 0x5432u) {
+						k_probe16_direct<true, 2, true, true><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, wsel, sum_w0,
+								sum_words, out, counts, acc, -1, dlo, dhi, run);
+					} else if (materialize) {
 						if (mode == 2) { if (pf) PD_LAUNCH(true, 2, true); else PD_LAUNCH(true, 2, false); }
 						else { if (pf) PD_LAUNCH(true, 1, true); else PD_LAUNCH(true, 1, false); }
 					} else {
