@@ -12,8 +12,8 @@
 // the bucket-major counts gives every CTA its first output slot per bucket.
 // Pass 2 (k_part_scatter) streams the chunk again in tiles staged in shared
 // memory by bulk copies (cp.async.bulk + mbarrier, double-buffered), ranks
-// tuples within the tile per bucket (warp match + per-warp counters, which
-// keeps the order stable), and writes each tile out grouped by bucket so a
+// tuples within the tile per bucket (per-warp ballots over the bucket bits +
+// per-warp counters, which keeps the order stable), and writes each tile out grouped by bucket so a
 // warp's stores go to consecutive addresses of one partition
 // (write-combining through shared memory).
 #include "pg_internal.cuh"
@@ -73,6 +73,7 @@ k_part_scatter(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t kof
 	__shared__ uint32_t carry;
 
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const uint32_t nbits = B > 1 ? 32 - __clz(B - 1) : 0;
 	const uint64_t first = (uint64_t) blockIdx.x * tiles_per_cta;
 	const uint64_t ntiles_total = pg_div_up(n, tile);
 	const uint64_t last = std::min<uint64_t>(ntiles_total, first + tiles_per_cta);
@@ -121,14 +122,22 @@ k_part_scatter(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t kof
 		if (t + 1 < last) next_bulk = issue(t + 1);
 
 		// (1) rank within the tile: warp w owns rows [w*sub, (w+1)*sub).
+		// Lanes with the same bucket are found with one ballot per bucket
+		// bit (the bucket index has nbits bits): cheaper than a match over
+		// 32-bit values, with the same peer masks.
 		const uint32_t sub = tile / NW;
 		uint16_t* mycnt = cnt + warp * B;
 		for (uint32_t it = 0; it < sub; it += 32) {
 			uint32_t p = warp * sub + it + lane;
 			bool valid = p < rows;
-			uint32_t b = valid ? pg_hash_field(f, reinterpret_cast<const char*>(cur) + (uint64_t) p * W + koff, kbytes) : 0xFFFFFFFFu;
+			uint32_t b = valid ? pg_hash_field(f, reinterpret_cast<const char*>(cur) + (uint64_t) p * W + koff, kbytes) : 0u;
 			if (valid && b >= B) { pg_set_status(status, PG_ERR_ARG); b = 0; }
-			uint32_t peers = __match_any_sync(0xffffffffu, b);
+			uint32_t peers = __ballot_sync(0xffffffffu, valid);
+			for (uint32_t k = 0; k < nbits; ++k) {
+				const bool on = (b >> k) & 1u;
+				const uint32_t m = __ballot_sync(0xffffffffu, on);
+				peers &= on ? m : ~m;
+			}
 			uint32_t leader = __ffs(peers) - 1;
 			uint32_t below = peers & ((1u << lane) - 1);
 			uint32_t old = 0;
