@@ -400,3 +400,9 @@ int pg_scan_u64(pg_ctx* ctx, cudaStream_t s, uint64_t* data, uint64_t n, uint64_
 	}
 	return PG_OK;
 }
+
+__global__ void k_fill_u64(unsigned long long* p, uint64_t n, unsigned long long v)
+{
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+		p[i] = v;
+}

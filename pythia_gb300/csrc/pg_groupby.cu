@@ -39,13 +39,13 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
 }
 
 // Adds v (+ compensation c) into (hi, lo): one atomic on hi, whose old value
-// gives the rounding error of this addition exactly, and one on lo when that
+// gives the rounding error of this addition exactly (computed from the bit
+// patterns with integer operations, pg_add_err), and one on lo when that
 // error (plus c) is not zero.
 __device__ __forceinline__ void atomic_comp_add(double* hi, double* lo, double v, double c)
 {
 	double old = atomicAdd(hi, v);
-	double s, e;
-	fast_two_sum(old, v, s, e);
+	double e = pg_add_err(old, v);
 	if (nonzero(c)) e += c;
 	if (nonzero(e)) atomicAdd(lo, e);
 }
@@ -260,8 +260,7 @@ k_gb_insert_ilp(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t ko
 			#pragma unroll
 			for (int j = 0; j < GB_ILP; ++j) {
 				if (!lead[j]) continue;
-				double sres, e;
-				fast_two_sum(old[j], dv[j], sres, e);
+				double e = pg_add_err(old[j], dv[j]);
 				if (MATCH && nonzero(dc[j])) e += dc[j];
 				if (nonzero(e)) atomicAdd(&t.lo[slot[j]], e);
 			}
@@ -526,10 +525,11 @@ k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, u
 			#pragma unroll
 			for (int j = 0; j < GBD_ILP; ++j) {
 				if (!ok[j]) continue;
-				double sres, e;
-				fast_two_sum(old[j], dv[j], sres, e);
+				const double e = pg_add_err(old[j], dv[j]);
 				if (nonzero(e)) atomicAdd(&lo[d[j]], e);
-				present[d[j]] = 1;
+				// hi starts at -0.0, which adds to any value exactly: the add
+				// that returns that pattern is the group's first, and marks it.
+				if ((unsigned long long) __double_as_longlong(old[j]) == PG_NEG_ZERO) present[d[j]] = 1;
 			}
 		} else {
 			#pragma unroll
@@ -571,7 +571,7 @@ __global__ void k_gb_dense_emit(const unsigned long long* __restrict__ acc, cons
 		if (aw == 4) *reinterpret_cast<uint32_t*>(o) = (uint32_t) acc[i];
 		else {
 			unsigned long long a = acc[i];
-			if (VT == PG_VAL_DEC && AGG == PG_AGG_SUM)
+			if (VT == PG_VAL_DEC && AGG == PG_AGG_SUM && nonzero(lo[i]))   // hi alone keeps the sign of a zero sum
 				a = (unsigned long long) __double_as_longlong(__longlong_as_double((long long) a) + lo[i]);
 			reinterpret_cast<uint32_t*>(o)[0] = (uint32_t) a;
 			reinterpret_cast<uint32_t*>(o)[1] = (uint32_t) (a >> 32);
@@ -614,6 +614,12 @@ static int gb_dense(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff
 	unsigned long long* cursor = reinterpret_cast<unsigned long long*>(lo + range);
 	unsigned char* present = reinterpret_cast<unsigned char*>(cursor + 1);
 	PG_CUDA(ctx, cudaMemsetAsync(mem, 0, bytes, s));
+	if (VT == PG_VAL_DEC && AGG == PG_AGG_SUM) {
+		// Sums start at -0.0 so that the first add of a group is recognisable.
+		k_fill_u64<<<(int) std::min<uint64_t>(pg_div_up(range, 256), (uint64_t) ctx->sm_count * 8), 256, 0, s>>>(
+				acc, range, PG_NEG_ZERO);
+		PG_LAUNCHED(ctx);
+	}
 	const int gblocks = (int) std::min<uint64_t>(pg_div_up(in->n, (uint64_t) GB_THREADS * GBD_ILP), (uint64_t) ctx->sm_count * 8);
 	if (vec16) k_gb_dense<VT, AGG, true><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, in->width,
 			in->key_off, in->key_bytes, voff, kmin, acc, lo, present);

@@ -1781,10 +1781,10 @@ k_probe16_groupby(const char* __restrict__ S, uint64_t n, uint32_t koff, const H
 			#pragma unroll
 			for (int j = 0; j < ITEMS; ++j) {
 				if (e[j] == 0xFFFFFFFFu) continue;
-				double sres, err;
-				fast_two_sum(old[j], v[j], sres, err);
+				const double err = pg_add_err(old[j], v[j]);
 				if (nonzero(err)) atomicAdd(&lo[e[j]], err);
-				present[e[j]] = 1;
+				// Sums start at -0.0: the add that returns it is the group's first.
+				if ((unsigned long long) __double_as_longlong(old[j]) == PG_NEG_ZERO) present[e[j]] = 1;
 			}
 		} else {
 			#pragma unroll
@@ -1833,6 +1833,11 @@ extern "C" int pg_hashjoin_groupby(pg_ctx* ctx, pg_stream stream, pg_hashtable* 
 	unsigned long long* cursor = reinterpret_cast<unsigned long long*>(lo + vrange);
 	unsigned char* present = reinterpret_cast<unsigned char*>(cursor + 1);
 	PG_CUDA(ctx, cudaMemsetAsync(mem, 0, bytes, s));
+	if (agg == PG_AGG_SUM && val_type == PG_VAL_DEC) {
+		k_fill_u64<<<(int) std::min<uint64_t>(pg_div_up(vrange, 256), (uint64_t) ctx->sm_count * 8), 256, 0, s>>>(
+				acc, vrange, PG_NEG_ZERO);
+		PG_LAUNCHED(ctx);
+	}
 	if (S->n) {
 		HjProbeTable tb = {};
 		tb.dense32 = ht->dense32; tb.vmin = ht->vmin; tb.dmin = ht->dmin; tb.drange = ht->drange;

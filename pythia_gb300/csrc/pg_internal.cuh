@@ -320,6 +320,15 @@ __device__ __forceinline__ bool nonzero(double x)
 	return ((unsigned long long) __double_as_longlong(x) << 1) != 0;
 }
 
+// Exact rounding error of a double addition with integer operations only
+// (pg_add_err.h); used by the compensated aggregations instead of FP64 adds.
+#include "pg_add_err.h"
+
+// Bit pattern of -0.0: the initial value of dense dec-sum accumulators.
+#define PG_NEG_ZERO 0x8000000000000000ull
+
+__global__ void k_fill_u64(unsigned long long* p, uint64_t n, unsigned long long v);
+
 // Dense group table emission (pg_groupby.cu).
 int pg_dense_groups_emit(pg_ctx* ctx, cudaStream_t s, const unsigned long long* acc, const double* lo,
 		const unsigned char* present, uint64_t range, long long kmin, uint32_t kbytes, int val_type, int agg,
