@@ -20,7 +20,7 @@
 #include <algorithm>
 
 #define PART_MAX_BUCKETS 4096
-#define PART_TILE_BYTES (32 * 1024)
+#define PART_TILE_BYTES (20 * 1024)     // measured best: 4 CTAs per SM
 
 __global__ void k_part_hist(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff,
 		uint32_t kbytes, pg_hashfn f, uint32_t tile, uint64_t tiles_per_cta,
@@ -299,7 +299,7 @@ int pg_partition_fn(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, const pg_hash
 	const uint64_t ntiles = pg_div_up(n, tile);
 	const size_t smem = part_smem_bytes(tile, W, B, NW);
 	if (smem > 220 * 1024) return pg_fail(ctx, PG_ERR_UNSUPPORTED, "pg_partition: tile does not fit shared memory");
-	int per_sm = (int) std::max<size_t>(1, std::min<size_t>(4, (228 * 1024) / (smem + 1024)));
+	int per_sm = (int) std::max<size_t>(1, std::min<size_t>(8, (228 * 1024) / (smem + 1024)));
 	uint64_t G = std::min<uint64_t>(ntiles, (uint64_t) ctx->sm_count * per_sm);
 	uint64_t tpc = pg_div_up(ntiles, G);
 	G = pg_div_up(ntiles, tpc);
