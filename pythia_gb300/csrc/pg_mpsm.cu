@@ -8,10 +8,9 @@
 // (mostfreqbuildkeyoccurances) and emitting the cartesian product of equal-key
 // groups.
 //
-// GPU plan: sort both relations (bitonic tile sort + merge-path merges,
-// pg_sort.cu), cut each sorted relation into equal-key runs (head flags +
-// scan), match build runs to probe runs by binary search over the sorted
-// probe run keys, scan the per-run output counts |R_k|*|S_k|, and either fold
+// GPU plan: sort both relations (pg_sort.cu), cut each sorted relation into
+// equal-key runs (stream compaction of run heads: run starts and run keys),
+// match build runs to probe runs by merging the two sorted run-key arrays, scan the per-run output counts |R_k|*|S_k|, and either fold
 // count and sum (no output materialised; a build column sums as
 // |S_k| * sum_R_k, a probe column as |R_k| * sum_S_k, wrapping int64 like the
 // reference's CtLong +=) or write every pair, each thread producing a
@@ -59,40 +58,96 @@ __device__ __forceinline__ unsigned long long mj_col64(const MjSide& sd, const p
 	return (unsigned long long) (long long) (int32_t) lo;
 }
 
-__global__ void k_run_heads(const pg_rec* __restrict__ rec, uint64_t n, uint64_t* __restrict__ head)
+// Equal-key runs of a sorted record array by stream compaction over chunks of
+// MJ_RUN_CHUNK records: k_run_count counts run heads per chunk, a scan of the
+// chunk counts gives each chunk its first run id, and k_run_write writes, in
+// order, every run's first record index and key.
+#define MJ_RUN_CHUNK 4096
+#define MJ_RUN_THREADS 256
+
+__device__ __forceinline__ bool mj_head(const pg_rec* rec, uint64_t i)
 {
-	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
-			i += (uint64_t) gridDim.x * blockDim.x)
-		head[i] = (i == 0 || rec[i].key != rec[i - 1].key) ? 1 : 0;
+	return i == 0 || rec[i].key != rec[i - 1].key;
 }
 
-// After an exclusive scan, head[i] is the run id of a head element.
-__global__ void k_run_starts(const pg_rec* __restrict__ rec, uint64_t n, const uint64_t* __restrict__ rid,
-		uint64_t* __restrict__ start)
+__global__ void __launch_bounds__(MJ_RUN_THREADS)
+k_run_count(const pg_rec* __restrict__ rec, uint64_t n, uint64_t* __restrict__ ccount)
 {
-	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
-			i += (uint64_t) gridDim.x * blockDim.x)
-		if (i == 0 || rec[i].key != rec[i - 1].key) start[rid[i]] = i;
+	__shared__ uint32_t wsum[MJ_RUN_THREADS / 32];
+	const uint64_t nchunks = pg_div_up(n, MJ_RUN_CHUNK);
+	for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+		const uint64_t lo = c * MJ_RUN_CHUNK, hi = pg_min64(n, lo + MJ_RUN_CHUNK);
+		uint32_t cnt = 0;
+		for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) cnt += mj_head(rec, i);
+		#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+		if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cnt;
+		__syncthreads();
+		if (threadIdx.x == 0) {
+			uint64_t t = 0;
+			for (int w = 0; w < MJ_RUN_THREADS / 32; ++w) t += wsum[w];
+			ccount[c] = t;
+		}
+		__syncthreads();
+	}
+}
+
+__global__ void __launch_bounds__(MJ_RUN_THREADS)
+k_run_write(const pg_rec* __restrict__ rec, uint64_t n, const uint64_t* __restrict__ cfirst,
+		uint64_t* __restrict__ start, long long* __restrict__ rkey)
+{
+	__shared__ uint32_t wsum[MJ_RUN_THREADS / 32];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint64_t nchunks = pg_div_up(n, MJ_RUN_CHUNK);
+	for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+		const uint64_t lo = c * MJ_RUN_CHUNK, hi = pg_min64(n, lo + MJ_RUN_CHUNK);
+		uint64_t base = cfirst[c];
+		for (uint64_t i0 = lo; i0 < hi; i0 += blockDim.x) {
+			const uint64_t i = i0 + threadIdx.x;
+			const bool h = i < hi && mj_head(rec, i);
+			const uint32_t ball = __ballot_sync(0xffffffffu, h);
+			if (lane == 0) wsum[warp] = __popc(ball);
+			__syncthreads();
+			uint32_t before = 0, total = 0;
+			#pragma unroll
+			for (int w = 0; w < MJ_RUN_THREADS / 32; ++w) { const uint32_t x = wsum[w]; before += w < warp ? x : 0; total += x; }
+			if (h) {
+				const uint64_t id = base + before + __popc(ball & ((1u << lane) - 1));
+				start[id] = i;
+				rkey[id] = rec[i].key;
+			}
+			base += total;
+			__syncthreads();
+		}
+	}
 }
 
 // For every build run: matching probe run (or none), output count, and the
-// folded count/sum contribution.
-__global__ void k_match_runs(MjSide R, MjSide S, MjCols pc, int sum_col,
-		uint64_t* __restrict__ counts, uint64_t* __restrict__ match, unsigned long long* __restrict__ agg)
+// folded count/sum contribution. Run keys are sorted on both sides, so each
+// thread merges MJ_MATCH consecutive build runs against the probe run keys:
+// one binary search for its first key, then a forward walk.
+#define MJ_MATCH 16
+__global__ void k_match_runs(MjSide R, MjSide S, const long long* __restrict__ RK, const long long* __restrict__ SK,
+		MjCols pc, int sum_col, uint64_t* __restrict__ counts, uint64_t* __restrict__ match,
+		unsigned long long* __restrict__ agg)
 {
 	unsigned long long sum_acc = 0;
-	for (uint64_t u = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; u < R.nruns;
-			u += (uint64_t) gridDim.x * blockDim.x) {
-		const uint64_t r0 = R.run_start[u], r1 = R.run_start[u + 1];
-		const long long k = R.rec[r0].key;
+	for (uint64_t t = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; t * MJ_MATCH < R.nruns;
+			t += (uint64_t) gridDim.x * blockDim.x) {
+		const uint64_t u0 = t * MJ_MATCH, u1 = pg_min64(R.nruns, u0 + MJ_MATCH);
 		uint64_t lo = 0, hi = S.nruns;
+		const long long k0 = RK[u0];
 		while (lo < hi) {
-			uint64_t mid = (lo + hi) >> 1;
-			if (S.rec[S.run_start[mid]].key < k) lo = mid + 1; else hi = mid;
+			const uint64_t mid = (lo + hi) >> 1;
+			if (SK[mid] < k0) lo = mid + 1; else hi = mid;
 		}
+		for (uint64_t u = u0; u < u1; ++u) {
+		const uint64_t r0 = R.run_start[u], r1 = R.run_start[u + 1];
+		const long long k = RK[u];
+		while (lo < S.nruns && SK[lo] < k) ++lo;
 		uint64_t c = 0;
 		match[u] = UINT64_MAX;
-		if (lo < S.nruns && S.rec[S.run_start[lo]].key == k) {
+		if (lo < S.nruns && SK[lo] == k) {
 			const uint64_t s0 = S.run_start[lo], s1 = S.run_start[lo + 1];
 			c = (r1 - r0) * (s1 - s0);
 			match[u] = lo;
@@ -108,6 +163,7 @@ __global__ void k_match_runs(MjSide R, MjSide S, MjCols pc, int sum_col,
 			}
 		}
 		counts[u] = c;
+		}
 	}
 	#pragma unroll
 	for (int o = 16; o > 0; o >>= 1) sum_acc += __shfl_down_sync(0xffffffffu, sum_acc, o);
@@ -154,26 +210,31 @@ __global__ void k_mj_write(MjSide R, MjSide S, MjCols pc, const uint64_t* __rest
 	}
 }
 
-static int mj_runs(pg_ctx* ctx, cudaStream_t s, const pg_rec* rec, uint64_t n, uint64_t** starts, uint64_t* nruns)
+static int mj_runs(pg_ctx* ctx, cudaStream_t s, const pg_rec* rec, uint64_t n, uint64_t** starts,
+		long long** keys, uint64_t* nruns)
 {
 	int rc;
-	uint64_t* head = nullptr;
+	const uint64_t nchunks = pg_div_up(std::max<uint64_t>(n, 1), MJ_RUN_CHUNK);
+	uint64_t* cc = nullptr;
 	uint64_t* total = nullptr;
-	if ((rc = pg_alloc_async(ctx, s, (void**) &head, (n + 1) * 8))) return rc;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &cc, (nchunks + 1) * 8))) return rc;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &total, 8))) return rc;
-	int blocks = (int) std::min<uint64_t>(pg_div_up(std::max<uint64_t>(n, 1), 256), (uint64_t) ctx->sm_count * 16);
-	if (n) { k_run_heads<<<blocks, 256, 0, s>>>(rec, n, head); PG_LAUNCHED(ctx); }
-	if ((rc = pg_scan_u64(ctx, s, head, n, total))) return rc;
+	const int blocks = (int) std::min<uint64_t>(nchunks, (uint64_t) ctx->sm_count * 8);
+	if (n) { k_run_count<<<blocks, MJ_RUN_THREADS, 0, s>>>(rec, n, cc); PG_LAUNCHED(ctx); }
+	else PG_CUDA(ctx, cudaMemsetAsync(cc, 0, 8, s));
+	if ((rc = pg_scan_u64(ctx, s, cc, nchunks, total))) return rc;
 	uint64_t nr = 0;
 	PG_CUDA(ctx, cudaMemcpyAsync(&nr, total, 8, cudaMemcpyDeviceToHost, s));
 	PG_CUDA(ctx, cudaStreamSynchronize(s));
 	uint64_t* st = nullptr;
+	long long* rk = nullptr;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &st, (nr + 1) * 8))) return rc;
-	if (n) { k_run_starts<<<blocks, 256, 0, s>>>(rec, n, head, st); PG_LAUNCHED(ctx); }
+	if ((rc = pg_alloc_async(ctx, s, (void**) &rk, (nr + 1) * 8))) return rc;
+	if (n) { k_run_write<<<blocks, MJ_RUN_THREADS, 0, s>>>(rec, n, cc, st, rk); PG_LAUNCHED(ctx); }
 	PG_CUDA(ctx, cudaMemcpyAsync(st + nr, &n, 8, cudaMemcpyHostToDevice, s));
-	pg_free_async(ctx, s, head);
+	pg_free_async(ctx, s, cc);
 	pg_free_async(ctx, s, total);
-	*starts = st; *nruns = nr;
+	*starts = st; *keys = rk; *nruns = nr;
 	return PG_OK;
 }
 
@@ -211,8 +272,9 @@ extern "C" int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, cons
 	MjSide RS{rr, (const char*) R->data, R->width, R->key_off, pg_sort_mode(R), nullptr, 0};
 	MjSide SS{sr, (const char*) S->data, S->width, S->key_off, pg_sort_mode(S), nullptr, 0};
 	uint64_t *rst = nullptr, *sst = nullptr;
-	if ((rc = mj_runs(ctx, s, rr, R->n, &rst, &RS.nruns))) return rc;
-	if ((rc = mj_runs(ctx, s, sr, S->n, &sst, &SS.nruns))) return rc;
+	long long *rk = nullptr, *sk = nullptr;
+	if ((rc = mj_runs(ctx, s, rr, R->n, &rst, &rk, &RS.nruns))) return rc;
+	if ((rc = mj_runs(ctx, s, sr, S->n, &sst, &sk, &SS.nruns))) return rc;
 	RS.run_start = rst; SS.run_start = sst;
 	uint64_t *counts = nullptr, *match = nullptr;
 	unsigned long long* acc = nullptr;  // [total, sum]
@@ -220,8 +282,8 @@ extern "C" int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, cons
 	if ((rc = pg_alloc_async(ctx, s, (void**) &match, (RS.nruns + 1) * 8))) return rc;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &acc, 16))) return rc;
 	PG_CUDA(ctx, cudaMemsetAsync(acc, 0, 16, s));
-	int blocks = (int) std::min<uint64_t>(pg_div_up(RS.nruns, 256), (uint64_t) ctx->sm_count * 16);
-	k_match_runs<<<blocks, 256, 0, s>>>(RS, SS, pc, sum_col, counts, match, acc + 1);
+	int blocks = (int) std::min<uint64_t>(pg_div_up(pg_div_up(RS.nruns, MJ_MATCH), 256), (uint64_t) ctx->sm_count * 16);
+	k_match_runs<<<blocks, 256, 0, s>>>(RS, SS, rk, sk, pc, sum_col, counts, match, acc + 1);
 	PG_LAUNCHED(ctx);
 	if ((rc = pg_scan_u64(ctx, s, counts, RS.nruns, (uint64_t*) acc))) return rc;
 	unsigned long long h[2];
@@ -240,7 +302,8 @@ extern "C" int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, cons
 			rc = pg_check_status(ctx, s, "pg_mpsm_join");
 		}
 	}
-	for (void* p : {(void*) rr, (void*) sr, (void*) rst, (void*) sst, (void*) counts, (void*) match, (void*) acc})
+	for (void* p : {(void*) rr, (void*) sr, (void*) rst, (void*) sst, (void*) rk, (void*) sk, (void*) counts,
+			(void*) match, (void*) acc})
 		pg_free_async(ctx, s, p);
 	return rc;
 }
