@@ -156,17 +156,26 @@ def expected_sum(R, S):
     return int(np.int64(tot))
 
 
+def cpu_sample_size():
+    """Probe tuples timed on the host per CPU measurement (1/32 of the probe)."""
+    return max(1, NS // 32)
+
+
 def cpu_join_sample(R, S, threads, sample):
-    """Times the oracle port of HashJoinOp: full build + a probe sample,
-    extrapolated linearly in probe size to the whole workload."""
+    """Times the oracle port of HashJoinOp: full build + a probe sample (one
+    materialising pass: a PK-FK join yields one row per probe tuple, so the
+    output capacity is the sample size), extrapolated linearly in probe size to
+    the whole workload. Inputs are copied to ordinary host memory first."""
     from oracle import oracle as orc
     cfg = orc.hashcfg("modulo", NR)
-    Ssub = np.ascontiguousarray(S[:sample])
+    Rc = np.array(R, copy=True)
+    Ssub = np.array(S[:sample], copy=True)
     t0 = time.perf_counter()
-    _, n0, _ = orc.hashjoin(R, Ssub[:1], hash=cfg, tuplesperbucket=4, threads=threads, materialise=False)
+    _, n0, _ = orc.hashjoin(Rc, Ssub[:1], hash=cfg, tuplesperbucket=4, threads=threads, materialise=False)
     t_build = time.perf_counter() - t0
     t0 = time.perf_counter()
-    _, n, _ = orc.hashjoin(R, Ssub, hash=cfg, tuplesperbucket=4, threads=threads, materialise=True)
+    _, n, _ = orc.hashjoin(Rc, Ssub, hash=cfg, tuplesperbucket=4, threads=threads, materialise=True,
+                           out_cap=sample)
     t_all = time.perf_counter() - t0
     t_probe = max(t_all - t_build, 1e-9)
     t_est = t_build + t_probe * (NS / sample)
@@ -182,7 +191,7 @@ def run_reference(args, ws, rank):
     R = np.empty((NR, 2), dtype=np.int64)
     S = np.empty((NS, 2), dtype=np.int64)
     make_inputs(R, S, threads)
-    sample = NS // 32
+    sample = cpu_sample_size()
     vals = []
     for i in range(args.warmup + args.steps):
         v, info = cpu_join_sample(R, S, threads, sample)
@@ -320,7 +329,7 @@ def run_gpu(args, ws, rank, local):
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        sample = NS // 64
+        sample = cpu_sample_size()
         v, info = cpu_join_sample(R, S, threads, sample)
         cpu = {"value": v, "unit": "tuples/s", "cores": threads, "kind": "port",
                "sample": f"full {NR}-tuple build + first {sample} probe tuples, probe time scaled to {NS} "
