@@ -379,7 +379,12 @@ OPS = {
                  workload="page sort of 64M (long key U[0,16M), long payload) tuples"),
     "mpsm": dict(n=1 << 26, metric="MPSM join tuples/s (64M x 64M, keys U[0,16M), fused count+sum)",
                  workload="sort-merge join of two 64M-tuple relations, keys U[0,16M) (~4 duplicates per side)"),
+    "groupjoin": dict(n=1 << 28, metric="join + group-by tuples/s (16M build x 256M probe, 1% groups, one pass)",
+                      workload="hash join of 16M unique keys (group column = payload mod 167,772) with 256M FK "
+                               "probes carrying dec values U[0,1e4), then aggregate_sum per group, one pass"),
 }
+GJ_BUILD = 1 << 24
+GJ_GROUPS = GJ_BUILD // 100
 
 
 def _pinned_array(ctx, L, n, cols=2):
@@ -396,6 +401,14 @@ def _op_inputs(op, n, threads):
         return [dg.groupby_rows(n, 1 << 20, 1e4, dg.seed_for(112), threads=threads)]
     if op == "sort":
         return [dg.uniform_keys(n, 1 << 24, dg.seed_for(113), threads=threads)]
+    if op == "groupjoin":
+        nb = min(GJ_BUILD, max(n // 16, 1024))
+        R = dg.build_relation(nb, dg.seed_for(116), threads=threads)
+        R[:, 1] = (dg.raw_words(dg.seed_for(116), 3, nb) % np.uint64(max(nb // 100, 1))).astype(np.int64)
+        S = dg.probe_uniform(n, R, dg.seed_for(117), threads=threads)
+        S[:, 1] = ((dg.raw_words(dg.seed_for(117), 4, n) >> np.uint64(11)).astype(np.float64)
+                   * (1e4 / 2.0 ** 53)).view(np.int64)
+        return [R, S]
     return [dg.uniform_keys(n, 1 << 24, dg.seed_for(114), threads=threads),
             dg.uniform_keys(n, 1 << 24, dg.seed_for(115), threads=threads)]
 
@@ -437,6 +450,27 @@ def _op_parity(op, ins, out, extra):
         ok = bool(np.all(np.diff(o[:, 0]) >= 0))
         ok &= int(o.astype(np.uint64).sum(dtype=np.uint64)) == int(ins[0].astype(np.uint64).sum(dtype=np.uint64))
         return {"sorted_and_same_multiset_checksum": ok}
+    if op == "groupjoin":
+        from oracle import oracle as orc
+        R, S = ins
+        g = out.view(np.int64).reshape(-1, 2)
+        gk_by_key = np.zeros(int(R[:, 0].max()) + 1, dtype=np.int64)
+        gk_by_key[R[:, 0]] = R[:, 1]
+        gk = gk_by_key[S[:, 0]]
+        ngroups_ok = g.shape[0] == int(np.unique(gk).shape[0])
+        total = orc.fsum(S[:, 1].view(np.float64))
+        got_total = orc.fsum(g[:, 1].view(np.float64))
+        pick = np.random.default_rng(9).choice(np.unique(gk), 16, replace=False)
+        sel = np.isin(gk, pick)
+        sk, sv = gk[sel], S[sel, 1].view(np.float64)
+        d = {int(k): float(v) for k, v in zip(g[:, 0], g[:, 1].view(np.float64))}
+        worst = 0.0
+        for k in pick:
+            ex = orc.fsum(sv[sk == k])
+            worst = max(worst, abs(d[int(k)] - ex) / abs(ex))
+        return {"groups_ok": bool(ngroups_ok), "total_rel_err": abs(got_total - total) / total,
+                "sampled_group_max_rel_err": worst, "tolerance": 1e-12,
+                "ok": bool(ngroups_ok and worst <= 1e-12)}
     R, S = ins
     cr = np.bincount(R[:, 0], minlength=1 << 24).astype(np.int64)
     cs = np.bincount(S[:, 0], minlength=1 << 24).astype(np.int64)
@@ -460,12 +494,15 @@ def run_op(args, ws, rank, local, op):
     d_in = [ctx.upload(a) for a in ins]
     stream = torch.cuda.ExternalStream(ctx.stream)
     c, nc = gpu.cols((("P", 8, 8), ("B", 8, 8)))
-    out_bytes = {"partition": n * 16, "groupby": (1 << 20) * 16 + 16, "sort": n * 16, "mpsm": 16}[op]
+    nb = ins[0].shape[0]
+    out_bytes = {"partition": n * 16, "groupby": (1 << 20) * 16 + 16, "sort": n * 16, "mpsm": 16,
+                 "groupjoin": (nb // 100 + 1) * 16}[op]
     d_out = ctx.alloc(out_bytes)
     offs = ctx.alloc(8 * 257)
     ng = ctypes.c_uint64()
     res = gpu.JoinResult()
-    rel = [gpu.Rel(d.ptr, n, 16, 0, 8) for d in d_in]
+    rel = [gpu.Rel(d.ptr, a.shape[0], 16, 0, 8) for d, a in zip(d_in, ins)]
+    gcols, gnc = gpu.cols((("B", 8, 8), ("P", 8, 8)))
 
     def step():
         if op == "partition":
@@ -476,6 +513,14 @@ def run_op(args, ws, rank, local, op):
                                     1 << 20, ctypes.byref(ng)))
         elif op == "sort":
             ctx._check(L.pg_sort_pages(ctx.h, ctx.stream, ctypes.byref(rel[0]), d_out.ptr))
+        elif op == "groupjoin":
+            ht = ctypes.c_void_p()
+            ctx._check(L.pg_hashjoin_build(ctx.h, ctx.stream, ctypes.byref(rel[0]), gcols, gnc, ctypes.byref(ht)))
+            try:
+                ctx._check(L.pg_hashjoin_groupby(ctx.h, ctx.stream, ht.value, ctypes.byref(rel[1]), 8, 2, 0,
+                                                 d_out.ptr, nb // 100 + 1, ctypes.byref(ng)))
+            finally:
+                L.pg_hashtable_free(ctx.h, ht.value)
         else:
             ctx._check(L.pg_mpsm_join(ctx.h, ctx.stream, ctypes.byref(rel[0]), ctypes.byref(rel[1]), c, nc,
                                       None, 0, gpu.JOIN_COUNT | gpu.JOIN_SUM, 1, ctypes.byref(res)))
@@ -496,9 +541,10 @@ def run_op(args, ws, rank, local, op):
     clk = clocks.stop()
     launches = gpu.kernel_launches() - k0
     ms = max_over_ranks(ws, e0.elapsed_time(e1) / args.steps)
-    units = 2 * n if op == "mpsm" else n
+    units = 2 * n if op == "mpsm" else (n + nb if op == "groupjoin" else n)
     value = ws * units / (ms / 1e3)
-    alg = {"partition": 32 * n, "groupby": 16 * n + 16 * (1 << 20), "sort": 32 * n, "mpsm": 16 * 2 * n}[op]
+    alg = {"partition": 32 * n, "groupby": 16 * n + 16 * (1 << 20), "sort": 32 * n, "mpsm": 16 * 2 * n,
+           "groupjoin": 16 * (n + nb) + 16 * (nb // 100)}[op]
     peak, peak_kind = measured_peak()
     achieved = alg / (ms / 1e3) / 1e9
     # Parity at full size.
@@ -509,6 +555,8 @@ def run_op(args, ws, rank, local, op):
         parity = _op_parity(op, ins, ctx.download(d_out, ng.value * 16), None)
     elif op == "sort":
         parity = _op_parity(op, ins, ctx.download(d_out, n * 16).view(np.int64), None)
+    elif op == "groupjoin":
+        parity = _op_parity(op, ins, ctx.download(d_out, ng.value * 16), None)
     else:
         parity = _op_parity(op, ins, None, (res.n_out, res.sum))
     cpu = None
@@ -517,7 +565,7 @@ def run_op(args, ws, rank, local, op):
     if rank == 0:
         line = {"metric": spec["metric"], "value": value, "unit": "tuples/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "int64" if op != "groupby" else "f64",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if op in ("groupby", "groupjoin") else "int64",
                 "data": "synthetic (seeded generator, resident in HBM)",
                 "config": {"workload": spec["workload"], "op": op, "tuples": n,
                            "l2": "inputs larger than L2; no flush"},
@@ -552,6 +600,25 @@ def cpu_op_sample(op, ins, threads):
         t0 = time.perf_counter()
         orc.sort(a)
         scale, kind = (n * np.log2(n)) / (m * np.log2(m)), "n log n"
+    elif op == "groupjoin":
+        R = ins[0]
+        n = ins[1].shape[0]
+        m = min(n, 1 << 22)
+        S = np.ascontiguousarray(ins[1][:m])
+        cfg = orc.hashcfg("modulo", R.shape[0])
+        t0 = time.perf_counter()
+        orc.hashjoin(R, S[:1], hash=cfg, threads=threads, materialise=False)
+        t_build = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        joined, _, _ = orc.hashjoin(R, S, proj=(("B", 8, 8), ("P", 8, 8)), hash=cfg, threads=threads, out_cap=m)
+        orc.groupby(joined.view(np.int64).reshape(-1, 2), val=(8, "dec"), agg="sum",
+                    hash=orc.hashcfg("modulo", 1 << 18), threads=threads)
+        t_rest = max(time.perf_counter() - t0 - t_build, 1e-9)
+        t = t_build + t_rest * n / m
+        units = n + R.shape[0]
+        return {"value": units / t, "unit": "tuples/s", "cores": threads, "kind": "port",
+                "sample": f"full {R.shape[0]}-tuple build + {m} probe tuples joined and grouped (oracle port), "
+                          f"probe and group-by time scaled linearly to {n}"}
     else:
         m = min(n, 1 << 22)
         R = np.ascontiguousarray(ins[0][:m]); S = np.ascontiguousarray(ins[1][:m])
@@ -560,7 +627,7 @@ def cpu_op_sample(op, ins, threads):
         orc.mergejoin(R, S, materialise=False, sum_col=1, threads=threads)
         scale, kind = n / m, "linear"
     t = (time.perf_counter() - t0) * scale
-    units = 2 * n if op == "mpsm" else n
+    units = 2 * n if op == "mpsm" else (n + ins[0].shape[0] if op == "groupjoin" else n)
     return {"value": units / t, "unit": "tuples/s", "cores": threads if op != "sort" else 1,
             "kind": "port", "sample": f"{m} tuples (oracle port), time scaled {kind} to {n}"}
 

@@ -518,15 +518,16 @@ k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, u
 			else iv[j] = vbits;
 		}
 		if (AGG == PG_AGG_SUM && VT == PG_VAL_DEC) {
+			// hi and lo of a group share one 16-byte slot (one L2 sector).
 			double old[GBD_ILP];
 			#pragma unroll
 			for (int j = 0; j < GBD_ILP; ++j)
-				if (ok[j]) old[j] = atomicAdd(reinterpret_cast<double*>(&acc[d[j]]), dv[j]);
+				if (ok[j]) old[j] = atomicAdd(reinterpret_cast<double*>(&acc[2 * d[j]]), dv[j]);
 			#pragma unroll
 			for (int j = 0; j < GBD_ILP; ++j) {
 				if (!ok[j]) continue;
 				const double e = pg_add_err(old[j], dv[j]);
-				if (nonzero(e)) atomicAdd(&lo[d[j]], e);
+				if (nonzero(e)) atomicAdd(reinterpret_cast<double*>(&acc[2 * d[j] + 1]), e);
 				// hi starts at -0.0, which adds to any value exactly: the add
 				// that returns that pattern is the group's first, and marks it.
 				if ((unsigned long long) __double_as_longlong(old[j]) == PG_NEG_ZERO) present[d[j]] = 1;
@@ -569,10 +570,15 @@ __global__ void k_gb_dense_emit(const unsigned long long* __restrict__ acc, cons
 		else { reinterpret_cast<uint32_t*>(o)[0] = (uint32_t) k; reinterpret_cast<uint32_t*>(o)[1] = (uint32_t) ((uint64_t) k >> 32); }
 		o += kbytes;
 		if (aw == 4) *reinterpret_cast<uint32_t*>(o) = (uint32_t) acc[i];
-		else {
+		else if (VT == PG_VAL_DEC && AGG == PG_AGG_SUM) {
+			// Interleaved (hi, lo); hi alone keeps the sign of a zero sum.
+			unsigned long long a = acc[2 * i];
+			const double l = __longlong_as_double((long long) acc[2 * i + 1]);
+			if (nonzero(l)) a = (unsigned long long) __double_as_longlong(__longlong_as_double((long long) a) + l);
+			reinterpret_cast<uint32_t*>(o)[0] = (uint32_t) a;
+			reinterpret_cast<uint32_t*>(o)[1] = (uint32_t) (a >> 32);
+		} else {
 			unsigned long long a = acc[i];
-			if (VT == PG_VAL_DEC && AGG == PG_AGG_SUM && nonzero(lo[i]))   // hi alone keeps the sign of a zero sum
-				a = (unsigned long long) __double_as_longlong(__longlong_as_double((long long) a) + lo[i]);
 			reinterpret_cast<uint32_t*>(o)[0] = (uint32_t) a;
 			reinterpret_cast<uint32_t*>(o)[1] = (uint32_t) (a >> 32);
 		}
@@ -615,9 +621,10 @@ static int gb_dense(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff
 	unsigned char* present = reinterpret_cast<unsigned char*>(cursor + 1);
 	PG_CUDA(ctx, cudaMemsetAsync(mem, 0, bytes, s));
 	if (VT == PG_VAL_DEC && AGG == PG_AGG_SUM) {
-		// Sums start at -0.0 so that the first add of a group is recognisable.
-		k_fill_u64<<<(int) std::min<uint64_t>(pg_div_up(range, 256), (uint64_t) ctx->sm_count * 8), 256, 0, s>>>(
-				acc, range, PG_NEG_ZERO);
+		// Interleaved (hi, lo) words start at -0.0 so that the first add of a
+		// group is recognisable (-0.0 + x = x exactly).
+		k_fill_u64<<<(int) std::min<uint64_t>(pg_div_up(2 * range, 256), (uint64_t) ctx->sm_count * 8), 256, 0, s>>>(
+				acc, 2 * range, PG_NEG_ZERO);
 		PG_LAUNCHED(ctx);
 	}
 	const int gblocks = (int) std::min<uint64_t>(pg_div_up(in->n, (uint64_t) GB_THREADS * GBD_ILP), (uint64_t) ctx->sm_count * 8);

@@ -1776,13 +1776,13 @@ k_probe16_groupby(const char* __restrict__ S, uint64_t n, uint32_t koff, const H
 			for (int j = 0; j < ITEMS; ++j) {
 				const uint4 t = cur[j];
 				v[j] = __longlong_as_double((long long) (voff == 0 ? (((uint64_t) t.y << 32) | t.x) : (((uint64_t) t.w << 32) | t.z)));
-				if (e[j] != 0xFFFFFFFFu) old[j] = atomicAdd(reinterpret_cast<double*>(&acc[e[j]]), v[j]);
+				if (e[j] != 0xFFFFFFFFu) old[j] = atomicAdd(reinterpret_cast<double*>(&acc[2 * (uint64_t) e[j]]), v[j]);
 			}
 			#pragma unroll
 			for (int j = 0; j < ITEMS; ++j) {
 				if (e[j] == 0xFFFFFFFFu) continue;
 				const double err = pg_add_err(old[j], v[j]);
-				if (nonzero(err)) atomicAdd(&lo[e[j]], err);
+				if (nonzero(err)) atomicAdd(reinterpret_cast<double*>(&acc[2 * (uint64_t) e[j] + 1]), err);
 				// Sums start at -0.0: the add that returns it is the group's first.
 				if ((unsigned long long) __double_as_longlong(old[j]) == PG_NEG_ZERO) present[e[j]] = 1;
 			}
@@ -1834,8 +1834,9 @@ extern "C" int pg_hashjoin_groupby(pg_ctx* ctx, pg_stream stream, pg_hashtable* 
 	unsigned char* present = reinterpret_cast<unsigned char*>(cursor + 1);
 	PG_CUDA(ctx, cudaMemsetAsync(mem, 0, bytes, s));
 	if (agg == PG_AGG_SUM && val_type == PG_VAL_DEC) {
-		k_fill_u64<<<(int) std::min<uint64_t>(pg_div_up(vrange, 256), (uint64_t) ctx->sm_count * 8), 256, 0, s>>>(
-				acc, vrange, PG_NEG_ZERO);
+		// Interleaved (hi, lo) slots, all words -0.0 (see k_gb_dense).
+		k_fill_u64<<<(int) std::min<uint64_t>(pg_div_up(2 * vrange, 256), (uint64_t) ctx->sm_count * 8), 256, 0, s>>>(
+				acc, 2 * vrange, PG_NEG_ZERO);
 		PG_LAUNCHED(ctx);
 	}
 	if (S->n) {
