@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 NR = 1 << 24            # overridable with --build-log2 / --probe-log2 (smaller configs)
 NS = 1 << 28
 TUPLE = 16
-PROBE_DRAM_BYTES_PER_TUPLE = (1.153772e9 + 0.516699e9) / (1 << 25)
+PROBE_DRAM_BYTES_PER_TUPLE = (1.133091e9 + 0.514387e9) / (1 << 25)
 METRIC = "join tuples/s (16M build x 256M probe, PK-FK, int64 keys, materialised)"
 WORKLOAD = "radix-scale PK-FK hash join: |R|=16M unique int64 keys, |S|=256M uniform FK, 16-byte tuples, output (P$1,B$1)"
 
@@ -352,7 +352,7 @@ def run_gpu(args, ws, rank, local):
                 "e2e": {"value": ws * (NR + NS) / (e2e / 1e3), "unit": "tuples/s",
                         "h2d_bytes_per_step": (NR + NS) * TUPLE, "d2h_bytes_per_step": NS * TUPLE,
                         "ms_per_step": e2e},
-                "roofline": {"bound": "hbm", "kernel": "k_probe16_direct (materialise)",
+                "roofline": {"bound": "hbm", "kernel": "k_probe16_deep (materialise)",
                              "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
                              "peak_source": peak_kind, "probe_ms": probe,

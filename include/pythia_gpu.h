@@ -116,8 +116,9 @@ uint64_t pg_kernel_launches(void);
 enum {
 	PG_TUNE_PROBE_CTAS_PER_SM = 0,   /* resident 8-warp CTAs per SM of the 16-byte probe (1..5) */
 	PG_TUNE_PROBE_VARIANT = 1,       /* 16-byte probe: 0 default, 1 warp-staged (bulk copies), 2 tiled with
-	                                    bulk stores, 3 register loads with prefetch (dense default),
-	                                    4 register loads without prefetch */
+	                                    bulk stores, 3 register loads with one-chunk prefetch (dense default
+	                                    for other projections), 4 register loads without prefetch, 5 deeper
+	                                    pipeline (default for (P$1, B$1) rows of narrow dense tables) */
 	PG_TUNE_DENSE = 2,               /* 1: allow dense tables (default), 2: always hash */
 	PG_TUNE_PARTITION_TILE = 3,      /* partition tile bytes (8192..65536) */
 	PG_TUNE_GROUPBY_SMEM_GROUPS = 4, /* largest group count aggregated in shared memory first */

@@ -982,6 +982,78 @@ k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const Hj
 	if (lane == 0) { atomicAdd(&agg[0], cnt_acc); if (!MATERIALIZE) atomicAdd(&agg[1], sum_acc); }
 }
 
+// ---------------------------------------------------------------------------
+// Deeper pipeline of the narrow dense probe (standard 16-byte output rows):
+// while chunk c's rows are written, the table lookups of chunk c + W are in
+// flight and the tuples of chunk c + 2W are loading, so lookup latency and
+// stream latency both overlap with the stores of another chunk.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void hj_lookup4(const HjProbeTable& tb, const uint4 (&t)[4], uint32_t rows, int lane,
+		uint32_t koff, uint64_t keep, uint32_t (&e)[4])
+{
+	#pragma unroll
+	for (int j = 0; j < 4; ++j) {
+		const int64_t key = koff == 0 ? (int64_t) (((uint64_t) t[j].y << 32) | t[j].x)
+			: (int64_t) (((uint64_t) t[j].w << 32) | t[j].z);
+		const unsigned long long d = (unsigned long long) key - (unsigned long long) tb.dmin;
+		e[j] = 0xFFFFFFFFu;
+		if ((uint32_t) (j * 32 + lane) < rows && d < tb.drange)
+			asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(e[j]) : "l"(tb.dense32 + d), "l"(keep));
+	}
+}
+
+__global__ void __launch_bounds__(PW_WARPS * 32, 3)
+k_probe16_deep(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb, char* __restrict__ out,
+		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg)
+{
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
+	const uint64_t W = (uint64_t) gridDim.x * PW_WARPS;
+	const uint64_t first = (uint64_t) blockIdx.x * PW_WARPS + warp;
+	const uint64_t keep = pg_policy_evict_last();
+	const uint64_t stream = pg_policy_evict_first();
+	unsigned long long cnt_acc = 0;
+	if (first >= nchunks) return;
+	auto rows_of = [&](uint64_t c) -> uint32_t { return (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK); };
+	auto load = [&](uint64_t c, uint4 (&t)[4]) {
+		const uint32_t rows = c < nchunks ? rows_of(c) : 0;
+		#pragma unroll
+		for (int j = 0; j < 4; ++j) {
+			const uint32_t p = j * 32 + lane;
+			t[j] = p < rows ? hj_ld_stream(S + (c * PW_CHUNK + p) * 16, stream) : make_uint4(0, 0, 0, 0);
+		}
+	};
+	uint4 cur[4], nxt[4], nx2[4];
+	uint32_t ecur[4], enxt[4];
+	load(first, cur);
+	load(first + W, nxt);
+	hj_lookup4(tb, cur, rows_of(first), lane, koff, keep, ecur);
+	for (uint64_t c = first; c < nchunks; c += W) {
+		const uint64_t c1 = c + W, c2 = c + 2 * W;
+		if (c1 < nchunks) hj_lookup4(tb, nxt, rows_of(c1), lane, koff, keep, enxt);
+		load(c2, nx2);
+		const uint32_t rows = rows_of(c);
+		uint32_t rank = 0;
+		#pragma unroll
+		for (int j = 0; j < 4; ++j) {
+			const bool h = ecur[j] != 0xFFFFFFFFu;
+			const uint32_t ball = __ballot_sync(0xffffffffu, h);
+			if (h) {
+				const uint64_t v = tb.vmin + ecur[j];
+				const uint64_t row = c * PW_CHUNK + rank + __popc(ball & ((1u << lane) - 1));
+				hj_st_stream(out + row * 16, make_uint4(cur[j].z, cur[j].w, (uint32_t) v, (uint32_t) (v >> 32)), stream);
+			}
+			rank += __popc(ball);
+		}
+		(void) rows;
+		cnt_acc += rank;
+		if (lane == 0) chunk_counts[c] = rank;
+		#pragma unroll
+		for (int j = 0; j < 4; ++j) { cur[j] = nxt[j]; nxt[j] = nx2[j]; ecur[j] = enxt[j]; }
+	}
+	if (lane == 0) atomicAdd(&agg[0], cnt_acc);
+}
+
 // Positional probe output: the 128-tuple chunk c (rows_c = min(128, n - 128c)
 // probe tuples) holds lo = counts[c] & 0xffffffff rows at its front,
 // [128c, 128c + lo), and hi = counts[c] >> 32 rows at its back,
@@ -1392,7 +1464,7 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 			// Dense tables take the register-loading probe unless the knob asks
 			// for the staged one (1) or the non-prefetching one (4).
 			const int64_t var = ctx->tune[PG_TUNE_PROBE_VARIANT];
-			const bool direct = mode != 0 && (var == 0 || var == 3 || var == 4);
+			const bool direct = mode != 0 && (var == 0 || var == 3 || var == 4 || var == 5);
 			const int passes = mode == 0 || pk == 1 ? 1
 				: (pk == 2 || (!direct && tbytes > HJ_TWO_PASS_MIN_BYTES && tbytes <= HJ_TWO_PASS_MAX_BYTES)) ? 2 : 1;
 			const uint64_t dr = mode == 0 ? 0 : ht->drange;
@@ -1411,7 +1483,15 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 					const int dgrid = (int) std::min<uint64_t>(wchunks, (uint64_t) ctx->sm_count * want);
 #define PD_LAUNCH(M, D, P) k_probe16_direct<M, D, P><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, wsel, sum_w0, \
 						sum_words, M ? out : nullptr, M ? counts : nullptr, M ? acc : acc + 1, M ? -1 : sum_col, dlo, dhi, run)
-					if (materialize && mode == 2 && pf && wsel == 0x5432u) {
+					// The standard (P$1, B$1) rows of a narrow dense table take the
+					// deeper pipeline by default (72 CTAs per SM, 3 resident:
+					// measured best on the 16M x 256M join); variant 3 selects
+					// the one-chunk-prefetch kernel.
+					if (materialize && mode == 2 && (var == 0 || var == 5) && wsel == 0x5432u && passes == 1) {
+						const int g5 = (int) std::min<uint64_t>(wchunks, (uint64_t) ctx->sm_count *
+								(ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] > 0 ? ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] : 72));
+						k_probe16_deep<<<g5, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, out, counts, acc);
+					} else if (materialize && mode == 2 && pf && wsel == 0x5432u) {
 						k_probe16_direct<true, 2, true, true><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, wsel, sum_w0,
 								sum_words, out, counts, acc, -1, dlo, dhi, run);
 					} else if (materialize) {

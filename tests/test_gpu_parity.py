@@ -154,7 +154,7 @@ def test_join_dense_keys_wide_values(ctx):
                                    dict(probe_variant=1, probe_passes=2, probe_items=8), dict(probe_cache=1),
                                    dict(probe_cache=14), dict(probe_passes=2), dict(probe_variant=4),
                                    dict(probe_variant=4, probe_passes=2, probe_ctas_per_sm=5),
-                                   dict(probe_variant=2)])
+                                   dict(probe_variant=2), dict(probe_variant=3), dict(probe_variant=5)])
 def test_join_probe_launch_shapes(ctx, knobs):
     # Probe kernel variants, lookups in flight, L2 policies, passes and grid
     # shapes change speed, never rows: narrow and wide dense tables, with
