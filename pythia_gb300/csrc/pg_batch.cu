@@ -165,18 +165,25 @@ __global__ void k_batch_probe_count(const BatchInst* __restrict__ inst, const Ba
 }
 
 // Per-instance key minimum and maximum (sign-flipped for unsigned atomics).
+// Keys equal to the empty marker never occur in the batch workloads' build
+// sides; a key equal to it fails the batch (PG_ERR_UNSUPPORTED) instead of a
+// side list per instance.
 __global__ void k_batch_minmax(const BatchInst* __restrict__ inst, const BatchTile* __restrict__ tiles,
-		uint64_t ntiles, unsigned long long* __restrict__ mm)
+		uint64_t ntiles, unsigned long long* __restrict__ mm, int* __restrict__ status)
 {
 	for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
 		const BatchTile tl = tiles[t];
 		const BatchInst in = inst[tl.inst];
 		unsigned long long lo = ~0ull, hi = 0;
+		bool marker = false;
 		for (uint64_t i = tl.begin + threadIdx.x; i < tl.end; i += blockDim.x) {
-			const unsigned long long u = (unsigned long long) reinterpret_cast<const long long*>(in.R)[2 * i] ^ (1ull << 63);
+			const long long k = reinterpret_cast<const long long*>(in.R)[2 * i];
+			marker |= k == PG_EMPTY_KEY;
+			const unsigned long long u = (unsigned long long) k ^ (1ull << 63);
 			lo = u < lo ? u : lo;
 			hi = u > hi ? u : hi;
 		}
+		if (marker) pg_set_status(status, PG_ERR_UNSUPPORTED);
 		#pragma unroll
 		for (int o = 16; o > 0; o >>= 1) {
 			const unsigned long long a = __shfl_down_sync(0xffffffffu, lo, o), b = __shfl_down_sync(0xffffffffu, hi, o);
@@ -187,16 +194,6 @@ __global__ void k_batch_minmax(const BatchInst* __restrict__ inst, const BatchTi
 	}
 }
 
-// Keys equal to the empty marker never occur in the batch workloads' build
-// sides; the host rejects them instead of carrying a side list per instance.
-__global__ void k_batch_check_keys(const BatchInst* __restrict__ inst, uint32_t ninst, int* __restrict__ status)
-{
-	for (uint32_t b = blockIdx.x; b < ninst; b += gridDim.x) {
-		const BatchInst in = inst[b];
-		for (uint64_t i = threadIdx.x; i < in.nR; i += blockDim.x)
-			if (reinterpret_cast<const long long*>(in.R)[2 * i] == PG_EMPTY_KEY) pg_set_status(status, PG_ERR_UNSUPPORTED);
-	}
-}
 
 // Synthetic foreign keys: S[j].key = R[h(seed, j) mod nR].key, payload from
 // the same counter hash (SplitMix64 finaliser; multiply-high reduction).
@@ -329,7 +326,7 @@ extern "C" int pg_batch_prepare(pg_ctx* ctx, pg_stream stream, const pg_batch_it
 		PG_CUDA(ctx, cudaMemcpyAsync(bb->d_inst, inst.data(), n * sizeof(BatchInst), cudaMemcpyHostToDevice, s));
 		PG_CUDA(ctx, cudaMemcpyAsync(bb->d_btiles, bt.data(), bt.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, s));
 		k_batch_minmax<<<(int) std::min<uint64_t>(bt.size(), (uint64_t) ctx->sm_count * 8), 256, 0, s>>>(
-				bb->d_inst, bb->d_btiles, bt.size(), mm);
+				bb->d_inst, bb->d_btiles, bt.size(), mm, ctx->d_status);
 		PG_LAUNCHED(ctx);
 		PG_CUDA(ctx, cudaMemcpyAsync(init.data(), mm, 16 * (size_t) n, cudaMemcpyDeviceToHost, s));
 		PG_CUDA(ctx, cudaStreamSynchronize(s));
@@ -378,10 +375,6 @@ extern "C" int pg_batch_prepare(pg_ctx* ctx, pg_stream stream, const pg_batch_it
 	if (n) PG_CUDA(ctx, cudaMemcpyAsync(bb->d_inst, inst.data(), n * sizeof(BatchInst), cudaMemcpyHostToDevice, s));
 	if (!bt.empty()) PG_CUDA(ctx, cudaMemcpyAsync(bb->d_btiles, bt.data(), bt.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, s));
 	if (!pt.empty()) PG_CUDA(ctx, cudaMemcpyAsync(bb->d_ptiles, pt.data(), pt.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, s));
-	if (n) {
-		k_batch_check_keys<<<(int) std::min<uint32_t>(n, ctx->sm_count * 8), 256, 0, s>>>(bb->d_inst, n, ctx->d_status);
-		PG_LAUNCHED(ctx);
-	}
 	if ((rc = pg_check_status(ctx, s, "pg_batch_prepare"))) {
 		pg_batch_free(ctx, bb);
 		return pg_fail(ctx, rc, "pg_batch_prepare: a build key equals -1 (not supported in batches)");

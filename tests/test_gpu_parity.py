@@ -535,6 +535,20 @@ def test_batch_join_count_matches_oracle(ctx):
         autotune.free(ctx, b)
 
 
+def test_batch_rejects_empty_marker_build_key(ctx):
+    # Batched tables use -1 as their empty-slot marker; a build key equal to it
+    # fails the batch at prepare instead of producing a wrong count.
+    from pythia_gb300 import autotune
+    R = dg.build_relation(3000, dg.seed_for(320))
+    R[7, 0] = -1
+    S = dg.probe_uniform(24_000, R, dg.seed_for(321))
+    dR, dS = ctx.upload(R), ctx.upload(S)
+    with pytest.raises(gpu.PgError) as e:
+        autotune.prepare(ctx, [(dR.ptr, R.shape[0], dS.ptr, S.shape[0])], autotune.BATCH_SHAPES[0])
+    assert e.value.code == gpu.PG_ERR_UNSUPPORTED
+    assert gpu.lib().pg_device_status(ctx.h) == 0      # the failing check cleared the status word
+
+
 def test_generate_fk_matches_host_replica(ctx):
     import bench
     R = dg.build_relation(5000, dg.seed_for(700))
