@@ -881,6 +881,127 @@ def run_serve(args, ws, rank, local):
     ctx.close()
 
 
+# ---------------------------------------------------------------------------
+# Join-table images (bench.py --op tableimage): the 16M-key build side of the
+# headline join written to pinned host memory and loaded back, against
+# rebuilding the table from its host relation (the warm start an image
+# replaces) and against a plain pinned copy of the same bytes (the link).
+# ---------------------------------------------------------------------------
+def run_tableimage(args, ws, rank, local):
+    import torch
+    from pythia_gb300 import datagen as dg
+    from pythia_gb300 import gpu
+    torch.cuda.set_device(local)
+    nb = GJ_BUILD >> args.scale_down
+    threads = host_threads()
+    ctx = make_ctx(args, local)
+    L = gpu.lib()
+    R = dg.build_relation(nb, dg.seed_for(118), threads=threads)
+    rp, Rh = _pinned_array(ctx, L, nb)
+    Rh[:] = R
+    dR = ctx.upload(R)
+    dR2 = ctx.alloc(R.nbytes)
+    c, nc = gpu.cols((("P", 8, 8), ("B", 8, 8)))
+    rel = gpu.Rel(dR.ptr, nb, 16, 0, 8)
+    rel2 = gpu.Rel(dR2.ptr, nb, 16, 0, 8)
+    ht = ctypes.c_void_p()
+    ctx._check(L.pg_hashjoin_build(ctx.h, ctx.stream, ctypes.byref(rel), c, nc, ctypes.byref(ht)))
+    size = ctypes.c_uint64()
+    ctx._check(L.pg_hashtable_image_size(ctx.h, ht.value, ctypes.byref(size)))
+    nbytes = size.value
+    ip = ctypes.c_void_p()
+    ctx._check(L.pg_host_alloc(ctx.h, nbytes, ctypes.byref(ip)))
+    dcopy = ctx.alloc(nbytes)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    got = ctypes.c_uint64()
+
+    def save():
+        ctx._check(L.pg_hashtable_serialize(ctx.h, ctx.stream, ht.value, ip.value, nbytes, ctypes.byref(got)))
+
+    def load():
+        t = ctypes.c_void_p()
+        ctx._check(L.pg_hashtable_deserialize(ctx.h, ctx.stream, ip.value, nbytes, ctypes.byref(t)))
+        L.pg_hashtable_free(ctx.h, t.value)
+
+    def rebuild():
+        t = ctypes.c_void_p()
+        ctx._check(L.pg_h2d(ctx.h, ctx.stream, dR2.ptr, rp, R.nbytes))
+        ctx._check(L.pg_hashjoin_build(ctx.h, ctx.stream, ctypes.byref(rel2), c, nc, ctypes.byref(t)))
+        L.pg_hashtable_free(ctx.h, t.value)
+
+    def copy():
+        ctx._check(L.pg_h2d(ctx.h, ctx.stream, dcopy.ptr, ip.value, nbytes))
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return max_over_ranks(ws, e0.elapsed_time(e1) / args.steps)
+
+    save()
+    k0 = gpu.kernel_launches()
+    clocks = Clocks(local)
+    barrier(ws)
+    clocks.start()
+    ms_load = timed(load)
+    clk = clocks.stop()
+    launches = (gpu.kernel_launches() - k0) * args.steps // (args.steps + args.warmup)
+    ms_save = timed(save)
+    ms_rebuild = timed(rebuild)
+    ms_copy = timed(copy)
+    # Parity: the loaded table probes a 4M-tuple FK sample exactly like the
+    # built one, and its own image is the same bytes.
+    S = dg.probe_uniform(1 << 22, R, dg.seed_for(119), threads=threads)
+    S[::97, 0] += 2 * nb
+    dS = ctx.upload(S)
+    relS = gpu.Rel(dS.ptr, S.shape[0], 16, 0, 8)
+    t2 = ctypes.c_void_p()
+    ctx._check(L.pg_hashtable_deserialize(ctx.h, ctx.stream, ip.value, nbytes, ctypes.byref(t2)))
+    r1, r2 = gpu.JoinResult(), gpu.JoinResult()
+    fl = gpu.JOIN_COUNT | gpu.JOIN_SUM
+    ctx._check(L.pg_hashjoin_probe(ctx.h, ctx.stream, ht.value, ctypes.byref(relS), c, nc, None, 0, fl, 1,
+                                   ctypes.byref(r1)))
+    ctx._check(L.pg_hashjoin_probe(ctx.h, ctx.stream, t2.value, ctypes.byref(relS), c, nc, None, 0, fl, 1,
+                                   ctypes.byref(r2)))
+    img1 = np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(ip.value)).copy()
+    ctx._check(L.pg_hashtable_serialize(ctx.h, ctx.stream, t2.value, ip.value, nbytes, ctypes.byref(got)))
+    img2 = np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(ip.value))
+    hit = S[:, 0] <= nb
+    parity = {"probe_count_equal": r1.n_out == r2.n_out == int(hit.sum()),
+              "probe_sum_equal": r1.sum == r2.sum, "reserialized_image_identical": bool(np.array_equal(img1, img2))}
+    L.pg_hashtable_free(ctx.h, t2.value)
+    L.pg_hashtable_free(ctx.h, ht.value)
+    link = nbytes / (ms_copy / 1e3) / 1e9
+    achieved = nbytes / (ms_load / 1e3) / 1e9
+    if rank == 0:
+        line = {"metric": "join-table image load GB/s (16M-key narrow dense table from pinned host memory)",
+                "value": ws * achieved, "unit": "GB/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms_load, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "u32", "data": "synthetic (seeded generator; image in pinned host memory)",
+                "config": {"workload": f"load (H2D + device checksum + allocation) of the {nbytes}-byte image of "
+                                       f"a {nb}-key join table; rebuild = H2D of the {R.nbytes}-byte relation + "
+                                       "build", "op": "tableimage", "build_tuples": nb, "image_bytes": nbytes,
+                           "l2": "copies are link-bound; no flush"},
+                "save_ms": ms_save, "save_gbs": nbytes / (ms_save / 1e3) / 1e9, "load_ms": ms_load,
+                "rebuild_from_host_relation_ms": ms_rebuild, "load_speedup_vs_rebuild": ms_rebuild / ms_load,
+                "parity": parity,
+                "roofline": {"bound": "host link", "kernel": "pg_hashtable_deserialize (copy + k_image_sum)",
+                             "achieved": achieved, "peak": link, "unit": "GB/s", "frac": achieved / link,
+                             "traffic": None, "peak_source": "pinned H2D copy of the same bytes, same run"},
+                "e2e": {"value": ws * achieved, "unit": "GB/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": 8},
+                "gpu_launches": int(launches), "clocks": clk}
+        print(json.dumps(line), flush=True)
+    L.pg_host_free(ctx.h, ip.value)
+    L.pg_host_free(ctx.h, rp)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -892,7 +1013,7 @@ def main():
     ap.add_argument("--key-domain", default="dense", choices=["dense", "sparse"],
                     help="dense: keys 1..|R| (direct-mapped table); sparse: the same keys "
                          "multiplied by an odd constant (hashed table)")
-    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "batch", "serve"] + sorted(OPS))
+    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "batch", "serve", "tableimage"] + sorted(OPS))
     ap.add_argument("--slots", type=int, default=8, help="worker slots for --op serve")
     ap.add_argument("--retune", action="store_true", help="rerun the autotuner for --op batch")
     ap.add_argument("--scale-down", type=int, default=0, help="divide --op sizes by 2^k")
@@ -909,6 +1030,8 @@ def main():
         run_batch(args, ws, rank, local)
     elif args.op == "serve":
         run_serve(args, ws, rank, local)
+    elif args.op == "tableimage":
+        run_tableimage(args, ws, rank, local)
     elif args.op != "hashjoin":
         run_op(args, ws, rank, local, args.op)
     else:

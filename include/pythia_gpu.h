@@ -175,6 +175,34 @@ int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 		void* out, uint64_t out_capacity, int flags, int sum_col,
 		pg_join_result* res);
 int pg_hashtable_free(pg_ctx* ctx, pg_hashtable* ht);
+
+/* Table images: HashTable::serialize / deserialize (util/hashtable.cpp:99-201)
+ * with the segment files of creatememsegment (operators/memsegmentwriter.cpp:
+ * 154-197) and attachmemsegment (util/hashtable.cpp:124-178). An image is a
+ * 512-byte self-describing header (layout, key domain, build projection,
+ * checksums) and the table's arrays; loading needs no build relation and no
+ * table parameters. Tables that store build row indices (build-projected
+ * columns wider than 8 bytes) are not self-contained: PG_ERR_UNSUPPORTED.
+ *
+ * pg_hashtable_image_size: bytes of the image of `ht`.
+ * pg_hashtable_serialize: writes the image into host memory `image`
+ *   (pinned memory from pg_host_alloc copies fastest); *bytes = image size.
+ *   image == NULL only reports the size; a smaller capacity gives
+ *   PG_ERR_OUTPUT_FULL.
+ * pg_hashtable_deserialize: a new table on this context's device from an
+ *   image in host memory; a damaged image (magic, version, layout, sizes,
+ *   header or payload checksum) gives PG_ERR_ARG and no table. The table is
+ *   probed, grouped and freed like one from pg_hashjoin_build.
+ * pg_hashtable_save / _load: the same through a file; save creates a new
+ *   file and fails if `path` exists, as the reference's segment writer does. */
+int pg_hashtable_image_size(pg_ctx* ctx, const pg_hashtable* ht, uint64_t* bytes);
+int pg_hashtable_serialize(pg_ctx* ctx, pg_stream stream, const pg_hashtable* ht,
+		void* image, uint64_t capacity, uint64_t* bytes);
+int pg_hashtable_deserialize(pg_ctx* ctx, pg_stream stream, const void* image, uint64_t bytes,
+		pg_hashtable** ht);
+int pg_hashtable_save(pg_ctx* ctx, pg_stream stream, const pg_hashtable* ht, const char* path);
+int pg_hashtable_load(pg_ctx* ctx, pg_stream stream, const char* path, pg_hashtable** ht);
+
 /* Whole operator through HOST buffers (the call a Page-draining operator
  * makes): copies in, builds, probes, copies out. Chunked so copies overlap
  * the probe. out_host may be NULL with flags lacking PG_JOIN_MATERIALIZE. */

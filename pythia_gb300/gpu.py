@@ -64,7 +64,9 @@ SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_st
            "pg_groupby", "pg_sort_pages", "pg_mpsm_join", "pg_hashjoin_agg_noalloc",
            "pg_tune_set", "pg_tune_get", "pg_batch_prepare", "pg_batch_run", "pg_batch_free",
            "pg_generate_fk", "pg_buffer_alloc_async", "pg_buffer_free_async", "pg_generate_zipf_fk",
-           "pg_hashjoin_groupby", "pg_stream_create_urgent", "pg_autotune_batch"]
+           "pg_hashjoin_groupby", "pg_stream_create_urgent", "pg_autotune_batch",
+           "pg_hashtable_image_size", "pg_hashtable_serialize", "pg_hashtable_deserialize",
+           "pg_hashtable_save", "pg_hashtable_load"]
 TUNE = {"probe_ctas_per_sm": 0, "probe_variant": 1, "dense": 2, "partition_tile": 3,
         "groupby_smem_groups": 4, "radix_bits": 5, "probe_items": 6, "probe_cache": 7, "probe_passes": 8, "groupby_path": 9}
 
@@ -121,6 +123,11 @@ def lib():
             "pg_hashjoin_groupby": ([vp, vp, vp, P(Rel), u32, ci, ci, vp, u64, P(u64)], ci),
             "pg_stream_create_urgent": ([vp, P(vp)], ci),
             "pg_autotune_batch": ([vp, vp, P(BatchItem), u32, P(BatchShape), u32, ci, P(u32), P(ctypes.c_double)], ci),
+            "pg_hashtable_image_size": ([vp, vp, P(u64)], ci),
+            "pg_hashtable_serialize": ([vp, vp, vp, vp, u64, P(u64)], ci),
+            "pg_hashtable_deserialize": ([vp, vp, vp, u64, P(vp)], ci),
+            "pg_hashtable_save": ([vp, vp, vp, ctypes.c_char_p], ci),
+            "pg_hashtable_load": ([vp, vp, ctypes.c_char_p, P(vp)], ci),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -242,60 +249,47 @@ class Context:
         out = self.download(o, a.nbytes).view(a.dtype).reshape(a.shape)
         return out, self.download(offs, 8 * (nb + 1), np.uint64)
 
-    def hashjoin(self, R, S, proj=(("P", 8, 8), ("B", 8, 8)), bkey=(0, 8), pkey=(0, 8),
-                 flags=JOIN_MATERIALIZE, sum_col=-1, out_cap=None):
-        Ra, Sa = np.ascontiguousarray(R), np.ascontiguousarray(S)
-        dR, dS = self.upload(Ra), self.upload(Sa)
+    def build_table(self, R, proj=(("P", 8, 8), ("B", 8, 8)), bkey=(0, 8)):
+        """Builds the join table of R (pg_hashjoin_build) for the projection
+        `proj`; the table stays on the device until JoinTable.free()."""
+        Ra = np.ascontiguousarray(R)
+        dR = self.upload(Ra)
         rR = self.rel(dR, Ra.shape[0], row_width(Ra), *bkey)
-        rS = self.rel(dS, Sa.shape[0], row_width(Sa), *pkey)
         c, nc = cols(proj)
-        ow = sum(b for _, _, b in proj)
         ht = ctypes.c_void_p()
         self._check(lib().pg_hashjoin_build(self.h, self.stream, ctypes.byref(rR), c, nc, ctypes.byref(ht)))
+        return JoinTable(self, ht.value, proj, dR)
+
+    def load_table(self, image, proj=None):
+        """A join table from an image: bytes-like / uint8 array (pg_hashtable_
+        deserialize) or a file path (pg_hashtable_load)."""
+        ht = ctypes.c_void_p()
+        if isinstance(image, (str, os.PathLike)):
+            self._check(lib().pg_hashtable_load(self.h, self.stream, os.fsencode(image), ctypes.byref(ht)))
+        else:
+            a = np.frombuffer(image, dtype=np.uint8) if not isinstance(image, np.ndarray) else image
+            a = np.ascontiguousarray(a)
+            self._check(lib().pg_hashtable_deserialize(self.h, self.stream, a.ctypes.data, a.nbytes,
+                                                       ctypes.byref(ht)))
+        return JoinTable(self, ht.value, proj, None)
+
+    def hashjoin(self, R, S, proj=(("P", 8, 8), ("B", 8, 8)), bkey=(0, 8), pkey=(0, 8),
+                 flags=JOIN_MATERIALIZE, sum_col=-1, out_cap=None):
+        t = self.build_table(R, proj, bkey)
         try:
-            res = JoinResult()
-            if flags & JOIN_MATERIALIZE:
-                cap = Sa.shape[0] if out_cap is None else out_cap
-                o = self.alloc(max(cap, 1) * ow)
-                rc = lib().pg_hashjoin_probe(self.h, self.stream, ht.value, ctypes.byref(rS), c, nc,
-                                             o.ptr, cap, flags, sum_col, ctypes.byref(res))
-                if rc == PG_ERR_OUTPUT_FULL and out_cap is None:
-                    cap = res.n_out
-                    o = self.alloc(max(cap, 1) * ow)
-                    rc = lib().pg_hashjoin_probe(self.h, self.stream, ht.value, ctypes.byref(rS), c, nc,
-                                                 o.ptr, cap, flags, sum_col, ctypes.byref(res))
-                self._check(rc)
-                out = self.download(o, res.n_out * ow).reshape(-1, ow) if ow else None
-            else:
-                self._check(lib().pg_hashjoin_probe(self.h, self.stream, ht.value, ctypes.byref(rS), c, nc,
-                                                    None, 0, flags, sum_col, ctypes.byref(res)))
-                out = None
+            return t.probe(S, pkey=pkey, flags=flags, sum_col=sum_col, out_cap=out_cap)
         finally:
-            lib().pg_hashtable_free(self.h, ht.value)
-        return out, res.n_out, res.sum
+            t.free()
 
     def hashjoin_groupby(self, R, S, group=(8, 8), val=(8, "dec"), agg="sum", bkey=(0, 8), pkey=(0, 8)):
         """Join R and S on their keys and aggregate the probe column `val`
         grouped by the build column `group` in one pass (pg_hashjoin_groupby).
         Returns (group, agg) rows."""
-        Ra, Sa = np.ascontiguousarray(R), np.ascontiguousarray(S)
-        dR, dS = self.upload(Ra), self.upload(Sa)
-        rR = self.rel(dR, Ra.shape[0], row_width(Ra), *bkey)
-        rS = self.rel(dS, Sa.shape[0], row_width(Sa), *pkey)
-        c, nc = cols((("B", group[0], group[1]), ("P", val[0], 4 if val[1] == "int" else 8)))
-        ht = ctypes.c_void_p()
-        self._check(lib().pg_hashjoin_build(self.h, self.stream, ctypes.byref(rR), c, nc, ctypes.byref(ht)))
+        t = self.build_table(R, (("B", group[0], group[1]), ("P", val[0], 4 if val[1] == "int" else 8)), bkey)
         try:
-            vtype = VAL[val[1]]
-            ow = group[1] + (4 if (agg == "sum" and vtype == 0) else 8)
-            cap = max(Ra.shape[0], 1)
-            o = self.alloc(cap * ow)
-            ng = ctypes.c_uint64()
-            self._check(lib().pg_hashjoin_groupby(self.h, self.stream, ht.value, ctypes.byref(rS), val[0], vtype,
-                                                  AGG[agg], o.ptr, cap, ctypes.byref(ng)))
-            return self.download(o, ng.value * ow).reshape(-1, ow)
+            return t.groupby(S, val=val, agg=agg, pkey=pkey, cap=max(np.asarray(R).shape[0], 1))
         finally:
-            lib().pg_hashtable_free(self.h, ht.value)
+            t.free()
 
     def groupby(self, rows, key=(0, 8), val=(8, "long"), agg="sum", groups_hint=0, has_key=True):
         a = np.ascontiguousarray(rows)
@@ -340,6 +334,86 @@ class Context:
         self._check(lib().pg_mpsm_join(self.h, self.stream, ctypes.byref(rR), ctypes.byref(rS), c, nc,
                                        o.ptr, res.n_out, flags, sum_col, ctypes.byref(res)))
         return self.download(o, res.n_out * ow).reshape(-1, ow), res.n_out, res.sum
+
+
+class JoinTable:
+    """A join table resident on the device (pg_hashtable): built from a
+    relation, or loaded from an image, and probed any number of times."""
+
+    def __init__(self, ctx, handle, proj, build_buf):
+        self.ctx, self.h, self.proj, self._build_buf = ctx, handle, proj, build_buf
+
+    def free(self):
+        if self.h:
+            lib().pg_hashtable_free(self.ctx.h, self.h)
+            self.h = None
+        self._build_buf = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def probe(self, S, proj=None, pkey=(0, 8), flags=JOIN_MATERIALIZE, sum_col=-1, out_cap=None):
+        """pg_hashjoin_probe with S; returns (rows or None, n_out, sum)."""
+        ctx, L = self.ctx, lib()
+        proj = proj if proj is not None else self.proj
+        Sa = np.ascontiguousarray(S)
+        dS = ctx.upload(Sa)
+        rS = ctx.rel(dS, Sa.shape[0], row_width(Sa), *pkey)
+        c, nc = cols(proj)
+        ow = sum(b for _, _, b in proj)
+        res = JoinResult()
+        if not flags & JOIN_MATERIALIZE:
+            ctx._check(L.pg_hashjoin_probe(ctx.h, ctx.stream, self.h, ctypes.byref(rS), c, nc,
+                                           None, 0, flags, sum_col, ctypes.byref(res)))
+            return None, res.n_out, res.sum
+        cap = Sa.shape[0] if out_cap is None else out_cap
+        o = ctx.alloc(max(cap, 1) * ow)
+        rc = L.pg_hashjoin_probe(ctx.h, ctx.stream, self.h, ctypes.byref(rS), c, nc,
+                                 o.ptr, cap, flags, sum_col, ctypes.byref(res))
+        if rc == PG_ERR_OUTPUT_FULL and out_cap is None:
+            cap = res.n_out
+            o = ctx.alloc(max(cap, 1) * ow)
+            rc = L.pg_hashjoin_probe(ctx.h, ctx.stream, self.h, ctypes.byref(rS), c, nc,
+                                     o.ptr, cap, flags, sum_col, ctypes.byref(res))
+        ctx._check(rc)
+        out = ctx.download(o, res.n_out * ow).reshape(-1, ow) if ow else None
+        return out, res.n_out, res.sum
+
+    def groupby(self, S, val=(8, "dec"), agg="sum", pkey=(0, 8), cap=None):
+        """pg_hashjoin_groupby with S: (group, agg) rows."""
+        ctx, L = self.ctx, lib()
+        Sa = np.ascontiguousarray(S)
+        dS = ctx.upload(Sa)
+        rS = ctx.rel(dS, Sa.shape[0], row_width(Sa), *pkey)
+        vtype = VAL[val[1]]
+        gbytes = sum(b for s, _, b in self.proj if s in ("B", 0)) if self.proj else 8
+        ow = gbytes + (4 if (agg == "sum" and vtype == 0) else 8)
+        cap = max(int(cap or 1), 1)
+        o = ctx.alloc(cap * ow)
+        ng = ctypes.c_uint64()
+        ctx._check(L.pg_hashjoin_groupby(ctx.h, ctx.stream, self.h, ctypes.byref(rS), val[0], vtype,
+                                         AGG[agg], o.ptr, cap, ctypes.byref(ng)))
+        return ctx.download(o, ng.value * ow).reshape(-1, ow)
+
+    def image_size(self):
+        n = ctypes.c_uint64()
+        self.ctx._check(lib().pg_hashtable_image_size(self.ctx.h, self.h, ctypes.byref(n)))
+        return n.value
+
+    def serialize(self):
+        """The table's image (pg_hashtable_serialize) as a uint8 array."""
+        n = self.image_size()
+        out = np.empty(n, dtype=np.uint8)
+        m = ctypes.c_uint64()
+        self.ctx._check(lib().pg_hashtable_serialize(self.ctx.h, self.ctx.stream, self.h, out.ctypes.data, n,
+                                                     ctypes.byref(m)))
+        return out[:m.value]
+
+    def save(self, path):
+        self.ctx._check(lib().pg_hashtable_save(self.ctx.h, self.ctx.stream, self.h, os.fsencode(path)))
 
 
 def row_width(a):
