@@ -1002,6 +1002,127 @@ def run_tableimage(args, ws, rank, local):
     ctx.close()
 
 
+# ---------------------------------------------------------------------------
+# A q1-shaped plan through the operator layer (bench.py --op plan): the
+# reference's join -> join -> aggregate shape (q1/query1.conf:115-166) as
+# gpuhashjoin(orders, gpuhashjoin(parts, lines)) under gpuaggregate_sum,
+# memscan leaves over host relations, 16 threads; timed with the device
+# exchange between the GPU operators on and off (host pages in between).
+# ---------------------------------------------------------------------------
+PLAN_Q1 = """
+buffsize = 1048576;
+treeroot = { name = "sum"; input = { name = "joinO"; build = { name = "scanO"; };
+             probe = { name = "joinP"; build = { name = "scanP"; }; probe = { name = "scanL"; }; }; }; };
+scanO = { type = "memscan"; relation = "O"; schema = ("long", "long"); };
+scanP = { type = "memscan"; relation = "P"; schema = ("long", "long"); };
+scanL = { type = "memscan"; relation = "L"; schema = ("long", "long", "dec"); };
+joinP = { type = "gpuhashjoin"; buildjattr = 0; probejattr = 1; projection = ("P$0", "P$2", "B$1");
+          threadgroups = (%(all)s); hash = { fn = "modulo"; buckets = 1024; }; tuplesperbucket = 4; };
+joinO = { type = "gpuhashjoin"; buildjattr = 0; probejattr = 0; projection = ("B$1", "P$1");
+          threadgroups = (%(all)s); hash = { fn = "modulo"; buckets = 1024; }; tuplesperbucket = 4; };
+sum = { type = "gpuaggregate_sum"; field = 0; sumfield = 1; global = true; threads = %(t)d; };
+"""
+PLAN_L, PLAN_O, PLAN_P, PLAN_GROUPS = 1 << 26, 1 << 24, 1 << 22, 1000
+
+
+def _plan_inputs(nL, nO, nP, threads):
+    from pythia_gb300 import datagen as dg
+    O = dg.build_relation(nO, dg.seed_for(120), threads=threads)
+    O[:, 1] = O[:, 0] % PLAN_GROUPS
+    P = dg.build_relation(nP, dg.seed_for(121), threads=threads)
+    lo = dg.probe_uniform(nL, O, dg.seed_for(122), threads=threads)
+    lp = dg.probe_uniform(nL, P, dg.seed_for(123), threads=threads)
+    L = np.empty((nL, 3), np.int64)
+    L[:, 0] = lo[:, 0]
+    L[:, 1] = lp[:, 0]
+    L[:, 2] = ((lo[:, 1] & 0xFFFF).astype(np.float64) * 0.01).view(np.int64)
+    return O, P, L
+
+
+def run_plan(args, ws, rank, local):
+    import torch
+    from pythia_gb300 import plans
+    torch.cuda.set_device(local)
+    threads = min(16, host_threads())
+    nL, nO, nP = PLAN_L >> args.scale_down, PLAN_O >> args.scale_down, PLAN_P >> args.scale_down
+    O, P, L = _plan_inputs(nL, nO, nP, host_threads())
+    plans.register("O", O); plans.register("P", P); plans.register("L", L)
+    plan = PLAN_Q1 % {"all": "(" + ", ".join(str(t) for t in range(threads)) + ")", "t": threads}
+
+    def timed(on):
+        plans.set_device_exchange(on)
+        for _ in range(args.warmup):
+            plans.run(plan, threads=threads)
+        plans.transfer_stats(reset=True)
+        torch.cuda.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rows, _ = plans.run(plan, threads=threads)
+        torch.cuda.synchronize()
+        ms = max_over_ranks(ws, (time.perf_counter() - t0) * 1e3 / args.steps)
+        st = plans.transfer_stats(reset=True)
+        return ms, rows, {k: v // args.steps for k, v in st.items()}
+
+    from pythia_gb300 import gpu
+    k0 = gpu.kernel_launches()
+    clocks = Clocks(local)
+    clocks.start()
+    ms_on, rows_on, st_on = timed(True)
+    clk = clocks.stop()
+    launches = (gpu.kernel_launches() - k0) * args.steps // (args.steps + args.warmup)
+    ms_off, rows_off, st_off = timed(False)
+    plans.set_device_exchange(True)
+    # Parity at full size: every line's price lands in its order's group.
+    from oracle import oracle as orc
+    g_on = orc.canonical(rows_on).view(np.int64).reshape(-1, 2)
+    g_off = orc.canonical(rows_off).view(np.int64).reshape(-1, 2)
+    grp = L[:, 0] % PLAN_GROUPS
+    price = L[:, 2].view(np.float64)
+    pick = np.random.default_rng(5).choice(PLAN_GROUPS, 8, replace=False)
+    worst = 0.0
+    d = {int(k): float(v) for k, v in zip(g_on[:, 0], g_on[:, 1].view(np.float64))}
+    for k in pick:
+        ex = orc.fsum(price[grp == k])
+        worst = max(worst, abs(d[int(k)] - ex) / abs(ex))
+    parity = {"groups": int(g_on.shape[0]), "groups_ok": int(g_on.shape[0]) == PLAN_GROUPS,
+              "same_groups_on_and_off": bool(np.array_equal(g_on[:, 0], g_off[:, 0])),
+              "sampled_group_max_rel_err": worst, "tolerance": 1e-12, "ok": worst <= 1e-12}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        m = min(nL, 1 << 22)
+        t0 = time.perf_counter()
+        jp, _, _ = orc.hashjoin(P, L[:m], proj=(("P", 0, 8), ("P", 16, 8), ("B", 8, 8)), pkey=(8, 8),
+                                hash=orc.hashcfg("modulo", nP), threads=host_threads())
+        jo, _, _ = orc.hashjoin(O, jp.view(np.int64).reshape(-1, 3), proj=(("B", 8, 8), ("P", 8, 8)),
+                                hash=orc.hashcfg("modulo", nO), threads=host_threads())
+        orc.groupby(jo.view(np.int64).reshape(-1, 2), val=(8, "dec"), hash=orc.hashcfg("modulo", 1 << 10),
+                    threads=host_threads())
+        t = (time.perf_counter() - t0) * nL / m
+        cpu = {"value": nL / t, "unit": "lines/s", "cores": host_threads(), "kind": "port",
+               "sample": f"{m} lines through the oracle port's join, join and group-by (full order and part "
+                         f"builds), time scaled linearly to {nL}"}
+    value = ws * nL / (ms_on / 1e3)
+    if rank == 0:
+        line = {"metric": "q1-shaped plan lines/s through the GPU operator layer (join -> join -> aggregate_sum)",
+                "value": value, "unit": "lines/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms_on, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "int64/f64", "data": "synthetic (seeded generator, host relations read by memscan)",
+                "config": {"workload": f"{nL} lines (long, long, dec) joined with {nP} parts and {nO} orders, "
+                                       f"summed into {PLAN_GROUPS} groups; {threads} plan threads, one thread group",
+                           "op": "plan", "timing": "wall clock per plan run, host relations in and host rows out",
+                           "l2": "inputs larger than L2; no flush"},
+                "exchange_off_ms": ms_off, "exchange_speedup": ms_off / ms_on,
+                "transfer_bytes_per_run": {"exchange_on": st_on, "exchange_off": st_off},
+                "parity": parity,
+                "e2e": {"value": value, "unit": "lines/s", "h2d_bytes_per_step": st_on["h2d"],
+                        "d2h_bytes_per_step": st_on["d2h"]},
+                "gpu_launches": int(launches), "clocks": clk}
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1013,7 +1134,7 @@ def main():
     ap.add_argument("--key-domain", default="dense", choices=["dense", "sparse"],
                     help="dense: keys 1..|R| (direct-mapped table); sparse: the same keys "
                          "multiplied by an odd constant (hashed table)")
-    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "batch", "serve", "tableimage"] + sorted(OPS))
+    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "batch", "serve", "tableimage", "plan"] + sorted(OPS))
     ap.add_argument("--slots", type=int, default=8, help="worker slots for --op serve")
     ap.add_argument("--retune", action="store_true", help="rerun the autotuner for --op batch")
     ap.add_argument("--scale-down", type=int, default=0, help="divide --op sizes by 2^k")
@@ -1032,6 +1153,8 @@ def main():
         run_serve(args, ws, rank, local)
     elif args.op == "tableimage":
         run_tableimage(args, ws, rank, local)
+    elif args.op == "plan":
+        run_plan(args, ws, rank, local)
     elif args.op != "hashjoin":
         run_op(args, ws, rank, local, args.op)
     else:

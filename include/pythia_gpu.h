@@ -105,6 +105,7 @@ int pg_host_alloc(pg_ctx* ctx, uint64_t bytes, void** hptr);   /* pinned */
 int pg_host_free(pg_ctx* ctx, void* hptr);
 int pg_h2d(pg_ctx* ctx, pg_stream stream, void* dst, const void* src, uint64_t bytes);
 int pg_d2h(pg_ctx* ctx, pg_stream stream, void* dst, const void* src, uint64_t bytes);
+int pg_d2d(pg_ctx* ctx, pg_stream stream, void* dst, const void* src, uint64_t bytes);
 int pg_memset(pg_ctx* ctx, pg_stream stream, void* dst, int value, uint64_t bytes);
 /* Number of kernels this library has launched (process-wide). */
 uint64_t pg_kernel_launches(void);

@@ -199,6 +199,13 @@ extern "C" int pg_d2h(pg_ctx* ctx, pg_stream s, void* dst, const void* src, uint
 	return PG_OK;
 }
 
+extern "C" int pg_d2d(pg_ctx* ctx, pg_stream s, void* dst, const void* src, uint64_t bytes)
+{
+	if (!ctx) return PG_ERR_ARG;
+	if (bytes) PG_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t) s));
+	return PG_OK;
+}
+
 extern "C" int pg_memset(pg_ctx* ctx, pg_stream s, void* dst, int value, uint64_t bytes)
 {
 	if (!ctx) return PG_ERR_ARG;

@@ -58,7 +58,7 @@ class BatchShape(ctypes.Structure):
 
 SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_stream_create",
            "pg_stream_destroy", "pg_sync", "pg_buffer_alloc", "pg_buffer_free", "pg_host_alloc",
-           "pg_host_free", "pg_h2d", "pg_d2h", "pg_memset", "pg_kernel_launches",
+           "pg_host_free", "pg_h2d", "pg_d2h", "pg_d2d", "pg_memset", "pg_kernel_launches",
            "pg_hash_buckets", "pg_hash_tuples", "pg_partition", "pg_partition_sort",
            "pg_hashjoin_build", "pg_hashjoin_probe", "pg_hashtable_free", "pg_hashjoin_host",
            "pg_groupby", "pg_sort_pages", "pg_mpsm_join", "pg_hashjoin_agg_noalloc",
@@ -97,6 +97,7 @@ def lib():
             "pg_host_free": ([vp, vp], ci),
             "pg_h2d": ([vp, vp, vp, vp, u64], ci),
             "pg_d2h": ([vp, vp, vp, vp, u64], ci),
+            "pg_d2d": ([vp, vp, vp, vp, u64], ci),
             "pg_memset": ([vp, vp, vp, ci, u64], ci),
             "pg_kernel_launches": ([], u64),
             "pg_hash_buckets": ([vp, P(HashCfg), P(u32)], ci),

@@ -17,6 +17,13 @@ pthread_once_t g_once = PTHREAD_ONCE_INIT;
 pg_ctx* g_ctx = 0;
 pthread_mutex_t g_fail_mu = PTHREAD_MUTEX_INITIALIZER;
 std::string g_fail;
+TransferStats g_stats = {0, 0, 0, 0};
+volatile int g_exchange = 1;
+
+void count(unsigned long long* c, unsigned long long v)
+{
+	__sync_fetch_and_add(c, v);
+}
 
 void make_context()
 {
@@ -83,6 +90,29 @@ std::string last_failure()
 	return s;
 }
 
+TransferStats transfer_stats()
+{
+	TransferStats t;
+	t.h2d = __sync_fetch_and_add(&g_stats.h2d, 0);
+	t.d2h = __sync_fetch_and_add(&g_stats.d2h, 0);
+	t.d2d = __sync_fetch_and_add(&g_stats.d2d, 0);
+	t.in_place = __sync_fetch_and_add(&g_stats.in_place, 0);
+	return t;
+}
+
+void reset_transfer_stats()
+{
+	__sync_lock_test_and_set(&g_stats.h2d, 0);
+	__sync_lock_test_and_set(&g_stats.d2h, 0);
+	__sync_lock_test_and_set(&g_stats.d2d, 0);
+	__sync_lock_test_and_set(&g_stats.in_place, 0);
+}
+
+void set_device_exchange(bool on)
+{
+	g_exchange = on ? 1 : 0;
+}
+
 void GroupBarrier::arrive()
 {
 	pthread_mutex_lock(&mu_);
@@ -131,8 +161,22 @@ void GroupedOutput::setup(const ThreadGroups& g, unsigned tuple_size, unsigned b
 	page_bytes_ = std::max(tuple_size_, buffsize / tuple_size_ * tuple_size_);
 	out_.assign(g.members.size(), std::vector<char>());
 	rows_.assign(g.members.size(), 0);
-	Cursor c = { 0, 0, 0, true };
+	dev_.assign(g.members.size(), (const char*) 0);
+	Cursor c = { 0, 0, 0, true, 0, 0 };
 	cur_.assign(MAX_THREADS, c);
+}
+
+void GroupedOutput::own_device(void* p)
+{
+	pthread_mutex_lock(&mu_);
+	owned_.push_back(p);
+	pthread_mutex_unlock(&mu_);
+}
+
+void GroupedOutput::set_device(int group, const char* data, unsigned long long rows)
+{
+	dev_[group] = data;
+	rows_[group] = rows;
 }
 
 void GroupedOutput::assign(int tid, int group, int pos, int k)
@@ -143,6 +187,16 @@ void GroupedOutput::assign(int tid, int group, int pos, int k)
 	c.at = out_[group].empty() ? 0 : &out_[group][0] + lo * tuple_size_;
 	c.left = (hi - lo) * tuple_size_;
 	c.done = false;
+	c.dev = dev_[group] && hi > lo ? dev_[group] + lo * tuple_size_ : 0;
+	c.dev_rows = dev_[group] ? hi - lo : 0;
+}
+
+DeviceSpan GroupedOutput::share(int tid) const
+{
+	DeviceSpan d;
+	d.data = cur_[tid].dev;
+	d.rows = cur_[tid].dev_rows;
+	return d;
 }
 
 Operator::GetNextResultT GroupedOutput::next(int tid)
@@ -162,6 +216,10 @@ void GroupedOutput::clear()
 	for (size_t i = 0; i < cur_.size(); ++i) { delete cur_[i].page; cur_[i].page = 0; }
 	out_.clear();
 	rows_.clear();
+	dev_.clear();
+	pg_ctx* ctx = owned_.empty() ? 0 : shared_context();
+	for (size_t i = 0; i < owned_.size(); ++i) pg_buffer_free(ctx, owned_[i]);
+	owned_.clear();
 }
 
 bool drain(Operator* child, unsigned short tid, std::vector<char>& sink)
@@ -179,6 +237,84 @@ bool drain(Operator* child, unsigned short tid, std::vector<char>& sink)
 		}
 		if (r.first == Operator::Finished) return true;
 	}
+}
+
+void InputSide::setup(Operator* child)
+{
+	dev_ = g_exchange ? dynamic_cast<DeviceProducer*>(child) : 0;
+	if (dev_) dev_->keep_on_device();
+	host_.assign(MAX_THREADS, std::vector<char>());
+	DeviceSpan none = { 0, 0 };
+	spans_.assign(MAX_THREADS, none);
+}
+
+bool InputSide::fetch(Operator* child, unsigned short tid)
+{
+	if (!dev_) return drain(child, tid, host_[tid]);
+	spans_[tid] = dev_->device_share(tid);
+	return true;
+}
+
+int InputSide::gather(pg_ctx* ctx, pg_stream st, const std::vector<int>& members, unsigned width,
+		const char** data, unsigned long long* rows, void** tmp)
+{
+	*data = 0; *rows = 0; *tmp = 0;
+	unsigned long long n = 0;
+	bool adjacent = true;
+	const char* first = 0;
+	const char* end = 0;
+	for (size_t i = 0; i < members.size(); ++i) {
+		const int t = members[i];
+		const unsigned long long r = dev_ ? spans_[t].rows : (width ? host_[t].size() / width : 0);
+		if (!r) continue;
+		if (dev_) {
+			if (!first) first = spans_[t].data;
+			else if (spans_[t].data != end) adjacent = false;
+			end = spans_[t].data + r * width;
+		}
+		n += r;
+	}
+	*rows = n;
+	if (!n) return PG_OK;
+	// In place when the shares are one run that starts 16-byte aligned (the
+	// alignment every operator's loads assume); copied otherwise.
+	if (dev_ && adjacent && ((unsigned long long) (size_t) first & 15) == 0) {
+		*data = first;
+		count(&g_stats.in_place, 1);
+		return PG_OK;
+	}
+	int rc = pg_buffer_alloc(ctx, n * width, tmp);
+	if (rc) return rc;
+	char* at = (char*) *tmp;
+	for (size_t i = 0; i < members.size() && !rc; ++i) {
+		const int t = members[i];
+		if (dev_) {
+			const unsigned long long b = spans_[t].rows * width;
+			if (b) rc = pg_d2d(ctx, st, at, spans_[t].data, b);
+			count(&g_stats.d2d, b);
+			at += b;
+		} else {
+			const unsigned long long b = host_[t].size();
+			if (b) rc = pg_h2d(ctx, st, at, &host_[t][0], b);
+			count(&g_stats.h2d, b);
+			at += b;
+		}
+	}
+	*data = (const char*) *tmp;
+	return rc;
+}
+
+void InputSide::concat(const std::vector<int>& members, std::vector<char>& all)
+{
+	for (size_t i = 0; i < members.size(); ++i) {
+		all.insert(all.end(), host_[members[i]].begin(), host_[members[i]].end());
+		release(members[i]);
+	}
+}
+
+void InputSide::release(int tid)
+{
+	std::vector<char>().swap(host_[tid]);
 }
 
 // ---------------------------------------------------------------------------
@@ -222,8 +358,8 @@ void GpuJoinBase::init(libconfig::Config& root, libconfig::Setting& node)
 		barriers_.push_back(new GroupBarrier());
 		barriers_.back()->init((unsigned) groups_.members[g].size());
 	}
-	build_in_.assign(MAX_THREADS, std::vector<char>());
-	probe_in_.assign(MAX_THREADS, std::vector<char>());
+	build_.setup(buildOp);
+	probe_.setup(probeOp);
 	group_rc_.assign(groups_.members.size(), PG_OK);
 	output_.setup(groups_, schema.getTupleSize(), buffsize);
 }
@@ -233,41 +369,91 @@ void GpuJoinBase::threadInit(unsigned short threadid)
 	if (groups_.group_of.at(threadid) < 0) throw std::invalid_argument("thread not in any thread group");
 }
 
-pg_rel GpuJoinBase::side_rel(Operator* child, unsigned attr, const std::vector<char>& data)
+pg_rel GpuJoinBase::side_rel(Operator* child, unsigned attr, const void* data, unsigned long long bytes)
 {
 	Schema& s = child->getOutSchema();
 	pg_rel r;
 	r.width = s.getTupleSize();
-	r.n = r.width ? data.size() / r.width : 0;
-	r.data = data.empty() ? 0 : &data[0];
+	r.n = r.width ? bytes / r.width : 0;
+	r.data = r.n ? data : 0;
 	r.key_off = col_offset(s, attr);
 	r.key_bytes = key_bytes(s, attr);
 	return r;
+}
+
+// One launch over the group's inputs: host buffers in and out when neither
+// side nor the parent is a GPU operator and the join has a host path, device
+// memory otherwise.
+int GpuJoinBase::run_group(int g)
+{
+	const std::vector<int>& mem = groups_.members[g];
+	const unsigned ow = schema.getTupleSize();
+	int rc;
+	if (host_path() && !build_.on_device() && !probe_.on_device() && !on_device_) {
+		std::vector<char> R, S;
+		build_.concat(mem, R);
+		probe_.concat(mem, S);
+		const pg_rel r = side_rel(buildOp, buildkey_, R.empty() ? 0 : &R[0], R.size());
+		const pg_rel s = side_rel(probeOp, probekey_, S.empty() ? 0 : &S[0], S.size());
+		unsigned long long rows = 0;
+		rc = run_host(r, s, output_.buffer(g), &rows);
+		if (rc == PG_OK) {
+			count(&g_stats.h2d, R.size() + S.size());
+			count(&g_stats.d2h, rows * ow);
+		}
+		output_.set_rows(g, rc == PG_OK ? rows : 0);
+		return rc;
+	}
+	pg_ctx* ctx = shared_context();
+	if (!ctx) return PG_ERR_CUDA;
+	pg_stream st = 0;
+	if ((rc = pg_stream_create(ctx, &st))) return rc;
+	const char *dR = 0, *dS = 0;
+	unsigned long long nR = 0, nS = 0;
+	void *tR = 0, *tS = 0, *dO = 0;
+	unsigned long long rows = 0;
+	const unsigned wR = buildOp->getOutSchema().getTupleSize(), wS = probeOp->getOutSchema().getTupleSize();
+	if (!(rc = build_.gather(ctx, st, mem, wR, &dR, &nR, &tR)) &&
+			!(rc = probe_.gather(ctx, st, mem, wS, &dS, &nS, &tS))) {
+		const pg_rel r = side_rel(buildOp, buildkey_, dR, nR * wR);
+		const pg_rel s = side_rel(probeOp, probekey_, dS, nS * wS);
+		rc = run_device(ctx, st, r, s, &dO, &rows);
+	}
+	if (!rc && !on_device_) {
+		std::vector<char>& out = output_.buffer(g);
+		out.resize((size_t) (rows * ow));
+		if (rows) rc = pg_d2h(ctx, st, &out[0], dO, rows * ow);
+		if (!rc) count(&g_stats.d2h, rows * ow);
+	}
+	if (!rc) rc = pg_sync(ctx, st);
+	for (size_t i = 0; i < mem.size(); ++i) { build_.release(mem[i]); probe_.release(mem[i]); }
+	if (tR) pg_buffer_free(ctx, tR);
+	if (tS) pg_buffer_free(ctx, tS);
+	if (!rc && on_device_) {
+		output_.set_device(g, (const char*) dO, rows);
+		if (dO) output_.own_device(dO);
+		dO = 0;
+	} else {
+		output_.set_rows(g, rc ? 0 : rows);
+	}
+	if (dO) pg_buffer_free(ctx, dO);
+	pg_stream_destroy(ctx, st);
+	return rc;
 }
 
 Operator::ResultCode GpuJoinBase::scanStart(unsigned short tid, Page* idx, Schema& idxs)
 {
 	const int g = groups_.group_of[tid];
 	ResultCode rc = buildOp->scanStart(tid, idx, idxs);
-	bool ok = rc != Error && drain(buildOp, tid, build_in_[tid]);
+	bool ok = rc != Error && build_.fetch(buildOp, tid);
 	if (probeOp->scanStart(tid, idx, idxs) == Error) ok = false;
-	ok = ok && drain(probeOp, tid, probe_in_[tid]);
+	ok = ok && probe_.fetch(probeOp, tid);
 	if (!ok) group_rc_[g] = PG_ERR_ARG;
 	barriers_[g]->arrive();
 	const std::vector<int>& mem = groups_.members[g];
 	if (tid == mem[0] && group_rc_[g] == PG_OK) {
-		std::vector<char> R, S;
-		for (size_t i = 0; i < mem.size(); ++i) {
-			R.insert(R.end(), build_in_[mem[i]].begin(), build_in_[mem[i]].end());
-			S.insert(S.end(), probe_in_[mem[i]].begin(), probe_in_[mem[i]].end());
-			std::vector<char>().swap(build_in_[mem[i]]);
-			std::vector<char>().swap(probe_in_[mem[i]]);
-		}
-		unsigned long long rows = 0;
-		const pg_rel r = side_rel(buildOp, buildkey_, R), s = side_rel(probeOp, probekey_, S);
-		group_rc_[g] = run_group(r, s, output_.buffer(g), &rows);
+		group_rc_[g] = run_group(g);
 		if (group_rc_[g] != PG_OK) note_failure("gpu join", group_rc_[g]);
-		output_.set_rows(g, group_rc_[g] == PG_OK ? rows : 0);
 	}
 	barriers_[g]->arrive();
 	if (group_rc_[g] != PG_OK) return Error;
@@ -277,7 +463,7 @@ Operator::ResultCode GpuJoinBase::scanStart(unsigned short tid, Page* idx, Schem
 
 Operator::GetNextResultT GpuJoinBase::getNext(unsigned short tid)
 {
-	if (group_rc_[groups_.group_of[tid]] != PG_OK) return std::make_pair(Error, (Page*) 0);
+	if (on_device_ || group_rc_[groups_.group_of[tid]] != PG_OK) return std::make_pair(Error, (Page*) 0);
 	return output_.next(tid);
 }
 
@@ -288,8 +474,8 @@ Operator::ResultCode GpuJoinBase::scanStop(unsigned short tid)
 
 void GpuJoinBase::threadClose(unsigned short tid)
 {
-	std::vector<char>().swap(build_in_[tid]);
-	std::vector<char>().swap(probe_in_[tid]);
+	build_.release(tid);
+	probe_.release(tid);
 }
 
 void GpuJoinBase::destroy()
@@ -299,7 +485,22 @@ void GpuJoinBase::destroy()
 	barriers_.clear();
 }
 
-int GpuHashJoinOp::run_group(const pg_rel& R, const pg_rel& S, std::vector<char>& out, unsigned long long* rows)
+int GpuJoinBase::run_host(const pg_rel&, const pg_rel&, std::vector<char>&, unsigned long long*)
+{
+	return PG_ERR_UNSUPPORTED;
+}
+
+bool GpuJoinBase::host_path() const
+{
+	return false;
+}
+
+bool GpuHashJoinOp::host_path() const
+{
+	return true;
+}
+
+int GpuHashJoinOp::run_host(const pg_rel& R, const pg_rel& S, std::vector<char>& out, unsigned long long* rows)
 {
 	pg_ctx* ctx = shared_context();
 	if (!ctx) return PG_ERR_CUDA;
@@ -320,38 +521,52 @@ int GpuHashJoinOp::run_group(const pg_rel& R, const pg_rel& S, std::vector<char>
 	return PG_ERR_OUTPUT_FULL;
 }
 
-int GpuMPSMJoinOp::run_group(const pg_rel& R, const pg_rel& S, std::vector<char>& out, unsigned long long* rows)
+int GpuHashJoinOp::run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
+		unsigned long long* rows)
 {
-	pg_ctx* ctx = shared_context();
-	if (!ctx) return PG_ERR_CUDA;
 	const unsigned ow = schema.getTupleSize();
-	pg_stream st = 0;
-	int rc = pg_stream_create(ctx, &st);
+	pg_hashtable* ht = 0;
+	int rc = pg_hashjoin_build(ctx, st, &R, &cols_[0], (int) cols_.size(), &ht);
 	if (rc) return rc;
-	void *dR = 0, *dS = 0, *dO = 0;
+	unsigned long long cap = std::max<unsigned long long>(S.n, 1);
+	void* o = 0;
 	pg_join_result res;
 	res.n_out = 0; res.sum = 0;
-	const unsigned long long bR = R.n * R.width, bS = S.n * S.width;
-	if (!(rc = pg_buffer_alloc(ctx, bR ? bR : 16, &dR)) && !(rc = pg_buffer_alloc(ctx, bS ? bS : 16, &dS)) &&
-			!(rc = pg_h2d(ctx, st, dR, R.data, bR)) && !(rc = pg_h2d(ctx, st, dS, S.data, bS))) {
-		pg_rel r = R, s = S;
-		r.data = dR; s.data = dS;
-		// Count first (exact output size), then write.
-		if (!(rc = pg_mpsm_join(ctx, st, &r, &s, &cols_[0], (int) cols_.size(), 0, 0, PG_JOIN_COUNT, -1, &res))) {
-			const unsigned long long n = res.n_out;
-			out.resize((size_t) (n * ow));
-			if (n && !(rc = pg_buffer_alloc(ctx, n * ow, &dO)) &&
-					!(rc = pg_mpsm_join(ctx, st, &r, &s, &cols_[0], (int) cols_.size(), dO, n, PG_JOIN_MATERIALIZE, -1, &res)))
-				rc = pg_d2h(ctx, st, &out[0], dO, n * ow);
-			if (!rc) rc = pg_sync(ctx, st);
-			*rows = n;
+	for (int attempt = 0; attempt < 2; ++attempt) {
+		if ((rc = pg_buffer_alloc(ctx, cap * ow, &o))) break;
+		rc = pg_hashjoin_probe(ctx, st, ht, &S, &cols_[0], (int) cols_.size(), o, cap, PG_JOIN_MATERIALIZE, -1, &res);
+		if (rc == PG_ERR_OUTPUT_FULL && attempt == 0) {
+			pg_buffer_free(ctx, o);
+			o = 0;
+			cap = res.n_out;
+			continue;
 		}
+		break;
 	}
-	if (dO) pg_buffer_free(ctx, dO);
-	if (dS) pg_buffer_free(ctx, dS);
-	if (dR) pg_buffer_free(ctx, dR);
-	pg_stream_destroy(ctx, st);
-	return rc;
+	pg_hashtable_free(ctx, ht);
+	if (rc) { if (o) pg_buffer_free(ctx, o); return rc; }
+	*out = o;
+	*rows = res.n_out;
+	return PG_OK;
+}
+
+int GpuMPSMJoinOp::run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
+		unsigned long long* rows)
+{
+	const unsigned ow = schema.getTupleSize();
+	pg_join_result res;
+	res.n_out = 0; res.sum = 0;
+	// Count first (exact output size), then write.
+	int rc = pg_mpsm_join(ctx, st, &R, &S, &cols_[0], (int) cols_.size(), 0, 0, PG_JOIN_COUNT, -1, &res);
+	if (rc) return rc;
+	const unsigned long long n = res.n_out;
+	void* o = 0;
+	if ((rc = pg_buffer_alloc(ctx, std::max<unsigned long long>(n, 1) * ow, &o))) return rc;
+	if (n) rc = pg_mpsm_join(ctx, st, &R, &S, &cols_[0], (int) cols_.size(), o, n, PG_JOIN_MATERIALIZE, -1, &res);
+	if (rc) { pg_buffer_free(ctx, o); return rc; }
+	*out = o;
+	*rows = n;
+	return PG_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -388,7 +603,7 @@ void GpuPartitionOp::init(libconfig::Config& root, libconfig::Setting& node)
 	if (sort_ && (sortattr_ >= schema.columns() || !key_bytes(schema, sortattr_)))
 		throw std::invalid_argument("gpupartition: sortattr must be an integer column");
 	barrier_.init(nparts_);
-	in_.assign(MAX_THREADS, std::vector<char>());
+	in_.setup(nextOp);
 	rc_ = PG_OK;
 	// One group of nparts_ threads; partition t is served whole by thread t.
 	one_group_.group_of.assign(MAX_THREADS, -1);
@@ -407,55 +622,70 @@ void GpuPartitionOp::threadInit(unsigned short tid)
 	if (tid >= nparts_) throw std::invalid_argument("gpupartition: more threads than partitions");
 }
 
+// One launch over all threads' input (thread order); partition t goes to
+// thread t, downloaded into its pages or left on the device for a GPU parent.
+int GpuPartitionOp::run_partition()
+{
+	const unsigned w = schema.getTupleSize();
+	pg_ctx* ctx = shared_context();
+	if (!ctx) return PG_ERR_CUDA;
+	std::vector<int> all(nparts_);
+	for (unsigned t = 0; t < nparts_; ++t) all[t] = (int) t;
+	pg_stream st = 0;
+	int rc = pg_stream_create(ctx, &st);
+	if (rc) return rc;
+	const char* din = 0;
+	unsigned long long n = 0;
+	void *tin = 0, *dout = 0, *doffs = 0, *scratch = 0;
+	offsets_.assign(nparts_ + 1, 0);
+	if (!rc) rc = in_.gather(ctx, st, all, w, &din, &n, &tin);
+	if (!rc) rc = pg_buffer_alloc(ctx, n ? n * w : 16, &dout);
+	if (!rc) rc = pg_buffer_alloc(ctx, (nparts_ + 1) * 8, &doffs);
+	pg_rel r;
+	r.data = din; r.n = n; r.width = w;
+	r.key_off = col_offset(schema, attr_); r.key_bytes = key_bytes(schema, attr_);
+	if (!rc) rc = pg_partition(ctx, st, &r, &cfg_, dout, (uint64_t*) doffs);
+	if (!rc) rc = pg_d2h(ctx, st, &offsets_[0], doffs, (nparts_ + 1) * 8);
+	if (!rc) rc = pg_sync(ctx, st);
+	if (!rc && sort_ && n) {
+		pg_rel p = r;
+		p.data = dout;
+		p.key_off = col_offset(schema, sortattr_); p.key_bytes = key_bytes(schema, sortattr_);
+		// The input may be the child's output: sort with scratch of our own.
+		if (tin) scratch = tin;
+		else if (!(rc = pg_buffer_alloc(ctx, n * w, &tin))) scratch = tin;
+		if (!rc) rc = pg_partition_sort(ctx, st, &p, &offsets_[0], nparts_, scratch);
+	}
+	for (unsigned t = 0; t < nparts_ && !rc; ++t) {
+		const unsigned long long rows = offsets_[t + 1] - offsets_[t];
+		if (on_device_) {
+			served_.set_device((int) t, (const char*) dout + offsets_[t] * w, rows);
+			continue;
+		}
+		std::vector<char>& o = served_.buffer((int) t);
+		o.resize((size_t) (rows * w));
+		if (rows) rc = pg_d2h(ctx, st, &o[0], (char*) dout + offsets_[t] * w, rows * w);
+		count(&g_stats.d2h, rows * w);
+		served_.set_rows((int) t, rows);
+	}
+	if (!rc) rc = pg_sync(ctx, st);
+	for (unsigned t = 0; t < nparts_; ++t) in_.release((int) t);
+	if (!rc && on_device_) { served_.own_device(dout); dout = 0; }
+	if (doffs) pg_buffer_free(ctx, doffs);
+	if (dout) pg_buffer_free(ctx, dout);
+	if (tin) pg_buffer_free(ctx, tin);
+	pg_stream_destroy(ctx, st);
+	return rc;
+}
+
 Operator::ResultCode GpuPartitionOp::scanStart(unsigned short tid, Page* idx, Schema& idxs)
 {
-	bool ok = nextOp->scanStart(tid, idx, idxs) != Error && drain(nextOp, tid, in_[tid]);
+	bool ok = nextOp->scanStart(tid, idx, idxs) != Error && in_.fetch(nextOp, tid);
 	if (!ok) rc_ = PG_ERR_ARG;
 	barrier_.arrive();
 	if (tid == 0 && rc_ == PG_OK) {
-		std::vector<char> all;
-		for (unsigned t = 0; t < nparts_; ++t) {
-			all.insert(all.end(), in_[t].begin(), in_[t].end());
-			std::vector<char>().swap(in_[t]);
-		}
-		const unsigned w = schema.getTupleSize();
-		const unsigned long long n = w ? all.size() / w : 0;
-		pg_ctx* ctx = shared_context();
-		int rc = ctx ? PG_OK : PG_ERR_CUDA;
-		pg_stream st = 0;
-		void *din = 0, *dout = 0, *doffs = 0;
-		offsets_.assign(nparts_ + 1, 0);
-		if (!rc) rc = pg_stream_create(ctx, &st);
-		if (!rc) rc = pg_buffer_alloc(ctx, n ? n * w : 16, &din);
-		if (!rc) rc = pg_buffer_alloc(ctx, n ? n * w : 16, &dout);
-		if (!rc) rc = pg_buffer_alloc(ctx, (nparts_ + 1) * 8, &doffs);
-		if (!rc && n) rc = pg_h2d(ctx, st, din, &all[0], n * w);
-		pg_rel r;
-		r.data = din; r.n = n; r.width = w;
-		r.key_off = col_offset(schema, attr_); r.key_bytes = key_bytes(schema, attr_);
-		if (!rc) rc = pg_partition(ctx, st, &r, &cfg_, dout, (uint64_t*) doffs);
-		if (!rc) rc = pg_d2h(ctx, st, &offsets_[0], doffs, (nparts_ + 1) * 8);
-		if (!rc) rc = pg_sync(ctx, st);
-		if (!rc && sort_ && n) {
-			pg_rel p = r;
-			p.data = dout;
-			p.key_off = col_offset(schema, sortattr_); p.key_bytes = key_bytes(schema, sortattr_);
-			rc = pg_partition_sort(ctx, st, &p, &offsets_[0], nparts_, din);
-		}
-		for (unsigned t = 0; t < nparts_ && !rc; ++t) {
-			std::vector<char>& o = served_.buffer((int) t);
-			const unsigned long long rows = offsets_[t + 1] - offsets_[t];
-			o.resize((size_t) (rows * w));
-			if (rows) rc = pg_d2h(ctx, st, &o[0], (char*) dout + offsets_[t] * w, rows * w);
-			served_.set_rows((int) t, rows);
-		}
-		if (!rc) rc = pg_sync(ctx, st);
-		if (doffs) pg_buffer_free(ctx, doffs);
-		if (dout) pg_buffer_free(ctx, dout);
-		if (din) pg_buffer_free(ctx, din);
-		if (st) pg_stream_destroy(ctx, st);
-		if (rc) note_failure("gpupartition", rc);
-		rc_ = rc;
+		rc_ = run_partition();
+		if (rc_) note_failure("gpupartition", rc_);
 	}
 	barrier_.arrive();
 	if (rc_ != PG_OK) return Error;
@@ -465,7 +695,7 @@ Operator::ResultCode GpuPartitionOp::scanStart(unsigned short tid, Page* idx, Sc
 
 Operator::GetNextResultT GpuPartitionOp::getNext(unsigned short tid)
 {
-	if (rc_ != PG_OK) return std::make_pair(Error, (Page*) 0);
+	if (on_device_ || rc_ != PG_OK) return std::make_pair(Error, (Page*) 0);
 	return served_.next(tid);
 }
 
@@ -524,7 +754,7 @@ void GpuAggregateOp::init(libconfig::Config& root, libconfig::Setting& node)
 		}
 	}
 	barrier_.init(threads_);
-	in_.assign(MAX_THREADS, std::vector<char>());
+	in_.setup(nextOp);
 	rc_ = PG_OK;
 	output_.setup(groups_, schema.getTupleSize(), buffsize);
 }
@@ -534,21 +764,22 @@ void GpuAggregateOp::threadInit(unsigned short tid)
 	if (global_ && tid >= threads_) throw std::invalid_argument("thread id beyond `threads'");
 }
 
-int GpuAggregateOp::aggregate(const std::vector<char>& in, std::vector<char>& out, unsigned long long* groups)
+int GpuAggregateOp::aggregate(const std::vector<int>& members, int g)
 {
 	pg_ctx* ctx = shared_context();
 	if (!ctx) return PG_ERR_CUDA;
 	Schema& is = nextOp->getOutSchema();
 	const unsigned w = is.getTupleSize(), ow = schema.getTupleSize();
-	const unsigned long long n = w ? in.size() / w : 0;
 	pg_stream st = 0;
 	int rc = pg_stream_create(ctx, &st);
 	if (rc) return rc;
-	void *din = 0, *dout = 0;
-	const unsigned long long cap = std::max<unsigned long long>(n, 1);
+	const char* din = 0;
+	unsigned long long n = 0;
+	void *tin = 0, *dout = 0;
 	uint64_t ng = 0;
-	if (!(rc = pg_buffer_alloc(ctx, n ? n * w : 16, &din)) && !(rc = pg_buffer_alloc(ctx, cap * ow, &dout)) &&
-			!(n && (rc = pg_h2d(ctx, st, din, &in[0], n * w)))) {
+	if (!(rc = in_.gather(ctx, st, members, w, &din, &n, &tin)) &&
+			!(rc = pg_buffer_alloc(ctx, std::max<unsigned long long>(n, 1) * ow, &dout))) {
+		const unsigned long long cap = std::max<unsigned long long>(n, 1);
 		pg_rel r;
 		r.data = din; r.n = n; r.width = w;
 		r.key_off = field_ >= 0 ? col_offset(is, field_) : 0;
@@ -559,45 +790,44 @@ int GpuAggregateOp::aggregate(const std::vector<char>& in, std::vector<char>& ou
 			const ColumnType t = is.getColumnType(sumfield_);
 			vt = t == CT_INTEGER ? PG_VAL_INT : t == CT_DECIMAL ? PG_VAL_DEC : PG_VAL_LONG;
 		}
-		if (!(rc = pg_groupby(ctx, st, &r, voff, vt, agg_, 0, dout, cap, &ng))) {
+		if (!(rc = pg_groupby(ctx, st, &r, voff, vt, agg_, 0, dout, cap, &ng)) && !on_device_) {
+			std::vector<char>& out = output_.buffer(g);
 			out.resize((size_t) (ng * ow));
 			if (ng) rc = pg_d2h(ctx, st, &out[0], dout, ng * ow);
-			if (!rc) rc = pg_sync(ctx, st);
+			count(&g_stats.d2h, ng * ow);
 		}
+		if (!rc) rc = pg_sync(ctx, st);
+	}
+	for (size_t i = 0; i < members.size(); ++i) in_.release(members[i]);
+	if (tin) pg_buffer_free(ctx, tin);
+	if (!rc && on_device_) {
+		output_.set_device(g, (const char*) dout, ng);
+		output_.own_device(dout);
+		dout = 0;
+	} else {
+		output_.set_rows(g, rc ? 0 : ng);
 	}
 	if (dout) pg_buffer_free(ctx, dout);
-	if (din) pg_buffer_free(ctx, din);
 	pg_stream_destroy(ctx, st);
-	*groups = ng;
 	return rc;
 }
 
 Operator::ResultCode GpuAggregateOp::scanStart(unsigned short tid, Page* idx, Schema& idxs)
 {
-	bool ok = nextOp->scanStart(tid, idx, idxs) != Error && drain(nextOp, tid, in_[tid]);
+	bool ok = nextOp->scanStart(tid, idx, idxs) != Error && in_.fetch(nextOp, tid);
 	// The scan of the input ends inside scanStart, as GenericAggregate's does.
 	if (nextOp->scanStop(tid) == Error) ok = false;
 	if (!global_) {
-		unsigned long long ng = 0;
-		int rc = ok ? aggregate(in_[tid], output_.buffer(tid), &ng) : PG_ERR_ARG;
-		std::vector<char>().swap(in_[tid]);
+		int rc = ok ? aggregate(std::vector<int>(1, (int) tid), tid) : PG_ERR_ARG;
 		if (rc) { note_failure("gpuaggregate", rc); return Error; }
-		output_.set_rows(tid, ng);
 		output_.assign(tid, tid, 0, 1);
 		return Ready;
 	}
 	if (!ok) rc_ = PG_ERR_ARG;
 	barrier_.arrive();
 	if (tid == 0 && rc_ == PG_OK) {
-		std::vector<char> all;
-		for (unsigned t = 0; t < threads_; ++t) {
-			all.insert(all.end(), in_[t].begin(), in_[t].end());
-			std::vector<char>().swap(in_[t]);
-		}
-		unsigned long long ng = 0;
-		rc_ = aggregate(all, output_.buffer(0), &ng);
+		rc_ = aggregate(groups_.members[0], 0);
 		if (rc_) note_failure("gpuaggregate", rc_);
-		output_.set_rows(0, rc_ ? 0 : ng);
 	}
 	barrier_.arrive();
 	if (rc_ != PG_OK) return Error;
@@ -607,7 +837,7 @@ Operator::ResultCode GpuAggregateOp::scanStart(unsigned short tid, Page* idx, Sc
 
 Operator::GetNextResultT GpuAggregateOp::getNext(unsigned short tid)
 {
-	if (global_ && rc_ != PG_OK) return std::make_pair(Error, (Page*) 0);
+	if (on_device_ || (global_ && rc_ != PG_OK)) return std::make_pair(Error, (Page*) 0);
 	return output_.next(tid);
 }
 

@@ -17,6 +17,16 @@
 //   scanStop     propagates down;
 //   destroy      frees the outputs.
 //
+// Adjacent GPU operators exchange their data on the device. A GPU operator
+// whose child is another GPU operator asks it, from init, to keep its output
+// in device memory; each of its threads then takes its share of the child's
+// output as a device span instead of reading pages, and the group's first
+// thread runs its launch over the group's shares: in place when they are
+// adjacent in the child's output, gathered by device copies otherwise. Only
+// the leaves' pages cross to the device and only the top GPU operator's output
+// comes back. This takes the place of the host-side page hand-over of
+// MergeOp (operators/merge.cpp:433-543) between GPU operators.
+//
 // Compiled against the engine's own headers (PYTHIA_REFERENCE_HEADERS) the
 // classes drop into its plans; otherwise against the mirror of its operator
 // interface in mirror/pythia_mirror.h.
@@ -42,6 +52,40 @@ namespace pythia_gpu_ops {
 pg_ctx* shared_context();
 // Message of the last failure seen by an operator of this process.
 std::string last_failure();
+
+// Data the operators moved (process-wide, bytes): pages uploaded to the
+// device, outputs downloaded to pages, device copies gathering inputs, and
+// the number of inputs taken on the device without any copy.
+struct TransferStats {
+	unsigned long long h2d, d2h, d2d, in_place;
+};
+TransferStats transfer_stats();
+void reset_transfer_stats();
+// Device exchange between adjacent GPU operators: on by default. Off, every
+// operator reads and writes host pages (for comparison and tests); takes
+// effect for operators initialised afterwards.
+void set_device_exchange(bool on);
+
+// Rows of one operator thread's output in device memory.
+struct DeviceSpan {
+	const char* data;           // device pointer; NULL when rows == 0
+	unsigned long long rows;
+};
+
+// A GPU operator that can leave its output on the device for a GPU parent.
+class DeviceProducer {
+public:
+	DeviceProducer() : on_device_(false) { }
+	virtual ~DeviceProducer() { }
+	// Called by the parent's init: keep the output on the device; getNext
+	// then reports Error (the parent takes device_share instead).
+	void keep_on_device() { on_device_ = true; }
+	// After scanStart(tid) returned Ready: the rows thread `tid` serves,
+	// valid until destroy.
+	virtual DeviceSpan device_share(unsigned short tid) = 0;
+protected:
+	bool on_device_;
+};
 
 class GroupBarrier {
 public:
@@ -69,22 +113,36 @@ struct ThreadGroups {
 	void parse(libconfig::Setting& node, int default_threads);
 };
 
-// Per-group shared output and per-thread serving state.
+// Per-group shared output and per-thread serving state. A group's output is
+// either host memory served as pages, or device memory taken by a GPU parent.
 class GroupedOutput {
 public:
-	GroupedOutput() : tuple_size_(0), page_bytes_(0) { }
-	~GroupedOutput() { clear(); }
+	GroupedOutput() : tuple_size_(0), page_bytes_(0) { pthread_mutex_init(&mu_, 0); }
+	~GroupedOutput() { clear(); pthread_mutex_destroy(&mu_); }
 	void setup(const ThreadGroups& g, unsigned tuple_size, unsigned buffsize);
 	std::vector<char>& buffer(int group) { return out_[group]; }
 	void set_rows(int group, unsigned long long rows) { rows_[group] = rows; }
+	// The group's output is `rows` tuples at device address `data`.
+	void set_device(int group, const char* data, unsigned long long rows);
+	// Device memory freed by clear(); threads may hand it over concurrently.
+	void own_device(void* p);
 	// Thread `tid` serves rows [pos * rows / k, (pos + 1) * rows / k) of its group.
 	void assign(int tid, int group, int pos, int k);
 	Operator::GetNextResultT next(int tid);
+	DeviceSpan share(int tid) const;
 	void clear();
 private:
-	struct Cursor { char* at; unsigned long long left; Operator::Page* page; bool done; };
+	GroupedOutput(const GroupedOutput&);
+	GroupedOutput& operator=(const GroupedOutput&);
+	struct Cursor {
+		char* at; unsigned long long left; Operator::Page* page; bool done;
+		const char* dev; unsigned long long dev_rows;
+	};
+	pthread_mutex_t mu_;
 	std::vector<std::vector<char> > out_;
 	std::vector<unsigned long long> rows_;
+	std::vector<const char*> dev_;
+	std::vector<void*> owned_;
 	std::vector<Cursor> cur_;
 	unsigned tuple_size_, page_bytes_;
 };
@@ -93,7 +151,33 @@ private:
 // Returns false when the child reports Error.
 bool drain(Operator* child, unsigned short tid, std::vector<char>& sink);
 
-class GpuJoinBase : public DualInputOp {
+// One input of a GPU operator: the child's pages drained into host memory,
+// or, when the child is a GPU operator keeping its output on the device,
+// each thread's device span.
+class InputSide {
+public:
+	InputSide() : dev_(0) { }
+	// From init: asks a GPU child to keep its output on the device.
+	void setup(Operator* child);
+	bool on_device() const { return dev_ != 0; }
+	// After child->scanStart(tid): drains the pages or takes the span.
+	bool fetch(Operator* child, unsigned short tid);
+	// The rows of `members`, in order, as one device array of `width`-byte
+	// tuples on stream `st`. *data points into the child's output when the
+	// shares are adjacent there, else into *tmp (device memory the caller
+	// frees after the stream's work).
+	int gather(pg_ctx* ctx, pg_stream st, const std::vector<int>& members, unsigned width,
+			const char** data, unsigned long long* rows, void** tmp);
+	// Host bytes of `members`, concatenated (host path).
+	void concat(const std::vector<int>& members, std::vector<char>& all);
+	void release(int tid);
+private:
+	DeviceProducer* dev_;
+	std::vector<std::vector<char> > host_;
+	std::vector<DeviceSpan> spans_;
+};
+
+class GpuJoinBase : public DualInputOp, public DeviceProducer {
 public:
 	GpuJoinBase() : buildkey_(0), probekey_(0) { }
 	virtual void init(libconfig::Config& root, libconfig::Setting& node);
@@ -103,19 +187,26 @@ public:
 	virtual ResultCode scanStop(unsigned short threadid);
 	virtual void threadClose(unsigned short threadid);
 	virtual void destroy();
+	virtual DeviceSpan device_share(unsigned short threadid) { return output_.share(threadid); }
 protected:
-	// Runs the join of one group's inputs into `out`; returns a PG_* code.
-	virtual int run_group(const pg_rel& R, const pg_rel& S, std::vector<char>& out,
+	// Whether run_host exists: it takes the group's host inputs and fills host
+	// rows (copies overlapped with the work); used when no input and not the
+	// output are on the device.
+	virtual bool host_path() const;
+	virtual int run_host(const pg_rel& R, const pg_rel& S, std::vector<char>& out, unsigned long long* rows);
+	// Joins device inputs on `st` into device rows *out (freed by the caller).
+	virtual int run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
 			unsigned long long* rows) = 0;
 	std::vector<pg_col> cols_;
 	unsigned buildkey_, probekey_;
 private:
+	int run_group(int g);
 	ThreadGroups groups_;
 	std::vector<GroupBarrier*> barriers_;
-	std::vector<std::vector<char> > build_in_, probe_in_;
+	InputSide build_, probe_;
 	std::vector<int> group_rc_;
 	GroupedOutput output_;
-	pg_rel side_rel(Operator* child, unsigned attr, const std::vector<char>& data);
+	pg_rel side_rel(Operator* child, unsigned attr, const void* data, unsigned long long bytes);
 };
 
 // "gpuhashjoin": HashJoinOp's keys (operators/join.cpp:184-366): projection,
@@ -123,7 +214,10 @@ private:
 // have no effect on the result.
 class GpuHashJoinOp : public GpuJoinBase {
 protected:
-	virtual int run_group(const pg_rel& R, const pg_rel& S, std::vector<char>& out, unsigned long long* rows);
+	virtual bool host_path() const;
+	virtual int run_host(const pg_rel& R, const pg_rel& S, std::vector<char>& out, unsigned long long* rows);
+	virtual int run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
+			unsigned long long* rows);
 };
 
 // "gpumpsmjoin": OldMPSMJoinOp / MPSMJoinOp keys (join.cpp:677-783,
@@ -131,7 +225,8 @@ protected:
 // and presorted keys are read and have no effect on the result.
 class GpuMPSMJoinOp : public GpuJoinBase {
 protected:
-	virtual int run_group(const pg_rel& R, const pg_rel& S, std::vector<char>& out, unsigned long long* rows);
+	virtual int run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
+			unsigned long long* rows);
 };
 
 // "gpupartition": PartitionOp (operators/partition.cpp:45-404): `attr`,
@@ -141,9 +236,10 @@ protected:
 // partition on `sortattr` (default `attr`). Thread t serves partition t.
 // Tuples keep the order in which threads 0, 1, ... read them, as the
 // reference's per-thread prefix sums arrange.
-class GpuPartitionOp : public SingleInputOp {
+class GpuPartitionOp : public SingleInputOp, public DeviceProducer {
 public:
 	GpuPartitionOp() : attr_(0), sortattr_(0), sort_(false), nparts_(1) { }
+	virtual DeviceSpan device_share(unsigned short threadid) { return served_.share(threadid); }
 	virtual void init(libconfig::Config& root, libconfig::Setting& node);
 	virtual void threadInit(unsigned short threadid);
 	virtual ResultCode scanStart(unsigned short threadid, Page* indexdatapage, Schema& indexdataschema);
@@ -155,9 +251,9 @@ private:
 	bool sort_;
 	unsigned nparts_;
 	pg_hashcfg cfg_;
+	int run_partition();
 	GroupBarrier barrier_;
-	std::vector<std::vector<char> > in_;
-	std::vector<char> out_;
+	InputSide in_;
 	std::vector<uint64_t> offsets_;
 	int rc_;
 	ThreadGroups one_group_;
@@ -172,9 +268,10 @@ private:
 // spreads the groups over the threads, otherwise every thread aggregates and
 // emits its own input. Output: (group column, aggregate), the aggregate typed
 // like the summed column (sum) or long (count).
-class GpuAggregateOp : public SingleInputOp {
+class GpuAggregateOp : public SingleInputOp, public DeviceProducer {
 public:
 	explicit GpuAggregateOp(int agg) : agg_(agg), field_(-1), sumfield_(0), global_(false), threads_(1) { }
+	virtual DeviceSpan device_share(unsigned short threadid) { return output_.share(threadid); }
 	virtual void init(libconfig::Config& root, libconfig::Setting& node);
 	virtual void threadInit(unsigned short threadid);
 	virtual ResultCode scanStart(unsigned short threadid, Page* indexdatapage, Schema& indexdataschema);
@@ -182,14 +279,15 @@ public:
 	virtual ResultCode scanStop(unsigned short threadid);
 	virtual void destroy();
 private:
-	int aggregate(const std::vector<char>& in, std::vector<char>& out, unsigned long long* groups);
+	// Aggregates the shares of `members` into group `g` of the output.
+	int aggregate(const std::vector<int>& members, int g);
 	int agg_;
 	int field_;
 	unsigned sumfield_;
 	bool global_;
 	unsigned threads_;
 	GroupBarrier barrier_;
-	std::vector<std::vector<char> > in_;
+	InputSide in_;
 	int rc_;
 	ThreadGroups groups_;
 	GroupedOutput output_;

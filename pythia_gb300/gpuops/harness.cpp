@@ -218,4 +218,19 @@ int pgo_run(const char* plan, int threads, void** out, unsigned long long* nbyte
 
 void pgo_free(void* p) { free(p); }
 
+// Bytes the GPU operators moved since the last reset: out[0] pages uploaded,
+// out[1] outputs downloaded, out[2] device copies gathering inputs, out[3]
+// inputs taken on the device in place.
+void pgo_transfer_stats(unsigned long long* out)
+{
+	const pythia_gpu_ops::TransferStats t = pythia_gpu_ops::transfer_stats();
+	out[0] = t.h2d; out[1] = t.d2h; out[2] = t.d2d; out[3] = t.in_place;
+}
+
+void pgo_reset_transfer_stats() { pythia_gpu_ops::reset_transfer_stats(); }
+
+// 1 (default): adjacent GPU operators exchange data on the device; 0: every
+// operator reads and writes host pages.
+void pgo_set_device_exchange(int on) { pythia_gpu_ops::set_device_exchange(on != 0); }
+
 }  // extern "C"

@@ -50,6 +50,12 @@ def lib():
         L.pgo_run.restype = ctypes.c_int
         L.pgo_free.argtypes = [ctypes.c_void_p]
         L.pgo_free.restype = None
+        L.pgo_transfer_stats.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)]
+        L.pgo_transfer_stats.restype = None
+        L.pgo_reset_transfer_stats.argtypes = []
+        L.pgo_reset_transfer_stats.restype = None
+        L.pgo_set_device_exchange.argtypes = [ctypes.c_int]
+        L.pgo_set_device_exchange.restype = None
         _LIB = L
     return _LIB
 
@@ -85,3 +91,20 @@ def run(plan, threads=1):
     finally:
         if out.value:
             lib().pgo_free(out)
+
+
+def transfer_stats(reset=False):
+    """Bytes the GPU operators moved since the last reset: pages uploaded
+    ("h2d"), outputs downloaded ("d2h"), device copies gathering inputs
+    ("d2d"), and inputs taken on the device in place ("in_place", a count)."""
+    a = (ctypes.c_ulonglong * 4)()
+    lib().pgo_transfer_stats(a)
+    if reset:
+        lib().pgo_reset_transfer_stats()
+    return {"h2d": a[0], "d2h": a[1], "d2d": a[2], "in_place": a[3]}
+
+
+def set_device_exchange(on):
+    """Adjacent GPU operators keep their data on the device (default True);
+    False makes every operator read and write host pages."""
+    lib().pgo_set_device_exchange(1 if on else 0)

@@ -90,6 +90,37 @@ def test_gpu_operator_without_gpu_returns_error():
     assert e.value.code == 1
 
 
+def test_gpu_chain_without_gpu_returns_error_and_moves_nothing():
+    # partition -> join with the device exchange set up at init: without a GPU
+    # the partition fails in scanStart, the join sees its child's Error, every
+    # thread returns Error and no bytes are counted as moved.
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    plans.register("R", np.arange(40, dtype=np.int64).reshape(20, 2))
+    plan = """
+    buffsize = 4096;
+    treeroot = { name = "join"; build = { name = "pr"; input = { name = "r"; }; };
+                                probe = { name = "ps"; input = { name = "s"; }; }; };
+    r = { type = "memscan"; relation = "R"; schema = ("long", "long"); };
+    s = { type = "memscan"; relation = "R"; schema = ("long", "long"); };
+    pr = { type = "gpupartition"; attr = 0; range = (0, 39); buckets = 2; };
+    ps = { type = "gpupartition"; attr = 0; range = (0, 39); buckets = 2; };
+    join = { type = "gpuhashjoin"; buildjattr = 0; probejattr = 0; projection = ("P$1", "B$1");
+             threadgroups = ((0), (1)); };
+    """
+    plans.transfer_stats(reset=True)
+    for on in (True, False):
+        plans.set_device_exchange(on)
+        try:
+            with pytest.raises(plans.PlanError) as e:
+                plans.run(plan, threads=2)
+        finally:
+            plans.set_device_exchange(True)
+        assert e.value.code == 1
+    assert plans.transfer_stats() == {"h2d": 0, "d2h": 0, "d2d": 0, "in_place": 0}
+
+
 def test_reference_engine_drives_gpu_operator():
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_gpuops_check")
     if not os.path.exists(exe):
