@@ -239,82 +239,200 @@ bool drain(Operator* child, unsigned short tid, std::vector<char>& sink)
 	}
 }
 
+// Pinned staging buffers shared by every operator of the process: made on
+// first use, kept for later plans (pinned allocation costs milliseconds).
+namespace {
+const unsigned long long STAGE_BYTES = 4ull << 20;
+const unsigned long long FIRST_CHUNK = 16ull << 20, LAST_CHUNK = 512ull << 20;
+pthread_mutex_t g_stage_mu = PTHREAD_MUTEX_INITIALIZER;
+std::vector<char*> g_stage_free;
+
+char* stage_take(pg_ctx* ctx)
+{
+	pthread_mutex_lock(&g_stage_mu);
+	char* p = 0;
+	if (!g_stage_free.empty()) { p = g_stage_free.back(); g_stage_free.pop_back(); }
+	pthread_mutex_unlock(&g_stage_mu);
+	if (!p) {
+		void* q = 0;
+		if (pg_host_alloc(ctx, STAGE_BYTES, &q) == PG_OK) p = (char*) q;
+	}
+	return p;
+}
+
+void stage_give(char* p)
+{
+	if (!p) return;
+	pthread_mutex_lock(&g_stage_mu);
+	g_stage_free.push_back(p);
+	pthread_mutex_unlock(&g_stage_mu);
+}
+}  // namespace
+
 void InputSide::setup(Operator* child)
 {
+	clear();
 	dev_ = g_exchange ? dynamic_cast<DeviceProducer*>(child) : 0;
 	if (dev_) dev_->keep_on_device();
 	host_.assign(MAX_THREADS, std::vector<char>());
+	staged_.assign(MAX_THREADS, Staged());
 	DeviceSpan none = { 0, 0 };
 	spans_.assign(MAX_THREADS, none);
 }
 
 bool InputSide::fetch(Operator* child, unsigned short tid)
 {
-	if (!dev_) return drain(child, tid, host_[tid]);
-	spans_[tid] = dev_->device_share(tid);
+	if (dev_) {
+		spans_[tid] = dev_->device_share(tid);
+		return true;
+	}
+	if (!shared_context()) return drain(child, tid, host_[tid]);
+	return stage(child, tid);
+}
+
+// Sends `n` staged bytes to the thread's device chunks, opening a new chunk
+// when the current one is full.
+bool InputSide::flush(pg_ctx* ctx, pg_stream st, Staged& u, const char* buf, unsigned long long n,
+		unsigned long long& room, unsigned long long& next_chunk)
+{
+	if (!n) return true;
+	if (n > room) {
+		const unsigned long long size = std::max(n, next_chunk);
+		void* c = 0;
+		if (pg_buffer_alloc_async(ctx, st, size, &c) != PG_OK) return false;
+		u.chunks.push_back((char*) c);
+		u.used.push_back(0);
+		room = size;
+		next_chunk = std::min(next_chunk * 2, LAST_CHUNK);
+	}
+	if (pg_h2d(ctx, st, u.chunks.back() + u.used.back(), buf, n) != PG_OK) return false;
+	u.used.back() += n;
+	room -= n;
+	count(&g_stats.h2d, n);
 	return true;
+}
+
+// Reads the child's pages into two pinned buffers in turn; a full buffer is
+// sent to the thread's device chunks on its own stream while the next one
+// fills. Chunks grow from 16 MB, doubling up to 512 MB.
+bool InputSide::stage(Operator* child, unsigned short tid)
+{
+	pg_ctx* ctx = shared_context();
+	Staged& u = staged_[tid];
+	pg_stream st = 0;
+	if (pg_stream_create(ctx, &st) != PG_OK) return false;
+	char* pin[2] = { stage_take(ctx), stage_take(ctx) };
+	bool ok = pin[0] && pin[1];
+	int cur = 0;
+	unsigned long long fill = 0, room = 0, next_chunk = FIRST_CHUNK;
+	bool in_flight[2] = { false, false };
+	while (ok) {
+		Operator::GetNextResultT r = child->getNext(tid);
+		if (r.first == Operator::Error) { ok = false; break; }
+		Operator::Page* p = r.second;
+		const unsigned long long used = p ? p->getUsedSpace() : 0;
+		const char* src = used ? (const char*) p->getTupleOffset(0) : 0;
+		unsigned long long left = used;
+		while (ok && left) {
+			const unsigned long long n = std::min(left, STAGE_BYTES - fill);
+			memcpy(pin[cur] + fill, src, (size_t) n);
+			fill += n; src += n; left -= n;
+			if (fill == STAGE_BYTES) {
+				ok = flush(ctx, st, u, pin[cur], fill, room, next_chunk);
+				in_flight[cur] = true;
+				cur ^= 1;
+				fill = 0;
+				// The other buffer's copy must be done before it refills.
+				if (ok && in_flight[cur]) { ok = pg_sync(ctx, st) == PG_OK; in_flight[0] = in_flight[1] = false; }
+			}
+		}
+		if (r.first == Operator::Finished) break;
+	}
+	if (ok) ok = flush(ctx, st, u, pin[cur], fill, room, next_chunk);
+	if (pg_sync(ctx, st) != PG_OK) ok = false;
+	stage_give(pin[0]);
+	stage_give(pin[1]);
+	pg_stream_destroy(ctx, st);
+	return ok;
 }
 
 int InputSide::gather(pg_ctx* ctx, pg_stream st, const std::vector<int>& members, unsigned width,
 		const char** data, unsigned long long* rows, void** tmp)
 {
 	*data = 0; *rows = 0; *tmp = 0;
-	unsigned long long n = 0;
-	bool adjacent = true;
-	const char* first = 0;
-	const char* end = 0;
+	// Pieces of the input in order: device spans of a GPU child, staged
+	// chunks, or (without staging) drained host bytes.
+	std::vector<const char*> at;
+	std::vector<unsigned long long> bytes;
+	bool host = false;
 	for (size_t i = 0; i < members.size(); ++i) {
 		const int t = members[i];
-		const unsigned long long r = dev_ ? spans_[t].rows : (width ? host_[t].size() / width : 0);
-		if (!r) continue;
 		if (dev_) {
-			if (!first) first = spans_[t].data;
-			else if (spans_[t].data != end) adjacent = false;
-			end = spans_[t].data + r * width;
+			at.push_back(spans_[t].data); bytes.push_back(spans_[t].rows * width);
+		} else if (!host_[t].empty()) {
+			host = true;
+			at.push_back(&host_[t][0]); bytes.push_back(host_[t].size());
+		} else {
+			for (size_t c = 0; c < staged_[t].chunks.size(); ++c) {
+				at.push_back(staged_[t].chunks[c]); bytes.push_back(staged_[t].used[c]);
+			}
 		}
-		n += r;
 	}
-	*rows = n;
-	if (!n) return PG_OK;
-	// In place when the shares are one run that starts 16-byte aligned (the
+	unsigned long long total = 0;
+	bool run = !host;
+	const char* first = 0;
+	const char* end = 0;
+	for (size_t i = 0; i < at.size(); ++i) {
+		if (!bytes[i]) continue;
+		if (!first) first = at[i];
+		else if (at[i] != end) run = false;
+		end = at[i] + bytes[i];
+		total += bytes[i];
+	}
+	*rows = width ? total / width : 0;
+	if (!total) return PG_OK;
+	// In place when the pieces are one run that starts 16-byte aligned (the
 	// alignment every operator's loads assume); copied otherwise.
-	if (dev_ && adjacent && ((unsigned long long) (size_t) first & 15) == 0) {
+	if (run && ((unsigned long long) (size_t) first & 15) == 0) {
 		*data = first;
-		count(&g_stats.in_place, 1);
+		if (dev_) count(&g_stats.in_place, 1);
 		return PG_OK;
 	}
-	int rc = pg_buffer_alloc(ctx, n * width, tmp);
-	if (rc) return rc;
-	char* at = (char*) *tmp;
-	for (size_t i = 0; i < members.size() && !rc; ++i) {
-		const int t = members[i];
-		if (dev_) {
-			const unsigned long long b = spans_[t].rows * width;
-			if (b) rc = pg_d2d(ctx, st, at, spans_[t].data, b);
-			count(&g_stats.d2d, b);
-			at += b;
+	int rc = pg_buffer_alloc_async(ctx, st, total, tmp);
+	char* o = (char*) *tmp;
+	for (size_t i = 0; i < at.size() && !rc; ++i) {
+		if (!bytes[i]) continue;
+		if (host) {
+			rc = pg_h2d(ctx, st, o, at[i], bytes[i]);
+			count(&g_stats.h2d, bytes[i]);
 		} else {
-			const unsigned long long b = host_[t].size();
-			if (b) rc = pg_h2d(ctx, st, at, &host_[t][0], b);
-			count(&g_stats.h2d, b);
-			at += b;
+			rc = pg_d2d(ctx, st, o, at[i], bytes[i]);
+			if (dev_) count(&g_stats.d2d, bytes[i]);
 		}
+		o += bytes[i];
 	}
 	*data = (const char*) *tmp;
 	return rc;
 }
 
-void InputSide::concat(const std::vector<int>& members, std::vector<char>& all)
-{
-	for (size_t i = 0; i < members.size(); ++i) {
-		all.insert(all.end(), host_[members[i]].begin(), host_[members[i]].end());
-		release(members[i]);
-	}
-}
-
-void InputSide::release(int tid)
+void InputSide::release(int tid, pg_stream st)
 {
 	std::vector<char>().swap(host_[tid]);
+	Staged& u = staged_[tid];
+	if (!u.chunks.empty()) {
+		pg_ctx* ctx = shared_context();
+		for (size_t c = 0; c < u.chunks.size(); ++c) pg_buffer_free_async(ctx, st, u.chunks[c]);
+	}
+	u.chunks.clear();
+	u.used.clear();
+}
+
+void InputSide::clear()
+{
+	for (size_t t = 0; t < staged_.size(); ++t) release((int) t);
+	host_.clear();
+	staged_.clear();
+	spans_.clear();
 }
 
 // ---------------------------------------------------------------------------
@@ -369,45 +487,30 @@ void GpuJoinBase::threadInit(unsigned short threadid)
 	if (groups_.group_of.at(threadid) < 0) throw std::invalid_argument("thread not in any thread group");
 }
 
-pg_rel GpuJoinBase::side_rel(Operator* child, unsigned attr, const void* data, unsigned long long bytes)
+pg_rel GpuJoinBase::side_rel(Operator* child, unsigned attr, const void* data, unsigned long long rows)
 {
 	Schema& s = child->getOutSchema();
 	pg_rel r;
 	r.width = s.getTupleSize();
-	r.n = r.width ? bytes / r.width : 0;
-	r.data = r.n ? data : 0;
+	r.n = rows;
+	r.data = rows ? data : 0;
 	r.key_off = col_offset(s, attr);
 	r.key_bytes = key_bytes(s, attr);
 	return r;
 }
 
-// One launch over the group's inputs: host buffers in and out when neither
-// side nor the parent is a GPU operator and the join has a host path, device
-// memory otherwise.
+// One launch over the group's inputs (staged uploads or a GPU child's device
+// output); the rows are downloaded into the group's pages, or stay on the
+// device for a GPU parent.
 int GpuJoinBase::run_group(int g)
 {
 	const std::vector<int>& mem = groups_.members[g];
 	const unsigned ow = schema.getTupleSize();
-	int rc;
-	if (host_path() && !build_.on_device() && !probe_.on_device() && !on_device_) {
-		std::vector<char> R, S;
-		build_.concat(mem, R);
-		probe_.concat(mem, S);
-		const pg_rel r = side_rel(buildOp, buildkey_, R.empty() ? 0 : &R[0], R.size());
-		const pg_rel s = side_rel(probeOp, probekey_, S.empty() ? 0 : &S[0], S.size());
-		unsigned long long rows = 0;
-		rc = run_host(r, s, output_.buffer(g), &rows);
-		if (rc == PG_OK) {
-			count(&g_stats.h2d, R.size() + S.size());
-			count(&g_stats.d2h, rows * ow);
-		}
-		output_.set_rows(g, rc == PG_OK ? rows : 0);
-		return rc;
-	}
 	pg_ctx* ctx = shared_context();
 	if (!ctx) return PG_ERR_CUDA;
 	pg_stream st = 0;
-	if ((rc = pg_stream_create(ctx, &st))) return rc;
+	int rc = pg_stream_create(ctx, &st);
+	if (rc) return rc;
 	const char *dR = 0, *dS = 0;
 	unsigned long long nR = 0, nS = 0;
 	void *tR = 0, *tS = 0, *dO = 0;
@@ -415,8 +518,8 @@ int GpuJoinBase::run_group(int g)
 	const unsigned wR = buildOp->getOutSchema().getTupleSize(), wS = probeOp->getOutSchema().getTupleSize();
 	if (!(rc = build_.gather(ctx, st, mem, wR, &dR, &nR, &tR)) &&
 			!(rc = probe_.gather(ctx, st, mem, wS, &dS, &nS, &tS))) {
-		const pg_rel r = side_rel(buildOp, buildkey_, dR, nR * wR);
-		const pg_rel s = side_rel(probeOp, probekey_, dS, nS * wS);
+		const pg_rel r = side_rel(buildOp, buildkey_, dR, nR);
+		const pg_rel s = side_rel(probeOp, probekey_, dS, nS);
 		rc = run_device(ctx, st, r, s, &dO, &rows);
 	}
 	if (!rc && !on_device_) {
@@ -425,10 +528,10 @@ int GpuJoinBase::run_group(int g)
 		if (rows) rc = pg_d2h(ctx, st, &out[0], dO, rows * ow);
 		if (!rc) count(&g_stats.d2h, rows * ow);
 	}
+	for (size_t i = 0; i < mem.size(); ++i) { build_.release(mem[i], st); probe_.release(mem[i], st); }
+	if (tR) pg_buffer_free_async(ctx, st, tR);
+	if (tS) pg_buffer_free_async(ctx, st, tS);
 	if (!rc) rc = pg_sync(ctx, st);
-	for (size_t i = 0; i < mem.size(); ++i) { build_.release(mem[i]); probe_.release(mem[i]); }
-	if (tR) pg_buffer_free(ctx, tR);
-	if (tS) pg_buffer_free(ctx, tS);
 	if (!rc && on_device_) {
 		output_.set_device(g, (const char*) dO, rows);
 		if (dO) output_.own_device(dO);
@@ -474,8 +577,7 @@ Operator::ResultCode GpuJoinBase::scanStop(unsigned short tid)
 
 void GpuJoinBase::threadClose(unsigned short tid)
 {
-	build_.release(tid);
-	probe_.release(tid);
+	(void) tid;     // inputs are released by the group's launch
 }
 
 void GpuJoinBase::destroy()
@@ -483,42 +585,6 @@ void GpuJoinBase::destroy()
 	output_.clear();
 	for (size_t g = 0; g < barriers_.size(); ++g) delete barriers_[g];
 	barriers_.clear();
-}
-
-int GpuJoinBase::run_host(const pg_rel&, const pg_rel&, std::vector<char>&, unsigned long long*)
-{
-	return PG_ERR_UNSUPPORTED;
-}
-
-bool GpuJoinBase::host_path() const
-{
-	return false;
-}
-
-bool GpuHashJoinOp::host_path() const
-{
-	return true;
-}
-
-int GpuHashJoinOp::run_host(const pg_rel& R, const pg_rel& S, std::vector<char>& out, unsigned long long* rows)
-{
-	pg_ctx* ctx = shared_context();
-	if (!ctx) return PG_ERR_CUDA;
-	const unsigned ow = schema.getTupleSize();
-	// A PK-FK join yields |S| rows: start there and grow once if asked.
-	unsigned long long cap = std::max<unsigned long long>(S.n, 1);
-	for (int attempt = 0; attempt < 2; ++attempt) {
-		out.resize((size_t) (cap * ow));
-		pg_join_result res;
-		const int rc = pg_hashjoin_host(ctx, &R, &S, &cols_[0], (int) cols_.size(), &out[0], cap,
-				PG_JOIN_MATERIALIZE, -1, &res);
-		if (rc == PG_ERR_OUTPUT_FULL && attempt == 0) { cap = res.n_out; continue; }
-		if (rc != PG_OK) return rc;
-		*rows = res.n_out;
-		out.resize((size_t) (res.n_out * ow));
-		return PG_OK;
-	}
-	return PG_ERR_OUTPUT_FULL;
 }
 
 int GpuHashJoinOp::run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
@@ -653,7 +719,7 @@ int GpuPartitionOp::run_partition()
 		p.key_off = col_offset(schema, sortattr_); p.key_bytes = key_bytes(schema, sortattr_);
 		// The input may be the child's output: sort with scratch of our own.
 		if (tin) scratch = tin;
-		else if (!(rc = pg_buffer_alloc(ctx, n * w, &tin))) scratch = tin;
+		else if (!(rc = pg_buffer_alloc_async(ctx, st, n * w, &tin))) scratch = tin;
 		if (!rc) rc = pg_partition_sort(ctx, st, &p, &offsets_[0], nparts_, scratch);
 	}
 	for (unsigned t = 0; t < nparts_ && !rc; ++t) {
@@ -668,12 +734,12 @@ int GpuPartitionOp::run_partition()
 		count(&g_stats.d2h, rows * w);
 		served_.set_rows((int) t, rows);
 	}
+	for (unsigned t = 0; t < nparts_; ++t) in_.release((int) t, st);
+	if (tin) pg_buffer_free_async(ctx, st, tin);
 	if (!rc) rc = pg_sync(ctx, st);
-	for (unsigned t = 0; t < nparts_; ++t) in_.release((int) t);
 	if (!rc && on_device_) { served_.own_device(dout); dout = 0; }
 	if (doffs) pg_buffer_free(ctx, doffs);
 	if (dout) pg_buffer_free(ctx, dout);
-	if (tin) pg_buffer_free(ctx, tin);
 	pg_stream_destroy(ctx, st);
 	return rc;
 }
@@ -796,10 +862,10 @@ int GpuAggregateOp::aggregate(const std::vector<int>& members, int g)
 			if (ng) rc = pg_d2h(ctx, st, &out[0], dout, ng * ow);
 			count(&g_stats.d2h, ng * ow);
 		}
-		if (!rc) rc = pg_sync(ctx, st);
 	}
-	for (size_t i = 0; i < members.size(); ++i) in_.release(members[i]);
-	if (tin) pg_buffer_free(ctx, tin);
+	for (size_t i = 0; i < members.size(); ++i) in_.release(members[i], st);
+	if (tin) pg_buffer_free_async(ctx, st, tin);
+	if (!rc) rc = pg_sync(ctx, st);
 	if (!rc && on_device_) {
 		output_.set_device(g, (const char*) dout, ng);
 		output_.own_device(dout);

@@ -148,32 +148,48 @@ private:
 };
 
 // Appends every tuple the child serves to `sink` until it reports Finished.
-// Returns false when the child reports Error.
+// Returns false when the child reports Error. (Inputs go through InputSide,
+// which stages them for the device; this is its path without a GPU context.)
 bool drain(Operator* child, unsigned short tid, std::vector<char>& sink);
 
-// One input of a GPU operator: the child's pages drained into host memory,
-// or, when the child is a GPU operator keeping its output on the device,
-// each thread's device span.
+// One input of a GPU operator. A host child's pages are staged on their way
+// in: each thread copies the pages it reads into pinned buffers and sends
+// every full buffer to device memory at once, so the upload overlaps the scan
+// (operators/parallelscan.cpp:176-190 hands pages to its parent the same way,
+// one page at a time). A GPU child keeping its output on the device gives
+// each thread's device span instead.
 class InputSide {
 public:
 	InputSide() : dev_(0) { }
+	~InputSide() { clear(); }
 	// From init: asks a GPU child to keep its output on the device.
 	void setup(Operator* child);
 	bool on_device() const { return dev_ != 0; }
-	// After child->scanStart(tid): drains the pages or takes the span.
+	// After child->scanStart(tid): stages the pages or takes the span; false
+	// when the child reported Error or the upload failed.
 	bool fetch(Operator* child, unsigned short tid);
 	// The rows of `members`, in order, as one device array of `width`-byte
-	// tuples on stream `st`. *data points into the child's output when the
-	// shares are adjacent there, else into *tmp (device memory the caller
-	// frees after the stream's work).
+	// tuples on stream `st`. *data points into the child's output or the
+	// staged upload when that is one aligned run, else into *tmp (device
+	// memory the caller frees after the stream's work).
 	int gather(pg_ctx* ctx, pg_stream st, const std::vector<int>& members, unsigned width,
 			const char** data, unsigned long long* rows, void** tmp);
-	// Host bytes of `members`, concatenated (host path).
-	void concat(const std::vector<int>& members, std::vector<char>& all);
-	void release(int tid);
+	// Frees thread `tid`'s staged input (after the work on `st` that reads it).
+	void release(int tid, pg_stream st = 0);
+	void clear();
 private:
+	InputSide(const InputSide&);
+	InputSide& operator=(const InputSide&);
+	struct Staged {
+		std::vector<char*> chunks;                // device memory
+		std::vector<unsigned long long> used;     // bytes of each chunk
+	};
+	bool stage(Operator* child, unsigned short tid);
+	static bool flush(pg_ctx* ctx, pg_stream st, Staged& u, const char* buf, unsigned long long n,
+			unsigned long long& room, unsigned long long& next_chunk);
 	DeviceProducer* dev_;
-	std::vector<std::vector<char> > host_;
+	std::vector<std::vector<char> > host_;        // pages read without a GPU context
+	std::vector<Staged> staged_;
 	std::vector<DeviceSpan> spans_;
 };
 
@@ -189,11 +205,6 @@ public:
 	virtual void destroy();
 	virtual DeviceSpan device_share(unsigned short threadid) { return output_.share(threadid); }
 protected:
-	// Whether run_host exists: it takes the group's host inputs and fills host
-	// rows (copies overlapped with the work); used when no input and not the
-	// output are on the device.
-	virtual bool host_path() const;
-	virtual int run_host(const pg_rel& R, const pg_rel& S, std::vector<char>& out, unsigned long long* rows);
 	// Joins device inputs on `st` into device rows *out (freed by the caller).
 	virtual int run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
 			unsigned long long* rows) = 0;
@@ -206,7 +217,7 @@ private:
 	InputSide build_, probe_;
 	std::vector<int> group_rc_;
 	GroupedOutput output_;
-	pg_rel side_rel(Operator* child, unsigned attr, const void* data, unsigned long long bytes);
+	pg_rel side_rel(Operator* child, unsigned attr, const void* data, unsigned long long rows);
 };
 
 // "gpuhashjoin": HashJoinOp's keys (operators/join.cpp:184-366): projection,
@@ -214,8 +225,6 @@ private:
 // have no effect on the result.
 class GpuHashJoinOp : public GpuJoinBase {
 protected:
-	virtual bool host_path() const;
-	virtual int run_host(const pg_rel& R, const pg_rel& S, std::vector<char>& out, unsigned long long* rows);
 	virtual int run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
 			unsigned long long* rows);
 };
