@@ -228,6 +228,42 @@ int pg_hashjoin_agg_noalloc(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 		pg_join_result* res);
 
 /* ---------------------------------------------------------------------- */
+/* Filter and Project: Filter::map and Project::map (operators/filter.cpp:
+ * 37-85, project.cpp:37-104) over MapWrapper's per-thread page loop
+ * (mapwrapper.cpp:38-138), one launch per relation. A predicate compares one
+ * column with a constant of the column's own type, as Filter's Comparator
+ * does (comparator.cpp:43-433, rawcompfns.cpp): int, long and date as signed
+ * integers, dec as double (IEEE: NaN compares unequal), char as strncmp over
+ * the column width. Several predicates form a conjunction (a Filter over a
+ * Filter).                                                                 */
+/* ---------------------------------------------------------------------- */
+enum { PG_PRED_INT = 1, PG_PRED_LONG = 2, PG_PRED_DEC = 3, PG_PRED_CHAR = 4 };
+enum { PG_CMP_EQ = 0, PG_CMP_NE = 1, PG_CMP_LT = 2, PG_CMP_LE = 3, PG_CMP_GT = 4, PG_CMP_GE = 5 };
+#define PG_PRED_MAX 4
+typedef struct {
+	uint32_t type;          /* PG_PRED_* (a date column: PG_PRED_LONG)            */
+	uint32_t op;            /* PG_CMP_*: column <op> value                         */
+	uint32_t off;           /* byte offset of the column, a multiple of 4 (char: any) */
+	uint32_t bytes;         /* 4 (int), 8 (long, dec), 1..128 (char)               */
+	uint8_t value[128];     /* the constant as the column stores it (char: strncpy'd) */
+} pg_pred;
+/* Stable: out = the tuples of `in` satisfying every predicate, in input
+ * order; *n_out = their number. `out` has room for in->n tuples.          */
+int pg_filter(pg_ctx* ctx, pg_stream stream, const pg_rel* in, const pg_pred* preds, int npred,
+		void* out, uint64_t* n_out);
+/* out[i] = the columns cols[0..ncols) of in[i] (byte offset `off`, width
+ * `bytes`, multiples of 4; `side` ignored), packed in order.               */
+int pg_project(pg_ctx* ctx, pg_stream stream, const pg_rel* in, const pg_col* cols, int ncols, void* out);
+/* pg_hashjoin_probe over the probe tuples that satisfy `preds`: the Filter
+ * under a join's probe side run as the probe's prologue. For 16-byte probe
+ * tuples of a dense table and predicates on int/long/dec columns the probe
+ * kernel evaluates them before its table lookups (no filtered copy of S);
+ * otherwise S is filtered first.                                          */
+int pg_hashjoin_probe_where(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht, const pg_rel* S,
+		const pg_pred* preds, int npred, const pg_col* proj, int nproj,
+		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res);
+
+/* ---------------------------------------------------------------------- */
 /* Group-by: GenericAggregate::remember + AggregateSum / AggregateCount fold
  * (operators/genericaggregate.cpp:240-487, aggregatesum.cpp:53-107,
  * aggregatecount.cpp:37-52). Key: in->key_bytes 4 or 8, or 0 for no GROUP BY

@@ -71,8 +71,60 @@ def lib():
         L.or_mergejoin.argtypes = [vp, u64, u32, u32, u32, vp, u64, u32, u32, u32,
                                    P(Col), ci, vp, u64, ci, ci, P(JoinResult)]
         L.or_mergejoin.restype = ci
+        L.or_filter.argtypes = [vp, u64, u32, P(Pred), ci, vp]; L.or_filter.restype = u64
+        L.or_project.argtypes = [vp, u64, u32, P(Col), ci, vp]; L.or_project.restype = None
         _LIB = L
     return _LIB
+
+
+class Pred(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_uint32), ("op", ctypes.c_uint32), ("off", ctypes.c_uint32),
+                ("bytes", ctypes.c_uint32), ("value", ctypes.c_uint8 * 128)]
+
+
+PRED_TYPE = {"int": 1, "long": 2, "date": 2, "dec": 3, "char": 4}
+PRED_OP = {"=": 0, "==": 0, "<>": 1, "!=": 1, "<": 2, "<=": 3, ">": 4, ">=": 5}
+
+
+def preds(spec):
+    """spec: [(type, op, byte offset, value[, char width])] -> (Pred array, n)."""
+    arr = (Pred * max(1, len(spec)))()
+    for i, sp in enumerate(spec):
+        t, op, off, v = sp[:4]
+        p = arr[i]
+        p.type, p.op, p.off = PRED_TYPE[t], PRED_OP[op], off
+        if t == "int":
+            b = np.int32(v).tobytes()
+        elif t in ("long", "date"):
+            b = np.int64(v).tobytes()
+        elif t == "dec":
+            b = np.float64(v).tobytes()
+        else:
+            width = sp[4]
+            raw = v if isinstance(v, bytes) else str(v).encode()
+            b = (raw[:width] + b"\0" * width)[:width]       # strncpy into the column
+        p.bytes = len(b)
+        ctypes.memmove(p.value, b, min(len(b), 128))
+    return arr, len(spec)
+
+
+def filter(rows, spec):
+    """Filter (filter.cpp:76-85) with the conjunction of `spec` predicates."""
+    a, p, n, w = _rows(rows)
+    pr, npr = preds(spec)
+    out = np.empty_like(a)
+    m = lib().or_filter(p, n, w, pr, npr, out.ctypes.data)
+    return out[:m]
+
+
+def project(rows, spec):
+    """Project (project.cpp:93-104): spec = [(byte offset, bytes)]."""
+    a, p, n, w = _rows(rows)
+    c = (Col * len(spec))(*[Col(0, o, b) for o, b in spec])
+    ow = sum(b for _, b in spec)
+    out = np.empty(n * ow, dtype=np.uint8)
+    lib().or_project(p, n, w, c, len(spec), out.ctypes.data)
+    return out.reshape(n, ow)
 
 
 def hashcfg(fn, buckets=1, min=0, max=0, skipbits=0, offset=0):

@@ -790,3 +790,83 @@ int or_mergejoin(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32
 	res->n_out = total; res->sum = sum;
 	return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Filter and Project: filter.cpp:37-85, project.cpp:37-104            */
+/* ------------------------------------------------------------------ */
+
+/* The raw comparison functions of rawcompfns.cpp for equal types: the left
+ * operand is the column, the right one Filter's parsed constant
+ * (Comparator::eval, comparator.h:72-76). */
+static int or_cmp_sign_ok(uint32_t op, int lt, int eq, int gt)
+{
+	switch (op) {
+	case OR_CMP_EQ: return eq;
+	case OR_CMP_NE: return !eq;
+	case OR_CMP_LT: return lt;
+	case OR_CMP_LE: return lt || eq;
+	case OR_CMP_GT: return gt;
+	default: return gt || eq;
+	}
+}
+
+static int or_pred_one(const or_pred* p, const char* t)
+{
+	const char* c = t + p->off;
+	if (p->type == OR_PRED_INT) {
+		int32_t a, b;
+		memcpy(&a, c, 4); memcpy(&b, p->value, 4);
+		return or_cmp_sign_ok(p->op, a < b, a == b, a > b);
+	}
+	if (p->type == OR_PRED_LONG) {
+		int64_t a, b;
+		memcpy(&a, c, 8); memcpy(&b, p->value, 8);
+		return or_cmp_sign_ok(p->op, a < b, a == b, a > b);
+	}
+	if (p->type == OR_PRED_DEC) {
+		/* DoubleDouble* (rawcompfns.cpp:294-327): C comparisons, so a NaN
+		 * is unequal to everything and only != holds. */
+		double a, b;
+		memcpy(&a, c, 8); memcpy(&b, p->value, 8);
+		switch (p->op) {
+		case OR_CMP_EQ: return a == b;
+		case OR_CMP_NE: return a != b;
+		case OR_CMP_LT: return a < b;
+		case OR_CMP_LE: return a <= b;
+		case OR_CMP_GT: return a > b;
+		default: return a >= b;
+		}
+	}
+	/* CharChar* (rawcompfns.cpp:329-357): strncmp over the column width
+	 * (Comparator::init, comparator.cpp:368). */
+	int d = strncmp(c, (const char*) p->value, p->bytes);
+	return or_cmp_sign_ok(p->op, d < 0, d == 0, d > 0);
+}
+
+/* Filter::map over every tuple (filter.cpp:76-85): a tuple is copied out
+ * when the comparator holds; Filter over Filter is the conjunction. */
+uint64_t or_filter(const void* in, uint64_t n, uint32_t w, const or_pred* preds, int npred, void* out)
+{
+	const char* src = (const char*) in;
+	char* dst = (char*) out;
+	uint64_t m = 0;
+	for (uint64_t i = 0; i < n; ++i) {
+		const char* t = src + i * w;
+		int ok = 1;
+		for (int k = 0; k < npred && ok; ++k) ok = or_pred_one(&preds[k], t);
+		if (ok) { memcpy(dst + m * w, t, w); ++m; }
+	}
+	return m;
+}
+
+/* Project::map (project.cpp:93-104): the listed columns written in order. */
+void or_project(const void* in, uint64_t n, uint32_t w, const or_col* cols, int ncols, void* out)
+{
+	const char* src = (const char*) in;
+	char* dst = (char*) out;
+	for (uint64_t i = 0; i < n; ++i)
+		for (int c = 0; c < ncols; ++c) {
+			memcpy(dst, src + i * w + cols[c].off, cols[c].bytes);
+			dst += cols[c].bytes;
+		}
+}

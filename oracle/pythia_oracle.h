@@ -89,6 +89,20 @@ int or_mergejoin(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32
 		const or_col* proj, int nproj, void* out, uint64_t out_cap,
 		int sum_col, int threads, or_join_result* res);
 
+/* Filter / Project (filter.cpp:37-85, project.cpp:37-104): column types and
+ * comparisons of Comparator (comparator.h:43-83). A date column compares as
+ * a long (CtDate is a long long, comparator.cpp:370-403). */
+enum { OR_PRED_INT = 1, OR_PRED_LONG = 2, OR_PRED_DEC = 3, OR_PRED_CHAR = 4 };
+enum { OR_CMP_EQ = 0, OR_CMP_NE = 1, OR_CMP_LT = 2, OR_CMP_LE = 3, OR_CMP_GT = 4, OR_CMP_GE = 5 };
+typedef struct {
+	uint32_t type, op, off, bytes;
+	uint8_t value[128];
+} or_pred;
+/* Tuples satisfying every predicate, in input order; returns their number. */
+uint64_t or_filter(const void* in, uint64_t n, uint32_t w, const or_pred* preds, int npred, void* out);
+/* out[i] = columns (off, bytes) of in[i], packed in order. */
+void or_project(const void* in, uint64_t n, uint32_t w, const or_col* cols, int ncols, void* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -113,10 +113,16 @@ static void addschema(Setting& parent, const string& schema)
 	for (size_t i = 0; i < cols.size(); ++i) s.add(Setting::TypeString) = cols[i];
 }
 
+// Tuple width of a schema list: int 4, char(N) N + 1 (Schema::create,
+// schema.cpp:221-259), everything else 8.
 static unsigned int schemawidth(const string& schema)
 {
 	vector<string> cols = split(schema); unsigned int w = 0;
-	for (size_t i = 0; i < cols.size(); ++i) w += (cols[i] == "int") ? 4 : 8;
+	for (size_t i = 0; i < cols.size(); ++i) {
+		if (cols[i] == "int") w += 4;
+		else if (cols[i].compare(0, 5, "char(") == 0) w += atoi(cols[i].c_str() + 5) + 1;
+		else w += 8;
+	}
 	return w;
 }
 
@@ -380,6 +386,47 @@ int main(int argc, char** argv)
 		for (unsigned long long i = 0; i < intuples; ++i) o[i] = th.hash(R.data + i * R.tuplesize);
 		o[intuples] = th.buckets();
 		th.destroy();
+	}
+	else if (mode == "filter" || mode == "project") {
+		// Filter (filter.cpp:37-85), or a chain of them (field2/op2/value2,
+		// ...), or Project (project.cpp:37-104) over one scanning thread, so
+		// the output keeps the input order. Schema columns are separated by
+		// ';' here (a date format may hold commas).
+		string schema = arg("schema", "long;long");
+		for (size_t k = 0; k < schema.size(); ++k) if (schema[k] == ';') schema[k] = ',';
+		Relation R = loadrel(arg("in"), schemawidth(schema));
+		intuples = R.bytes / R.tuplesize;
+		Setting& root = cfg.getRoot();
+		Setting& s = root.add("scan", Setting::TypeGroup); addschema(s, schema);
+		MemScan sc; sc.rel = R; sc.threads = 1;
+		sc.init(cfg, s);
+		Filter f[4]; Project pj;
+		Operator* top = &sc;
+		if (mode == "filter") {
+			for (int k = 0; k < 4; ++k) {
+				string sfx = k ? string(1, (char) ('1' + k)) : string();
+				if (!args.count("field" + sfx)) break;
+				Setting& fn = root.add("filter" + sfx, Setting::TypeGroup);
+				fn.add("field", Setting::TypeInt) = (int) argl(("field" + sfx).c_str());
+				fn.add("op", Setting::TypeString) = arg(("op" + sfx).c_str());
+				fn.add("value", Setting::TypeString) = arg(("value" + sfx).c_str());
+				f[k].nextOp = top;
+				f[k].init(cfg, fn);
+				top = &f[k];
+			}
+		} else {
+			Setting& pn = root.add("project", Setting::TypeGroup);
+			Setting& pl = pn.add("projection", Setting::TypeArray);
+			vector<string> cols = split(arg("projection"));
+			for (size_t k = 0; k < cols.size(); ++k) pl.add(Setting::TypeString) = "$" + cols[k];
+			pj.nextOp = top;
+			pj.init(cfg, pn);
+			top = &pj;
+		}
+		Query q; q.tree = top;
+		out.clear();
+		best = runquery(q, out);
+		q.destroynofree();
 	}
 	else { fprintf(stderr, "unknown mode %s\n", mode.c_str()); return 2; }
 

@@ -19,7 +19,7 @@ BUILD = os.path.join(PKG, "_build")
 GENCODE = "arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["pg_core.cu", "pg_partition.cu", "pg_hashjoin.cu", "pg_groupby.cu",
-              "pg_sort.cu", "pg_mpsm.cu", "pg_batch.cu", "pg_noalloc.cu", "pg_htimage.cu"]
+              "pg_sort.cu", "pg_mpsm.cu", "pg_batch.cu", "pg_noalloc.cu", "pg_htimage.cu", "pg_filter.cu"]
 NVCC_FLAGS = ["-gencode", GENCODE, "-O3", "-lineinfo", "-std=c++17",
               "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-O3",
               "-I" + os.path.join(ROOT, "include")]

@@ -26,6 +26,7 @@
 // aggregatesum.cpp:81-107).
 #include "pg_internal.cuh"
 #include "pg_hashtable.cuh"
+#include "pg_pred.cuh"
 #include <algorithm>
 #include <vector>
 
@@ -844,12 +845,14 @@ __device__ __forceinline__ void hj_st_stream(char* p, uint4 v, uint64_t pol)
 
 // STD: the output row is (probe words 2-3, value) = the (P$1, B$1) projection
 // of 16-byte tuples, picked without the general word selector.
-template <bool MATERIALIZE, int MODE, bool PF, bool STD = false>
+// PRED: probe tuples failing the predicates `pr` skip their lookup (a Filter
+// on the probe side run as the probe's prologue).
+template <bool MATERIALIZE, int MODE, bool PF, bool STD = false, bool PRED = false>
 __global__ void __launch_bounds__(PW_WARPS * 32, PF ? 4 : 5)
 k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb,
 		uint32_t wsel, uint32_t sum_w0, uint32_t sum_words, char* __restrict__ out,
 		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg,
-		int sum_col, uint64_t dlo, uint64_t dhi, int run)
+		int sum_col, uint64_t dlo, uint64_t dhi, int run, const PgPred16 pr = PgPred16())
 {
 	static_assert(MODE == 1 || MODE == 2, "dense tables only");
 	constexpr int ITEMS = PW_CHUNK / 32;
@@ -890,7 +893,7 @@ k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const Hj
 			const uint4 t = cur[j];
 			const int64_t key = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
 			const unsigned long long d = (unsigned long long) key - (unsigned long long) tb.dmin;
-			if (p < rows && d >= dlo && d < dhi) {
+			if (p < rows && d >= dlo && d < dhi && (!PRED || pg_pred16(pr, t))) {
 				if (MODE == 2) {
 					asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;"
 							: "=r"(e32[j]) : "l"(tb.dense32 + d), "l"(keep));
@@ -949,8 +952,9 @@ k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const Hj
 // flight and the tuples of chunk c + 2W are loading, so lookup latency and
 // stream latency both overlap with the stores of another chunk.
 // ---------------------------------------------------------------------------
+template <bool PRED>
 __device__ __forceinline__ void hj_lookup4(const HjProbeTable& tb, const uint4 (&t)[4], uint32_t rows, int lane,
-		uint32_t koff, uint64_t keep, uint32_t (&e)[4])
+		uint32_t koff, uint64_t keep, uint32_t (&e)[4], const PgPred16& pr)
 {
 	#pragma unroll
 	for (int j = 0; j < 4; ++j) {
@@ -958,14 +962,15 @@ __device__ __forceinline__ void hj_lookup4(const HjProbeTable& tb, const uint4 (
 			: (int64_t) (((uint64_t) t[j].w << 32) | t[j].z);
 		const unsigned long long d = (unsigned long long) key - (unsigned long long) tb.dmin;
 		e[j] = 0xFFFFFFFFu;
-		if ((uint32_t) (j * 32 + lane) < rows && d < tb.drange)
+		if ((uint32_t) (j * 32 + lane) < rows && d < tb.drange && (!PRED || pg_pred16(pr, t[j])))
 			asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(e[j]) : "l"(tb.dense32 + d), "l"(keep));
 	}
 }
 
+template <bool PRED>
 __global__ void __launch_bounds__(PW_WARPS * 32, 3)
 k_probe16_deep(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb, char* __restrict__ out,
-		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg)
+		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg, const PgPred16 pr)
 {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
@@ -988,10 +993,10 @@ k_probe16_deep(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 	uint32_t ecur[4], enxt[4];
 	load(first, cur);
 	load(first + W, nxt);
-	hj_lookup4(tb, cur, rows_of(first), lane, koff, keep, ecur);
+	hj_lookup4<PRED>(tb, cur, rows_of(first), lane, koff, keep, ecur, pr);
 	for (uint64_t c = first; c < nchunks; c += W) {
 		const uint64_t c1 = c + W, c2 = c + 2 * W;
-		if (c1 < nchunks) hj_lookup4(tb, nxt, rows_of(c1), lane, koff, keep, enxt);
+		if (c1 < nchunks) hj_lookup4<PRED>(tb, nxt, rows_of(c1), lane, koff, keep, enxt, pr);
 		load(c2, nx2);
 		const uint32_t rows = rows_of(c);
 		uint32_t rank = 0;
@@ -1383,7 +1388,7 @@ static int hj_make_cols(pg_ctx* ctx, const pg_hashtable* ht, const pg_col* proj,
 static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht, const char* S,
 		uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes, const HjCols& pc, char* out,
 		uint64_t cap, unsigned long long* acc, bool materialize, int sum_col,
-		uint64_t* counts = nullptr, bool* positional = nullptr)
+		uint64_t* counts = nullptr, bool* positional = nullptr, const PgPred16* pred = nullptr)
 {
 	if (positional) *positional = false;
 	const uint64_t ntiles = pg_div_up(n, HJ_TILE);
@@ -1395,6 +1400,8 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 	const int mode = ht->dense ? (ht->dense32 ? 2 : 1) : 0;
 	const bool fast16 = W == 16 && (koff == 0 || koff == 8) && kbytes == 8 && pc.ow_words == 4 &&
 		(reinterpret_cast<uintptr_t>(S) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+	if (pred && !fast16)
+		return pg_fail(ctx, PG_ERR_UNSUPPORTED, "join probe: predicates need 16-byte probe tuples and output rows");
 	if (fast16) {
 		const int smem = 3 * HJT_TILE * 16;
 		uint32_t wsel = 0, o = 0, sum_w0 = 0, sum_words = 0;
@@ -1403,7 +1410,10 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 			for (int q = 0; q < pc.words[c]; ++q, ++o)
 				wsel |= (pc.side[c] ? (pc.src[c] + q) : (4u + pc.src[c] + q)) << (4 * o);
 		}
-		const bool tiled = ctx->tune[PG_TUNE_PROBE_VARIANT] == 2;
+		// Predicates run in the register-loading dense kernels only.
+		if (pred && (mode == 0 || (materialize && !(counts && cap >= n))))
+			return pg_fail(ctx, PG_ERR_UNSUPPORTED, "join probe: predicates need a dense table and room for every probe row");
+		const bool tiled = !pred && ctx->tune[PG_TUNE_PROBE_VARIANT] == 2;
 		if (!materialize || (counts && cap >= n && !tiled)) {
 			// Lookups in flight per lane: 8 for dense tables when asked, else 4.
 			const int items = (mode != 0 && ctx->tune[PG_TUNE_PROBE_ITEMS] == 8) ? 8 : 4;
@@ -1421,10 +1431,10 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 			// larger than L2 keeps next to the streams (knob: 1 one pass,
 			// 2 two passes, 0 by table size).
 			const uint64_t tbytes = mode == 2 ? ht->drange * 4 : ht->drange * 8;
-			const int64_t pk = ctx->tune[PG_TUNE_PROBE_PASSES];
+			const int64_t pk = pred ? 1 : ctx->tune[PG_TUNE_PROBE_PASSES];
 			// Dense tables take the register-loading probe unless the knob asks
 			// for the staged one (1) or the non-prefetching one (4).
-			const int64_t var = ctx->tune[PG_TUNE_PROBE_VARIANT];
+			const int64_t var = pred ? 0 : ctx->tune[PG_TUNE_PROBE_VARIANT];
 			const bool direct = mode != 0 && (var == 0 || var == 3 || var == 4 || var == 5);
 			const int passes = mode == 0 || pk == 1 ? 1
 				: (pk == 2 || (!direct && tbytes > HJ_TWO_PASS_MIN_BYTES && tbytes <= HJ_TWO_PASS_MAX_BYTES)) ? 2 : 1;
@@ -1448,10 +1458,26 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 					// deeper pipeline by default (72 CTAs per SM, 3 resident:
 					// measured best on the 16M x 256M join); variant 3 selects
 					// the one-chunk-prefetch kernel.
-					if (materialize && mode == 2 && (var == 0 || var == 5) && wsel == 0x5432u && passes == 1) {
-						const int g5 = (int) std::min<uint64_t>(wchunks, (uint64_t) ctx->sm_count *
-								(ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] > 0 ? ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] : 72));
-						k_probe16_deep<<<g5, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, out, counts, acc);
+					const int g5 = (int) std::min<uint64_t>(wchunks, (uint64_t) ctx->sm_count *
+							(ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] > 0 ? ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] : 72));
+					if (pred) {
+						const PgPred16 pr = *pred;
+						if (materialize && mode == 2 && wsel == 0x5432u)
+							k_probe16_deep<true><<<g5, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, out, counts, acc, pr);
+						else if (materialize && mode == 2)
+							k_probe16_direct<true, 2, true, false, true><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb,
+									wsel, sum_w0, sum_words, out, counts, acc, -1, dlo, dhi, run, pr);
+						else if (materialize)
+							k_probe16_direct<true, 1, true, false, true><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb,
+									wsel, sum_w0, sum_words, out, counts, acc, -1, dlo, dhi, run, pr);
+						else if (mode == 2)
+							k_probe16_direct<false, 2, true, false, true><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb,
+									wsel, sum_w0, sum_words, nullptr, nullptr, acc + 1, sum_col, dlo, dhi, run, pr);
+						else
+							k_probe16_direct<false, 1, true, false, true><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb,
+									wsel, sum_w0, sum_words, nullptr, nullptr, acc + 1, sum_col, dlo, dhi, run, pr);
+					} else if (materialize && mode == 2 && (var == 0 || var == 5) && wsel == 0x5432u && passes == 1) {
+						k_probe16_deep<false><<<g5, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, out, counts, acc, PgPred16());
 					} else if (materialize && mode == 2 && pf && wsel == 0x5432u) {
 						k_probe16_direct<true, 2, true, true><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, wsel, sum_w0,
 								sum_words, out, counts, acc, -1, dlo, dhi, run);
@@ -1532,9 +1558,11 @@ static int hj_compact(pg_ctx* ctx, cudaStream_t s, char* out, uint64_t n, uint64
 	return PG_OK;
 }
 
-extern "C" int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
+// pg_hashjoin_probe; with `pred`, the probe tuples failing it take no part
+// (only for the dense 16-byte layouts the register-loading kernels handle).
+static int hj_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 		const pg_rel* S, const pg_col* proj, int nproj,
-		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res)
+		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res, const PgPred16* pred)
 {
 	if (!ctx || !ht || !res) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe: null argument");
 	int rc;
@@ -1562,7 +1590,7 @@ extern "C" int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht
 			bool positional = false;
 			if ((rc = pg_alloc_async(ctx, s, (void**) &counts, pg_div_up(S->n, PW_CHUNK) * 8))) return rc;
 			if ((rc = hj_launch_unique(ctx, s, ht, Sd, S->n, S->width, S->key_off, S->key_bytes, pc,
-					(char*) out, out_capacity, acc, true, -1, counts, &positional))) return rc;
+					(char*) out, out_capacity, acc, true, -1, counts, &positional, pred))) return rc;
 			PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
 			if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
 			res->n_out = host_acc[0];
@@ -1574,14 +1602,14 @@ extern "C" int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht
 			if (sum_col >= 0 || (flags & PG_JOIN_COUNT)) {
 				// Fold count/sum with a second, non-materialising pass.
 				if ((rc = hj_launch_unique(ctx, s, ht, Sd, S->n, S->width, S->key_off, S->key_bytes, pc,
-						nullptr, 0, acc, false, sum_col))) return rc;
+						nullptr, 0, acc, false, sum_col, nullptr, nullptr, pred))) return rc;
 				PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
 				if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
 				res->sum = (int64_t) host_acc[2];
 			}
 		} else {
 			if ((rc = hj_launch_unique(ctx, s, ht, Sd, S->n, S->width, S->key_off, S->key_bytes, pc,
-					nullptr, 0, acc, false, sum_col))) return rc;
+					nullptr, 0, acc, false, sum_col, nullptr, nullptr, pred))) return rc;
 			PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
 			if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
 			res->n_out = host_acc[1];
@@ -1621,6 +1649,53 @@ extern "C" int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht
 	pg_free_async(ctx, s, tile_counts);
 	pg_free_async(ctx, s, acc);
 	return PG_OK;
+}
+
+extern "C" int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
+		const pg_rel* S, const pg_col* proj, int nproj,
+		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res)
+{
+	return hj_probe(ctx, stream, ht, S, proj, nproj, out, out_capacity, flags, sum_col, res, nullptr);
+}
+
+extern "C" int pg_hashjoin_probe_where(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht, const pg_rel* S,
+		const pg_pred* preds, int npred, const pg_col* proj, int nproj,
+		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res)
+{
+	if (!ctx || !ht || !S || !res) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe_where: null argument");
+	if (npred == 0)
+		return hj_probe(ctx, stream, ht, S, proj, nproj, out, out_capacity, flags, sum_col, res, nullptr);
+	int rc;
+	PgPredSet P;
+	bool has_char = false;
+	if ((rc = pg_pred_prepare(ctx, preds, npred, S->width, &P, &has_char))) return rc;
+	if ((rc = hj_validate_rel(ctx, S, "pg_hashjoin_probe_where"))) return rc;
+	if ((rc = hj_validate_proj(ctx, proj, nproj, ht->wR, S->width))) return rc;
+	HjCols pc;
+	if ((rc = hj_make_cols(ctx, ht, proj, nproj, &pc))) return rc;
+	const bool materialize = (flags & PG_JOIN_MATERIALIZE) != 0;
+	PgPred16 p16;
+	// In the probe kernel when its register-loading dense path runs: 16-byte
+	// tuples and rows, numeric predicates, room for a row per probe tuple.
+	const bool fused = ht->unique && ht->inline_val && ht->dense && S->width == 16 &&
+		(S->key_off == 0 || S->key_off == 8) && S->key_bytes == 8 && pc.ow_words == 4 &&
+		(reinterpret_cast<uintptr_t>(S->data) & 15) == 0 &&
+		(!materialize || (out_capacity >= S->n && (reinterpret_cast<uintptr_t>(out) & 15) == 0)) &&
+		pg_pred_as16(preds, npred, &p16);
+	if (fused)
+		return hj_probe(ctx, stream, ht, S, proj, nproj, out, out_capacity, flags, sum_col, res, &p16);
+	// Otherwise the filtered probe side first, then the plain probe.
+	cudaStream_t s = (cudaStream_t) stream;
+	void* tmp = nullptr;
+	if ((rc = pg_alloc_async(ctx, s, &tmp, std::max<uint64_t>(S->n, 1) * S->width))) return rc;
+	uint64_t m = 0;
+	if ((rc = pg_filter(ctx, stream, S, preds, npred, tmp, &m))) { pg_free_async(ctx, s, tmp); return rc; }
+	pg_rel F = *S;
+	F.data = tmp;
+	F.n = m;
+	rc = hj_probe(ctx, stream, ht, &F, proj, nproj, out, out_capacity, flags, sum_col, res, nullptr);
+	pg_free_async(ctx, s, tmp);
+	return rc;
 }
 
 // ---------------------------------------------------------------------------

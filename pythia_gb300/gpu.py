@@ -66,7 +66,7 @@ SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_st
            "pg_generate_fk", "pg_buffer_alloc_async", "pg_buffer_free_async", "pg_generate_zipf_fk",
            "pg_hashjoin_groupby", "pg_stream_create_urgent", "pg_autotune_batch",
            "pg_hashtable_image_size", "pg_hashtable_serialize", "pg_hashtable_deserialize",
-           "pg_hashtable_save", "pg_hashtable_load"]
+           "pg_hashtable_save", "pg_hashtable_load", "pg_filter", "pg_project", "pg_hashjoin_probe_where"]
 TUNE = {"probe_ctas_per_sm": 0, "probe_variant": 1, "dense": 2, "partition_tile": 3,
         "groupby_smem_groups": 4, "radix_bits": 5, "probe_items": 6, "probe_cache": 7, "probe_passes": 8, "groupby_path": 9}
 
@@ -129,12 +129,49 @@ def lib():
             "pg_hashtable_deserialize": ([vp, vp, vp, u64, P(vp)], ci),
             "pg_hashtable_save": ([vp, vp, vp, ctypes.c_char_p], ci),
             "pg_hashtable_load": ([vp, vp, ctypes.c_char_p, P(vp)], ci),
+            "pg_filter": ([vp, vp, P(Rel), P(Pred), ci, vp, P(u64)], ci),
+            "pg_project": ([vp, vp, P(Rel), P(Col), ci, vp], ci),
+            "pg_hashjoin_probe_where": ([vp, vp, vp, P(Rel), P(Pred), ci, P(Col), ci, vp, u64, ci, ci,
+                                         P(JoinResult)], ci),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
             f.argtypes, f.restype = args, res
         _LIB = L
     return _LIB
+
+
+class Pred(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_uint32), ("op", ctypes.c_uint32), ("off", ctypes.c_uint32),
+                ("bytes", ctypes.c_uint32), ("value", ctypes.c_uint8 * 128)]
+
+
+PRED_TYPE = {"int": 1, "long": 2, "date": 2, "dec": 3, "char": 4}
+PRED_OP = {"=": 0, "==": 0, "<>": 1, "!=": 1, "<": 2, "<=": 3, ">": 4, ">=": 5}
+
+
+def preds(spec):
+    """spec: [(type, op, byte offset, value[, char width])], type int / long /
+    date (a long) / dec / char; value a number, or bytes / str for char
+    (copied as strncpy copies into the column) -> (pg_pred array, n)."""
+    arr = (Pred * max(1, len(spec)))()
+    for i, sp in enumerate(spec):
+        t, op, off, v = sp[:4]
+        p = arr[i]
+        p.type, p.op, p.off = PRED_TYPE[t], PRED_OP[op], off
+        if t == "int":
+            b = np.int32(v).tobytes()
+        elif t in ("long", "date"):
+            b = np.int64(v).tobytes()
+        elif t == "dec":
+            b = np.float64(v).tobytes()
+        else:
+            width = sp[4]
+            raw = v if isinstance(v, bytes) else str(v).encode()
+            b = (raw[:width] + b"\0" * width)[:width]
+        p.bytes = len(b)
+        ctypes.memmove(p.value, b, min(len(b), 128))
+    return arr, len(spec)
 
 
 def hashcfg(fn, buckets=1, min=0, max=0, skipbits=0, offset=0):
@@ -308,6 +345,30 @@ class Context:
                                      groups_hint, o.ptr, cap, ctypes.byref(ng)))
         return self.download(o, ng.value * ow).reshape(-1, ow)
 
+    def filter(self, rows, spec):
+        """pg_filter: the rows satisfying every predicate of `spec`, in order."""
+        a = np.ascontiguousarray(rows)
+        n, w = a.shape[0], row_width(a)
+        d = self.upload(a)
+        o = self.alloc(max(a.nbytes, 16))
+        r = self.rel(d, n, w, 0, 0)
+        pr, npr = preds(spec)
+        m = ctypes.c_uint64()
+        self._check(lib().pg_filter(self.h, self.stream, ctypes.byref(r), pr, npr, o.ptr, ctypes.byref(m)))
+        return self.download(o, m.value * w).view(a.dtype).reshape((-1,) + a.shape[1:])
+
+    def project(self, rows, spec):
+        """pg_project: spec = [(byte offset, bytes)] -> (n, sum of bytes) uint8 rows."""
+        a = np.ascontiguousarray(rows)
+        n, w = a.shape[0], row_width(a)
+        ow = sum(b for _, b in spec)
+        d = self.upload(a)
+        o = self.alloc(max(n * ow, 16))
+        r = self.rel(d, n, w, 0, 0)
+        c = (Col * len(spec))(*[Col(0, off, b) for off, b in spec])
+        self._check(lib().pg_project(self.h, self.stream, ctypes.byref(r), c, len(spec), o.ptr))
+        return self.download(o, n * ow).reshape(n, ow)
+
     def sort(self, rows, key=(0, 8)):
         a = np.ascontiguousarray(rows)
         n, w = a.shape[0], row_width(a)
@@ -356,9 +417,17 @@ class JoinTable:
         except Exception:
             pass
 
-    def probe(self, S, proj=None, pkey=(0, 8), flags=JOIN_MATERIALIZE, sum_col=-1, out_cap=None):
-        """pg_hashjoin_probe with S; returns (rows or None, n_out, sum)."""
+    def probe(self, S, proj=None, pkey=(0, 8), flags=JOIN_MATERIALIZE, sum_col=-1, out_cap=None, where=None):
+        """pg_hashjoin_probe with S (pg_hashjoin_probe_where when `where`, a
+        predicate spec as for preds(), is given); returns (rows or None, n_out, sum)."""
         ctx, L = self.ctx, lib()
+        if where:
+            pr, npr = preds(where)
+
+            def call(*a):
+                return L.pg_hashjoin_probe_where(a[0], a[1], a[2], a[3], pr, npr, *a[4:])
+        else:
+            call = L.pg_hashjoin_probe
         proj = proj if proj is not None else self.proj
         Sa = np.ascontiguousarray(S)
         dS = ctx.upload(Sa)
@@ -367,18 +436,18 @@ class JoinTable:
         ow = sum(b for _, _, b in proj)
         res = JoinResult()
         if not flags & JOIN_MATERIALIZE:
-            ctx._check(L.pg_hashjoin_probe(ctx.h, ctx.stream, self.h, ctypes.byref(rS), c, nc,
-                                           None, 0, flags, sum_col, ctypes.byref(res)))
+            ctx._check(call(ctx.h, ctx.stream, self.h, ctypes.byref(rS), c, nc,
+                            None, 0, flags, sum_col, ctypes.byref(res)))
             return None, res.n_out, res.sum
         cap = Sa.shape[0] if out_cap is None else out_cap
         o = ctx.alloc(max(cap, 1) * ow)
-        rc = L.pg_hashjoin_probe(ctx.h, ctx.stream, self.h, ctypes.byref(rS), c, nc,
-                                 o.ptr, cap, flags, sum_col, ctypes.byref(res))
+        rc = call(ctx.h, ctx.stream, self.h, ctypes.byref(rS), c, nc,
+                  o.ptr, cap, flags, sum_col, ctypes.byref(res))
         if rc == PG_ERR_OUTPUT_FULL and out_cap is None:
             cap = res.n_out
             o = ctx.alloc(max(cap, 1) * ow)
-            rc = L.pg_hashjoin_probe(ctx.h, ctx.stream, self.h, ctypes.byref(rS), c, nc,
-                                     o.ptr, cap, flags, sum_col, ctypes.byref(res))
+            rc = call(ctx.h, ctx.stream, self.h, ctypes.byref(rS), c, nc,
+                      o.ptr, cap, flags, sum_col, ctypes.byref(res))
         ctx._check(rc)
         out = ctx.download(o, res.n_out * ow).reshape(-1, ow) if ow else None
         return out, res.n_out, res.sum

@@ -166,10 +166,10 @@ void GroupedOutput::setup(const ThreadGroups& g, unsigned tuple_size, unsigned b
 	cur_.assign(MAX_THREADS, c);
 }
 
-void GroupedOutput::own_device(void* p)
+void GroupedOutput::own_device(void* p, bool pool)
 {
 	pthread_mutex_lock(&mu_);
-	owned_.push_back(p);
+	(pool ? owned_pool_ : owned_).push_back(p);
 	pthread_mutex_unlock(&mu_);
 }
 
@@ -217,9 +217,11 @@ void GroupedOutput::clear()
 	out_.clear();
 	rows_.clear();
 	dev_.clear();
-	pg_ctx* ctx = owned_.empty() ? 0 : shared_context();
+	pg_ctx* ctx = owned_.empty() && owned_pool_.empty() ? 0 : shared_context();
 	for (size_t i = 0; i < owned_.size(); ++i) pg_buffer_free(ctx, owned_[i]);
+	for (size_t i = 0; i < owned_pool_.size(); ++i) pg_buffer_free_async(ctx, 0, owned_pool_[i]);
 	owned_.clear();
+	owned_pool_.clear();
 }
 
 bool drain(Operator* child, unsigned short tid, std::vector<char>& sink)
@@ -476,6 +478,12 @@ void GpuJoinBase::init(libconfig::Config& root, libconfig::Setting& node)
 		barriers_.push_back(new GroupBarrier());
 		barriers_.back()->init((unsigned) groups_.members[g].size());
 	}
+	probe_filter_ = g_exchange ? dynamic_cast<GpuFilterOp*>(probeOp) : 0;
+	probe_preds_.clear();
+	if (probe_filter_) {
+		probe_filter_->fuse_into_parent();
+		probe_preds_ = probe_filter_->predicates();
+	}
 	build_.setup(buildOp);
 	probe_.setup(probeOp);
 	group_rc_.assign(groups_.members.size(), PG_OK);
@@ -516,11 +524,22 @@ int GpuJoinBase::run_group(int g)
 	void *tR = 0, *tS = 0, *dO = 0;
 	unsigned long long rows = 0;
 	const unsigned wR = buildOp->getOutSchema().getTupleSize(), wS = probeOp->getOutSchema().getTupleSize();
+	void* tF = 0;
 	if (!(rc = build_.gather(ctx, st, mem, wR, &dR, &nR, &tR)) &&
 			!(rc = probe_.gather(ctx, st, mem, wS, &dS, &nS, &tS))) {
+		if (!probe_preds_.empty() && !probe_predicates() && nS) {
+			// A fused gpufilter's predicates, applied to the probe side here.
+			const pg_rel all = side_rel(probeOp, probekey_, dS, nS);
+			uint64_t m = 0;
+			if (!(rc = pg_buffer_alloc_async(ctx, st, nS * wS, &tF)) &&
+					!(rc = pg_filter(ctx, st, &all, &probe_preds_[0], (int) probe_preds_.size(), tF, &m))) {
+				dS = (const char*) tF;
+				nS = m;
+			}
+		}
 		const pg_rel r = side_rel(buildOp, buildkey_, dR, nR);
 		const pg_rel s = side_rel(probeOp, probekey_, dS, nS);
-		rc = run_device(ctx, st, r, s, &dO, &rows);
+		if (!rc) rc = run_device(ctx, st, r, s, &dO, &rows);
 	}
 	if (!rc && !on_device_) {
 		std::vector<char>& out = output_.buffer(g);
@@ -531,6 +550,7 @@ int GpuJoinBase::run_group(int g)
 	for (size_t i = 0; i < mem.size(); ++i) { build_.release(mem[i], st); probe_.release(mem[i], st); }
 	if (tR) pg_buffer_free_async(ctx, st, tR);
 	if (tS) pg_buffer_free_async(ctx, st, tS);
+	if (tF) pg_buffer_free_async(ctx, st, tF);
 	if (!rc) rc = pg_sync(ctx, st);
 	if (!rc && on_device_) {
 		output_.set_device(g, (const char*) dO, rows);
@@ -562,6 +582,19 @@ Operator::ResultCode GpuJoinBase::scanStart(unsigned short tid, Page* idx, Schem
 	if (group_rc_[g] != PG_OK) return Error;
 	output_.assign(tid, g, groups_.pos_in[tid], (int) mem.size());
 	return Ready;
+}
+
+void GpuJoinBase::narrow_projection(const std::vector<unsigned>& keep)
+{
+	std::vector<pg_col> cols;
+	Schema narrowed;
+	for (size_t i = 0; i < keep.size(); ++i) {
+		cols.push_back(cols_.at(keep[i]));
+		narrowed.add(schema.get(keep[i]));
+	}
+	cols_ = cols;
+	schema = narrowed;
+	output_.setup(groups_, schema.getTupleSize(), buffsize);
 }
 
 Operator::GetNextResultT GpuJoinBase::getNext(unsigned short tid)
@@ -600,7 +633,8 @@ int GpuHashJoinOp::run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const 
 	res.n_out = 0; res.sum = 0;
 	for (int attempt = 0; attempt < 2; ++attempt) {
 		if ((rc = pg_buffer_alloc(ctx, cap * ow, &o))) break;
-		rc = pg_hashjoin_probe(ctx, st, ht, &S, &cols_[0], (int) cols_.size(), o, cap, PG_JOIN_MATERIALIZE, -1, &res);
+		rc = pg_hashjoin_probe_where(ctx, st, ht, &S, probe_preds_.empty() ? 0 : &probe_preds_[0],
+				(int) probe_preds_.size(), &cols_[0], (int) cols_.size(), o, cap, PG_JOIN_MATERIALIZE, -1, &res);
 		if (rc == PG_ERR_OUTPUT_FULL && attempt == 0) {
 			pg_buffer_free(ctx, o);
 			o = 0;
@@ -918,6 +952,275 @@ void GpuAggregateOp::destroy()
 	output_.clear();
 }
 
+// ---------------------------------------------------------------------------
+// Filter and Project.
+// ---------------------------------------------------------------------------
+namespace {
+// Comparator::parseString (comparator.cpp:415-431).
+uint32_t cmp_code(const std::string& op)
+{
+	if (op == "<") return PG_CMP_LT;
+	if (op == "<=") return PG_CMP_LE;
+	if (op == "=" || op == "==") return PG_CMP_EQ;
+	if (op == "<>" || op == "!=") return PG_CMP_NE;
+	if (op == ">=") return PG_CMP_GE;
+	if (op == ">") return PG_CMP_GT;
+	throw std::invalid_argument("gpufilter: unknown comparison `" + op + "'");
+}
+
+// Per-thread groups: every thread a group of its own.
+void one_group_per_thread(ThreadGroups& g)
+{
+	g.group_of.assign(MAX_THREADS, -1);
+	g.pos_in.assign(MAX_THREADS, -1);
+	g.members.clear();
+	for (int t = 0; t < MAX_THREADS; ++t) {
+		g.group_of[t] = t; g.pos_in[t] = 0;
+		g.members.push_back(std::vector<int>(1, t));
+	}
+}
+}  // namespace
+
+void GpuFilterOp::init(libconfig::Config& root, libconfig::Setting& node)
+{
+	Operator::init(root, node);
+	schema = nextOp->getOutSchema();
+	const unsigned field = (int) node["field"];
+	if (field >= schema.columns()) throw std::invalid_argument("gpufilter: field out of range");
+	std::string op = node["op"];
+	std::string value = node["value"];
+	pg_pred p;
+	memset(&p, 0, sizeof p);
+	p.op = cmp_code(op);
+	p.off = col_offset(schema, field);
+	p.bytes = schema.getColumnWidth(field);
+	switch (schema.getColumnType(field)) {
+	case CT_INTEGER: p.type = PG_PRED_INT; break;
+	case CT_LONG: case CT_DATE: p.type = PG_PRED_LONG; break;
+	case CT_DECIMAL: p.type = PG_PRED_DEC; break;
+	case CT_CHAR: p.type = PG_PRED_CHAR; break;
+	default: throw std::invalid_argument("gpufilter: unsupported column type");
+	}
+	if (p.bytes > sizeof p.value) throw std::invalid_argument("gpufilter: column wider than 128 bytes");
+	// The constant in the column's own form, parsed as Filter parses it
+	// (filter.cpp:57-64): a one-column schema of the same column.
+	Schema one;
+	one.add(schema.get(field));
+	const char* text = value.c_str();
+	one.parseTuple(p.value, &text);
+	preds_.clear();
+	preds_.push_back(p);
+	// A gpufilter right below hands its input up: both predicates in one pass.
+	GpuFilterOp* below = g_exchange ? dynamic_cast<GpuFilterOp*>(nextOp) : 0;
+	if (below) {
+		below->fuse_into_parent();
+		const std::vector<pg_pred>& more = below->predicates();
+		preds_.insert(preds_.end(), more.begin(), more.end());
+		if (preds_.size() > PG_PRED_MAX) throw std::invalid_argument("gpufilter: at most 4 filters in a row");
+	}
+	in_.setup(nextOp);
+	one_group_per_thread(groups_);
+	output_.setup(groups_, schema.getTupleSize(), buffsize);
+	rc_.assign(MAX_THREADS, PG_OK);
+}
+
+void GpuFilterOp::threadInit(unsigned short tid)
+{
+	(void) tid;
+}
+
+// This thread's input, filtered (or, fused, handed through unfiltered).
+int GpuFilterOp::run(unsigned short tid)
+{
+	pg_ctx* ctx = shared_context();
+	if (!ctx) return PG_ERR_CUDA;
+	const unsigned w = schema.getTupleSize();
+	pg_stream st = 0;
+	int rc = pg_stream_create(ctx, &st);
+	if (rc) return rc;
+	const char* din = 0;
+	unsigned long long n = 0;
+	void *tin = 0, *dout = 0;
+	uint64_t m = 0;
+	rc = in_.gather(ctx, st, std::vector<int>(1, (int) tid), w, &din, &n, &tin);
+	if (!rc && fused_) {
+		// The parent applies the predicates; the input stays as it is (its
+		// staged memory lives until destroy).
+		if (!(rc = pg_sync(ctx, st))) {
+			output_.set_device(tid, din, n);
+			if (tin) output_.own_device(tin, true);
+			tin = 0;
+		}
+	} else if (!rc) {
+		pg_rel r;
+		r.data = din; r.n = n; r.width = w; r.key_off = 0; r.key_bytes = 0;
+		if (!(rc = pg_buffer_alloc(ctx, std::max<unsigned long long>(n, 1) * w, &dout)) &&
+				!(rc = pg_filter(ctx, st, &r, &preds_[0], (int) preds_.size(), dout, &m))) {
+			if (on_device_) {
+				output_.set_device(tid, (const char*) dout, m);
+				output_.own_device(dout);
+				dout = 0;
+			} else {
+				std::vector<char>& out = output_.buffer(tid);
+				out.resize((size_t) (m * w));
+				if (m) rc = pg_d2h(ctx, st, &out[0], dout, m * w);
+				count(&g_stats.d2h, m * w);
+				output_.set_rows(tid, rc ? 0 : m);
+			}
+		}
+		in_.release(tid, st);
+		if (tin) pg_buffer_free_async(ctx, st, tin);
+		if (!rc) rc = pg_sync(ctx, st);
+	}
+	if (dout) pg_buffer_free(ctx, dout);
+	pg_stream_destroy(ctx, st);
+	return rc;
+}
+
+Operator::ResultCode GpuFilterOp::scanStart(unsigned short tid, Page* idx, Schema& idxs)
+{
+	bool ok = nextOp->scanStart(tid, idx, idxs) != Error && in_.fetch(nextOp, tid);
+	int rc = ok ? run(tid) : PG_ERR_ARG;
+	rc_[tid] = rc;
+	if (rc) { note_failure("gpufilter", rc); return Error; }
+	output_.assign(tid, tid, 0, 1);
+	return Ready;
+}
+
+Operator::GetNextResultT GpuFilterOp::getNext(unsigned short tid)
+{
+	if (on_device_ || rc_[tid] != PG_OK) return std::make_pair(Error, (Page*) 0);
+	return output_.next(tid);
+}
+
+Operator::ResultCode GpuFilterOp::scanStop(unsigned short tid)
+{
+	return nextOp->scanStop(tid);
+}
+
+void GpuFilterOp::destroy()
+{
+	output_.clear();
+	in_.clear();
+}
+
+void GpuProjectOp::init(libconfig::Config& root, libconfig::Setting& node)
+{
+	Operator::init(root, node);
+	Schema& src = nextOp->getOutSchema();
+	libconfig::Setting& pr = node["projection"];
+	proj_.clear();
+	cols_.clear();
+	for (int i = 0; i < pr.getLength(); ++i) {
+		// "$i" as Project's parseInput reads it (project.cpp:37-50).
+		std::string s = pr[i];
+		const std::string::size_type d = s.find('$');
+		unsigned attr = 0;
+		std::istringstream is(d == std::string::npos ? std::string() : s.substr(d + 1));
+		is >> attr;
+		if (d == std::string::npos || !is) throw std::invalid_argument("gpuproject: bad projection `" + s + "'");
+		if (attr >= src.columns()) throw std::invalid_argument("gpuproject: projection column out of range");
+		proj_.push_back(attr);
+		pg_col c;
+		c.side = 0;
+		c.off = col_offset(src, attr);
+		c.bytes = src.getColumnWidth(attr);
+		cols_.push_back(c);
+		schema.add(src.get(attr));
+	}
+	join_ = g_exchange ? dynamic_cast<GpuJoinBase*>(nextOp) : 0;
+	if (join_) {
+		join_->narrow_projection(proj_);
+		return;
+	}
+	in_.setup(nextOp);
+	one_group_per_thread(groups_);
+	output_.setup(groups_, schema.getTupleSize(), buffsize);
+	rc_.assign(MAX_THREADS, PG_OK);
+}
+
+void GpuProjectOp::threadInit(unsigned short tid)
+{
+	(void) tid;
+}
+
+void GpuProjectOp::keep_on_device()
+{
+	on_device_ = true;
+	if (join_) join_->keep_on_device();
+}
+
+DeviceSpan GpuProjectOp::device_share(unsigned short tid)
+{
+	return join_ ? join_->device_share(tid) : output_.share(tid);
+}
+
+int GpuProjectOp::run(unsigned short tid)
+{
+	pg_ctx* ctx = shared_context();
+	if (!ctx) return PG_ERR_CUDA;
+	const unsigned w = nextOp->getOutSchema().getTupleSize(), ow = schema.getTupleSize();
+	pg_stream st = 0;
+	int rc = pg_stream_create(ctx, &st);
+	if (rc) return rc;
+	const char* din = 0;
+	unsigned long long n = 0;
+	void *tin = 0, *dout = 0;
+	if (!(rc = in_.gather(ctx, st, std::vector<int>(1, (int) tid), w, &din, &n, &tin)) &&
+			!(rc = pg_buffer_alloc(ctx, std::max<unsigned long long>(n, 1) * ow, &dout))) {
+		pg_rel r;
+		r.data = din; r.n = n; r.width = w; r.key_off = 0; r.key_bytes = 0;
+		if (!(rc = pg_project(ctx, st, &r, &cols_[0], (int) cols_.size(), dout))) {
+			if (on_device_) {
+				output_.set_device(tid, (const char*) dout, n);
+				output_.own_device(dout);
+				dout = 0;
+			} else {
+				std::vector<char>& out = output_.buffer(tid);
+				out.resize((size_t) (n * ow));
+				if (n) rc = pg_d2h(ctx, st, &out[0], dout, n * ow);
+				count(&g_stats.d2h, n * ow);
+				output_.set_rows(tid, rc ? 0 : n);
+			}
+		}
+	}
+	in_.release(tid, st);
+	if (tin) pg_buffer_free_async(ctx, st, tin);
+	if (!rc) rc = pg_sync(ctx, st);
+	if (dout) pg_buffer_free(ctx, dout);
+	pg_stream_destroy(ctx, st);
+	return rc;
+}
+
+Operator::ResultCode GpuProjectOp::scanStart(unsigned short tid, Page* idx, Schema& idxs)
+{
+	if (join_) return nextOp->scanStart(tid, idx, idxs);
+	bool ok = nextOp->scanStart(tid, idx, idxs) != Error && in_.fetch(nextOp, tid);
+	int rc = ok ? run(tid) : PG_ERR_ARG;
+	rc_[tid] = rc;
+	if (rc) { note_failure("gpuproject", rc); return Error; }
+	output_.assign(tid, tid, 0, 1);
+	return Ready;
+}
+
+Operator::GetNextResultT GpuProjectOp::getNext(unsigned short tid)
+{
+	if (join_) return nextOp->getNext(tid);
+	if (on_device_ || rc_[tid] != PG_OK) return std::make_pair(Error, (Page*) 0);
+	return output_.next(tid);
+}
+
+Operator::ResultCode GpuProjectOp::scanStop(unsigned short tid)
+{
+	return nextOp->scanStop(tid);
+}
+
+void GpuProjectOp::destroy()
+{
+	output_.clear();
+	in_.clear();
+}
+
 Operator* create(const std::string& type)
 {
 	if (type == "gpuhashjoin") return new GpuHashJoinOp();
@@ -925,6 +1228,8 @@ Operator* create(const std::string& type)
 	if (type == "gpupartition") return new GpuPartitionOp();
 	if (type == "gpuaggregate_sum") return new GpuAggregateSumOp();
 	if (type == "gpuaggregate_count") return new GpuAggregateCountOp();
+	if (type == "gpufilter") return new GpuFilterOp();
+	if (type == "gpuproject") return new GpuProjectOp();
 	return 0;
 }
 

@@ -79,7 +79,7 @@ public:
 	virtual ~DeviceProducer() { }
 	// Called by the parent's init: keep the output on the device; getNext
 	// then reports Error (the parent takes device_share instead).
-	void keep_on_device() { on_device_ = true; }
+	virtual void keep_on_device() { on_device_ = true; }
 	// After scanStart(tid) returned Ready: the rows thread `tid` serves,
 	// valid until destroy.
 	virtual DeviceSpan device_share(unsigned short tid) = 0;
@@ -124,8 +124,9 @@ public:
 	void set_rows(int group, unsigned long long rows) { rows_[group] = rows; }
 	// The group's output is `rows` tuples at device address `data`.
 	void set_device(int group, const char* data, unsigned long long rows);
-	// Device memory freed by clear(); threads may hand it over concurrently.
-	void own_device(void* p);
+	// Device memory freed by clear() (pool: from pg_buffer_alloc_async);
+	// threads may hand it over concurrently.
+	void own_device(void* p, bool pool = false);
 	// Thread `tid` serves rows [pos * rows / k, (pos + 1) * rows / k) of its group.
 	void assign(int tid, int group, int pos, int k);
 	Operator::GetNextResultT next(int tid);
@@ -142,7 +143,7 @@ private:
 	std::vector<std::vector<char> > out_;
 	std::vector<unsigned long long> rows_;
 	std::vector<const char*> dev_;
-	std::vector<void*> owned_;
+	std::vector<void*> owned_, owned_pool_;
 	std::vector<Cursor> cur_;
 	unsigned tuple_size_, page_bytes_;
 };
@@ -193,9 +194,11 @@ private:
 	std::vector<DeviceSpan> spans_;
 };
 
+class GpuFilterOp;
+
 class GpuJoinBase : public DualInputOp, public DeviceProducer {
 public:
-	GpuJoinBase() : buildkey_(0), probekey_(0) { }
+	GpuJoinBase() : buildkey_(0), probekey_(0), probe_filter_(0) { }
 	virtual void init(libconfig::Config& root, libconfig::Setting& node);
 	virtual void threadInit(unsigned short threadid);
 	virtual ResultCode scanStart(unsigned short threadid, Page* indexdatapage, Schema& indexdataschema);
@@ -204,12 +207,22 @@ public:
 	virtual void threadClose(unsigned short threadid);
 	virtual void destroy();
 	virtual DeviceSpan device_share(unsigned short threadid) { return output_.share(threadid); }
+	// A gpuproject above folds into the join: output columns `keep` (indices
+	// into the current projection), in that order.
+	void narrow_projection(const std::vector<unsigned>& keep);
 protected:
+	// Whether run_device applies probe_preds_ itself (else the probe side is
+	// filtered before it runs).
+	virtual bool probe_predicates() const { return false; }
 	// Joins device inputs on `st` into device rows *out (freed by the caller).
 	virtual int run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
 			unsigned long long* rows) = 0;
 	std::vector<pg_col> cols_;
 	unsigned buildkey_, probekey_;
+	// Predicates of a gpufilter directly under the probe side, applied by
+	// the join (the filter hands its input through).
+	GpuFilterOp* probe_filter_;
+	std::vector<pg_pred> probe_preds_;
 private:
 	int run_group(int g);
 	ThreadGroups groups_;
@@ -225,6 +238,7 @@ private:
 // have no effect on the result.
 class GpuHashJoinOp : public GpuJoinBase {
 protected:
+	virtual bool probe_predicates() const { return true; }
 	virtual int run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
 			unsigned long long* rows);
 };
@@ -310,6 +324,64 @@ public:
 class GpuAggregateCountOp : public GpuAggregateOp {
 public:
 	GpuAggregateCountOp() : GpuAggregateOp(PG_AGG_COUNT) { }
+};
+
+// "gpufilter": Filter (operators/filter.cpp:37-85): `field`, `op` ("<",
+// "<=", "=", "==", "<>", "!=", ">=", ">") and `value`, text in the column's
+// own form, parsed as Filter parses it (Schema::parseTuple). Each thread
+// filters its own input, in order, as MapWrapper's per-thread loop does
+// (mapwrapper.cpp:71-138). Fused forms: a gpufilter under another gpufilter
+// hands its input up and the upper one evaluates both predicates in one
+// launch; a gpufilter directly under the probe side of a gpuhashjoin hands
+// its input to the join, whose probe evaluates the predicates before its
+// table lookups (gpumpsmjoin filters the probe side on the device first).
+class GpuFilterOp : public SingleInputOp, public DeviceProducer {
+public:
+	GpuFilterOp() : fused_(false) { }
+	virtual void init(libconfig::Config& root, libconfig::Setting& node);
+	virtual void threadInit(unsigned short threadid);
+	virtual ResultCode scanStart(unsigned short threadid, Page* indexdatapage, Schema& indexdataschema);
+	virtual GetNextResultT getNext(unsigned short threadid);
+	virtual ResultCode scanStop(unsigned short threadid);
+	virtual void destroy();
+	virtual DeviceSpan device_share(unsigned short threadid) { return output_.share(threadid); }
+	// Called by the parent that applies predicates() itself.
+	void fuse_into_parent() { fused_ = true; keep_on_device(); }
+	const std::vector<pg_pred>& predicates() const { return preds_; }
+private:
+	int run(unsigned short tid);
+	std::vector<pg_pred> preds_;     // this filter's, then those of fused filters below
+	bool fused_;
+	InputSide in_;
+	ThreadGroups groups_;            // one group per thread
+	GroupedOutput output_;
+	std::vector<int> rc_;
+};
+
+// "gpuproject": Project (operators/project.cpp:37-104): `projection` =
+// ("$i", ...), the input columns to keep, in order. Over a GPU join it folds
+// into the join's projection (the join writes only these columns) and hands
+// the join's output through; otherwise each thread projects its own input.
+class GpuProjectOp : public SingleInputOp, public DeviceProducer {
+public:
+	GpuProjectOp() : join_(0) { }
+	virtual void init(libconfig::Config& root, libconfig::Setting& node);
+	virtual void threadInit(unsigned short threadid);
+	virtual ResultCode scanStart(unsigned short threadid, Page* indexdatapage, Schema& indexdataschema);
+	virtual GetNextResultT getNext(unsigned short threadid);
+	virtual ResultCode scanStop(unsigned short threadid);
+	virtual void destroy();
+	virtual DeviceSpan device_share(unsigned short threadid);
+	virtual void keep_on_device();
+private:
+	int run(unsigned short tid);
+	std::vector<unsigned> proj_;
+	std::vector<pg_col> cols_;
+	GpuJoinBase* join_;              // the join this projection folded into
+	InputSide in_;
+	ThreadGroups groups_;
+	GroupedOutput output_;
+	std::vector<int> rc_;
 };
 
 // The operator for a plan `type:` string ("gpuhashjoin", ...), or NULL.

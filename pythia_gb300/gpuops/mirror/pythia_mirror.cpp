@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cctype>
 #include <cstdlib>
+#include <time.h>
 #include <sstream>
 
 namespace libconfig {
@@ -274,7 +275,51 @@ void Schema::add(ColumnType ct, unsigned int size)
 	}
 	vct.push_back(ct);
 	voffset.push_back(totalsize);
+	vformat.push_back(std::string());
 	totalsize += w;
+}
+
+void Schema::add(ColumnType ct, const std::string& formatstr)
+{
+	add(ct, 0);
+	vformat.back() = formatstr;
+}
+
+void Schema::add(ColumnSpec desc)
+{
+	if (desc.type == CT_DATE) add(CT_DATE, desc.formatstr);
+	else add(desc.type, desc.size);
+}
+
+void Schema::parseTuple(void* dest, const char** input) const
+{
+	for (unsigned int i = 0; i < columns(); ++i) {
+		char* d = (char*) dest + voffset[i];
+		switch (vct[i]) {
+		case CT_INTEGER: { int v = atoi(input[i]); memcpy(d, &v, sizeof v); break; }
+		case CT_LONG: { long long v = atoll(input[i]); memcpy(d, &v, sizeof v); break; }
+		case CT_DECIMAL: { double v = atof(input[i]); memcpy(d, &v, sizeof v); break; }
+		case CT_CHAR: strncpy(d, input[i], getColumnWidth(i)); break;
+		case CT_DATE: {
+			// Packed fields, least significant first: 20 bits below the
+			// seconds, then seconds and minutes (6 bits), hours and days (5),
+			// months (4) and years since 1900 (18).
+			struct tm t;
+			memset(&t, 0, sizeof t);
+			strptime(input[i], vformat[i].c_str(), &t);
+			unsigned long long v = 0;
+			v |= ((unsigned long long) t.tm_sec & 0x3Full) << 20;
+			v |= ((unsigned long long) t.tm_min & 0x3Full) << 26;
+			v |= ((unsigned long long) t.tm_hour & 0x1Full) << 32;
+			v |= ((unsigned long long) t.tm_mday & 0x1Full) << 37;
+			v |= ((unsigned long long) t.tm_mon & 0xFull) << 42;
+			v |= ((unsigned long long) t.tm_year & 0x3FFFFull) << 46;
+			memcpy(d, &v, sizeof v);
+			break;
+		}
+		case CT_POINTER: throw std::invalid_argument("pointer columns have no text form");
+		}
+	}
 }
 
 Schema Schema::create(const libconfig::Setting& line)
@@ -290,7 +335,7 @@ Schema Schema::create(const libconfig::Setting& line)
 		else if (head.find("dec") == 0) ret.add(CT_DECIMAL);
 		else if (head.find("date") == 0) {
 			if (paren == std::string::npos) throw std::invalid_argument("date needs a format: " + v);
-			ret.add(CT_DATE);
+			ret.add(CT_DATE, v.substr(paren + 1));
 		} else if (head.find("char") == 0) {
 			if (paren == std::string::npos) throw std::invalid_argument("char needs a length: " + v);
 			std::istringstream is(v.substr(paren + 1));

@@ -145,19 +145,27 @@ typedef long long CtLong;
 typedef double CtDecimal;
 typedef char CtChar;
 
+// A column: type, width, and (dates) the strptime format of its text form.
 struct ColumnSpec {
-	ColumnSpec(ColumnType ct, unsigned int sz) : type(ct), size(sz) { }
+	ColumnSpec(ColumnType ct, unsigned int sz, const std::string& str = std::string())
+		: type(ct), size(sz), formatstr(str) { }
 	ColumnType type;
 	unsigned int size;
+	std::string formatstr;
 };
 
 class Schema {
 public:
 	Schema() : totalsize(0) { }
 	void add(ColumnType ct, unsigned int size = 0);
-	void add(ColumnSpec desc) { add(desc.type, desc.size); }
+	void add(ColumnType ct, const std::string& formatstr);
+	void add(ColumnSpec desc);
 	ColumnType getColumnType(unsigned int pos) const { return vct.at(pos); }
-	ColumnSpec get(unsigned int pos) const { return ColumnSpec(vct.at(pos), getColumnWidth(pos)); }
+	ColumnSpec get(unsigned int pos) const { return ColumnSpec(vct.at(pos), getColumnWidth(pos), vformat.at(pos)); }
+	// Text to tuple, one string per column: int/long/dec as atoi/atoll/atof,
+	// char copied with strncpy into the column, date through strptime and the
+	// engine's packed date form (schema.cpp:129-168, schema.h:66-104).
+	void parseTuple(void* dest, const char** input) const;
 	unsigned int getColumnWidth(unsigned int pos) const
 	{
 		return (pos + 1 < voffset.size() ? voffset[pos + 1] : totalsize) - voffset.at(pos);
@@ -170,6 +178,7 @@ public:
 private:
 	std::vector<ColumnType> vct;
 	std::vector<unsigned int> voffset;
+	std::vector<std::string> vformat;
 	unsigned int totalsize;
 };
 

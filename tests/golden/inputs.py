@@ -57,7 +57,95 @@ def _formula(name, n):
         out = w.view(np.int32).reshape(n, 2).copy()
         out[:, 0] = np.abs(out[:, 0] % 37)
         return out
+    if name == "mixed_cols":
+        return mixed_cols(n)
     raise KeyError(name)
+
+
+MIXED_SCHEMA = "int;long;dec;char(11);date(%Y-%m-%d)"
+MIXED_OFF = {"int": 0, "long": 4, "dec": 12, "char": 20, "date": 32}
+MIXED_WIDTH = 40
+WORDS = [b"", b"a", b"ab", b"abc", b"abd", b"b", b"alpha", b"alphabet", b"beta", b"gamma",
+         b"delta epsil", b"zz", b"Zeta", b"abc\xe9"]
+
+
+def date_bits(year, month, day):
+    """The engine's packed date (schema.h:66-104): years since 1900 << 46,
+    month - 1 << 42, day << 37."""
+    return ((year - 1900) << 46) | ((month - 1) << 42) | (day << 37)
+
+
+def mixed_cols(n):
+    """Rows (int, long, dec, char(11), date) = 40 bytes: small-domain ints
+    and longs (many equal to the filter constants), decs with NaN, signed
+    zeros and infinities, strings sharing prefixes, dates over seven years."""
+    w = dg.raw_words(dg.seed_for(43), 0, 5 * n).astype(np.uint64).reshape(5, n) if n else np.zeros((5, 0), np.uint64)
+    out = np.zeros((n, MIXED_WIDTH), dtype=np.uint8)
+    ints = (w[0] % 41).astype(np.int64) - 20
+    longs = (w[1] % 2001).astype(np.int64) * (1 << 31) - 1000 * (1 << 31)
+    decs = (w[2] % 1000).astype(np.float64) / 8.0 - 60.0
+    sel = w[2] >> np.uint64(40)
+    decs[(sel % 53) == 0] = np.nan
+    decs[(sel % 59) == 1] = -0.0
+    decs[(sel % 61) == 2] = 0.0
+    decs[(sel % 67) == 3] = np.inf
+    decs[(sel % 71) == 4] = -np.inf
+    out[:, 0:4] = ints.astype(np.int32).view(np.uint8).reshape(n, 4)
+    out[:, 4:12] = longs.view(np.uint8).reshape(n, 8)
+    out[:, 12:20] = decs.view(np.uint8).reshape(n, 8)
+    for i in range(n):
+        s = WORDS[int(w[3][i] % len(WORDS))]
+        out[i, 20:20 + len(s)] = np.frombuffer(s, dtype=np.uint8)
+    years = 1992 + (w[4] % 7).astype(np.int64)
+    months = 1 + ((w[4] >> np.uint64(8)) % 12).astype(np.int64)
+    days = 1 + ((w[4] >> np.uint64(16)) % 28).astype(np.int64)
+    out[:, 32:40] = date_bits(years, months, days).astype(np.int64).view(np.uint8).reshape(n, 8)
+    return out
+
+
+def schema_columns(schema):
+    """[(type, offset, width)] of a ';'-separated schema list (Schema::create,
+    schema.cpp:221-259: char(N) holds N + 1 bytes)."""
+    out, off = [], 0
+    for c in schema.split(";"):
+        if c == "int":
+            t, w = "int", 4
+        elif c.startswith("char("):
+            t, w = "char", int(c[5:-1]) + 1
+        elif c.startswith("date"):
+            t, w = "date", 8
+        else:
+            t, w = ("dec" if c == "dec" else "long"), 8
+        out.append((t, off, w))
+        off += w
+    return out
+
+
+def filter_value(t, text):
+    """Filter's constant parsed as Schema::parseTuple does (schema.cpp:129-168):
+    atoi / atoll / atof, strncpy of the text, strptime + packed date."""
+    import time
+    if t == "int":
+        return int(text)
+    if t == "long":
+        return int(text)
+    if t == "dec":
+        return float(text)
+    if t == "date":
+        tm = time.strptime(text, "%Y-%m-%d")
+        return date_bits(tm.tm_year, tm.tm_mon, tm.tm_mday)
+    return text.encode()
+
+
+def filter_preds(schema, filters):
+    """Oracle / GPU predicate specs [(type, op, offset, value, width)] of
+    [(field index, op, text)] filters (Filter's field / op / value keys)."""
+    cols = schema_columns(schema)
+    out = []
+    for field, op, text in filters:
+        t, off, w = cols[field]
+        out.append(("long" if t == "date" else t, op, off, filter_value(t, text), w))
+    return out
 
 
 def make(spec):

@@ -218,6 +218,54 @@ def main():
                           "ref": {"keys_sha256": sha(raw[:, :8]),
                                   "canonical_sha256": sha(canonical(raw))}})
 
+        # ---- Filter (filter.cpp:37-85) and Project (project.cpp:37-104) ----
+        # One scanning thread: the output keeps the input order exactly.
+        MIX = {"gen": "formula", "name": "mixed_cols", "n": 5000}
+        mixed = gin.make(MIX)
+        FIELD = {"int": 0, "long": 1, "dec": 2, "char": 3, "date": 4}
+        filters = [
+            [("int", "<", "0")], [("int", "=", "7")], [("int", "!=", "-3")], [("int", ">=", "15")],
+            [("long", "<=", str(-300 * (1 << 31)))], [("long", ">", "0")], [("long", "==", str(17 * (1 << 31)))],
+            [("dec", "<", "0")], [("dec", "==", "0")], [("dec", "!=", "nan")], [("dec", ">", "-inf")],
+            [("dec", "<>", "1.5")], [("dec", ">=", "inf")], [("dec", "<=", "-12.375")],
+            [("char", "=", "abc")], [("char", "<", "alpha")], [("char", ">", "ab")], [("char", "<>", "")],
+            [("char", ">=", "b")], [("char", "==", "delta epsilon")], [("char", "<", "abc\xe9")],
+            [("date", "<", "1995-03-15")], [("date", ">=", "1993-01-01")], [("date", "==", "1994-06-10")],
+            [("int", ">", "-5"), ("dec", "<", "30"), ("char", "!=", "zz")],
+            [("date", ">=", "1994-01-01"), ("date", "<", "1995-01-01"), ("long", ">=", "0"), ("int", "<>", "0")],
+        ]
+        for k, flt in enumerate(filters):
+            kw = {}
+            for j, (col, op, val) in enumerate(flt):
+                sfx = str(j + 1) if j else ""
+                kw["field" + sfx] = FIELD[col]
+                kw["op" + sfx] = op
+                kw["value" + sfx] = val
+            raw = run(tmp, "filter", {"in": mixed}, schema=gin.MIXED_SCHEMA, buffsize=4096, **kw)
+            rows = raw.reshape(-1, gin.MIXED_WIDTH)
+            cases.append({"name": f"filter_{k}_{'_'.join(c for c, _, _ in flt)}", "op": "filter",
+                          "inputs": {"in": MIX}, "input_sha256": {"in": sha(mixed)},
+                          "params": {"schema": gin.MIXED_SCHEMA,
+                                     "filters": [[FIELD[c], o, v] for c, o, v in flt]},
+                          "ref": {"n": int(rows.shape[0]), "sha256": sha(rows)}})
+        # The reference's own test: 20 rows (i, i), field 0 < 10 (unit_tests/querymap.cpp:41-190).
+        ii = {"gen": "formula", "name": "i_i", "n": 20}
+        raw = run(tmp, "filter", {"in": gin.make(ii)}, schema="long;long", field=0, op="<", value="10", buffsize=64)
+        cases.append({"name": "filter_reference_querymap", "op": "filter", "inputs": {"in": ii},
+                      "input_sha256": {"in": sha(gin.make(ii))},
+                      "params": {"schema": "long;long", "filters": [[0, "<", "10"]]},
+                      "ref": {"n": int(raw.size // 16), "sha256": sha(raw.reshape(-1, 16))}})
+        for proj in ("3,0", "4,2,1", "0,0,1", "2"):
+            raw = run(tmp, "project", {"in": mixed}, schema=gin.MIXED_SCHEMA, projection=proj, buffsize=4096)
+            cases.append({"name": f"project_{proj.replace(',', '_')}", "op": "project", "inputs": {"in": MIX},
+                          "input_sha256": {"in": sha(mixed)}, "params": {"schema": gin.MIXED_SCHEMA, "projection": proj},
+                          "ref": {"bytes": int(raw.size), "sha256": sha(raw)}})
+        # unit_tests/queryproject.cpp: ("$1") of 20 rows (i, i).
+        raw = run(tmp, "project", {"in": gin.make(ii)}, schema="long;long", projection="1", buffsize=64)
+        cases.append({"name": "project_reference_queryproject", "op": "project", "inputs": {"in": ii},
+                      "input_sha256": {"in": sha(gin.make(ii))}, "params": {"schema": "long;long", "projection": "1"},
+                      "ref": {"bytes": int(raw.size), "sha256": sha(raw)}})
+
     path = os.path.join(ROOT, "tests", "golden", "golden.json")
     with open(path, "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py",

@@ -110,5 +110,20 @@ def test_golden(case):
         out = orc.sort(a)
         assert sha(out[:, :1].copy()) == ref["keys_sha256"]
         assert sha(orc.canonical(out)) == ref["canonical_sha256"]
+    elif op == "filter":
+        a = inputs["in"]
+        w = sum(cw for _, _, cw in gin.schema_columns(p["schema"]))
+        rows = np.ascontiguousarray(a).view(np.uint8).reshape(a.shape[0], w)
+        out = orc.filter(rows, gin.filter_preds(p["schema"], p["filters"]))
+        assert out.shape[0] == ref["n"]
+        assert sha(out) == ref["sha256"]
+    elif op == "project":
+        a = inputs["in"]
+        cols = gin.schema_columns(p["schema"])
+        w = sum(cw for _, _, cw in cols)
+        rows = np.ascontiguousarray(a).view(np.uint8).reshape(a.shape[0], w)
+        out = orc.project(rows, [(cols[int(i)][1], cols[int(i)][2]) for i in p["projection"].split(",")])
+        assert out.size == ref["bytes"]
+        assert sha(out) == ref["sha256"]
     else:
         pytest.fail(f"unknown op {op}")
