@@ -1123,6 +1123,125 @@ def run_plan(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Filter fused into the probe (bench.py --op filterjoin): the headline 16M x
+# 256M join with a Filter on the probe side (payload < 2^30, half the probe
+# tuples pass). Timed: the fused probe (pg_hashjoin_probe_where), the same
+# work as filter then probe, and pg_filter / pg_project alone.
+# ---------------------------------------------------------------------------
+def run_filterjoin(args, ws, rank, local):
+    import torch
+    from pythia_gb300 import gpu
+    torch.cuda.set_device(local)
+    threads = host_threads()
+    ctx = make_ctx(args, local)
+    L = gpu.lib()
+    hR, R = _pinned_array(ctx, L, NR)
+    hS, S = _pinned_array(ctx, L, NS)
+    make_inputs(R, S, threads)
+    dR, dS = ctx.alloc(NR * TUPLE), ctx.alloc(NS * TUPLE)
+    dT, dO = ctx.alloc(NS * TUPLE), ctx.alloc(NS * TUPLE)
+    ctx._check(L.pg_h2d(ctx.h, ctx.stream, dR.ptr, hR, NR * TUPLE))
+    ctx._check(L.pg_h2d(ctx.h, ctx.stream, dS.ptr, hS, NS * TUPLE))
+    ctx.sync()
+    rR = gpu.Rel(dR.ptr, NR, TUPLE, 0, 8)
+    rS = gpu.Rel(dS.ptr, NS, TUPLE, 0, 8)
+    proj, nproj = gpu.cols((("P", 8, 8), ("B", 8, 8)))
+    where, nwhere = gpu.preds([("long", "<", 8, 1 << 30)])
+    pcols = (gpu.Col * 2)(gpu.Col(0, 8, 8), gpu.Col(0, 0, 8))
+    ht = ctypes.c_void_p()
+    ctx._check(L.pg_hashjoin_build(ctx.h, ctx.stream, ctypes.byref(rR), proj, nproj, ctypes.byref(ht)))
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    res = gpu.JoinResult()
+    m = ctypes.c_uint64()
+    MAT = gpu.JOIN_MATERIALIZE
+
+    def fused():
+        ctx._check(L.pg_hashjoin_probe_where(ctx.h, ctx.stream, ht.value, ctypes.byref(rS), where, nwhere, proj, nproj,
+                                             dO.ptr, NS, MAT, -1, ctypes.byref(res)))
+
+    def unfused():
+        ctx._check(L.pg_filter(ctx.h, ctx.stream, ctypes.byref(rS), where, nwhere, dT.ptr, ctypes.byref(m)))
+        rT = gpu.Rel(dT.ptr, m.value, TUPLE, 0, 8)
+        ctx._check(L.pg_hashjoin_probe(ctx.h, ctx.stream, ht.value, ctypes.byref(rT), proj, nproj,
+                                       dO.ptr, NS, MAT, -1, ctypes.byref(res)))
+
+    def filter_only():
+        ctx._check(L.pg_filter(ctx.h, ctx.stream, ctypes.byref(rS), where, nwhere, dT.ptr, ctypes.byref(m)))
+
+    def project_only():
+        ctx._check(L.pg_project(ctx.h, ctx.stream, ctypes.byref(rS), pcols, 2, dT.ptr))
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ctx.sync()
+        barrier(ws)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return max_over_ranks(ws, e0.elapsed_time(e1) / args.steps)
+
+    k0 = gpu.kernel_launches()
+    clocks = Clocks(local)
+    clocks.start()
+    ms_fused = timed(fused)
+    clk = clocks.stop()
+    launches = (gpu.kernel_launches() - k0) * args.steps // (args.steps + args.warmup)
+    n_fused = res.n_out
+    ms_unfused = timed(unfused)
+    n_unfused = res.n_out
+    ms_filter = timed(filter_only)
+    n_filter = m.value
+    ms_project = timed(project_only)
+    # Parity: every probe key is in R (keys 1..|R|), so the rows are exactly
+    # the probe tuples passing the filter; count and build-payload sums of
+    # both paths agree with the host's count.
+    want = int((S[:, 1] < (1 << 30)).sum())
+    fl = gpu.JOIN_COUNT | gpu.JOIN_SUM
+    r1, r2 = gpu.JoinResult(), gpu.JoinResult()
+    ctx._check(L.pg_hashjoin_probe_where(ctx.h, ctx.stream, ht.value, ctypes.byref(rS), where, nwhere, proj, nproj,
+                                         None, 0, fl, 1, ctypes.byref(r1)))
+    ctx._check(L.pg_filter(ctx.h, ctx.stream, ctypes.byref(rS), where, nwhere, dT.ptr, ctypes.byref(m)))
+    rT = gpu.Rel(dT.ptr, m.value, TUPLE, 0, 8)
+    ctx._check(L.pg_hashjoin_probe(ctx.h, ctx.stream, ht.value, ctypes.byref(rT), proj, nproj, None, 0, fl, 1,
+                                   ctypes.byref(r2)))
+    L.pg_hashtable_free(ctx.h, ht.value)
+    parity = {"rows": int(n_fused), "rows_ok": n_fused == n_unfused == n_filter == want,
+              "count_and_sum_equal": (r1.n_out, r1.sum) == (r2.n_out, r2.sum)}
+    peak, peak_kind = measured_peak()
+    alg_probe = NS * 16 + want * 16                      # read the probe, write passing rows
+    alg_filter = NS * 16 + want * 16
+    alg_project = NS * 16 + NS * 16
+    gbs = lambda b, ms: b / (ms / 1e3) / 1e9
+    if rank == 0:
+        line = {"metric": "filtered probe tuples/s (16M build x 256M probe, Filter payload < 2^30 fused into the probe)",
+                "value": ws * NS / (ms_fused / 1e3), "unit": "tuples/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_fused, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded generator, resident in HBM)",
+                "config": {"workload": "probe of a prebuilt 16M-key table by 256M FK tuples through a Filter on "
+                                       "the probe payload (half pass)", "op": "filterjoin", "probe_tuples": NS,
+                           "l2": "inputs larger than L2; no flush"},
+                "unfused_filter_then_probe_ms": ms_unfused, "fused_speedup": ms_unfused / ms_fused,
+                "pg_filter": {"ms": ms_filter, "gbs": gbs(alg_filter, ms_filter), "frac": gbs(alg_filter, ms_filter) / peak,
+                              "algorithmic_bytes": alg_filter},
+                "pg_project": {"ms": ms_project, "gbs": gbs(alg_project, ms_project),
+                               "frac": gbs(alg_project, ms_project) / peak, "algorithmic_bytes": alg_project},
+                "parity": parity,
+                "roofline": {"bound": "hbm", "kernel": "k_probe16_deep<true> (filter fused)",
+                             "achieved": gbs(alg_probe, ms_fused), "peak": peak, "unit": "GB/s",
+                             "frac": gbs(alg_probe, ms_fused) / peak, "traffic": None, "peak_source": peak_kind,
+                             "algorithmic_bytes": alg_probe},
+                "gpu_launches": int(launches), "clocks": clk}
+        print(json.dumps(line), flush=True)
+    L.pg_host_free(ctx.h, hR)
+    L.pg_host_free(ctx.h, hS)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1134,7 +1253,7 @@ def main():
     ap.add_argument("--key-domain", default="dense", choices=["dense", "sparse"],
                     help="dense: keys 1..|R| (direct-mapped table); sparse: the same keys "
                          "multiplied by an odd constant (hashed table)")
-    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "batch", "serve", "tableimage", "plan"] + sorted(OPS))
+    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "batch", "serve", "tableimage", "plan", "filterjoin"] + sorted(OPS))
     ap.add_argument("--slots", type=int, default=8, help="worker slots for --op serve")
     ap.add_argument("--retune", action="store_true", help="rerun the autotuner for --op batch")
     ap.add_argument("--scale-down", type=int, default=0, help="divide --op sizes by 2^k")
@@ -1155,6 +1274,8 @@ def main():
         run_tableimage(args, ws, rank, local)
     elif args.op == "plan":
         run_plan(args, ws, rank, local)
+    elif args.op == "filterjoin":
+        run_filterjoin(args, ws, rank, local)
     elif args.op != "hashjoin":
         run_op(args, ws, rank, local, args.op)
     else:

@@ -10,7 +10,8 @@
 // writes each survivor at its tile offset plus its rank in input order (warp
 // ballots, then warp totals in shared memory). Both passes stream the input
 // once, so the traffic is two reads of the relation and one write of the
-// survivors. Project gathers columns tuple by tuple: one read, one write.
+// survivors. Project stages tiles in shared memory so that both its loads and
+// its stores are coalesced: one read, one write.
 #include "pg_pred.cuh"
 #include <algorithm>
 #include <cstring>
@@ -181,7 +182,61 @@ struct ProjCols {
 	uint32_t ow;                  // output words
 };
 
-__global__ void k_project(const uint32_t* __restrict__ in, uint64_t n, uint32_t iw, const ProjCols pc,
+// Tiles of up to PJ_TILE_WORDS input words (whole tuples): the block loads
+// the tile with consecutive threads on consecutive 16-byte vectors (or words
+// when the tuple is not a multiple of 16 bytes), then writes the tile's output
+// the same way, each output word read from shared memory through the
+// output-word -> input-word map.
+#define PJ_TILE_WORDS 8192
+#define PJ_MAX_WORDS 32
+__global__ void __launch_bounds__(256)
+k_project(const uint32_t* __restrict__ in, uint64_t n, uint32_t iw, const ProjCols pc,
+		uint32_t* __restrict__ out, bool vin, bool vout)
+{
+	__shared__ uint4 tile4[PJ_TILE_WORDS / 4];
+	__shared__ uint16_t map[PJ_MAX_WORDS * 2];
+	uint32_t* tile = reinterpret_cast<uint32_t*>(tile4);
+	if (threadIdx.x == 0) {
+		uint32_t k = 0;
+		for (int c = 0; c < pc.n; ++c)
+			for (uint32_t q = 0; q < pc.words[c]; ++q) map[k++] = (uint16_t) (pc.src[c] + q);
+	}
+	__syncthreads();
+	const uint32_t ow = pc.ow;
+	const uint32_t rpt = PJ_TILE_WORDS / iw;
+	const uint64_t ntiles = pg_div_up(n, rpt);
+	for (uint64_t tl = blockIdx.x; tl < ntiles; tl += gridDim.x) {
+		const uint64_t t0 = tl * rpt;
+		const uint32_t rows = (uint32_t) pg_min64(rpt, n - t0);
+		const uint32_t iwords = rows * iw, owords = rows * ow;
+		const uint32_t* src = in + t0 * iw;
+		if (vin) {
+			const uint4* s4 = reinterpret_cast<const uint4*>(src);
+			for (uint32_t i = threadIdx.x; i < iwords / 4; i += blockDim.x) tile4[i] = __ldcs(s4 + i);
+		} else {
+			for (uint32_t i = threadIdx.x; i < iwords; i += blockDim.x) tile[i] = __ldcs(src + i);
+		}
+		__syncthreads();
+		uint32_t* dst = out + t0 * ow;
+		if (vout) {
+			uint4* d4 = reinterpret_cast<uint4*>(dst);
+			for (uint32_t i = threadIdx.x; i < owords / 4; i += blockDim.x) {
+				const uint32_t t = 4 * i / ow, k = 4 * i - t * ow;
+				const uint32_t* r = tile + t * iw;
+				__stcs(d4 + i, make_uint4(r[map[k]], r[map[k + 1]], r[map[k + 2]], r[map[k + 3]]));
+			}
+		} else {
+			for (uint32_t i = threadIdx.x; i < owords; i += blockDim.x) {
+				const uint32_t t = i / ow, k = i - t * ow;
+				__stcs(dst + i, tile[t * iw + map[k]]);
+			}
+		}
+		__syncthreads();
+	}
+}
+
+// Tuples wider than PJ_MAX_WORDS words: one thread per tuple.
+__global__ void k_project_wide(const uint32_t* __restrict__ in, uint64_t n, uint32_t iw, const ProjCols pc,
 		uint32_t* __restrict__ out)
 {
 	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
@@ -216,8 +271,19 @@ extern "C" int pg_project(pg_ctx* ctx, pg_stream stream, const pg_rel* in, const
 	}
 	if (in->n == 0) return PG_OK;
 	cudaStream_t s = (cudaStream_t) stream;
-	const int grid = (int) std::min<uint64_t>(pg_div_up(in->n, 256), (uint64_t) ctx->sm_count * 16);
-	k_project<<<grid, 256, 0, s>>>((const uint32_t*) in->data, in->n, in->width / 4, pc, (uint32_t*) out);
+	const uint32_t iw = in->width / 4;
+	if (iw <= PJ_MAX_WORDS && pc.ow <= 2 * PJ_MAX_WORDS) {
+		// 32 KB of tile per block: up to 6 blocks per SM. Vectors when the
+		// tuples (and so every tile) start on 16-byte boundaries.
+		const bool vin = (iw & 3) == 0 && (reinterpret_cast<uintptr_t>(in->data) & 15) == 0;
+		const bool vout = (pc.ow & 3) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+		const uint64_t ntiles = pg_div_up(in->n, PJ_TILE_WORDS / iw);
+		const int grid = (int) std::min<uint64_t>(ntiles, (uint64_t) ctx->sm_count * 6);
+		k_project<<<grid, 256, 0, s>>>((const uint32_t*) in->data, in->n, iw, pc, (uint32_t*) out, vin, vout);
+	} else {
+		const int grid = (int) std::min<uint64_t>(pg_div_up(in->n, 256), (uint64_t) ctx->sm_count * 16);
+		k_project_wide<<<grid, 256, 0, s>>>((const uint32_t*) in->data, in->n, iw, pc, (uint32_t*) out);
+	}
 	PG_LAUNCHED(ctx);
 	return pg_check_status(ctx, s, "pg_project");
 }

@@ -1020,6 +1020,79 @@ k_probe16_deep(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 	if (lane == 0) atomicAdd(&agg[0], cnt_acc);
 }
 
+// Compacting form of the deep pipeline, for probes where a fraction of the
+// probe tuples yields rows (a Filter fused into the probe): each warp appends
+// its rows to a 512-row stage in shared memory and, before a chunk could
+// overflow it, reserves an output range with one atomicAdd on `cursor` and
+// writes the stage out with coalesced 16-byte stores. One pass, no positional
+// rows to compact afterwards; row order is unspecified (as for every join
+// output). Rows past `cap` are counted but not written.
+#define HJ_STAGE_ROWS 512
+template <bool PRED>
+__global__ void __launch_bounds__(PW_WARPS * 32, 3)
+k_probe16_stage(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb, uint32_t wsel,
+		char* __restrict__ out, uint64_t cap, unsigned long long* __restrict__ cursor, const PgPred16 pr)
+{
+	extern __shared__ uint4 hj_stage[];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	uint4* stage = hj_stage + warp * HJ_STAGE_ROWS;
+	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
+	const uint64_t W = (uint64_t) gridDim.x * PW_WARPS;
+	const uint64_t first = (uint64_t) blockIdx.x * PW_WARPS + warp;
+	const uint64_t keep = pg_policy_evict_last();
+	const uint64_t stream = pg_policy_evict_first();
+	const uint32_t w0 = wsel & 15, w1 = (wsel >> 4) & 15, w2 = (wsel >> 8) & 15, w3 = (wsel >> 12) & 15;
+	if (first >= nchunks) return;
+	auto rows_of = [&](uint64_t c) -> uint32_t { return (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK); };
+	auto load = [&](uint64_t c, uint4 (&t)[4]) {
+		const uint32_t rows = c < nchunks ? rows_of(c) : 0;
+		#pragma unroll
+		for (int j = 0; j < 4; ++j) {
+			const uint32_t p = j * 32 + lane;
+			t[j] = p < rows ? hj_ld_stream(S + (c * PW_CHUNK + p) * 16, stream) : make_uint4(0, 0, 0, 0);
+		}
+	};
+	uint32_t fill = 0;
+	auto flush = [&]() {
+		unsigned long long base = 0;
+		if (lane == 0) base = atomicAdd(cursor, (unsigned long long) fill);
+		base = __shfl_sync(0xffffffffu, base, 0);
+		__syncwarp();
+		for (uint32_t i = lane; i < fill; i += 32)
+			if (base + i < cap) hj_st_stream(out + (base + i) * 16, stage[i], stream);
+		__syncwarp();
+		fill = 0;
+	};
+	uint4 cur[4], nxt[4], nx2[4];
+	uint32_t ecur[4], enxt[4];
+	load(first, cur);
+	load(first + W, nxt);
+	hj_lookup4<PRED>(tb, cur, rows_of(first), lane, koff, keep, ecur, pr);
+	for (uint64_t c = first; c < nchunks; c += W) {
+		const uint64_t c1 = c + W, c2 = c + 2 * W;
+		if (c1 < nchunks) hj_lookup4<PRED>(tb, nxt, rows_of(c1), lane, koff, keep, enxt, pr);
+		load(c2, nx2);
+		uint32_t rank = 0;
+		#pragma unroll
+		for (int j = 0; j < 4; ++j) {
+			const bool h = ecur[j] != 0xFFFFFFFFu;
+			const uint32_t ball = __ballot_sync(0xffffffffu, h);
+			if (h) {
+				const uint64_t v = tb.vmin + ecur[j];
+				const uint4 t = cur[j];
+				stage[fill + rank + __popc(ball & ((1u << lane) - 1))] =
+					make_uint4(hj_pick(t, v, w0), hj_pick(t, v, w1), hj_pick(t, v, w2), hj_pick(t, v, w3));
+			}
+			rank += __popc(ball);
+		}
+		fill += rank;
+		if (fill > HJ_STAGE_ROWS - PW_CHUNK) flush();
+		#pragma unroll
+		for (int j = 0; j < 4; ++j) { cur[j] = nxt[j]; nxt[j] = nx2[j]; ecur[j] = enxt[j]; }
+	}
+	if (fill) flush();
+}
+
 // Positional probe output: the 128-tuple chunk c (rows_c = min(128, n - 128c)
 // probe tuples) holds lo = counts[c] & 0xffffffff rows at its front,
 // [128c, 128c + lo), and hi = counts[c] >> 32 rows at its back,
@@ -1462,9 +1535,15 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 							(ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] > 0 ? ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] : 72));
 					if (pred) {
 						const PgPred16 pr = *pred;
-						if (materialize && mode == 2 && wsel == 0x5432u)
-							k_probe16_deep<true><<<g5, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, out, counts, acc, pr);
-						else if (materialize && mode == 2)
+						if (materialize && mode == 2) {
+							// Compacting pipeline: rows land compact, nothing to move after.
+							const int ssmem = PW_WARPS * HJ_STAGE_ROWS * 16;
+							PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_stage<true>,
+									cudaFuncAttributeMaxDynamicSharedMemorySize, ssmem));
+							k_probe16_stage<true><<<g5, PW_WARPS * 32, ssmem, s>>>(S, n, koff, tb, wsel, out, cap, acc, pr);
+							PG_LAUNCHED(ctx);
+							return PG_OK;
+						} else if (materialize && mode == 2)
 							k_probe16_direct<true, 2, true, false, true><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb,
 									wsel, sum_w0, sum_words, out, counts, acc, -1, dlo, dhi, run, pr);
 						else if (materialize)
