@@ -1231,7 +1231,7 @@ def run_filterjoin(args, ws, rank, local):
                 "pg_project": {"ms": ms_project, "gbs": gbs(alg_project, ms_project),
                                "frac": gbs(alg_project, ms_project) / peak, "algorithmic_bytes": alg_project},
                 "parity": parity,
-                "roofline": {"bound": "hbm", "kernel": "k_probe16_deep<true> (filter fused)",
+                "roofline": {"bound": "hbm", "kernel": "k_probe16_stage<true, true> (filter fused, compacting stages)",
                              "achieved": gbs(alg_probe, ms_fused), "peak": peak, "unit": "GB/s",
                              "frac": gbs(alg_probe, ms_fused) / peak, "traffic": None, "peak_source": peak_kind,
                              "algorithmic_bytes": alg_probe},

@@ -91,6 +91,36 @@ k_filter_count(const char* __restrict__ in, uint64_t n, uint32_t w, const PgPred
 	}
 }
 
+// 16-byte tuples and numeric predicates: whole-tuple vector loads and the
+// predicates evaluated on the registers.
+__global__ void __launch_bounds__(FL_THREADS)
+k_filter_count16(const uint4* __restrict__ in, uint64_t n, const PgPred16 P, uint64_t* __restrict__ counts)
+{
+	__shared__ uint32_t wsum[FL_THREADS / 32];
+	const uint64_t base = (uint64_t) blockIdx.x * FL_TILE;
+	uint4 t[FL_ITEMS];
+	#pragma unroll
+	for (int j = 0; j < FL_ITEMS; ++j) {
+		const uint64_t i = base + j * FL_THREADS + threadIdx.x;
+		t[j] = i < n ? __ldcs(in + i) : make_uint4(0, 0, 0, 0);
+	}
+	uint32_t c = 0;
+	#pragma unroll
+	for (int j = 0; j < FL_ITEMS; ++j) {
+		const uint64_t i = base + j * FL_THREADS + threadIdx.x;
+		if (i < n && pg_pred16(P, t[j])) ++c;
+	}
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+	if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		uint32_t tot = 0;
+		for (int k = 0; k < FL_THREADS / 32; ++k) tot += wsum[k];
+		counts[blockIdx.x] = tot;
+	}
+}
+
 // vec: tuples start on 16-byte boundaries (width and both bases multiples of 16).
 __device__ __forceinline__ void fl_copy(char* __restrict__ dst, const char* __restrict__ src, uint32_t w, bool vec)
 {
@@ -103,31 +133,50 @@ __device__ __forceinline__ void fl_copy(char* __restrict__ dst, const char* __re
 	}
 }
 
-// Writes each tile's survivors at offs[tile] in input order.
-__global__ void __launch_bounds__(FL_THREADS)
-k_filter_write(const char* __restrict__ in, uint64_t n, uint32_t w, const PgPredSet P,
+// Writes each tile's survivors at offs[tile] in input order. All of a
+// thread's items are loaded (16-byte tuples into registers) and evaluated
+// before the block ranks them, so eight loads per thread are in flight and
+// the tile needs two barriers.
+// REG16 (with VEC16): the predicates are evaluated on the loaded registers.
+template <bool VEC16, bool REG16>
+__global__ void __launch_bounds__(FL_THREADS, 4)
+k_filter_write(const char* __restrict__ in, uint64_t n, uint32_t w, const PgPredSet P, const PgPred16 P16,
 		const uint64_t* __restrict__ offs, char* __restrict__ out, bool vec)
 {
-	__shared__ uint32_t wsum[FL_THREADS / 32];
+	__shared__ uint32_t cnt[FL_ITEMS][FL_THREADS / 32];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint64_t base = (uint64_t) blockIdx.x * FL_TILE;
-	uint64_t at = offs[blockIdx.x];
+	uint4 t[VEC16 ? FL_ITEMS : 1];
+	if (VEC16) {
+		#pragma unroll
+		for (int j = 0; j < FL_ITEMS; ++j) {
+			const uint64_t i = base + j * FL_THREADS + threadIdx.x;
+			t[VEC16 ? j : 0] = i < n ? __ldcs(reinterpret_cast<const uint4*>(in) + i) : make_uint4(0, 0, 0, 0);
+		}
+	}
+	uint32_t ball[FL_ITEMS];
+	#pragma unroll
 	for (int j = 0; j < FL_ITEMS; ++j) {
 		const uint64_t i = base + j * FL_THREADS + threadIdx.x;
-		const bool f = i < n && pg_pred_eval(P, in + i * w);
-		const uint32_t b = __ballot_sync(0xffffffffu, f);
-		if (lane == 0) wsum[warp] = __popc(b);
-		__syncthreads();
-		uint32_t before = 0, total = 0;
-		#pragma unroll
-		for (int k = 0; k < FL_THREADS / 32; ++k) {
-			const uint32_t s = wsum[k];
-			before += k < warp ? s : 0;
-			total += s;
-		}
-		if (f) fl_copy(out + (at + before + __popc(b & ((1u << lane) - 1))) * w, in + i * w, w, vec);
-		at += total;
-		__syncthreads();
+		ball[j] = __ballot_sync(0xffffffffu, i < n && (REG16 ? pg_pred16(P16, t[VEC16 ? j : 0])
+				: pg_pred_eval(P, in + i * w)));
+		if (lane == 0) cnt[j][warp] = __popc(ball[j]);
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		uint32_t run = 0;
+		for (int j = 0; j < FL_ITEMS; ++j)
+			for (int k = 0; k < FL_THREADS / 32; ++k) { const uint32_t c = cnt[j][k]; cnt[j][k] = run; run += c; }
+	}
+	__syncthreads();
+	const uint64_t at = offs[blockIdx.x];
+	#pragma unroll
+	for (int j = 0; j < FL_ITEMS; ++j) {
+		if (!((ball[j] >> lane) & 1)) continue;
+		const uint64_t i = base + j * FL_THREADS + threadIdx.x;
+		const uint64_t o = at + cnt[j][warp] + __popc(ball[j] & ((1u << lane) - 1));
+		if (VEC16) __stcs(reinterpret_cast<uint4*>(out) + o, t[VEC16 ? j : 0]);
+		else fl_copy(out + o * w, in + i * w, w, vec);
 	}
 }
 
@@ -161,10 +210,23 @@ extern "C" int pg_filter(pg_ctx* ctx, pg_stream stream, const pg_rel* in, const 
 		PG_CUDA(ctx, cudaStreamSynchronize(s));     // `host` leaves scope
 		P.chars = chars;
 	}
-	k_filter_count<<<(unsigned) ntiles, FL_THREADS, 0, s>>>((const char*) in->data, in->n, w, P, offs);
+	PgPred16 P16;
+	const bool reg16 = vec && w == 16 && pg_pred_as16(preds, npred, &P16);
+	if (reg16)
+		k_filter_count16<<<(unsigned) ntiles, FL_THREADS, 0, s>>>((const uint4*) in->data, in->n, P16, offs);
+	else
+		k_filter_count<<<(unsigned) ntiles, FL_THREADS, 0, s>>>((const char*) in->data, in->n, w, P, offs);
 	PG_LAUNCHED(ctx);
 	if ((rc = pg_scan_u64(ctx, s, offs, ntiles, offs + ntiles))) return rc;
-	k_filter_write<<<(unsigned) ntiles, FL_THREADS, 0, s>>>((const char*) in->data, in->n, w, P, offs, (char*) out, vec);
+	if (reg16)
+		k_filter_write<true, true><<<(unsigned) ntiles, FL_THREADS, 0, s>>>((const char*) in->data, in->n, w, P, P16,
+				offs, (char*) out, vec);
+	else if (vec && w == 16)
+		k_filter_write<true, false><<<(unsigned) ntiles, FL_THREADS, 0, s>>>((const char*) in->data, in->n, w, P, P16,
+				offs, (char*) out, vec);
+	else
+		k_filter_write<false, false><<<(unsigned) ntiles, FL_THREADS, 0, s>>>((const char*) in->data, in->n, w, P, P16,
+				offs, (char*) out, vec);
 	PG_LAUNCHED(ctx);
 	uint64_t total = 0;
 	PG_CUDA(ctx, cudaMemcpyAsync(&total, offs + ntiles, 8, cudaMemcpyDeviceToHost, s));

@@ -1028,7 +1028,8 @@ k_probe16_deep(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 // rows to compact afterwards; row order is unspecified (as for every join
 // output). Rows past `cap` are counted but not written.
 #define HJ_STAGE_ROWS 512
-template <bool PRED>
+// STD: (P$1, B$1) rows, picked without the word selector.
+template <bool PRED, bool STD>
 __global__ void __launch_bounds__(PW_WARPS * 32, 3)
 k_probe16_stage(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb, uint32_t wsel,
 		char* __restrict__ out, uint64_t cap, unsigned long long* __restrict__ cursor, const PgPred16 pr)
@@ -1080,8 +1081,9 @@ k_probe16_stage(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjP
 			if (h) {
 				const uint64_t v = tb.vmin + ecur[j];
 				const uint4 t = cur[j];
-				stage[fill + rank + __popc(ball & ((1u << lane) - 1))] =
-					make_uint4(hj_pick(t, v, w0), hj_pick(t, v, w1), hj_pick(t, v, w2), hj_pick(t, v, w3));
+				stage[fill + rank + __popc(ball & ((1u << lane) - 1))] = STD
+					? make_uint4(t.z, t.w, (uint32_t) v, (uint32_t) (v >> 32))
+					: make_uint4(hj_pick(t, v, w0), hj_pick(t, v, w1), hj_pick(t, v, w2), hj_pick(t, v, w3));
 			}
 			rank += __popc(ball);
 		}
@@ -1538,9 +1540,17 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 						if (materialize && mode == 2) {
 							// Compacting pipeline: rows land compact, nothing to move after.
 							const int ssmem = PW_WARPS * HJ_STAGE_ROWS * 16;
-							PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_stage<true>,
-									cudaFuncAttributeMaxDynamicSharedMemorySize, ssmem));
-							k_probe16_stage<true><<<g5, PW_WARPS * 32, ssmem, s>>>(S, n, koff, tb, wsel, out, cap, acc, pr);
+							if (wsel == 0x5432u) {
+								PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_stage<true, true>,
+										cudaFuncAttributeMaxDynamicSharedMemorySize, ssmem));
+								k_probe16_stage<true, true><<<g5, PW_WARPS * 32, ssmem, s>>>(S, n, koff, tb, wsel, out,
+										cap, acc, pr);
+							} else {
+								PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_stage<true, false>,
+										cudaFuncAttributeMaxDynamicSharedMemorySize, ssmem));
+								k_probe16_stage<true, false><<<g5, PW_WARPS * 32, ssmem, s>>>(S, n, koff, tb, wsel, out,
+										cap, acc, pr);
+							}
 							PG_LAUNCHED(ctx);
 							return PG_OK;
 						} else if (materialize && mode == 2)
