@@ -123,51 +123,90 @@ k_run_write(const pg_rec* __restrict__ rec, uint64_t n, const uint64_t* __restri
 }
 
 // For every build run: matching probe run (or none), output count, and the
-// folded count/sum contribution. Run keys are sorted on both sides, so each
-// thread merges MJ_MATCH consecutive build runs against the probe run keys:
-// one binary search for its first key, then a forward walk.
-#define MJ_MATCH 16
-__global__ void k_match_runs(MjSide R, MjSide S, const long long* __restrict__ RK, const long long* __restrict__ SK,
+// folded count/sum contribution. A warp takes MJ_WARP_RUNS consecutive build
+// runs: one lane finds the window of probe runs whose keys lie in the batch's
+// key range (two binary searches), then the lanes take consecutive build runs
+// (coalesced reads of keys and starts, coalesced count/match writes) and
+// binary-search their key inside the window, which stays in L1. The summed
+// column of a matched run is added by its lane when the run is short, and by
+// the whole warp (strided loads, shuffle reduction) when it is long, so skewed
+// keys do not serialise on one lane.
+#define MJ_WARP_RUNS 512
+#define MJ_SHORT_RUN 64
+
+__device__ __forceinline__ uint64_t mj_lower(const long long* __restrict__ K, uint64_t lo, uint64_t hi, long long k)
+{
+	while (lo < hi) {
+		const uint64_t mid = (lo + hi) >> 1;
+		if (K[mid] < k) lo = mid + 1; else hi = mid;
+	}
+	return lo;
+}
+
+__global__ void __launch_bounds__(256)
+k_match_runs(MjSide R, MjSide S, const long long* __restrict__ RK, const long long* __restrict__ SK,
 		MjCols pc, int sum_col, uint64_t* __restrict__ counts, uint64_t* __restrict__ match,
 		unsigned long long* __restrict__ agg)
 {
+	const int lane = threadIdx.x & 31;
+	const uint64_t gwarp = ((uint64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const uint64_t nwarps = ((uint64_t) gridDim.x * blockDim.x) >> 5;
+	const bool sum_r = sum_col >= 0 && pc.side[sum_col] == 0, sum_s = sum_col >= 0 && pc.side[sum_col] != 0;
+	const uint32_t soff = sum_col >= 0 ? pc.off[sum_col] : 0, swords = sum_col >= 0 ? pc.words[sum_col] : 0;
 	unsigned long long sum_acc = 0;
-	for (uint64_t t = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; t * MJ_MATCH < R.nruns;
-			t += (uint64_t) gridDim.x * blockDim.x) {
-		const uint64_t u0 = t * MJ_MATCH, u1 = pg_min64(R.nruns, u0 + MJ_MATCH);
-		uint64_t lo = 0, hi = S.nruns;
-		const long long k0 = RK[u0];
-		while (lo < hi) {
-			const uint64_t mid = (lo + hi) >> 1;
-			if (SK[mid] < k0) lo = mid + 1; else hi = mid;
+	for (uint64_t u0 = gwarp * MJ_WARP_RUNS; u0 < R.nruns; u0 += nwarps * MJ_WARP_RUNS) {
+		const uint64_t u1 = pg_min64(R.nruns, u0 + MJ_WARP_RUNS);
+		uint64_t slo = 0, shi = 0;
+		if (lane == 0) {
+			slo = mj_lower(SK, 0, S.nruns, RK[u0]);
+			const long long klast = RK[u1 - 1];
+			shi = klast == LLONG_MAX ? S.nruns : mj_lower(SK, slo, S.nruns, klast + 1);
 		}
-		for (uint64_t u = u0; u < u1; ++u) {
-		const uint64_t r0 = R.run_start[u], r1 = R.run_start[u + 1];
-		const long long k = RK[u];
-		while (lo < S.nruns && SK[lo] < k) ++lo;
-		uint64_t c = 0;
-		match[u] = UINT64_MAX;
-		if (lo < S.nruns && SK[lo] == k) {
-			const uint64_t s0 = S.run_start[lo], s1 = S.run_start[lo + 1];
-			c = (r1 - r0) * (s1 - s0);
-			match[u] = lo;
-			if (sum_col >= 0) {
-				unsigned long long part = 0;
-				if (pc.side[sum_col] == 0) {
-					for (uint64_t i = r0; i < r1; ++i) part += mj_col64(R, R.rec[i], pc.off[sum_col], pc.words[sum_col]);
-					sum_acc += part * (unsigned long long) (s1 - s0);
-				} else {
-					for (uint64_t i = s0; i < s1; ++i) part += mj_col64(S, S.rec[i], pc.off[sum_col], pc.words[sum_col]);
-					sum_acc += part * (unsigned long long) (r1 - r0);
+		slo = __shfl_sync(0xffffffffu, slo, 0);
+		shi = __shfl_sync(0xffffffffu, shi, 0);
+		for (uint64_t j = u0; j < u1; j += 32) {
+			const uint64_t u = j + lane;
+			const bool valid = u < u1;
+			uint64_t c = 0, m = UINT64_MAX, lo_i = 0, hi_i = 0, other = 0;
+			if (valid) {
+				const long long k = RK[u];
+				const uint64_t v = mj_lower(SK, slo, shi, k);
+				if (v < shi && SK[v] == k) {
+					const uint64_t r0 = R.run_start[u], r1 = R.run_start[u + 1];
+					const uint64_t s0 = S.run_start[v], s1 = S.run_start[v + 1];
+					c = (r1 - r0) * (s1 - s0);
+					m = v;
+					if (sum_r) { lo_i = r0; hi_i = r1; other = s1 - s0; }
+					else if (sum_s) { lo_i = s0; hi_i = s1; other = r1 - r0; }
 				}
+				counts[u] = c;
+				match[u] = m;
 			}
-		}
-		counts[u] = c;
+			if (sum_col < 0) continue;
+			const MjSide& sd = sum_r ? R : S;
+			const bool longrun = hi_i - lo_i > MJ_SHORT_RUN;
+			if (!longrun && hi_i > lo_i) {
+				unsigned long long part = 0;
+				for (uint64_t i = lo_i; i < hi_i; ++i) part += mj_col64(sd, sd.rec[i], soff, swords);
+				sum_acc += part * (unsigned long long) other;
+			}
+			uint32_t longs = __ballot_sync(0xffffffffu, longrun);
+			while (longs) {
+				const int l = __ffs(longs) - 1;
+				longs &= longs - 1;
+				const uint64_t a = __shfl_sync(0xffffffffu, lo_i, l), b = __shfl_sync(0xffffffffu, hi_i, l);
+				const uint64_t o = __shfl_sync(0xffffffffu, other, l);
+				unsigned long long part = 0;
+				for (uint64_t i = a + lane; i < b; i += 32) part += mj_col64(sd, sd.rec[i], soff, swords);
+				#pragma unroll
+				for (int q = 16; q > 0; q >>= 1) part += __shfl_xor_sync(0xffffffffu, part, q);
+				if (lane == 0) sum_acc += part * (unsigned long long) o;
+			}
 		}
 	}
 	#pragma unroll
 	for (int o = 16; o > 0; o >>= 1) sum_acc += __shfl_down_sync(0xffffffffu, sum_acc, o);
-	if ((threadIdx.x & 31) == 0 && sum_acc) atomicAdd(agg, sum_acc);
+	if (lane == 0 && sum_acc) atomicAdd(agg, sum_acc);
 }
 
 #define MJ_PER_THREAD 8
@@ -282,8 +321,9 @@ extern "C" int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, cons
 	if ((rc = pg_alloc_async(ctx, s, (void**) &match, (RS.nruns + 1) * 8))) return rc;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &acc, 16))) return rc;
 	PG_CUDA(ctx, cudaMemsetAsync(acc, 0, 16, s));
-	int blocks = (int) std::min<uint64_t>(pg_div_up(pg_div_up(RS.nruns, MJ_MATCH), 256), (uint64_t) ctx->sm_count * 16);
-	k_match_runs<<<blocks, 256, 0, s>>>(RS, SS, rk, sk, pc, sum_col, counts, match, acc + 1);
+	// One warp per MJ_WARP_RUNS build runs, 8 warps per CTA.
+	int blocks = (int) std::min<uint64_t>(pg_div_up(pg_div_up(RS.nruns, MJ_WARP_RUNS), 8), (uint64_t) ctx->sm_count * 16);
+	k_match_runs<<<std::max(blocks, 1), 256, 0, s>>>(RS, SS, rk, sk, pc, sum_col, counts, match, acc + 1);
 	PG_LAUNCHED(ctx);
 	if ((rc = pg_scan_u64(ctx, s, counts, RS.nruns, (uint64_t*) acc))) return rc;
 	unsigned long long h[2];

@@ -22,6 +22,20 @@
 #define PART_MAX_BUCKETS 4096
 #define PART_TILE_BYTES (20 * 1024)     // measured best: 4 CTAs per SM
 
+// Bucket of the key at p: the radix function (parammodulo, the sort's
+// digits) inlined when FN says so, else the general bucket function.
+#define PART_FN_ANY (-1)
+template <int FN>
+__device__ __forceinline__ uint32_t part_bucket(const pg_hashfn& f, const char* p, uint32_t kbytes)
+{
+	if (FN == PG_FN_PARAMMODULO) {
+		const int64_t v = pg_load_key(p, kbytes);
+		return (uint32_t) (((v - f.min) & f.k) >> f.skipbits);
+	}
+	return pg_hash_field(f, p, kbytes);
+}
+
+template <int FN>
 __global__ void k_part_hist(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff,
 		uint32_t kbytes, pg_hashfn f, uint32_t tile, uint64_t tiles_per_cta,
 		uint64_t* __restrict__ counts, uint32_t G, int* __restrict__ status)
@@ -34,7 +48,7 @@ __global__ void k_part_hist(const char* __restrict__ in, uint64_t n, uint32_t W,
 	uint64_t hi = std::min<uint64_t>(n, lo + tiles_per_cta * tile);
 	bool bad = false;
 	for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-		uint32_t b = pg_hash_field(f, in + i * W + koff, kbytes);
+		uint32_t b = part_bucket<FN>(f, in + i * W + koff, kbytes);
 		if (b < B) atomicAdd(&hist[b], 1u); else bad = true;
 	}
 	if (bad) pg_set_status(status, PG_ERR_ARG);
@@ -50,7 +64,8 @@ __device__ __forceinline__ void part_copy_words(uint32_t* dst, const uint32_t* s
 	for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
 }
 
-template <int NW>
+// NBITS > 0: the bucket index has exactly NBITS bits (ranking loop unrolled).
+template <int NW, int FN, int NBITS>
 __global__ void __launch_bounds__(NW * 32)
 k_part_scatter(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes,
 		pg_hashfn f, uint32_t tile, uint64_t tiles_per_cta, const uint64_t* __restrict__ offs,
@@ -73,7 +88,7 @@ k_part_scatter(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t kof
 	__shared__ uint32_t carry;
 
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-	const uint32_t nbits = B > 1 ? 32 - __clz(B - 1) : 0;
+	const uint32_t nbits = NBITS > 0 ? NBITS : (B > 1 ? 32 - __clz(B - 1) : 0);
 	const uint64_t first = (uint64_t) blockIdx.x * tiles_per_cta;
 	const uint64_t ntiles_total = pg_div_up(n, tile);
 	const uint64_t last = std::min<uint64_t>(ntiles_total, first + tiles_per_cta);
@@ -130,10 +145,11 @@ k_part_scatter(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t kof
 		for (uint32_t it = 0; it < sub; it += 32) {
 			uint32_t p = warp * sub + it + lane;
 			bool valid = p < rows;
-			uint32_t b = valid ? pg_hash_field(f, reinterpret_cast<const char*>(cur) + (uint64_t) p * W + koff, kbytes) : 0u;
+			uint32_t b = valid ? part_bucket<FN>(f, reinterpret_cast<const char*>(cur) + (uint64_t) p * W + koff, kbytes) : 0u;
 			if (valid && b >= B) { pg_set_status(status, PG_ERR_ARG); b = 0; }
 			uint32_t peers = __ballot_sync(0xffffffffu, valid);
-			for (uint32_t k = 0; k < nbits; ++k) {
+			#pragma unroll
+			for (uint32_t k = 0; k < (NBITS > 0 ? (uint32_t) NBITS : nbits); ++k) {
 				const bool on = (b >> k) & 1u;
 				const uint32_t m = __ballot_sync(0xffffffffu, on);
 				peers &= on ? m : ~m;
@@ -307,20 +323,26 @@ int pg_partition_fn(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, const pg_hash
 	int rc;
 	uint64_t* counts = nullptr;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &counts, (size_t) B * G * 8 + 8))) return rc;
-	k_part_hist<<<(unsigned) G, 512, B * sizeof(uint32_t), s>>>((const char*) in->data, n, W,
-			in->key_off, in->key_bytes, f, tile, tpc, counts, (uint32_t) G, ctx->d_status);
+	const bool radix = f.fn == PG_FN_PARAMMODULO;
+	if (radix)
+		k_part_hist<PG_FN_PARAMMODULO><<<(unsigned) G, 512, B * sizeof(uint32_t), s>>>((const char*) in->data, n, W,
+				in->key_off, in->key_bytes, f, tile, tpc, counts, (uint32_t) G, ctx->d_status);
+	else
+		k_part_hist<PART_FN_ANY><<<(unsigned) G, 512, B * sizeof(uint32_t), s>>>((const char*) in->data, n, W,
+				in->key_off, in->key_bytes, f, tile, tpc, counts, (uint32_t) G, ctx->d_status);
 	PG_LAUNCHED(ctx);
 	if ((rc = pg_scan_u64(ctx, s, counts, (uint64_t) B * G, nullptr))) return rc;
 	bool bulk_ok = ((reinterpret_cast<uintptr_t>(in->data) & 15) == 0) && (((uint64_t) tile * W) % 16 == 0);
-	if (NW == 8) {
-		PG_CUDA(ctx, cudaFuncSetAttribute(k_part_scatter<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
-		k_part_scatter<8><<<(unsigned) G, 256, smem, s>>>((const char*) in->data, n, W, in->key_off,
-				in->key_bytes, f, tile, tpc, counts, (uint32_t) G, (char*) out, bulk_ok, ctx->d_status);
-	} else {
-		PG_CUDA(ctx, cudaFuncSetAttribute(k_part_scatter<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
-		k_part_scatter<4><<<(unsigned) G, 128, smem, s>>>((const char*) in->data, n, W, in->key_off,
-				in->key_bytes, f, tile, tpc, counts, (uint32_t) G, (char*) out, bulk_ok, ctx->d_status);
-	}
+#define PS_LAUNCH(NWv, FNv, NB) do { \
+		PG_CUDA(ctx, cudaFuncSetAttribute(k_part_scatter<NWv, FNv, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)); \
+		k_part_scatter<NWv, FNv, NB><<<(unsigned) G, NWv * 32, smem, s>>>((const char*) in->data, n, W, in->key_off, \
+				in->key_bytes, f, tile, tpc, counts, (uint32_t) G, (char*) out, bulk_ok, ctx->d_status); } while (0)
+	// The sort's radix passes (parammodulo, 256 buckets) take the specialised
+	// kernel; everything else the general one.
+	if (NW == 8 && radix && B == 256) PS_LAUNCH(8, PG_FN_PARAMMODULO, 8);
+	else if (NW == 8) PS_LAUNCH(8, PART_FN_ANY, 0);
+	else PS_LAUNCH(4, PART_FN_ANY, 0);
+#undef PS_LAUNCH
 	PG_LAUNCHED(ctx);
 	// offsets[b] = first slot of bucket b = scanned count of (b, CTA 0).
 	// Strided copy: counts[b*G] for b < B, then n.

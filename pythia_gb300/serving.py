@@ -21,6 +21,7 @@ Host-side failures (an exception in one query's execution) are recorded for
 that query and the loop continues.
 """
 import ctypes
+import os
 import threading
 import time
 
@@ -39,10 +40,16 @@ class Table:
 
 
 class Catalog:
-    """Resident build tables (hash tables built once) and probe pools."""
+    """Resident build tables (hash tables built once) and probe pools.
 
-    def __init__(self, ctx, sizes, zipf=(0.0, 0.8), probe_factor=10, seed_base=500, threads=None):
+    With `images` (a directory written by save()), every table is loaded from
+    its table image (pg_hashtable_load) instead of being built: the warm start
+    of a server that keeps its tables across restarts. `table_seconds` is the
+    time spent building or loading the tables."""
+
+    def __init__(self, ctx, sizes, zipf=(0.0, 0.8), probe_factor=10, seed_base=500, threads=None, images=None):
         self.ctx, self.tables, self.resident_bytes = ctx, [], 0
+        self.table_seconds = 0.0
         L = gpu.lib()
         c, nc = gpu.cols(PROJ)
         self._cols = (c, nc)
@@ -54,7 +61,14 @@ class Catalog:
             dR = ctx.upload(R)
             rel = gpu.Rel(dR.ptr, r, 16, 0, 8)
             ht = ctypes.c_void_p()
-            ctx._check(L.pg_hashjoin_build(ctx.h, ctx.stream, ctypes.byref(rel), c, nc, ctypes.byref(ht)))
+            t0 = time.perf_counter()
+            if images:
+                ctx._check(L.pg_hashtable_load(ctx.h, ctx.stream, os.fsencode(self.image_path(images, t)),
+                                               ctypes.byref(ht)))
+            else:
+                ctx._check(L.pg_hashjoin_build(ctx.h, ctx.stream, ctypes.byref(rel), c, nc, ctypes.byref(ht)))
+            ctx.sync()
+            self.table_seconds += time.perf_counter() - t0
             pools = {}
             for s in zipf:
                 buf = ctx.alloc(16 * probe_factor * r)
@@ -67,6 +81,17 @@ class Catalog:
             self.tables.append(Table(t, r, groups, dR, ht.value, pools))
         self.probe_factor = probe_factor
         ctx.sync()
+
+    @staticmethod
+    def image_path(directory, tid):
+        return os.path.join(directory, f"table_{tid}.img")
+
+    def save(self, directory):
+        """Writes every table's image (pg_hashtable_save) into `directory`."""
+        os.makedirs(directory, exist_ok=True)
+        for t in self.tables:
+            self.ctx._check(gpu.lib().pg_hashtable_save(self.ctx.h, self.ctx.stream, t.ht,
+                                                        os.fsencode(self.image_path(directory, t.tid))))
 
     def close(self):
         for t in self.tables:

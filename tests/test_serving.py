@@ -102,3 +102,17 @@ def test_short_first_policy_serves_everything_with_same_results(ctx, catalog):
     assert all(q.error is None and q.end is not None for q in qb)
     for a, b in zip(qa, qb):
         _same(a.result, b.result)
+
+
+def test_warm_start_from_table_images(ctx, catalog, tmp_path):
+    # The catalog's tables written as images and a second catalog loaded from
+    # them (no builds): every query gives the same groups and sums.
+    catalog.save(str(tmp_path))
+    warm = serving.Catalog(ctx, [10_000, 31_000, 100_000, 320_000, 1_000_000], images=str(tmp_path))
+    try:
+        for q in _queries(10):
+            _same(serving.execute(ctx, ctx.stream, warm, q), serving.execute(ctx, ctx.stream, catalog, q))
+    finally:
+        warm.close()
+    with pytest.raises(gpu.PgError):
+        serving.Catalog(ctx, [10_000], images=str(tmp_path / "missing"))
