@@ -8,6 +8,9 @@
 // (mostfreqbuildkeyoccurances) and emitting the cartesian product of equal-key
 // groups.
 //
+// Count/sum joins whose key span is 2^13..2^24 values take the bucketed form
+// further down (high-bit sort + shared-memory merge of 4096-key buckets).
+//
 // GPU plan: sort both relations (pg_sort.cu), cut each sorted relation into
 // equal-key runs (stream compaction of run heads: run starts and run keys),
 // match build runs to probe runs by merging the two sorted run-key arrays, scan the per-run output counts |R_k|*|S_k|, and either fold
@@ -277,6 +280,181 @@ static int mj_runs(pg_ctx* ctx, cudaStream_t s, const pg_rec* rec, uint64_t n, u
 	return PG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Count/sum without materialising, for key spans of 2^13 .. 2^24 values: both
+// relations are sorted on the bits of (key - kmin) above the low 12 (one
+// stable radix partition each, 2..4096 buckets), and each bucket pair, 4096
+// consecutive key values, is merged in shared memory: per key, the tuples on
+// each side and the summed column; then sum over keys of |R_k| * |S_k| and
+// sum_R_k * |S_k| (or sum_S_k * |R_k|). This is the sort-merge of the
+// general path with its last radix digit, run detection and run matching
+// fused into one pass over both relations.
+// ---------------------------------------------------------------------------
+#define MJ_LOCAL_BITS 12
+#define MJ_LOCAL (1u << MJ_LOCAL_BITS)
+
+__device__ __forceinline__ unsigned long long mj_tuple_col(const char* t, uint32_t off, uint32_t words)
+{
+	const uint32_t* w = reinterpret_cast<const uint32_t*>(t + off);
+	if (words == 2) return ((unsigned long long) w[1] << 32) | w[0];
+	return (unsigned long long) (long long) (int32_t) w[0];
+}
+
+__global__ void __launch_bounds__(256)
+k_mj_bucket_join(const char* __restrict__ R, const uint64_t* __restrict__ roffs, uint32_t wR, uint32_t rkoff,
+		uint32_t rkb, const char* __restrict__ S, const uint64_t* __restrict__ soffs, uint32_t wS, uint32_t skoff,
+		uint32_t skb, long long kmin, int sum_side, uint32_t soff, uint32_t swords,
+		unsigned long long* __restrict__ agg)
+{
+	extern __shared__ __align__(16) unsigned char mj_smem[];
+	unsigned long long* sm = reinterpret_cast<unsigned long long*>(mj_smem);    // [MJ_LOCAL]
+	uint32_t* cR = reinterpret_cast<uint32_t*>(sm + MJ_LOCAL);                   // [MJ_LOCAL]
+	uint32_t* cS = cR + MJ_LOCAL;                                                // [MJ_LOCAL]
+	const uint32_t b = blockIdx.x;
+	for (uint32_t k = threadIdx.x; k < MJ_LOCAL; k += blockDim.x) { sm[k] = 0; cR[k] = 0; cS[k] = 0; }
+	__syncthreads();
+	const uint64_t r0 = roffs[b], r1 = roffs[b + 1], s0 = soffs[b], s1 = soffs[b + 1];
+	for (uint64_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+		const char* t = R + i * wR;
+		const uint32_t k = (uint32_t) ((unsigned long long) (pg_load_key(t + rkoff, rkb) - kmin) & (MJ_LOCAL - 1));
+		atomicAdd(&cR[k], 1u);
+		if (sum_side == 0) atomicAdd(&sm[k], mj_tuple_col(t, soff, swords));
+	}
+	for (uint64_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+		const char* t = S + i * wS;
+		const uint32_t k = (uint32_t) ((unsigned long long) (pg_load_key(t + skoff, skb) - kmin) & (MJ_LOCAL - 1));
+		atomicAdd(&cS[k], 1u);
+		if (sum_side == 1) atomicAdd(&sm[k], mj_tuple_col(t, soff, swords));
+	}
+	__syncthreads();
+	unsigned long long c = 0, sum = 0;
+	for (uint32_t k = threadIdx.x; k < MJ_LOCAL; k += blockDim.x) {
+		const unsigned long long a = cR[k], d = cS[k];
+		c += a * d;
+		if (sum_side == 0) sum += sm[k] * d;
+		else if (sum_side == 1) sum += sm[k] * a;
+	}
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		c += __shfl_down_sync(0xffffffffu, c, o);
+		sum += __shfl_down_sync(0xffffffffu, sum, o);
+	}
+	if ((threadIdx.x & 31) == 0) {
+		if (c) atomicAdd(&agg[0], c);
+		if (sum) atomicAdd(&agg[1], sum);
+	}
+}
+
+// offs[b] = first index of the sorted relation whose bucket (key - kmin) >>
+// MJ_LOCAL_BITS is >= b, for b in [0, B]; the relation is sorted on the bucket.
+__global__ void k_mj_bounds(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes,
+		long long kmin, uint32_t B, uint64_t* __restrict__ offs)
+{
+	const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+	if (b > B) return;
+	uint64_t lo = 0, hi = n;
+	while (lo < hi) {
+		const uint64_t mid = (lo + hi) >> 1;
+		const unsigned long long d = (unsigned long long) (pg_load_key(in + mid * W + koff, kbytes) - kmin);
+		if ((d >> MJ_LOCAL_BITS) < b) lo = mid + 1; else hi = mid;
+	}
+	offs[b] = lo;
+}
+
+__global__ void k_mj_minmax(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes,
+		unsigned long long* __restrict__ mm)
+{
+	unsigned long long lo = ~0ull, hi = 0;
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x) {
+		const unsigned long long u = (unsigned long long) pg_load_key(in + i * W + koff, kbytes) ^ (1ull << 63);
+		lo = u < lo ? u : lo;
+		hi = u > hi ? u : hi;
+	}
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		const unsigned long long a = __shfl_down_sync(0xffffffffu, lo, o), b = __shfl_down_sync(0xffffffffu, hi, o);
+		lo = a < lo ? a : lo;
+		hi = b > hi ? b : hi;
+	}
+	if ((threadIdx.x & 31) == 0) { atomicMin(&mm[0], lo); atomicMax(&mm[1], hi); }
+}
+
+// The fused count/sum above; *handled = false (nothing done) when the key span
+// is outside its range.
+static int mj_bucket_count_sum(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, const pg_rel* S, const MjCols& pc,
+		int sum_col, pg_join_result* res, bool* handled)
+{
+	*handled = false;
+	int rc;
+	unsigned long long* mm = nullptr;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 32))) return rc;
+	const unsigned long long init[4] = {~0ull, 0ull, 0ull, 0ull};
+	PG_CUDA(ctx, cudaMemcpyAsync(mm, init, 32, cudaMemcpyHostToDevice, s));
+	for (const pg_rel* r : {R, S}) {
+		const int blocks = (int) std::min<uint64_t>(pg_div_up(r->n, 256), (uint64_t) ctx->sm_count * 8);
+		k_mj_minmax<<<blocks, 256, 0, s>>>((const char*) r->data, r->n, r->width, r->key_off, r->key_bytes, mm);
+		PG_LAUNCHED(ctx);
+	}
+	unsigned long long h[2];
+	PG_CUDA(ctx, cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, s));
+	PG_CUDA(ctx, cudaStreamSynchronize(s));
+	const unsigned long long span = h[1] - h[0];
+	const int bits = span == 0 ? 0 : 64 - __builtin_clzll(span);
+	if (bits <= (int) MJ_LOCAL_BITS || bits > (int) MJ_LOCAL_BITS + 12) { pg_free_async(ctx, s, mm); return PG_OK; }
+	const long long kmin = (long long) (h[0] ^ (1ull << 63));
+	const int hb = bits - MJ_LOCAL_BITS;
+	const uint32_t B = 1u << hb;
+	// Stable radix passes over the bucket bits (one of up to 8 bits, or two
+	// halves of at most 6: the fast partition shapes), then the bucket
+	// bounds by binary search.
+	const int npass = hb <= 8 ? 1 : 2;
+	const int d0 = npass == 1 ? hb : hb / 2;
+	char *pR = nullptr, *pS = nullptr, *tmp = nullptr;
+	uint64_t *oR = nullptr, *oS = nullptr;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &pR, R->n * R->width))) return rc;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &pS, S->n * S->width))) return rc;
+	if (npass == 2 && (rc = pg_alloc_async(ctx, s, (void**) &tmp, std::max(R->n * R->width, S->n * S->width)))) return rc;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &oR, (B + 1) * 8))) return rc;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &oS, (B + 1) * 8))) return rc;
+	for (int side = 0; side < 2; ++side) {
+		const pg_rel* in = side ? S : R;
+		char* dst = side ? pS : pR;
+		pg_rel cur = *in;
+		for (int p = 0; p < npass; ++p) {
+			const int d = p == 0 ? d0 : hb - d0;
+			pg_hashfn f;
+			f.fn = PG_FN_PARAMMODULO;
+			f.skipbits = MJ_LOCAL_BITS + (p == 0 ? 0 : d0);
+			f.k = (int64_t) ((1u << d) - 1) << f.skipbits;
+			f.min = kmin;
+			f.max = 0; f.bucketrange = 0;
+			f.nbuckets = 1u << d;
+			char* o = (npass == 2 && p == 0) ? tmp : dst;
+			if ((rc = pg_partition_fn(ctx, s, &cur, f, o, nullptr))) return rc;
+			cur.data = o;
+		}
+		k_mj_bounds<<<(B + 256) / 256, 256, 0, s>>>(dst, in->n, in->width, in->key_off, in->key_bytes, kmin, B,
+				side ? oS : oR);
+		PG_LAUNCHED(ctx);
+	}
+	PG_CUDA(ctx, cudaMemsetAsync(mm + 2, 0, 16, s));
+	const int sum_side = sum_col < 0 ? -1 : (int) pc.side[sum_col];
+	const size_t smem = MJ_LOCAL * (8 + 4 + 4);
+	PG_CUDA(ctx, cudaFuncSetAttribute(k_mj_bucket_join, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+	k_mj_bucket_join<<<B, 256, smem, s>>>(pR, oR, R->width, R->key_off, R->key_bytes, pS, oS, S->width, S->key_off,
+			S->key_bytes, kmin, sum_side, sum_col >= 0 ? pc.off[sum_col] : 0, sum_col >= 0 ? pc.words[sum_col] : 0,
+			mm + 2);
+	PG_LAUNCHED(ctx);
+	unsigned long long o[2];
+	PG_CUDA(ctx, cudaMemcpyAsync(o, mm + 2, 16, cudaMemcpyDeviceToHost, s));
+	for (void* p : {(void*) pR, (void*) pS, (void*) tmp, (void*) oR, (void*) oS, (void*) mm}) pg_free_async(ctx, s, p);
+	if ((rc = pg_check_status(ctx, s, "pg_mpsm_join"))) return rc;
+	res->n_out = o[0];
+	res->sum = (int64_t) o[1];
+	*handled = true;
+	return PG_OK;
+}
+
 extern "C" int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, const pg_rel* S,
 		const pg_col* proj, int nproj, void* out, uint64_t out_capacity,
 		int flags, int sum_col, pg_join_result* res)
@@ -305,6 +483,11 @@ extern "C" int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, cons
 	if (R->n == 0 || S->n == 0) return PG_OK;
 	cudaStream_t s = (cudaStream_t) stream;
 	int rc;
+	if (!materialize && R->n < (1ull << 32) && S->n < (1ull << 32)) {
+		bool handled = false;
+		if ((rc = mj_bucket_count_sum(ctx, s, R, S, pc, sum_col, res, &handled))) return rc;
+		if (handled) return PG_OK;
+	}
 	pg_rec *rr = nullptr, *sr = nullptr;
 	if ((rc = pg_sort_records(ctx, s, R, &rr))) return rc;
 	if ((rc = pg_sort_records(ctx, s, S, &sr))) return rc;

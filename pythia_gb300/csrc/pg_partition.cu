@@ -337,9 +337,10 @@ int pg_partition_fn(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, const pg_hash
 		PG_CUDA(ctx, cudaFuncSetAttribute(k_part_scatter<NWv, FNv, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)); \
 		k_part_scatter<NWv, FNv, NB><<<(unsigned) G, NWv * 32, smem, s>>>((const char*) in->data, n, W, in->key_off, \
 				in->key_bytes, f, tile, tpc, counts, (uint32_t) G, (char*) out, bulk_ok, ctx->d_status); } while (0)
-	// The sort's radix passes (parammodulo, 256 buckets) take the specialised
+	// Radix passes (parammodulo) of 256 or 64 buckets take the specialised
 	// kernel; everything else the general one.
 	if (NW == 8 && radix && B == 256) PS_LAUNCH(8, PG_FN_PARAMMODULO, 8);
+	else if (NW == 8 && radix && B == 64) PS_LAUNCH(8, PG_FN_PARAMMODULO, 6);
 	else if (NW == 8) PS_LAUNCH(8, PART_FN_ANY, 0);
 	else PS_LAUNCH(4, PART_FN_ANY, 0);
 #undef PS_LAUNCH
