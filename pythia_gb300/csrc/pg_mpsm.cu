@@ -314,17 +314,35 @@ k_mj_bucket_join(const char* __restrict__ R, const uint64_t* __restrict__ roffs,
 	for (uint32_t k = threadIdx.x; k < MJ_LOCAL; k += blockDim.x) { sm[k] = 0; cR[k] = 0; cS[k] = 0; }
 	__syncthreads();
 	const uint64_t r0 = roffs[b], r1 = roffs[b + 1], s0 = soffs[b], s1 = soffs[b + 1];
-	for (uint64_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-		const char* t = R + i * wR;
-		const uint32_t k = (uint32_t) ((unsigned long long) (pg_load_key(t + rkoff, rkb) - kmin) & (MJ_LOCAL - 1));
-		atomicAdd(&cR[k], 1u);
-		if (sum_side == 0) atomicAdd(&sm[k], mj_tuple_col(t, soff, swords));
-	}
-	for (uint64_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
-		const char* t = S + i * wS;
-		const uint32_t k = (uint32_t) ((unsigned long long) (pg_load_key(t + skoff, skb) - kmin) & (MJ_LOCAL - 1));
-		atomicAdd(&cS[k], 1u);
-		if (sum_side == 1) atomicAdd(&sm[k], mj_tuple_col(t, soff, swords));
+	// Eight tuples per thread are loaded before their shared-memory updates,
+	// so eight loads are in flight per thread.
+	for (int side = 0; side < 2; ++side) {
+		const char* base = side ? S : R;
+		const uint64_t lo = side ? s0 : r0, hi = side ? s1 : r1;
+		const uint32_t w = side ? wS : wR, koff = side ? skoff : rkoff, kb = side ? skb : rkb;
+		uint32_t* cnt = side ? cS : cR;
+		const bool sums = sum_side == side;
+		for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += 8 * (uint64_t) blockDim.x) {
+			uint32_t k[8];
+			unsigned long long v[8];
+			#pragma unroll
+			for (int u = 0; u < 8; ++u) {
+				const uint64_t i = i0 + (uint64_t) u * blockDim.x;
+				k[u] = MJ_LOCAL;
+				v[u] = 0;
+				if (i < hi) {
+					const char* t = base + i * w;
+					k[u] = (uint32_t) ((unsigned long long) (pg_load_key(t + koff, kb) - kmin) & (MJ_LOCAL - 1));
+					if (sums) v[u] = mj_tuple_col(t, soff, swords);
+				}
+			}
+			#pragma unroll
+			for (int u = 0; u < 8; ++u) {
+				if (k[u] == MJ_LOCAL) continue;
+				atomicAdd(&cnt[k[u]], 1u);
+				if (sums) atomicAdd(&sm[k[u]], v[u]);
+			}
+		}
 	}
 	__syncthreads();
 	unsigned long long c = 0, sum = 0;
