@@ -464,6 +464,32 @@ def test_mpsm_reference_unit_tests(ctx):
     assert _mpsm_check(ctx, f("ones", 200), f("ones", 200)) == 40_000
 
 
+@pytest.mark.parametrize("span_bits", [13, 17, 21, 24])
+def test_mpsm_count_sum_bucketed_key_spans(ctx, span_bits):
+    # Count/sum joins with key spans of 2^13..2^24 take the bucketed merge (one
+    # radix pass of up to 8 bucket bits, or two halves); both summed sides,
+    # a hot key and negative keys included.
+    n = 300_000
+    R = dg.uniform_keys(n, 1 << span_bits, dg.seed_for(72 + span_bits))
+    S = dg.uniform_keys(n, 1 << span_bits, dg.seed_for(73 + span_bits))
+    R[::50, 0] = 77                                   # a hot key on both sides
+    S[::40, 0] = 77
+    R[:, 0] -= 1 << (span_bits - 1)
+    S[:, 0] -= 1 << (span_bits - 1)
+    proj = (("P", 8, 8), ("B", 8, 8))
+    for sc in (0, 1):
+        _, n2, s2 = ctx.mpsm(R, S, proj=proj, flags=gpu.JOIN_COUNT | gpu.JOIN_SUM, sum_col=sc)
+        _, wn2, ws2 = orc.mergejoin(R, S, proj=proj, materialise=False, sum_col=sc)
+        assert (n2, s2) == (wn2, ws2)
+    I = gin.make({"gen": "formula", "name": "int_pairs", "n": 60_000})
+    I[:, 0] %= 1 << 15
+    _, n3, s3 = ctx.mpsm(I, I, proj=(("P", 4, 4), ("B", 4, 4)), bkey=(0, 4), pkey=(0, 4),
+                         flags=gpu.JOIN_COUNT | gpu.JOIN_SUM, sum_col=1)
+    _, wn3, ws3 = orc.mergejoin(I, I, proj=(("P", 4, 4), ("B", 4, 4)), bkey=(0, 4), pkey=(0, 4),
+                                materialise=False, sum_col=1)
+    assert (n3, s3) == (wn3, ws3)
+
+
 def test_mpsm_duplicates(ctx):
     R = dg.uniform_keys(50_000, 12_500, dg.seed_for(70))
     S = dg.uniform_keys(50_000, 12_500, dg.seed_for(71))
