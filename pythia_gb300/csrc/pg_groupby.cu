@@ -452,13 +452,16 @@ __global__ void k_gb_emit(GbTable t, uint32_t kbytes, char* __restrict__ out, ui
 // atomic (or one integer reduction) and, for sums, a byte store marking the
 // group present.
 // ---------------------------------------------------------------------------
+// Min and max key over rows 0, step, 2 step, ... (step 1: every row).
 template <bool VEC16>
 __global__ void k_gb_key_minmax(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff,
-		uint32_t kbytes, unsigned long long* __restrict__ mm)
+		uint32_t kbytes, unsigned long long* __restrict__ mm, uint64_t step)
 {
 	unsigned long long lo = ~0ull, hi = 0;
 	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
-	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += stride) {
+	const uint64_t ns = pg_div_up(n, step);
+	for (uint64_t j = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; j < ns; j += stride) {
+		const uint64_t i = j * step;
 		int64_t k;
 		if (VEC16) {
 			const uint4 t = __ldg(reinterpret_cast<const uint4*>(in) + i);
@@ -483,10 +486,11 @@ __global__ void k_gb_key_minmax(const char* __restrict__ in, uint64_t n, uint32_
 template <int VT, int AGG, bool VEC16>
 __global__ void __launch_bounds__(GB_THREADS)
 k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes, uint32_t voff,
-		long long kmin, unsigned long long* __restrict__ acc, double* __restrict__ lo,
-		unsigned char* __restrict__ present)
+		long long kmin, uint64_t range, unsigned long long* __restrict__ acc, double* __restrict__ lo,
+		unsigned char* __restrict__ present, unsigned int* __restrict__ overflow)
 {
 	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	bool outside = false;
 	for (uint64_t base = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; base < n; base += stride * GBD_ILP) {
 		uint64_t d[GBD_ILP];
 		unsigned long long iv[GBD_ILP];
@@ -513,6 +517,7 @@ k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, u
 					: (uint64_t) pg_load_key(r + voff, 8);
 			}
 			d[j] = (uint64_t) k - (uint64_t) kmin;
+			if (d[j] >= range) { ok[j] = false; outside = true; d[j] = 0; continue; }   // key outside the table
 			if (AGG == PG_AGG_COUNT) iv[j] = 1;
 			else if (VT == PG_VAL_DEC) dv[j] = __longlong_as_double((long long) vbits);
 			else iv[j] = vbits;
@@ -543,6 +548,7 @@ k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, u
 			}
 		}
 	}
+	if (outside) *overflow = 1;
 }
 
 template <int VT, int AGG>
@@ -587,38 +593,22 @@ __global__ void k_gb_dense_emit(const unsigned long long* __restrict__ acc, cons
 
 // Runs the dense path when the key range allows it; *done = false leaves the
 // work to the hashed paths.
+// One dense aggregation over the key window [kmin, kmin + range): table, fill,
+// aggregation, emission. *overflow: some key lay outside the window (nothing
+// of this run is usable then).
 template <int VT, int AGG>
-static int gb_dense(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, uint64_t hint,
-		void* out, uint64_t out_cap, uint64_t* ngroups, bool* done)
+static int gb_dense_window(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, bool vec16, long long kmin,
+		uint64_t range, void* out, uint64_t out_cap, uint64_t* ngroups, bool* overflow)
 {
-	*done = false;
 	int rc;
-	const bool vec16 = in->width == 16 && (in->key_off == 0 || in->key_off == 8) && in->key_bytes == 8 &&
-		(reinterpret_cast<uintptr_t>(in->data) & 15) == 0 &&
-		(AGG == PG_AGG_COUNT || (VT == PG_VAL_INT ? (voff & 3) == 0 : (voff == 0 || voff == 8)));
-	unsigned long long* mm = nullptr;
-	if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 32))) return rc;
-	const unsigned long long init[2] = {~0ull, 0ull};
-	PG_CUDA(ctx, cudaMemcpyAsync(mm, init, 16, cudaMemcpyHostToDevice, s));
-	const int blocks = (int) std::min<uint64_t>(pg_div_up(in->n, 256), (uint64_t) ctx->sm_count * 8);
-	if (vec16) k_gb_key_minmax<true><<<blocks, 256, 0, s>>>((const char*) in->data, in->n, in->width, in->key_off, in->key_bytes, mm);
-	else k_gb_key_minmax<false><<<blocks, 256, 0, s>>>((const char*) in->data, in->n, in->width, in->key_off, in->key_bytes, mm);
-	PG_LAUNCHED(ctx);
-	unsigned long long h[2];
-	PG_CUDA(ctx, cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, s));
-	PG_CUDA(ctx, cudaStreamSynchronize(s));
-	pg_free_async(ctx, s, mm);
-	const long long kmin = (long long) (h[0] ^ (1ull << 63)), kmax = (long long) (h[1] ^ (1ull << 63));
-	const uint64_t range = (uint64_t) kmax - (uint64_t) kmin + 1;
-	const uint64_t limit = std::max<uint64_t>(4 * std::max<uint64_t>(hint, 1), std::min<uint64_t>(2 * in->n, 1ull << 22));
-	if (range == 0 || range > limit || range > (1ull << 28)) return PG_OK;
 	char* mem = nullptr;
-	const size_t bytes = range * 17 + 64;
+	const size_t bytes = range * 17 + 128;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &mem, bytes))) return rc;
 	unsigned long long* acc = reinterpret_cast<unsigned long long*>(mem);
 	double* lo = reinterpret_cast<double*>(acc + range);
 	unsigned long long* cursor = reinterpret_cast<unsigned long long*>(lo + range);
 	unsigned char* present = reinterpret_cast<unsigned char*>(cursor + 1);
+	unsigned int* oflag = reinterpret_cast<unsigned int*>((reinterpret_cast<uintptr_t>(present + range) + 15) & ~uintptr_t(15));
 	PG_CUDA(ctx, cudaMemsetAsync(mem, 0, bytes, s));
 	if (VT == PG_VAL_DEC && AGG == PG_AGG_SUM) {
 		// Interleaved (hi, lo) words start at -0.0 so that the first add of a
@@ -629,21 +619,86 @@ static int gb_dense(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff
 	}
 	const int gblocks = (int) std::min<uint64_t>(pg_div_up(in->n, (uint64_t) GB_THREADS * GBD_ILP), (uint64_t) ctx->sm_count * 8);
 	if (vec16) k_gb_dense<VT, AGG, true><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, in->width,
-			in->key_off, in->key_bytes, voff, kmin, acc, lo, present);
+			in->key_off, in->key_bytes, voff, kmin, range, acc, lo, present, oflag);
 	else k_gb_dense<VT, AGG, false><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, in->width,
-			in->key_off, in->key_bytes, voff, kmin, acc, lo, present);
+			in->key_off, in->key_bytes, voff, kmin, range, acc, lo, present, oflag);
 	PG_LAUNCHED(ctx);
 	const int eblocks = (int) std::min<uint64_t>(pg_div_up(range, 256), (uint64_t) ctx->sm_count * 8);
 	k_gb_dense_emit<VT, AGG><<<eblocks, 256, 0, s>>>(acc, lo, present, range, kmin, in->key_bytes, (char*) out,
 			out_cap, cursor);
 	PG_LAUNCHED(ctx);
-	unsigned long long ng = 0;
-	PG_CUDA(ctx, cudaMemcpyAsync(&ng, cursor, 8, cudaMemcpyDeviceToHost, s));
+	unsigned long long h[2] = {0, 0};
+	PG_CUDA(ctx, cudaMemcpyAsync(&h[0], cursor, 8, cudaMemcpyDeviceToHost, s));
+	PG_CUDA(ctx, cudaMemcpyAsync(&h[1], oflag, 4, cudaMemcpyDeviceToHost, s));
 	PG_CUDA(ctx, cudaStreamSynchronize(s));
 	pg_free_async(ctx, s, mem);
-	*ngroups = ng;
+	*ngroups = h[0];
+	*overflow = (h[1] & 0xFFFFFFFFull) != 0;
+	return PG_OK;
+}
+
+// Key range of rows 0, step, 2 step, ...: h[0], h[1] = min and max with the
+// sign bit flipped (unsigned order = signed order).
+static int gb_key_range(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, bool vec16, uint64_t step, unsigned long long* h)
+{
+	int rc;
+	unsigned long long* mm = nullptr;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 32))) return rc;
+	const unsigned long long init[2] = {~0ull, 0ull};
+	PG_CUDA(ctx, cudaMemcpyAsync(mm, init, 16, cudaMemcpyHostToDevice, s));
+	const uint64_t ns = pg_div_up(in->n, step);
+	const int blocks = (int) std::max<uint64_t>(1, std::min<uint64_t>(pg_div_up(ns, 256), (uint64_t) ctx->sm_count * 8));
+	if (vec16) k_gb_key_minmax<true><<<blocks, 256, 0, s>>>((const char*) in->data, in->n, in->width, in->key_off,
+			in->key_bytes, mm, step);
+	else k_gb_key_minmax<false><<<blocks, 256, 0, s>>>((const char*) in->data, in->n, in->width, in->key_off,
+			in->key_bytes, mm, step);
+	PG_LAUNCHED(ctx);
+	PG_CUDA(ctx, cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, s));
+	PG_CUDA(ctx, cudaStreamSynchronize(s));
+	pg_free_async(ctx, s, mm);
+	return PG_OK;
+}
+
+// Dense keys: slot = key - kmin. Large inputs first try a key window from a
+// sample of every 1024th row widened by an eighth on each side (no full
+// min/max pass); a key outside it sends the operator to the exact window.
+template <int VT, int AGG>
+static int gb_dense(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, uint64_t hint,
+		void* out, uint64_t out_cap, uint64_t* ngroups, bool* done)
+{
+	*done = false;
+	int rc;
+	const bool vec16 = in->width == 16 && (in->key_off == 0 || in->key_off == 8) && in->key_bytes == 8 &&
+		(reinterpret_cast<uintptr_t>(in->data) & 15) == 0 &&
+		(AGG == PG_AGG_COUNT || (VT == PG_VAL_INT ? (voff & 3) == 0 : (voff == 0 || voff == 8)));
+	const uint64_t limit = std::max<uint64_t>(4 * std::max<uint64_t>(hint, 1), std::min<uint64_t>(2 * in->n, 1ull << 22));
+	unsigned long long h[2];
+	if (in->n >= (1ull << 22)) {
+		if ((rc = gb_key_range(ctx, s, in, vec16, 1024, h))) return rc;
+		const unsigned long long span = h[1] - h[0];
+		const unsigned long long slack = span / 8 + 64;
+		const unsigned long long lo_u = h[0] > slack ? h[0] - slack : 0;
+		const unsigned long long hi_u = ~0ull - h[1] > slack ? h[1] + slack : ~0ull;
+		const uint64_t range = hi_u - lo_u + 1;
+		if (range != 0 && range <= limit && range <= (1ull << 28)) {
+			bool overflow = false;
+			if ((rc = gb_dense_window<VT, AGG>(ctx, s, in, voff, vec16, (long long) (lo_u ^ (1ull << 63)), range,
+					out, out_cap, ngroups, &overflow))) return rc;
+			if (!overflow) {
+				*done = true;
+				if (*ngroups > out_cap) return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_groupby: output capacity too small");
+				return pg_check_status(ctx, s, "pg_groupby");
+			}
+		}
+	}
+	if ((rc = gb_key_range(ctx, s, in, vec16, 1, h))) return rc;
+	const long long kmin = (long long) (h[0] ^ (1ull << 63)), kmax = (long long) (h[1] ^ (1ull << 63));
+	const uint64_t range = (uint64_t) kmax - (uint64_t) kmin + 1;
+	if (range == 0 || range > limit || range > (1ull << 28)) return PG_OK;
+	bool overflow = false;
+	if ((rc = gb_dense_window<VT, AGG>(ctx, s, in, voff, vec16, kmin, range, out, out_cap, ngroups, &overflow))) return rc;
 	*done = true;
-	if (ng > out_cap) return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_groupby: output capacity too small");
+	if (*ngroups > out_cap) return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_groupby: output capacity too small");
 	return pg_check_status(ctx, s, "pg_groupby");
 }
 

@@ -396,6 +396,27 @@ def test_hashjoin_groupby_unsupported_layouts(ctx):
     assert e.value.code == gpu.PG_ERR_UNSUPPORTED
 
 
+def test_groupby_key_window_from_sample(ctx):
+    # Inputs of 4M+ rows take the dense window from a sample of every 1024th
+    # row. Keys outside it (rows the sample skipped) send the operator to the
+    # exact window; keys the sample caught only widen it. Same groups either way.
+    n = (1 << 22) + 4097
+    rows = dg.uniform_keys(n, 5000, dg.seed_for(81))
+    rows[:, 1] = (rows[:, 1] % 1000).astype(np.float64).view(np.int64)
+    for outlier_at, key in ((1025, 7000), (2048, 9999), (n - 1, -3000)):
+        r = rows.copy()
+        r[outlier_at, 0] = key
+        got = ctx.groupby(r, val=(8, "dec"), agg="sum", groups_hint=5000)
+        want = orc.groupby_exact(r)
+        g, w = canon(got), canon(want)
+        assert np.array_equal(g[:, :8], w[:, :8])
+        gv, wv = g[:, 8:].copy().view(np.float64).ravel(), w[:, 8:].copy().view(np.float64).ravel()
+        assert np.all(np.abs(gv - wv) <= DEC_RTOL * np.abs(wv))
+    got = ctx.groupby(rows, val=(8, "long"), agg="count", groups_hint=5000)
+    assert np.array_equal(canon(got), canon(orc.groupby(rows, val=(8, "long"), agg="count",
+                                                        hash=orc.hashcfg("modulo", 1024))))
+
+
 def test_groupby_reference_unit_test(gbctx):
     ctx = gbctx
     # unit_tests/queryaggsum.cpp: group i holds 1..i; sum must be i(i+1)/2.
