@@ -1115,6 +1115,11 @@ def run_plan(args, ws, rank, local):
     clk = clocks.stop()
     launches = (gpu.kernel_launches() - k0) * args.steps // (args.steps + args.warmup)
     ms_off, rows_off, st_off = timed(False)
+    # Leaves in registered memory (a loader reading into pinned memory): their
+    # pages go to the device without the staging copy.
+    plans.register("O", O, pin=True); plans.register("P", P, pin=True); plans.register("L", L, pin=True)
+    ms_pin, rows_pin, st_pin = timed(True)
+    plans.register("O", O); plans.register("P", P); plans.register("L", L)
     plans.set_device_exchange(True)
     # Parity at full size: every line's price lands in its order's group.
     from oracle import oracle as orc
@@ -1130,6 +1135,8 @@ def run_plan(args, ws, rank, local):
         worst = max(worst, abs(d[int(k)] - ex) / abs(ex))
     parity = {"groups": int(g_on.shape[0]), "groups_ok": int(g_on.shape[0]) == PLAN_GROUPS,
               "same_groups_on_and_off": bool(np.array_equal(g_on[:, 0], g_off[:, 0])),
+              "same_groups_pinned_leaves": bool(np.array_equal(
+                  orc.canonical(rows_pin).view(np.int64).reshape(-1, 2)[:, 0], g_on[:, 0])),
               "sampled_group_max_rel_err": worst, "tolerance": 1e-12, "ok": worst <= 1e-12}
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -1156,7 +1163,9 @@ def run_plan(args, ws, rank, local):
                            "op": "plan", "timing": "wall clock per plan run, host relations in and host rows out",
                            "l2": "inputs larger than L2; no flush"},
                 "exchange_off_ms": ms_off, "exchange_speedup": ms_off / ms_on,
-                "transfer_bytes_per_run": {"exchange_on": st_on, "exchange_off": st_off},
+                "pinned_leaves_ms": ms_pin, "pinned_leaves_lines_per_s": ws * nL / (ms_pin / 1e3),
+                "transfer_bytes_per_run": {"exchange_on": st_on, "exchange_off": st_off,
+                                           "exchange_on_pinned_leaves": st_pin},
                 "parity": parity,
                 "e2e": {"value": value, "unit": "lines/s", "h2d_bytes_per_step": st_on["h2d"],
                         "d2h_bytes_per_step": st_on["d2h"]},

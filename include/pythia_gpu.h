@@ -103,6 +103,12 @@ int pg_buffer_alloc_async(pg_ctx* ctx, pg_stream stream, uint64_t bytes, void** 
 int pg_buffer_free_async(pg_ctx* ctx, pg_stream stream, void* dptr);
 int pg_host_alloc(pg_ctx* ctx, uint64_t bytes, void** hptr);   /* pinned */
 int pg_host_free(pg_ctx* ctx, void* hptr);
+/* Page-locks existing host memory (a relation a loader read into memory) so
+ * that copies from it run at the host link's rate; pg_host_is_pinned tells
+ * whether a host pointer lies in pinned or registered memory (1) or not (0). */
+int pg_host_register(pg_ctx* ctx, void* hptr, uint64_t bytes);
+int pg_host_unregister(pg_ctx* ctx, void* hptr);
+int pg_host_is_pinned(pg_ctx* ctx, const void* hptr);
 int pg_h2d(pg_ctx* ctx, pg_stream stream, void* dst, const void* src, uint64_t bytes);
 int pg_d2h(pg_ctx* ctx, pg_stream stream, void* dst, const void* src, uint64_t bytes);
 int pg_d2d(pg_ctx* ctx, pg_stream stream, void* dst, const void* src, uint64_t bytes);

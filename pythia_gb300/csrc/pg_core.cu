@@ -178,6 +178,28 @@ extern "C" int pg_host_alloc(pg_ctx* ctx, uint64_t bytes, void** p)
 	return PG_OK;
 }
 
+extern "C" int pg_host_register(pg_ctx* ctx, void* p, uint64_t bytes)
+{
+	if (!ctx || (!p && bytes)) return pg_fail(ctx, PG_ERR_ARG, "pg_host_register: null argument");
+	if (bytes) PG_CUDA(ctx, cudaHostRegister(p, bytes, cudaHostRegisterDefault));
+	return PG_OK;
+}
+
+extern "C" int pg_host_unregister(pg_ctx* ctx, void* p)
+{
+	if (!ctx) return PG_ERR_ARG;
+	if (p) PG_CUDA(ctx, cudaHostUnregister(p));
+	return PG_OK;
+}
+
+extern "C" int pg_host_is_pinned(pg_ctx* ctx, const void* p)
+{
+	if (!ctx || !p) return 0;
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return 0; }
+	return a.type == cudaMemoryTypeHost ? 1 : 0;
+}
+
 extern "C" int pg_host_free(pg_ctx* ctx, void* p)
 {
 	if (!ctx) return PG_ERR_ARG;

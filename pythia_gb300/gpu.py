@@ -66,7 +66,8 @@ SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_st
            "pg_generate_fk", "pg_buffer_alloc_async", "pg_buffer_free_async", "pg_generate_zipf_fk",
            "pg_hashjoin_groupby", "pg_stream_create_urgent", "pg_autotune_batch",
            "pg_hashtable_image_size", "pg_hashtable_serialize", "pg_hashtable_deserialize",
-           "pg_hashtable_save", "pg_hashtable_load", "pg_filter", "pg_project", "pg_hashjoin_probe_where"]
+           "pg_hashtable_save", "pg_hashtable_load", "pg_filter", "pg_project", "pg_hashjoin_probe_where",
+           "pg_host_register", "pg_host_unregister", "pg_host_is_pinned"]
 TUNE = {"probe_ctas_per_sm": 0, "probe_variant": 1, "dense": 2, "partition_tile": 3,
         "groupby_smem_groups": 4, "radix_bits": 5, "probe_items": 6, "probe_cache": 7, "probe_passes": 8, "groupby_path": 9}
 
@@ -95,6 +96,9 @@ def lib():
             "pg_buffer_free": ([vp, vp], ci),
             "pg_host_alloc": ([vp, u64, P(vp)], ci),
             "pg_host_free": ([vp, vp], ci),
+            "pg_host_register": ([vp, vp, u64], ci),
+            "pg_host_unregister": ([vp, vp], ci),
+            "pg_host_is_pinned": ([vp, vp], ci),
             "pg_h2d": ([vp, vp, vp, vp, u64], ci),
             "pg_d2h": ([vp, vp, vp, vp, u64], ci),
             "pg_d2d": ([vp, vp, vp, vp, u64], ci),

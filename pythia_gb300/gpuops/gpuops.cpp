@@ -17,7 +17,7 @@ pthread_once_t g_once = PTHREAD_ONCE_INIT;
 pg_ctx* g_ctx = 0;
 pthread_mutex_t g_fail_mu = PTHREAD_MUTEX_INITIALIZER;
 std::string g_fail;
-TransferStats g_stats = {0, 0, 0, 0};
+TransferStats g_stats = {0, 0, 0, 0, 0};
 volatile int g_exchange = 1;
 
 void count(unsigned long long* c, unsigned long long v)
@@ -97,6 +97,7 @@ TransferStats transfer_stats()
 	t.d2h = __sync_fetch_and_add(&g_stats.d2h, 0);
 	t.d2d = __sync_fetch_and_add(&g_stats.d2d, 0);
 	t.in_place = __sync_fetch_and_add(&g_stats.in_place, 0);
+	t.direct = __sync_fetch_and_add(&g_stats.direct, 0);
 	return t;
 }
 
@@ -106,6 +107,7 @@ void reset_transfer_stats()
 	__sync_lock_test_and_set(&g_stats.d2h, 0);
 	__sync_lock_test_and_set(&g_stats.d2d, 0);
 	__sync_lock_test_and_set(&g_stats.in_place, 0);
+	__sync_lock_test_and_set(&g_stats.direct, 0);
 }
 
 void set_device_exchange(bool on)
@@ -334,6 +336,18 @@ bool InputSide::stage(Operator* child, unsigned short tid)
 		Operator::Page* p = r.second;
 		const unsigned long long used = p ? p->getUsedSpace() : 0;
 		const char* src = used ? (const char*) p->getTupleOffset(0) : 0;
+		if (used && pg_host_is_pinned(ctx, src)) {
+			// A page in pinned or registered memory goes to the device
+			// directly, after the bytes staged before it; the copy ends before
+			// the next getNext, which may reuse the page.
+			ok = flush(ctx, st, u, pin[cur], fill, room, next_chunk) &&
+				flush(ctx, st, u, src, used, room, next_chunk) && pg_sync(ctx, st) == PG_OK;
+			fill = 0;
+			in_flight[0] = in_flight[1] = false;
+			count(&g_stats.direct, used);
+			if (r.first == Operator::Finished) break;
+			continue;
+		}
 		unsigned long long left = used;
 		while (ok && left) {
 			const unsigned long long n = std::min(left, STAGE_BYTES - fill);

@@ -58,6 +58,7 @@ std::string last_failure();
 // the number of inputs taken on the device without any copy.
 struct TransferStats {
 	unsigned long long h2d, d2h, d2d, in_place;
+	unsigned long long direct;   // of h2d: bytes copied straight from pinned or registered pages
 };
 TransferStats transfer_stats();
 void reset_transfer_stats();

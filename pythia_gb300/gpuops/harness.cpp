@@ -218,13 +218,32 @@ int pgo_run(const char* plan, int threads, void** out, unsigned long long* nbyte
 
 void pgo_free(void* p) { free(p); }
 
+// Page-locks (pin = 1) or releases (pin = 0) the memory of a registered
+// relation, as a loader that reads tables into pinned memory would leave
+// it: GPU operators then copy its pages to the device directly. Returns 0,
+// or 1 when the relation is unknown or the GPU call failed.
+int pgo_pin(const char* name, int pin)
+{
+	pthread_mutex_lock(&g_rel_mu);
+	std::map<std::string, Relation>::iterator it = g_relations.find(name ? name : "");
+	const bool found = it != g_relations.end();
+	Relation r = found ? it->second : Relation();
+	pthread_mutex_unlock(&g_rel_mu);
+	if (!found) return 1;
+	pg_ctx* ctx = pythia_gpu_ops::shared_context();
+	if (!ctx || !r.data || !r.n) return ctx ? 0 : 1;
+	const int rc = pin ? pg_host_register(ctx, (void*) r.data, r.n * r.width) : pg_host_unregister(ctx, (void*) r.data);
+	return rc ? 1 : 0;
+}
+
 // Bytes the GPU operators moved since the last reset: out[0] pages uploaded,
 // out[1] outputs downloaded, out[2] device copies gathering inputs, out[3]
-// inputs taken on the device in place.
+// inputs taken on the device in place (a count), out[4] of out[0] the bytes
+// copied straight from pinned or registered pages.
 void pgo_transfer_stats(unsigned long long* out)
 {
 	const pythia_gpu_ops::TransferStats t = pythia_gpu_ops::transfer_stats();
-	out[0] = t.h2d; out[1] = t.d2h; out[2] = t.d2d; out[3] = t.in_place;
+	out[0] = t.h2d; out[1] = t.d2h; out[2] = t.d2d; out[3] = t.in_place; out[4] = t.direct;
 }
 
 void pgo_reset_transfer_stats() { pythia_gpu_ops::reset_transfer_stats(); }

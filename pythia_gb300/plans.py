@@ -56,20 +56,34 @@ def lib():
         L.pgo_reset_transfer_stats.restype = None
         L.pgo_set_device_exchange.argtypes = [ctypes.c_int]
         L.pgo_set_device_exchange.restype = None
+        L.pgo_pin.argtypes = [ctypes.c_char_p, ctypes.c_int]
+        L.pgo_pin.restype = ctypes.c_int
         _LIB = L
     return _LIB
 
 
-def register(name, rows):
+_PINNED = set()
+
+
+def register(name, rows, pin=False):
     """Makes `rows` (a C-contiguous 2-D array, one row per tuple) readable by
-    memscan nodes with `relation = name`."""
+    memscan nodes with `relation = name`. pin=True page-locks its memory (a
+    loader reading into pinned memory): GPU operators then copy its pages to
+    the device directly instead of through staging buffers."""
     a = np.ascontiguousarray(rows)
     if a.ndim != 2:
         raise ValueError("rows must be 2-D")
     width = a.shape[1] * a.itemsize
+    if name in _PINNED:
+        lib().pgo_pin(name.encode(), 0)
+        _PINNED.discard(name)
     _KEEP[name] = a
     if lib().pgo_register(name.encode(), a.ctypes.data if a.size else None, a.shape[0], width):
         raise ValueError("pgo_register refused the relation")
+    if pin and a.size:
+        if lib().pgo_pin(name.encode(), 1):
+            raise RuntimeError("pgo_pin failed (no GPU, or the memory could not be page-locked)")
+        _PINNED.add(name)
 
 
 def run(plan, threads=1):
@@ -96,12 +110,13 @@ def run(plan, threads=1):
 def transfer_stats(reset=False):
     """Bytes the GPU operators moved since the last reset: pages uploaded
     ("h2d"), outputs downloaded ("d2h"), device copies gathering inputs
-    ("d2d"), and inputs taken on the device in place ("in_place", a count)."""
-    a = (ctypes.c_ulonglong * 4)()
+    ("d2d"), inputs taken on the device in place ("in_place", a count), and
+    the part of "h2d" copied straight from pinned or registered pages ("direct")."""
+    a = (ctypes.c_ulonglong * 5)()
     lib().pgo_transfer_stats(a)
     if reset:
         lib().pgo_reset_transfer_stats()
-    return {"h2d": a[0], "d2h": a[1], "d2d": a[2], "in_place": a[3]}
+    return {"h2d": a[0], "d2h": a[1], "d2d": a[2], "in_place": a[3], "direct": a[4]}
 
 
 def set_device_exchange(on):

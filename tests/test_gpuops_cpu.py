@@ -118,7 +118,7 @@ def test_gpu_chain_without_gpu_returns_error_and_moves_nothing():
         finally:
             plans.set_device_exchange(True)
         assert e.value.code == 1
-    assert plans.transfer_stats() == {"h2d": 0, "d2h": 0, "d2d": 0, "in_place": 0}
+    assert plans.transfer_stats() == {"h2d": 0, "d2h": 0, "d2d": 0, "in_place": 0, "direct": 0}
 
 
 def test_reference_engine_drives_gpu_operator():

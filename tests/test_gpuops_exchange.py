@@ -187,3 +187,22 @@ def test_thread_local_aggregate_over_device_join():
         assert tot.sum() == 200_000
         assert np.array_equal(tot, np.bincount(S[:, 0] % 50, minlength=50))
     assert st_on["in_place"] == 4 and st_on["d2d"] == 0
+
+
+def test_pinned_leaves_copy_to_the_device_directly():
+    # Relations in registered memory (a loader that reads into pinned memory):
+    # their pages go to the device without the staging copy; same rows.
+    R = dg.build_relation(20_000, dg.seed_for(414))
+    S = dg.probe_uniform(90_000, R, dg.seed_for(415))
+    plan = PART_JOIN.format(hi=20_000, jtype="gpuhashjoin", groups="((0), (1), (2), (3))")
+    want, n, _ = orc.hashjoin(R, S, proj=(("P", 8, 8), ("B", 8, 8)), hash=orc.hashcfg("modulo", 1 << 12))
+    try:
+        plans.register("R", R, pin=True); plans.register("S", S, pin=True)
+        plans.transfer_stats(reset=True)
+        rows, per = plans.run(plan, threads=4)
+        st = plans.transfer_stats(reset=True)
+    finally:
+        plans.register("R", R); plans.register("S", S)      # unpins
+    assert sum(per) == n
+    assert np.array_equal(canon(rows), canon(want))
+    assert st["h2d"] == R.nbytes + S.nbytes == st["direct"]
