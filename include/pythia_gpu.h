@@ -32,7 +32,7 @@ extern "C" {
 #define PG_ERR_TIMEOUT      4  /* a bounded device-side wait gave up               */
 #define PG_ERR_TABLE_FULL   5  /* hash table probe sequence exhausted             */
 #define PG_ERR_OUTPUT_FULL  6  /* output capacity too small; *n_out = rows needed */
-#define PG_ERR_UNSUPPORTED  7  /* configuration this build does not implement     */
+#define PG_ERR_UNSUPPORTED  7  /* configuration the library does not implement    */
 
 typedef struct pg_ctx pg_ctx;
 typedef struct pg_hashtable pg_hashtable;
