@@ -138,6 +138,10 @@ enum {
 	PG_TUNE_GROUPBY_PATH = 9,        /* group-by: 0 by key range and size, 1 hashed global table, 2 partitioned,
 	                                    3 hashed global without warp combining, 4 partitioned without warp
 	                                    combining, 6 dense when the key range allows */
+	PG_TUNE_PROBE_WIDE = 10,         /* probe of tuples or rows other than 16 bytes: 0 materialised rows staged
+	                                    through shared memory where the width allows, counts and sums per-thread
+	                                    loads; 1 per-thread loads; 2 staged, 4 lookups per thread; 3 staged,
+	                                    2 lookups per thread */
 	PG_TUNE_COUNT = 12
 };
 int pg_tune_set(pg_ctx* ctx, int knob, int64_t value);

@@ -241,6 +241,69 @@ def test_join_wide_tuples(ctx):
     _join_check(ctx, R, S, proj=(("P", 0, 4), ("P", 12, 8), ("B", 12, 8)), bkey=(4, 8), pkey=(4, 8))
 
 
+def _lines(n, R, seed, miss_every=0):
+    """(order, part, price) 24-byte probe tuples whose part keys are drawn from R."""
+    fk = dg.probe_uniform(n, R, dg.seed_for(seed))
+    L = np.zeros((n, 3), np.int64)
+    L[:, 0] = np.arange(n) * 3 + 1
+    L[:, 1] = fk[:, 0]
+    L[:, 2] = ((dg.raw_words(dg.seed_for(seed + 1), 2, n) >> np.uint64(11)).astype(np.float64) * 1e-9).view(np.int64)
+    if miss_every:
+        L[::miss_every, 1] += 1 << 40
+    return L
+
+
+@pytest.mark.parametrize("wide", [0, 1, 2, 3])
+def test_join_other_widths(ctx, wide):
+    # Probe tuples and output rows other than 16 bytes: staged through shared
+    # memory (2: 4 lookups per thread, 3: 2; 0: rows staged, counts and sums
+    # per thread) or loaded per thread (1); same rows, counts and sums. Dense narrow, dense wide and hashed
+    # tables; ragged final tiles whose bytes are not a multiple of 16.
+    R = dg.build_relation(60_000, dg.seed_for(601))
+    Rw = R.copy(); Rw[:, 1] = dg.raw_words(dg.seed_for(602), 1, 60_000).view(np.int64)
+    Rh = R.copy(); Rh[:, 0] = Rh[:, 0] * 7919 - (1 << 40)
+    try:
+        ctx.tune(probe_wide=wide)
+        L = _lines(300_001, R, 603, miss_every=37)
+        for table in (R, Rw):
+            _join_check(ctx, table, L, proj=(("P", 0, 8), ("P", 16, 8), ("B", 8, 8)), pkey=(8, 8))
+            _join_check(ctx, table, L, proj=(("P", 16, 8), ("B", 8, 8)), pkey=(8, 8))
+            _join_check(ctx, table, L, proj=(("B", 8, 4), ("P", 4, 8), ("P", 20, 4), ("B", 12, 4)), pkey=(8, 8))
+        Lh = L.copy(); Lh[:, 1] = Lh[:, 1] * 7919 - (1 << 40)
+        Lh[::101, 1] = -1; Rh[7, 0] = -1                      # the empty marker as a real key
+        _join_check(ctx, Rh, Lh, proj=(("P", 0, 8), ("P", 16, 8), ("B", 8, 8)), pkey=(8, 8))
+        # 12-byte tuples with an int key at byte 4; odd counts leave 4 or 8
+        # bytes past the last multiple of 16.
+        I = np.zeros((20_001, 3), np.int32)
+        I[:, 0] = np.arange(20_001); I[:, 1] = (np.arange(20_001) * 7) % 5000; I[:, 2] = -np.arange(20_001)
+        Ri = np.zeros((5000, 2), np.int32); Ri[:, 0] = np.arange(5000); Ri[:, 1] = np.arange(5000) * 3 - 7000
+        for n in (20_001, 20_002, 3, 1):
+            _join_check(ctx, Ri, I[:n], proj=(("P", 8, 4), ("B", 4, 4), ("P", 0, 4)), bkey=(0, 4), pkey=(4, 4))
+        # 16-byte tuples keyed at byte 4 and 12-byte rows; 64-byte tuples (the
+        # widest staged) and 68-byte ones (per-thread loads).
+        S16 = dg.probe_uniform(100_003, R, dg.seed_for(604)).view(np.int32)
+        S16 = np.ascontiguousarray(np.roll(S16, 1, axis=1))
+        _join_check(ctx, R, S16, proj=(("P", 0, 4), ("B", 8, 8)), pkey=(4, 8))
+        for words in (16, 17):
+            Wd = np.zeros((70_000, words), np.int32)
+            Wd[:, :] = np.arange(words)[None, :] + np.arange(70_000)[:, None]
+            Wd[:, 10:12] = dg.probe_uniform(70_000, R, dg.seed_for(605))[:, :1].view(np.int32)
+            _join_check(ctx, R, Wd, proj=(("P", 60, 4), ("P", 0, 8), ("B", 8, 8), ("P", 36, 4)), pkey=(40, 8))
+        # A probe side several grid waves long; an exact and a short output.
+        Lbig = _lines(2_000_000, R, 606, miss_every=13)
+        n = _join_check(ctx, R, Lbig, proj=(("P", 0, 8), ("P", 16, 8), ("B", 8, 8)), pkey=(8, 8))
+        t = ctx.build_table(R, (("P", 0, 8), ("P", 16, 8), ("B", 8, 8)))
+        try:
+            got, n2, _ = t.probe(Lbig, pkey=(8, 8), out_cap=n)
+            assert n2 == n and got.shape[0] == n
+            with pytest.raises(gpu.PgError):
+                t.probe(Lbig, pkey=(8, 8), out_cap=n - 1)
+        finally:
+            t.free()
+    finally:
+        ctx.tune(probe_wide=0)
+
+
 def test_join_reference_unit_test(ctx):
     # unit_tests/queryhashjoin.cpp: build (i, i), probe (i, i+0.1), i = 1..20.
     R = gin.make({"gen": "formula", "name": "i_i", "n": 20})
