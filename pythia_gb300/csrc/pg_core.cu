@@ -53,6 +53,10 @@ extern "C" int pg_init(int device, uint64_t reserved_bytes, pg_ctx** out)
 	for (int i = 0; i < PG_TUNE_COUNT; ++i) ctx->tune[i] = 0;
 	if ((e = cudaSetDevice(device)) != cudaSuccess) { delete ctx; return pg_cuda_fail(nullptr, e, "cudaSetDevice"); }
 	cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+	ctx->pageable_access = 0;
+	ctx->host_ptr_registered = 0;
+	cudaDeviceGetAttribute(&ctx->pageable_access, cudaDevAttrPageableMemoryAccess, device);
+	cudaDeviceGetAttribute(&ctx->host_ptr_registered, cudaDevAttrCanUseHostPointerForRegisteredMem, device);
 	cudaDeviceGetDefaultMemPool(&ctx->pool, device);
 	// Keep freed blocks in the pool: operators allocate scratch per call.
 	uint64_t thresh = UINT64_MAX;
@@ -198,6 +202,59 @@ extern "C" int pg_host_is_pinned(pg_ctx* ctx, const void* p)
 	cudaPointerAttributes a;
 	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return 0; }
 	return a.type == cudaMemoryTypeHost ? 1 : 0;
+}
+
+extern "C" int pg_host_readable(pg_ctx* ctx, const void* p)
+{
+	if (!ctx || !p) return 0;
+	return pg_host_is_pinned(ctx, p) || ctx->pageable_access ? 1 : 0;
+}
+
+// Host-to-device copy by the SMs: bytes [0, head) one per thread until dst is
+// 16-byte aligned, then units of U (the widest that src + head allows), then
+// the remaining bytes one per thread.
+template <typename U>
+__global__ void k_sm_copy(const char* __restrict__ src, char* __restrict__ dst, uint64_t n, uint32_t head)
+{
+	const uint64_t tid = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	if (tid < head) dst[tid] = src[tid];
+	const uint64_t units = (n - head) / sizeof(U);
+	const U* s = reinterpret_cast<const U*>(src + head);
+	U* d = reinterpret_cast<U*>(dst + head);
+	for (uint64_t i = tid; i < units; i += stride) d[i] = s[i];
+	const uint64_t done = head + units * sizeof(U);
+	if (tid < n - done) dst[done + tid] = src[done + tid];
+}
+
+extern "C" int pg_h2d_sm(pg_ctx* ctx, pg_stream stream, void* dst, const void* src, uint64_t bytes)
+{
+	if (!ctx) return PG_ERR_ARG;
+	if (!bytes) return PG_OK;
+	if (!dst || !src) return pg_fail(ctx, PG_ERR_ARG, "pg_h2d_sm: null pointer");
+	const char* from = (const char*) src;
+	if (pg_host_is_pinned(ctx, src)) {
+		if (!ctx->host_ptr_registered) {
+			void* d = nullptr;
+			PG_CUDA(ctx, cudaHostGetDevicePointer(&d, const_cast<void*>(src), 0));
+			from = (const char*) d;
+		}
+	} else if (!ctx->pageable_access) {
+		return pg_fail(ctx, PG_ERR_ARG, "pg_h2d_sm: host memory the device cannot read (not pinned, no pageable access)");
+	}
+	cudaStream_t s = (cudaStream_t) stream;
+	const uint32_t head = (uint32_t) std::min<uint64_t>(bytes, (16 - (reinterpret_cast<uintptr_t>(dst) & 15)) & 15);
+	const uintptr_t a = reinterpret_cast<uintptr_t>(from + head);
+	const uint32_t unit = (a & 15) == 0 ? 16 : (a & 7) == 0 ? 8 : (a & 3) == 0 ? 4 : 1;
+	const uint64_t units = (bytes - head) / unit;
+	const int blocks = (int) std::max<uint64_t>(1, std::min<uint64_t>(pg_div_up(units, 256 * 4), (uint64_t) ctx->sm_count * 2));
+	char* to = (char*) dst;
+	if (unit == 16) k_sm_copy<uint4><<<blocks, 256, 0, s>>>(from, to, bytes, head);
+	else if (unit == 8) k_sm_copy<uint2><<<blocks, 256, 0, s>>>(from, to, bytes, head);
+	else if (unit == 4) k_sm_copy<uint32_t><<<blocks, 256, 0, s>>>(from, to, bytes, head);
+	else k_sm_copy<unsigned char><<<blocks, 256, 0, s>>>(from, to, bytes, head);
+	PG_LAUNCHED(ctx);
+	return PG_OK;
 }
 
 extern "C" int pg_host_free(pg_ctx* ctx, void* p)

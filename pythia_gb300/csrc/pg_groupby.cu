@@ -551,6 +551,91 @@ k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, u
 	if (outside) *overflow = 1;
 }
 
+// Dense group-by over a window of at most GBS_MAX_SLOTS keys: each CTA sums
+// its rows into a copy of the table in shared memory (the same words and
+// compensation as the global table: dec (hi, lo) with hi from -0.0, int sums in
+// the low 4 bytes, counts and long sums in 8), then adds each slot it saw into
+// the global table once, dec partials through the compensated add. Few groups
+// otherwise put every row's atomic on a handful of L2 lines.
+#define GBS_MAX_SLOTS 4096
+template <int VT, int AGG, bool VEC16>
+__global__ void __launch_bounds__(GB_THREADS)
+k_gb_dense_smem(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes, uint32_t voff,
+		long long kmin, uint32_t range, unsigned long long* __restrict__ acc,
+		unsigned char* __restrict__ present, unsigned int* __restrict__ overflow)
+{
+	constexpr bool DEC = AGG == PG_AGG_SUM && VT == PG_VAL_DEC;
+	extern __shared__ __align__(16) unsigned char gsm[];
+	unsigned long long* const sacc = reinterpret_cast<unsigned long long*>(gsm);      // DEC ? 2 : 1 words per slot
+	unsigned char* const spres = gsm + (size_t) range * (DEC ? 16 : 8);
+	for (uint32_t i = threadIdx.x; i < range; i += blockDim.x) {
+		if (DEC) { sacc[2 * i] = PG_NEG_ZERO; sacc[2 * i + 1] = 0; }
+		else sacc[i] = 0;
+		spres[i] = 0;
+	}
+	__syncthreads();
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	bool outside = false;
+	for (uint64_t base = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; base < n; base += stride * GBD_ILP) {
+		uint32_t d[GBD_ILP];
+		unsigned long long iv[GBD_ILP];
+		double dv[GBD_ILP];
+		bool ok[GBD_ILP];
+		#pragma unroll
+		for (int j = 0; j < GBD_ILP; ++j) {
+			const uint64_t i = base + j * stride;
+			ok[j] = i < n;
+			d[j] = 0; iv[j] = 0; dv[j] = 0.0;
+			if (!ok[j]) continue;
+			int64_t k;
+			uint64_t vbits;
+			if (VEC16) {
+				const uint4 t = __ldg(reinterpret_cast<const uint4*>(in) + i);
+				k = koff == 0 ? (int64_t) (((uint64_t) t.y << 32) | t.x) : (int64_t) (((uint64_t) t.w << 32) | t.z);
+				vbits = voff == 0 ? (((uint64_t) t.y << 32) | t.x) : voff == 8 ? (((uint64_t) t.w << 32) | t.z)
+					: voff == 4 ? t.y : t.w;
+				if (VT == PG_VAL_INT) vbits = (uint64_t) (int64_t) (int32_t) (voff == 0 ? t.x : voff == 4 ? t.y : voff == 8 ? t.z : t.w);
+			} else {
+				const char* r = in + i * W;
+				k = pg_load_key(r + koff, kbytes);
+				vbits = VT == PG_VAL_INT ? (uint64_t) (int64_t) *reinterpret_cast<const int32_t*>(r + voff)
+					: (uint64_t) pg_load_key(r + voff, 8);
+			}
+			const uint64_t dd = (uint64_t) k - (uint64_t) kmin;
+			if (dd >= range) { ok[j] = false; outside = true; continue; }   // key outside the table
+			d[j] = (uint32_t) dd;
+			if (AGG == PG_AGG_COUNT) iv[j] = 1;
+			else if (DEC) dv[j] = __longlong_as_double((long long) vbits);
+			else iv[j] = vbits;
+		}
+		#pragma unroll
+		for (int j = 0; j < GBD_ILP; ++j) {
+			if (!ok[j]) continue;
+			if (DEC) atomic_comp_add(reinterpret_cast<double*>(&sacc[2 * d[j]]), reinterpret_cast<double*>(&sacc[2 * d[j] + 1]),
+					dv[j], 0.0);
+			else if (VT == PG_VAL_INT && AGG == PG_AGG_SUM)
+				atomicAdd(reinterpret_cast<unsigned int*>(&sacc[d[j]]), (unsigned int) iv[j]);
+			else atomicAdd(&sacc[d[j]], iv[j]);
+			if (AGG == PG_AGG_SUM) spres[d[j]] = 1;
+		}
+	}
+	if (outside) *overflow = 1;
+	__syncthreads();
+	for (uint32_t i = threadIdx.x; i < range; i += blockDim.x) {
+		if (AGG == PG_AGG_COUNT) {
+			if (sacc[i]) atomicAdd(&acc[i], sacc[i]);
+			continue;
+		}
+		if (!spres[i]) continue;
+		if (DEC)
+			atomic_comp_add(reinterpret_cast<double*>(&acc[2 * i]), reinterpret_cast<double*>(&acc[2 * i + 1]),
+					__longlong_as_double((long long) sacc[2 * i]), __longlong_as_double((long long) sacc[2 * i + 1]));
+		else if (VT == PG_VAL_INT) atomicAdd(reinterpret_cast<unsigned int*>(&acc[i]), (unsigned int) sacc[i]);
+		else atomicAdd(&acc[i], sacc[i]);
+		present[i] = 1;
+	}
+}
+
 template <int VT, int AGG>
 __global__ void k_gb_dense_emit(const unsigned long long* __restrict__ acc, const double* __restrict__ lo,
 		const unsigned char* __restrict__ present, uint64_t range, long long kmin, uint32_t kbytes,
@@ -617,12 +702,33 @@ static int gb_dense_window(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32
 				acc, 2 * range, PG_NEG_ZERO);
 		PG_LAUNCHED(ctx);
 	}
-	const int gblocks = (int) std::min<uint64_t>(pg_div_up(in->n, (uint64_t) GB_THREADS * GBD_ILP), (uint64_t) ctx->sm_count * 8);
-	if (vec16) k_gb_dense<VT, AGG, true><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, in->width,
-			in->key_off, in->key_bytes, voff, kmin, range, acc, lo, present, oflag);
-	else k_gb_dense<VT, AGG, false><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, in->width,
-			in->key_off, in->key_bytes, voff, kmin, range, acc, lo, present, oflag);
-	PG_LAUNCHED(ctx);
+	if (range <= GBS_MAX_SLOTS && ctx->tune[PG_TUNE_GROUPBY_PATH] != 7) {
+		// Few groups: per-CTA tables in shared memory, one flush each.
+		const int sbytes = (int) (range * ((VT == PG_VAL_DEC && AGG == PG_AGG_SUM) ? 17 : 9));
+		int per_sm = 0;
+		if (vec16) {
+			PG_CUDA(ctx, cudaFuncSetAttribute(k_gb_dense_smem<VT, AGG, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbytes));
+			PG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gb_dense_smem<VT, AGG, true>, GB_THREADS, sbytes));
+		} else {
+			PG_CUDA(ctx, cudaFuncSetAttribute(k_gb_dense_smem<VT, AGG, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbytes));
+			PG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gb_dense_smem<VT, AGG, false>, GB_THREADS, sbytes));
+		}
+		const int sblocks = (int) std::min<uint64_t>(pg_div_up(in->n, (uint64_t) GB_THREADS * GBD_ILP),
+				(uint64_t) ctx->sm_count * std::max(per_sm, 1));
+		if (vec16) k_gb_dense_smem<VT, AGG, true><<<sblocks, GB_THREADS, sbytes, s>>>((const char*) in->data, in->n,
+				in->width, in->key_off, in->key_bytes, voff, kmin, (uint32_t) range, acc, present, oflag);
+		else k_gb_dense_smem<VT, AGG, false><<<sblocks, GB_THREADS, sbytes, s>>>((const char*) in->data, in->n,
+				in->width, in->key_off, in->key_bytes, voff, kmin, (uint32_t) range, acc, present, oflag);
+		PG_LAUNCHED(ctx);
+	} else {
+		const int gblocks = (int) std::min<uint64_t>(pg_div_up(in->n, (uint64_t) GB_THREADS * GBD_ILP),
+				(uint64_t) ctx->sm_count * 8);
+		if (vec16) k_gb_dense<VT, AGG, true><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, in->width,
+				in->key_off, in->key_bytes, voff, kmin, range, acc, lo, present, oflag);
+		else k_gb_dense<VT, AGG, false><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, in->width,
+				in->key_off, in->key_bytes, voff, kmin, range, acc, lo, present, oflag);
+		PG_LAUNCHED(ctx);
+	}
 	const int eblocks = (int) std::min<uint64_t>(pg_div_up(range, 256), (uint64_t) ctx->sm_count * 8);
 	k_gb_dense_emit<VT, AGG><<<eblocks, 256, 0, s>>>(acc, lo, present, range, kmin, in->key_bytes, (char*) out,
 			out_cap, cursor);
@@ -708,7 +814,7 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 {
 	const bool haskey = in->key_bytes != 0;
 	const int64_t gpath = ctx->tune[PG_TUNE_GROUPBY_PATH];
-	if (haskey && in->n && (gpath == 0 || gpath == 6)) {
+	if (haskey && in->n && (gpath == 0 || gpath == 6 || gpath == 7)) {
 		bool done = false;
 		int rc = gb_dense<VT, AGG>(ctx, s, in, voff, hint, out, out_cap, ngroups, &done);
 		if (rc || done) return rc;

@@ -17,6 +17,8 @@ struct pg_ctx {
 	cudaMemPool_t pool;
 	int* d_status;          // sticky device error word (PG_ERR_*), 0 = fine
 	unsigned long long* d_scratch64;  // small per-context device scratch (counters)
+	int pageable_access;    // kernels may read pageable host memory (cudaDevAttrPageableMemoryAccess)
+	int host_ptr_registered;  // registered host memory is read through its host address
 	std::mutex mu;
 	std::string last_error;
 };

@@ -67,7 +67,7 @@ SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_st
            "pg_hashjoin_groupby", "pg_stream_create_urgent", "pg_autotune_batch",
            "pg_hashtable_image_size", "pg_hashtable_serialize", "pg_hashtable_deserialize",
            "pg_hashtable_save", "pg_hashtable_load", "pg_filter", "pg_project", "pg_hashjoin_probe_where",
-           "pg_host_register", "pg_host_unregister", "pg_host_is_pinned"]
+           "pg_host_register", "pg_host_unregister", "pg_host_is_pinned", "pg_host_readable", "pg_h2d_sm"]
 TUNE = {"probe_ctas_per_sm": 0, "probe_variant": 1, "dense": 2, "partition_tile": 3,
         "groupby_smem_groups": 4, "radix_bits": 5, "probe_items": 6, "probe_cache": 7, "probe_passes": 8, "groupby_path": 9,
         "probe_wide": 10}
@@ -100,6 +100,8 @@ def lib():
             "pg_host_register": ([vp, vp, u64], ci),
             "pg_host_unregister": ([vp, vp], ci),
             "pg_host_is_pinned": ([vp, vp], ci),
+            "pg_host_readable": ([vp, vp], ci),
+            "pg_h2d_sm": ([vp, vp, vp, vp, u64], ci),
             "pg_h2d": ([vp, vp, vp, vp, u64], ci),
             "pg_d2h": ([vp, vp, vp, vp, u64], ci),
             "pg_d2d": ([vp, vp, vp, vp, u64], ci),

@@ -67,6 +67,16 @@ void reset_transfer_stats();
 // effect for operators initialised afterwards.
 void set_device_exchange(bool on);
 
+// Phase trace of the GPU operators, the counterpart of the engine's TRACELOG
+// ring of (thread, label, timestamp) entries (operators/join.cpp:55-120):
+// off by default; when on, operator threads append (plan node, thread,
+// phase, host monotonic ns) entries to a fixed ring until it is full.
+// trace_enable(true) also empties the ring; trace_dump writes one line per entry,
+// "ns node thread phase", and returns the bytes the whole dump needs.
+void trace_enable(bool on);
+void trace(const std::string& node, int tid, const char* phase);
+unsigned long long trace_dump(char* buf, unsigned long long len);
+
 // Rows of one operator thread's output in device memory.
 struct DeviceSpan {
 	const char* data;           // device pointer; NULL when rows == 0
@@ -86,6 +96,7 @@ public:
 	virtual DeviceSpan device_share(unsigned short tid) = 0;
 protected:
 	bool on_device_;
+	std::string node_;          // plan node name, for the phase trace
 };
 
 class GroupBarrier {
@@ -125,9 +136,9 @@ public:
 	void set_rows(int group, unsigned long long rows) { rows_[group] = rows; }
 	// The group's output is `rows` tuples at device address `data`.
 	void set_device(int group, const char* data, unsigned long long rows);
-	// Device memory freed by clear() (pool: from pg_buffer_alloc_async);
-	// threads may hand it over concurrently.
-	void own_device(void* p, bool pool = false);
+	// Pool memory (pg_buffer_alloc_async) freed by clear(), after every
+	// reader has synchronised; threads may hand it over concurrently.
+	void own_device(void* p);
 	// Thread `tid` serves rows [pos * rows / k, (pos + 1) * rows / k) of its group.
 	void assign(int tid, int group, int pos, int k);
 	Operator::GetNextResultT next(int tid);
@@ -144,7 +155,7 @@ private:
 	std::vector<std::vector<char> > out_;
 	std::vector<unsigned long long> rows_;
 	std::vector<const char*> dev_;
-	std::vector<void*> owned_, owned_pool_;
+	std::vector<void*> owned_;
 	std::vector<Cursor> cur_;
 	unsigned tuple_size_, page_bytes_;
 };
@@ -164,8 +175,9 @@ class InputSide {
 public:
 	InputSide() : dev_(0) { }
 	~InputSide() { clear(); }
-	// From init: asks a GPU child to keep its output on the device.
-	void setup(Operator* child);
+	// From init: asks a GPU child to keep its output on the device; `node`
+	// names the reading operator in the phase trace.
+	void setup(Operator* child, const std::string& node);
 	bool on_device() const { return dev_ != 0; }
 	// After child->scanStart(tid): stages the pages or takes the span; false
 	// when the child reported Error or the upload failed.
@@ -188,11 +200,12 @@ private:
 	};
 	bool stage(Operator* child, unsigned short tid);
 	static bool flush(pg_ctx* ctx, pg_stream st, Staged& u, const char* buf, unsigned long long n,
-			unsigned long long& room, unsigned long long& next_chunk);
+			unsigned long long& room, unsigned long long& next_chunk, bool sm);
 	DeviceProducer* dev_;
 	std::vector<std::vector<char> > host_;        // pages read without a GPU context
 	std::vector<Staged> staged_;
 	std::vector<DeviceSpan> spans_;
+	std::string node_;
 };
 
 class GpuFilterOp;

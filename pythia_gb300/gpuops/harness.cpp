@@ -252,4 +252,12 @@ void pgo_reset_transfer_stats() { pythia_gpu_ops::reset_transfer_stats(); }
 // operator reads and writes host pages.
 void pgo_set_device_exchange(int on) { pythia_gpu_ops::set_device_exchange(on != 0); }
 
+// Phase trace of the GPU operators: pgo_trace(1) empties the ring and turns
+// it on, pgo_trace(0) turns it off; pgo_trace_dump copies "ns node thread
+// phase" lines into buf (NUL-terminated, truncated to len) and returns the
+// bytes the whole dump needs.
+void pgo_trace(int on) { pythia_gpu_ops::trace_enable(on != 0); }
+
+unsigned long long pgo_trace_dump(char* buf, unsigned long long len) { return pythia_gpu_ops::trace_dump(buf, len); }
+
 }  // extern "C"

@@ -58,6 +58,10 @@ def lib():
         L.pgo_set_device_exchange.restype = None
         L.pgo_pin.argtypes = [ctypes.c_char_p, ctypes.c_int]
         L.pgo_pin.restype = ctypes.c_int
+        L.pgo_trace.argtypes = [ctypes.c_int]
+        L.pgo_trace.restype = None
+        L.pgo_trace_dump.argtypes = [ctypes.c_char_p, ctypes.c_ulonglong]
+        L.pgo_trace_dump.restype = ctypes.c_ulonglong
         _LIB = L
     return _LIB
 
@@ -117,6 +121,25 @@ def transfer_stats(reset=False):
     if reset:
         lib().pgo_reset_transfer_stats()
     return {"h2d": a[0], "d2h": a[1], "d2d": a[2], "in_place": a[3], "direct": a[4]}
+
+
+def trace(on=True):
+    """Turns the GPU operators' phase trace on (emptying it) or off."""
+    lib().pgo_trace(1 if on else 0)
+
+
+def trace_read():
+    """The phase trace as (ns, node, thread, phase) tuples in arrival order:
+    host monotonic nanoseconds, the plan node of the operator, the operator
+    thread and the phase it reached."""
+    need = lib().pgo_trace_dump(None, 0)
+    buf = ctypes.create_string_buffer(int(need))
+    lib().pgo_trace_dump(buf, need)
+    out = []
+    for line in buf.value.decode().splitlines():
+        ns, node, tid, phase = line.split(" ", 3)
+        out.append((int(ns), node, int(tid), phase))
+    return out
 
 
 def set_device_exchange(on):

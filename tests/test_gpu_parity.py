@@ -358,9 +358,10 @@ def test_groupby_empty_marker_key(gbctx):
 
 
 # Every group-by path: 0 chooses (dense direct-indexed table for compact key
-# ranges), 3 hashed global table, 4 partitioned, 1 and 2 the same with warp
-# combining of equal keys.
-GB_PATHS = [0, 1, 2, 3, 4]
+# ranges, summed per CTA in shared memory first for windows up to 4096 keys),
+# 3 hashed global table, 4 partitioned, 1 and 2 the same with warp combining of
+# equal keys, 7 dense with global atomics only.
+GB_PATHS = [0, 1, 2, 3, 4, 7]
 
 
 @pytest.fixture(params=GB_PATHS)
@@ -388,6 +389,28 @@ def test_groupby_dec_compensated(gbctx, groups):
     rows = dg.groupby_rows(1_000_000, groups, 1e4, dg.seed_for(53))
     _gb_dec_check(ctx, rows)
     _gb_dec_check(ctx, rows, hint=groups)
+
+
+@pytest.mark.parametrize("path", [0, 7])
+def test_groupby_few_groups_large_input(ctx, path):
+    # 5M rows in 1000 groups take the key window from a sample; path 0 sums
+    # each CTA's rows in shared memory before one flush per group, path 7
+    # adds every row into the global table. Integer results are exact, dec
+    # sums within the contract; one key holding a third of the rows too.
+    rows = dg.groupby_rows(5_000_000, 1000, 1e4, dg.seed_for(56))
+    rows[::3, 0] = 17
+    try:
+        ctx.tune(groupby_path=path)
+        _gb_dec_check(ctx, rows)
+        ints = rows.copy()
+        ints[:, 1] = (ints[:, 1] & 0xFFFFF) - 0x80000
+        for agg in ("sum", "count"):
+            _gb_int_check(ctx, ints, agg, "long")
+        i32 = np.ascontiguousarray(ints.view(np.int32)[:, [0, 2]])
+        got = ctx.groupby(i32, key=(0, 4), val=(4, "int"), agg="sum")
+        assert np.array_equal(canon(got), canon(orc.groupby(i32, key=(0, 4), val=(4, "int"), agg="sum")))
+    finally:
+        ctx.tune(groupby_path=0)
 
 
 def test_groupby_dec_ill_conditioned(gbctx):
@@ -667,3 +690,29 @@ def test_generate_fk_matches_host_replica(ctx):
     ctx._check(gpu.lib().pg_generate_fk(ctx.h, ctx.stream, dR.ptr, 5000, 12345, dS.ptr, 40_000))
     got = ctx.download(dS, 16 * 40_000).view(np.int64).reshape(-1, 2)
     assert np.array_equal(got, bench.fk_host(R, 12345, 40_000))
+
+
+# ---------------------------------------------------------------- host ingest
+def test_h2d_by_sm_loads_any_alignment(ctx):
+    # pg_h2d_sm: bytes arrive exactly for every source and destination
+    # alignment (byte head, 16/8/4/1-byte units, byte tail) from registered
+    # memory, and from ordinary memory where the device reads it in place.
+    L = gpu.lib()
+    src = dg.raw_words(dg.seed_for(710), 0, (3 << 20) // 8).view(np.uint8)
+    reg = src.copy()
+    ctx._check(L.pg_host_register(ctx.h, reg.ctypes.data, reg.nbytes))
+    try:
+        assert L.pg_host_readable(ctx.h, reg.ctypes.data) == 1
+        sources = [reg] + ([src] if L.pg_host_readable(ctx.h, src.ctypes.data) else [])
+        dst = ctx.alloc(3 << 20)
+        for host in sources:
+            for so in (0, 1, 3, 4, 8, 12, 16):
+                for do in (0, 1, 5, 8, 15):
+                    for n in (0, 1, 15, 16, 17, 1000, (1 << 20) + 7):
+                        ctx._check(L.pg_memset(ctx.h, ctx.stream, dst.ptr, 0xA5, do + n + 16))
+                        ctx._check(L.pg_h2d_sm(ctx.h, ctx.stream, dst.ptr + do, host.ctypes.data + so, n))
+                        got = ctx.download(dst, do + n + 16, np.uint8)
+                        assert np.array_equal(got[do:do + n], host[so:so + n]), (so, do, n)
+                        assert (got[:do] == 0xA5).all() and (got[do + n:] == 0xA5).all(), (so, do, n)
+    finally:
+        ctx._check(L.pg_host_unregister(ctx.h, reg.ctypes.data))

@@ -90,6 +90,32 @@ def test_gpu_operator_without_gpu_returns_error():
     assert e.value.code == 1
 
 
+def test_phase_trace_records_operator_threads():
+    # The trace names the plan node, the thread and the phase; each of the
+    # group's two threads starts, and its first thread launches once, even
+    # when the launch fails for want of a GPU. Off, nothing is recorded.
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    plans.register("R", np.arange(40, dtype=np.int64).reshape(20, 2))
+    plans.trace(True)
+    try:
+        with pytest.raises(plans.PlanError):
+            plans.run(JOIN, threads=2)
+        t = plans.trace_read()
+    finally:
+        plans.trace(False)
+    assert sorted((node, tid) for _, node, tid, ph in t if ph == "start") == [("join", 0), ("join", 1)]
+    assert [(node, tid) for _, node, tid, ph in t if ph == "launch"] == [("join", 0)]
+    assert [ph for _, _, tid, ph in t if tid == 0][-2:] == ["launch", "done"]
+    for tid in (0, 1):
+        ns = [e[0] for e in t if e[2] == tid]
+        assert ns == sorted(ns)
+    with pytest.raises(plans.PlanError):
+        plans.run(JOIN, threads=2)
+    assert plans.trace_read() == t                                     # off: nothing added
+
+
 def test_gpu_chain_without_gpu_returns_error_and_moves_nothing():
     # partition -> join with the device exchange set up at init: without a GPU
     # the partition fails in scanStart, the join sees its child's Error, every
