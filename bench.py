@@ -82,8 +82,12 @@ class Clocks:
 
     def __init__(self, index):
         self.index, self.proc, self.lines = index, None, []
+        self.first = threading.Event()
 
     def start(self):
+        """Starts nvidia-smi and returns once its first sample arrived (at most
+        5 s): its start-up holds driver calls for up to a second, which must
+        not fall into a timed region."""
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -93,12 +97,15 @@ class Clocks:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self.first.wait(5.0)
         except FileNotFoundError:
             self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+            self.first.set()
+        self.first.set()
 
     def stop(self):
         if not self.proc:
@@ -1318,6 +1325,106 @@ def run_filterjoin(args, ws, rank, local):
     ctx.close()
 
 
+def run_wideprobe(args, ws, rank, local):
+    """The q1-shaped plan's first join as one probe: 64M 24-byte lines (order,
+    part, price) against a prebuilt 4M-part dense table, 24-byte rows (order,
+    price, part payload). Tuples and rows other than 16 bytes take the probe
+    staged through shared memory; the per-thread-load probe is timed beside it."""
+    import torch
+    from pythia_gb300 import gpu
+    torch.cuda.set_device(local)
+    threads = host_threads()
+    ctx = make_ctx(args, local)
+    L = gpu.lib()
+    nL, nP = 1 << (args.probe_log2 - 2), 1 << (args.build_log2 - 2)
+    _, P, Ln = _plan_inputs(nL, 1 << 10, nP, threads)
+    dP, dL, dO = ctx.upload(P), ctx.upload(Ln), ctx.alloc(nL * 24)
+    rP = gpu.Rel(dP.ptr, nP, 16, 0, 8)
+    rL = gpu.Rel(dL.ptr, nL, 24, 8, 8)
+    proj, nproj = gpu.cols((("P", 0, 8), ("P", 16, 8), ("B", 8, 8)))
+    ht = ctypes.c_void_p()
+    ctx._check(L.pg_hashjoin_build(ctx.h, ctx.stream, ctypes.byref(rP), proj, nproj, ctypes.byref(ht)))
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    res = gpu.JoinResult()
+
+    def probe():
+        ctx._check(L.pg_hashjoin_probe(ctx.h, ctx.stream, ht.value, ctypes.byref(rL), proj, nproj, dO.ptr, nL,
+                                       gpu.JOIN_MATERIALIZE, -1, ctypes.byref(res)))
+
+    def timed():
+        for _ in range(args.warmup):
+            probe()
+        ctx.sync()
+        barrier(ws)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            probe()
+        e1.record(stream)
+        e1.synchronize()
+        return max_over_ranks(ws, e0.elapsed_time(e1) / args.steps)
+
+    k0 = gpu.kernel_launches()
+    clocks = Clocks(local)
+    clocks.start()
+    ms = timed()
+    clk = clocks.stop()
+    launches = (gpu.kernel_launches() - k0) * args.steps // (args.steps + args.warmup)
+    n_rows = res.n_out
+    # Parity at full size: every line finds its part, so the rows' columns sum
+    # (wrapping) to the lines' orders, the lines' prices and the parts'
+    # payloads looked up by each line's part key.
+    out = ctx.download(dO, n_rows * 24, np.int64).reshape(-1, 3)
+    by_key = np.zeros(nP + 1, np.int64)
+    by_key[P[:, 0]] = P[:, 1]
+    with np.errstate(over="ignore"):
+        want = [int(Ln[:, 0].sum()), int(Ln[:, 2].sum()), int(by_key[Ln[:, 1]].sum())]
+        got = [int(out[:, 0].sum()), int(out[:, 1].sum()), int(out[:, 2].sum())]
+    del out
+    ctx.tune(probe_wide=1)
+    ms_plain = timed()
+    ctx.tune(probe_wide=0)
+    L.pg_hashtable_free(ctx.h, ht.value)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as orc
+        m = min(nL, 1 << 22)
+        cfg = orc.hashcfg("modulo", nP)
+        Lsub = np.array(Ln[:m], copy=True)
+        t0 = time.perf_counter()
+        orc.hashjoin(P, Lsub[:1], proj=(("P", 0, 8), ("P", 16, 8), ("B", 8, 8)), pkey=(8, 8), hash=cfg,
+                     threads=threads, materialise=False)
+        t_build = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        orc.hashjoin(P, Lsub, proj=(("P", 0, 8), ("P", 16, 8), ("B", 8, 8)), pkey=(8, 8), hash=cfg,
+                     threads=threads, out_cap=m)
+        t = max(time.perf_counter() - t0 - t_build, 1e-9) * nL / m
+        cpu = {"value": nL / t, "unit": "tuples/s", "cores": threads, "kind": "port",
+               "sample": f"probe of the first {m} lines against the full {nP}-part table (oracle port; its build, "
+                         f"{t_build:.2f} s, not counted), time scaled linearly to {nL}"}
+    peak, peak_kind = measured_peak()
+    alg = nL * 24 + n_rows * 24
+    gbs = alg / (ms / 1e3) / 1e9
+    if rank == 0:
+        line = {"metric": "probe tuples/s, 24-byte lines into 24-byte rows (64M lines x 4M-part dense table)",
+                "value": ws * nL / (ms / 1e3), "unit": "tuples/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded generator, resident in HBM)",
+                "config": {"workload": f"{nL} lines (order, part, price) probing a prebuilt {nP}-part table, rows "
+                                       "(order, price, part payload): the q1-shaped plan's first join",
+                           "op": "wideprobe", "l2": "inputs larger than L2; no flush"},
+                "per_thread_load_probe_ms": ms_plain, "staged_speedup": ms_plain / ms,
+                "parity": {"rows": int(n_rows), "rows_ok": int(n_rows) == nL, "column_sums_ok": got == want},
+                "roofline": {"bound": "hbm", "kernel": "k_probe_staged<true, 2, 2>", "achieved": gbs, "peak": peak,
+                             "unit": "GB/s", "frac": gbs / peak, "traffic": None, "peak_source": peak_kind,
+                             "algorithmic_bytes": alg},
+                "gpu_launches": int(launches), "clocks": clk}
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1329,7 +1436,8 @@ def main():
     ap.add_argument("--key-domain", default="dense", choices=["dense", "sparse"],
                     help="dense: keys 1..|R| (direct-mapped table); sparse: the same keys "
                          "multiplied by an odd constant (hashed table)")
-    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "batch", "serve", "tableimage", "plan", "filterjoin"] + sorted(OPS))
+    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "batch", "serve", "tableimage", "plan", "filterjoin",
+                                                      "wideprobe"] + sorted(OPS))
     ap.add_argument("--slots", type=int, default=8, help="worker slots for --op serve")
     ap.add_argument("--retune", action="store_true", help="rerun the autotuner for --op batch")
     ap.add_argument("--scale-down", type=int, default=0, help="divide --op sizes by 2^k")
@@ -1352,6 +1460,8 @@ def main():
         run_plan(args, ws, rank, local)
     elif args.op == "filterjoin":
         run_filterjoin(args, ws, rank, local)
+    elif args.op == "wideprobe":
+        run_wideprobe(args, ws, rank, local)
     elif args.op != "hashjoin":
         run_op(args, ws, rank, local, args.op)
     else:

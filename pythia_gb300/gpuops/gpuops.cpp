@@ -716,12 +716,14 @@ int GpuHashJoinOp::run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const 
 	pg_hashtable* ht = 0;
 	int rc = pg_hashjoin_build(ctx, st, &R, &cols_[0], (int) cols_.size(), &ht);
 	if (rc) return rc;
+	trace(node_, 0, "built");
 	unsigned long long cap = std::max<unsigned long long>(S.n, 1);
 	void* o = 0;
 	pg_join_result res;
 	res.n_out = 0; res.sum = 0;
 	for (int attempt = 0; attempt < 2; ++attempt) {
 		if ((rc = pg_buffer_alloc_async(ctx, st, cap * ow, &o))) break;
+		trace(node_, 0, "out allocated");
 		rc = pg_hashjoin_probe_where(ctx, st, ht, &S, probe_preds_.empty() ? 0 : &probe_preds_[0],
 				(int) probe_preds_.size(), &cols_[0], (int) cols_.size(), o, cap, PG_JOIN_MATERIALIZE, -1, &res);
 		if (rc == PG_ERR_OUTPUT_FULL && attempt == 0) {
