@@ -149,10 +149,10 @@ enum {
 	                                    3 hashed global without warp combining, 4 partitioned without warp
 	                                    combining, 6 dense when the key range allows, 7 as 6 without the
 	                                    shared-memory tables of windows up to 4096 keys */
-	PG_TUNE_PROBE_WIDE = 10,         /* probe of tuples or rows other than 16 bytes: 0 materialised rows staged
-	                                    through shared memory where the width allows, counts and sums per-thread
-	                                    loads; 1 per-thread loads; 2 staged, 4 lookups per thread; 3 staged,
-	                                    2 lookups per thread */
+	PG_TUNE_PROBE_WIDE = 10,         /* probe of tuples or rows other than 16 bytes: 0 materialised rows of dense
+	                                    tables staged through shared memory where the width allows, everything
+	                                    else per-thread loads; 1 per-thread loads; 2 staged, 4 lookups per
+	                                    thread; 3 staged, 2 lookups per thread */
 	PG_TUNE_COUNT = 12
 };
 int pg_tune_set(pg_ctx* ctx, int knob, int64_t value);

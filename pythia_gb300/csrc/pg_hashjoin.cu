@@ -748,6 +748,121 @@ __device__ __forceinline__ void hjg_issue(const char* S, uint64_t n, uint32_t W,
 	if (bulk) pg_bulk_g2s_hint(tin0 + (size_t) b * T * W, S + t * (uint64_t) T * W, bulk, &bar[b], pol);
 }
 
+// Table loads of one tile's ITEMS keys per thread, issued and not yet used:
+// dense tables the 4-byte entry (narrow) or the bitmap word and 8-byte value
+// (wide); hashed tables the first 32-byte bucket.
+template <int MODE, int ITEMS>
+struct HjPending {
+	uint32_t e[ITEMS];
+	uint64_t v[ITEMS];
+	pg_u64x4 bk[ITEMS];
+	uint64_t slot[ITEMS];
+	bool in[ITEMS];
+};
+
+template <int MODE, int ITEMS>
+__device__ __forceinline__ void hj_issue_items(const HjProbeTable& tb, const int64_t (&key)[ITEMS],
+		const bool (&valid)[ITEMS], HjPending<MODE, ITEMS>& pd, uint64_t keep)
+{
+	#pragma unroll
+	for (int j = 0; j < ITEMS; ++j) {
+		pd.in[j] = false;
+		if (MODE != 0) {
+			const unsigned long long d = (unsigned long long) key[j] - (unsigned long long) tb.dmin;
+			pd.e[j] = 0xFFFFFFFFu;
+			if (!valid[j] || d >= tb.drange) continue;
+			pd.in[j] = true;
+			if (MODE == 2) {
+				asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;"
+						: "=r"(pd.e[j]) : "l"(tb.dense32 + d), "l"(keep));
+			} else {
+				pd.e[j] = __ldg(tb.dense_bits + (d >> 5)) >> (d & 31);
+				asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u64 %0, [%1], %2;"
+						: "=l"(pd.v[j]) : "l"(tb.dense_val + d), "l"(keep));
+			}
+		} else {
+			if (!valid[j] || key[j] == PG_EMPTY_KEY) continue;
+			pd.in[j] = true;
+			pd.slot[j] = hj_slot0(key[j], tb.log2cap);
+			pd.bk[j] = pg_ld_bucket32(tb.slots + 2 * pd.slot[j], keep);
+		}
+	}
+}
+
+// Uses the loads hj_issue_items started: hit and value per key (hashed keys
+// that need further buckets probe on, in rounds, here).
+template <int MODE, int ITEMS>
+__device__ __forceinline__ void hj_resolve_items(const HjProbeTable& tb, const int64_t (&key)[ITEMS],
+		const bool (&valid)[ITEMS], HjPending<MODE, ITEMS>& pd, bool (&hit)[ITEMS], uint64_t (&val)[ITEMS],
+		uint64_t keep)
+{
+	if (MODE != 0) {
+		#pragma unroll
+		for (int j = 0; j < ITEMS; ++j) {
+			if (MODE == 2) { hit[j] = pd.in[j] && pd.e[j] != 0xFFFFFFFFu; val[j] = tb.vmin + pd.e[j]; }
+			else { hit[j] = pd.in[j] && (pd.e[j] & 1); val[j] = pd.in[j] ? pd.v[j] : 0; }
+		}
+		return;
+	}
+	const uint64_t mask = (1ull << tb.log2cap) - 1;
+	#pragma unroll
+	for (int j = 0; j < ITEMS; ++j) {
+		hit[j] = false; val[j] = 0;
+		if (valid[j] && key[j] == PG_EMPTY_KEY && tb.nside) { hit[j] = true; val[j] = tb.side[0]; }
+	}
+	for (uint32_t round = 0; ; ++round) {
+		bool any = false;
+		#pragma unroll
+		for (int j = 0; j < ITEMS; ++j) {
+			if (!pd.in[j]) continue;
+			const pg_u64x4 b = pd.bk[j];
+			if ((long long) b.a == key[j]) { hit[j] = true; val[j] = b.b; pd.in[j] = false; }
+			else if (b.a == (unsigned long long) PG_EMPTY_KEY) pd.in[j] = false;
+			else if ((long long) b.c == key[j]) { hit[j] = true; val[j] = b.d; pd.in[j] = false; }
+			else if (b.c == (unsigned long long) PG_EMPTY_KEY) pd.in[j] = false;
+			else if (round >= (mask >> 1)) pd.in[j] = false;     // every bucket seen
+			else pd.slot[j] = (pd.slot[j] + 2) & mask;
+		}
+		#pragma unroll
+		for (int j = 0; j < ITEMS; ++j)
+			if (pd.in[j]) { pd.bk[j] = pg_ld_bucket32(tb.slots + 2 * pd.slot[j], keep); any = true; }
+		if (!any) break;
+	}
+}
+
+// Waits for the tile in buffer b (bounded: a wait that gives up leaves the
+// tile's contents unspecified, every access stays in bounds and the host sees
+// the status); the final tile's bytes past a multiple of 16 are loaded here.
+__device__ __forceinline__ void hjg_arrive(const char* S, uint64_t base, uint32_t rows, uint32_t W,
+		unsigned char* tp, uint64_t* bar, int b, uint32_t& phases, int* status)
+{
+	if (!pg_mbar_wait(&bar[b], (phases >> b) & 1)) pg_set_status(status, PG_ERR_TIMEOUT);
+	phases ^= 1u << b;
+	const uint32_t bytes = rows * W, bulk = bytes & ~15u;
+	if (bulk != bytes) {     // final tile only; block-uniform
+		if (threadIdx.x < (bytes - bulk) / 4)
+			reinterpret_cast<uint32_t*>(tp + bulk)[threadIdx.x] =
+				reinterpret_cast<const uint32_t*>(S + base * W + bulk)[threadIdx.x];
+		__syncthreads();
+	}
+}
+
+template <int ITEMS>
+__device__ __forceinline__ void hjg_keys(const uint32_t* tw, uint32_t rows, uint32_t Ww, uint32_t kw, uint32_t kbytes,
+		int warp, int lane, int64_t (&key)[ITEMS], bool (&valid)[ITEMS])
+{
+	#pragma unroll
+	for (int j = 0; j < ITEMS; ++j) {
+		const uint32_t p = warp * 32 * ITEMS + j * 32 + lane;
+		valid[j] = p < rows;
+		key[j] = 0;
+		if (valid[j]) {
+			const uint32_t* k = tw + p * Ww + kw;
+			key[j] = kbytes == 4 ? (int64_t) (int32_t) k[0] : (int64_t) (((uint64_t) k[1] << 32) | k[0]);
+		}
+	}
+}
+
 template <bool MATERIALIZE, int MODE, int ITEMS>
 __global__ void __launch_bounds__(HJG_THREADS, 2)
 k_probe_staged(const char* __restrict__ S, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes,
@@ -787,48 +902,52 @@ k_probe_staged(const char* __restrict__ S, uint64_t n, uint32_t W, uint32_t koff
 	const bool need_val = src0 >= 64 || (uw == 2 && src1 >= 64);
 	uint64_t tile = blockIdx.x;
 	if (tile >= ntiles) return;
-	if (tid == 0) hjg_issue(S, n, W, T, tile, tin0, bar, 0, stream);
+	const uint64_t G = gridDim.x;
+	// Software pipeline over the CTA's tiles t0, t1, t2, ... in buffers 0, 1,
+	// 2, 0, ...: while tile t is ranked and written out, the table loads of
+	// tile t + 1 are in flight and tile t + 2 is arriving. The copy of t + 2
+	// is issued after tile t's first barrier, when every thread has finished
+	// writing out tile t - 1, whose buffer it takes.
+	if (tid == 0) {
+		hjg_issue(S, n, W, T, tile, tin0, bar, 0, stream);
+		if (tile + G < ntiles) hjg_issue(S, n, W, T, tile + G, tin0, bar, 1, stream);
+	}
 	uint32_t phases = 0;      // bit b: parity expected next on bar[b]
-	int b = 0;
-	for (; tile < ntiles; tile += gridDim.x, b = b == HJG_BUFS - 1 ? 0 : b + 1) {
+	int64_t key[ITEMS];
+	bool valid[ITEMS];
+	HjPending<MODE, ITEMS> pd;
+	{
+		const uint32_t rows = (uint32_t) pg_min64(T, n - tile * T);
+		hjg_arrive(S, tile * T, rows, W, tin0, bar, 0, phases, status);
+		hjg_keys<ITEMS>(reinterpret_cast<const uint32_t*>(tin0), rows, Ww, kw, kbytes, warp, lane, key, valid);
+		hj_issue_items<MODE, ITEMS>(tb, key, valid, pd, keep);
+	}
+	for (int b = 0; tile < ntiles; tile += G, b = b == HJG_BUFS - 1 ? 0 : b + 1) {
+		const int nb = b == HJG_BUFS - 1 ? 0 : b + 1, fb = nb == HJG_BUFS - 1 ? 0 : nb + 1;
 		unsigned char* const tp = tin0 + (size_t) b * T * W;
-		const uint64_t base = tile * T;
-		const uint32_t rows = (uint32_t) pg_min64(T, n - base);
-		// A wait that gives up leaves the tile's contents unspecified; every
-		// later access stays in bounds and the host sees the status.
-		if (!pg_mbar_wait(&bar[b], (phases >> b) & 1)) pg_set_status(status, PG_ERR_TIMEOUT);
-		phases ^= 1u << b;
-		const uint32_t bytes = rows * W, bulk = bytes & ~15u;
-		if (bulk != bytes) {     // final tile only; block-uniform
-			if (tid < (bytes - bulk) / 4)
-				reinterpret_cast<uint32_t*>(tp + bulk)[tid] =
-					reinterpret_cast<const uint32_t*>(S + base * W + bulk)[tid];
-			__syncthreads();
-		}
-		if (tid == 0 && tile + gridDim.x < ntiles)
-			hjg_issue(S, n, W, T, tile + gridDim.x, tin0, bar, b == HJG_BUFS - 1 ? 0 : b + 1, stream);
-
 		const uint32_t* const tw = reinterpret_cast<const uint32_t*>(tp);
-		int64_t key[ITEMS];
-		bool valid[ITEMS], hit[ITEMS];
-		uint64_t val[ITEMS];
-		#pragma unroll
-		for (int j = 0; j < ITEMS; ++j) {
-			const uint32_t p = warp * 32 * ITEMS + j * 32 + lane;
-			valid[j] = p < rows;
-			key[j] = 0;
-			if (valid[j]) {
-				const uint32_t* k = tw + p * Ww + kw;
-				key[j] = kbytes == 4 ? (int64_t) (int32_t) k[0] : (int64_t) (((uint64_t) k[1] << 32) | k[0]);
-			}
+		// Next tile: arrive, keys, table loads issued (used next iteration).
+		int64_t nkey[ITEMS];
+		bool nvalid[ITEMS];
+		HjPending<MODE, ITEMS> npd;
+		const bool has_next = tile + G < ntiles;
+		if (has_next) {
+			unsigned char* const np = tin0 + (size_t) nb * T * W;
+			const uint32_t nrows = (uint32_t) pg_min64(T, n - (tile + G) * T);
+			hjg_arrive(S, (tile + G) * T, nrows, W, np, bar, nb, phases, status);
+			hjg_keys<ITEMS>(reinterpret_cast<const uint32_t*>(np), nrows, Ww, kw, kbytes, warp, lane, nkey, nvalid);
+			hj_issue_items<MODE, ITEMS>(tb, nkey, nvalid, npd, keep);
 		}
-		hj_lookup_items<MODE, ITEMS>(tb, key, valid, hit, val, keep);
+		bool hit[ITEMS];
+		uint64_t val[ITEMS];
+		hj_resolve_items<MODE, ITEMS>(tb, key, valid, pd, hit, val, keep);
 		if (MATERIALIZE) {
 			uint32_t ball[ITEMS], mine = 0;
 			#pragma unroll
 			for (int j = 0; j < ITEMS; ++j) { ball[j] = __ballot_sync(0xffffffffu, hit[j]); mine += __popc(ball[j]); }
 			if (lane == 0) wsum[warp] = mine;
 			__syncthreads();
+			if (tid == 0 && tile + 2 * G < ntiles) hjg_issue(S, n, W, T, tile + 2 * G, tin0, bar, fb, stream);
 			uint32_t pos = 0, total = 0;
 			#pragma unroll
 			for (int w = 0; w < HJG_WARPS; ++w) { const uint32_t c = wsum[w]; pos += w < warp ? c : 0; total += c; }
@@ -871,7 +990,13 @@ k_probe_staged(const char* __restrict__ S, uint64_t n, uint32_t W, uint32_t koff
 					else sum_acc += (unsigned long long) (long long) (int32_t) lo;
 				}
 			}
-			__syncthreads();   // every thread is done with this buffer before it is refilled
+			__syncthreads();   // every thread is done with this tile's buffer
+			if (tid == 0 && tile + 2 * G < ntiles) hjg_issue(S, n, W, T, tile + 2 * G, tin0, bar, fb, stream);
+		}
+		if (has_next) {
+			#pragma unroll
+			for (int j = 0; j < ITEMS; ++j) { key[j] = nkey[j]; valid[j] = nvalid[j]; }
+			pd = npd;
 		}
 	}
 	if (!MATERIALIZE) {
@@ -1874,12 +1999,14 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 		PG_LAUNCHED(ctx);
 		return PG_OK;
 	}
-	// Other widths: materialised rows are staged through shared memory when
-	// tuples and rows are whole words and a tile fits the buffers; counts and
-	// sums, which write nothing, read their key and sum words per thread
-	// (measured faster: 0.44 against 0.51 ms on 64M 24-byte tuples).
+	// Other widths: materialised rows from dense tables are staged through
+	// shared memory when tuples and rows are whole words and a tile fits the
+	// buffers. Counts and sums, which write nothing, read their key and sum
+	// words per thread (0.44 against 0.51 ms staged on 64M 24-byte tuples), and
+	// so do hashed tables, whose pending bucket loads cost the staged kernel
+	// registers (2.34 against 2.40 ms).
 	const int64_t wide = ctx->tune[PG_TUNE_PROBE_WIDE];
-	const bool staged = wide == 2 || wide == 3 || (wide == 0 && materialize);
+	const bool staged = wide == 2 || wide == 3 || (wide == 0 && materialize && mode != 0);
 	if (staged && W % 4 == 0 && W <= HJG_MAX_W && koff % 4 == 0 && pc.ow_words >= 1 &&
 			pc.ow_words <= HJG_MAX_OW && (reinterpret_cast<uintptr_t>(S) & 15) == 0 &&
 			(!materialize || (reinterpret_cast<uintptr_t>(out) & 3) == 0)) {

@@ -256,8 +256,9 @@ def _lines(n, R, seed, miss_every=0):
 @pytest.mark.parametrize("wide", [0, 1, 2, 3])
 def test_join_other_widths(ctx, wide):
     # Probe tuples and output rows other than 16 bytes: staged through shared
-    # memory (2: 4 lookups per thread, 3: 2; 0: rows staged, counts and sums
-    # per thread) or loaded per thread (1); same rows, counts and sums. Dense narrow, dense wide and hashed
+    # memory (2: 4 lookups per thread, 3: 2; 0: rows of dense tables staged,
+    # hashed tables, counts and sums per thread) or loaded per thread (1);
+    # same rows, counts and sums. Dense narrow, dense wide and hashed
     # tables; ragged final tiles whose bytes are not a multiple of 16.
     R = dg.build_relation(60_000, dg.seed_for(601))
     Rw = R.copy(); Rw[:, 1] = dg.raw_words(dg.seed_for(602), 1, 60_000).view(np.int64)
