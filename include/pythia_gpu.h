@@ -114,7 +114,9 @@ int pg_host_is_pinned(pg_ctx* ctx, const void* hptr);
  * memory (cudaDevAttrPageableMemoryAccess, e.g. over NVLink-C2C); else 0. */
 int pg_host_readable(pg_ctx* ctx, const void* hptr);
 /* Host-to-device copy made by the SMs' loads of host memory instead of a
- * copy engine; src must be readable (pg_host_readable), any alignment.
+ * copy engine; src must be readable (pg_host_readable), any alignment, and
+ * stay mapped until the copy has run: unlike pg_h2d, which reports a bad host
+ * range as an error, the kernel's loads of an unmapped address fault it.
  * Replaces the page hand-over of ParallelScanOp (operators/parallelscan.cpp:
  * 176-190) for pages a GPU operator uploads one at a time: measured 181 GB/s
  * for 1 MB pages from 16 threads, against 117 GB/s by copy engine. */

@@ -523,12 +523,37 @@ void InputSide::clear()
 // ---------------------------------------------------------------------------
 // Joins.
 // ---------------------------------------------------------------------------
+namespace {
+// Column pruning between adjacent GPU joins: a join child that keeps its
+// output on the device produces only the columns its parent reads (the
+// parent's join key on that side and its projected columns of that side);
+// `key` and the references' column numbers are remapped to the narrowed rows.
+void prune_join_child(Operator* child, int side, unsigned& key, std::vector<std::pair<int, unsigned> >& refs)
+{
+	GpuJoinBase* cj = dynamic_cast<GpuJoinBase*>(child);
+	if (!cj) return;
+	const unsigned ncols = child->getOutSchema().columns();
+	std::vector<bool> used(ncols, false);
+	used[key] = true;
+	for (size_t i = 0; i < refs.size(); ++i)
+		if (refs[i].first == side) used[refs[i].second] = true;
+	std::vector<unsigned> keep, remap(ncols, 0);
+	for (unsigned i = 0; i < ncols; ++i)
+		if (used[i]) { remap[i] = (unsigned) keep.size(); keep.push_back(i); }
+	if (keep.size() == ncols) return;
+	cj->narrow_projection(keep);
+	key = remap[key];
+	for (size_t i = 0; i < refs.size(); ++i)
+		if (refs[i].first == side) refs[i].second = remap[refs[i].second];
+}
+}  // namespace
+
 void GpuJoinBase::init(libconfig::Config& root, libconfig::Setting& node)
 {
 	Operator::init(root, node);
 	libconfig::Setting& pr = node["projection"];
-	Schema& bs = buildOp->getOutSchema();
-	Schema& ps = probeOp->getOutSchema();
+	// (side, column) of every output column: side 0 build, 1 probe.
+	std::vector<std::pair<int, unsigned> > refs;
 	for (int i = 0; i < pr.getLength(); ++i) {
 		// "B$i" / "P$i" as createProjectionVector reads them (join.cpp:141-182).
 		std::string s = pr[i];
@@ -540,19 +565,30 @@ void GpuJoinBase::init(libconfig::Config& root, libconfig::Setting& node)
 		if (!is) throw std::invalid_argument("bad projection `" + s + "'");
 		const char side = s[d - 1];
 		if (side != 'B' && side != 'P') throw std::invalid_argument("bad projection `" + s + "'");
-		Schema& src = side == 'B' ? bs : ps;
+		Schema& src = side == 'B' ? buildOp->getOutSchema() : probeOp->getOutSchema();
 		if (attr >= src.columns()) throw std::invalid_argument("projection column out of range `" + s + "'");
+		refs.push_back(std::make_pair(side == 'B' ? 0 : 1, attr));
+	}
+	buildkey_ = (int) node["buildjattr"];
+	probekey_ = (int) node["probejattr"];
+	if (buildkey_ >= buildOp->getOutSchema().columns() || probekey_ >= probeOp->getOutSchema().columns())
+		throw std::invalid_argument("join attribute out of range");
+	if (g_exchange) {
+		prune_join_child(buildOp, 0, buildkey_, refs);
+		prune_join_child(probeOp, 1, probekey_, refs);
+	}
+	Schema& bs = buildOp->getOutSchema();
+	Schema& ps = probeOp->getOutSchema();
+	for (size_t i = 0; i < refs.size(); ++i) {
+		Schema& src = refs[i].first == 0 ? bs : ps;
+		const unsigned attr = refs[i].second;
 		schema.add(src.get(attr));
 		pg_col c;
-		c.side = side == 'B' ? 0 : 1;
+		c.side = refs[i].first == 0 ? 0 : 1;
 		c.off = col_offset(src, attr);
 		c.bytes = src.getColumnWidth(attr);
 		cols_.push_back(c);
 	}
-	buildkey_ = (int) node["buildjattr"];
-	probekey_ = (int) node["probejattr"];
-	if (buildkey_ >= bs.columns() || probekey_ >= ps.columns())
-		throw std::invalid_argument("join attribute out of range");
 	if (!key_bytes(bs, buildkey_) || key_bytes(bs, buildkey_) != key_bytes(ps, probekey_))
 		throw std::invalid_argument("GPU joins need integer join keys of the same width on both sides");
 	groups_.parse(node, 1);

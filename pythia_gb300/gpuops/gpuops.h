@@ -72,7 +72,8 @@ void set_device_exchange(bool on);
 // off by default; when on, operator threads append (plan node, thread,
 // phase, host monotonic ns) entries to a fixed ring until it is full.
 // trace_enable(true) also empties the ring; trace_dump writes one line per entry,
-// "ns node thread phase", and returns the bytes the whole dump needs.
+// "ns node thread phase", and returns the bytes the whole dump needs. Turn
+// it on or off between plan runs, not while operator threads run.
 void trace_enable(bool on);
 void trace(const std::string& node, int tid, const char* phase);
 unsigned long long trace_dump(char* buf, unsigned long long len);
@@ -221,8 +222,9 @@ public:
 	virtual void threadClose(unsigned short threadid);
 	virtual void destroy();
 	virtual DeviceSpan device_share(unsigned short threadid) { return output_.share(threadid); }
-	// A gpuproject above folds into the join: output columns `keep` (indices
-	// into the current projection), in that order.
+	// A gpuproject above folds into the join, or a GPU join above reads only
+	// some columns: output columns `keep` (indices into the current
+	// projection), in that order.
 	void narrow_projection(const std::vector<unsigned>& keep);
 protected:
 	// Whether run_device applies probe_preds_ itself (else the probe side is

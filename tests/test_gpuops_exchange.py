@@ -206,3 +206,59 @@ def test_pinned_leaves_copy_to_the_device_directly():
     assert sum(per) == n
     assert np.array_equal(canon(rows), canon(want))
     assert st["h2d"] == R.nbytes + S.nbytes == st["direct"]
+
+
+def test_ordinary_pages_go_in_place_where_the_device_reads_host_memory():
+    # Pages of an ordinary (pageable) relation are uploaded by the SMs' loads
+    # when the device reads pageable memory (GB300 over NVLink-C2C), and are
+    # staged through pinned buffers otherwise; the rows are the same.
+    from pythia_gb300 import gpu
+    R = dg.build_relation(20_000, dg.seed_for(416))
+    S = dg.probe_uniform(90_000, R, dg.seed_for(417))
+    plans.register("R", R); plans.register("S", S)
+    plan = PART_JOIN.format(hi=20_000, jtype="gpuhashjoin", groups="((0), (1), (2), (3))")
+    want, n, _ = orc.hashjoin(R, S, proj=(("P", 8, 8), ("B", 8, 8)), hash=orc.hashcfg("modulo", 1 << 12))
+    plans.transfer_stats(reset=True)
+    rows, per = plans.run(plan, threads=4)
+    st = plans.transfer_stats(reset=True)
+    assert sum(per) == n and np.array_equal(canon(rows), canon(want))
+    ctx = gpu.Context(0)
+    try:
+        readable = gpu.lib().pg_host_readable(ctx.h, S.ctypes.data) == 1
+    finally:
+        ctx.close()
+    assert st["h2d"] == R.nbytes + S.nbytes
+    assert st["direct"] == (st["h2d"] if readable else 0)
+
+
+def test_join_over_join_reads_only_the_columns_it_uses():
+    # The parent joins on the child's third column and projects its first;
+    # the child's second column is dropped on the device (column pruning)
+    # and the parent's key is remapped. Same rows with the exchange off.
+    nR, nT = 30_000, 5_000
+    R = dg.build_relation(nR, dg.seed_for(418))
+    R[:, 1] = R[:, 0] % nT + 1
+    T = dg.build_relation(nT, dg.seed_for(419))
+    S = dg.probe_uniform(120_000, R, dg.seed_for(420))
+    plans.register("R", R); plans.register("S", S); plans.register("T", T)
+    plan = """
+    buffsize = 8192;
+    treeroot = { name = "jb"; build = { name = "t"; }; probe = { name = "ja"; build = { name = "r"; }; probe = { name = "s"; }; }; };
+    r = { type = "memscan"; relation = "R"; schema = ("long", "long"); };
+    s = { type = "memscan"; relation = "S"; schema = ("long", "long"); };
+    t = { type = "memscan"; relation = "T"; schema = ("long", "long"); };
+    ja = { type = "gpuhashjoin"; buildjattr = 0; probejattr = 0; projection = ("P$0", "P$1", "B$1");
+           threadgroups = ((0, 1, 2, 3)); hash = { fn = "modulo"; buckets = 1024; }; tuplesperbucket = 4; };
+    jb = { type = "gpuhashjoin"; buildjattr = 0; probejattr = 2; projection = ("P$0", "B$1");
+           threadgroups = ((0, 1, 2, 3)); hash = { fn = "modulo"; buckets = 1024; }; tuplesperbucket = 4; };
+    """
+    ja, _, _ = orc.hashjoin(R, S, proj=(("P", 0, 8), ("P", 8, 8), ("B", 8, 8)), hash=orc.hashcfg("modulo", 1 << 12))
+    want, n, _ = orc.hashjoin(T, ja.view(np.int64).reshape(-1, 3), proj=(("P", 0, 8), ("B", 8, 8)), pkey=(16, 8),
+                              hash=orc.hashcfg("modulo", 1 << 12))
+    assert n == 120_000
+    (rows_on, _, st_on), (rows_off, _, st_off) = run_both(plan, 4)
+    assert np.array_equal(canon(rows_on), canon(want))
+    assert np.array_equal(canon(rows_off), canon(want))
+    assert st_on["in_place"] == 1 and st_on["d2h"] == n * 16            # jb takes ja's rows in place
+    # Off, the child's rows travel whole: 24 bytes each, down and up again.
+    assert st_off["d2h"] == 120_000 * 24 + n * 16
