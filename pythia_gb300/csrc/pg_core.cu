@@ -61,6 +61,19 @@ extern "C" int pg_init(int device, uint64_t reserved_bytes, pg_ctx** out)
 	// Keep freed blocks in the pool: operators allocate scratch per call.
 	uint64_t thresh = UINT64_MAX;
 	cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &thresh);
+	// Large buffers (join outputs, gathered inputs) come from a pool of their
+	// own: interleaved with the many smaller staging chunks they left the
+	// shared pool too fragmented to reuse, and a 1 GB output then mapped new
+	// memory on every plan run (about 1.1 ms).
+	ctx->big_pool = nullptr;
+	cudaMemPoolProps props;
+	memset(&props, 0, sizeof(props));
+	props.allocType = cudaMemAllocationTypePinned;
+	props.location.type = cudaMemLocationTypeDevice;
+	props.location.id = device;
+	if (cudaMemPoolCreate(&ctx->big_pool, &props) == cudaSuccess)
+		cudaMemPoolSetAttribute(ctx->big_pool, cudaMemPoolAttrReleaseThreshold, &thresh);
+	else { ctx->big_pool = nullptr; cudaGetLastError(); }
 	if (reserved_bytes) {
 		// Warm the pool so the first operator does not pay for growth.
 		void* p = nullptr;
@@ -82,6 +95,8 @@ extern "C" int pg_shutdown(pg_ctx* ctx)
 	cudaSetDevice(ctx->device);
 	cudaDeviceSynchronize();
 	cudaFree(ctx->d_status);
+	// Released once its last allocation is freed, if any is still out.
+	if (ctx->big_pool) cudaMemPoolDestroy(ctx->big_pool);
 	delete ctx;
 	return PG_OK;
 }
@@ -294,7 +309,8 @@ extern "C" int pg_memset(pg_ctx* ctx, pg_stream s, void* dst, int value, uint64_
 
 int pg_alloc_async(pg_ctx* ctx, cudaStream_t s, void** p, size_t bytes)
 {
-	cudaError_t e = cudaMallocFromPoolAsync(p, bytes ? bytes : 16, ctx->pool, s);
+	cudaMemPool_t pool = bytes >= PG_BIG_ALLOC && ctx->big_pool ? ctx->big_pool : ctx->pool;
+	cudaError_t e = cudaMallocFromPoolAsync(p, bytes ? bytes : 16, pool, s);
 	if (e != cudaSuccess) return pg_cuda_fail(ctx, e, "cudaMallocFromPoolAsync");
 	return PG_OK;
 }

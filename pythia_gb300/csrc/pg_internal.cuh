@@ -15,6 +15,7 @@ struct pg_ctx {
 	int sm_count;
 	int64_t tune[PG_TUNE_COUNT];   // launch-shape knobs, PG_TUNE_* (0 = built-in choice)
 	cudaMemPool_t pool;
+	cudaMemPool_t big_pool;  // allocations of PG_BIG_ALLOC bytes or more (NULL: all from `pool`)
 	int* d_status;          // sticky device error word (PG_ERR_*), 0 = fine
 	unsigned long long* d_scratch64;  // small per-context device scratch (counters)
 	int pageable_access;    // kernels may read pageable host memory (cudaDevAttrPageableMemoryAccess)
@@ -42,7 +43,9 @@ int pg_cuda_fail(pg_ctx* ctx, cudaError_t e, const char* what);
 		if (e_ != cudaSuccess) return pg_cuda_fail((ctx), e_, "kernel launch"); \
 	} while (0)
 
-// Stream-ordered scratch from the context's pool.
+// Stream-ordered scratch from the context's pools (PG_BIG_ALLOC bytes and more
+// from the large-buffer pool).
+#define PG_BIG_ALLOC (256ull << 20)
 int pg_alloc_async(pg_ctx* ctx, cudaStream_t s, void** p, size_t bytes);
 void pg_free_async(pg_ctx* ctx, cudaStream_t s, void* p);
 // Reads the sticky status after synchronising `s`; returns its PG_ERR_* code.

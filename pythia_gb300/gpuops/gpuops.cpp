@@ -331,6 +331,30 @@ void stage_give(char* p)
 }
 }  // namespace
 
+namespace {
+pthread_mutex_t g_stream_mu = PTHREAD_MUTEX_INITIALIZER;
+pg_stream g_thread_streams[MAX_THREADS];
+
+// The stream of plan thread `tid`, made on first use and kept for the
+// process. Device memory an operator frees on it in one plan run is allocated
+// again on it in the next, in stream order, so the pool reuses its blocks
+// instead of mapping new memory (a stream destroyed after each launch left
+// 1 GB buffers that later runs did not reuse). A plan thread runs one
+// operator phase at a time; plans run at the same time share the streams
+// of equal thread ids, which orders their work but keeps it correct.
+pg_stream thread_stream(pg_ctx* ctx, int tid)
+{
+	pthread_mutex_lock(&g_stream_mu);
+	if (!g_thread_streams[tid]) {
+		pg_stream s = 0;
+		if (pg_stream_create(ctx, &s) == PG_OK) g_thread_streams[tid] = s;
+	}
+	const pg_stream s = g_thread_streams[tid];
+	pthread_mutex_unlock(&g_stream_mu);
+	return s;
+}
+}  // namespace
+
 void InputSide::setup(Operator* child, const std::string& node)
 {
 	clear();
@@ -392,8 +416,7 @@ bool InputSide::stage(Operator* child, unsigned short tid)
 {
 	pg_ctx* ctx = shared_context();
 	Staged& u = staged_[tid];
-	pg_stream st = 0;
-	if (pg_stream_create(ctx, &st) != PG_OK) return false;
+	const pg_stream st = thread_stream(ctx, tid);
 	char* pin[2] = { stage_take(ctx), stage_take(ctx) };
 	bool ok = pin[0] && pin[1];
 	int cur = 0;
@@ -437,7 +460,6 @@ bool InputSide::stage(Operator* child, unsigned short tid)
 	if (pg_sync(ctx, st) != PG_OK) ok = false;
 	stage_give(pin[0]);
 	stage_give(pin[1]);
-	pg_stream_destroy(ctx, st);
 	return ok;
 }
 
@@ -636,9 +658,8 @@ int GpuJoinBase::run_group(int g)
 	const unsigned ow = schema.getTupleSize();
 	pg_ctx* ctx = shared_context();
 	if (!ctx) return PG_ERR_CUDA;
-	pg_stream st = 0;
-	int rc = pg_stream_create(ctx, &st);
-	if (rc) return rc;
+	const pg_stream st = thread_stream(ctx, mem[0]);
+	int rc = PG_OK;
 	const char *dR = 0, *dS = 0;
 	unsigned long long nR = 0, nS = 0;
 	void *tR = 0, *tS = 0, *dO = 0;
@@ -682,7 +703,6 @@ int GpuJoinBase::run_group(int g)
 		output_.set_rows(g, rc ? 0 : rows);
 	}
 	if (dO) pg_buffer_free_async(ctx, st, dO);
-	pg_stream_destroy(ctx, st);
 	return rc;
 }
 
@@ -859,9 +879,8 @@ int GpuPartitionOp::run_partition()
 	if (!ctx) return PG_ERR_CUDA;
 	std::vector<int> all(nparts_);
 	for (unsigned t = 0; t < nparts_; ++t) all[t] = (int) t;
-	pg_stream st = 0;
-	int rc = pg_stream_create(ctx, &st);
-	if (rc) return rc;
+	const pg_stream st = thread_stream(ctx, 0);
+	int rc = PG_OK;
 	const char* din = 0;
 	unsigned long long n = 0;
 	void *tin = 0, *dout = 0, *doffs = 0, *scratch = 0;
@@ -902,7 +921,6 @@ int GpuPartitionOp::run_partition()
 	if (!rc && on_device_) { served_.own_device(dout); dout = 0; }
 	if (doffs) pg_buffer_free_async(ctx, st, doffs);
 	if (dout) pg_buffer_free_async(ctx, st, dout);
-	pg_stream_destroy(ctx, st);
 	return rc;
 }
 
@@ -999,9 +1017,8 @@ int GpuAggregateOp::aggregate(const std::vector<int>& members, int g)
 	if (!ctx) return PG_ERR_CUDA;
 	Schema& is = nextOp->getOutSchema();
 	const unsigned w = is.getTupleSize(), ow = schema.getTupleSize();
-	pg_stream st = 0;
-	int rc = pg_stream_create(ctx, &st);
-	if (rc) return rc;
+	const pg_stream st = thread_stream(ctx, members[0]);
+	int rc = PG_OK;
 	const char* din = 0;
 	unsigned long long n = 0;
 	void *tin = 0, *dout = 0;
@@ -1038,7 +1055,6 @@ int GpuAggregateOp::aggregate(const std::vector<int>& members, int g)
 		output_.set_rows(g, rc ? 0 : ng);
 	}
 	if (dout) pg_buffer_free_async(ctx, st, dout);
-	pg_stream_destroy(ctx, st);
 	return rc;
 }
 
@@ -1169,9 +1185,8 @@ int GpuFilterOp::run(unsigned short tid)
 	pg_ctx* ctx = shared_context();
 	if (!ctx) return PG_ERR_CUDA;
 	const unsigned w = schema.getTupleSize();
-	pg_stream st = 0;
-	int rc = pg_stream_create(ctx, &st);
-	if (rc) return rc;
+	const pg_stream st = thread_stream(ctx, tid);
+	int rc = PG_OK;
 	const char* din = 0;
 	unsigned long long n = 0;
 	void *tin = 0, *dout = 0;
@@ -1207,7 +1222,6 @@ int GpuFilterOp::run(unsigned short tid)
 		if (!rc) rc = pg_sync(ctx, st);
 	}
 	if (dout) pg_buffer_free_async(ctx, st, dout);
-	pg_stream_destroy(ctx, st);
 	return rc;
 }
 
@@ -1295,9 +1309,8 @@ int GpuProjectOp::run(unsigned short tid)
 	pg_ctx* ctx = shared_context();
 	if (!ctx) return PG_ERR_CUDA;
 	const unsigned w = nextOp->getOutSchema().getTupleSize(), ow = schema.getTupleSize();
-	pg_stream st = 0;
-	int rc = pg_stream_create(ctx, &st);
-	if (rc) return rc;
+	const pg_stream st = thread_stream(ctx, tid);
+	int rc = PG_OK;
 	const char* din = 0;
 	unsigned long long n = 0;
 	void *tin = 0, *dout = 0;
@@ -1323,7 +1336,6 @@ int GpuProjectOp::run(unsigned short tid)
 	if (tin) pg_buffer_free_async(ctx, st, tin);
 	if (!rc) rc = pg_sync(ctx, st);
 	if (dout) pg_buffer_free_async(ctx, st, dout);
-	pg_stream_destroy(ctx, st);
 	return rc;
 }
 
