@@ -1023,10 +1023,14 @@ int GpuAggregateOp::aggregate(const std::vector<int>& members, int g)
 	unsigned long long n = 0;
 	void *tin = 0, *dout = 0;
 	uint64_t ng = 0;
-	if (!(rc = in_.gather(ctx, st, members, w, &din, &n, &tin)) &&
-			!(rc = pg_buffer_alloc_async(ctx, st, std::max<unsigned long long>(n, 1) * ow, &dout))) {
+	// Output room for up to 1M groups first (at most one per input row); a
+	// larger count is reported by pg_groupby and the aggregation reruns with
+	// room for exactly that many.
+	unsigned long long cap = 1;
+	if (!(rc = in_.gather(ctx, st, members, w, &din, &n, &tin)))
+		cap = std::max<unsigned long long>(1, std::min<unsigned long long>(n, 1ull << 20));
+	if (!rc && !(rc = pg_buffer_alloc_async(ctx, st, cap * ow, &dout))) {
 		trace(node_, members[0], "gathered");
-		const unsigned long long cap = std::max<unsigned long long>(n, 1);
 		pg_rel r;
 		r.data = din; r.n = n; r.width = w;
 		r.key_off = field_ >= 0 ? col_offset(is, field_) : 0;
@@ -1037,7 +1041,15 @@ int GpuAggregateOp::aggregate(const std::vector<int>& members, int g)
 			const ColumnType t = is.getColumnType(sumfield_);
 			vt = t == CT_INTEGER ? PG_VAL_INT : t == CT_DECIMAL ? PG_VAL_DEC : PG_VAL_LONG;
 		}
-		if (!(rc = pg_groupby(ctx, st, &r, voff, vt, agg_, 0, dout, cap, &ng)) && !on_device_) {
+		rc = pg_groupby(ctx, st, &r, voff, vt, agg_, 0, dout, cap, &ng);
+		if (rc == PG_ERR_OUTPUT_FULL) {
+			pg_buffer_free_async(ctx, st, dout);
+			dout = 0;
+			cap = ng;
+			if (!(rc = pg_buffer_alloc_async(ctx, st, cap * ow, &dout)))
+				rc = pg_groupby(ctx, st, &r, voff, vt, agg_, 0, dout, cap, &ng);
+		}
+		if (!rc && !on_device_) {
 			std::vector<char>& out = output_.buffer(g);
 			out.resize((size_t) (ng * ow));
 			if (ng) rc = pg_d2h(ctx, st, &out[0], dout, ng * ow);

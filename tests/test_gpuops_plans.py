@@ -141,6 +141,20 @@ def test_aggregate_sum_global_dec():
     assert np.all(np.abs(g - e) <= DEC_RTOL * np.abs(e))
 
 
+def test_aggregate_more_groups_than_its_first_output_room():
+    # 1.2M groups: more than the 1M rows of output room a GPU aggregate starts
+    # with; the operator reruns with room for the count pg_groupby reported.
+    n, groups = 1_500_000, 1_200_000
+    R = dg.uniform_keys(n, groups, dg.seed_for(79))
+    R[:, 0] = np.arange(n, dtype=np.int64) * 7919 % groups          # exactly 1.2M keys
+    plans.register("R", R)
+    rows, _ = plans.run(agg_plan("gpuaggregate_sum", "field = 0; sumfield = 1;", "global = true; threads = 4;",
+                                 schema='("long", "long")'), threads=4)
+    want = orc.groupby(R, key=(0, 8), val=(8, "long"), agg="sum", hash=orc.hashcfg("modulo", 1 << 20))
+    assert rows.shape[0] == want.shape[0] > (1 << 20)
+    assert np.array_equal(canon(rows), canon(want))
+
+
 def test_aggregate_thread_local_each_thread_its_own_groups():
     R = dg.uniform_keys(50_000, 700, dg.seed_for(78))
     plans.register("R", R)
