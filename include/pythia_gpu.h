@@ -282,6 +282,17 @@ int pg_project(pg_ctx* ctx, pg_stream stream, const pg_rel* in, const pg_col* co
  * tuples of a dense table and predicates on int/long/dec columns the probe
  * kernel evaluates them before its table lookups (no filtered copy of S);
  * otherwise S is filtered first.                                          */
+/* pg_hashjoin_probe over a probe side held as `nspans` separate arrays (the
+ * pages several engine threads uploaded), as if they were one relation:
+ * same rows (order across spans unspecified), count and sum, without first
+ * copying the spans together. All spans share width and key position.
+ * Tables with repeated build keys: PG_ERR_UNSUPPORTED (gather and use
+ * pg_hashjoin_probe). Replaces HashJoinOp's probe of each thread's own pages
+ * against its group's table (getNext and readNextTupleFromProbe,
+ * operators/join.cpp:503-603). */
+int pg_hashjoin_probe_spans(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht, const pg_rel* spans, int nspans,
+		const pg_col* proj, int nproj, void* out, uint64_t out_capacity, int flags, int sum_col,
+		pg_join_result* res);
 int pg_hashjoin_probe_where(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht, const pg_rel* S,
 		const pg_pred* preds, int npred, const pg_col* proj, int nproj,
 		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res);

@@ -2201,6 +2201,63 @@ extern "C" int pg_hashjoin_probe_where(pg_ctx* ctx, pg_stream stream, pg_hashtab
 	return rc;
 }
 
+// Probe side held as separate arrays (the chunks several threads uploaded):
+// one launch per span, all reserving output ranges from one cursor, then one
+// readback. Unique-key tables only, where every probe kernel but the
+// positional 16-byte one writes through the cursor; with counts == nullptr
+// hj_launch_unique never takes the positional path.
+extern "C" int pg_hashjoin_probe_spans(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht, const pg_rel* spans,
+		int nspans, const pg_col* proj, int nproj, void* out, uint64_t out_capacity, int flags, int sum_col,
+		pg_join_result* res)
+{
+	if (!ctx || !ht || !res || (nspans > 0 && !spans) || nspans < 0)
+		return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe_spans: null argument");
+	if (!ht->unique || !ht->inline_val)
+		return pg_fail(ctx, PG_ERR_UNSUPPORTED, "pg_hashjoin_probe_spans: the table has repeated keys");
+	res->n_out = 0; res->sum = 0;
+	if (nspans == 0) return PG_OK;
+	int rc;
+	for (int i = 0; i < nspans; ++i) {
+		if ((rc = hj_validate_rel(ctx, &spans[i], "pg_hashjoin_probe_spans"))) return rc;
+		if (spans[i].width != spans[0].width || spans[i].key_off != spans[0].key_off ||
+				spans[i].key_bytes != spans[0].key_bytes)
+			return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe_spans: spans of different layouts");
+	}
+	if ((rc = hj_validate_proj(ctx, proj, nproj, ht->wR, spans[0].width))) return rc;
+	HjCols pc;
+	if ((rc = hj_make_cols(ctx, ht, proj, nproj, &pc))) return rc;
+	const bool materialize = (flags & PG_JOIN_MATERIALIZE) != 0;
+	if (sum_col >= nproj) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe_spans: sum_col out of range");
+	if (!(flags & PG_JOIN_SUM)) sum_col = -1;
+	if (materialize && out_capacity && !out) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe_spans: null output");
+	cudaStream_t s = (cudaStream_t) stream;
+	unsigned long long* acc = nullptr;   // [cursor, count, sum, spare]
+	if ((rc = pg_alloc_async(ctx, s, (void**) &acc, 64))) return rc;
+	PG_CUDA(ctx, cudaMemsetAsync(acc, 0, 64, s));
+	const bool fold = materialize && (sum_col >= 0 || (flags & PG_JOIN_COUNT));
+	for (int pass = 0; pass < (fold ? 2 : 1); ++pass) {
+		const bool m = materialize && pass == 0;
+		for (int i = 0; i < nspans && !rc; ++i) {
+			const pg_rel& S = spans[i];
+			if (!S.n) continue;
+			rc = hj_launch_unique(ctx, s, ht, (const char*) S.data, S.n, S.width, S.key_off, S.key_bytes, pc,
+					m ? (char*) out : nullptr, m ? out_capacity : 0, acc, m, m ? -1 : sum_col);
+		}
+	}
+	unsigned long long h[4] = {0, 0, 0, 0};
+	if (!rc) {
+		PG_CUDA(ctx, cudaMemcpyAsync(h, acc, 32, cudaMemcpyDeviceToHost, s));
+		rc = pg_check_status(ctx, s, "pg_hashjoin_probe_spans");
+	}
+	pg_free_async(ctx, s, acc);
+	if (rc) return rc;
+	res->n_out = materialize ? h[0] : h[1];
+	res->sum = (int64_t) h[2];
+	if (materialize && res->n_out > out_capacity)
+		return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_hashjoin_probe_spans: output capacity too small");
+	return PG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Whole join through host buffers: build from R, then stream S through the
 // device in chunks on three streams so that the host->device copy of chunk

@@ -67,7 +67,8 @@ SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_st
            "pg_hashjoin_groupby", "pg_stream_create_urgent", "pg_autotune_batch",
            "pg_hashtable_image_size", "pg_hashtable_serialize", "pg_hashtable_deserialize",
            "pg_hashtable_save", "pg_hashtable_load", "pg_filter", "pg_project", "pg_hashjoin_probe_where",
-           "pg_host_register", "pg_host_unregister", "pg_host_is_pinned", "pg_host_readable", "pg_h2d_sm"]
+           "pg_host_register", "pg_host_unregister", "pg_host_is_pinned", "pg_host_readable", "pg_h2d_sm",
+           "pg_hashjoin_probe_spans"]
 TUNE = {"probe_ctas_per_sm": 0, "probe_variant": 1, "dense": 2, "partition_tile": 3,
         "groupby_smem_groups": 4, "radix_bits": 5, "probe_items": 6, "probe_cache": 7, "probe_passes": 8, "groupby_path": 9,
         "probe_wide": 10}
@@ -113,6 +114,7 @@ def lib():
             "pg_partition_sort": ([vp, vp, P(Rel), vp, u32, vp], ci),
             "pg_hashjoin_build": ([vp, vp, P(Rel), P(Col), ci, P(vp)], ci),
             "pg_hashjoin_probe": ([vp, vp, vp, P(Rel), P(Col), ci, vp, u64, ci, ci, P(JoinResult)], ci),
+            "pg_hashjoin_probe_spans": ([vp, vp, vp, P(Rel), ci, P(Col), ci, vp, u64, ci, ci, P(JoinResult)], ci),
             "pg_hashtable_free": ([vp, vp], ci),
             "pg_hashjoin_host": ([vp, P(Rel), P(Rel), P(Col), ci, vp, u64, ci, ci, P(JoinResult)], ci),
             "pg_groupby": ([vp, vp, P(Rel), u32, ci, ci, u64, vp, u64, P(u64)], ci),

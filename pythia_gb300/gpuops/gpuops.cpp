@@ -522,6 +522,32 @@ int InputSide::gather(pg_ctx* ctx, pg_stream st, const std::vector<int>& members
 	return rc;
 }
 
+bool InputSide::pieces(const std::vector<int>& members, unsigned width,
+		std::vector<std::pair<const char*, unsigned long long> >& out) const
+{
+	out.clear();
+	if (!width) return false;
+	std::vector<std::pair<const char*, unsigned long long> > all;
+	for (size_t i = 0; i < members.size(); ++i) {
+		const int t = members[i];
+		if (dev_) {
+			if (spans_[t].rows) all.push_back(std::make_pair(spans_[t].data, spans_[t].rows));
+		} else if (!host_[t].empty()) {
+			return false;
+		} else {
+			for (size_t c = 0; c < staged_[t].chunks.size(); ++c)
+				if (staged_[t].used[c])
+					all.push_back(std::make_pair((const char*) staged_[t].chunks[c], staged_[t].used[c] / width));
+		}
+	}
+	// Arrays that follow each other in memory are one piece.
+	for (size_t i = 0; i < all.size(); ++i) {
+		if (!out.empty() && out.back().first + out.back().second * width == all[i].first) out.back().second += all[i].second;
+		else out.push_back(all[i]);
+	}
+	return true;
+}
+
 void InputSide::release(int tid, pg_stream st)
 {
 	std::vector<char>().swap(host_[tid]);
@@ -666,8 +692,25 @@ int GpuJoinBase::run_group(int g)
 	unsigned long long rows = 0;
 	const unsigned wR = buildOp->getOutSchema().getTupleSize(), wS = probeOp->getOutSchema().getTupleSize();
 	void* tF = 0;
-	if (!(rc = build_.gather(ctx, st, mem, wR, &dR, &nR, &tR)) &&
-			!(rc = probe_.gather(ctx, st, mem, wS, &dS, &nS, &tS))) {
+	// A probe side of several device arrays whose tuples are not 16 bytes is
+	// probed array by array (the kernels for those widths append through one
+	// output cursor), not copied together first; 16-byte tuples keep the
+	// copy, for the positional kernel that needs one array.
+	bool spans = false;
+	if (!(rc = build_.gather(ctx, st, mem, wR, &dR, &nR, &tR)) && probe_preds_.empty() && wS != 16) {
+		std::vector<std::pair<const char*, unsigned long long> > pcs;
+		if (probe_.pieces(mem, wS, pcs) && pcs.size() > 1) {
+			std::vector<pg_rel> srels;
+			for (size_t i = 0; i < pcs.size(); ++i) srels.push_back(side_rel(probeOp, probekey_, pcs[i].first, pcs[i].second));
+			trace(node_, mem[0], "gathered");
+			const pg_rel r = side_rel(buildOp, buildkey_, dR, nR);
+			rc = run_device_spans(ctx, st, r, srels, &dO, &rows);
+			spans = rc != PG_ERR_UNSUPPORTED;
+			if (!spans) rc = PG_OK;
+			else trace(node_, mem[0], "joined");
+		}
+	}
+	if (!rc && !spans && !(rc = probe_.gather(ctx, st, mem, wS, &dS, &nS, &tS))) {
 		trace(node_, mem[0], "gathered");
 		if (!probe_preds_.empty() && !probe_predicates() && nS) {
 			// A fused gpufilter's predicates, applied to the probe side here.
@@ -782,6 +825,39 @@ int GpuHashJoinOp::run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const 
 		trace(node_, 0, "out allocated");
 		rc = pg_hashjoin_probe_where(ctx, st, ht, &S, probe_preds_.empty() ? 0 : &probe_preds_[0],
 				(int) probe_preds_.size(), &cols_[0], (int) cols_.size(), o, cap, PG_JOIN_MATERIALIZE, -1, &res);
+		if (rc == PG_ERR_OUTPUT_FULL && attempt == 0) {
+			pg_buffer_free_async(ctx, st, o);
+			o = 0;
+			cap = res.n_out;
+			continue;
+		}
+		break;
+	}
+	pg_hashtable_free(ctx, ht);
+	if (rc) { if (o) pg_buffer_free_async(ctx, st, o); return rc; }
+	*out = o;
+	*rows = res.n_out;
+	return PG_OK;
+}
+
+int GpuHashJoinOp::run_device_spans(pg_ctx* ctx, pg_stream st, const pg_rel& R, const std::vector<pg_rel>& S,
+		void** out, unsigned long long* rows)
+{
+	const unsigned ow = schema.getTupleSize();
+	pg_hashtable* ht = 0;
+	int rc = pg_hashjoin_build(ctx, st, &R, &cols_[0], (int) cols_.size(), &ht);
+	if (rc) return rc;
+	trace(node_, 0, "built");
+	unsigned long long cap = 0;
+	for (size_t i = 0; i < S.size(); ++i) cap += S[i].n;
+	cap = std::max<unsigned long long>(cap, 1);
+	void* o = 0;
+	pg_join_result res;
+	res.n_out = 0; res.sum = 0;
+	for (int attempt = 0; attempt < 2; ++attempt) {
+		if ((rc = pg_buffer_alloc_async(ctx, st, cap * ow, &o))) break;
+		rc = pg_hashjoin_probe_spans(ctx, st, ht, &S[0], (int) S.size(), &cols_[0], (int) cols_.size(), o, cap,
+				PG_JOIN_MATERIALIZE, -1, &res);
 		if (rc == PG_ERR_OUTPUT_FULL && attempt == 0) {
 			pg_buffer_free_async(ctx, st, o);
 			o = 0;

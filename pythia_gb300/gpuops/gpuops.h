@@ -189,6 +189,11 @@ public:
 	// memory the caller frees after the stream's work).
 	int gather(pg_ctx* ctx, pg_stream st, const std::vector<int>& members, unsigned width,
 			const char** data, unsigned long long* rows, void** tmp);
+	// The rows of `members` as the device arrays they lie in (GPU child spans
+	// or staged chunks), in order, without copying: (data, tuples) pairs.
+	// False when some rows are in host memory.
+	bool pieces(const std::vector<int>& members, unsigned width,
+			std::vector<std::pair<const char*, unsigned long long> >& out) const;
 	// Frees thread `tid`'s staged input (after the work on `st` that reads it).
 	void release(int tid, pg_stream st = 0);
 	void clear();
@@ -233,6 +238,14 @@ protected:
 	// Joins device inputs on `st` into device rows *out (freed by the caller).
 	virtual int run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
 			unsigned long long* rows) = 0;
+	// The same with the probe side as separate device arrays, not copied
+	// together; PG_ERR_UNSUPPORTED sends the caller to run_device.
+	virtual int run_device_spans(pg_ctx* ctx, pg_stream st, const pg_rel& R, const std::vector<pg_rel>& S,
+			void** out, unsigned long long* rows)
+	{
+		(void) ctx; (void) st; (void) R; (void) S; (void) out; (void) rows;
+		return PG_ERR_UNSUPPORTED;
+	}
 	std::vector<pg_col> cols_;
 	unsigned buildkey_, probekey_;
 	// Predicates of a gpufilter directly under the probe side, applied by
@@ -257,6 +270,8 @@ protected:
 	virtual bool probe_predicates() const { return true; }
 	virtual int run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
 			unsigned long long* rows);
+	virtual int run_device_spans(pg_ctx* ctx, pg_stream st, const pg_rel& R, const std::vector<pg_rel>& S,
+			void** out, unsigned long long* rows);
 };
 
 // "gpumpsmjoin": OldMPSMJoinOp / MPSMJoinOp keys (join.cpp:677-783,

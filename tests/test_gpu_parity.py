@@ -305,6 +305,62 @@ def test_join_other_widths(ctx, wide):
         ctx.tune(probe_wide=0)
 
 
+def _probe_spans(ctx, R, parts, proj, pkey, bkey=(0, 8), flags=gpu.JOIN_MATERIALIZE, sum_col=-1):
+    # The probe side as separate device arrays, probed as one relation.
+    import ctypes
+    L = gpu.lib()
+    t = ctx.build_table(R, proj, bkey)
+    try:
+        bufs = [ctx.upload(np.ascontiguousarray(p)) for p in parts]
+        rels = (gpu.Rel * len(parts))(*[ctx.rel(b, p.shape[0], gpu.row_width(p), *pkey) for b, p in zip(bufs, parts)])
+        c, nc = gpu.cols(proj)
+        ow = sum(b for _, _, b in proj)
+        total = sum(p.shape[0] for p in parts)
+        o = ctx.alloc(max(total, 1) * ow)
+        res = gpu.JoinResult()
+        ctx._check(L.pg_hashjoin_probe_spans(ctx.h, ctx.stream, t.h, rels, len(parts), c, nc,
+                                             o.ptr if flags & gpu.JOIN_MATERIALIZE else None, total, flags, sum_col,
+                                             ctypes.byref(res)))
+        rows = ctx.download(o, res.n_out * ow).reshape(-1, ow) if flags & gpu.JOIN_MATERIALIZE else None
+        return rows, res.n_out, res.sum
+    finally:
+        t.free()
+
+
+def test_join_probe_spans_as_one_relation(ctx):
+    # 24-byte lines split into uneven arrays (one empty) against dense narrow,
+    # dense wide and hashed tables; 16-byte tuples too: the rows, count and
+    # sum of one probe over the concatenation.
+    R = dg.build_relation(50_000, dg.seed_for(620))
+    Rw = R.copy(); Rw[:, 1] = dg.raw_words(dg.seed_for(621), 1, 50_000).view(np.int64)
+    Rh = R.copy(); Rh[:, 0] = Rh[:, 0] * 7919 - (1 << 40)
+    L = _lines(210_001, R, 622, miss_every=31)
+    Lh = L.copy(); Lh[:, 1] = Lh[:, 1] * 7919 - (1 << 40)
+    cuts = [0, 70_000, 70_000, 150_001, 210_001]
+    proj = (("P", 0, 8), ("P", 16, 8), ("B", 8, 8))
+    for table, lines in ((R, L), (Rw, L), (Rh, Lh)):
+        parts = [lines[a:b] for a, b in zip(cuts, cuts[1:])]
+        got, n, _ = _probe_spans(ctx, table, parts, proj, (8, 8))
+        want, wn, _ = orc.hashjoin(table, lines, proj=proj, pkey=(8, 8), hash=orc.hashcfg("modulo", 1024))
+        assert n == wn and np.array_equal(canon(got), canon(want))
+        _, n2, s2 = _probe_spans(ctx, table, parts, proj, (8, 8), flags=gpu.JOIN_COUNT | gpu.JOIN_SUM, sum_col=2)
+        _, wn2, ws2 = orc.hashjoin(table, lines, proj=proj, pkey=(8, 8), materialise=False, sum_col=2,
+                                   hash=orc.hashcfg("modulo", 1024))
+        assert (n2, s2) == (wn2, ws2)
+    S = dg.probe_uniform(100_000, R, dg.seed_for(623))
+    got, n, _ = _probe_spans(ctx, R, [S[:33_333], S[33_333:]], (("P", 8, 8), ("B", 8, 8)), (0, 8))
+    want, wn, _ = orc.hashjoin(R, S, hash=orc.hashcfg("modulo", 1024))
+    assert n == wn and np.array_equal(canon(got), canon(want))
+
+
+def test_join_probe_spans_refuses_repeated_build_keys(ctx):
+    R = dg.uniform_keys(5000, 700, dg.seed_for(624))
+    S = dg.uniform_keys(9000, 900, dg.seed_for(625))
+    with pytest.raises(gpu.PgError) as e:
+        _probe_spans(ctx, R, [S[:4000], S[4000:]], (("P", 8, 8), ("B", 8, 8)), (0, 8))
+    assert e.value.code == gpu.PG_ERR_UNSUPPORTED
+
+
 def test_join_reference_unit_test(ctx):
     # unit_tests/queryhashjoin.cpp: build (i, i), probe (i, i+0.1), i = 1..20.
     R = gin.make({"gen": "formula", "name": "i_i", "n": 20})
