@@ -344,6 +344,7 @@ pg_stream g_thread_streams[MAX_THREADS];
 // of equal thread ids, which orders their work but keeps it correct.
 pg_stream thread_stream(pg_ctx* ctx, int tid)
 {
+	if (tid < 0 || tid >= MAX_THREADS) return 0;     // the legacy stream: ordered, still correct
 	pthread_mutex_lock(&g_stream_mu);
 	if (!g_thread_streams[tid]) {
 		pg_stream s = 0;
