@@ -39,6 +39,9 @@ NR = 1 << 24            # overridable with --build-log2 / --probe-log2 (smaller 
 NS = 1 << 28
 TUPLE = 16
 PROBE_DRAM_BYTES_PER_TUPLE = (1.133091e9 + 0.514387e9) / (1 << 25)
+# DRAM bytes per 24-byte line of the staged probe against a 4M-part table, measured
+# by ncu on 16M lines (profiles/wideprobe_64Mx4M.md); traffic scales with the lines.
+WIDE_DRAM_BYTES_PER_LINE = (419.517440e6 + 358.811904e6) / (1 << 24)
 METRIC = "join tuples/s (16M build x 256M probe, PK-FK, int64 keys, materialised)"
 WORKLOAD = "radix-scale PK-FK hash join: |R|=16M unique int64 keys, |S|=256M uniform FK, 16-byte tuples, output (P$1,B$1)"
 
@@ -1416,8 +1419,9 @@ def run_wideprobe(args, ws, rank, local):
                 "per_thread_load_probe_ms": ms_plain, "staged_speedup": ms_plain / ms,
                 "parity": {"rows": int(n_rows), "rows_ok": int(n_rows) == nL, "column_sums_ok": got == want},
                 "roofline": {"bound": "hbm", "kernel": "k_probe_staged<true, 2, 2>", "achieved": gbs, "peak": peak,
-                             "unit": "GB/s", "frac": gbs / peak, "traffic": None, "peak_source": peak_kind,
-                             "algorithmic_bytes": alg},
+                             "unit": "GB/s", "frac": gbs / peak,
+                             "traffic": WIDE_DRAM_BYTES_PER_LINE * nL if nP == 1 << 22 else None,
+                             "peak_source": peak_kind, "algorithmic_bytes": alg},
                 "gpu_launches": int(launches), "clocks": clk}
         if cpu:
             line["cpu_baseline"] = cpu
