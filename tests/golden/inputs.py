@@ -148,10 +148,28 @@ def filter_preds(schema, filters):
     return out
 
 
+def _lines(spec):
+    """(order, part, price) 24-byte lines: orders 3i + 1, parts drawn from the
+    build relation, prices as float64 bits; every miss_every-th part lies past
+    the build's keys."""
+    n = spec["n"]
+    fk = dg.probe_uniform(n, make(spec["build"]), dg.seed_for(spec["rel"]))
+    L = np.zeros((n, 3), np.int64)
+    L[:, 0] = np.arange(n, dtype=np.int64) * 3 + 1
+    L[:, 1] = fk[:, 0]
+    raw = dg.raw_words(dg.seed_for(spec["rel"] + 1), 2, n) >> np.uint64(11)
+    L[:, 2] = (raw.astype(np.float64) * 1e-9).view(np.int64)
+    if spec.get("miss_every"):
+        L[::spec["miss_every"], 1] += 1 << 40
+    return L
+
+
 def make(spec):
     g = spec["gen"]
     if g == "formula":
         return _formula(spec["name"], spec["n"])
+    if g == "lines":
+        return _lines(spec)
     seed = dg.seed_for(spec["rel"])
     if g == "build":
         return dg.build_relation(spec["n"], seed)

@@ -57,8 +57,11 @@ def test_golden(case):
         proj = parse_proj(p["proj"], p.get("bschema", "long,long"), p.get("pschema", "long,long"))
         if op == "hashjoin":
             cfg = orc.hashcfg(p["fn"], p["buckets"])
+            bw, pw = widths(p.get("bschema", "long,long")), widths(p.get("pschema", "long,long"))
+            ba, pa = p.get("buildjattr", 0), p.get("probejattr", 0)
             out, n, s = orc.hashjoin(R, S, proj=proj, hash=cfg, tuplesperbucket=p["tuplesperbucket"],
-                                     threads=p["threads"], sum_col=1)
+                                     threads=p["threads"], sum_col=1, bkey=(sum(bw[:ba]), bw[ba]),
+                                     pkey=(sum(pw[:pa]), pw[pa]))
             assert n == ref["n_out"] == ref["count"]
             side, idx = proj_types(p["proj"])[1]
             if (p["bschema"] if side == "B" else p["pschema"]).split(",")[idx] == "dec":
