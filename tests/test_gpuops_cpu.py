@@ -148,8 +148,15 @@ def test_gpu_chain_without_gpu_returns_error_and_moves_nothing():
 
 
 def test_reference_engine_drives_gpu_operator():
+    # The engine's own Query::create, with this repository's plan factory in
+    # place of query.o, builds hashjoin, gpuhashjoin, gpumpsmjoin and
+    # gpuaggregate_count plans (the GPU joins are dual-input types the engine
+    # cannot take as user-defined operators); the CPU join must give the
+    # engine's answer and every GPU plan must be constructed and initialised.
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_gpuops_check")
     if not os.path.exists(exe):
         pytest.skip("reference engine not built here")
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
+    for name in ("hashjoin:", "gpuhashjoin:", "gpumpsmjoin:", "gpuaggregate_count:"):
+        assert any(ln.startswith(name) and ln.endswith("ok") for ln in r.stdout.splitlines()), r.stdout
