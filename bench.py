@@ -1,24 +1,34 @@
-"""Benchmark: radix-scale PK-FK hash join, 16M build x 256M probe, on one GB300.
+"""Benchmark: radix-scale PK-FK hash join, 16M build x 256M probe, on one GB300,
+followed by every other configuration of the operator path.
 
-One step = build the hash table over |R| = 16,777,216 (int64 key, int64
+Headline step = build the hash table over |R| = 16,777,216 (int64 key, int64
 payload) tuples and probe it with |S| = 268,435,456 foreign-key tuples,
-materialising every (probe payload, build payload) output row: the workload
-of the "16M join 256M" configuration. Keys of R are a random permutation of
-1..|R|; probe keys are uniform over R's keys (seeded synthetic data).
+materialising every (probe payload, build payload) output row. Keys of R are
+a random permutation of 1..|R|; probe keys are uniform over R's keys (seeded
+synthetic data).
 
   value   join tuples/s = (|R| + |S|) / step time, inputs resident in HBM,
           CUDA events on the operator's stream, max over ranks.
   e2e     the same metric through pg_hashjoin_host with pinned HOST buffers:
           host->device copies of R and S and the device->host copy of every
           output row are inside the timed region.
+  parity  a whole-row digest (row count, column sums, sum of a row hash) of
+          the rows the timed kernel wrote, against the oracle join's.
   roofline  the dominant kernel (the probe) against the measured HBM copy
           bandwidth: algorithmic bytes per launch = 16|S| + 16|out|.
   cpu_baseline  the oracle's port of the reference HashJoinOp (chained
-          buckets, per-bucket spinlocks, all host threads) on a bounded sample.
+          buckets, per-bucket spinlocks, rows into 1 MiB output pages, all
+          host threads) on a bounded sample.
+  configs  (one GPU, unless --headline-only) the line of every other
+          configuration, measured in this run at full size: the 1M x 16M
+          join into aggregate_count + aggregate_sum, the 16M x 256M join
+          with Zipf s=1.0 probes and with sparse keys (hashed table), the
+          256M-row group-by, the 64M x 64M MPSM join (count/sum and
+          materialised), the page sorts, the partition, the 10,000-instance
+          batch and the serving loop.
 
---impl reference times the reference algorithm on the host cores instead
-(the oracle port; the reference engine itself is compiled from its own
-sources only where its source tree exists).
+--impl reference times the reference algorithm on the host cores instead:
+the oracle port of HashJoinOp over the whole workload every step.
 """
 import argparse
 import ctypes
@@ -38,12 +48,13 @@ sys.path.insert(0, ROOT)
 NR = 1 << 24            # overridable with --build-log2 / --probe-log2 (smaller configs)
 NS = 1 << 28
 TUPLE = 16
+# DRAM bytes per probe tuple of the materialising probe against the 16M-key
+# (64 MB) dense table, measured by ncu on a 32M-tuple probe of the same table;
+# traffic scales with the probe tuples.
 PROBE_DRAM_BYTES_PER_TUPLE = (1.133091e9 + 0.514387e9) / (1 << 25)
 # DRAM bytes per 24-byte line of the staged probe against a 4M-part table, measured
-# by ncu on 16M lines (profiles/wideprobe_64Mx4M.md); traffic scales with the lines.
+# by ncu on 16M lines; traffic scales with the lines.
 WIDE_DRAM_BYTES_PER_LINE = (419.517440e6 + 358.811904e6) / (1 << 24)
-METRIC = "join tuples/s (16M build x 256M probe, PK-FK, int64 keys, materialised)"
-WORKLOAD = "radix-scale PK-FK hash join: |R|=16M unique int64 keys, |S|=256M uniform FK, 16-byte tuples, output (P$1,B$1)"
 
 
 def env_int(k, d):
@@ -148,77 +159,122 @@ def host_threads():
     return max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count())
 
 
-def make_inputs(R, S, threads):
+# ---------------------------------------------------------------------------
+# Hash joins: the 16M x 256M headline (uniform probe), its Zipf s=1.0 and
+# sparse-key (hashed table) runs, and the 1M x 16M join feeding
+# aggregate_count + aggregate_sum. One step = build + probe over inputs
+# resident in HBM.
+# ---------------------------------------------------------------------------
+PROJ = (("P", 8, 8), ("B", 8, 8))
+SPARSE_MUL = 0x9E3779B97F4A7C15 - (1 << 64)      # odd: a bijection on int64 keys
+
+
+def join_spec(nr, ns, dist="uniform", zipf_s=1.0, key_domain="dense", mode="materialise"):
+    what = {"materialise": "output (P$1,B$1) rows materialised",
+            "count_sum": "aggregate_count + aggregate_sum(B$1) over the join output, fused into the probe"}[mode]
+    probe = "uniform FK" if dist == "uniform" else f"Zipf s={zipf_s} FK (hot ranks scattered over R's keys)"
+    keys = ("keys 1..|R| (random permutation)" if key_domain == "dense"
+            else "keys 1..|R| times an odd 64-bit constant (hashed table)")
+    return {"nr": nr, "ns": ns, "dist": dist, "zipf_s": zipf_s, "key_domain": key_domain, "mode": mode,
+            "workload": f"PK-FK hash join: |R|={nr} unique int64 {keys}, |S|={ns} {probe}, 16-byte tuples, {what}"}
+
+
+def _count(n):
+    return f"{n >> 20}M" if n >= 1 << 20 and n % (1 << 20) == 0 else f"{n >> 10}K" if n % 1024 == 0 else str(n)
+
+
+def join_metric(sp):
+    size = f"{_count(sp['nr'])} build x {_count(sp['ns'])} probe"
+    if sp["mode"] == "count_sum":
+        return f"join tuples/s ({size}, PK-FK, int64 keys, count+sum)"
+    tail = "" if sp["dist"] == "uniform" else f", Zipf s={sp['zipf_s']}"
+    tail += "" if sp["key_domain"] == "dense" else ", sparse keys"
+    return f"join tuples/s ({size}, PK-FK, int64 keys, materialised{tail})"
+
+
+def join_config(sp, ws):
+    """The config dict both arms print for a join workload."""
+    return {"workload": sp["workload"], "build_tuples": sp["nr"], "probe_tuples": sp["ns"],
+            "probe_dist": sp["dist"] if sp["dist"] == "uniform" else f"zipf s={sp['zipf_s']}",
+            "key_domain": sp["key_domain"], "output": sp["mode"],
+            "l2": (f"probe side ({16 * sp['ns'] >> 20} MiB) larger than L2 (129 MB); no flush"
+                   if 16 * sp["ns"] > 129_000_000 else "probe side fits in L2 (small case; not a bench config)"),
+            "parallelism": f"replicas x{ws}"}
+
+
+def make_join_inputs(sp, R, S, threads):
     from pythia_gb300 import datagen as dg
-    dg.build_relation(NR, dg.seed_for(101), out=R, threads=threads)
-    dg.probe_uniform(NS, R, dg.seed_for(102), out=S, threads=threads)
+    dg.build_relation(sp["nr"], dg.seed_for(101), out=R, threads=threads)
+    if sp["dist"] == "zipf":
+        dg.probe_zipf(sp["ns"], sp["zipf_s"], R, dg.seed_for(103), out=S, threads=threads)
+    else:
+        dg.probe_uniform(sp["ns"], R, dg.seed_for(102), out=S, threads=threads)
+    if sp["key_domain"] == "sparse":
+        R[:, 0] *= SPARSE_MUL
+        S[:, 0] *= SPARSE_MUL
 
 
-def expected_sum(R, S):
-    """Checksum of the build-payload output column: sum over probe tuples of
-    the payload of the build tuple with the same key (keys are 1..|R|)."""
-    pay = np.zeros(NR + 1, dtype=np.int64)
-    pay[R[:, 0]] = R[:, 1]
-    tot = np.uint64(0)
-    step = 1 << 24
-    for i in range(0, S.shape[0], step):
-        tot += pay[S[i:i + step, 0]].astype(np.uint64).sum(dtype=np.uint64)
-    return int(np.int64(tot))
-
-
-def cpu_sample_size():
-    """Probe tuples timed on the host per CPU measurement (1/32 of the probe)."""
-    return max(1, NS // 32)
-
-
-def cpu_join_sample(R, S, threads, sample):
-    """Times the oracle port of HashJoinOp: full build + a probe sample (one
-    materialising pass: a PK-FK join yields one row per probe tuple, so the
-    output capacity is the sample size), extrapolated linearly in probe size to
-    the whole workload. Inputs are copied to ordinary host memory first."""
+def cpu_join(sp, R, S, threads, sample=None):
+    """Times the oracle port of HashJoinOp (chained buckets, fn=modulo with
+    |R| buckets, 4 tuples per bucket, all host threads), every output row
+    written into the thread's 1 MiB output page as HashJoinOp::getNext does.
+    sample=None: one timed build + probe of the whole workload. Else the
+    build alone, then the build with the first `sample` probe tuples, and the
+    probe time scaled linearly to |S|. Returns (tuples/s, info)."""
     from oracle import oracle as orc
-    cfg = orc.hashcfg("modulo", NR)
-    Rc = np.array(R, copy=True)
-    Ssub = np.array(S[:sample], copy=True)
+    nr, ns = sp["nr"], sp["ns"]
+    cfg = orc.hashcfg("modulo", nr)
+    sc = 1 if sp["mode"] == "count_sum" else -1
+    if sample is None or sample >= ns:
+        t0 = time.perf_counter()
+        n, _ = orc.hashjoin_paged(R, S, hash=cfg, threads=threads, sum_col=sc)
+        t = time.perf_counter() - t0
+        return (nr + ns) / t, {"build_probe_s": t, "probe_tuples_timed": ns, "rows": int(n), "scaled": False}
+    Ssub = np.ascontiguousarray(S[:sample])
     t0 = time.perf_counter()
-    _, n0, _ = orc.hashjoin(Rc, Ssub[:1], hash=cfg, tuplesperbucket=4, threads=threads, materialise=False)
+    orc.hashjoin_paged(R, Ssub[:1], hash=cfg, threads=threads)
     t_build = time.perf_counter() - t0
     t0 = time.perf_counter()
-    _, n, _ = orc.hashjoin(Rc, Ssub, hash=cfg, tuplesperbucket=4, threads=threads, materialise=True,
-                           out_cap=sample)
+    n, _ = orc.hashjoin_paged(R, Ssub, hash=cfg, threads=threads, sum_col=sc)
     t_all = time.perf_counter() - t0
-    t_probe = max(t_all - t_build, 1e-9)
-    t_est = t_build + t_probe * (NS / sample)
-    return (NR + NS) / t_est, {"build_s": t_build, "probe_sample_s": t_probe, "sample_probe": sample,
-                               "matches": int(n)}
+    t_est = t_build + max(t_all - t_build, 1e-9) * (ns / sample)
+    return (nr + ns) / t_est, {"build_s": t_build, "build_probe_s": t_all, "probe_tuples_timed": sample,
+                               "rows": int(n), "scaled": True}
 
 
 def run_reference(args, ws, rank):
+    """The reference algorithm on the host cores, on the GPU arm's workload:
+    every step builds the table and probes all |S| tuples (rows written into
+    1 MiB output pages), all host threads."""
     if rank != 0:
         return
     threads = host_threads()
-    from pythia_gb300 import datagen as dg  # noqa: F401
-    R = np.empty((NR, 2), dtype=np.int64)
-    S = np.empty((NS, 2), dtype=np.int64)
-    make_inputs(R, S, threads)
-    sample = cpu_sample_size()
-    vals = []
+    sp = headline_spec(args)
+    R = np.empty((sp["nr"], 2), dtype=np.int64)
+    S = np.empty((sp["ns"], 2), dtype=np.int64)
+    make_join_inputs(sp, R, S, threads)
+    vals, infos = [], []
     for i in range(args.warmup + args.steps):
-        v, info = cpu_join_sample(R, S, threads, sample)
+        v, info = cpu_join(sp, R, S, threads)
         if i >= args.warmup:
-            vals.append(v)
+            vals.append(v); infos.append(info)
     value = statistics.median(vals)
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "tuples/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": (NR + NS) / value * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded generator)",
-            "config": {"workload": WORKLOAD, "build_tuples": NR, "probe_tuples": NS,
-                       "hash": f"modulo, {NR} buckets, tuplesperbucket=4", "threads": threads},
+    ms = (sp["nr"] + sp["ns"]) / value * 1e3
+    line = {"impl": "reference", "metric": join_metric(sp), "value": value, "unit": "tuples/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+            "data": "synthetic (seeded generator)", "config": join_config(sp, ws),
             "cpu_baseline": {"value": value, "unit": "tuples/s", "cores": threads, "kind": "port",
-                             "sample": f"full {NR}-tuple build + first {sample} probe tuples per step, "
-                                       f"probe time scaled to {NS}"},
+                             "sample": f"whole workload every step: {sp['nr']}-tuple build + all {sp['ns']} probe "
+                                       f"tuples (oracle port of HashJoinOp, modulo {sp['nr']} buckets, 4 tuples "
+                                       f"per bucket, rows into 1 MiB pages)",
+                             "detail": infos[len(infos) // 2]},
             "e2e": {"value": value, "unit": "tuples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def headline_spec(args):
+    return join_spec(NR, NS, args.probe_dist, args.zipf_s, args.key_domain, "materialise")
 
 
 def make_ctx(args, local):
@@ -230,68 +286,69 @@ def make_ctx(args, local):
     return ctx
 
 
-def run_gpu(args, ws, rank, local):
+def run_join(args, ws, rank, local, sp, steps, warmup, e2e_steps=3, cpu_sample=None, want_cpu=True):
+    """One join workload on the GPU: device-resident steps (value), the probe
+    kernel alone (roofline), the host-buffer entry point (e2e), a whole-row
+    digest of the timed kernel's output against the oracle's (parity) and
+    the CPU port (cpu_baseline). Returns the JSON dict (rank 0) or None."""
     import torch
+    from oracle import oracle as orc
     from pythia_gb300 import gpu
     torch.cuda.set_device(local)
     threads = host_threads()
+    nr, ns, mode = sp["nr"], sp["ns"], sp["mode"]
+    mat = mode == "materialise"
     ctx = make_ctx(args, local)
     L = gpu.lib()
-    # Pinned host relations (also the e2e sources) and output.
+
     def pinned(nbytes):
         p = ctypes.c_void_p()
-        ctx._check(L.pg_host_alloc(ctx.h, nbytes, ctypes.byref(p)))
+        ctx._check(L.pg_host_alloc(ctx.h, max(nbytes, 16), ctypes.byref(p)))
         return p.value
-    hR, hS, hO = pinned(NR * TUPLE), pinned(NS * TUPLE), pinned(NS * TUPLE)
-    R = np.ctypeslib.as_array((ctypes.c_int64 * (NR * 2)).from_address(hR)).reshape(NR, 2)
-    S = np.ctypeslib.as_array((ctypes.c_int64 * (NS * 2)).from_address(hS)).reshape(NS, 2)
-    make_inputs(R, S, threads)
-    want_sum = expected_sum(R, S)
-    if args.key_domain == "sparse":
-        # Same join spread over a wide key domain: odd multiplier, a bijection
-        # on int64, so matches and the checksum are unchanged.
-        R[:, 0] *= 0x9E3779B97F4A7C15 - (1 << 64)
-        S[:, 0] *= 0x9E3779B97F4A7C15 - (1 << 64)
+    hR, hS = pinned(nr * TUPLE), pinned(ns * TUPLE)
+    hO = pinned(ns * TUPLE) if mat else pinned(64)
+    R = np.ctypeslib.as_array((ctypes.c_int64 * (nr * 2)).from_address(hR)).reshape(nr, 2)
+    S = np.ctypeslib.as_array((ctypes.c_int64 * (ns * 2)).from_address(hS)).reshape(ns, 2)
+    make_join_inputs(sp, R, S, threads)
+    # Expected results from the oracle (the same rows whatever the key domain).
+    cfg = orc.hashcfg("modulo", nr)
+    if mat:
+        want = orc.hashjoin_digest(R, S, proj=PROJ, hash=cfg, threads=threads)
+    else:
+        _, wn, wsum = orc.hashjoin(R, S, proj=PROJ, hash=cfg, threads=threads, materialise=False, sum_col=1)
+        want = {"rows": int(wn), "sum_B1": int(wsum)}
 
-    dR, dS, dO = ctx.alloc(NR * TUPLE), ctx.alloc(NS * TUPLE), ctx.alloc(NS * TUPLE)
-    ctx._check(L.pg_h2d(ctx.h, ctx.stream, dR.ptr, hR, NR * TUPLE))
-    ctx._check(L.pg_h2d(ctx.h, ctx.stream, dS.ptr, hS, NS * TUPLE))
+    dR, dS = ctx.alloc(nr * TUPLE), ctx.alloc(ns * TUPLE)
+    dO = ctx.alloc(ns * TUPLE) if mat else None
+    ctx._check(L.pg_h2d(ctx.h, ctx.stream, dR.ptr, hR, nr * TUPLE))
+    ctx._check(L.pg_h2d(ctx.h, ctx.stream, dS.ptr, hS, ns * TUPLE))
     ctx.sync()
-    rR = gpu.Rel(dR.ptr, NR, TUPLE, 0, 8)
-    rS = gpu.Rel(dS.ptr, NS, TUPLE, 0, 8)
-    proj, nproj = gpu.cols((("P", 8, 8), ("B", 8, 8)))
+    rR = gpu.Rel(dR.ptr, nr, TUPLE, 0, 8)
+    rS = gpu.Rel(dS.ptr, ns, TUPLE, 0, 8)
+    proj, nproj = gpu.cols(PROJ)
     stream = torch.cuda.ExternalStream(ctx.stream)
-
+    flags = gpu.JOIN_MATERIALIZE if mat else gpu.JOIN_COUNT | gpu.JOIN_SUM
+    sum_col = -1 if mat else 1
     probe_ms = []
+    last = gpu.JoinResult()
 
     def step(timed_probe=False):
         ht = ctypes.c_void_p()
         ctx._check(L.pg_hashjoin_build(ctx.h, ctx.stream, ctypes.byref(rR), proj, nproj, ctypes.byref(ht)))
-        res = gpu.JoinResult()
         if timed_probe:
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
         ctx._check(L.pg_hashjoin_probe(ctx.h, ctx.stream, ht.value, ctypes.byref(rS), proj, nproj,
-                                       dO.ptr, NS, gpu.JOIN_MATERIALIZE, -1, ctypes.byref(res)))
+                                       dO.ptr if mat else None, ns if mat else 0, flags, sum_col,
+                                       ctypes.byref(last)))
         if timed_probe:
             e1.record(stream)
             e1.synchronize()
             probe_ms.append(e0.elapsed_time(e1))
         L.pg_hashtable_free(ctx.h, ht.value)
-        return res.n_out
 
-    for _ in range(args.warmup):
-        n = step()
-    assert n == NS, f"expected {NS} join rows, got {n}"
-    # Parity on the full workload: row count and the build-payload checksum.
-    res = gpu.JoinResult()
-    ht = ctypes.c_void_p()
-    ctx._check(L.pg_hashjoin_build(ctx.h, ctx.stream, ctypes.byref(rR), proj, nproj, ctypes.byref(ht)))
-    ctx._check(L.pg_hashjoin_probe(ctx.h, ctx.stream, ht.value, ctypes.byref(rS), proj, nproj, None, 0,
-                                   gpu.JOIN_COUNT | gpu.JOIN_SUM, 1, ctypes.byref(res)))
-    L.pg_hashtable_free(ctx.h, ht.value)
-    parity = res.n_out == NS and res.sum == want_sum
-
+    for _ in range(warmup):
+        step()
     clocks = Clocks(local)
     barrier(ws)
     torch.cuda.synchronize()
@@ -299,81 +356,99 @@ def run_gpu(args, ws, rank, local):
     k0 = gpu.kernel_launches()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    for _ in range(args.steps):
-        step(timed_probe=False)
+    for _ in range(steps):
+        step()
     ev1.record(stream)
     ev1.synchronize()
     launches = gpu.kernel_launches() - k0
     torch.cuda.synchronize()
     barrier(ws)
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    ms = max_over_ranks(ws, ms)
-    value = ws * (NR + NS) / (ms / 1e3)
+    ms = max_over_ranks(ws, ev0.elapsed_time(ev1) / steps)
+    value = ws * (nr + ns) / (ms / 1e3)
+    # Parity of the timed kernel's own output (the last timed step's rows).
+    if mat:
+        ctx._check(L.pg_d2h(ctx.h, ctx.stream, hO, dO.ptr, last.n_out * TUPLE))
+        ctx.sync()
+        O = np.ctypeslib.as_array((ctypes.c_int64 * (last.n_out * 2)).from_address(hO)).reshape(-1, 2) \
+            if last.n_out else np.zeros((0, 2), dtype=np.int64)
+        got = orc.rows_digest(O, threads=threads)
+    else:
+        got = {"rows": int(last.n_out), "sum_B1": int(last.sum)}
+    parity = {"check": "whole-row digest of the timed step's output rows vs the oracle join's"
+              if mat else "count and wrapping int64 sum of B$1 vs the oracle join's",
+              "expected": want, "got": got, "ok": got == want}
 
     # Dominant kernel (probe) timed alone with events on its stream.
-    for _ in range(max(2, min(args.steps, 5))):
+    for _ in range(max(3, min(steps, 5))):
         step(timed_probe=True)
     probe = statistics.median(probe_ms)
     peak, peak_kind = measured_peak()
-    alg_probe = TUPLE * NS + TUPLE * NS
+    alg_probe = TUPLE * ns + (TUPLE * last.n_out if mat else 0)
     achieved = alg_probe / (probe / 1e3) / 1e9
+    alg_step = TUPLE * (nr + ns) + (TUPLE * last.n_out if mat else 0)
 
     # End to end through the host-buffer entry point.
     e2e_ms = []
     hres = gpu.JoinResult()
-    for i in range(max(1, args.e2e_steps) + 1):
-        rRh = gpu.Rel(hR, NR, TUPLE, 0, 8)
-        rSh = gpu.Rel(hS, NS, TUPLE, 0, 8)
+    for i in range(max(1, e2e_steps) + 1):
+        rRh = gpu.Rel(hR, nr, TUPLE, 0, 8)
+        rSh = gpu.Rel(hS, ns, TUPLE, 0, 8)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ctx._check(L.pg_hashjoin_host(ctx.h, ctypes.byref(rRh), ctypes.byref(rSh), proj, nproj, hO, NS,
-                                      gpu.JOIN_MATERIALIZE, -1, ctypes.byref(hres)))
+        ctx._check(L.pg_hashjoin_host(ctx.h, ctypes.byref(rRh), ctypes.byref(rSh), proj, nproj,
+                                      hO if mat else None, ns if mat else 0, flags, sum_col, ctypes.byref(hres)))
         t1 = time.perf_counter()
         if i:
             e2e_ms.append((t1 - t0) * 1e3)
-    assert hres.n_out == NS
-    O = np.ctypeslib.as_array((ctypes.c_int64 * (NS * 2)).from_address(hO)).reshape(NS, 2)
-    e2e_parity = int(O[:, 1].astype(np.uint64).sum(dtype=np.uint64).astype(np.int64)) == want_sum
+    if mat:
+        O = np.ctypeslib.as_array((ctypes.c_int64 * (hres.n_out * 2)).from_address(hO)).reshape(-1, 2) \
+            if hres.n_out else np.zeros((0, 2), dtype=np.int64)
+        e2e_ok = orc.rows_digest(O, threads=threads) == want
+    else:
+        e2e_ok = {"rows": int(hres.n_out), "sum_B1": int(hres.sum)} == want
+    parity["e2e_ok"] = bool(e2e_ok)
     e2e = max_over_ranks(ws, statistics.median(e2e_ms))
 
     cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
-        sample = cpu_sample_size()
-        v, info = cpu_join_sample(R, S, threads, sample)
+    if rank == 0 and ws == 1 and want_cpu:
+        v, info = cpu_join(sp, R, S, threads, cpu_sample)
+        m = info["probe_tuples_timed"]
         cpu = {"value": v, "unit": "tuples/s", "cores": threads, "kind": "port",
-               "sample": f"full {NR}-tuple build + first {sample} probe tuples, probe time scaled to {NS} "
-                         f"(oracle port of HashJoinOp, modulo {NR} buckets, 4 tuples/bucket)",
+               "sample": (f"full {nr}-tuple build + " + (f"first {m} probe tuples, probe time scaled to {ns}"
+                          if m != ns else f"all {ns} probe tuples")) +
+                         f" (oracle port of HashJoinOp, modulo {nr} buckets, 4 tuples/bucket, rows into 1 MiB pages)",
                "detail": info}
-
+    line = None
     if rank == 0:
-        # DRAM bytes per probe tuple measured by ncu on the same 64 MB table
-        # (profiles/hashjoin_probe_16Mx256M.md); traffic scales with |S|.
-        traffic = PROBE_DRAM_BYTES_PER_TUPLE * NS if args.key_domain == "dense" else None
-        line = {"metric": METRIC, "value": value, "unit": "tuples/s", "n_gpus": ws,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        kern = ("k_probe16_deep (materialise)" if mat else "k_probe16_direct (count + sum)") \
+            if sp["key_domain"] == "dense" else "hashed-table probe"
+        line = {"metric": join_metric(sp), "value": value, "unit": "tuples/s", "n_gpus": ws,
+                "steps": steps, "warmup": warmup, "ms_per_step": ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
                 "data": "synthetic (seeded generator, resident in HBM)",
-                "config": {"workload": WORKLOAD, "build_tuples": NR, "probe_tuples": NS,
-                           "output_rows": NS, "l2": "inputs (4.3 GB) larger than L2; no flush",
-                           "key_domain": args.key_domain,
-                           "parallelism": f"replicas x{ws}"},
-                "parity": {"rows": int(res.n_out), "checksum_ok": bool(parity), "e2e_checksum_ok": bool(e2e_parity)},
-                "e2e": {"value": ws * (NR + NS) / (e2e / 1e3), "unit": "tuples/s",
-                        "h2d_bytes_per_step": (NR + NS) * TUPLE, "d2h_bytes_per_step": NS * TUPLE,
+                "config": join_config(sp, ws),
+                "parity": parity,
+                "e2e": {"value": ws * (nr + ns) / (e2e / 1e3), "unit": "tuples/s",
+                        "h2d_bytes_per_step": (nr + ns) * TUPLE,
+                        "d2h_bytes_per_step": (int(hres.n_out) * TUPLE) if mat else 16,
                         "ms_per_step": e2e},
-                "roofline": {"bound": "hbm", "kernel": "k_probe16_deep (materialise)",
-                             "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": traffic,
+                "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak,
+                             "traffic": PROBE_DRAM_BYTES_PER_TUPLE * ns
+                             if (mat and sp["key_domain"] == "dense" and sp["dist"] == "uniform" and nr == 1 << 24)
+                             else None,
                              "peak_source": peak_kind, "probe_ms": probe,
-                             "step_frac": (TUPLE * (NR + 2 * NS)) / (ms / 1e3) / 1e9 / peak},
+                             "algorithmic_bytes_per_launch": alg_probe,
+                             "step_frac": alg_step / (ms / 1e3) / 1e9 / peak,
+                             "step_algorithmic_bytes": alg_step},
                 "gpu_launches": int(launches), "clocks": clk}
         if cpu:
             line["cpu_baseline"] = cpu
-        print(json.dumps(line), flush=True)
     for h in (hR, hS, hO):
         L.pg_host_free(ctx.h, h)
     ctx.close()
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -389,6 +464,13 @@ OPS = {
                  workload="page sort of 64M (long key U[0,16M), long payload) tuples"),
     "mpsm": dict(n=1 << 26, metric="MPSM join tuples/s (64M x 64M, keys U[0,16M), fused count+sum)",
                  workload="sort-merge join of two 64M-tuple relations, keys U[0,16M) (~4 duplicates per side)"),
+    "mpsmmat": dict(n=1 << 26, metric="MPSM join tuples/s (64M x 64M, keys U[0,16M), output rows materialised)",
+                    workload="sort-merge join of two 64M-tuple relations, keys U[0,16M) (~4 duplicates per side), "
+                             "every (P$1,B$1) pair written (~268M rows): page sort, then run matching and the "
+                             "per-key cartesian write"),
+    "sortwide": dict(n=1 << 26, metric="page sort tuples/s (64M int64-keyed 16-byte tuples, keys over 2^40)",
+                     workload="page sort of 64M (long key U[0,2^40), long payload) tuples: key span above 2^32, "
+                              "so 4096-tuple bitonic tiles in shared memory then merge-path merges"),
     "groupjoin": dict(n=1 << 28, metric="join + group-by tuples/s (16M build x 256M probe, 1% groups, one pass)",
                       workload="hash join of 16M unique keys (group column = payload mod 167,772) with 256M FK "
                                "probes carrying dec values U[0,1e4), then aggregate_sum per group, one pass"),
@@ -411,6 +493,8 @@ def _op_inputs(op, n, threads):
         return [dg.groupby_rows(n, 1 << 20, 1e4, dg.seed_for(112), threads=threads)]
     if op == "sort":
         return [dg.uniform_keys(n, 1 << 24, dg.seed_for(113), threads=threads)]
+    if op == "sortwide":
+        return [dg.uniform_keys(n, 1 << 40, dg.seed_for(118), threads=threads)]
     if op == "groupjoin":
         nb = min(GJ_BUILD, max(n // 16, 1024))
         R = dg.build_relation(nb, dg.seed_for(116), threads=threads)
@@ -455,7 +539,7 @@ def _op_parity(op, ins, out, extra):
         return {"groups_ok": bool(ngroups_ok), "total_rel_err": abs(got_total - total) / total,
                 "sampled_group_max_rel_err": worst, "tolerance": 1e-12,
                 "ok": bool(ngroups_ok and worst <= 1e-12)}
-    if op == "sort":
+    if op in ("sort", "sortwide"):
         o = out.reshape(-1, 2)
         ok = bool(np.all(np.diff(o[:, 0]) >= 0))
         ok &= int(o.astype(np.uint64).sum(dtype=np.uint64)) == int(ins[0].astype(np.uint64).sum(dtype=np.uint64))
@@ -481,6 +565,10 @@ def _op_parity(op, ins, out, extra):
         return {"groups_ok": bool(ngroups_ok), "total_rel_err": abs(got_total - total) / total,
                 "sampled_group_max_rel_err": worst, "tolerance": 1e-12,
                 "ok": bool(ngroups_ok and worst <= 1e-12)}
+    if op == "mpsmmat":
+        got, want = extra
+        return {"check": "whole-row digest of the timed step's output rows vs the oracle join's",
+                "expected": want, "got": got, "ok": got == want}
     R, S = ins
     cr = np.bincount(R[:, 0], minlength=1 << 24).astype(np.int64)
     cs = np.bincount(S[:, 0], minlength=1 << 24).astype(np.int64)
@@ -505,13 +593,20 @@ def run_op(args, ws, rank, local, op):
     stream = torch.cuda.ExternalStream(ctx.stream)
     c, nc = gpu.cols((("P", 8, 8), ("B", 8, 8)))
     nb = ins[0].shape[0]
-    out_bytes = {"partition": n * 16, "groupby": (1 << 20) * 16 + 16, "sort": n * 16, "mpsm": 16,
-                 "groupjoin": (nb // 100 + 1) * 16}[op]
+    rel = [gpu.Rel(d.ptr, a.shape[0], 16, 0, 8) for d, a in zip(d_in, ins)]
+    n_pairs = 0
+    if op == "mpsmmat":
+        # Output room from a counting pass (not timed).
+        r0 = gpu.JoinResult()
+        ctx._check(L.pg_mpsm_join(ctx.h, ctx.stream, ctypes.byref(rel[0]), ctypes.byref(rel[1]), c, nc,
+                                  None, 0, gpu.JOIN_COUNT, -1, ctypes.byref(r0)))
+        n_pairs = int(r0.n_out)
+    out_bytes = {"partition": n * 16, "groupby": (1 << 20) * 16 + 16, "sort": n * 16, "sortwide": n * 16,
+                 "mpsm": 16, "mpsmmat": max(n_pairs, 1) * 16, "groupjoin": (nb // 100 + 1) * 16}[op]
     d_out = ctx.alloc(out_bytes)
     offs = ctx.alloc(8 * 257)
     ng = ctypes.c_uint64()
     res = gpu.JoinResult()
-    rel = [gpu.Rel(d.ptr, a.shape[0], 16, 0, 8) for d, a in zip(d_in, ins)]
     gcols, gnc = gpu.cols((("B", 8, 8), ("P", 8, 8)))
 
     def step():
@@ -521,8 +616,11 @@ def run_op(args, ws, rank, local, op):
         elif op == "groupby":
             ctx._check(L.pg_groupby(ctx.h, ctx.stream, ctypes.byref(rel[0]), 8, 2, 0, 1 << 20, d_out.ptr,
                                     1 << 20, ctypes.byref(ng)))
-        elif op == "sort":
+        elif op in ("sort", "sortwide"):
             ctx._check(L.pg_sort_pages(ctx.h, ctx.stream, ctypes.byref(rel[0]), d_out.ptr))
+        elif op == "mpsmmat":
+            ctx._check(L.pg_mpsm_join(ctx.h, ctx.stream, ctypes.byref(rel[0]), ctypes.byref(rel[1]), c, nc,
+                                      d_out.ptr, n_pairs, gpu.JOIN_MATERIALIZE, -1, ctypes.byref(res)))
         elif op == "groupjoin":
             ht = ctypes.c_void_p()
             ctx._check(L.pg_hashjoin_build(ctx.h, ctx.stream, ctypes.byref(rel[0]), gcols, gnc, ctypes.byref(ht)))
@@ -551,9 +649,10 @@ def run_op(args, ws, rank, local, op):
     clk = clocks.stop()
     launches = gpu.kernel_launches() - k0
     ms = max_over_ranks(ws, e0.elapsed_time(e1) / args.steps)
-    units = 2 * n if op == "mpsm" else (n + nb if op == "groupjoin" else n)
+    units = 2 * n if op in ("mpsm", "mpsmmat") else (n + nb if op == "groupjoin" else n)
     value = ws * units / (ms / 1e3)
-    alg = {"partition": 32 * n, "groupby": 16 * n + 16 * (1 << 20), "sort": 32 * n, "mpsm": 16 * 2 * n,
+    alg = {"partition": 32 * n, "groupby": 16 * n + 16 * (1 << 20), "sort": 32 * n, "sortwide": 32 * n,
+           "mpsm": 16 * 2 * n, "mpsmmat": 16 * 2 * n + 16 * n_pairs,
            "groupjoin": 16 * (n + nb) + 16 * (nb // 100)}[op]
     peak, peak_kind = measured_peak()
     achieved = alg / (ms / 1e3) / 1e9
@@ -563,8 +662,15 @@ def run_op(args, ws, rank, local, op):
         parity = _op_parity(op, ins, out, ctx.download(offs, 8 * 257, np.uint64))
     elif op == "groupby":
         parity = _op_parity(op, ins, ctx.download(d_out, ng.value * 16), None)
-    elif op == "sort":
+    elif op in ("sort", "sortwide"):
         parity = _op_parity(op, ins, ctx.download(d_out, n * 16).view(np.int64), None)
+    elif op == "mpsmmat":
+        from oracle import oracle as orc
+        got = orc.rows_digest(ctx.download(d_out, int(res.n_out) * 16).view(np.int64).reshape(-1, 2),
+                              threads=threads)
+        want = orc.hashjoin_digest(ins[0], ins[1], proj=PROJ, hash=orc.hashcfg("modulo", 1 << 24),
+                                   threads=threads)
+        parity = _op_parity(op, ins, None, (got, want))
     elif op == "groupjoin":
         parity = _op_parity(op, ins, ctx.download(d_out, ng.value * 16), None)
     else:
@@ -578,7 +684,7 @@ def run_op(args, ws, rank, local, op):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if op in ("groupby", "groupjoin") else "int64",
                 "data": "synthetic (seeded generator, resident in HBM)",
                 "config": {"workload": spec["workload"], "op": op, "tuples": n,
-                           "l2": "inputs larger than L2; no flush"},
+                           "l2": "inputs larger than L2; no flush"} | ({"output_rows": n_pairs} if n_pairs else {}),
                 "parity": parity,
                 "roofline": {"bound": "hbm", "kernel": f"pg_{op} (whole operator)", "achieved": achieved,
                              "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
@@ -604,7 +710,7 @@ def cpu_op_sample(op, ins, threads):
     elif op == "groupby":
         orc.groupby(a, val=(8, "dec"), agg="sum", hash=orc.hashcfg("modulo", 1 << 20), threads=threads)
         scale, kind = n / m, "linear"
-    elif op == "sort":
+    elif op in ("sort", "sortwide"):
         m = min(n, 1 << 22)
         a = np.ascontiguousarray(ins[0][:m])
         t0 = time.perf_counter()
@@ -637,9 +743,11 @@ def cpu_op_sample(op, ins, threads):
         orc.mergejoin(R, S, materialise=False, sum_col=1, threads=threads)
         scale, kind = n / m, "linear"
     t = (time.perf_counter() - t0) * scale
-    units = 2 * n if op == "mpsm" else (n + ins[0].shape[0] if op == "groupjoin" else n)
-    return {"value": units / t, "unit": "tuples/s", "cores": threads if op != "sort" else 1,
-            "kind": "port", "sample": f"{m} tuples (oracle port), time scaled {kind} to {n}"}
+    units = 2 * n if op in ("mpsm", "mpsmmat") else (n + ins[0].shape[0] if op == "groupjoin" else n)
+    one = op in ("sort", "sortwide")
+    return {"value": units / t, "unit": "tuples/s", "cores": 1 if one else threads,
+            "kind": "port", "sample": f"{m} tuples (oracle port{', one thread' if one else ''}), "
+                                      f"time scaled {kind} to {n}"}
 
 
 # ---------------------------------------------------------------------------
@@ -1200,7 +1308,7 @@ def run_filterjoin(args, ws, rank, local):
     L = gpu.lib()
     hR, R = _pinned_array(ctx, L, NR)
     hS, S = _pinned_array(ctx, L, NS)
-    make_inputs(R, S, threads)
+    make_join_inputs(join_spec(NR, NS), R, S, threads)
     dR, dS = ctx.alloc(NR * TUPLE), ctx.alloc(NS * TUPLE)
     dT, dO = ctx.alloc(NS * TUPLE), ctx.alloc(NS * TUPLE)
     ctx._check(L.pg_h2d(ctx.h, ctx.stream, dR.ptr, hR, NR * TUPLE))
@@ -1429,6 +1537,72 @@ def run_wideprobe(args, ws, rank, local):
     ctx.close()
 
 
+# ---------------------------------------------------------------------------
+# The default run: the headline line carries every other configuration's
+# line under "configs", each measured in this same process.
+# ---------------------------------------------------------------------------
+def _captured(fn, *a):
+    """Runs a bench function that prints one JSON line; returns that line."""
+    import contextlib
+    import io
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        fn(*a)
+    for ln in reversed(buf.getvalue().strip().splitlines()):
+        try:
+            return json.loads(ln)
+        except ValueError:
+            continue
+    return None
+
+
+def suite(args, ws, rank, local):
+    """The configurations other than the headline, at their full sizes, with
+    fewer steps (warm-up 3, timed 5) to keep the whole run within minutes."""
+    import copy
+    import gc
+    import torch
+    sub = copy.copy(args)
+    sub.steps, sub.warmup = min(args.steps, 5), max(3, min(args.warmup, 3))
+    jobs = [
+        ("cfg1_join_1Mx16M_count_sum",
+         lambda: run_join(sub, ws, rank, local, join_spec(1 << 20, 1 << 24, mode="count_sum"),
+                          max(sub.steps, 10), sub.warmup, cpu_sample=None, want_cpu=not args.no_cpu)),
+        ("cfg2a_join_16Mx256M_zipf1.0",
+         lambda: run_join(sub, ws, rank, local, join_spec(1 << 24, 1 << 28, "zipf", 1.0), sub.steps, sub.warmup,
+                          e2e_steps=1, cpu_sample=1 << 23, want_cpu=not args.no_cpu)),
+        ("cfg2a_join_16Mx256M_sparse_keys",
+         lambda: run_join(sub, ws, rank, local, join_spec(1 << 24, 1 << 28, key_domain="sparse"), sub.steps,
+                          sub.warmup, e2e_steps=1, cpu_sample=1 << 23, want_cpu=not args.no_cpu)),
+        ("cfg2b_groupby_256M_1M_groups", lambda: _captured(run_op, sub, ws, rank, local, "groupby")),
+        ("cfg3_mpsm_64Mx64M_count_sum", lambda: _captured(run_op, sub, ws, rank, local, "mpsm")),
+        ("cfg3_mpsm_64Mx64M_materialised", lambda: _captured(run_op, sub, ws, rank, local, "mpsmmat")),
+        ("sort_64M_keys_over_2e32_bitonic", lambda: _captured(run_op, sub, ws, rank, local, "sortwide")),
+        ("sort_64M_keys_16M_radix", lambda: _captured(run_op, sub, ws, rank, local, "sort")),
+        ("partition_256M_256way", lambda: _captured(run_op, sub, ws, rank, local, "partition")),
+        ("cfg4_batch_10000", lambda: _captured(run_batch, sub, ws, rank, local)),
+        ("cfg5_serve", lambda: _captured(run_serve, sub, ws, rank, local)),
+    ]
+    only = set(args.suite.split(",")) if args.suite else None
+    out = {}
+    for name, fn in jobs:
+        if only and name not in only:
+            continue
+        t0 = time.perf_counter()
+        try:
+            r = fn()
+        except Exception as e:  # one configuration failing must not take the others down
+            r = {"error": f"{type(e).__name__}: {e}"}
+        if r is not None:
+            r["wall_s"] = time.perf_counter() - t0
+            out[name] = r
+        print(f"[suite] {name}: {r.get('value') if r else None} ({time.perf_counter() - t0:.1f} s)",
+              file=sys.stderr, flush=True)
+        gc.collect()
+        torch.cuda.empty_cache()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1440,12 +1614,18 @@ def main():
     ap.add_argument("--key-domain", default="dense", choices=["dense", "sparse"],
                     help="dense: keys 1..|R| (direct-mapped table); sparse: the same keys "
                          "multiplied by an odd constant (hashed table)")
-    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "batch", "serve", "tableimage", "plan", "filterjoin",
-                                                      "wideprobe"] + sorted(OPS))
+    ap.add_argument("--probe-dist", default="uniform", choices=["uniform", "zipf"],
+                    help="probe foreign keys: uniform over R's keys, or Zipf ranks (--zipf-s)")
+    ap.add_argument("--zipf-s", type=float, default=1.0)
+    ap.add_argument("--op", default="hashjoin", choices=["hashjoin", "join1m", "batch", "serve", "tableimage", "plan",
+                                                      "filterjoin", "wideprobe"] + sorted(OPS))
+    ap.add_argument("--headline-only", action="store_true",
+                    help="the headline join alone, without the other configurations")
+    ap.add_argument("--suite", default="", help="comma-separated subset of the other configurations")
     ap.add_argument("--slots", type=int, default=8, help="worker slots for --op serve")
     ap.add_argument("--retune", action="store_true", help="rerun the autotuner for --op batch")
     ap.add_argument("--scale-down", type=int, default=0, help="divide --op sizes by 2^k")
-    ap.add_argument("--tune", default="", help="tuning knobs, e.g. probe_items=8,l2_persist=1")
+    ap.add_argument("--tune", default="", help="tuning knobs, e.g. probe_items=8,build_spec=2")
     ap.add_argument("--build-log2", type=int, default=24)
     ap.add_argument("--probe-log2", type=int, default=28)
     args = ap.parse_args()
@@ -1466,10 +1646,22 @@ def main():
         run_filterjoin(args, ws, rank, local)
     elif args.op == "wideprobe":
         run_wideprobe(args, ws, rank, local)
+    elif args.op == "join1m":
+        line = run_join(args, ws, rank, local, join_spec(1 << 20, 1 << 24, mode="count_sum"), args.steps,
+                        args.warmup, args.e2e_steps, None, not args.no_cpu)
+        if line:
+            print(json.dumps(line), flush=True)
     elif args.op != "hashjoin":
         run_op(args, ws, rank, local, args.op)
     else:
-        run_gpu(args, ws, rank, local)
+        line = run_join(args, ws, rank, local, headline_spec(args), args.steps, args.warmup, args.e2e_steps,
+                        max(1, NS // 32), not args.no_cpu)
+        if ws == 1 and not args.headline_only:
+            configs = suite(args, ws, rank, local)
+            if line is not None:
+                line["configs"] = configs
+        if line is not None:
+            print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -131,7 +131,9 @@ uint64_t pg_kernel_launches(void);
 /* Launch-shape knobs of a context, set by the autotuner (pythia_gb300/autotune.py).
  * No reference counterpart: they replace the reference's compile-time and plan
  * constants that size per-thread work (buffsize, tuplesperbucket, thread counts).
- * Value 0 restores the built-in choice. Results never depend on them. */
+ * Value 0 restores the built-in choice. Results never depend on them; a low
+ * PG_TUNE_SPIN_LIMIT can make a call fail with PG_ERR_TIMEOUT, which is how the
+ * bounded device waits are tested. */
 enum {
 	PG_TUNE_PROBE_CTAS_PER_SM = 0,   /* resident 8-warp CTAs per SM of the 16-byte probe (1..5) */
 	PG_TUNE_PROBE_VARIANT = 1,       /* 16-byte probe: 0 default, 1 warp-staged (bulk copies), 2 tiled with
@@ -155,7 +157,15 @@ enum {
 	                                    tables staged through shared memory where the width allows, everything
 	                                    else per-thread loads; 1 per-thread loads; 2 staged, 4 lookups per
 	                                    thread; 3 staged, 2 lookups per thread */
-	PG_TUNE_COUNT = 12
+	PG_TUNE_BUILD_SPEC = 11,         /* narrow dense build of 16-byte tuples: 0 on the device alone (key window
+	                                    from a sample, checked by the table's first use) for 65,536 tuples or
+	                                    more, 1 on the device alone at every size, 2 exact key range read back
+	                                    to the host first */
+	PG_TUNE_SPIN_LIMIT = 12,         /* polls a device-side wait for a bulk copy makes before the call fails with
+	                                    PG_ERR_TIMEOUT (the copy is still waited for, so the kernel ends
+	                                    cleanly): 0 the built-in limit (2^26 blocking polls), else that many
+	                                    non-blocking polls */
+	PG_TUNE_COUNT = 13
 };
 int pg_tune_set(pg_ctx* ctx, int knob, int64_t value);
 int64_t pg_tune_get(pg_ctx* ctx, int knob);
@@ -190,7 +200,11 @@ int pg_partition_sort(pg_ctx* ctx, pg_stream stream, const pg_rel* data,
  * (probe, join.cpp:503-562) with constructOutputTuple (join.cpp:475-501).
  * Equi-join on R.key = S.key; duplicates on either side give every pair.
  * `proj` lists the output columns in order. Output rows are packed to the
- * sum of the projected widths; their order is unspecified.               */
+ * sum of the projected widths; their order is unspecified.
+ * pg_hashjoin_build may return while its kernels still read R, and the
+ * table's first use may rebuild it from R (a dense layout taken from a
+ * sample and then refuted): R must stay valid and unchanged until the
+ * first probe (or other use) of the table has returned.                  */
 /* ---------------------------------------------------------------------- */
 int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 		const pg_col* proj, int nproj, pg_hashtable** ht);
@@ -243,9 +257,13 @@ int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* R_host, const pg_rel* S_host,
  * (-1: none). The hash table lives in one fixed 16 MiB device array that the
  * library declares; the build side may hold at most 524288 tuples (PG_ERR_ARG
  * beyond), and build-side projected columns at most 8 bytes in total. The
- * first call on a device looks the array up and should precede any stream
- * capture. Calls share the array (each clears it first), so calls that overlap
- * on the GPU race. Synchronous: returns after the result is on the host. */
+ * first call on each device in a process loads the library's device code and
+ * places the array there (CUDA loads modules lazily), which can allocate
+ * device memory: make it, with empty inputs if need be, before a pool takes
+ * the device's memory; later calls allocate nothing. Runs on ctx's device
+ * whatever device is current. Synchronous (returns after the result is on
+ * the host), so never call it while a stream is being captured. Calls share
+ * the array (each clears it first), so calls that overlap on the GPU race. */
 int pg_hashjoin_agg_noalloc(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 		const pg_rel* S, const pg_col* proj, int nproj, int sum_col,
 		pg_join_result* res);

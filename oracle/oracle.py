@@ -38,6 +38,13 @@ class JoinResult(ctypes.Structure):
     _fields_ = [("n_out", ctypes.c_uint64), ("sum", ctypes.c_int64)]
 
 
+class Digest(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint64), ("w0", ctypes.c_uint64), ("w1", ctypes.c_uint64), ("h", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {"rows": int(self.n), "sum_word0": int(self.w0), "sum_word1": int(self.w1), "sum_row_hash": int(self.h)}
+
+
 def lib():
     global _LIB
     if _LIB is None:
@@ -71,6 +78,16 @@ def lib():
         L.or_mergejoin.argtypes = [vp, u64, u32, u32, u32, vp, u64, u32, u32, u32,
                                    P(Col), ci, vp, u64, ci, ci, P(JoinResult)]
         L.or_mergejoin.restype = ci
+        L.or_hashjoin_paged.argtypes = [vp, u64, u32, u32, u32, vp, u64, u32, u32, u32,
+                                        P(HashCfg), u32, P(Col), ci, u32, ci, ci, P(JoinResult)]
+        L.or_hashjoin_paged.restype = ci
+        L.or_rows_digest.argtypes = [vp, u64, u32, ci, P(Digest)]; L.or_rows_digest.restype = None
+        L.or_hashjoin_digest.argtypes = [vp, u64, u32, u32, u32, vp, u64, u32, u32, u32,
+                                         P(HashCfg), u32, P(Col), ci, ci, P(Digest)]
+        L.or_hashjoin_digest.restype = ci
+        L.or_mergejoin_digest.argtypes = [vp, u64, u32, u32, u32, vp, u64, u32, u32, u32,
+                                          P(Col), ci, ci, P(Digest)]
+        L.or_mergejoin_digest.restype = ci
         L.or_filter.argtypes = [vp, u64, u32, P(Pred), ci, vp]; L.or_filter.restype = u64
         L.or_project.argtypes = [vp, u64, u32, P(Col), ci, vp]; L.or_project.restype = None
         _LIB = L
@@ -191,6 +208,59 @@ def hashjoin(R, S, proj=(("P", 8, 8), ("B", 8, 8)), hash=None, tuplesperbucket=4
     if rc:
         raise ValueError("or_hashjoin failed")
     return None, res.n_out, res.sum
+
+
+def hashjoin_paged(R, S, proj=(("P", 8, 8), ("B", 8, 8)), hash=None, tuplesperbucket=4,
+                   bkey=(0, 8), pkey=(0, 8), page_bytes=1 << 20, sum_col=-1, threads=1):
+    """The hash join with each thread writing its rows into one reused output
+    page of page_bytes (HashJoinOp::getNext's output page), returning
+    (rows, wrapping sum of column sum_col)."""
+    Ra, Rp, nR, wR = _rows(R)
+    Sa, Sp, nS, wS = _rows(S)
+    hash = hash or hashcfg("modulo", 1 << 10)
+    c, nc = cols(proj)
+    res = JoinResult()
+    if lib().or_hashjoin_paged(Rp, nR, wR, bkey[0], bkey[1], Sp, nS, wS, pkey[0], pkey[1],
+                               ctypes.byref(hash), tuplesperbucket, c, nc, page_bytes, sum_col, threads,
+                               ctypes.byref(res)):
+        raise ValueError("or_hashjoin_paged failed")
+    return res.n_out, res.sum
+
+
+def rows_digest(rows, threads=1):
+    """Order-independent digest of a row array (any row width): row count,
+    sums of the first and second 8-byte words, sum of a whole-row hash, all
+    mod 2^64 (or_rows_digest)."""
+    a, p, n, w = _rows(rows)
+    d = Digest()
+    lib().or_rows_digest(p, n, w, threads, ctypes.byref(d))
+    return d.as_dict()
+
+
+def hashjoin_digest(R, S, proj=(("P", 8, 8), ("B", 8, 8)), hash=None, tuplesperbucket=4,
+                    bkey=(0, 8), pkey=(0, 8), threads=1):
+    """rows_digest of the oracle hash join's output, without materialising it."""
+    Ra, Rp, nR, wR = _rows(R)
+    Sa, Sp, nS, wS = _rows(S)
+    hash = hash or hashcfg("modulo", 1 << 10)
+    c, nc = cols(proj)
+    d = Digest()
+    if lib().or_hashjoin_digest(Rp, nR, wR, bkey[0], bkey[1], Sp, nS, wS, pkey[0], pkey[1],
+                                ctypes.byref(hash), tuplesperbucket, c, nc, threads, ctypes.byref(d)):
+        raise ValueError("or_hashjoin_digest failed")
+    return d.as_dict()
+
+
+def mergejoin_digest(R, S, proj=(("P", 8, 8), ("B", 8, 8)), bkey=(0, 8), pkey=(0, 8), threads=1):
+    """rows_digest of the oracle sort-merge join's output, without materialising it."""
+    Ra, Rp, nR, wR = _rows(R)
+    Sa, Sp, nS, wS = _rows(S)
+    c, nc = cols(proj)
+    d = Digest()
+    if lib().or_mergejoin_digest(Rp, nR, wR, bkey[0], bkey[1], Sp, nS, wS, pkey[0], pkey[1],
+                                 c, nc, threads, ctypes.byref(d)):
+        raise ValueError("or_mergejoin_digest failed")
+    return d.as_dict()
 
 
 def mergejoin(R, S, proj=(("P", 8, 8), ("B", 8, 8)), bkey=(0, 8), pkey=(0, 8),

@@ -167,6 +167,67 @@ static void run_threads(int T, thr_fn fn, void* args, size_t argsz)
 static inline uint64_t slice_lo(uint64_t n, int t, int T) { return (uint64_t) ((__uint128_t) n * t / T); }
 
 /* ------------------------------------------------------------------ */
+/* Row-multiset digests (a checker utility, not a reference function)  */
+/* ------------------------------------------------------------------ */
+/* SplitMix64's finaliser (Steele, Lea and Flood, "Fast splittable
+ * pseudorandom number generators", 2014). */
+static inline uint64_t dg_mix(uint64_t z)
+{
+	z ^= z >> 30; z *= 0xBF58476D1CE4E5B9ull;
+	z ^= z >> 27; z *= 0x94D049BB133111EBull;
+	return z ^ (z >> 31);
+}
+
+/* Hash of one row: its 8-byte words (a short last word zero-filled) folded
+ * in order, so two rows with the same words in other columns differ. */
+static inline uint64_t dg_row_hash(const char* r, uint32_t w)
+{
+	uint64_t h = 0x243F6A8885A308D3ull ^ w;
+	for (uint32_t o = 0; o < w; o += 8) {
+		uint64_t x = 0;
+		memcpy(&x, r + o, w - o < 8 ? w - o : 8);
+		h = dg_mix(h ^ x) + 0x9E3779B97F4A7C15ull;
+	}
+	return h;
+}
+
+static inline void dg_add(or_digest* d, const char* r, uint32_t w)
+{
+	uint64_t x0 = 0, x1 = 0;
+	memcpy(&x0, r, w < 8 ? w : 8);
+	if (w > 8) memcpy(&x1, r + 8, w - 8 < 8 ? w - 8 : 8);
+	d->n++; d->w0 += x0; d->w1 += x1; d->h += dg_row_hash(r, w);
+}
+
+static inline void dg_merge(or_digest* d, const or_digest* e)
+{
+	d->n += e->n; d->w0 += e->w0; d->w1 += e->w1; d->h += e->h;
+}
+
+typedef struct { const char* rows; uint64_t n; uint32_t w; int T, tid; or_digest d; } dg_arg;
+
+static void* dg_thread(void* p)
+{
+	dg_arg* a = (dg_arg*) p;
+	uint64_t lo = slice_lo(a->n, a->tid, a->T), hi = slice_lo(a->n, a->tid + 1, a->T);
+	for (uint64_t i = lo; i < hi; ++i) dg_add(&a->d, a->rows + i * a->w, a->w);
+	return 0;
+}
+
+void or_rows_digest(const void* rows, uint64_t n, uint32_t w, int threads, or_digest* d)
+{
+	if (threads < 1) threads = 1;
+	dg_arg* args = (dg_arg*) calloc(threads, sizeof(dg_arg));
+	for (int t = 0; t < threads; ++t) {
+		args[t].rows = (const char*) rows; args[t].n = n; args[t].w = w; args[t].T = threads; args[t].tid = t;
+	}
+	run_threads(threads, dg_thread, args, sizeof(dg_arg));
+	memset(d, 0, sizeof *d);
+	for (int t = 0; t < threads; ++t) dg_merge(d, &args[t].d);
+	free(args);
+}
+
+/* ------------------------------------------------------------------ */
 /* Chained-bucket hash table: util/hashtable.{h,cpp}                   */
 /* ------------------------------------------------------------------ */
 /* BucketHeader {Lock (1 byte TAS), unsigned short used, BucketHeader* next},
@@ -271,9 +332,11 @@ typedef struct {
 	uint32_t sw, ow; int sum_col; int T; pthread_barrier_t* bar;
 	uint32_t* bproj_off; uint32_t nbproj; /* build-projected source offsets/bytes */
 	uint32_t* bproj_bytes;
-	int materialise;
+	int materialise, digest;
+	uint32_t page_bytes;   /* > 0: rows go to one reused output page per thread */
 	/* per thread */
-	int tid; arena ar; growbuf out; uint64_t nout; int64_t sum;
+	int tid; arena ar; growbuf out; uint64_t nout; int64_t sum; or_digest dg;
+	char* page; uint32_t page_used; uint64_t pages;
 } hj_arg;
 
 static int64_t col_as_i64(const char* p, uint32_t bytes)
@@ -304,7 +367,7 @@ static void* hj_thread(void* p)
 	/* getNext probe loop, join.cpp:503-562: hash the probe key, walk the
 	 * bucket chain, compare keys, constructOutputTuple (join.cpp:475-501). */
 	lo = slice_lo(a->nS, a->tid, a->T); hi = slice_lo(a->nS, a->tid + 1, a->T);
-	char row[1024];
+	char rowbuf[1024];
 	for (uint64_t i = lo; i < hi; ++i) {
 		const char* ptup = a->S + i * a->wS;
 		uint32_t h = or_hash_value(&a->fn, ptup + a->pkoff, a->pkbytes);
@@ -312,6 +375,10 @@ static void* hj_thread(void* p)
 			const char* b = (const char*) bh + sizeof(bhdr);
 			for (uint32_t u = 0; u < bh->used; u += a->sw, b += a->sw) {
 				if (!keys_equal(b, a->bkbytes, ptup + a->pkoff, a->pkbytes)) continue;
+				/* With pages, constructOutputTuple writes straight into the
+				 * thread's output page, which is handed on (here: reused)
+				 * once the next row would not fit (join.cpp:510-545). */
+				char* row = a->page ? a->page + a->page_used : rowbuf;
 				uint32_t o = 0, battr = a->bkbytes;
 				for (int j = 0; j < a->nproj; ++j) {
 					const or_col* c = &a->proj[j];
@@ -322,17 +389,60 @@ static void* hj_thread(void* p)
 				}
 				a->nout++;
 				if (a->materialise) gb_push(&a->out, row, a->ow);
+				if (a->digest) dg_add(&a->dg, row, a->ow);
+				if (a->page) {
+					a->page_used += a->ow;
+					if (a->page_used + a->ow > a->page_bytes) { a->page_used = 0; a->pages++; }
+				}
 			}
 		}
 	}
 	return 0;
 }
 
+static int hashjoin_run(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_t bkbytes,
+		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
+		const or_hashcfg* hash, uint32_t tuplesperbucket,
+		const or_col* proj, int nproj, void* out, uint64_t out_cap,
+		int sum_col, int threads, or_join_result* res, or_digest* dg, uint32_t page_bytes);
+
 int or_hashjoin(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_t bkbytes,
 		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
 		const or_hashcfg* hash, uint32_t tuplesperbucket,
 		const or_col* proj, int nproj, void* out, uint64_t out_cap,
 		int sum_col, int threads, or_join_result* res)
+{
+	return hashjoin_run(R, nR, wR, bkoff, bkbytes, S, nS, wS, pkoff, pkbytes, hash, tuplesperbucket,
+			proj, nproj, out, out_cap, sum_col, threads, res, 0, 0);
+}
+
+int or_hashjoin_paged(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_t bkbytes,
+		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
+		const or_hashcfg* hash, uint32_t tuplesperbucket,
+		const or_col* proj, int nproj, uint32_t page_bytes,
+		int sum_col, int threads, or_join_result* res)
+{
+	if (page_bytes == 0) return -1;
+	return hashjoin_run(R, nR, wR, bkoff, bkbytes, S, nS, wS, pkoff, pkbytes, hash, tuplesperbucket,
+			proj, nproj, 0, 0, sum_col, threads, res, 0, page_bytes);
+}
+
+int or_hashjoin_digest(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_t bkbytes,
+		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
+		const or_hashcfg* hash, uint32_t tuplesperbucket,
+		const or_col* proj, int nproj, int threads, or_digest* dg)
+{
+	or_join_result res;
+	memset(dg, 0, sizeof *dg);
+	return hashjoin_run(R, nR, wR, bkoff, bkbytes, S, nS, wS, pkoff, pkbytes, hash, tuplesperbucket,
+			proj, nproj, 0, 0, -1, threads, &res, dg, 0);
+}
+
+static int hashjoin_run(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_t bkbytes,
+		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
+		const or_hashcfg* hash, uint32_t tuplesperbucket,
+		const or_col* proj, int nproj, void* out, uint64_t out_cap,
+		int sum_col, int threads, or_join_result* res, or_digest* dg, uint32_t page_bytes)
 {
 	or_hashfn fn;
 	if (or_hashfn_make(hash, &fn)) return -1;
@@ -344,7 +454,7 @@ int or_hashjoin(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_
 		ow += proj[j].bytes;
 		if (proj[j].side == 0) { sw += proj[j].bytes; boff[nb] = proj[j].off; bbytes[nb++] = proj[j].bytes; }
 	}
-	if (ow > 1024 || nb > 64) return -1;
+	if (ow > 1024 || nb > 64 || (page_bytes && page_bytes < ow)) return -1;
 	chtable ht;
 	if (ch_init(&ht, fn.nbuckets, tuplesperbucket * sw, sw)) return -1;
 	pthread_barrier_t bar; pthread_barrier_init(&bar, 0, threads);
@@ -356,13 +466,17 @@ int or_hashjoin(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_
 		a->pkoff = pkoff; a->pkbytes = pkbytes; a->fn = fn; a->ht = &ht;
 		a->proj = proj; a->nproj = nproj; a->sw = sw; a->ow = ow; a->sum_col = sum_col;
 		a->T = threads; a->bar = &bar; a->bproj_off = boff; a->bproj_bytes = bbytes;
-		a->nbproj = nb; a->materialise = out != 0; a->tid = t;
+		a->nbproj = nb; a->materialise = out != 0; a->digest = dg != 0; a->tid = t;
+		a->page_bytes = page_bytes;
+		a->page = page_bytes ? (char*) malloc(page_bytes) : 0;
 	}
 	run_threads(threads, hj_thread, args, sizeof(hj_arg));
 	uint64_t total = 0, written = 0; int64_t sum = 0;
 	for (int t = 0; t < threads; ++t) {
 		hj_arg* a = &args[t];
 		total += a->nout; sum = (int64_t) ((uint64_t) sum + (uint64_t) a->sum);
+		if (dg) dg_merge(dg, &a->dg);
+		free(a->page);
 		if (out) {
 			uint64_t rows = a->out.used / ow;
 			uint64_t take = rows;
@@ -696,10 +810,10 @@ int or_groupby_exact(const void* in, uint64_t n, uint32_t w, int has_key, uint32
 /* ------------------------------------------------------------------ */
 typedef struct {
 	const char *R, *S; uint64_t nR, nS; uint32_t wR, wS, bkoff, bkbytes, pkoff, pkbytes;
-	const or_col* proj; int nproj; uint32_t ow; int sum_col, T, tid, materialise;
+	const or_col* proj; int nproj; uint32_t ow; int sum_col, T, tid, materialise, digest;
 	kidx** rruns; kidx** sruns; uint64_t *rlen, *slen; uint64_t *rlo, *slo;
 	pthread_barrier_t* bar;
-	growbuf out; uint64_t nout; int64_t sum;
+	growbuf out; uint64_t nout; int64_t sum; or_digest dg;
 } mj_arg;
 
 static void* mj_thread(void* p)
@@ -743,6 +857,7 @@ static void* mj_thread(void* p)
 					}
 					a->nout++;
 					if (a->materialise) gb_push(&a->out, row, a->ow);
+					if (a->digest) dg_add(&a->dg, row, a->ow);
 				}
 			i = i1; j = j1;
 		}
@@ -750,10 +865,34 @@ static void* mj_thread(void* p)
 	return 0;
 }
 
+static int mergejoin_run(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_t bkbytes,
+		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
+		const or_col* proj, int nproj, void* out, uint64_t out_cap,
+		int sum_col, int threads, or_join_result* res, or_digest* dg);
+
 int or_mergejoin(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_t bkbytes,
 		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
 		const or_col* proj, int nproj, void* out, uint64_t out_cap,
 		int sum_col, int threads, or_join_result* res)
+{
+	return mergejoin_run(R, nR, wR, bkoff, bkbytes, S, nS, wS, pkoff, pkbytes, proj, nproj, out, out_cap,
+			sum_col, threads, res, 0);
+}
+
+int or_mergejoin_digest(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_t bkbytes,
+		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
+		const or_col* proj, int nproj, int threads, or_digest* dg)
+{
+	or_join_result res;
+	memset(dg, 0, sizeof *dg);
+	return mergejoin_run(R, nR, wR, bkoff, bkbytes, S, nS, wS, pkoff, pkbytes, proj, nproj, 0, 0, -1,
+			threads, &res, dg);
+}
+
+static int mergejoin_run(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_t bkbytes,
+		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
+		const or_col* proj, int nproj, void* out, uint64_t out_cap,
+		int sum_col, int threads, or_join_result* res, or_digest* dg)
 {
 	if (threads < 1) threads = 1;
 	uint32_t ow = 0;
@@ -770,6 +909,7 @@ int or_mergejoin(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32
 		a->wR = wR; a->wS = wS; a->bkoff = bkoff; a->bkbytes = bkbytes;
 		a->pkoff = pkoff; a->pkbytes = pkbytes; a->proj = proj; a->nproj = nproj;
 		a->ow = ow; a->sum_col = sum_col; a->T = threads; a->tid = t; a->materialise = out != 0;
+		a->digest = dg != 0;
 		a->rruns = rruns; a->sruns = sruns; a->rlen = lens; a->slen = lens + threads;
 		a->rlo = lens + 2 * threads; a->slo = lens + 3 * threads; a->bar = &bar;
 	}
@@ -778,6 +918,7 @@ int or_mergejoin(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32
 	for (int t = 0; t < threads; ++t) {
 		mj_arg* a = &args[t];
 		total += a->nout; sum = (int64_t) ((uint64_t) sum + (uint64_t) a->sum);
+		if (dg) dg_merge(dg, &a->dg);
 		if (out) {
 			uint64_t rows = a->out.used / ow, take = rows;
 			if (written + take > out_cap) take = out_cap > written ? out_cap - written : 0;

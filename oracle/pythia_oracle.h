@@ -70,6 +70,29 @@ int or_hashjoin(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_
 		const or_col* proj, int nproj, void* out, uint64_t out_cap,
 		int sum_col, int threads, or_join_result* res);
 
+/* or_hashjoin with every output row written into one output page of
+ * page_bytes per thread that is reused once full, as HashJoinOp::getNext
+ * fills and hands on its output page (join.cpp:510-545): the CPU timing
+ * of the reference operator, with no result array. */
+int or_hashjoin_paged(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_t bkbytes,
+		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
+		const or_hashcfg* hash, uint32_t tuplesperbucket,
+		const or_col* proj, int nproj, uint32_t page_bytes,
+		int sum_col, int threads, or_join_result* res);
+
+/* Order-independent digest of a multiset of rows, all sums mod 2^64: the
+ * row count, the sums of each row's first and second 8-byte words (zero
+ * where a row is shorter) and the sum of a hash of each whole row. A
+ * checker utility for outputs too large to compare row by row. */
+typedef struct { uint64_t n, w0, w1, h; } or_digest;
+void or_rows_digest(const void* rows, uint64_t n, uint32_t w, int threads, or_digest* d);
+/* The digest of or_hashjoin's / or_mergejoin's output rows, without
+ * materialising them. */
+int or_hashjoin_digest(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_t bkbytes,
+		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
+		const or_hashcfg* hash, uint32_t tuplesperbucket,
+		const or_col* proj, int nproj, int threads, or_digest* d);
+
 int or_partition(const void* in, uint64_t n, uint32_t w, uint32_t koff, uint32_t kbytes,
 		const or_hashcfg* hash, void* out, uint64_t* offsets, int threads);
 
@@ -88,6 +111,9 @@ int or_mergejoin(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32
 		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
 		const or_col* proj, int nproj, void* out, uint64_t out_cap,
 		int sum_col, int threads, or_join_result* res);
+int or_mergejoin_digest(const void* R, uint64_t nR, uint32_t wR, uint32_t bkoff, uint32_t bkbytes,
+		const void* S, uint64_t nS, uint32_t wS, uint32_t pkoff, uint32_t pkbytes,
+		const or_col* proj, int nproj, int threads, or_digest* d);
 
 /* Filter / Project (filter.cpp:37-85, project.cpp:37-104): column types and
  * comparisons of Comparator (comparator.h:43-83). A date column compares as

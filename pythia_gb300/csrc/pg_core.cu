@@ -2,6 +2,7 @@
 // every operator of libpythia_gpu.
 #include "pg_internal.cuh"
 #include <cstring>
+#include <algorithm>
 #include <cstdio>
 
 std::atomic<uint64_t> g_kernel_launches{0};
@@ -31,6 +32,11 @@ extern "C" int pg_tune_set(pg_ctx* ctx, int knob, int64_t value)
 	if (!ctx || knob < 0 || knob >= PG_TUNE_COUNT || value < 0)
 		return pg_fail(ctx, PG_ERR_ARG, "pg_tune_set: unknown knob or negative value");
 	ctx->tune[knob] = value;
+	if (knob == PG_TUNE_SPIN_LIMIT) {
+		// Kernels read the limit from word 1 of the device status block.
+		const uint32_t v = (uint32_t) std::min<int64_t>(value, (int64_t) PG_SPIN_LIMIT);
+		PG_CUDA(ctx, cudaMemcpy(ctx->d_status + 1, &v, sizeof v, cudaMemcpyHostToDevice));
+	}
 	return PG_OK;
 }
 

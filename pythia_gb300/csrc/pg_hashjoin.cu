@@ -57,6 +57,7 @@ struct HjProbeTable {
 	uint32_t cache;                        // L2 policy knob: bits 0-1 table loads (0 evict-last,
 	                                       // 1 normal, 2 unchanged, 3 first); bit 2 probe reads,
 	                                       // bit 3 output stores normal instead of evict-first
+	const HjDenseHdr* hdr;                 // speculative narrow dense table: window and checks, else null
 };
 
 
@@ -252,6 +253,181 @@ __global__ void k_dense32_count(const uint32_t* __restrict__ table, uint64_t ran
 	#pragma unroll
 	for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
 	if ((threadIdx.x & 31) == 0 && c) atomicAdd(cnt, c);
+}
+
+// ---------------------------------------------------------------------------
+// Narrow dense build of 16-byte tuples without host round trips. The layout
+// is chosen from a sample and checked afterwards: a key outside the window, a
+// value outside the entry range or fewer present entries than tuples (a
+// repeated key) marks the header bad, and the table's first use rebuilds it
+// exactly. Four launches: sample, fill, store, count.
+// ---------------------------------------------------------------------------
+#define HJ_SPEC_SAMPLE 4096
+#define HJ_SPEC_MIN_TUPLES 65536
+
+__device__ __forceinline__ void hj_minmax4(unsigned long long& lo, unsigned long long& hi, unsigned long long& vlo,
+		unsigned long long& vhi)
+{
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		unsigned long long a = __shfl_down_sync(0xffffffffu, lo, o), b = __shfl_down_sync(0xffffffffu, hi, o);
+		unsigned long long c = __shfl_down_sync(0xffffffffu, vlo, o), d = __shfl_down_sync(0xffffffffu, vhi, o);
+		lo = a < lo ? a : lo; hi = b > hi ? b : hi;
+		vlo = c < vlo ? c : vlo; vhi = d > vhi ? d : vhi;
+	}
+}
+
+// One CTA of 1024 threads: key and value ranges of HJ_SPEC_SAMPLE evenly
+// spaced build tuples (all of them when fewer) set the window: the sampled key
+// span widened by a sixteenth of itself plus 1024 keys on each side (exact
+// when every tuple was sampled), and the value base: 0 when the sampled
+// values leave room for it, else centred on them. `cap` = entries allocated.
+__global__ void __launch_bounds__(1024) k_dense_prep16(const uint4* __restrict__ R, uint64_t n, uint32_t kw,
+		HjBuildCols bc, uint64_t cap, HjDenseHdr* __restrict__ hdr)
+{
+	__shared__ unsigned long long red[4][32];
+	const uint64_t m = n < HJ_SPEC_SAMPLE ? n : HJ_SPEC_SAMPLE;
+	const uint64_t q = n / m, r = n % m;
+	unsigned long long lo = ~0ull, hi = 0, vlo = ~0ull, vhi = 0;
+	for (uint64_t t = threadIdx.x; t < m; t += blockDim.x) {
+		const uint64_t i = t * q + (t * r) / m;      // < n: t < m, t*r < 2^24
+		const uint4 v = __ldg(R + i);
+		const unsigned long long k = (((unsigned long long) hj_word4(v, kw + 1) << 32) | hj_word4(v, kw)) ^ (1ull << 63);
+		const unsigned long long p = hj_pack_value16(v, bc);
+		lo = k < lo ? k : lo; hi = k > hi ? k : hi;
+		vlo = p < vlo ? p : vlo; vhi = p > vhi ? p : vhi;
+	}
+	hj_minmax4(lo, hi, vlo, vhi);
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	if (lane == 0) { red[0][warp] = lo; red[1][warp] = hi; red[2][warp] = vlo; red[3][warp] = vhi; }
+	__syncthreads();
+	if (warp != 0) return;
+	const int nw = blockDim.x >> 5;
+	lo = lane < nw ? red[0][lane] : ~0ull; hi = lane < nw ? red[1][lane] : 0;
+	vlo = lane < nw ? red[2][lane] : ~0ull; vhi = lane < nw ? red[3][lane] : 0;
+	hj_minmax4(lo, hi, vlo, vhi);
+	if (lane != 0) return;
+	HjDenseHdr h;
+	h.n = n; h.present = 0; h.kmin = ~0ull; h.kmax = 0; h.vlo = ~0ull; h.vhi = 0; h.flags = 0; h.pad = 0;
+	unsigned long long wlo = lo, whi = hi;
+	if (m != n) {
+		const unsigned long long d = (hi - lo) / 16 + 1024;
+		wlo = lo >= d ? lo - d : 0;
+		whi = hi <= ~0ull - d ? hi + d : ~0ull;
+	}
+	h.dmin = (long long) (wlo ^ (1ull << 63));
+	h.drange = whi - wlo < cap ? whi - wlo + 1 : 0;
+	const unsigned long long vspan = vhi - vlo;
+	h.vmin = 0;
+	if (h.drange == 0 || vspan >= 0xFFFFFFFEull) {
+		h.flags = 4;
+		h.drange = 0;
+	} else {
+		const unsigned long long slack = m == n ? 0 : (0xFFFFFFFEull - vspan) / 2;
+		h.vmin = vlo <= slack ? 0 : vlo - slack;
+	}
+	*hdr = h;
+}
+
+// All ones over the window's entries (nothing when the sample ruled it out).
+__global__ void k_dense_fill16(uint32_t* __restrict__ table, const HjDenseHdr* __restrict__ hdr)
+{
+	const unsigned long long range = hdr->drange;
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	const uint64_t n4 = range / 4;
+	uint4* t4 = reinterpret_cast<uint4*>(table);
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n4; i += stride)
+		t4[i] = make_uint4(~0u, ~0u, ~0u, ~0u);
+	for (uint64_t i = 4 * n4 + blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < range; i += stride)
+		table[i] = ~0u;
+}
+
+// Store pass: entry key - dmin = value - vmin, plain stores kept in L2
+// (evict-last measured fastest for the scattered 4-byte stores); records the
+// exact key and value ranges, and flags keys and values the window misses.
+__global__ void k_dense32_spec16(const uint4* __restrict__ R, uint64_t n, uint32_t kw, HjBuildCols bc,
+		uint32_t* __restrict__ table, HjDenseHdr* __restrict__ hdr)
+{
+	if (hdr->flags) return;
+	const unsigned long long dmin = (unsigned long long) hdr->dmin, range = hdr->drange, vmin = hdr->vmin;
+	const uint64_t keep = pg_policy_evict_last();
+	unsigned long long lo = ~0ull, hi = 0, vlo = ~0ull, vhi = 0;
+	int bad = 0;
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	for (uint64_t i0 = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+		uint4 t[4];
+		#pragma unroll
+		for (int u = 0; u < 4; ++u) if (i0 + u * stride < n) t[u] = __ldg(R + i0 + u * stride);
+		#pragma unroll
+		for (int u = 0; u < 4; ++u) {
+			if (i0 + u * stride >= n) break;
+			const unsigned long long key = ((unsigned long long) hj_word4(t[u], kw + 1) << 32) | hj_word4(t[u], kw);
+			const unsigned long long v = hj_pack_value16(t[u], bc);
+			const unsigned long long ko = key ^ (1ull << 63);
+			lo = ko < lo ? ko : lo; hi = ko > hi ? ko : hi;
+			vlo = v < vlo ? v : vlo; vhi = v > vhi ? v : vhi;
+			const unsigned long long d = key - dmin, e = v - vmin;
+			if (d >= range) bad |= 1;
+			else if (e >= 0xFFFFFFFFull) bad |= 2;
+			else asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;"
+					:: "l"(table + d), "r"((uint32_t) e), "l"(keep) : "memory");
+		}
+	}
+	hj_minmax4(lo, hi, vlo, vhi);
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) bad |= __shfl_down_sync(0xffffffffu, bad, o);
+	if ((threadIdx.x & 31) == 0) {
+		if (lo <= hi) {
+			atomicMin(&hdr->kmin, lo); atomicMax(&hdr->kmax, hi);
+			atomicMin(&hdr->vlo, vlo); atomicMax(&hdr->vhi, vhi);
+		}
+		if (bad) atomicOr(&hdr->flags, bad);
+	}
+}
+
+// Count pass: present entries of the window into hdr->present (equal to n
+// exactly when no key repeated).
+__global__ void k_dense32_count_spec(const uint32_t* __restrict__ table, HjDenseHdr* __restrict__ hdr)
+{
+	if (hdr->flags) return;
+	const unsigned long long range = hdr->drange;
+	unsigned long long c = 0;
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	const uint64_t n4 = range / 4;
+	const uint4* t4 = reinterpret_cast<const uint4*>(table);
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n4; i += stride) {
+		const uint4 v = t4[i];
+		c += (v.x != 0xFFFFFFFFu) + (v.y != 0xFFFFFFFFu) + (v.z != 0xFFFFFFFFu) + (v.w != 0xFFFFFFFFu);
+	}
+	for (uint64_t i = 4 * n4 + blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < range; i += stride)
+		c += table[i] != 0xFFFFFFFFu;
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+	if ((threadIdx.x & 31) == 0 && c) atomicAdd(&hdr->present, c);
+}
+
+// Entries of a settled table re-based from the sample's value base to the
+// exact smallest value, into a new array: present entries drop by `shift`.
+__global__ void k_dense32_rebase(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, uint64_t range,
+		uint32_t shift)
+{
+	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < range; i += (uint64_t) gridDim.x * blockDim.x) {
+		const uint32_t e = src[i];
+		dst[i] = e != 0xFFFFFFFFu ? e - shift : e;
+	}
+}
+
+// Probe kernels given a speculative table read its window here; false: the
+// build's checks failed, the kernel does nothing and the host rebuilds.
+__device__ __forceinline__ bool hj_spec_resolve(HjProbeTable& tb)
+{
+	if (!tb.hdr) return true;
+	const HjDenseHdr* h = tb.hdr;
+	if (h->flags != 0 || h->present != h->n) return false;
+	tb.dmin = h->dmin;
+	tb.drange = h->drange;
+	tb.vmin = h->vmin;
+	return true;
 }
 
 // Dense table: presence bit and value at key - dmin. A bit found already set
@@ -506,14 +682,17 @@ k_probe16_tma(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPro
 	};
 	if (tid == 0) issue(tile, 0);
 	uint32_t phases = 0;     // bit b: parity expected next on bar[b]
+	const uint32_t spin = pg_spin_knob(status);
 	for (int it = 0; tile < ntiles; tile += gridDim.x, ++it) {
 		const int b = it & 1;
 		const uint4* const tp = tin0 + b * HJT_TILE;
 		const uint64_t base = tile * HJT_TILE;
 		const uint32_t rows = (uint32_t) pg_min64(HJT_TILE, n - base);
-		// A wait that gives up leaves the tile's contents unspecified; every
-		// later access stays in bounds and the host sees the status.
-		if (!pg_mbar_wait(&bar[b], (phases >> b) & 1)) pg_set_status(status, PG_ERR_TIMEOUT);
+		// A wait past the context's limit records PG_ERR_TIMEOUT and drains
+		// the copy; if even that gives up, the tile's contents are
+		// unspecified, every later access stays in bounds and the host sees
+		// the status.
+		pg_mbar_wait_timed(&bar[b], (phases >> b) & 1, spin, status);
 		phases ^= 1u << b;
 		// Prefetch the next tile into the other buffer; its previous contents
 		// were last read before the final barrier of the previous tile.
@@ -836,7 +1015,7 @@ __device__ __forceinline__ void hj_resolve_items(const HjProbeTable& tb, const i
 __device__ __forceinline__ void hjg_arrive(const char* S, uint64_t base, uint32_t rows, uint32_t W,
 		unsigned char* tp, uint64_t* bar, int b, uint32_t& phases, int* status)
 {
-	if (!pg_mbar_wait(&bar[b], (phases >> b) & 1)) pg_set_status(status, PG_ERR_TIMEOUT);
+	pg_mbar_wait_timed(&bar[b], (phases >> b) & 1, pg_spin_knob(status), status);
 	phases ^= 1u << b;
 	const uint32_t bytes = rows * W, bulk = bytes & ~15u;
 	if (bulk != bytes) {     // final tile only; block-uniform
@@ -1071,12 +1250,14 @@ k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 			if (first + i * W < nchunks) issue(first + i * W, i);
 	}
 	__syncwarp();
+	const uint32_t spin = pg_spin_knob(status);
 	for (uint64_t k = 0, c = first; c < nchunks; ++k, c += W) {
 		const int stg = (int) (k % PW_STAGES);
 		const uint32_t parity = (uint32_t) ((k / PW_STAGES) & 1);
-		// A wait that gives up leaves the chunk unspecified; all accesses stay
-		// in bounds and the host reads the status.
-		if (!pg_mbar_wait(&bar[stg], parity)) pg_set_status(status, PG_ERR_TIMEOUT);
+		// A wait past the context's limit records PG_ERR_TIMEOUT and drains
+		// the copy; if even that gives up the chunk is unspecified, all
+		// accesses stay in bounds and the host reads the status.
+		pg_mbar_wait_timed(&bar[stg], parity, spin, status);
 		const uint4* const tp = st0 + stg * BLK;
 		const uint32_t rows = (uint32_t) pg_min64(BLK, n - c * BLK);
 		uint32_t rank[SUB];
@@ -1217,12 +1398,14 @@ __device__ __forceinline__ void hj_st_stream(char* p, uint4 v, uint64_t pol)
 // on the probe side run as the probe's prologue).
 template <bool MATERIALIZE, int MODE, bool PF, bool STD = false, bool PRED = false>
 __global__ void __launch_bounds__(PW_WARPS * 32, PF ? 4 : 5)
-k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb,
+k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb0,
 		uint32_t wsel, uint32_t sum_w0, uint32_t sum_words, char* __restrict__ out,
 		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg,
 		int sum_col, uint64_t dlo, uint64_t dhi, int run, const PgPred16 pr = PgPred16())
 {
 	static_assert(MODE == 1 || MODE == 2, "dense tables only");
+	HjProbeTable tb = tb0;
+	if (!hj_spec_resolve(tb)) return;
 	constexpr int ITEMS = PW_CHUNK / 32;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
@@ -1337,9 +1520,11 @@ __device__ __forceinline__ void hj_lookup4(const HjProbeTable& tb, const uint4 (
 
 template <bool PRED>
 __global__ void __launch_bounds__(PW_WARPS * 32, 3)
-k_probe16_deep(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb, char* __restrict__ out,
+k_probe16_deep(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb0, char* __restrict__ out,
 		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg, const PgPred16 pr)
 {
+	HjProbeTable tb = tb0;
+	if (!hj_spec_resolve(tb)) return;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
 	const uint64_t W = (uint64_t) gridDim.x * PW_WARPS;
@@ -1651,36 +1836,30 @@ static int hj_validate_proj(pg_ctx* ctx, const pg_col* proj, int nproj, uint32_t
 	return PG_OK;
 }
 
-extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
-		const pg_col* proj, int nproj, pg_hashtable** out)
+// Build sides of 16-byte tuples whose key and build-projected columns lie in
+// the tuple (one vector load per tuple).
+static bool hj_vec16(const pg_rel* R, const HjBuildCols& bc)
 {
-	if (!ctx || !out) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_build: null argument");
+	bool v = R->width == 16 && (R->key_off == 0 || R->key_off == 8) && R->key_bytes == 8 &&
+		(reinterpret_cast<uintptr_t>(R->data) & 15) == 0;
+	for (int c = 0; c < bc.n; ++c) v = v && bc.roff[c] + bc.words[c] <= 4;
+	return v;
+}
+
+// The table of R with host round trips: exact key and value ranges read back
+// first, then a dense layout (duplicates counted and read back) or the hashed
+// table. Fills the layout fields of `ht`.
+static int hj_build_exact(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, pg_hashtable* ht)
+{
 	int rc;
-	if ((rc = hj_validate_rel(ctx, R, "pg_hashjoin_build"))) return rc;
-	if ((rc = hj_validate_proj(ctx, proj, nproj, R->width, 1u << 30))) return rc;
-	cudaStream_t s = (cudaStream_t) stream;
-	pg_hashtable* ht = new pg_hashtable();
-	ht->nbuild = R->n; ht->R = (const char*) R->data; ht->wR = R->width; ht->bkey_bytes = R->key_bytes;
-	ht->nproj = nproj;
-	ht->stream = s;
-	for (int i = 0; i < nproj; ++i) ht->proj[i] = proj[i];
-	uint32_t bbytes = 0;
-	ht->bcols.n = 0;
-	for (int i = 0; i < nproj; ++i)
-		if (proj[i].side == 0) {
-			ht->bcols.roff[ht->bcols.n] = (uint16_t) (proj[i].off / 4);
-			ht->bcols.words[ht->bcols.n] = (uint8_t) (proj[i].bytes / 4);
-			ht->bcols.n++;
-			bbytes += proj[i].bytes;
-		}
-	ht->inline_val = bbytes <= 8;
 	ht->dense = false; ht->dense_val = nullptr; ht->dense_bits = nullptr; ht->dense32 = nullptr; ht->vmin = 0;
+	ht->slots = nullptr; ht->side = nullptr; ht->nside = 0;
 	if (R->n && ht->inline_val && ctx->tune[PG_TUNE_DENSE] != 2) {
 		// Dense key domain (unique keys spanning at most 2|R| values, e.g. a
 		// surrogate primary key 1..N): index by key - min, no hashing. Only
 		// for packed values: the unique-key probe kernels read them inline.
 		unsigned long long* mm = nullptr;
-		if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 64))) { delete ht; return rc; }
+		if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 64))) return rc;
 		unsigned long long init[4] = {~0ull, 0, ~0ull, 0};
 		PG_CUDA(ctx, cudaMemcpyAsync(mm, init, 32, cudaMemcpyHostToDevice, s));
 		int blocks = (int) std::min<uint64_t>(pg_div_up(R->n, 256), (uint64_t) ctx->sm_count * 8);
@@ -1707,7 +1886,7 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 			PG_CUDA(ctx, cudaMemsetAsync(dupflag_dev, 0, 16, s));
 			bool counted = false;
 			if (narrow) {
-				if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense32, range * 4))) { delete ht; return rc; }
+				if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense32, range * 4))) return rc;
 				PG_CUDA(ctx, cudaMemsetAsync(ht->dense32, 0xFF, range * 4, s));
 				if (vec16) {
 					// Plain stores; a duplicate key leaves fewer than |R| entries.
@@ -1723,8 +1902,8 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 				}
 			} else {
 				const uint64_t words = pg_div_up(range, 32);
-				if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense_val, range * 8))) { delete ht; return rc; }
-				if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense_bits, words * 4))) { delete ht; return rc; }
+				if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense_val, range * 8))) return rc;
+				if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense_bits, words * 4))) return rc;
 				PG_CUDA(ctx, cudaMemsetAsync(ht->dense_bits, 0, words * 4, s));
 				k_dense_build<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off,
 						R->key_bytes, ht->bcols, ht->inline_val, kmin, ht->dense_val, ht->dense_bits, dupflag_dev);
@@ -1736,9 +1915,9 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 			const bool dup = counted ? dh[1] != R->n : (dh[0] & 0xFFFFFFFFull) != 0;
 			if (!dup) {
 				ht->dense = true; ht->unique = true; ht->dmin = kmin; ht->drange = range; ht->vmin = h[2]; ht->vmax = h[3];
+				ht->vlo = h[2];
 				ht->slots = nullptr; ht->side = nullptr; ht->nside = 0; ht->log2cap = 1; ht->capacity = 0;
 				pg_free_async(ctx, s, mm);
-				*out = ht;
 				return PG_OK;
 			}
 			pg_free_async(ctx, s, ht->dense_val);
@@ -1753,8 +1932,8 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 	while ((1ull << lg) < want) ++lg;
 	ht->log2cap = lg; ht->capacity = 1ull << lg;
 	ht->side_cap = HJ_SIDE_CAP0;
-	if ((rc = pg_alloc_async(ctx, s, (void**) &ht->slots, ht->capacity * 16))) { delete ht; return rc; }
-	if ((rc = pg_alloc_async(ctx, s, (void**) &ht->side, ht->side_cap * 8 + 64))) { delete ht; return rc; }
+	if ((rc = pg_alloc_async(ctx, s, (void**) &ht->slots, ht->capacity * 16))) return rc;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &ht->side, ht->side_cap * 8 + 64))) return rc;
 	// side buffer tail: [side_count u32][flags i32]
 	unsigned int* side_count = reinterpret_cast<unsigned int*>(ht->side + ht->side_cap);
 	int* flags = reinterpret_cast<int*>(side_count + 1);
@@ -1770,17 +1949,138 @@ extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 		}
 		unsigned int hdr[2];
 		PG_CUDA(ctx, cudaMemcpyAsync(hdr, side_count, 8, cudaMemcpyDeviceToHost, s));
-		if ((rc = pg_check_status(ctx, s, "pg_hashjoin_build"))) { pg_hashtable_free(ctx, ht); return rc; }
+		if ((rc = pg_check_status(ctx, s, "pg_hashjoin_build"))) return rc;
 		ht->nside = hdr[0];
 		ht->unique = (hdr[1] & 1) == 0 && ht->nside <= 1;
 		if (!(hdr[1] & 2)) break;
 		// More empty-marker keys than the side list holds: grow it and rebuild.
 		pg_free_async(ctx, s, ht->side);
 		ht->side_cap = hdr[0];
-		if ((rc = pg_alloc_async(ctx, s, (void**) &ht->side, ht->side_cap * 8 + 64))) { delete ht; return rc; }
+		if ((rc = pg_alloc_async(ctx, s, (void**) &ht->side, ht->side_cap * 8 + 64))) return rc;
 		side_count = reinterpret_cast<unsigned int*>(ht->side + ht->side_cap);
 		flags = reinterpret_cast<int*>(side_count + 1);
 	}
+	return PG_OK;
+}
+
+
+// The narrow dense table of 16-byte tuples queued without host round trips
+// (sample, fill, store, count); the header's checks are read by the probe
+// kernels that take speculative tables, or by hj_settle.
+static int hj_build_spec(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, pg_hashtable* ht)
+{
+	int rc;
+	const uint64_t cap = 2 * R->n + R->n / 8 + 4096;       // window entries the allocation holds
+	ht->dense = true; ht->unique = true;
+	ht->slots = nullptr; ht->side = nullptr; ht->nside = 0; ht->log2cap = 1; ht->capacity = 0;
+	ht->dense_val = nullptr; ht->dense_bits = nullptr;
+	ht->hdr = nullptr; ht->dense32_base = nullptr; ht->dense32 = nullptr;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &ht->hdr, sizeof(HjDenseHdr)))) return rc;
+	if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense32_base, cap * 4))) return rc;
+	ht->dense32 = ht->dense32_base;
+	ht->dmin = 0; ht->drange = cap; ht->vmin = 0; ht->vlo = 0; ht->vmax = 0;     // bounds until settled
+	const uint32_t kw = R->key_off / 4;
+	k_dense_prep16<<<1, 1024, 0, s>>>((const uint4*) R->data, R->n, kw, ht->bcols, cap, ht->hdr);
+	PG_LAUNCHED(ctx);
+	const int fgrid = (int) std::min<uint64_t>(pg_div_up(cap / 4 + 1, 256), (uint64_t) ctx->sm_count * 8);
+	k_dense_fill16<<<fgrid, 256, 0, s>>>(ht->dense32_base, ht->hdr);
+	PG_LAUNCHED(ctx);
+	const int sgrid = (int) std::min<uint64_t>(pg_div_up(R->n, 4 * 256), (uint64_t) ctx->sm_count * 16);
+	k_dense32_spec16<<<sgrid, 256, 0, s>>>((const uint4*) R->data, R->n, kw, ht->bcols, ht->dense32_base, ht->hdr);
+	PG_LAUNCHED(ctx);
+	k_dense32_count_spec<<<fgrid, 256, 0, s>>>(ht->dense32_base, ht->hdr);
+	PG_LAUNCHED(ctx);
+	// Probes on other streams wait for these kernels (the build returns
+	// without synchronising).
+	PG_CUDA(ctx, cudaEventCreateWithFlags(&ht->built, cudaEventDisableTiming));
+	PG_CUDA(ctx, cudaEventRecord(ht->built, s));
+	ht->spec.store(true, std::memory_order_release);
+	return PG_OK;
+}
+
+static bool hj_hdr_ok(const HjDenseHdr& h)
+{
+	return h.flags == 0 && h.present == h.n;
+}
+
+int hj_settle(pg_ctx* ctx, pg_hashtable* ht)
+{
+	if (!ht || !ht->spec.load(std::memory_order_acquire)) return PG_OK;
+	std::lock_guard<std::mutex> g(ht->mu);
+	if (!ht->spec.load(std::memory_order_relaxed)) return PG_OK;
+	cudaStream_t s = ht->stream;
+	HjDenseHdr h;
+	PG_CUDA(ctx, cudaMemcpyAsync(&h, ht->hdr, sizeof h, cudaMemcpyDeviceToHost, s));
+	PG_CUDA(ctx, cudaStreamSynchronize(s));
+	if (hj_hdr_ok(h)) {
+		// Exact layout, as hj_build_exact would have made it: the window
+		// narrowed to the keys present, entries based on the smallest value.
+		const long long kmin = (long long) (h.kmin ^ (1ull << 63)), kmax = (long long) (h.kmax ^ (1ull << 63));
+		const unsigned long long off = (unsigned long long) kmin - (unsigned long long) h.dmin;
+		uint32_t* win = ht->dense32_base + off;
+		const unsigned long long range = (unsigned long long) kmax - (unsigned long long) kmin + 1;
+		// A copy too when the narrowed window would not start on a 16-byte
+		// boundary: table readers (the image checksum's 8-byte words, vector
+		// loads) rely on the alignment of an allocation.
+		if (h.vlo != h.vmin || (off & 3) != 0) {
+			int rc;
+			if ((rc = pg_alloc_async(ctx, s, (void**) &ht->dense32_copy, range * 4))) return rc;
+			const int grid = (int) std::min<uint64_t>(pg_div_up(range, 256), (uint64_t) ctx->sm_count * 8);
+			k_dense32_rebase<<<grid, 256, 0, s>>>(win, ht->dense32_copy, range, (uint32_t) (h.vlo - h.vmin));
+			PG_LAUNCHED(ctx);
+			PG_CUDA(ctx, cudaStreamSynchronize(s));      // users on other streams read the copy next
+			win = ht->dense32_copy;
+		}
+		ht->dense32 = win;
+		ht->dmin = kmin;
+		ht->drange = range;
+		ht->vmin = h.vlo; ht->vlo = h.vlo; ht->vmax = h.vhi;
+		ht->spec.store(false, std::memory_order_release);
+		return PG_OK;
+	}
+	// Refuted (a repeated key, a key or value the sample missed): rebuild
+	// from the build relation with the exact ranges. Probes queued with the
+	// header see it refuted and touch no entry, so the window can go.
+	pg_free_async(ctx, s, ht->dense32_base);
+	ht->dense32_base = nullptr; ht->dense32 = nullptr;
+	int rc = hj_build_exact(ctx, s, &ht->rel, ht);
+	ht->spec.store(false, std::memory_order_release);
+	return rc;
+}
+
+extern "C" int pg_hashjoin_build(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
+		const pg_col* proj, int nproj, pg_hashtable** out)
+{
+	if (!ctx || !out) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_build: null argument");
+	int rc;
+	if ((rc = hj_validate_rel(ctx, R, "pg_hashjoin_build"))) return rc;
+	if ((rc = hj_validate_proj(ctx, proj, nproj, R->width, 1u << 30))) return rc;
+	cudaStream_t s = (cudaStream_t) stream;
+	pg_hashtable* ht = new pg_hashtable();
+	ht->nbuild = R->n; ht->R = (const char*) R->data; ht->wR = R->width; ht->bkey_bytes = R->key_bytes;
+	ht->nproj = nproj;
+	ht->stream = s;
+	for (int i = 0; i < nproj; ++i) ht->proj[i] = proj[i];
+	uint32_t bbytes = 0;
+	ht->bcols.n = 0;
+	for (int i = 0; i < nproj; ++i)
+		if (proj[i].side == 0) {
+			ht->bcols.roff[ht->bcols.n] = (uint16_t) (proj[i].off / 4);
+			ht->bcols.words[ht->bcols.n] = (uint8_t) (proj[i].bytes / 4);
+			ht->bcols.n++;
+			bbytes += proj[i].bytes;
+		}
+	ht->inline_val = bbytes <= 8;
+	ht->rel = *R;
+	ht->spec.store(false); ht->hdr = nullptr; ht->dense32_base = nullptr; ht->dense32_copy = nullptr;
+	ht->built = nullptr;
+	const int64_t spec = ctx->tune[PG_TUNE_BUILD_SPEC];
+	if (R->n && ht->inline_val && ctx->tune[PG_TUNE_DENSE] != 2 && spec != 2 && hj_vec16(R, ht->bcols) &&
+			(spec == 1 || R->n >= HJ_SPEC_MIN_TUPLES))
+		rc = hj_build_spec(ctx, s, R, ht);
+	else
+		rc = hj_build_exact(ctx, s, R, ht);
+	if (rc) { pg_hashtable_free(ctx, ht); return rc; }
 	*out = ht;
 	return PG_OK;
 }
@@ -1795,7 +2095,14 @@ extern "C" int pg_hashtable_free(pg_ctx* ctx, pg_hashtable* ht)
 	pg_free_async(ctx, ht->stream, ht->side);
 	pg_free_async(ctx, ht->stream, ht->dense_val);
 	pg_free_async(ctx, ht->stream, ht->dense_bits);
-	pg_free_async(ctx, ht->stream, ht->dense32);
+	if (ht->dense32_base || ht->dense32_copy) {
+		pg_free_async(ctx, ht->stream, ht->dense32_base);
+		pg_free_async(ctx, ht->stream, ht->dense32_copy);
+	} else {
+		pg_free_async(ctx, ht->stream, ht->dense32);
+	}
+	pg_free_async(ctx, ht->stream, ht->hdr);
+	if (ht->built) cudaEventDestroy(ht->built);
 	delete ht;
 	return PG_OK;
 }
@@ -1819,6 +2126,12 @@ static int hj_make_cols(pg_ctx* ctx, const pg_hashtable* ht, const pg_col* proj,
 	pc->ow_words = ow;
 	return PG_OK;
 }
+
+// Internal results of the probe launch on a speculative table (never returned
+// through the C ABI): the chosen kernel needs the settled table, or the
+// build's checks failed and the probe wrote nothing.
+#define HJ_NEED_SETTLE 1001
+#define HJ_SPEC_REFUTED 1002
 
 #define HJ_TWO_PASS_MIN_BYTES (56ull << 20)   // dense tables above this probe in two passes
 #define HJ_TWO_PASS_MAX_BYTES (112ull << 20)  // ... up to this (half must fit in L2)
@@ -1855,11 +2168,20 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 	if (positional) *positional = false;
 	const uint64_t ntiles = pg_div_up(n, HJ_TILE);
 	HjProbeTable tb;
-	tb.slots = ht->slots; tb.log2cap = ht->log2cap; tb.side = ht->side; tb.nside = ht->nside;
-	tb.dense_val = ht->dense_val; tb.dense_bits = ht->dense_bits; tb.dmin = ht->dmin; tb.drange = ht->drange;
-	tb.dense32 = ht->dense32; tb.vmin = ht->vmin;
+	// A speculative table is described by its header and window base alone
+	// (read once: another thread may settle it meanwhile).
+	const bool spec = ht->spec.load(std::memory_order_acquire);
+	if (spec) {
+		tb = HjProbeTable();
+		tb.hdr = ht->hdr; tb.dense32 = ht->dense32_base;
+	} else {
+		tb.slots = ht->slots; tb.log2cap = ht->log2cap; tb.side = ht->side; tb.nside = ht->nside;
+		tb.dense_val = ht->dense_val; tb.dense_bits = ht->dense_bits; tb.dmin = ht->dmin; tb.drange = ht->drange;
+		tb.dense32 = ht->dense32; tb.vmin = ht->vmin;
+		tb.hdr = nullptr;
+	}
 	tb.cache = (uint32_t) (ctx->tune[PG_TUNE_PROBE_CACHE] & 15);
-	const int mode = ht->dense ? (ht->dense32 ? 2 : 1) : 0;
+	const int mode = spec ? 2 : ht->dense ? (ht->dense32 ? 2 : 1) : 0;
 	const bool fast16 = W == 16 && (koff == 0 || koff == 8) && kbytes == 8 && pc.ow_words == 4 &&
 		(reinterpret_cast<uintptr_t>(S) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
 	if (pred && !fast16)
@@ -1901,6 +2223,9 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 			const int passes = mode == 0 || pk == 1 ? 1
 				: (pk == 2 || (!direct && tbytes > HJ_TWO_PASS_MIN_BYTES && tbytes <= HJ_TWO_PASS_MAX_BYTES)) ? 2 : 1;
 			const uint64_t dr = mode == 0 ? 0 : ht->drange;
+			// Only the register-loading dense kernels read a speculative
+			// table's window from its header.
+			if (spec && (!direct || pred || passes != 1)) return HJ_NEED_SETTLE;
 			for (int pass = 0; pass < passes; ++pass) {
 				const int run = passes == 1 ? -1 : pass;
 				const uint64_t dlo = passes == 1 ? 0 : (pass == 0 ? 0 : dr / 2);
@@ -1988,6 +2313,7 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 			if (positional) *positional = materialize;
 			return PG_OK;
 		}
+		if (spec) return HJ_NEED_SETTLE;
 		const int grid = (int) std::min<uint64_t>(pg_div_up(n, HJT_TILE), (uint64_t) ctx->sm_count * 3);
 #define HJT_LAUNCH(M, D) do { \
 			PG_CUDA(ctx, cudaFuncSetAttribute(k_probe16_tma<M, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
@@ -2005,6 +2331,7 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 	// words per thread (0.44 against 0.51 ms staged on 64M 24-byte tuples), and
 	// so do hashed tables, whose pending bucket loads cost the staged kernel
 	// registers (2.34 against 2.40 ms).
+	if (spec) return HJ_NEED_SETTLE;
 	const int64_t wide = ctx->tune[PG_TUNE_PROBE_WIDE];
 	const bool staged = wide == 2 || wide == 3 || (wide == 0 && materialize && mode != 0);
 	if (staged && W % 4 == 0 && W <= HJG_MAX_W && koff % 4 == 0 && pc.ow_words >= 1 &&
@@ -2063,7 +2390,7 @@ static int hj_compact(pg_ctx* ctx, cudaStream_t s, char* out, uint64_t n, uint64
 
 // pg_hashjoin_probe; with `pred`, the probe tuples failing it take no part
 // (only for the dense 16-byte layouts the register-loading kernels handle).
-static int hj_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
+static int hj_probe_run(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 		const pg_rel* S, const pg_col* proj, int nproj,
 		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res, const PgPred16* pred)
 {
@@ -2088,14 +2415,28 @@ static int hj_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 
 	if (ht->unique && ht->inline_val) {
 		const char* Sd = (const char*) S->data;
+		// A speculative table's checks come back with the counts; when they
+		// failed, the kernels wrote nothing and the caller rebuilds.
+		HjDenseHdr hh;
+		const bool spec = ht->spec.load(std::memory_order_acquire);
+		auto refuted = [&]() { return spec && !hj_hdr_ok(hh); };
+		if (spec) PG_CUDA(ctx, cudaStreamWaitEvent(s, ht->built, 0));
 		if (materialize) {
 			uint64_t* counts = nullptr;
 			bool positional = false;
 			if ((rc = pg_alloc_async(ctx, s, (void**) &counts, pg_div_up(S->n, PW_CHUNK) * 8))) return rc;
 			if ((rc = hj_launch_unique(ctx, s, ht, Sd, S->n, S->width, S->key_off, S->key_bytes, pc,
-					(char*) out, out_capacity, acc, true, -1, counts, &positional, pred))) return rc;
+					(char*) out, out_capacity, acc, true, -1, counts, &positional, pred))) {
+				pg_free_async(ctx, s, counts); pg_free_async(ctx, s, acc);
+				return rc;
+			}
 			PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
+			if (spec) PG_CUDA(ctx, cudaMemcpyAsync(&hh, ht->hdr, sizeof hh, cudaMemcpyDeviceToHost, s));
 			if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
+			if (refuted()) {
+				pg_free_async(ctx, s, counts); pg_free_async(ctx, s, acc);
+				return HJ_SPEC_REFUTED;
+			}
 			res->n_out = host_acc[0];
 			if (positional && res->n_out < S->n) {
 				if ((rc = hj_compact(ctx, s, (char*) out, S->n, counts, res->n_out))) return rc;
@@ -2112,9 +2453,17 @@ static int hj_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 			}
 		} else {
 			if ((rc = hj_launch_unique(ctx, s, ht, Sd, S->n, S->width, S->key_off, S->key_bytes, pc,
-					nullptr, 0, acc, false, sum_col, nullptr, nullptr, pred))) return rc;
+					nullptr, 0, acc, false, sum_col, nullptr, nullptr, pred))) {
+				pg_free_async(ctx, s, acc);
+				return rc;
+			}
 			PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
+			if (spec) PG_CUDA(ctx, cudaMemcpyAsync(&hh, ht->hdr, sizeof hh, cudaMemcpyDeviceToHost, s));
 			if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
+			if (refuted()) {
+				pg_free_async(ctx, s, acc);
+				return HJ_SPEC_REFUTED;
+			}
 			res->n_out = host_acc[1];
 			res->sum = (int64_t) host_acc[2];
 		}
@@ -2154,6 +2503,18 @@ static int hj_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 	return PG_OK;
 }
 
+// pg_hashjoin_probe; a speculative table is settled (and possibly rebuilt)
+// when the probe's kernel cannot take it or its checks failed.
+static int hj_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
+		const pg_rel* S, const pg_col* proj, int nproj,
+		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res, const PgPred16* pred)
+{
+	int rc = hj_probe_run(ctx, stream, ht, S, proj, nproj, out, out_capacity, flags, sum_col, res, pred);
+	if (rc != HJ_NEED_SETTLE && rc != HJ_SPEC_REFUTED) return rc;
+	if ((rc = hj_settle(ctx, ht))) return rc;
+	return hj_probe_run(ctx, stream, ht, S, proj, nproj, out, out_capacity, flags, sum_col, res, pred);
+}
+
 extern "C" int pg_hashjoin_probe(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 		const pg_rel* S, const pg_col* proj, int nproj,
 		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res)
@@ -2169,6 +2530,7 @@ extern "C" int pg_hashjoin_probe_where(pg_ctx* ctx, pg_stream stream, pg_hashtab
 	if (npred == 0)
 		return hj_probe(ctx, stream, ht, S, proj, nproj, out, out_capacity, flags, sum_col, res, nullptr);
 	int rc;
+	if ((rc = hj_settle(ctx, ht))) return rc;
 	PgPredSet P;
 	bool has_char = false;
 	if ((rc = pg_pred_prepare(ctx, preds, npred, S->width, &P, &has_char))) return rc;
@@ -2212,6 +2574,7 @@ extern "C" int pg_hashjoin_probe_spans(pg_ctx* ctx, pg_stream stream, pg_hashtab
 {
 	if (!ctx || !ht || !res || (nspans > 0 && !spans) || nspans < 0)
 		return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe_spans: null argument");
+	if (int rs = hj_settle(ctx, ht)) return rs;
 	if (!ht->unique || !ht->inline_val)
 		return pg_fail(ctx, PG_ERR_UNSUPPORTED, "pg_hashjoin_probe_spans: the table has repeated keys");
 	res->n_out = 0; res->sum = 0;
@@ -2308,6 +2671,7 @@ extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
 	HJH_TRY(cudaMemcpyAsync(dR, Rh->data, nR * Rh->width, cudaMemcpyHostToDevice, scomp));
 	pg_rel R = *Rh; R.data = dR;
 	if ((rc = pg_hashjoin_build(ctx, scomp, &R, proj, nproj, &ht))) { cleanup(); return rc; }
+	if ((rc = hj_settle(ctx, ht))) { cleanup(); return rc; }
 	HjCols pc;
 	if ((rc = hj_make_cols(ctx, ht, proj, nproj, &pc))) { cleanup(); return rc; }
 	if (!(flags & PG_JOIN_SUM)) sum_col = -1;
@@ -2412,7 +2776,7 @@ extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
 template <int VT, int AGG>
 __global__ void __launch_bounds__(PW_WARPS * 32, 4)
 k_probe16_groupby(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb, uint32_t voff,
-		unsigned long long* __restrict__ acc, double* __restrict__ lo, unsigned char* __restrict__ present)
+		uint32_t goff, unsigned long long* __restrict__ acc, double* __restrict__ lo, unsigned char* __restrict__ present)
 {
 	constexpr int ITEMS = PW_CHUNK / 32;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -2445,6 +2809,7 @@ k_probe16_groupby(const char* __restrict__ S, uint64_t n, uint32_t koff, const H
 			if (j * 32 + lane < rows && d < tb.drange)
 				asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;"
 						: "=r"(e[j]) : "l"(tb.dense32 + d), "l"(keep));
+			if (e[j] != 0xFFFFFFFFu) e[j] -= goff;      // group slot: value - smallest value
 		}
 		if (AGG == PG_AGG_SUM && VT == PG_VAL_DEC) {
 			double v[ITEMS], old[ITEMS];
@@ -2491,7 +2856,8 @@ extern "C" int pg_hashjoin_groupby(pg_ctx* ctx, pg_stream stream, pg_hashtable* 
 			val_off + (val_type == PG_VAL_INT ? 4 : 8) > S->width))
 		return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_groupby: bad value column");
 	*ngroups = 0;
-	const uint64_t vrange = ht->dense32 ? ht->vmax - ht->vmin + 1 : 0;
+	if ((rc = hj_settle(ctx, ht))) return rc;
+	const uint64_t vrange = ht->dense32 ? ht->vmax - ht->vlo + 1 : 0;
 	uint32_t gbytes = 0;
 	for (int c = 0; c < ht->bcols.n; ++c) gbytes += 4 * ht->bcols.words[c];
 	if (!ht->dense32 || ht->bcols.n != 1 || (gbytes != 4 && gbytes != 8) || vrange == 0 ||
@@ -2520,7 +2886,7 @@ extern "C" int pg_hashjoin_groupby(pg_ctx* ctx, pg_stream stream, pg_hashtable* 
 		tb.dense32 = ht->dense32; tb.vmin = ht->vmin; tb.dmin = ht->dmin; tb.drange = ht->drange;
 		const int grid = (int) std::min<uint64_t>(pg_div_up(pg_div_up(S->n, PW_CHUNK), PW_WARPS), (uint64_t) ctx->sm_count * 24);
 #define PG_LAUNCH(VT, AGG) k_probe16_groupby<VT, AGG><<<grid, PW_WARPS * 32, 0, s>>>((const char*) S->data, S->n, \
-				S->key_off, tb, val_off, acc, lo, present)
+				S->key_off, tb, val_off, (uint32_t) (ht->vlo - ht->vmin), acc, lo, present)
 		if (agg == PG_AGG_COUNT) PG_LAUNCH(PG_VAL_LONG, PG_AGG_COUNT);
 		else if (val_type == PG_VAL_INT) PG_LAUNCH(PG_VAL_INT, PG_AGG_SUM);
 		else if (val_type == PG_VAL_LONG) PG_LAUNCH(PG_VAL_LONG, PG_AGG_SUM);
@@ -2528,7 +2894,7 @@ extern "C" int pg_hashjoin_groupby(pg_ctx* ctx, pg_stream stream, pg_hashtable* 
 #undef PG_LAUNCH
 		PG_LAUNCHED(ctx);
 	}
-	if ((rc = pg_dense_groups_emit(ctx, s, acc, lo, present, vrange, (long long) ht->vmin, gbytes, val_type, agg,
+	if ((rc = pg_dense_groups_emit(ctx, s, acc, lo, present, vrange, (long long) ht->vlo, gbytes, val_type, agg,
 			out, out_capacity, cursor))) return rc;
 	unsigned long long ng = 0;
 	PG_CUDA(ctx, cudaMemcpyAsync(&ng, cursor, 8, cudaMemcpyDeviceToHost, s));

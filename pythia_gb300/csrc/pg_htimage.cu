@@ -120,6 +120,9 @@ static void img_layout(ImgHeader& h)
 
 static int table_header(pg_ctx* ctx, const pg_hashtable* ht, ImgHeader& h)
 {
+	// An image describes the exact layout: a table still checked on the
+	// device is settled first (the table is logically unchanged).
+	if (int rc = hj_settle(ctx, const_cast<pg_hashtable*>(ht))) return rc;
 	if (!ht->inline_val)
 		return pg_fail(ctx, PG_ERR_UNSUPPORTED,
 				"table image: the table stores build row indices (build columns wider than 8 bytes)");
@@ -191,6 +194,9 @@ extern "C" int pg_hashtable_serialize(pg_ctx* ctx, pg_stream stream, const pg_ha
 	PG_CUDA(ctx, cudaMemsetAsync(acc, 0, 8, s));
 	char* img = (char*) image;
 	uint64_t prev_end = IMG_HEADER;
+	for (int i = 0; i < IMG_SECTIONS; ++i)
+		if (h.sec_bytes[i] && (reinterpret_cast<uintptr_t>(table_section(ht, i)) & 15))
+			return pg_fail(ctx, PG_ERR_ARG, "pg_hashtable_serialize: table array not 16-byte aligned");
 	for (int i = 0; i < IMG_SECTIONS; ++i) {
 		if (!h.sec_bytes[i]) continue;
 		memset(img + prev_end, 0, h.sec_off[i] - prev_end);
@@ -271,7 +277,7 @@ extern "C" int pg_hashtable_deserialize(pg_ctx* ctx, pg_stream stream, const voi
 	ht->inline_val = true;
 	ht->unique = (h.flags & 1) != 0;
 	ht->dense = h.layout != IMG_HASHED;
-	ht->dmin = h.dmin; ht->drange = h.drange; ht->vmin = h.vmin; ht->vmax = h.vmax;
+	ht->dmin = h.dmin; ht->drange = h.drange; ht->vmin = h.vmin; ht->vmax = h.vmax; ht->vlo = h.vmin;
 	ht->log2cap = ht->dense ? 1 : h.log2cap;
 	ht->capacity = ht->dense ? 0 : 1ull << h.log2cap;
 	ht->nside = h.nside;

@@ -151,7 +151,7 @@ __device__ __forceinline__ uint64_t pg_mix64(uint64_t k)
 // clears with one memset). A real key equal to it takes a separate path.
 #define PG_EMPTY_KEY ((long long) -1)
 
-// Bounded spin budget for device-side waits.
+// Bounded spin budget for device-side waits (try_wait polls).
 #define PG_SPIN_LIMIT (1u << 26)
 
 __device__ __forceinline__ void pg_set_status(int* status, int code)
@@ -213,6 +213,42 @@ __device__ __forceinline__ bool pg_mbar_wait(uint64_t* bar, uint32_t parity)
 		if (done) return true;
 	}
 	return false;
+}
+
+// Non-blocking test of phase `parity` of `bar`.
+__device__ __forceinline__ bool pg_mbar_test(uint64_t* bar, uint32_t parity)
+{
+	uint32_t done;
+	asm volatile("{\n\t.reg .pred p;\n\t"
+			"mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+			"selp.u32 %0, 1, 0, p;\n\t}"
+			: "=r"(done) : "r"(pg_smem_addr(bar)), "r"(parity) : "memory");
+	return done != 0;
+}
+
+// The context's bounded-wait knob (PG_TUNE_SPIN_LIMIT), kept in word 1 of its
+// device status block: 0 = the built-in limit. Kernels read it once.
+__device__ __forceinline__ uint32_t pg_spin_knob(const int* status)
+{
+	return *reinterpret_cast<const volatile uint32_t*>(status + 1);
+}
+
+// Wait for a bulk copy's phase with the context's limit: `spin` = 0 polls with
+// try_wait up to PG_SPIN_LIMIT times, else `spin` non-blocking tests. When the
+// limit runs out the status word records PG_ERR_TIMEOUT and the wait goes on,
+// bounded by PG_SPIN_LIMIT, until the copy has landed, so that no copy into
+// shared memory outlives its wait (a buffer reused or a block exited with the
+// copy in flight). False only when that drain also gave up.
+__device__ __forceinline__ bool pg_mbar_wait_timed(uint64_t* bar, uint32_t parity, uint32_t spin, int* status)
+{
+	if (spin == 0) {
+		if (pg_mbar_wait(bar, parity)) return true;
+	} else {
+		for (uint32_t i = 0; i < spin; ++i)
+			if (pg_mbar_test(bar, parity)) return true;
+	}
+	pg_set_status(status, PG_ERR_TIMEOUT);
+	return pg_mbar_wait(bar, parity);
 }
 
 // L2 cache policies (createpolicy): streams are evict-first so that the

@@ -13,11 +13,16 @@
 // Limits and sharing:
 //   * at most PG_NOALLOC_MAX_BUILD (524,288) build tuples; larger build sides
 //     are rejected with PG_ERR_ARG. The array is 16 MiB of table plus a small
-//     tail, and every GPU that loads this library holds it until the process
-//     exits.
-//   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress, with that device current). Make that first call
-//     before any stream capture begins.
+//     tail.
+//   * the first call on each device in a process sets up: with the device
+//     current it loads this file's device code (the array and both kernels:
+//     CUDA loads modules lazily, on first use) and looks up the array's device
+//     address (cudaGetSymbolAddress). That first call can allocate device
+//     memory; make it, with empty inputs if need be, before a pool reserves
+//     the device's memory. Later calls allocate nothing, and the array stays
+//     placed until the process exits.
+//   * the call is synchronous (it reads the result back before returning), so
+//     it must not be made while any stream is being captured.
 //   * every call reuses the same array and clears it at the start; calls
 //     whose work overlaps on the GPU (different streams, or different host
 //     threads without ordering) race on it and must be serialised by the
@@ -33,29 +38,6 @@
 
 // Layout: [slots: 2 words each][side list][count, sum, side count, flags, ...]
 static __device__ __align__(256) unsigned long long g_noalloc_scratch[PG_NOALLOC_WORDS];
-
-static std::mutex g_noalloc_mu;
-static unsigned long long* g_noalloc_addr[256];
-
-// Device address of g_noalloc_scratch on `device` (looked up once, with the
-// device current).
-static int noalloc_scratch(pg_ctx* ctx, unsigned long long** out)
-{
-	if (ctx->device < 0 || ctx->device >= 256) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_agg_noalloc: bad device");
-	std::lock_guard<std::mutex> g(g_noalloc_mu);
-	if (!g_noalloc_addr[ctx->device]) {
-		int cur = -1;
-		cudaGetDevice(&cur);
-		cudaError_t e = cudaSetDevice(ctx->device);
-		void* p = nullptr;
-		if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-		if (cur >= 0 && cur != ctx->device) cudaSetDevice(cur);
-		if (e != cudaSuccess) return pg_cuda_fail(ctx, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-		g_noalloc_addr[ctx->device] = static_cast<unsigned long long*>(p);
-	}
-	*out = g_noalloc_addr[ctx->device];
-	return PG_OK;
-}
 
 struct NaCols {             // packed build value and the summed output column
 	int nb;
@@ -158,6 +140,46 @@ __global__ void k_na_probe(const char* __restrict__ S, uint64_t n, uint32_t W, u
 	if ((threadIdx.x & 31) == 0) { atomicAdd(&tail[0], cnt); atomicAdd(&tail[1], sum); }
 }
 
+static std::mutex g_noalloc_mu;
+static unsigned long long* g_noalloc_addr[256];
+
+// Makes ctx->device current for one call and restores the caller's device.
+struct NaDevice {
+	int prev = -1;
+	cudaError_t err = cudaSuccess;
+	explicit NaDevice(int dev)
+	{
+		cudaGetDevice(&prev);
+		if (prev != dev) err = cudaSetDevice(dev);
+	}
+	~NaDevice() { if (prev >= 0) cudaSetDevice(prev); }
+};
+
+// Device address of g_noalloc_scratch on the current device (ctx->device).
+// The first time per device: both kernels are launched once with nothing to
+// do, so that their code and the array are loaded now, then the array's
+// address is looked up.
+static int noalloc_scratch(pg_ctx* ctx, cudaStream_t s, unsigned long long** out)
+{
+	if (ctx->device < 0 || ctx->device >= 256) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_agg_noalloc: bad device");
+	std::lock_guard<std::mutex> g(g_noalloc_mu);
+	if (!g_noalloc_addr[ctx->device]) {
+		void* p = nullptr;
+		cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+		if (e != cudaSuccess) return pg_cuda_fail(ctx, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+		unsigned long long* a = static_cast<unsigned long long*>(p);
+		NaCols nc = {};
+		nc.sum_side = -1;
+		k_na_build<<<1, 32, 0, s>>>(nullptr, 0, 16, 0, 8, nc, a);
+		k_na_probe<<<1, 32, 0, s>>>(nullptr, 0, 16, 0, 8, nc, a);
+		if ((e = cudaGetLastError()) != cudaSuccess) return pg_cuda_fail(ctx, e, "pg_hashjoin_agg_noalloc set-up");
+		if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return pg_cuda_fail(ctx, e, "pg_hashjoin_agg_noalloc set-up");
+		g_noalloc_addr[ctx->device] = a;
+	}
+	*out = g_noalloc_addr[ctx->device];
+	return PG_OK;
+}
+
 extern "C" int pg_hashjoin_agg_noalloc(pg_ctx* ctx, pg_stream stream, const pg_rel* R,
 		const pg_rel* S, const pg_col* proj, int nproj, int sum_col, pg_join_result* res)
 {
@@ -190,10 +212,12 @@ extern "C" int pg_hashjoin_agg_noalloc(pg_ctx* ctx, pg_stream stream, const pg_r
 	}
 	if (bwords > 2)
 		return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_agg_noalloc: build-side columns limited to 8 bytes in total");
+	NaDevice dev(ctx->device);
+	if (dev.err != cudaSuccess) return pg_cuda_fail(ctx, dev.err, "pg_hashjoin_agg_noalloc: cudaSetDevice");
+	cudaStream_t s = (cudaStream_t) stream;
 	unsigned long long* scratch = nullptr;
 	int rc;
-	if ((rc = noalloc_scratch(ctx, &scratch))) return rc;
-	cudaStream_t s = (cudaStream_t) stream;
+	if ((rc = noalloc_scratch(ctx, s, &scratch))) return rc;
 	unsigned long long* tail = scratch + 2ull * PG_NOALLOC_SLOTS + PG_NOALLOC_SIDE;
 	// The array keeps the previous call's contents: clear the table and the tail.
 	PG_CUDA(ctx, cudaMemsetAsync(scratch, 0xFF, 2ull * PG_NOALLOC_SLOTS * 8, s));

@@ -119,13 +119,14 @@ k_part_scatter(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t kof
 		return false;
 	};
 	uint32_t phase[2] = {0, 0};
+	const uint32_t spin = pg_spin_knob(status);
 	bool bulk_pending = issue(first);
 
 	for (uint64_t t = first; t < last; ++t) {
 		const uint32_t rows = tile_rows(t);
 		unsigned char* cur = (t & 1) ? buf1 : buf0;
 		if (bulk_pending) {
-			if (!pg_mbar_wait(&bar[t & 1], phase[t & 1])) { pg_set_status(status, PG_ERR_TIMEOUT); return; }
+			if (!pg_mbar_wait_timed(&bar[t & 1], phase[t & 1], spin, status)) return;
 			phase[t & 1] ^= 1;
 		} else {
 			part_copy_words(reinterpret_cast<uint32_t*>(cur),

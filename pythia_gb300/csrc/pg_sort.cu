@@ -51,7 +51,9 @@ k_tile_sort(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, 
 				pg_bulk_g2s(rec, in + base * 16, bytes, &bar);
 			}
 			__syncthreads();
-			if (!pg_mbar_wait(&bar, 0)) { pg_set_status(status, PG_ERR_TIMEOUT); return; }
+			// A wait past the context's limit records PG_ERR_TIMEOUT and then
+			// drains the copy; only a copy that never lands ends the block.
+			if (!pg_mbar_wait_timed(&bar, 0, pg_spin_knob(status), status)) return;
 		} else {
 			const uint4* src = reinterpret_cast<const uint4*>(in + base * 16);
 			for (uint32_t i = tid; i < rows; i += blockDim.x) reinterpret_cast<uint4*>(rec)[i] = src[i];

@@ -183,6 +183,80 @@ def test_join_dense_keys_with_repeated_rows(ctx):
     _join_check(ctx, R, S)
 
 
+def _spec_cases():
+    """Build sides for the device-only dense build: ones it keeps and ones
+    its checks refute (rebuilt exactly at the table's first use)."""
+    R = dg.build_relation(100_000, dg.seed_for(41))
+    cases = {"dense": R}
+    d = np.concatenate([R, R[:2]])                       # a repeated row: fewer entries than tuples
+    cases["repeated_row"] = d
+    o = R.copy(); o[12_345, 0] = 5_000_000_000           # one key far outside the sampled window
+    cases["key_outlier"] = o
+    v = R.copy(); v[:, 1] %= 1000; v[777, 1] = 1 << 40   # one value outside the 32-bit entry range
+    cases["value_outlier"] = v
+    w = R.copy(); w[:, 1] = dg.raw_words(dg.seed_for(41), 1, R.shape[0]).view(np.int64)   # 64-bit values
+    cases["wide_values"] = w
+    n = R.copy(); n[:, 1] = -n[:, 1] - 1; n[:, 0] -= 200_000   # negative keys and values
+    cases["negative"] = n
+    h = R.copy(); h[:, 1] = 7_000_000_000 + (h[:, 1] % 100_000)   # values far from 0 (base not 0)
+    cases["high_values"] = h
+    z = R.copy(); z[:, 1] %= 1000                        # values from 0: the sample's base is the smallest value
+    cases["zero_based_values"] = z
+    return cases
+
+
+@pytest.mark.parametrize("spec", [1, 2])
+@pytest.mark.parametrize("case", sorted(_spec_cases()))
+def test_join_dense_build_on_device(ctx, spec, case):
+    # The dense build that takes its key window and value base from a sample
+    # (build_spec=1 forces it at every size, 2 is the host-checked build) must
+    # give the same rows, counts and sums whether the sample's layout holds or
+    # the table is rebuilt at its first use.
+    R = _spec_cases()[case]
+    S = dg.probe_uniform(300_000, R[:100_000], dg.seed_for(42))
+    S[::101, 0] += 3_000_000                              # misses outside every window
+    try:
+        ctx.tune(build_spec=spec)
+        _join_check(ctx, R, S)
+        _join_check(ctx, R, S, proj=(("B", 8, 8), ("P", 8, 8)))      # a projection the fast kernels do not take
+        small = R[:5000].copy()
+        _join_check(ctx, small, S[:20_000])
+    finally:
+        ctx.tune(build_spec=0)
+
+
+@pytest.mark.parametrize("case", ["dense", "high_values", "negative", "zero_based_values"])
+def test_dense_build_on_device_settles_to_the_exact_table(ctx, case):
+    # A table built on the device and then used by a path that needs its
+    # exact layout (an image here) is the table the host-checked build makes,
+    # byte for byte; so is the one-pass join + group-by on it.
+    R = _spec_cases()[case]
+    images = []
+    for spec in (1, 2):
+        ctx.tune(build_spec=spec)
+        try:
+            t = ctx.build_table(R)
+            try:
+                images.append(t.serialize())
+            finally:
+                t.free()
+        finally:
+            ctx.tune(build_spec=0)
+    assert np.array_equal(images[0], images[1])
+    G = R.copy()
+    G[:, 1] = (G[:, 1] % 997) + 5000                      # group column with its smallest value far from 0
+    S = dg.probe_uniform(200_000, G, dg.seed_for(43))
+    S[:, 1] = (S[:, 1] % 1000)
+    outs = []
+    for spec in (1, 2):
+        ctx.tune(build_spec=spec)
+        try:
+            outs.append(canon(ctx.hashjoin_groupby(G, S, group=(8, 8), val=(8, "long"))))
+        finally:
+            ctx.tune(build_spec=0)
+    assert np.array_equal(outs[0], outs[1])
+
+
 def test_join_many_to_many(ctx):
     R = dg.uniform_keys(5000, 700, dg.seed_for(5))
     S = dg.uniform_keys(9000, 900, dg.seed_for(6))
@@ -842,3 +916,46 @@ def test_h2d_by_sm_loads_any_alignment(ctx):
                         assert (got[:do] == 0xA5).all() and (got[do + n:] == 0xA5).all(), (so, do, n)
     finally:
         ctx._check(L.pg_host_unregister(ctx.h, reg.ctypes.data))
+
+
+# ---------------------------------------------------------------- bounded waits
+PG_ERR_TIMEOUT = 4
+
+
+@pytest.mark.parametrize("op", ["sort", "partition", "staged_probe"])
+def test_bounded_wait_gives_up_and_the_next_call_succeeds(ctx, op):
+    # Kernels that stage input through bulk copies wait on an mbarrier for
+    # each copy. With the context's wait limit at one non-blocking poll the
+    # first wait gives up before its copy lands: the call must fail with
+    # PG_ERR_TIMEOUT (the kernel still waits for the copy before its block
+    # ends), and the next call with the built-in limit must be right.
+    rows = dg.uniform_keys(1 << 20, 1 << 40, dg.seed_for(70))   # key span over 2^32: bitonic tiles
+    R = dg.build_relation(70_000, dg.seed_for(71))
+    S = dg.probe_uniform(500_000, R, dg.seed_for(72))
+
+    def run():
+        if op == "sort":
+            return ctx.sort(rows)
+        if op == "partition":
+            return ctx.partition(rows, gpu.hashcfg("parammodulo", 256), 0, 8)[0]
+        return ctx.hashjoin(R, S)[0]
+
+    ctx.tune(spin_limit=1, probe_variant=1 if op == "staged_probe" else 0)
+    try:
+        with pytest.raises(gpu.PgError) as err:
+            run()
+        assert err.value.code == PG_ERR_TIMEOUT
+    finally:
+        ctx.tune(spin_limit=0)
+    try:
+        got = run()
+    finally:
+        ctx.tune(probe_variant=0)
+    if op == "sort":
+        _sort_check(ctx, rows)
+    elif op == "partition":
+        want, _ = orc.partition(rows, orc.hashcfg("parammodulo", 256))
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    else:
+        want, _, _ = orc.hashjoin(R, S, hash=orc.hashcfg("modulo", 1 << 16))
+        assert np.array_equal(canon(got), canon(want))
