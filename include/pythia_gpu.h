@@ -147,7 +147,9 @@ enum {
 	PG_TUNE_PROBE_ITEMS = 6,         /* dense-table lookups in flight per lane of the 16-byte probe: 4 or 8 */
 	PG_TUNE_PROBE_CACHE = 7,         /* 16-byte probe L2 policies: bits 0-1 table loads (0 evict-last,
 	                                    1 normal, 2 unchanged, 3 first), bit 2 probe reads and bit 3
-	                                    output stores normal instead of evict-first */
+	                                    output stores normal instead of evict-first, bits 4-6 evict-last
+	                                    for that many eighths of the table's lines only (0: all), bit 7
+	                                    table loads kept in L1 (dense-table probes) */
 	PG_TUNE_PROBE_PASSES = 8,        /* dense-table probe passes: 1, 2 (half the table each), 0 by size */
 	PG_TUNE_GROUPBY_PATH = 9,        /* group-by: 0 by key range and size, 1 hashed global table, 2 partitioned,
 	                                    3 hashed global without warp combining, 4 partitioned without warp

@@ -121,17 +121,23 @@ extern "C" int pg_device_status(pg_ctx* ctx)
 	return st;
 }
 
+int pg_status_fail(pg_ctx* ctx, cudaStream_t s, int st, const char* what)
+{
+	cudaMemsetAsync(ctx->d_status, 0, sizeof(int), s);
+	cudaStreamSynchronize(s);
+	const char* why = st == PG_ERR_TIMEOUT ? "a bounded device wait gave up"
+		: st == PG_ERR_TABLE_FULL ? "hash table probe sequence exhausted" : "device error";
+	return pg_fail(ctx, st, std::string(what) + ": " + why);
+}
+
 int pg_check_status(pg_ctx* ctx, cudaStream_t s, const char* what)
 {
-	PG_CUDA(ctx, cudaStreamSynchronize(s));
+	// Stream-ordered read of the status word: no synchronisation with other
+	// streams, one round trip for the wait and the read.
 	int st = 0;
-	PG_CUDA(ctx, cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
-	if (st) {
-		cudaMemset(ctx->d_status, 0, sizeof(int));
-		const char* why = st == PG_ERR_TIMEOUT ? "a bounded device wait gave up"
-			: st == PG_ERR_TABLE_FULL ? "hash table probe sequence exhausted" : "device error";
-		return pg_fail(ctx, st, std::string(what) + ": " + why);
-	}
+	PG_CUDA(ctx, cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+	PG_CUDA(ctx, cudaStreamSynchronize(s));
+	if (st) return pg_status_fail(ctx, s, st, what);
 	return PG_OK;
 }
 

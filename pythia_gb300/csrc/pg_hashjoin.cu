@@ -56,7 +56,9 @@ struct HjProbeTable {
 	unsigned long long drange;
 	uint32_t cache;                        // L2 policy knob: bits 0-1 table loads (0 evict-last,
 	                                       // 1 normal, 2 unchanged, 3 first); bit 2 probe reads,
-	                                       // bit 3 output stores normal instead of evict-first
+	                                       // bit 3 output stores normal instead of evict-first;
+	                                       // bits 4-6 evict-last for that many eighths of the
+	                                       // table's lines (0: all); bit 7 table loads kept in L1
 	const HjDenseHdr* hdr;                 // speculative narrow dense table: window and checks, else null
 };
 
@@ -1231,7 +1233,7 @@ k_probe16_warp(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 	const uint64_t first = (uint64_t) blockIdx.x * PW_WARPS + warp;
 	const uint64_t mask = (1ull << tb.log2cap) - 1;
 	const uint32_t tp_ = tb.cache & 3;
-	const uint64_t keep = tp_ == 0 ? pg_policy_evict_last() : tp_ == 1 ? pg_policy_evict_normal()
+	const uint64_t keep = tp_ == 0 ? pg_policy_keep((tb.cache >> 4) & 7) : tp_ == 1 ? pg_policy_evict_normal()
 		: tp_ == 2 ? pg_policy_evict_unchanged() : pg_policy_evict_first();
 	const uint64_t instream = (tb.cache & 4) ? pg_policy_evict_normal() : pg_policy_evict_first();
 	const uint64_t stream = (tb.cache & 8) ? pg_policy_evict_normal() : pg_policy_evict_first();
@@ -1406,13 +1408,16 @@ k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const Hj
 	static_assert(MODE == 1 || MODE == 2, "dense tables only");
 	HjProbeTable tb = tb0;
 	if (!hj_spec_resolve(tb)) return;
+	// A speculative table is probed in one pass over its window: the host
+	// passed the allocation's capacity, past the entries the build filled.
+	if (tb0.hdr) { dlo = 0; dhi = tb.drange; }
 	constexpr int ITEMS = PW_CHUNK / 32;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
 	const uint64_t W = (uint64_t) gridDim.x * PW_WARPS;
 	const uint64_t first = (uint64_t) blockIdx.x * PW_WARPS + warp;
 	const uint32_t tp_ = tb.cache & 3;
-	const uint64_t keep = tp_ == 0 ? pg_policy_evict_last() : tp_ == 1 ? pg_policy_evict_normal()
+	const uint64_t keep = tp_ == 0 ? pg_policy_keep((tb.cache >> 4) & 7) : tp_ == 1 ? pg_policy_evict_normal()
 		: tp_ == 2 ? pg_policy_evict_unchanged() : pg_policy_evict_first();
 	const uint64_t instream = (tb.cache & 4) ? pg_policy_evict_normal() : pg_policy_evict_first();
 	const uint64_t stream = (tb.cache & 8) ? pg_policy_evict_normal() : pg_policy_evict_first();
@@ -1513,8 +1518,12 @@ __device__ __forceinline__ void hj_lookup4(const HjProbeTable& tb, const uint4 (
 			: (int64_t) (((uint64_t) t[j].w << 32) | t[j].z);
 		const unsigned long long d = (unsigned long long) key - (unsigned long long) tb.dmin;
 		e[j] = 0xFFFFFFFFu;
-		if ((uint32_t) (j * 32 + lane) < rows && d < tb.drange && (!PRED || pg_pred16(pr, t[j])))
-			asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(e[j]) : "l"(tb.dense32 + d), "l"(keep));
+		if ((uint32_t) (j * 32 + lane) < rows && d < tb.drange && (!PRED || pg_pred16(pr, t[j]))) {
+			if (tb.cache & 128)
+				asm("ld.global.nc.L1::evict_last.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(e[j]) : "l"(tb.dense32 + d), "l"(keep));
+			else
+				asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(e[j]) : "l"(tb.dense32 + d), "l"(keep));
+		}
 	}
 }
 
@@ -1529,7 +1538,7 @@ k_probe16_deep(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
 	const uint64_t W = (uint64_t) gridDim.x * PW_WARPS;
 	const uint64_t first = (uint64_t) blockIdx.x * PW_WARPS + warp;
-	const uint64_t keep = pg_policy_evict_last();
+	const uint64_t keep = pg_policy_keep((tb.cache >> 4) & 7);
 	const uint64_t stream = pg_policy_evict_first();
 	unsigned long long cnt_acc = 0;
 	if (first >= nchunks) return;
@@ -2180,7 +2189,7 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 		tb.dense32 = ht->dense32; tb.vmin = ht->vmin;
 		tb.hdr = nullptr;
 	}
-	tb.cache = (uint32_t) (ctx->tune[PG_TUNE_PROBE_CACHE] & 15);
+	tb.cache = (uint32_t) (ctx->tune[PG_TUNE_PROBE_CACHE] & 255);
 	const int mode = spec ? 2 : ht->dense ? (ht->dense32 ? 2 : 1) : 0;
 	const bool fast16 = W == 16 && (koff == 0 || koff == 8) && kbytes == 8 && pc.ow_words == 4 &&
 		(reinterpret_cast<uintptr_t>(S) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
@@ -2388,6 +2397,32 @@ static int hj_compact(pg_ctx* ctx, cudaStream_t s, char* out, uint64_t n, uint64
 	return PG_OK;
 }
 
+// The probe's accumulators acc[0..3] with, in acc[4..7], a speculative
+// table's checks (flags, present entries, tuples) and the context's status
+// word, so that one copy brings all of them back.
+__global__ void k_probe_tail(unsigned long long* __restrict__ acc, const HjDenseHdr* __restrict__ hdr,
+		const int* __restrict__ status)
+{
+	acc[4] = hdr ? (unsigned long long) (unsigned) hdr->flags : 0;
+	acc[5] = hdr ? hdr->present : 0;
+	acc[6] = hdr ? hdr->n : 0;
+	acc[7] = (unsigned long long) (unsigned) *status;
+}
+
+// One round trip after a probe: h = acc[0..7]; a non-zero status fails the
+// call; *refuted: the speculative table's checks failed (nothing was probed).
+static int hj_readback(pg_ctx* ctx, cudaStream_t s, unsigned long long* acc, const HjDenseHdr* hdr,
+		unsigned long long (&h)[8], bool* refuted, const char* what)
+{
+	k_probe_tail<<<1, 1, 0, s>>>(acc, hdr, ctx->d_status);
+	PG_LAUNCHED(ctx);
+	PG_CUDA(ctx, cudaMemcpyAsync(h, acc, sizeof h, cudaMemcpyDeviceToHost, s));
+	PG_CUDA(ctx, cudaStreamSynchronize(s));
+	if (h[7]) return pg_status_fail(ctx, s, (int) h[7], what);
+	*refuted = hdr && !(h[4] == 0 && h[5] == h[6]);
+	return PG_OK;
+}
+
 // pg_hashjoin_probe; with `pred`, the probe tuples failing it take no part
 // (only for the dense 16-byte layouts the register-loading kernels handle).
 static int hj_probe_run(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
@@ -2411,15 +2446,15 @@ static int hj_probe_run(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 	if ((rc = pg_alloc_async(ctx, s, (void**) &acc, 64))) return rc;
 	PG_CUDA(ctx, cudaMemsetAsync(acc, 0, 64, s));
 	const uint64_t ntiles = pg_div_up(S->n, HJ_TILE);
-	unsigned long long host_acc[4] = {0, 0, 0, 0};
+	unsigned long long host_acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
 	if (ht->unique && ht->inline_val) {
 		const char* Sd = (const char*) S->data;
 		// A speculative table's checks come back with the counts; when they
 		// failed, the kernels wrote nothing and the caller rebuilds.
-		HjDenseHdr hh;
 		const bool spec = ht->spec.load(std::memory_order_acquire);
-		auto refuted = [&]() { return spec && !hj_hdr_ok(hh); };
+		const HjDenseHdr* hdr = spec ? ht->hdr : nullptr;
+		bool refuted = false;
 		if (spec) PG_CUDA(ctx, cudaStreamWaitEvent(s, ht->built, 0));
 		if (materialize) {
 			uint64_t* counts = nullptr;
@@ -2430,10 +2465,8 @@ static int hj_probe_run(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 				pg_free_async(ctx, s, counts); pg_free_async(ctx, s, acc);
 				return rc;
 			}
-			PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
-			if (spec) PG_CUDA(ctx, cudaMemcpyAsync(&hh, ht->hdr, sizeof hh, cudaMemcpyDeviceToHost, s));
-			if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
-			if (refuted()) {
+			if ((rc = hj_readback(ctx, s, acc, hdr, host_acc, &refuted, "pg_hashjoin_probe"))) return rc;
+			if (refuted) {
 				pg_free_async(ctx, s, counts); pg_free_async(ctx, s, acc);
 				return HJ_SPEC_REFUTED;
 			}
@@ -2457,10 +2490,8 @@ static int hj_probe_run(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 				pg_free_async(ctx, s, acc);
 				return rc;
 			}
-			PG_CUDA(ctx, cudaMemcpyAsync(host_acc, acc, 32, cudaMemcpyDeviceToHost, s));
-			if (spec) PG_CUDA(ctx, cudaMemcpyAsync(&hh, ht->hdr, sizeof hh, cudaMemcpyDeviceToHost, s));
-			if ((rc = pg_check_status(ctx, s, "pg_hashjoin_probe"))) return rc;
-			if (refuted()) {
+			if ((rc = hj_readback(ctx, s, acc, hdr, host_acc, &refuted, "pg_hashjoin_probe"))) return rc;
+			if (refuted) {
 				pg_free_async(ctx, s, acc);
 				return HJ_SPEC_REFUTED;
 			}

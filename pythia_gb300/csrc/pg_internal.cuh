@@ -50,6 +50,8 @@ int pg_alloc_async(pg_ctx* ctx, cudaStream_t s, void** p, size_t bytes);
 void pg_free_async(pg_ctx* ctx, cudaStream_t s, void* p);
 // Reads the sticky status after synchronising `s`; returns its PG_ERR_* code.
 int pg_check_status(pg_ctx* ctx, cudaStream_t s, const char* what);
+// Clears a non-zero status `st` read back by the caller and reports it.
+int pg_status_fail(pg_ctx* ctx, cudaStream_t s, int st, const char* what);
 
 // ---------------------------------------------------------------------------
 // Bucket functions (hash.h:51-479) in the form their constructors leave them.
@@ -257,6 +259,24 @@ __device__ __forceinline__ uint64_t pg_policy_evict_first()
 {
 	uint64_t p;
 	asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+	return p;
+}
+
+// Table-load policy: evict-last for `eighths`/8 of the accessed lines (the
+// rest keep their priority), all lines when eighths is 0 or 8 or more.
+__device__ __forceinline__ uint64_t pg_policy_keep(uint32_t eighths)
+{
+	uint64_t p;
+	switch (eighths) {
+	case 1: asm volatile("createpolicy.fractional.L2::evict_last.L2::evict_unchanged.b64 %0, 0.125;" : "=l"(p)); break;
+	case 2: asm volatile("createpolicy.fractional.L2::evict_last.L2::evict_unchanged.b64 %0, 0.25;" : "=l"(p)); break;
+	case 3: asm volatile("createpolicy.fractional.L2::evict_last.L2::evict_unchanged.b64 %0, 0.375;" : "=l"(p)); break;
+	case 4: asm volatile("createpolicy.fractional.L2::evict_last.L2::evict_unchanged.b64 %0, 0.5;" : "=l"(p)); break;
+	case 5: asm volatile("createpolicy.fractional.L2::evict_last.L2::evict_unchanged.b64 %0, 0.625;" : "=l"(p)); break;
+	case 6: asm volatile("createpolicy.fractional.L2::evict_last.L2::evict_unchanged.b64 %0, 0.75;" : "=l"(p)); break;
+	case 7: asm volatile("createpolicy.fractional.L2::evict_last.L2::evict_unchanged.b64 %0, 0.875;" : "=l"(p)); break;
+	default: asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p)); break;
+	}
 	return p;
 }
 

@@ -154,7 +154,8 @@ def test_join_dense_keys_wide_values(ctx):
                                    dict(probe_variant=1, probe_passes=2, probe_items=8), dict(probe_cache=1),
                                    dict(probe_cache=14), dict(probe_passes=2), dict(probe_variant=4),
                                    dict(probe_variant=4, probe_passes=2, probe_ctas_per_sm=5),
-                                   dict(probe_variant=2), dict(probe_variant=3), dict(probe_variant=5)])
+                                   dict(probe_variant=2), dict(probe_variant=3), dict(probe_variant=5),
+                                   dict(probe_cache=64), dict(probe_cache=192), dict(probe_cache=48 + 4)])
 def test_join_probe_launch_shapes(ctx, knobs):
     # Probe kernel variants, lookups in flight, L2 policies, passes and grid
     # shapes change speed, never rows: narrow and wide dense tables, with
@@ -215,6 +216,8 @@ def test_join_dense_build_on_device(ctx, spec, case):
     R = _spec_cases()[case]
     S = dg.probe_uniform(300_000, R[:100_000], dg.seed_for(42))
     S[::101, 0] += 3_000_000                              # misses outside every window
+    # Misses past the sampled window but inside the build's allocation.
+    S[::97, 0] = R[:100_000, 0].max() + 50_000 + (S[::97, 1] % 60_000)
     try:
         ctx.tune(build_spec=spec)
         _join_check(ctx, R, S)
