@@ -149,7 +149,8 @@ enum {
 	                                    1 normal, 2 unchanged, 3 first), bit 2 probe reads and bit 3
 	                                    output stores normal instead of evict-first, bits 4-6 evict-last
 	                                    for that many eighths of the table's lines only (0: all), bit 7
-	                                    table loads kept in L1 (dense-table probes) */
+	                                    table loads kept in L1 (dense-table probes); 0 = the built-in
+	                                    4/8 evict-last with L1 (bits 4-7 = 0xC), 256 = all bits clear */
 	PG_TUNE_PROBE_PASSES = 8,        /* dense-table probe passes: 1, 2 (half the table each), 0 by size */
 	PG_TUNE_GROUPBY_PATH = 9,        /* group-by: 0 by key range and size, 1 hashed global table, 2 partitioned,
 	                                    3 hashed global without warp combining, 4 partitioned without warp

@@ -304,14 +304,16 @@ __global__ void __launch_bounds__(256)
 k_mj_bucket_join(const char* __restrict__ R, const uint64_t* __restrict__ roffs, uint32_t wR, uint32_t rkoff,
 		uint32_t rkb, const char* __restrict__ S, const uint64_t* __restrict__ soffs, uint32_t wS, uint32_t skoff,
 		uint32_t skb, long long kmin, int sum_side, uint32_t soff, uint32_t swords,
-		unsigned long long* __restrict__ agg)
+		unsigned long long* __restrict__ agg, uint64_t* __restrict__ bucket_rows)
 {
+	__shared__ unsigned long long btot;
 	extern __shared__ __align__(16) unsigned char mj_smem[];
 	unsigned long long* sm = reinterpret_cast<unsigned long long*>(mj_smem);    // [MJ_LOCAL]
 	uint32_t* cR = reinterpret_cast<uint32_t*>(sm + MJ_LOCAL);                   // [MJ_LOCAL]
 	uint32_t* cS = cR + MJ_LOCAL;                                                // [MJ_LOCAL]
 	const uint32_t b = blockIdx.x;
 	for (uint32_t k = threadIdx.x; k < MJ_LOCAL; k += blockDim.x) { sm[k] = 0; cR[k] = 0; cS[k] = 0; }
+	if (threadIdx.x == 0) btot = 0;
 	__syncthreads();
 	const uint64_t r0 = roffs[b], r1 = roffs[b + 1], s0 = soffs[b], s1 = soffs[b + 1];
 	// Eight tuples per thread are loaded before their shared-memory updates,
@@ -358,8 +360,12 @@ k_mj_bucket_join(const char* __restrict__ R, const uint64_t* __restrict__ roffs,
 		sum += __shfl_down_sync(0xffffffffu, sum, o);
 	}
 	if ((threadIdx.x & 31) == 0) {
-		if (c) atomicAdd(&agg[0], c);
+		if (c) { atomicAdd(&agg[0], c); atomicAdd(&btot, c); }
 		if (sum) atomicAdd(&agg[1], sum);
+	}
+	if (bucket_rows) {
+		__syncthreads();
+		if (threadIdx.x == 0) bucket_rows[b] = btot;
 	}
 }
 
@@ -397,15 +403,208 @@ __global__ void k_mj_minmax(const char* __restrict__ in, uint64_t n, uint32_t W,
 	if ((threadIdx.x & 31) == 0) { atomicMin(&mm[0], lo); atomicMax(&mm[1], hi); }
 }
 
-// The fused count/sum above; *handled = false (nothing done) when the key span
-// is outside its range.
-static int mj_bucket_count_sum(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, const pg_rel* S, const MjCols& pc,
-		int sum_col, pg_join_result* res, bool* handled)
+// ---------------------------------------------------------------------------
+// Materialised MPSM over key buckets (16-byte tuples, 8-byte keys, 16-byte
+// output rows). After the bucket partition of both sides (as for the
+// count/sum), k_mj_bucket_join writes each bucket's output row count, a scan
+// turns them into output offsets, and k_mj_bucket_write joins each bucket
+// pair in one CTA: the build side's packed values counting-sorted by key into
+// shared memory (a run per key), then every probe tuple writes one row per
+// build tuple of its key at a block-scanned position. Output rows are in
+// bucket order; within a bucket their order is unspecified (as for every
+// join output).
+// ---------------------------------------------------------------------------
+#define MJW_THREADS 512
+#define MJW_CAP 24576            // build tuples of one bucket held in shared memory (192 KB)
+
+// The build-projected words of a row that are not the join key, packed.
+struct MjPack {
+	int n;
+	uint8_t roff[2];             // word offsets in the build tuple
+};
+
+__device__ __forceinline__ uint32_t mjw_word(const uint4& t, uint32_t i)
+{
+	return i == 0 ? t.x : i == 1 ? t.y : i == 2 ? t.z : t.w;
+}
+
+// Output word source: 0-3 probe tuple word, 4-5 packed build word.
+__device__ __forceinline__ uint32_t mjw_pick(const uint4& t, unsigned long long v, uint32_t sel)
+{
+	return sel < 4 ? mjw_word(t, sel) : sel == 4 ? (uint32_t) v : (uint32_t) (v >> 32);
+}
+
+// Exclusive scan of x over the CTA's MJW_THREADS threads; *total = the sum.
+// wsum: MJW_THREADS / 32 words of shared memory. Ends with a barrier.
+__device__ __forceinline__ uint32_t mjw_block_scan(uint32_t x, uint32_t* wsum, uint32_t* total)
+{
+	const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	uint32_t inc = x;
+	#pragma unroll
+	for (int o = 1; o < 32; o <<= 1) {
+		const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+		if (lane >= (uint32_t) o) inc += y;
+	}
+	if (lane == 31) wsum[warp] = inc;
+	__syncthreads();
+	if (warp == 0) {
+		uint32_t w = lane < MJW_THREADS / 32 ? wsum[lane] : 0;
+		#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+			if (lane >= (uint32_t) o) w += y;
+		}
+		if (lane < MJW_THREADS / 32) wsum[lane] = w;
+	}
+	__syncthreads();
+	const uint32_t before = (warp ? wsum[warp - 1] : 0) + inc - x;
+	*total = wsum[MJW_THREADS / 32 - 1];
+	__syncthreads();
+	return before;
+}
+
+__global__ void __launch_bounds__(MJW_THREADS, 1)
+k_mj_bucket_write(const uint4* __restrict__ R, const uint64_t* __restrict__ roffs, uint32_t rkw, MjPack bp,
+		const uint4* __restrict__ S, const uint64_t* __restrict__ soffs, uint32_t skw, long long kmin,
+		const uint64_t* __restrict__ bucket_off, uint32_t wsel, uint4* __restrict__ out, int* __restrict__ status)
+{
+	extern __shared__ __align__(16) unsigned char mw_smem[];
+	unsigned long long* rv = reinterpret_cast<unsigned long long*>(mw_smem);     // [MJW_CAP]
+	uint32_t* start = reinterpret_cast<uint32_t*>(rv + MJW_CAP);                // [MJ_LOCAL + 1]
+	uint32_t* fill = start + MJ_LOCAL + 1;                                       // [MJ_LOCAL]
+	uint32_t* wsum = fill + MJ_LOCAL;                                            // [MJW_THREADS / 32]
+	const uint32_t b = blockIdx.x, tid = threadIdx.x;
+	const uint64_t r0 = roffs[b], r1 = roffs[b + 1], s0 = soffs[b], s1 = soffs[b + 1];
+	if (r1 - r0 > MJW_CAP) {             // the host checked every bucket; never taken
+		if (tid == 0) pg_set_status(status, PG_ERR_UNSUPPORTED);
+		return;
+	}
+	const unsigned long long kbase = (unsigned long long) kmin;
+	for (uint32_t k = tid; k < MJ_LOCAL; k += MJW_THREADS) { start[k] = 0; fill[k] = 0; }
+	__syncthreads();
+	// Build side: per-key counts, their exclusive scan (run starts), then the
+	// packed values scattered into their key's run.
+	for (uint64_t i = r0 + tid; i < r1; i += MJW_THREADS) {
+		const uint4 t = R[i];
+		const unsigned long long key = ((unsigned long long) mjw_word(t, rkw + 1) << 32) | mjw_word(t, rkw);
+		atomicAdd(&start[(key - kbase) & (MJ_LOCAL - 1)], 1u);
+	}
+	__syncthreads();
+	{
+		constexpr uint32_t PER = MJ_LOCAL / MJW_THREADS;        // 8 entries per thread
+		uint32_t v[PER], run = 0;
+		#pragma unroll
+		for (uint32_t j = 0; j < PER; ++j) { v[j] = start[tid * PER + j]; run += v[j]; }
+		uint32_t total;
+		uint32_t base = mjw_block_scan(run, wsum, &total);
+		#pragma unroll
+		for (uint32_t j = 0; j < PER; ++j) { start[tid * PER + j] = base; base += v[j]; }
+		if (tid == 0) start[MJ_LOCAL] = total;
+	}
+	__syncthreads();
+	for (uint64_t i = r0 + tid; i < r1; i += MJW_THREADS) {
+		const uint4 t = R[i];
+		const unsigned long long key = ((unsigned long long) mjw_word(t, rkw + 1) << 32) | mjw_word(t, rkw);
+		const uint32_t k = (uint32_t) ((key - kbase) & (MJ_LOCAL - 1));
+		const uint32_t pos = start[k] + atomicAdd(&fill[k], 1u);
+		unsigned long long pv = 0;
+		if (bp.n > 0) pv = mjw_word(t, bp.roff[0]);
+		if (bp.n > 1) pv |= (unsigned long long) mjw_word(t, bp.roff[1]) << 32;
+		rv[pos] = pv;
+	}
+	__syncthreads();
+	// Probe side in chunks of MJW_THREADS tuples: tuple i makes one row per
+	// build tuple of its key, at the chunk's running offset.
+	const uint32_t w0 = wsel & 15, w1 = (wsel >> 4) & 15, w2 = (wsel >> 8) & 15, w3 = (wsel >> 12) & 15;
+	uint64_t row = bucket_off[b];
+	for (uint64_t c0 = s0; c0 < s1; c0 += MJW_THREADS) {
+		const uint64_t i = c0 + tid;
+		uint4 t = make_uint4(0, 0, 0, 0);
+		uint32_t m = 0, rs = 0;
+		if (i < s1) {
+			t = S[i];
+			const unsigned long long key = ((unsigned long long) mjw_word(t, skw + 1) << 32) | mjw_word(t, skw);
+			const uint32_t k = (uint32_t) ((key - kbase) & (MJ_LOCAL - 1));
+			rs = start[k];
+			m = start[k + 1] - rs;
+		}
+		uint32_t total;
+		const uint32_t off = mjw_block_scan(m, wsum, &total);
+		uint4* o = out + row + off;
+		for (uint32_t r = 0; r < m; ++r) {
+			const unsigned long long v = rv[rs + r];
+			o[r] = make_uint4(mjw_pick(t, v, w0), mjw_pick(t, v, w1), mjw_pick(t, v, w2), mjw_pick(t, v, w3));
+		}
+		row += total;
+	}
+}
+
+// Largest build-side bucket (roffs[b + 1] - roffs[b]) into *mx.
+__global__ void k_mj_max_bucket(const uint64_t* __restrict__ offs, uint32_t B, unsigned long long* __restrict__ mx)
+{
+	unsigned long long m = 0;
+	for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x)
+		m = max(m, (unsigned long long) (offs[b + 1] - offs[b]));
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+	if ((threadIdx.x & 31) == 0 && m) atomicMax(mx, m);
+}
+
+// Word selector (4 bits per output word: 0-3 probe tuple word, 4-5 packed
+// build word) and packed build words of the 16-byte output rows of the
+// bucketed materialising join; false when the layout is not one it takes:
+// 16-byte tuples with 8-byte keys on both sides, 16-byte rows whose build
+// words other than the key (taken from the probe tuple's equal key) fit 8 bytes.
+static bool mj_bucket_rows_fit(const pg_rel* R, const pg_rel* S, const MjCols& pc, uint32_t* wsel, MjPack* bp)
+{
+	if (R->width != 16 || S->width != 16 || R->key_bytes != 8 || S->key_bytes != 8 || (R->key_off & 7) ||
+			(S->key_off & 7) || pc.ow_words != 4 ||
+			(reinterpret_cast<uintptr_t>(R->data) & 15) || (reinterpret_cast<uintptr_t>(S->data) & 15))
+		return false;
+	bp->n = 0; bp->roff[0] = bp->roff[1] = 0;
+	*wsel = 0;
+	uint32_t o = 0;
+	for (int c = 0; c < pc.n; ++c)
+		for (uint32_t j = 0; j < pc.words[c]; ++j, ++o) {
+			const uint32_t byte = pc.off[c] + 4 * j;
+			uint32_t sel;
+			if (pc.side[c]) {
+				sel = byte / 4;
+			} else if (byte >= R->key_off && byte < R->key_off + 8) {
+				sel = (S->key_off + (byte - R->key_off)) / 4;
+			} else {
+				int p = -1;
+				for (int q = 0; q < bp->n; ++q) if (bp->roff[q] == byte / 4) p = q;
+				if (p < 0) {
+					if (bp->n == 2) return false;
+					p = bp->n;
+					bp->roff[bp->n++] = (uint8_t) (byte / 4);
+				}
+				sel = 4 + (uint32_t) p;
+			}
+			*wsel |= sel << (4 * o);
+		}
+	return true;
+}
+
+// Joins over key buckets when the key span is 2^13..2^24 values: both sides
+// partitioned on the key bits above the low 12, then each bucket pair in
+// shared memory. Without `materialize` the per-key counts give the count and
+// sum (MjCols sum column); with it, the rows are written (16-byte layouts
+// that mj_bucket_rows_fit takes, every bucket's build side within MJW_CAP
+// tuples). *handled = false (nothing produced) when the case is not one it
+// takes: the caller then sorts.
+static int mj_bucket_join(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, const pg_rel* S, const MjCols& pc,
+		int sum_col, bool materialize, void* out, uint64_t out_capacity, pg_join_result* res, bool* handled)
 {
 	*handled = false;
+	uint32_t wsel = 0;
+	MjPack bp;
+	if (materialize && (!mj_bucket_rows_fit(R, S, pc, &wsel, &bp) || (reinterpret_cast<uintptr_t>(out) & 15)))
+		return PG_OK;
 	int rc;
-	unsigned long long* mm = nullptr;
-	if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 32))) return rc;
+	unsigned long long* mm = nullptr;    // [key min, key max, count, sum, largest build bucket]
+	if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 64))) return rc;
 	const unsigned long long init[4] = {~0ull, 0ull, 0ull, 0ull};
 	PG_CUDA(ctx, cudaMemcpyAsync(mm, init, 32, cudaMemcpyHostToDevice, s));
 	for (const pg_rel* r : {R, S}) {
@@ -428,12 +627,17 @@ static int mj_bucket_count_sum(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, con
 	const int npass = hb <= 8 ? 1 : 2;
 	const int d0 = npass == 1 ? hb : hb / 2;
 	char *pR = nullptr, *pS = nullptr, *tmp = nullptr;
-	uint64_t *oR = nullptr, *oS = nullptr;
+	uint64_t *oR = nullptr, *oS = nullptr, *brows = nullptr;
+	auto release = [&]() {
+		for (void* p : {(void*) pR, (void*) pS, (void*) tmp, (void*) oR, (void*) oS, (void*) brows, (void*) mm})
+			pg_free_async(ctx, s, p);
+	};
 	if ((rc = pg_alloc_async(ctx, s, (void**) &pR, R->n * R->width))) return rc;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &pS, S->n * S->width))) return rc;
 	if (npass == 2 && (rc = pg_alloc_async(ctx, s, (void**) &tmp, std::max(R->n * R->width, S->n * S->width)))) return rc;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &oR, (B + 1) * 8))) return rc;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &oS, (B + 1) * 8))) return rc;
+	if (materialize && (rc = pg_alloc_async(ctx, s, (void**) &brows, (B + 1) * 8))) return rc;
 	for (int side = 0; side < 2; ++side) {
 		const pg_rel* in = side ? S : R;
 		char* dst = side ? pS : pR;
@@ -455,22 +659,41 @@ static int mj_bucket_count_sum(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, con
 				side ? oS : oR);
 		PG_LAUNCHED(ctx);
 	}
-	PG_CUDA(ctx, cudaMemsetAsync(mm + 2, 0, 16, s));
+	PG_CUDA(ctx, cudaMemsetAsync(mm + 2, 0, 24, s));
 	const int sum_side = sum_col < 0 ? -1 : (int) pc.side[sum_col];
 	const size_t smem = MJ_LOCAL * (8 + 4 + 4);
 	PG_CUDA(ctx, cudaFuncSetAttribute(k_mj_bucket_join, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
 	k_mj_bucket_join<<<B, 256, smem, s>>>(pR, oR, R->width, R->key_off, R->key_bytes, pS, oS, S->width, S->key_off,
 			S->key_bytes, kmin, sum_side, sum_col >= 0 ? pc.off[sum_col] : 0, sum_col >= 0 ? pc.words[sum_col] : 0,
-			mm + 2);
+			mm + 2, brows);
 	PG_LAUNCHED(ctx);
-	unsigned long long o[2];
-	PG_CUDA(ctx, cudaMemcpyAsync(o, mm + 2, 16, cudaMemcpyDeviceToHost, s));
-	for (void* p : {(void*) pR, (void*) pS, (void*) tmp, (void*) oR, (void*) oS, (void*) mm}) pg_free_async(ctx, s, p);
-	if ((rc = pg_check_status(ctx, s, "pg_mpsm_join"))) return rc;
+	if (materialize) {
+		if ((rc = pg_scan_u64(ctx, s, brows, B, nullptr))) { release(); return rc; }
+		k_mj_max_bucket<<<(B + 255) / 256, 256, 0, s>>>(oR, B, mm + 4);
+		PG_LAUNCHED(ctx);
+	}
+	unsigned long long o[3];
+	PG_CUDA(ctx, cudaMemcpyAsync(o, mm + 2, 24, cudaMemcpyDeviceToHost, s));
+	if ((rc = pg_check_status(ctx, s, "pg_mpsm_join"))) { release(); return rc; }
+	if (materialize && o[2] > MJW_CAP) { release(); return PG_OK; }     // a bucket too large: sort instead
 	res->n_out = o[0];
 	res->sum = (int64_t) o[1];
 	*handled = true;
-	return PG_OK;
+	if (materialize && o[0]) {
+		if (o[0] > out_capacity) {
+			release();
+			return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_mpsm_join: output capacity too small");
+		}
+		const size_t wsmem = MJW_CAP * 8 + (2 * MJ_LOCAL + 1) * 4 + (MJW_THREADS / 32) * 4;
+		PG_CUDA(ctx, cudaFuncSetAttribute(k_mj_bucket_write, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) wsmem));
+		k_mj_bucket_write<<<B, MJW_THREADS, wsmem, s>>>(reinterpret_cast<const uint4*>(pR), oR, R->key_off / 4, bp,
+				reinterpret_cast<const uint4*>(pS), oS, S->key_off / 4, kmin, brows, wsel,
+				reinterpret_cast<uint4*>(out), ctx->d_status);
+		PG_LAUNCHED(ctx);
+		rc = pg_check_status(ctx, s, "pg_mpsm_join");
+	}
+	release();
+	return rc;
 }
 
 extern "C" int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, const pg_rel* S,
@@ -501,9 +724,9 @@ extern "C" int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, cons
 	if (R->n == 0 || S->n == 0) return PG_OK;
 	cudaStream_t s = (cudaStream_t) stream;
 	int rc;
-	if (!materialize && R->n < (1ull << 32) && S->n < (1ull << 32)) {
+	if (R->n < (1ull << 32) && S->n < (1ull << 32)) {
 		bool handled = false;
-		if ((rc = mj_bucket_count_sum(ctx, s, R, S, pc, sum_col, res, &handled))) return rc;
+		if ((rc = mj_bucket_join(ctx, s, R, S, pc, sum_col, materialize, out, out_capacity, res, &handled))) return rc;
 		if (handled) return PG_OK;
 	}
 	pg_rec *rr = nullptr, *sr = nullptr;

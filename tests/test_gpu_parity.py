@@ -155,7 +155,8 @@ def test_join_dense_keys_wide_values(ctx):
                                    dict(probe_cache=14), dict(probe_passes=2), dict(probe_variant=4),
                                    dict(probe_variant=4, probe_passes=2, probe_ctas_per_sm=5),
                                    dict(probe_variant=2), dict(probe_variant=3), dict(probe_variant=5),
-                                   dict(probe_cache=64), dict(probe_cache=192), dict(probe_cache=48 + 4)])
+                                   dict(probe_cache=64), dict(probe_cache=192), dict(probe_cache=48 + 4),
+                                   dict(probe_cache=256)])
 def test_join_probe_launch_shapes(ctx, knobs):
     # Probe kernel variants, lookups in flight, L2 policies, passes and grid
     # shapes change speed, never rows: narrow and wide dense tables, with
@@ -798,6 +799,35 @@ def test_mpsm_count_sum_bucketed_key_spans(ctx, span_bits):
     _, wn3, ws3 = orc.mergejoin(I, I, proj=(("P", 4, 4), ("B", 4, 4)), bkey=(0, 4), pkey=(0, 4),
                                 materialise=False, sum_col=1)
     assert (n3, s3) == (wn3, ws3)
+
+
+@pytest.mark.parametrize("span_bits", [13, 16, 20, 24])
+def test_mpsm_materialised_bucketed_key_spans(ctx, span_bits):
+    # Materialised joins of 16-byte tuples with key spans of 2^13..2^24 take
+    # the bucketed form (each bucket pair joined in shared memory): rows must
+    # be the oracle's multiset for every 16-byte projection, including the
+    # build key (taken from the probe's equal key) and the probe key, with a
+    # hot key and negative keys.
+    n = 300_000
+    R = dg.uniform_keys(n, 1 << span_bits, dg.seed_for(90 + span_bits))
+    S = dg.uniform_keys(n, 1 << span_bits, dg.seed_for(91 + span_bits))
+    R[::97, 0] = 4242                                 # a hot key on both sides
+    S[::89, 0] = 4242
+    R[:, 0] -= 1 << (span_bits - 1)
+    S[:, 0] -= 1 << (span_bits - 1)
+    for proj in ((("P", 8, 8), ("B", 8, 8)), (("B", 0, 8), ("P", 8, 8)), (("B", 8, 8), ("P", 0, 8)),
+                 (("P", 8, 4), ("B", 12, 4), ("B", 0, 8)), (("B", 8, 8), ("B", 0, 4), ("P", 12, 4))):
+        _mpsm_check(ctx, R, S, proj=proj)
+
+
+def test_mpsm_materialised_bucket_too_large_for_shared_memory(ctx):
+    # One key bucket holding more build tuples than shared memory takes
+    # (30,000 > 24,576): the join falls back to sorting, with the same rows.
+    R = dg.uniform_keys(100_000, 1 << 20, dg.seed_for(96))
+    R[:30_000, 0] = (R[:30_000, 0] % 4096) + (1 << 19)     # all in one 4096-key bucket
+    S = dg.uniform_keys(100_000, 1 << 20, dg.seed_for(97))
+    S[::3, 0] = (S[::3, 0] % 4096) + (1 << 19)
+    _mpsm_check(ctx, R, S)
 
 
 def test_mpsm_duplicates(ctx):
