@@ -79,6 +79,12 @@ typedef struct {
 } pg_join_result;
 
 enum { PG_JOIN_MATERIALIZE = 1, PG_JOIN_COUNT = 2, PG_JOIN_SUM = 4 };
+/* pg_mpsm_join only: that side is already sorted on its key, as a plan's
+ * buildpresorted / probepresorted = "yes" states (SortMergeJoinOp::init,
+ * operators/join.cpp:750-762). The device confirms it while it reads the key
+ * range and then skips that side's sort or partition; a side that is not
+ * sorted is sorted as usual, so the result never depends on the flags. */
+enum { PG_JOIN_BUILD_SORTED = 8, PG_JOIN_PROBE_SORTED = 16 };
 
 /* ---------------------------------------------------------------------- */
 /* Context, memory, streams (replace numaallocate_*, util/numaallocate.h:35-37,

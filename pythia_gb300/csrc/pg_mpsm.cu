@@ -385,15 +385,21 @@ __global__ void k_mj_bounds(const char* __restrict__ in, uint64_t n, uint32_t W,
 	offs[b] = lo;
 }
 
+// Key range into mm[0..1] (keys ^ 2^63 as unsigned); with `unsorted`, also
+// whether some key is greater than the next one.
 __global__ void k_mj_minmax(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes,
-		unsigned long long* __restrict__ mm)
+		unsigned long long* __restrict__ mm, unsigned long long* __restrict__ unsorted)
 {
 	unsigned long long lo = ~0ull, hi = 0;
+	bool down = false;
 	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x) {
-		const unsigned long long u = (unsigned long long) pg_load_key(in + i * W + koff, kbytes) ^ (1ull << 63);
+		const long long k = pg_load_key(in + i * W + koff, kbytes);
+		const unsigned long long u = (unsigned long long) k ^ (1ull << 63);
 		lo = u < lo ? u : lo;
 		hi = u > hi ? u : hi;
+		if (unsorted && i + 1 < n && k > pg_load_key(in + (i + 1) * W + koff, kbytes)) down = true;
 	}
+	if (unsorted && __any_sync(0xffffffffu, down) && (threadIdx.x & 31) == 0) *unsorted = 1;
 	#pragma unroll
 	for (int o = 16; o > 0; o >>= 1) {
 		const unsigned long long a = __shfl_down_sync(0xffffffffu, lo, o), b = __shfl_down_sync(0xffffffffu, hi, o);
@@ -595,26 +601,36 @@ static bool mj_bucket_rows_fit(const pg_rel* R, const pg_rel* S, const MjCols& p
 // tuples). *handled = false (nothing produced) when the case is not one it
 // takes: the caller then sorts.
 static int mj_bucket_join(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, const pg_rel* S, const MjCols& pc,
-		int sum_col, bool materialize, void* out, uint64_t out_capacity, pg_join_result* res, bool* handled)
+		int sum_col, int flags, void* out, uint64_t out_capacity, pg_join_result* res, bool* handled,
+		bool* r_sorted, bool* s_sorted)
 {
 	*handled = false;
+	*r_sorted = *s_sorted = false;
+	const bool materialize = (flags & PG_JOIN_MATERIALIZE) != 0;
 	uint32_t wsel = 0;
 	MjPack bp;
-	if (materialize && (!mj_bucket_rows_fit(R, S, pc, &wsel, &bp) || (reinterpret_cast<uintptr_t>(out) & 15)))
-		return PG_OK;
+	const bool rows_fit = mj_bucket_rows_fit(R, S, pc, &wsel, &bp) && !(reinterpret_cast<uintptr_t>(out) & 15);
 	int rc;
-	unsigned long long* mm = nullptr;    // [key min, key max, count, sum, largest build bucket]
+	// [key min, key max, count, sum, largest build bucket, R unsorted, S unsorted]
+	unsigned long long* mm = nullptr;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &mm, 64))) return rc;
-	const unsigned long long init[4] = {~0ull, 0ull, 0ull, 0ull};
-	PG_CUDA(ctx, cudaMemcpyAsync(mm, init, 32, cudaMemcpyHostToDevice, s));
-	for (const pg_rel* r : {R, S}) {
+	const unsigned long long init[8] = {~0ull, 0ull, 0ull, 0ull, 0ull, 0ull, 0ull, 0ull};
+	PG_CUDA(ctx, cudaMemcpyAsync(mm, init, 64, cudaMemcpyHostToDevice, s));
+	for (int side = 0; side < 2; ++side) {
+		const pg_rel* r = side ? S : R;
+		const bool check = (flags & (side ? PG_JOIN_PROBE_SORTED : PG_JOIN_BUILD_SORTED)) != 0;
 		const int blocks = (int) std::min<uint64_t>(pg_div_up(r->n, 256), (uint64_t) ctx->sm_count * 8);
-		k_mj_minmax<<<blocks, 256, 0, s>>>((const char*) r->data, r->n, r->width, r->key_off, r->key_bytes, mm);
+		k_mj_minmax<<<blocks, 256, 0, s>>>((const char*) r->data, r->n, r->width, r->key_off, r->key_bytes, mm,
+				check ? mm + 5 + side : nullptr);
 		PG_LAUNCHED(ctx);
 	}
-	unsigned long long h[2];
-	PG_CUDA(ctx, cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, s));
+	unsigned long long h[8];
+	PG_CUDA(ctx, cudaMemcpyAsync(h, mm, 64, cudaMemcpyDeviceToHost, s));
 	PG_CUDA(ctx, cudaStreamSynchronize(s));
+	// A side confirmed sorted skips its sort (here: its bucket partition).
+	*r_sorted = (flags & PG_JOIN_BUILD_SORTED) && !h[5];
+	*s_sorted = (flags & PG_JOIN_PROBE_SORTED) && !h[6];
+	if (materialize && !rows_fit) { pg_free_async(ctx, s, mm); return PG_OK; }
 	const unsigned long long span = h[1] - h[0];
 	const int bits = span == 0 ? 0 : 64 - __builtin_clzll(span);
 	if (bits <= (int) MJ_LOCAL_BITS || bits > (int) MJ_LOCAL_BITS + 12) { pg_free_async(ctx, s, mm); return PG_OK; }
@@ -632,17 +648,21 @@ static int mj_bucket_join(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, const pg
 		for (void* p : {(void*) pR, (void*) pS, (void*) tmp, (void*) oR, (void*) oS, (void*) brows, (void*) mm})
 			pg_free_async(ctx, s, p);
 	};
-	if ((rc = pg_alloc_async(ctx, s, (void**) &pR, R->n * R->width))) return rc;
-	if ((rc = pg_alloc_async(ctx, s, (void**) &pS, S->n * S->width))) return rc;
-	if (npass == 2 && (rc = pg_alloc_async(ctx, s, (void**) &tmp, std::max(R->n * R->width, S->n * S->width)))) return rc;
+	if (!*r_sorted && (rc = pg_alloc_async(ctx, s, (void**) &pR, R->n * R->width))) return rc;
+	if (!*s_sorted && (rc = pg_alloc_async(ctx, s, (void**) &pS, S->n * S->width))) return rc;
+	if (npass == 2 && !(*r_sorted && *s_sorted) &&
+			(rc = pg_alloc_async(ctx, s, (void**) &tmp, std::max(R->n * R->width, S->n * S->width)))) return rc;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &oR, (B + 1) * 8))) return rc;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &oS, (B + 1) * 8))) return rc;
 	if (materialize && (rc = pg_alloc_async(ctx, s, (void**) &brows, (B + 1) * 8))) return rc;
+	const char* bR = *r_sorted ? (const char*) R->data : pR;   // each side in bucket order
+	const char* bS = *s_sorted ? (const char*) S->data : pS;
 	for (int side = 0; side < 2; ++side) {
 		const pg_rel* in = side ? S : R;
 		char* dst = side ? pS : pR;
 		pg_rel cur = *in;
-		for (int p = 0; p < npass; ++p) {
+		const bool sorted = side ? *s_sorted : *r_sorted;
+		for (int p = 0; p < npass && !sorted; ++p) {
 			const int d = p == 0 ? d0 : hb - d0;
 			pg_hashfn f;
 			f.fn = PG_FN_PARAMMODULO;
@@ -655,15 +675,15 @@ static int mj_bucket_join(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, const pg
 			if ((rc = pg_partition_fn(ctx, s, &cur, f, o, nullptr))) return rc;
 			cur.data = o;
 		}
-		k_mj_bounds<<<(B + 256) / 256, 256, 0, s>>>(dst, in->n, in->width, in->key_off, in->key_bytes, kmin, B,
-				side ? oS : oR);
+		k_mj_bounds<<<(B + 256) / 256, 256, 0, s>>>(side ? bS : bR, in->n, in->width, in->key_off, in->key_bytes,
+				kmin, B, side ? oS : oR);
 		PG_LAUNCHED(ctx);
 	}
 	PG_CUDA(ctx, cudaMemsetAsync(mm + 2, 0, 24, s));
 	const int sum_side = sum_col < 0 ? -1 : (int) pc.side[sum_col];
 	const size_t smem = MJ_LOCAL * (8 + 4 + 4);
 	PG_CUDA(ctx, cudaFuncSetAttribute(k_mj_bucket_join, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
-	k_mj_bucket_join<<<B, 256, smem, s>>>(pR, oR, R->width, R->key_off, R->key_bytes, pS, oS, S->width, S->key_off,
+	k_mj_bucket_join<<<B, 256, smem, s>>>(bR, oR, R->width, R->key_off, R->key_bytes, bS, oS, S->width, S->key_off,
 			S->key_bytes, kmin, sum_side, sum_col >= 0 ? pc.off[sum_col] : 0, sum_col >= 0 ? pc.words[sum_col] : 0,
 			mm + 2, brows);
 	PG_LAUNCHED(ctx);
@@ -686,8 +706,8 @@ static int mj_bucket_join(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, const pg
 		}
 		const size_t wsmem = MJW_CAP * 8 + (2 * MJ_LOCAL + 1) * 4 + (MJW_THREADS / 32) * 4;
 		PG_CUDA(ctx, cudaFuncSetAttribute(k_mj_bucket_write, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) wsmem));
-		k_mj_bucket_write<<<B, MJW_THREADS, wsmem, s>>>(reinterpret_cast<const uint4*>(pR), oR, R->key_off / 4, bp,
-				reinterpret_cast<const uint4*>(pS), oS, S->key_off / 4, kmin, brows, wsel,
+		k_mj_bucket_write<<<B, MJW_THREADS, wsmem, s>>>(reinterpret_cast<const uint4*>(bR), oR, R->key_off / 4, bp,
+				reinterpret_cast<const uint4*>(bS), oS, S->key_off / 4, kmin, brows, wsel,
 				reinterpret_cast<uint4*>(out), ctx->d_status);
 		PG_LAUNCHED(ctx);
 		rc = pg_check_status(ctx, s, "pg_mpsm_join");
@@ -724,14 +744,21 @@ extern "C" int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, cons
 	if (R->n == 0 || S->n == 0) return PG_OK;
 	cudaStream_t s = (cudaStream_t) stream;
 	int rc;
+	bool r_sorted = false, s_sorted = false;   // confirmed on the device
 	if (R->n < (1ull << 32) && S->n < (1ull << 32)) {
 		bool handled = false;
-		if ((rc = mj_bucket_join(ctx, s, R, S, pc, sum_col, materialize, out, out_capacity, res, &handled))) return rc;
+		if ((rc = mj_bucket_join(ctx, s, R, S, pc, sum_col, flags, out, out_capacity, res, &handled, &r_sorted,
+				&s_sorted))) return rc;
 		if (handled) return PG_OK;
 	}
+	// A sorted 16-byte tuple keyed at offset 0 is its own sorted record array.
 	pg_rec *rr = nullptr, *sr = nullptr;
-	if ((rc = pg_sort_records(ctx, s, R, &rr))) return rc;
-	if ((rc = pg_sort_records(ctx, s, S, &sr))) return rc;
+	const bool r_own = !(r_sorted && pg_sort_mode(R) == 0 && !(reinterpret_cast<uintptr_t>(R->data) & 15));
+	const bool s_own = !(s_sorted && pg_sort_mode(S) == 0 && !(reinterpret_cast<uintptr_t>(S->data) & 15));
+	if (r_own) { if ((rc = pg_sort_records(ctx, s, R, &rr))) return rc; }
+	else rr = (pg_rec*) R->data;
+	if (s_own) { if ((rc = pg_sort_records(ctx, s, S, &sr))) return rc; }
+	else sr = (pg_rec*) S->data;
 	MjSide RS{rr, (const char*) R->data, R->width, R->key_off, pg_sort_mode(R), nullptr, 0};
 	MjSide SS{sr, (const char*) S->data, S->width, S->key_off, pg_sort_mode(S), nullptr, 0};
 	uint64_t *rst = nullptr, *sst = nullptr;
@@ -766,8 +793,8 @@ extern "C" int pg_mpsm_join(pg_ctx* ctx, pg_stream stream, const pg_rel* R, cons
 			rc = pg_check_status(ctx, s, "pg_mpsm_join");
 		}
 	}
-	for (void* p : {(void*) rr, (void*) sr, (void*) rst, (void*) sst, (void*) rk, (void*) sk, (void*) counts,
-			(void*) match, (void*) acc})
+	for (void* p : {r_own ? (void*) rr : nullptr, s_own ? (void*) sr : nullptr, (void*) rst, (void*) sst, (void*) rk,
+			(void*) sk, (void*) counts, (void*) match, (void*) acc})
 		pg_free_async(ctx, s, p);
 	return rc;
 }

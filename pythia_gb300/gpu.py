@@ -15,6 +15,7 @@ _LIB = None
 PG_OK, PG_ERR_ARG, PG_ERR_OOM, PG_ERR_CUDA, PG_ERR_TIMEOUT = 0, 1, 2, 3, 4
 PG_ERR_TABLE_FULL, PG_ERR_OUTPUT_FULL, PG_ERR_UNSUPPORTED = 5, 6, 7
 JOIN_MATERIALIZE, JOIN_COUNT, JOIN_SUM = 1, 2, 4
+JOIN_BUILD_SORTED, JOIN_PROBE_SORTED = 8, 16       # pg_mpsm_join: that side is sorted on its key
 FN = {"bytes": 0, "modulo": 1, "range": 2, "exactrange": 3, "parammodulo": 4,
       "knuth": 5, "tpchorderkey": 6, "willis": 7, "alwayszero": 8, "tpchq1magic": 9}
 VAL = {"int": 0, "long": 1, "dec": 2}

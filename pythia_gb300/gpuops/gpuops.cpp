@@ -874,23 +874,40 @@ int GpuHashJoinOp::run_device_spans(pg_ctx* ctx, pg_stream st, const pg_rel& R, 
 	return PG_OK;
 }
 
+void GpuMPSMJoinOp::init(libconfig::Config& root, libconfig::Setting& node)
+{
+	GpuJoinBase::init(root, node);
+	std::string v;
+	sorted_flags_ = 0;
+	if (node.lookupValue("buildpresorted", v) && v == "yes") sorted_flags_ |= PG_JOIN_BUILD_SORTED;
+	if (node.lookupValue("probepresorted", v) && v == "yes") sorted_flags_ |= PG_JOIN_PROBE_SORTED;
+}
+
 int GpuMPSMJoinOp::run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
 		unsigned long long* rows)
 {
 	const unsigned ow = schema.getTupleSize();
 	pg_join_result res;
 	res.n_out = 0; res.sum = 0;
-	// Count first (exact output size), then write.
-	int rc = pg_mpsm_join(ctx, st, &R, &S, &cols_[0], (int) cols_.size(), 0, 0, PG_JOIN_COUNT, -1, &res);
-	if (rc) return rc;
-	const unsigned long long n = res.n_out;
-	void* o = 0;
-	if ((rc = pg_buffer_alloc_async(ctx, st, std::max<unsigned long long>(n, 1) * ow, &o))) return rc;
-	if (n) rc = pg_mpsm_join(ctx, st, &R, &S, &cols_[0], (int) cols_.size(), o, n, PG_JOIN_MATERIALIZE, -1, &res);
-	if (rc) { pg_buffer_free_async(ctx, st, o); return rc; }
-	*out = o;
-	*rows = n;
-	return PG_OK;
+	// Room for |R| + |S| rows first (a PK-FK join's output); a join that needs
+	// more reports its size and runs again into a buffer of exactly that.
+	unsigned long long cap = std::max<unsigned long long>(R.n + S.n, 1);
+	for (int attempt = 0; attempt < 2; ++attempt) {
+		void* o = 0;
+		int rc = pg_buffer_alloc_async(ctx, st, cap * ow, &o);
+		if (rc) return rc;
+		rc = pg_mpsm_join(ctx, st, &R, &S, &cols_[0], (int) cols_.size(), o, cap,
+				PG_JOIN_MATERIALIZE | sorted_flags_, -1, &res);
+		if (rc == PG_OK) {
+			*out = o;
+			*rows = res.n_out;
+			return PG_OK;
+		}
+		pg_buffer_free_async(ctx, st, o);
+		if (rc != PG_ERR_OUTPUT_FULL || attempt) return rc;
+		cap = std::max<unsigned long long>(res.n_out, 1);
+	}
+	return PG_ERR_OUTPUT_FULL;
 }
 
 // ---------------------------------------------------------------------------

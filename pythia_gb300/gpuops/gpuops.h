@@ -275,12 +275,23 @@ protected:
 };
 
 // "gpumpsmjoin": OldMPSMJoinOp / MPSMJoinOp keys (join.cpp:677-783,
-// 1383-1538): projection, buildjattr, probejattr, threadgroups; the run-size
-// and presorted keys are read and have no effect on the result.
+// 1383-1538): projection, buildjattr, probejattr, threadgroups, and
+// buildpresorted / probepresorted = "yes" (join.cpp:750-762): the device
+// confirms that the group's input on that side is sorted and then skips its
+// sort or partition. maxbuildtuples[inM] / maxprobetuples[inM] size the CPU
+// operator's staging runs, mostfreqbuildkeyoccurances its per-key buffer and
+// buildprepartitioned the key range each CPU thread merges: device memory
+// is sized from the inputs and any multiplicity is joined, so they are read
+// and change nothing, the result included.
 class GpuMPSMJoinOp : public GpuJoinBase {
+public:
+	GpuMPSMJoinOp() : sorted_flags_(0) { }
+	virtual void init(libconfig::Config& root, libconfig::Setting& node);
 protected:
 	virtual int run_device(pg_ctx* ctx, pg_stream st, const pg_rel& R, const pg_rel& S, void** out,
 			unsigned long long* rows);
+private:
+	int sorted_flags_;          // PG_JOIN_BUILD_SORTED / PG_JOIN_PROBE_SORTED
 };
 
 // "gpupartition": PartitionOp (operators/partition.cpp:45-404): `attr`,

@@ -830,6 +830,26 @@ def test_mpsm_materialised_bucket_too_large_for_shared_memory(ctx):
     _mpsm_check(ctx, R, S)
 
 
+@pytest.mark.parametrize("span", [1 << 20, 1 << 40])
+def test_mpsm_presorted_sides(ctx, span):
+    # buildpresorted / probepresorted: a side the device confirms sorted skips
+    # its partition (key spans up to 2^24) or its sort (wider spans); a side
+    # flagged sorted that is not must still join correctly.
+    R = dg.uniform_keys(200_000, span, dg.seed_for(98))
+    S = dg.uniform_keys(300_000, span, dg.seed_for(99))
+    S[::7, 0] = R[::7, 0][: S[::7].shape[0]]          # some matches at the wide span
+    Rs = R[np.argsort(R[:, 0], kind="stable")]
+    Ss = S[np.argsort(S[:, 0], kind="stable")]
+    want, wn, _ = orc.mergejoin(R, S)
+    both = gpu.JOIN_MATERIALIZE | gpu.JOIN_BUILD_SORTED | gpu.JOIN_PROBE_SORTED
+    for r, s_, fl in ((Rs, Ss, both), (Rs, S, both), (R, Ss, both), (Rs, Ss, gpu.JOIN_MATERIALIZE)):
+        got, n, _ = ctx.mpsm(r, s_, flags=fl)
+        assert n == wn
+        assert np.array_equal(canon(got), canon(want))
+        _, n2, s2 = ctx.mpsm(r, s_, flags=(fl & ~gpu.JOIN_MATERIALIZE) | gpu.JOIN_COUNT | gpu.JOIN_SUM, sum_col=1)
+        assert (n2, s2) == orc.mergejoin(R, S, materialise=False, sum_col=1)[1:]
+
+
 def test_mpsm_duplicates(ctx):
     R = dg.uniform_keys(50_000, 12_500, dg.seed_for(70))
     S = dg.uniform_keys(50_000, 12_500, dg.seed_for(71))

@@ -66,6 +66,28 @@ def test_join_two_groups_join_their_own_inputs(jtype):
     assert np.array_equal(canon(rows[g0:]), canon(halves[1]))
 
 
+@pytest.mark.parametrize("sort_r,sort_s", [(True, True), (True, False)])
+def test_mpsm_plan_presorted_keys(sort_r, sort_s):
+    # buildpresorted / probepresorted = "yes" (join.cpp:750-762) on a
+    # gpumpsmjoin: sorted relations skip the device's sort or partition; a
+    # side declared sorted that is not (sort_s False: S shuffled) still joins
+    # right. The run-size, buffer and range keys are accepted and change
+    # nothing.
+    R = dg.uniform_keys(40_000, 1 << 18, dg.seed_for(75))
+    S = dg.uniform_keys(90_000, 1 << 18, dg.seed_for(76))
+    if sort_r:
+        R = R[np.argsort(R[:, 0], kind="stable")]
+    if sort_s:
+        S = S[np.argsort(S[:, 0], kind="stable")]
+    plans.register("R", R); plans.register("S", S)
+    extra = ('buildpresorted = "yes"; probepresorted = "yes"; maxbuildtuplesinM = 1; maxprobetuplesinM = 1; '
+             'mostfreqbuildkeyoccurances = 16; buildprepartitioned = { range = [0, 262143]; buckets = 2; };')
+    rows, per = plans.run(join_plan("gpumpsmjoin", "((0, 1))", extra=extra), threads=2)
+    want, n, _ = orc.mergejoin(R, S)
+    assert rows.shape == (n, 16) and sum(per) == n
+    assert np.array_equal(canon(rows), canon(want))
+
+
 def test_hashjoin_reference_unit_scenario():
     # The reference's hash join test: build keys 1..20 with payload k + 0.1
     # (dec), probe keys 1..20 (int-valued long payload), projection
