@@ -179,13 +179,37 @@ __device__ __forceinline__ uint32_t hj_word4(const uint4& t, uint32_t i)
 	return i == 0 ? t.x : i == 1 ? t.y : i == 2 ? t.z : t.w;
 }
 
+// The packed value's word positions in a 16-byte tuple as one word for the
+// kernels of the device-side build: bits 0-1 the number of words (0..2),
+// bits 2-3 and 4-5 the tuple words (a structure parameter indexed at run
+// time would be copied to local memory).
+static uint32_t hj_pack16_code(const HjBuildCols& bc)
+{
+	uint32_t code = 0, o = 0;
+	for (int c = 0; c < bc.n; ++c)
+		for (int j = 0; j < bc.words[c] && o < 2; ++j, ++o) code |= (uint32_t) ((bc.roff[c] + j) & 3) << (2 + 2 * o);
+	return code | o;
+}
+
+__device__ __forceinline__ uint64_t hj_pack16(const uint4& t, uint32_t code)
+{
+	const uint32_t nw = code & 3;
+	uint64_t v = 0;
+	if (nw > 0) v = hj_word4(t, (code >> 2) & 3);
+	if (nw > 1) v |= (uint64_t) hj_word4(t, (code >> 4) & 3) << 32;
+	return v;
+}
+
+// (At most two words: packed values are 8 bytes or less. Built by shifts,
+// not an indexed array, so nothing goes to local memory.)
 __device__ __forceinline__ uint64_t hj_pack_value16(const uint4& t, const HjBuildCols& bc)
 {
-	uint32_t w[2] = {0, 0};
-	int o = 0;
+	uint64_t v = 0;
+	uint32_t o = 0;
 	for (int c = 0; c < bc.n; ++c)
-		for (int j = 0; j < bc.words[c]; ++j) w[o++] = hj_word4(t, bc.roff[c] + j);
-	return ((uint64_t) w[1] << 32) | w[0];
+		for (int j = 0; j < bc.words[c]; ++j, ++o)
+			if (o < 2) v |= (uint64_t) hj_word4(t, bc.roff[c] + j) << (32 * o);
+	return v;
 }
 
 __global__ void k_key_minmax16(const uint4* __restrict__ R, uint64_t n, uint32_t kw, HjBuildCols bc,
@@ -285,7 +309,7 @@ __device__ __forceinline__ void hj_minmax4(unsigned long long& lo, unsigned long
 // when every tuple was sampled), and the value base: 0 when the sampled
 // values leave room for it, else centred on them. `cap` = entries allocated.
 __global__ void __launch_bounds__(1024) k_dense_prep16(const uint4* __restrict__ R, uint64_t n, uint32_t kw,
-		HjBuildCols bc, uint64_t cap, HjDenseHdr* __restrict__ hdr)
+		uint32_t pk, uint64_t cap, HjDenseHdr* __restrict__ hdr)
 {
 	__shared__ unsigned long long red[4][32];
 	const uint64_t m = n < HJ_SPEC_SAMPLE ? n : HJ_SPEC_SAMPLE;
@@ -295,7 +319,7 @@ __global__ void __launch_bounds__(1024) k_dense_prep16(const uint4* __restrict__
 		const uint64_t i = t * q + (t * r) / m;      // < n: t < m, t*r < 2^24
 		const uint4 v = __ldg(R + i);
 		const unsigned long long k = (((unsigned long long) hj_word4(v, kw + 1) << 32) | hj_word4(v, kw)) ^ (1ull << 63);
-		const unsigned long long p = hj_pack_value16(v, bc);
+		const unsigned long long p = hj_pack16(v, pk);
 		lo = k < lo ? k : lo; hi = k > hi ? k : hi;
 		vlo = p < vlo ? p : vlo; vhi = p > vhi ? p : vhi;
 	}
@@ -345,67 +369,70 @@ __global__ void k_dense_fill16(uint32_t* __restrict__ table, const HjDenseHdr* _
 }
 
 // Store pass: entry key - dmin = value - vmin, plain stores kept in L2
-// (evict-last measured fastest for the scattered 4-byte stores); records the
-// exact key and value ranges, and flags keys and values the window misses.
-__global__ void k_dense32_spec16(const uint4* __restrict__ R, uint64_t n, uint32_t kw, HjBuildCols bc,
-		uint32_t* __restrict__ table, HjDenseHdr* __restrict__ hdr)
+// (evict-last measured fastest for the scattered 4-byte stores), eight build
+// tuples in flight per thread read evict-first; flags keys outside the window
+// and values outside the entry range.
+__global__ void __launch_bounds__(256) k_dense32_spec16(const uint4* __restrict__ R, uint64_t n, uint32_t kw,
+		uint32_t pk, uint32_t* __restrict__ table, HjDenseHdr* __restrict__ hdr)
 {
 	if (hdr->flags) return;
 	const unsigned long long dmin = (unsigned long long) hdr->dmin, range = hdr->drange, vmin = hdr->vmin;
-	const uint64_t keep = pg_policy_evict_last();
-	unsigned long long lo = ~0ull, hi = 0, vlo = ~0ull, vhi = 0;
+	const uint64_t keep = pg_policy_evict_last(), stream = pg_policy_evict_first();
 	int bad = 0;
 	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
-	for (uint64_t i0 = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
-		uint4 t[4];
+	for (uint64_t i0 = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i0 < n; i0 += 8 * stride) {
+		uint4 t[8];
 		#pragma unroll
-		for (int u = 0; u < 4; ++u) if (i0 + u * stride < n) t[u] = __ldg(R + i0 + u * stride);
+		for (int u = 0; u < 8; ++u)
+			if (i0 + u * stride < n) t[u] = pg_ld_hint16(R + i0 + u * stride, stream);
 		#pragma unroll
-		for (int u = 0; u < 4; ++u) {
+		for (int u = 0; u < 8; ++u) {
 			if (i0 + u * stride >= n) break;
 			const unsigned long long key = ((unsigned long long) hj_word4(t[u], kw + 1) << 32) | hj_word4(t[u], kw);
-			const unsigned long long v = hj_pack_value16(t[u], bc);
-			const unsigned long long ko = key ^ (1ull << 63);
-			lo = ko < lo ? ko : lo; hi = ko > hi ? ko : hi;
-			vlo = v < vlo ? v : vlo; vhi = v > vhi ? v : vhi;
-			const unsigned long long d = key - dmin, e = v - vmin;
+			const unsigned long long d = key - dmin, e = hj_pack16(t[u], pk) - vmin;
 			if (d >= range) bad |= 1;
 			else if (e >= 0xFFFFFFFFull) bad |= 2;
 			else asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;"
 					:: "l"(table + d), "r"((uint32_t) e), "l"(keep) : "memory");
 		}
 	}
-	hj_minmax4(lo, hi, vlo, vhi);
 	#pragma unroll
 	for (int o = 16; o > 0; o >>= 1) bad |= __shfl_down_sync(0xffffffffu, bad, o);
-	if ((threadIdx.x & 31) == 0) {
-		if (lo <= hi) {
-			atomicMin(&hdr->kmin, lo); atomicMax(&hdr->kmax, hi);
-			atomicMin(&hdr->vlo, vlo); atomicMax(&hdr->vhi, vhi);
-		}
-		if (bad) atomicOr(&hdr->flags, bad);
-	}
+	if ((threadIdx.x & 31) == 0 && bad) atomicOr(&hdr->flags, bad);
 }
 
 // Count pass: present entries of the window into hdr->present (equal to n
-// exactly when no key repeated).
+// exactly when no key repeated), and the exact key and value ranges from the
+// first and last present entries and the smallest and largest entry.
 __global__ void k_dense32_count_spec(const uint32_t* __restrict__ table, HjDenseHdr* __restrict__ hdr)
 {
 	if (hdr->flags) return;
 	const unsigned long long range = hdr->drange;
-	unsigned long long c = 0;
+	unsigned long long c = 0, dlo = ~0ull, dhi = 0, elo = ~0ull, ehi = 0;
+	auto see = [&](uint32_t e, unsigned long long d) {
+		if (e == 0xFFFFFFFFu) return;
+		++c;
+		dlo = d < dlo ? d : dlo; dhi = d > dhi ? d : dhi;
+		elo = e < elo ? e : elo; ehi = e > ehi ? e : ehi;
+	};
 	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
 	const uint64_t n4 = range / 4;
 	const uint4* t4 = reinterpret_cast<const uint4*>(table);
 	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n4; i += stride) {
 		const uint4 v = t4[i];
-		c += (v.x != 0xFFFFFFFFu) + (v.y != 0xFFFFFFFFu) + (v.z != 0xFFFFFFFFu) + (v.w != 0xFFFFFFFFu);
+		see(v.x, 4 * i); see(v.y, 4 * i + 1); see(v.z, 4 * i + 2); see(v.w, 4 * i + 3);
 	}
 	for (uint64_t i = 4 * n4 + blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < range; i += stride)
-		c += table[i] != 0xFFFFFFFFu;
+		see(table[i], i);
+	hj_minmax4(dlo, dhi, elo, ehi);
 	#pragma unroll
 	for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-	if ((threadIdx.x & 31) == 0 && c) atomicAdd(&hdr->present, c);
+	if ((threadIdx.x & 31) == 0 && c) {
+		const unsigned long long dmin = (unsigned long long) hdr->dmin, vmin = hdr->vmin;
+		atomicAdd(&hdr->present, c);
+		atomicMin(&hdr->kmin, (dmin + dlo) ^ (1ull << 63)); atomicMax(&hdr->kmax, (dmin + dhi) ^ (1ull << 63));
+		atomicMin(&hdr->vlo, vmin + elo); atomicMax(&hdr->vhi, vmin + ehi);
+	}
 }
 
 // Entries of a settled table re-based from the sample's value base to the
@@ -1993,13 +2020,14 @@ static int hj_build_spec(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, pg_hashta
 	ht->dense32 = ht->dense32_base;
 	ht->dmin = 0; ht->drange = cap; ht->vmin = 0; ht->vlo = 0; ht->vmax = 0;     // bounds until settled
 	const uint32_t kw = R->key_off / 4;
-	k_dense_prep16<<<1, 1024, 0, s>>>((const uint4*) R->data, R->n, kw, ht->bcols, cap, ht->hdr);
+	const uint32_t pk = hj_pack16_code(ht->bcols);
+	k_dense_prep16<<<1, 1024, 0, s>>>((const uint4*) R->data, R->n, kw, pk, cap, ht->hdr);
 	PG_LAUNCHED(ctx);
 	const int fgrid = (int) std::min<uint64_t>(pg_div_up(cap / 4 + 1, 256), (uint64_t) ctx->sm_count * 8);
 	k_dense_fill16<<<fgrid, 256, 0, s>>>(ht->dense32_base, ht->hdr);
 	PG_LAUNCHED(ctx);
 	const int sgrid = (int) std::min<uint64_t>(pg_div_up(R->n, 4 * 256), (uint64_t) ctx->sm_count * 16);
-	k_dense32_spec16<<<sgrid, 256, 0, s>>>((const uint4*) R->data, R->n, kw, ht->bcols, ht->dense32_base, ht->hdr);
+	k_dense32_spec16<<<sgrid, 256, 0, s>>>((const uint4*) R->data, R->n, kw, pk, ht->dense32_base, ht->hdr);
 	PG_LAUNCHED(ctx);
 	k_dense32_count_spec<<<fgrid, 256, 0, s>>>(ht->dense32_base, ht->hdr);
 	PG_LAUNCHED(ctx);
