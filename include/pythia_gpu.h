@@ -174,7 +174,10 @@ enum {
 	                                    PG_ERR_TIMEOUT (the copy is still waited for, so the kernel ends
 	                                    cleanly): 0 the built-in limit (2^26 blocking polls), else that many
 	                                    non-blocking polls */
-	PG_TUNE_COUNT = 13
+	PG_TUNE_L2_FETCH = 13,           /* L2 fetch granularity hint of the context in bytes: 0 leaves the CUDA
+	                                    default, else 32, 64 or 128 (cudaLimitMaxL2FetchGranularity, a limit of
+	                                    the calling process that ends with it) */
+	PG_TUNE_COUNT = 14
 };
 int pg_tune_set(pg_ctx* ctx, int knob, int64_t value);
 int64_t pg_tune_get(pg_ctx* ctx, int knob);

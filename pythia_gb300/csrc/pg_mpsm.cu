@@ -420,7 +420,7 @@ __global__ void k_mj_minmax(const char* __restrict__ in, uint64_t n, uint32_t W,
 // bucket order; within a bucket their order is unspecified (as for every
 // join output).
 // ---------------------------------------------------------------------------
-#define MJW_THREADS 512
+#define MJW_THREADS 1024
 #define MJW_CAP 24576            // build tuples of one bucket held in shared memory (192 KB)
 
 // The build-projected words of a row that are not the join key, packed.
@@ -497,7 +497,7 @@ k_mj_bucket_write(const uint4* __restrict__ R, const uint64_t* __restrict__ roff
 	}
 	__syncthreads();
 	{
-		constexpr uint32_t PER = MJ_LOCAL / MJW_THREADS;        // 8 entries per thread
+		constexpr uint32_t PER = MJ_LOCAL / MJW_THREADS;        // 4 entries per thread
 		uint32_t v[PER], run = 0;
 		#pragma unroll
 		for (uint32_t j = 0; j < PER; ++j) { v[j] = start[tid * PER + j]; run += v[j]; }
@@ -519,27 +519,46 @@ k_mj_bucket_write(const uint4* __restrict__ R, const uint64_t* __restrict__ roff
 		rv[pos] = pv;
 	}
 	__syncthreads();
-	// Probe side in chunks of MJW_THREADS tuples: tuple i makes one row per
-	// build tuple of its key, at the chunk's running offset.
+	// Probe side in chunks of MJW_THREADS tuples, the next chunk's tuples
+	// loaded while the current one is written. Tuple i of a chunk makes m_i
+	// rows (one per build tuple of its key) at its scanned offset; the rows are
+	// written load-balanced, thread j of the CTA taking the chunk's rows j,
+	// j + MJW_THREADS, ..., so a warp stores 32 consecutive rows whatever the
+	// duplicates. A row finds its probe tuple by binary search over the
+	// offsets, which reuse the fill counters' shared memory (dead after the
+	// build side).
+	uint32_t* coff = fill;                                                       // [MJW_THREADS]
+	uint32_t* crs = fill + MJW_THREADS;                                          // [MJW_THREADS]
 	const uint32_t w0 = wsel & 15, w1 = (wsel >> 4) & 15, w2 = (wsel >> 8) & 15, w3 = (wsel >> 12) & 15;
 	uint64_t row = bucket_off[b];
+	uint4 tn = make_uint4(0, 0, 0, 0);
+	if (s0 + tid < s1) tn = S[s0 + tid];
 	for (uint64_t c0 = s0; c0 < s1; c0 += MJW_THREADS) {
+		const uint4 t = tn;
 		const uint64_t i = c0 + tid;
-		uint4 t = make_uint4(0, 0, 0, 0);
+		if (i + MJW_THREADS < s1) tn = S[i + MJW_THREADS];
 		uint32_t m = 0, rs = 0;
 		if (i < s1) {
-			t = S[i];
 			const unsigned long long key = ((unsigned long long) mjw_word(t, skw + 1) << 32) | mjw_word(t, skw);
 			const uint32_t k = (uint32_t) ((key - kbase) & (MJ_LOCAL - 1));
 			rs = start[k];
 			m = start[k + 1] - rs;
 		}
 		uint32_t total;
+		// The scan's barriers also order this chunk's offset writes after
+		// every thread's reads of the previous chunk's offsets.
 		const uint32_t off = mjw_block_scan(m, wsum, &total);
-		uint4* o = out + row + off;
-		for (uint32_t r = 0; r < m; ++r) {
-			const unsigned long long v = rv[rs + r];
-			o[r] = make_uint4(mjw_pick(t, v, w0), mjw_pick(t, v, w1), mjw_pick(t, v, w2), mjw_pick(t, v, w3));
+		coff[tid] = off;
+		crs[tid] = rs;
+		__syncthreads();
+		for (uint32_t j = tid; j < total; j += MJW_THREADS) {
+			uint32_t x = 0;                  // the last tuple whose offset is <= j (it has m > 0)
+			#pragma unroll
+			for (uint32_t step = MJW_THREADS / 2; step; step >>= 1)
+				if (coff[x + step] <= j) x += step;
+			const unsigned long long v = rv[crs[x] + (j - coff[x])];
+			const uint4 p = S[c0 + x];
+			out[row + j] = make_uint4(mjw_pick(p, v, w0), mjw_pick(p, v, w1), mjw_pick(p, v, w2), mjw_pick(p, v, w3));
 		}
 		row += total;
 	}

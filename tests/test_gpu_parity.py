@@ -837,7 +837,8 @@ def test_mpsm_presorted_sides(ctx, span):
     # flagged sorted that is not must still join correctly.
     R = dg.uniform_keys(200_000, span, dg.seed_for(98))
     S = dg.uniform_keys(300_000, span, dg.seed_for(99))
-    S[::7, 0] = R[::7, 0][: S[::7].shape[0]]          # some matches at the wide span
+    m = R[::7].shape[0]
+    S[: 7 * m : 7, 0] = R[::7, 0]                     # some matches at the wide span
     Rs = R[np.argsort(R[:, 0], kind="stable")]
     Ss = S[np.argsort(S[:, 0], kind="stable")]
     want, wn, _ = orc.mergejoin(R, S)
