@@ -37,6 +37,14 @@ extern "C" int pg_tune_set(pg_ctx* ctx, int knob, int64_t value)
 		const uint32_t v = (uint32_t) std::min<int64_t>(value, (int64_t) PG_SPIN_LIMIT);
 		PG_CUDA(ctx, cudaMemcpy(ctx->d_status + 1, &v, sizeof v, cudaMemcpyHostToDevice));
 	}
+	if (knob == PG_TUNE_L2_FETCH && value) {
+		// A hint of how many bytes an L2 miss fetches from DRAM; random 32-byte
+		// bucket reads of a table larger than L2 want the smallest.
+		if (value != 32 && value != 64 && value != 128)
+			return pg_fail(ctx, PG_ERR_ARG, "pg_tune_set: L2 fetch granularity must be 32, 64 or 128");
+		PG_CUDA(ctx, cudaSetDevice(ctx->device));
+		PG_CUDA(ctx, cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t) value));
+	}
 	return PG_OK;
 }
 
@@ -513,10 +521,4 @@ int pg_scan_u64(pg_ctx* ctx, cudaStream_t s, uint64_t* data, uint64_t n, uint64_
 		pg_free_async(ctx, s, last);
 	}
 	return PG_OK;
-}
-
-__global__ void k_fill_u64(unsigned long long* p, uint64_t n, unsigned long long v)
-{
-	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
-		p[i] = v;
 }

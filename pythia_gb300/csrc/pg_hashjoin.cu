@@ -2837,15 +2837,17 @@ extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
 // AggregateCount: join.cpp:503-562 with genericaggregate.cpp:240-282). The
 // group key is the table's value (the one projected build column); a narrow
 // dense table stores value - vmin, which is the row's group slot directly. The
-// probe-side value is folded into a dense group table with the compensated
-// atomics of the group-by (one atomic on hi whose old value gives the exact
-// rounding error, one on lo), so the join rows are never written.
+// probe-side value is folded into a dense group table with the atomics of the
+// group-by (a dec value as an exact count of units 2^s in three words: for a
+// value near the column's largest, one returning atomic and one plain), so
+// the join rows are never written.
 // ---------------------------------------------------------------------------
 template <int VT, int AGG>
 __global__ void __launch_bounds__(PW_WARPS * 32, 4)
 k_probe16_groupby(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb, uint32_t voff,
-		uint32_t goff, unsigned long long* __restrict__ acc, double* __restrict__ lo, unsigned char* __restrict__ present)
+		uint32_t goff, unsigned long long* __restrict__ acc, PgFx fx, unsigned char* __restrict__ present)
 {
+	constexpr bool DEC = AGG == PG_AGG_SUM && VT == PG_VAL_DEC;
 	constexpr int ITEMS = PW_CHUNK / 32;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
@@ -2854,6 +2856,8 @@ k_probe16_groupby(const char* __restrict__ S, uint64_t n, uint32_t koff, const H
 	const uint64_t keep = pg_policy_evict_last();
 	const uint64_t instream = pg_policy_evict_first();
 	if (first >= nchunks) return;
+	const int fs = DEC ? fx.p[0] : 0, fb = DEC ? fx.p[1] : 0;
+	uint32_t fl = 0;
 	uint4 cur[ITEMS], nxt[ITEMS];
 	auto load = [&](uint64_t c, uint4 (&t)[ITEMS]) {
 		const uint32_t rows = (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK);
@@ -2879,21 +2883,35 @@ k_probe16_groupby(const char* __restrict__ S, uint64_t n, uint32_t koff, const H
 						: "=r"(e[j]) : "l"(tb.dense32 + d), "l"(keep));
 			if (e[j] != 0xFFFFFFFFu) e[j] -= goff;      // group slot: value - smallest value
 		}
-		if (AGG == PG_AGG_SUM && VT == PG_VAL_DEC) {
-			double v[ITEMS], old[ITEMS];
+		if (DEC) {
+			// PG_FX_SLOT words per group; each word's adds for all items before
+			// the next word's, carries from the returned old words.
+			pg_fx3 f[ITEMS];
+			uint64_t c[ITEMS], x1[ITEMS];
+			unsigned long long o[ITEMS];
 			#pragma unroll
 			for (int j = 0; j < ITEMS; ++j) {
 				const uint4 t = cur[j];
-				v[j] = __longlong_as_double((long long) (voff == 0 ? (((uint64_t) t.y << 32) | t.x) : (((uint64_t) t.w << 32) | t.z)));
-				if (e[j] != 0xFFFFFFFFu) old[j] = atomicAdd(reinterpret_cast<double*>(&acc[2 * (uint64_t) e[j]]), v[j]);
+				f[j] = pg_fx3{0, 0, 0}; c[j] = 0;
+				if (e[j] == 0xFFFFFFFFu) continue;
+				f[j] = pg_fx_take(voff == 0 ? (((uint64_t) t.y << 32) | t.x) : (((uint64_t) t.w << 32) | t.z), fs, fb, fl);
+				if (f[j].w0) {
+					const unsigned long long old = atomicAdd(&acc[PG_FX_SLOT * (uint64_t) e[j]], (unsigned long long) f[j].w0);
+					c[j] = (uint64_t) (old + f[j].w0) < (uint64_t) old;
+				}
+			}
+			#pragma unroll
+			for (int j = 0; j < ITEMS; ++j) {
+				x1[j] = f[j].w1 + c[j];
+				c[j] = x1[j] < c[j];
+				o[j] = e[j] != 0xFFFFFFFFu && x1[j] ? atomicAdd(&acc[PG_FX_SLOT * (uint64_t) e[j] + 1], (unsigned long long) x1[j]) : 0;
 			}
 			#pragma unroll
 			for (int j = 0; j < ITEMS; ++j) {
 				if (e[j] == 0xFFFFFFFFu) continue;
-				const double err = pg_add_err(old[j], v[j]);
-				if (nonzero(err)) atomicAdd(reinterpret_cast<double*>(&acc[2 * (uint64_t) e[j] + 1]), err);
-				// Sums start at -0.0: the add that returns it is the group's first.
-				if ((unsigned long long) __double_as_longlong(old[j]) == PG_NEG_ZERO) present[e[j]] = 1;
+				const uint64_t x2 = f[j].w2 + c[j] + ((uint64_t) (o[j] + x1[j]) < (uint64_t) o[j]);
+				if (x2) atomicAdd(&acc[PG_FX_SLOT * (uint64_t) e[j] + 2], (unsigned long long) x2);
+				present[e[j]] = 1;
 			}
 		} else {
 			#pragma unroll
@@ -2911,6 +2929,7 @@ k_probe16_groupby(const char* __restrict__ S, uint64_t n, uint32_t koff, const H
 		#pragma unroll
 		for (int j = 0; j < ITEMS; ++j) cur[j] = nxt[j];
 	}
+	if (fl) atomicOr(reinterpret_cast<unsigned int*>(fx.p + 2), fl);
 }
 
 extern "C" int pg_hashjoin_groupby(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht, const pg_rel* S,
@@ -2935,40 +2954,52 @@ extern "C" int pg_hashjoin_groupby(pg_ctx* ctx, pg_stream stream, pg_hashtable* 
 		return pg_fail(ctx, PG_ERR_UNSUPPORTED, "pg_hashjoin_groupby: needs a narrow dense table with one build "
 				"column of compact range and 16-byte probe tuples");
 	cudaStream_t s = (cudaStream_t) stream;
+	const bool dec = agg == PG_AGG_SUM && val_type == PG_VAL_DEC;
 	char* mem = nullptr;
-	const size_t bytes = vrange * 17 + 64;
+	const uint64_t words = vrange * (dec ? PG_FX_SLOT : 1);
+	const size_t pres_end = (words + 1) * 8 + ((vrange + 15) & ~15ull);
+	const size_t bytes = pres_end + 16;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &mem, bytes))) return rc;
-	unsigned long long* acc = reinterpret_cast<unsigned long long*>(mem);
-	double* lo = reinterpret_cast<double*>(acc + vrange);
-	unsigned long long* cursor = reinterpret_cast<unsigned long long*>(lo + vrange);
+	unsigned long long* acc = reinterpret_cast<unsigned long long*>(mem);   // PG_FX_SLOT words per group for a dec sum
+	unsigned long long* cursor = acc + words;
 	unsigned char* present = reinterpret_cast<unsigned char*>(cursor + 1);
-	PG_CUDA(ctx, cudaMemsetAsync(mem, 0, bytes, s));
-	if (agg == PG_AGG_SUM && val_type == PG_VAL_DEC) {
-		// Interleaved (hi, lo) slots, all words -0.0 (see k_gb_dense).
-		k_fill_u64<<<(int) std::min<uint64_t>(pg_div_up(2 * vrange, 256), (uint64_t) ctx->sm_count * 8), 256, 0, s>>>(
-				acc, 2 * vrange, PG_NEG_ZERO);
-		PG_LAUNCHED(ctx);
-	}
-	if (S->n) {
-		HjProbeTable tb = {};
-		tb.dense32 = ht->dense32; tb.vmin = ht->vmin; tb.dmin = ht->dmin; tb.drange = ht->drange;
-		const int grid = (int) std::min<uint64_t>(pg_div_up(pg_div_up(S->n, PW_CHUNK), PW_WARPS), (uint64_t) ctx->sm_count * 24);
+	PgFx fx = {reinterpret_cast<int*>(mem + pres_end)};
+	// A dec sum's unit: the probe column's largest exponent, from every 1024th
+	// tuple (4x margin) on large inputs; redone exactly if a value lies above.
+	const bool sampled = S->n >= (1ull << 22);
+	for (int pass = 0; pass < 2; ++pass) {
+		PG_CUDA(ctx, cudaMemsetAsync(mem, 0, pres_end, s));
+		if (dec && (rc = pg_fx_prepare(ctx, s, (const char*) S->data, S->n, 16, val_off, pass == 0 && sampled ? 1024 : 1,
+				2, fx))) return rc;
+		if (S->n) {
+			HjProbeTable tb = {};
+			tb.dense32 = ht->dense32; tb.vmin = ht->vmin; tb.dmin = ht->dmin; tb.drange = ht->drange;
+			const int grid = (int) std::min<uint64_t>(pg_div_up(pg_div_up(S->n, PW_CHUNK), PW_WARPS), (uint64_t) ctx->sm_count * 24);
 #define PG_LAUNCH(VT, AGG) k_probe16_groupby<VT, AGG><<<grid, PW_WARPS * 32, 0, s>>>((const char*) S->data, S->n, \
-				S->key_off, tb, val_off, (uint32_t) (ht->vlo - ht->vmin), acc, lo, present)
-		if (agg == PG_AGG_COUNT) PG_LAUNCH(PG_VAL_LONG, PG_AGG_COUNT);
-		else if (val_type == PG_VAL_INT) PG_LAUNCH(PG_VAL_INT, PG_AGG_SUM);
-		else if (val_type == PG_VAL_LONG) PG_LAUNCH(PG_VAL_LONG, PG_AGG_SUM);
-		else PG_LAUNCH(PG_VAL_DEC, PG_AGG_SUM);
+					S->key_off, tb, val_off, (uint32_t) (ht->vlo - ht->vmin), acc, fx, present)
+			if (agg == PG_AGG_COUNT) PG_LAUNCH(PG_VAL_LONG, PG_AGG_COUNT);
+			else if (val_type == PG_VAL_INT) PG_LAUNCH(PG_VAL_INT, PG_AGG_SUM);
+			else if (val_type == PG_VAL_LONG) PG_LAUNCH(PG_VAL_LONG, PG_AGG_SUM);
+			else PG_LAUNCH(PG_VAL_DEC, PG_AGG_SUM);
 #undef PG_LAUNCH
-		PG_LAUNCHED(ctx);
+			PG_LAUNCHED(ctx);
+		}
+		if ((rc = pg_dense_groups_emit(ctx, s, acc, fx, present, vrange, (long long) ht->vlo, gbytes, val_type, agg,
+				out, out_capacity, cursor))) return rc;
+		unsigned long long ng = 0;
+		unsigned int fl = 0;
+		PG_CUDA(ctx, cudaMemcpyAsync(&ng, cursor, 8, cudaMemcpyDeviceToHost, s));
+		if (dec) PG_CUDA(ctx, cudaMemcpyAsync(&fl, fx.p + 2, 4, cudaMemcpyDeviceToHost, s));
+		if ((rc = pg_check_status(ctx, s, "pg_hashjoin_groupby"))) return rc;
+		*ngroups = ng;
+		if ((fl & PG_FX_RANGE) && pass == 0) continue;
+		pg_free_async(ctx, s, mem);
+		if (fl & PG_FX_SPECIALS)
+			return pg_fail(ctx, PG_ERR_UNSUPPORTED, "pg_hashjoin_groupby: infinities or NaNs in the summed column "
+					"(probe, then pg_groupby)");
+		if (ng > out_capacity) return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_hashjoin_groupby: output capacity too small");
+		return PG_OK;
 	}
-	if ((rc = pg_dense_groups_emit(ctx, s, acc, lo, present, vrange, (long long) ht->vlo, gbytes, val_type, agg,
-			out, out_capacity, cursor))) return rc;
-	unsigned long long ng = 0;
-	PG_CUDA(ctx, cudaMemcpyAsync(&ng, cursor, 8, cudaMemcpyDeviceToHost, s));
-	if ((rc = pg_check_status(ctx, s, "pg_hashjoin_groupby"))) return rc;
 	pg_free_async(ctx, s, mem);
-	*ngroups = ng;
-	if (ng > out_capacity) return pg_fail(ctx, PG_ERR_OUTPUT_FULL, "pg_hashjoin_groupby: output capacity too small");
-	return PG_OK;
+	return pg_fail(ctx, PG_ERR_CUDA, "pg_hashjoin_groupby: dec sum unit refuted twice");
 }

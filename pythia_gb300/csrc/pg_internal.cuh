@@ -362,35 +362,71 @@ __host__ __device__ __forceinline__ uint32_t pg_min32(uint32_t a, uint32_t b) { 
 // Exclusive scan of n uint64 values in place on the device (multi-block).
 int pg_scan_u64(pg_ctx* ctx, cudaStream_t s, uint64_t* data, uint64_t n, uint64_t* total_dev);
 
-// Exact rounding error of s = a + b by Dekker's Fast2Sum (3 FP64 adds: the
-// larger operand first). The magnitudes are ordered by an integer compare of
-// the bit patterns, and the zero test is an integer test too: on this GPU the
-// FP64 pipe is narrow and the dominant cost of a compensated aggregation, so
-// only the three additions use it.
-__device__ __forceinline__ void fast_two_sum(double a, double b, double& s, double& e)
+// Dec sums as exact 128-bit fixed-point integers (pg_fixsum.h): order-
+// independent, so a group's sum is the same on every run.
+#include "pg_fixsum.h"
+
+// The unit of one dec sum, in four device words made by pg_fx_prepare:
+// p[0] the unit exponent s (a value is a count of units 2^s), p[1] the largest
+// exponent field quantised, p[2] flags (PG_FX_RANGE: a value above that bound,
+// the sum is redone with the exact bound; PG_FX_SPECIALS: infinities or NaNs,
+// whose groups are patched afterwards), p[3] scratch. Kernels read s and the
+// bound at their start, so no host round trip sits between the sampling pass
+// and the aggregation.
+struct PgFx {
+	int* p;
+};
+#define PG_FX_RANGE 2u
+// Words per group of a dense dec-sum table: the count's three and a spare,
+// so that a row's atomics fall in one 32-byte sector.
+#define PG_FX_SLOT 4
+#define PG_FX_SPECIALS 4u
+
+// Quantises the dec value with bit pattern b for unit 2^s and bound `bound`.
+// Values above the bound or not finite contribute 0 and set their flag in fl.
+__device__ __forceinline__ pg_fx3 pg_fx_take(uint64_t b, int s, int bound, uint32_t& fl)
 {
-	const unsigned long long ma = (unsigned long long) __double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFull;
-	const unsigned long long mb = (unsigned long long) __double_as_longlong(b) & 0x7FFFFFFFFFFFFFFFull;
-	const double big = ma >= mb ? a : b, small = ma >= mb ? b : a;
-	s = a + b;
-	e = small - (s - big);
+	const int e = pg_fx_field(b);
+	if (e > bound) { fl |= e == PG_FX_EXP_SPECIAL ? PG_FX_SPECIALS : PG_FX_RANGE; return pg_fx3{0, 0, 0}; }
+	return pg_fx_quant(b, s);
 }
 
-__device__ __forceinline__ bool nonzero(double x)
+// Adds the count a into table words (*w0, *w1, *w2): an add that can carry
+// returns the old word, whose overflow is the carry into the next word. A
+// value near the column's largest has w0 = 0, so this is one returning add
+// and one plain add.
+__device__ __forceinline__ void pg_fx_atomic_add(unsigned long long* w0, unsigned long long* w1, unsigned long long* w2,
+		const pg_fx3& a)
 {
-	return ((unsigned long long) __double_as_longlong(x) << 1) != 0;
+	uint64_t c = 0;
+	if (a.w0) {
+		const unsigned long long old = atomicAdd(w0, (unsigned long long) a.w0);
+		c = (uint64_t) (old + a.w0) < (uint64_t) old;
+	}
+	const uint64_t x1 = a.w1 + c;
+	c = x1 < c;
+	if (x1) {
+		const unsigned long long old = atomicAdd(w1, (unsigned long long) x1);
+		c += (uint64_t) (old + x1) < (uint64_t) old;
+	}
+	const uint64_t x2 = a.w2 + c;
+	if (x2) atomicAdd(w2, (unsigned long long) x2);
 }
 
-// Exact rounding error of a double addition with integer operations only
-// (pg_add_err.h); used by the compensated aggregations instead of FP64 adds.
-#include "pg_add_err.h"
+// Fills fx->p (16 bytes of device memory, allocated by the caller) for a dec
+// sum over the 8-byte column at voff of n rows of width W: the largest finite
+// exponent field over rows 0, step, 2 step, ..., widened by `margin` fields
+// when sampled. Stream-ordered; no host round trip.
+int pg_fx_prepare(pg_ctx* ctx, cudaStream_t s, const char* data, uint64_t n, uint32_t W, uint32_t voff,
+		uint64_t step, int margin, PgFx fx);
 
-// Bit pattern of -0.0: the initial value of dense dec-sum accumulators.
-#define PG_NEG_ZERO 0x8000000000000000ull
+// Patches the dec sums of groups that met infinities or NaNs: out holds
+// ngroups rows (key of kbytes, 0 for no key, then the 8-byte sum) of the
+// aggregation of `in` grouped on its key column.
+int pg_fx_patch_specials(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, char* out, uint64_t ngroups);
 
-__global__ void k_fill_u64(unsigned long long* p, uint64_t n, unsigned long long v);
-
-// Dense group table emission (pg_groupby.cu).
-int pg_dense_groups_emit(pg_ctx* ctx, cudaStream_t s, const unsigned long long* acc, const double* lo,
+// Dense group table emission (pg_groupby.cu): acc holds a word per slot, or
+// for a dec sum four words per slot, the first three its count of units (fx).
+int pg_dense_groups_emit(pg_ctx* ctx, cudaStream_t s, const unsigned long long* acc, PgFx fx,
 		const unsigned char* present, uint64_t range, long long kmin, uint32_t kbytes, int val_type, int agg,
 		void* out, uint64_t out_cap, unsigned long long* cursor);
