@@ -101,25 +101,26 @@ def build_host():
     return lib
 
 
-def build_oracle():
-    """The C oracle (test infrastructure) and, where the reference source tree
-    is present, the reference engine itself (oracle/Makefile.ref)."""
+def build_oracle(reference=None):
+    """The C oracle (test infrastructure) and, when `reference` (or the
+    PYTHIA_REFERENCE environment variable) names the reference source tree and
+    it is present, the reference engine itself (oracle/Makefile.ref)."""
     src = os.path.join(ROOT, "oracle", "pythia_oracle.c")
     lib = os.path.join(ROOT, "oracle", "liboracle.so")
     if _stale(lib, [src, os.path.join(ROOT, "oracle", "pythia_oracle.h")]):
         _run(["gcc", "-O3", "-fPIC", "-shared", "-Wall", src, "-o", lib, "-lpthread", "-lm"])
-    ref = os.environ.get("PYTHIA_REFERENCE", "/root/reference")
-    if os.path.isdir(ref) and os.path.exists(os.path.join(ref, "operators", "join.cpp")):
+    ref = reference or os.environ.get("PYTHIA_REFERENCE")
+    if ref and os.path.isdir(ref) and os.path.exists(os.path.join(ref, "operators", "join.cpp")):
         _run(["make", "-s", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"),
               "REF=" + ref, "-j", str(min(8, os.cpu_count() or 4))], cwd=ROOT)
     return lib
 
 
-def build_all(verbose=False):
+def build_all(verbose=False, reference=None):
     build_datagen()
     build_gpu(verbose=verbose)
     build_host()
-    build_oracle()      # after libpythia_gpu: the reference build links the operators against it
+    build_oracle(reference)     # after libpythia_gpu: the reference build links the operators against it
 
 
 if __name__ == "__main__":

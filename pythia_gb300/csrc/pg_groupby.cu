@@ -182,10 +182,14 @@ k_gb_insert(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, 
 // Adds dec counts v[j] of the lead rows into their slots' words, all rows'
 // adds of one word before the next word's: the low words (rarely non-zero)
 // return their old value for the carry, then the middle words (likewise),
-// then the top words without a return.
+// then the top words without a return. With `present`, a row marks its slot
+// present when its middle-word add returned the initial 0 (the slot's first
+// such add) or it made none: one byte store per group, not per row, since
+// stores of every row onto a small present array contend on its L2 lines.
 template <int ILP>
 __device__ __forceinline__ void gb_fx_add_rows(unsigned long long* acc, unsigned long long* mid, unsigned long long* top,
-		const uint64_t (&slot)[ILP], const bool (&lead)[ILP], const pg_fx3 (&v)[ILP], uint64_t stride = 1)
+		const uint64_t (&slot)[ILP], const bool (&lead)[ILP], const pg_fx3 (&v)[ILP], uint64_t stride = 1,
+		unsigned char* present = nullptr)
 {
 	uint64_t c[ILP], x1[ILP];
 	unsigned long long o[ILP];
@@ -208,6 +212,7 @@ __device__ __forceinline__ void gb_fx_add_rows(unsigned long long* acc, unsigned
 		if (!lead[j]) continue;
 		const uint64_t x2 = v[j].w2 + c[j] + ((uint64_t) (o[j] + x1[j]) < (uint64_t) o[j]);
 		if (x2) atomicAdd(&top[slot[j] * stride], (unsigned long long) x2);
+		if (present && (x1[j] == 0 || o[j] == 0)) present[slot[j]] = 1;
 	}
 }
 
@@ -554,10 +559,7 @@ k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, u
 			else iv[j] = vbits;
 		}
 		if (GB_DEC) {
-			gb_fx_add_rows<GBD_ILP>(acc, acc + 1, acc + 2, d, ok, f, PG_FX_SLOT);
-			#pragma unroll
-			for (int j = 0; j < GBD_ILP; ++j)
-				if (ok[j]) present[d[j]] = 1;
+			gb_fx_add_rows<GBD_ILP>(acc, acc + 1, acc + 2, d, ok, f, PG_FX_SLOT, present);
 		} else {
 			#pragma unroll
 			for (int j = 0; j < GBD_ILP; ++j) {

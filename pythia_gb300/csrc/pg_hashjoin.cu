@@ -2911,7 +2911,10 @@ k_probe16_groupby(const char* __restrict__ S, uint64_t n, uint32_t koff, const H
 				if (e[j] == 0xFFFFFFFFu) continue;
 				const uint64_t x2 = f[j].w2 + c[j] + ((uint64_t) (o[j] + x1[j]) < (uint64_t) o[j]);
 				if (x2) atomicAdd(&acc[PG_FX_SLOT * (uint64_t) e[j] + 2], (unsigned long long) x2);
-				present[e[j]] = 1;
+				// Present once per group: the first middle-word add returns the
+				// initial 0 (a row without one marks it itself). Every row storing
+				// onto the small present array would contend on its L2 lines.
+				if (x1[j] == 0 || o[j] == 0) present[e[j]] = 1;
 			}
 		} else {
 			#pragma unroll

@@ -9,8 +9,8 @@ Inputs are not stored: each case names the generator call that makes it
 (pythia_gb300.datagen) and the SHA-256 of the bytes, so a test can rebuild
 the input on any machine and first check that the generator agrees.
 
-Run here, where the reference tree exists:
-    make -f oracle/Makefile.ref REF=/root/reference -j8
+Run where the reference source tree exists (REF names it):
+    make -f oracle/Makefile.ref REF=<reference source tree> -j8
     python tests/golden/make_golden.py [--keep-existing]
 """
 import hashlib
