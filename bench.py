@@ -51,7 +51,7 @@ TUPLE = 16
 # DRAM bytes per probe tuple of the materialising probe against the 16M-key
 # (64 MB) dense table, measured by ncu on a 32M-tuple probe of the same table;
 # traffic scales with the probe tuples.
-PROBE_DRAM_BYTES_PER_TUPLE = (1.133091e9 + 0.514387e9) / (1 << 25)
+PROBE_DRAM_BYTES_PER_TUPLE = (1.054382e9 + 0.514778e9) / (1 << 25)
 # DRAM bytes per 24-byte line of the staged probe against a 4M-part table, measured
 # by ncu on 16M lines; traffic scales with the lines.
 WIDE_DRAM_BYTES_PER_LINE = (419.517440e6 + 358.811904e6) / (1 << 24)
