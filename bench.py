@@ -458,7 +458,7 @@ def run_join(args, ws, rank, local, sp, steps, warmup, e2e_steps=3, cpu_sample=N
 OPS = {
     "partition": dict(n=1 << 28, metric="partition tuples/s (256M int64 tuples, 256-way radix, stable)",
                       workload="radix partition of 256M 16-byte tuples on the low 8 key bits (parammodulo)"),
-    "groupby": dict(n=1 << 28, metric="group-by rows/s (256M rows, 1M groups, compensated FP64 sum)",
+    "groupby": dict(n=1 << 28, metric="group-by rows/s (256M rows, 1M groups, exact FP64 sum)",
                     workload="aggregate_sum over (long key U[0,1M), dec value U[0,1e4)), 256M rows"),
     "sort": dict(n=1 << 26, metric="page sort tuples/s (64M int64-keyed 16-byte tuples)",
                  workload="page sort of 64M (long key U[0,16M), long payload) tuples"),
@@ -469,12 +469,17 @@ OPS = {
                              "every (P$1,B$1) pair written (~268M rows): page sort, then run matching and the "
                              "per-key cartesian write"),
     "sortwide": dict(n=1 << 26, metric="page sort tuples/s (64M int64-keyed 16-byte tuples, keys over 2^40)",
-                     workload="page sort of 64M (long key U[0,2^40), long payload) tuples: key span above 2^32, "
-                              "so 4096-tuple bitonic tiles in shared memory then merge-path merges"),
+                     workload="page sort of 64M (long key U[0,2^40), long payload) tuples: LSD radix over the 40 "
+                              "bits of key - min, five 8-bit passes"),
+    "sortbitonic": dict(n=1 << 26, metric="page sort tuples/s (64M int64-keyed 16-byte tuples, keys over 2^40, "
+                                          "bitonic)",
+                        workload="page sort of 64M (long key U[0,2^40), long payload) tuples as 4096-tuple bitonic "
+                                 "tiles in shared memory then merge-path merges (sort path 2)"),
     "groupjoin": dict(n=1 << 28, metric="join + group-by tuples/s (16M build x 256M probe, 1% groups, one pass)",
                       workload="hash join of 16M unique keys (group column = payload mod 167,772) with 256M FK "
                                "probes carrying dec values U[0,1e4), then aggregate_sum per group, one pass"),
 }
+SORT_OPS = ("sort", "sortwide", "sortbitonic")
 GJ_BUILD = 1 << 24
 GJ_GROUPS = GJ_BUILD // 100
 
@@ -493,7 +498,7 @@ def _op_inputs(op, n, threads):
         return [dg.groupby_rows(n, 1 << 20, 1e4, dg.seed_for(112), threads=threads)]
     if op == "sort":
         return [dg.uniform_keys(n, 1 << 24, dg.seed_for(113), threads=threads)]
-    if op == "sortwide":
+    if op in ("sortwide", "sortbitonic"):
         return [dg.uniform_keys(n, 1 << 40, dg.seed_for(118), threads=threads)]
     if op == "groupjoin":
         nb = min(GJ_BUILD, max(n // 16, 1024))
@@ -539,7 +544,7 @@ def _op_parity(op, ins, out, extra):
         return {"groups_ok": bool(ngroups_ok), "total_rel_err": abs(got_total - total) / total,
                 "sampled_group_max_rel_err": worst, "tolerance": 1e-12,
                 "ok": bool(ngroups_ok and worst <= 1e-12)}
-    if op in ("sort", "sortwide"):
+    if op in SORT_OPS:
         o = out.reshape(-1, 2)
         ok = bool(np.all(np.diff(o[:, 0]) >= 0))
         ok &= int(o.astype(np.uint64).sum(dtype=np.uint64)) == int(ins[0].astype(np.uint64).sum(dtype=np.uint64))
@@ -587,6 +592,8 @@ def run_op(args, ws, rank, local, op):
     n = spec["n"] >> args.scale_down
     threads = host_threads()
     ctx = make_ctx(args, local)
+    if op == "sortbitonic":
+        ctx.tune(sort_path=2)
     L = gpu.lib()
     ins = _op_inputs(op, n, threads)
     d_in = [ctx.upload(a) for a in ins]
@@ -601,7 +608,7 @@ def run_op(args, ws, rank, local, op):
         ctx._check(L.pg_mpsm_join(ctx.h, ctx.stream, ctypes.byref(rel[0]), ctypes.byref(rel[1]), c, nc,
                                   None, 0, gpu.JOIN_COUNT, -1, ctypes.byref(r0)))
         n_pairs = int(r0.n_out)
-    out_bytes = {"partition": n * 16, "groupby": (1 << 20) * 16 + 16, "sort": n * 16, "sortwide": n * 16,
+    out_bytes = {"partition": n * 16, "groupby": (1 << 20) * 16 + 16, "sort": n * 16, "sortwide": n * 16, "sortbitonic": n * 16,
                  "mpsm": 16, "mpsmmat": max(n_pairs, 1) * 16, "groupjoin": (nb // 100 + 1) * 16}[op]
     d_out = ctx.alloc(out_bytes)
     offs = ctx.alloc(8 * 257)
@@ -616,7 +623,7 @@ def run_op(args, ws, rank, local, op):
         elif op == "groupby":
             ctx._check(L.pg_groupby(ctx.h, ctx.stream, ctypes.byref(rel[0]), 8, 2, 0, 1 << 20, d_out.ptr,
                                     1 << 20, ctypes.byref(ng)))
-        elif op in ("sort", "sortwide"):
+        elif op in SORT_OPS:
             ctx._check(L.pg_sort_pages(ctx.h, ctx.stream, ctypes.byref(rel[0]), d_out.ptr))
         elif op == "mpsmmat":
             ctx._check(L.pg_mpsm_join(ctx.h, ctx.stream, ctypes.byref(rel[0]), ctypes.byref(rel[1]), c, nc,
@@ -651,7 +658,7 @@ def run_op(args, ws, rank, local, op):
     ms = max_over_ranks(ws, e0.elapsed_time(e1) / args.steps)
     units = 2 * n if op in ("mpsm", "mpsmmat") else (n + nb if op == "groupjoin" else n)
     value = ws * units / (ms / 1e3)
-    alg = {"partition": 32 * n, "groupby": 16 * n + 16 * (1 << 20), "sort": 32 * n, "sortwide": 32 * n,
+    alg = {"partition": 32 * n, "groupby": 16 * n + 16 * (1 << 20), "sort": 32 * n, "sortwide": 32 * n, "sortbitonic": 32 * n,
            "mpsm": 16 * 2 * n, "mpsmmat": 16 * 2 * n + 16 * n_pairs,
            "groupjoin": 16 * (n + nb) + 16 * (nb // 100)}[op]
     peak, peak_kind = measured_peak()
@@ -662,7 +669,7 @@ def run_op(args, ws, rank, local, op):
         parity = _op_parity(op, ins, out, ctx.download(offs, 8 * 257, np.uint64))
     elif op == "groupby":
         parity = _op_parity(op, ins, ctx.download(d_out, ng.value * 16), None)
-    elif op in ("sort", "sortwide"):
+    elif op in SORT_OPS:
         parity = _op_parity(op, ins, ctx.download(d_out, n * 16).view(np.int64), None)
     elif op == "mpsmmat":
         from oracle import oracle as orc
@@ -710,7 +717,7 @@ def cpu_op_sample(op, ins, threads):
     elif op == "groupby":
         orc.groupby(a, val=(8, "dec"), agg="sum", hash=orc.hashcfg("modulo", 1 << 20), threads=threads)
         scale, kind = n / m, "linear"
-    elif op in ("sort", "sortwide"):
+    elif op in SORT_OPS:
         m = min(n, 1 << 22)
         a = np.ascontiguousarray(ins[0][:m])
         t0 = time.perf_counter()
@@ -744,7 +751,7 @@ def cpu_op_sample(op, ins, threads):
         scale, kind = n / m, "linear"
     t = (time.perf_counter() - t0) * scale
     units = 2 * n if op in ("mpsm", "mpsmmat") else (n + ins[0].shape[0] if op == "groupjoin" else n)
-    one = op in ("sort", "sortwide")
+    one = op in SORT_OPS
     return {"value": units / t, "unit": "tuples/s", "cores": 1 if one else threads,
             "kind": "port", "sample": f"{m} tuples (oracle port{', one thread' if one else ''}), "
                                       f"time scaled {kind} to {n}"}
@@ -1577,7 +1584,8 @@ def suite(args, ws, rank, local):
         ("cfg2b_groupby_256M_1M_groups", lambda: _captured(run_op, sub, ws, rank, local, "groupby")),
         ("cfg3_mpsm_64Mx64M_count_sum", lambda: _captured(run_op, sub, ws, rank, local, "mpsm")),
         ("cfg3_mpsm_64Mx64M_materialised", lambda: _captured(run_op, sub, ws, rank, local, "mpsmmat")),
-        ("sort_64M_keys_over_2e32_bitonic", lambda: _captured(run_op, sub, ws, rank, local, "sortwide")),
+        ("sort_64M_keys_over_2e32_radix", lambda: _captured(run_op, sub, ws, rank, local, "sortwide")),
+        ("sort_64M_keys_over_2e32_bitonic", lambda: _captured(run_op, sub, ws, rank, local, "sortbitonic")),
         ("sort_64M_keys_16M_radix", lambda: _captured(run_op, sub, ws, rank, local, "sort")),
         ("partition_256M_256way", lambda: _captured(run_op, sub, ws, rank, local, "partition")),
         ("cfg4_batch_10000", lambda: _captured(run_batch, sub, ws, rank, local)),

@@ -177,7 +177,11 @@ enum {
 	PG_TUNE_L2_FETCH = 13,           /* L2 fetch granularity hint of the context in bytes: 0 leaves the CUDA
 	                                    default, else 32, 64 or 128 (cudaLimitMaxL2FetchGranularity, a limit of
 	                                    the calling process that ends with it) */
-	PG_TUNE_COUNT = 14
+	PG_TUNE_SORT_PATH = 14,          /* page sort and the MPSM's sorts: 0 LSD radix over key - min while the span
+	                                    fits 63 bits (bitonic tiles and merge-path merges for wider spans and for
+	                                    inputs of at most 2^18 tuples whose span needs over 32 bits), 1 radix
+	                                    whenever the span fits 63 bits, 2 bitonic tiles and merges always */
+	PG_TUNE_COUNT = 15
 };
 int pg_tune_set(pg_ctx* ctx, int knob, int64_t value);
 int64_t pg_tune_get(pg_ctx* ctx, int knob);

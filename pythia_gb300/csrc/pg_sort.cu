@@ -234,7 +234,14 @@ static int radix_sort(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, void* out, 
 	pg_free_async(ctx, s, mm);
 	const unsigned long long span = h[1] - h[0];
 	const int bits = span == 0 ? 0 : 64 - __builtin_clzll(span);
-	if (bits > 32) return PG_OK;
+	// LSD radix over the bits of key - min while they fit 63 bits (the digit
+	// function masks a signed difference). Bitonic tiles and merge-path
+	// merges instead for wider spans, and for small inputs whose span needs
+	// more than four 8-bit passes: there the few merge passes cost less than
+	// the radix passes (a histogram read and a scatter each).
+	const int64_t path = ctx->tune[PG_TUNE_SORT_PATH];
+	if (path == 2 || bits > 63) return PG_OK;
+	if (path == 0 && bits > 32 && n <= (1ull << 18)) return PG_OK;
 	const long long kmin = (long long) (h[0] ^ (1ull << 63));
 	if (bits == 0) {   // one key value: already sorted
 		PG_CUDA(ctx, cudaMemcpyAsync(out, in->data, n * in->width, cudaMemcpyDeviceToDevice, s));

@@ -813,8 +813,15 @@ def _sort_check(ctx, rows, key=(0, 8)):
 
 
 @pytest.mark.parametrize("n", [0, 1, 100, 4095, 4096, 4097, 8192, 100_000, 1_000_003])
-def test_sort_sizes(ctx, n):
-    _sort_check(ctx, dg.uniform_keys(n, 1 << 40, dg.seed_for(60)))
+@pytest.mark.parametrize("path", [0, 1, 2])
+def test_sort_sizes(ctx, n, path):
+    # Keys over 2^40: path 0 sorts by 8-bit LSD radix passes above 2^18 tuples and
+    # by bitonic tiles and merges below, 1 always radix, 2 always bitonic.
+    try:
+        ctx.tune(sort_path=path)
+        _sort_check(ctx, dg.uniform_keys(n, 1 << 40, dg.seed_for(60)))
+    finally:
+        ctx.tune(sort_path=0)
 
 
 def test_sort_duplicates_and_negatives(ctx):
@@ -823,7 +830,10 @@ def test_sort_duplicates_and_negatives(ctx):
     a = dg.uniform_keys(10_000, 10, dg.seed_for(62))
     a[:, 0] = np.iinfo(np.int64).max - a[:, 0]
     a[::3, 0] = np.iinfo(np.int64).min
-    _sort_check(ctx, a)
+    _sort_check(ctx, a)                              # span 2^64 - 1: bitonic
+    b = dg.uniform_keys(400_000, 1 << 62, dg.seed_for(65))
+    b[::2, 0] -= 1 << 61                             # span just under 2^63, negatives: eight radix passes
+    _sort_check(ctx, b)
 
 
 def test_sort_layouts(ctx):
