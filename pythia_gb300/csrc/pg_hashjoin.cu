@@ -75,43 +75,82 @@ __device__ __forceinline__ uint32_t hj_word(const char* tuple, uint32_t w)
 	return reinterpret_cast<const uint32_t*>(tuple)[w];
 }
 
-__global__ void k_ht_build(const char* __restrict__ R, uint64_t n, uint32_t W, uint32_t koff,
-		uint32_t kbytes, HjBuildCols bc, bool inline_val, unsigned long long* __restrict__ slots,
+// The packed value's word positions in a build tuple of any width as one
+// word: bits 0-1 the word count (0..2), bits 2-9 and 10-17 the two word
+// indices. Read in the kernel without an indexed local array.
+static uint32_t hj_pack_code(const HjBuildCols& bc)
+{
+	uint32_t code = 0, o = 0;
+	for (int c = 0; c < bc.n; ++c)
+		for (int j = 0; j < bc.words[c] && o < 2; ++j, ++o) code |= (uint32_t) ((bc.roff[c] + j) & 255) << (2 + 8 * o);
+	return code | o;
+}
+
+__device__ __forceinline__ uint64_t hj_pack(const char* t, uint32_t code)
+{
+	const uint32_t nw = code & 3;
+	uint64_t v = 0;
+	if (nw > 0) v = hj_word(t, (code >> 2) & 255);
+	if (nw > 1) v |= (uint64_t) hj_word(t, (code >> 10) & 255) << 32;
+	return v;
+}
+
+// Open-addressing build: each thread inserts HT_ILP tuples at once. Their
+// key loads and their atomicCAS on the slots' key words are issued together,
+// and each tuple then walks on to the next slot only when its slot was taken,
+// so the L2 round trips of several inserts overlap instead of running one
+// tuple at a time. A key already present is inserted again (duplicates are
+// kept) and flags the table as not unique.
+#define HT_ILP 4
+__global__ void __launch_bounds__(256)
+k_ht_build(const char* __restrict__ R, uint64_t n, uint32_t W, uint32_t koff,
+		uint32_t kbytes, uint32_t pcode, bool inline_val, unsigned long long* __restrict__ slots,
 		uint32_t log2cap, unsigned long long* __restrict__ side, uint32_t side_cap,
 		unsigned int* __restrict__ side_count, int* __restrict__ flags, int* __restrict__ status)
 {
 	const uint64_t mask = (1ull << log2cap) - 1;
-	bool dup = false;
-	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n;
-			i += (uint64_t) gridDim.x * blockDim.x) {
-		const char* t = R + i * W;
-		int64_t k = pg_load_key(t + koff, kbytes);
-		uint64_t v;
-		if (inline_val) {
-			uint32_t w[2] = {0, 0};
-			int o = 0;
-			for (int c = 0; c < bc.n; ++c)
-				for (int j = 0; j < bc.words[c]; ++j) w[o++] = hj_word(t, bc.roff[c] + j);
-			v = ((uint64_t) w[1] << 32) | w[0];
-		} else {
-			v = i;
+	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+	bool dup = false, full = false;
+	for (uint64_t base = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; base < n; base += stride * HT_ILP) {
+		int64_t k[HT_ILP];
+		uint64_t v[HT_ILP], s[HT_ILP], tries[HT_ILP];
+		bool act[HT_ILP];
+		#pragma unroll
+		for (int j = 0; j < HT_ILP; ++j) {
+			const uint64_t i = base + j * stride;
+			act[j] = i < n;
+			k[j] = 0; v[j] = 0; s[j] = 0; tries[j] = 0;
+			if (!act[j]) continue;
+			const char* t = R + i * W;
+			k[j] = pg_load_key(t + koff, kbytes);
+			v[j] = inline_val ? hj_pack(t, pcode) : i;
+			if (k[j] == PG_EMPTY_KEY) {
+				const unsigned int idx = atomicAdd(side_count, 1u);
+				if (idx < side_cap) side[idx] = v[j]; else atomicOr(flags, 2);
+				act[j] = false;
+				continue;
+			}
+			s[j] = hj_slot0(k[j], log2cap);
 		}
-		if (k == PG_EMPTY_KEY) {
-			unsigned int idx = atomicAdd(side_count, 1u);
-			if (idx < side_cap) side[idx] = v; else atomicOr(flags, 2);
-			continue;
+		for (;;) {
+			bool any = false;
+			unsigned long long old[HT_ILP];
+			#pragma unroll
+			for (int j = 0; j < HT_ILP; ++j)
+				if (act[j]) old[j] = atomicCAS(&slots[2 * s[j]], (unsigned long long) PG_EMPTY_KEY, (unsigned long long) k[j]);
+			#pragma unroll
+			for (int j = 0; j < HT_ILP; ++j) {
+				if (!act[j]) continue;
+				if (old[j] == (unsigned long long) PG_EMPTY_KEY) { slots[2 * s[j] + 1] = v[j]; act[j] = false; continue; }
+				if ((long long) old[j] == k[j]) dup = true;
+				s[j] = (s[j] + 1) & mask;
+				if (++tries[j] > mask) { full = true; act[j] = false; continue; }
+				any = true;
+			}
+			if (!any) break;
 		}
-		uint64_t s = hj_slot0(k, log2cap);
-		uint64_t probe = 0;
-		for (; probe <= mask; ++probe) {
-			unsigned long long old = atomicCAS(&slots[2 * s], (unsigned long long) PG_EMPTY_KEY,
-					(unsigned long long) k);
-			if (old == (unsigned long long) PG_EMPTY_KEY) { slots[2 * s + 1] = v; break; }
-			if ((long long) old == k) dup = true;
-			s = (s + 1) & mask;
-		}
-		if (probe > mask) pg_set_status(status, PG_ERR_TABLE_FULL);
 	}
+	if (full) pg_set_status(status, PG_ERR_TABLE_FULL);
 	if (__any_sync(__activemask(), dup) && dup) atomicOr(flags, 1);
 }
 
@@ -1981,9 +2020,9 @@ static int hj_build_exact(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, pg_hasht
 		PG_CUDA(ctx, cudaMemsetAsync(ht->slots, 0xFF, ht->capacity * 16, s));
 		PG_CUDA(ctx, cudaMemsetAsync(side_count, 0, 8, s));
 		if (R->n) {
-			int blocks = (int) std::min<uint64_t>(pg_div_up(R->n, 256), (uint64_t) ctx->sm_count * 16);
+			int blocks = (int) std::min<uint64_t>(pg_div_up(R->n, 256 * HT_ILP), (uint64_t) ctx->sm_count * 16);
 			k_ht_build<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off, R->key_bytes,
-					ht->bcols, ht->inline_val, ht->slots, ht->log2cap, ht->side, ht->side_cap,
+					hj_pack_code(ht->bcols), ht->inline_val, ht->slots, ht->log2cap, ht->side, ht->side_cap,
 					side_count, flags, ctx->d_status);
 			PG_LAUNCHED(ctx);
 		}
