@@ -528,7 +528,8 @@ __device__ __forceinline__ void gb_row_kv(const char* __restrict__ in, uint64_t 
 }
 
 #define GBD_ILP 4
-template <int VT, int AGG, bool VEC16>
+// ILP rows per thread in flight (their loads and atomics issued together).
+template <int VT, int AGG, bool VEC16, int ILP>
 __global__ void __launch_bounds__(GB_THREADS)
 k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes, uint32_t voff,
 		long long kmin, uint64_t range, unsigned long long* __restrict__ acc, PgFx fx,
@@ -538,13 +539,13 @@ k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, u
 	bool outside = false;
 	uint32_t fl = 0;
 	const int fs = GB_DEC ? fx.p[0] : 0, fb = GB_DEC ? fx.p[1] : 0;
-	for (uint64_t base = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; base < n; base += stride * GBD_ILP) {
-		uint64_t d[GBD_ILP];
-		unsigned long long iv[GBD_ILP];
-		pg_fx3 f[GBD_ILP];
-		bool ok[GBD_ILP];
+	for (uint64_t base = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; base < n; base += stride * ILP) {
+		uint64_t d[ILP];
+		unsigned long long iv[ILP];
+		pg_fx3 f[ILP];
+		bool ok[ILP];
 		#pragma unroll
-		for (int j = 0; j < GBD_ILP; ++j) {
+		for (int j = 0; j < ILP; ++j) {
 			const uint64_t i = base + j * stride;
 			ok[j] = i < n;
 			d[j] = 0; iv[j] = 0; f[j] = pg_fx3{0, 0, 0};
@@ -559,10 +560,10 @@ k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, u
 			else iv[j] = vbits;
 		}
 		if (GB_DEC) {
-			gb_fx_add_rows<GBD_ILP>(acc, acc + 1, acc + 2, d, ok, f, PG_FX_SLOT, present);
+			gb_fx_add_rows<ILP>(acc, acc + 1, acc + 2, d, ok, f, PG_FX_SLOT, present);
 		} else {
 			#pragma unroll
-			for (int j = 0; j < GBD_ILP; ++j) {
+			for (int j = 0; j < ILP; ++j) {
 				if (!ok[j]) continue;
 				if (VT == PG_VAL_INT && AGG == PG_AGG_SUM)
 					atomicAdd(reinterpret_cast<unsigned int*>(&acc[d[j]]), (unsigned int) iv[j]);
@@ -848,12 +849,16 @@ static int gb_dense_window(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32
 				in->width, in->key_off, in->key_bytes, voff, kmin, (uint32_t) range, acc, fx, present, oflag);
 		PG_LAUNCHED(ctx);
 	} else {
-		const int gblocks = (int) std::min<uint64_t>(pg_div_up(in->n, (uint64_t) GB_THREADS * GBD_ILP),
+		const int ilp = ctx->tune[PG_TUNE_GROUPBY_ILP] == 8 ? 8 : GBD_ILP;
+		const int gblocks = (int) std::min<uint64_t>(pg_div_up(in->n, (uint64_t) GB_THREADS * ilp),
 				(uint64_t) ctx->sm_count * 8);
-		if (vec16) k_gb_dense<VT, AGG, true><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, in->width,
-				in->key_off, in->key_bytes, voff, kmin, range, acc, fx, present, oflag);
-		else k_gb_dense<VT, AGG, false><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, in->width,
-				in->key_off, in->key_bytes, voff, kmin, range, acc, fx, present, oflag);
+#define GBD_LAUNCH(V, I) k_gb_dense<VT, AGG, V, I><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, \
+				in->width, in->key_off, in->key_bytes, voff, kmin, range, acc, fx, present, oflag)
+		if (vec16 && ilp == 8) GBD_LAUNCH(true, 8);
+		else if (vec16) GBD_LAUNCH(true, GBD_ILP);
+		else if (ilp == 8) GBD_LAUNCH(false, 8);
+		else GBD_LAUNCH(false, GBD_ILP);
+#undef GBD_LAUNCH
 		PG_LAUNCHED(ctx);
 	}
 	const int eblocks = (int) std::min<uint64_t>(pg_div_up(range, 256), (uint64_t) ctx->sm_count * 8);
