@@ -181,8 +181,8 @@ enum {
 	                                    fits 63 bits (bitonic tiles and merge-path merges for wider spans and for
 	                                    inputs of at most 2^18 tuples whose span needs over 32 bits), 1 radix
 	                                    whenever the span fits 63 bits, 2 bitonic tiles and merges always */
-	PG_TUNE_GROUPBY_ILP = 15,        /* rows in flight per thread of the dense group-by over a global table: 4
-	                                    (0: built-in) or 8 */
+	PG_TUNE_GROUPBY_ILP = 15,        /* rows in flight per thread of the dense group-by over a global table: 8
+	                                    (0: built-in) or 4 */
 	PG_TUNE_COUNT = 16
 };
 int pg_tune_set(pg_ctx* ctx, int knob, int64_t value);
