@@ -78,8 +78,8 @@ k_part_scatter(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t kof
 	unsigned char* buf1 = smem + tile_bytes;
 	uint16_t* cnt = reinterpret_cast<uint16_t*>(smem + 2 * tile_bytes);        // [NW][B]
 	uint32_t* tstart = reinterpret_cast<uint32_t*>(cnt + NW * B);               // [B]
-	uint32_t* gbase = tstart + B;                                                // [B]
-	uint32_t* running = gbase + B;                                               // [B]
+	uint32_t* delta = tstart + B;                                                // [B]
+	uint32_t* running = delta + B;                                               // [B]
 	uint16_t* inv = reinterpret_cast<uint16_t*>(running + B);                   // [tile]
 	uint16_t* bkt = inv + tile;                                                  // [tile]
 	uint64_t* bar = reinterpret_cast<uint64_t*>(
@@ -206,36 +206,37 @@ k_part_scatter(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t kof
 			}
 			__syncthreads();
 			if (b < B) {
-				tstart[b] = carry + x - tot + warp_sums[warp];
-				gbase[b] = running[b];
+				const uint32_t ts = carry + x - tot + warp_sums[warp];
+				tstart[b] = ts;
+				// Output row of grouped slot s of bucket b: running[b] + (s - ts),
+				// kept as one word mod 2^32 (rows stay below 2^32).
+				delta[b] = running[b] - ts;
 				running[b] += tot;
 			}
 			__syncthreads();
 			if (tid == 0) carry += warp_sums[31];
 			__syncthreads();
 		}
-		// (3) grouped position of every row.
+		// (3) grouped slot of every row, recorded as the permutation
+		// slot -> row.
+		uint16_t* perm = reinterpret_cast<uint16_t*>(bar + 2);
 		for (uint32_t it = 0; it < sub; it += 32) {
 			uint32_t p = warp * sub + it + lane;
 			if (p < rows) {
 				uint32_t b = bkt[p];
-				uint32_t s = tstart[b] + cnt[warp * B + b] + inv[p];
-				inv[p] = (uint16_t) s;   // inv now maps row -> grouped slot
+				perm[tstart[b] + cnt[warp * B + b] + inv[p]] = (uint16_t) p;
 			}
 		}
 		__syncthreads();
-		// (4) write out: row p goes to gbase[b] + (s - tstart[b]). Threads walk
-		// the tile in grouped order (via the inverse permutation) so that
-		// neighbouring lanes store to neighbouring slots of one partition.
+		// (4) write out: slot s of bucket b goes to row delta[b] + s. Threads
+		// walk the tile in grouped order so that neighbouring lanes store to
+		// neighbouring rows of one partition.
 		{
-			uint16_t* perm = reinterpret_cast<uint16_t*>(bar + 2);
-			for (uint32_t p = tid; p < rows; p += blockDim.x) perm[inv[p]] = (uint16_t) p;
-			__syncthreads();
 			if (W == 16) {
 				for (uint32_t s = tid; s < rows; s += blockDim.x) {
 					uint32_t p = perm[s];
 					uint32_t b = bkt[p];
-					uint64_t dest = (uint64_t) gbase[b] + (s - tstart[b]);
+					uint64_t dest = (uint32_t) (delta[b] + s);
 					uint4 v = reinterpret_cast<const uint4*>(cur)[p];
 					pg_st_stream16(out + dest * 16, v);
 				}
@@ -245,7 +246,7 @@ k_part_scatter(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t kof
 					uint32_t s = e / words, wd = e - s * words;
 					uint32_t p = perm[s];
 					uint32_t b = bkt[p];
-					uint64_t dest = (uint64_t) gbase[b] + (s - tstart[b]);
+					uint64_t dest = (uint32_t) (delta[b] + s);
 					reinterpret_cast<uint32_t*>(out + dest * W)[wd] =
 						reinterpret_cast<const uint32_t*>(cur + (uint64_t) p * W)[wd];
 				}
@@ -272,7 +273,7 @@ static size_t part_smem_bytes(uint32_t tile, uint32_t W, uint32_t B, int NW)
 {
 	size_t s = 2 * (size_t) tile * W;          // tile buffers
 	s += (size_t) NW * B * 2;                  // per-warp counters
-	s += 3 * (size_t) B * 4;                   // tstart, gbase, running
+	s += 3 * (size_t) B * 4;                   // tstart, delta, running
 	s += 2 * (size_t) tile * 2;                // inv, bkt
 	s = (s + 15) & ~size_t(15);
 	s += 16;                                   // mbarriers
