@@ -442,35 +442,53 @@ __global__ void __launch_bounds__(256) k_dense32_spec16(const uint4* __restrict_
 
 // Count pass: present entries of the window into hdr->present (equal to n
 // exactly when no key repeated), and the exact key and value ranges from the
-// first and last present entries and the smallest and largest entry.
+// first and last present entries and the smallest and largest entry. Each
+// thread reads its 16-byte words four at a time (four loads in flight: one at
+// a time the pass waited on DRAM latency), and since its words come in
+// increasing order, its first and last present index need no compares.
 __global__ void k_dense32_count_spec(const uint32_t* __restrict__ table, HjDenseHdr* __restrict__ hdr)
 {
 	if (hdr->flags) return;
 	const unsigned long long range = hdr->drange;
-	unsigned long long c = 0, dlo = ~0ull, dhi = 0, elo = ~0ull, ehi = 0;
+	unsigned long long c = 0, dlo = ~0ull, dhi = 0;
+	uint32_t elo = 0xFFFFFFFFu, ehi = 0;
 	auto see = [&](uint32_t e, unsigned long long d) {
 		if (e == 0xFFFFFFFFu) return;
 		++c;
-		dlo = d < dlo ? d : dlo; dhi = d > dhi ? d : dhi;
-		elo = e < elo ? e : elo; ehi = e > ehi ? e : ehi;
+		if (dlo == ~0ull) dlo = d;
+		dhi = d;
+		elo = e < elo ? e : elo;
+		ehi = e > ehi ? e : ehi;
 	};
 	const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
 	const uint64_t n4 = range / 4;
 	const uint4* t4 = reinterpret_cast<const uint4*>(table);
-	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n4; i += stride) {
+	uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+	for (; i + 3 * stride < n4; i += 4 * stride) {
+		uint4 v[4];
+		#pragma unroll
+		for (int j = 0; j < 4; ++j) v[j] = t4[i + j * stride];
+		#pragma unroll
+		for (int j = 0; j < 4; ++j) {
+			const unsigned long long d = 4 * (i + j * stride);
+			see(v[j].x, d); see(v[j].y, d + 1); see(v[j].z, d + 2); see(v[j].w, d + 3);
+		}
+	}
+	for (; i < n4; i += stride) {
 		const uint4 v = t4[i];
 		see(v.x, 4 * i); see(v.y, 4 * i + 1); see(v.z, 4 * i + 2); see(v.w, 4 * i + 3);
 	}
-	for (uint64_t i = 4 * n4 + blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < range; i += stride)
-		see(table[i], i);
-	hj_minmax4(dlo, dhi, elo, ehi);
+	for (uint64_t j = 4 * n4 + blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; j < range; j += stride)
+		see(table[j], j);
+	unsigned long long vlo = c ? elo : ~0ull, vhi = ehi;
+	hj_minmax4(dlo, dhi, vlo, vhi);
 	#pragma unroll
 	for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
 	if ((threadIdx.x & 31) == 0 && c) {
 		const unsigned long long dmin = (unsigned long long) hdr->dmin, vmin = hdr->vmin;
 		atomicAdd(&hdr->present, c);
 		atomicMin(&hdr->kmin, (dmin + dlo) ^ (1ull << 63)); atomicMax(&hdr->kmax, (dmin + dhi) ^ (1ull << 63));
-		atomicMin(&hdr->vlo, vmin + elo); atomicMax(&hdr->vhi, vmin + ehi);
+		atomicMin(&hdr->vlo, vmin + vlo); atomicMax(&hdr->vhi, vmin + vhi);
 	}
 }
 
