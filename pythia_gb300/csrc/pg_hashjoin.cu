@@ -484,11 +484,24 @@ __global__ void k_dense32_count_spec(const uint32_t* __restrict__ table, HjDense
 	hj_minmax4(dlo, dhi, vlo, vhi);
 	#pragma unroll
 	for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-	if ((threadIdx.x & 31) == 0 && c) {
-		const unsigned long long dmin = (unsigned long long) hdr->dmin, vmin = hdr->vmin;
-		atomicAdd(&hdr->present, c);
-		atomicMin(&hdr->kmin, (dmin + dlo) ^ (1ull << 63)); atomicMax(&hdr->kmax, (dmin + dhi) ^ (1ull << 63));
-		atomicMin(&hdr->vlo, vmin + vlo); atomicMax(&hdr->vhi, vmin + vhi);
+	// One set of header atomics per CTA, not per warp: the five words share
+	// one L2 line, where thousands of warps' atomics queued up.
+	__shared__ unsigned long long red[5][8];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	if (lane == 0) { red[0][warp] = c; red[1][warp] = dlo; red[2][warp] = dhi; red[3][warp] = vlo; red[4][warp] = vhi; }
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		for (int w = 1; w < (int) (blockDim.x >> 5); ++w) {
+			c += red[0][w];
+			dlo = red[1][w] < dlo ? red[1][w] : dlo; dhi = red[2][w] > dhi ? red[2][w] : dhi;
+			vlo = red[3][w] < vlo ? red[3][w] : vlo; vhi = red[4][w] > vhi ? red[4][w] : vhi;
+		}
+		if (c) {
+			const unsigned long long dmin = (unsigned long long) hdr->dmin, vmin = hdr->vmin;
+			atomicAdd(&hdr->present, c);
+			atomicMin(&hdr->kmin, (dmin + dlo) ^ (1ull << 63)); atomicMax(&hdr->kmax, (dmin + dhi) ^ (1ull << 63));
+			atomicMin(&hdr->vlo, vmin + vlo); atomicMax(&hdr->vhi, vmin + vhi);
+		}
 	}
 }
 
@@ -1507,7 +1520,8 @@ k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const Hj
 	const uint64_t stream = (tb.cache & 8) ? pg_policy_evict_normal() : pg_policy_evict_first();
 	const uint32_t w0 = wsel & 15, w1 = (wsel >> 4) & 15, w2 = (wsel >> 8) & 15, w3 = (wsel >> 12) & 15;
 	unsigned long long cnt_acc = 0, sum_acc = 0;
-	if (first >= nchunks) return;
+	// Warps past the last chunk load nothing but still join the block's sum.
+	const bool busy = first < nchunks;
 	uint4 cur[ITEMS], nxt[ITEMS];
 	auto load = [&](uint64_t c, uint4 (&t)[ITEMS]) {
 		const uint32_t rows = (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK);
@@ -1517,7 +1531,7 @@ k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const Hj
 			t[j] = p < rows ? hj_ld_stream(S + (c * PW_CHUNK + p) * 16, instream) : make_uint4(0, 0, 0, 0);
 		}
 	};
-	if (PF) load(first, cur);
+	if (PF && busy) load(first, cur);
 	for (uint64_t c = first; c < nchunks; c += W) {
 		if (PF) { if (c + W < nchunks) load(c + W, nxt); }
 		else load(c, cur);
@@ -1587,7 +1601,19 @@ k_probe16_direct(const char* __restrict__ S, uint64_t n, uint32_t koff, const Hj
 		#pragma unroll
 		for (int o = 16; o > 0; o >>= 1) sum_acc += __shfl_down_sync(0xffffffffu, sum_acc, o);
 	}
-	if (lane == 0) { atomicAdd(&agg[0], cnt_acc); if (!MATERIALIZE) atomicAdd(&agg[1], sum_acc); }
+	// One pair of global atomics per CTA: thousands of warps adding into the
+	// same two words queue up at one L2 slice, which on short probes (16M
+	// tuples) was a good part of the kernel's time.
+	__shared__ unsigned long long red[2][PW_WARPS];
+	if (lane == 0) { red[0][warp] = cnt_acc; red[1][warp] = sum_acc; }
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		unsigned long long c = 0, t = 0;
+		#pragma unroll
+		for (int w = 0; w < PW_WARPS; ++w) { c += red[0][w]; t += red[1][w]; }
+		if (c) atomicAdd(&agg[0], c);
+		if (!MATERIALIZE && t) atomicAdd(&agg[1], t);
+	}
 }
 
 // ---------------------------------------------------------------------------
