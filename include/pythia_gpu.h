@@ -339,8 +339,11 @@ int pg_hashjoin_probe_where(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht, con
  * aggregatecount.cpp:37-52). Key: in->key_bytes 4 or 8, or 0 for no GROUP BY
  * (the "alwayszero" plan). Output rows: (key, agg) packed; agg is int32 for
  * an int sum (wrapping, as the reference's CtInt +=), int64 for a long sum or
- * a count, double for a dec sum. Integer results are exact; dec sums use
- * error-compensated FP64 accumulation. groups_hint sizes the table (0: n).  */
+ * a count, double for a dec sum. Integer results are exact; dec sums are exact
+ * 192-bit fixed-point sums rounded once (the correctly rounded sum whenever the
+ * values lie within about 2^109 of the column's largest; the same bits in any
+ * row order); infinities and NaNs give IEEE's result for their groups.
+ * groups_hint sizes the table (0: n).                                      */
 /* ---------------------------------------------------------------------- */
 enum { PG_VAL_INT = 0, PG_VAL_LONG = 1, PG_VAL_DEC = 2 };
 enum { PG_AGG_SUM = 0, PG_AGG_COUNT = 1 };
@@ -353,10 +356,11 @@ int pg_groupby(pg_ctx* ctx, pg_stream stream, const pg_rel* in,
  * (join.cpp:503-562 + genericaggregate.cpp:240-282). `ht` must have been built
  * with exactly one build-side projected column (the group key, 4 or 8 bytes);
  * the probe column at val_off (val_type) is summed, or matches are counted.
- * Output rows as pg_groupby: (group, agg), order unspecified; dec sums
- * compensated. Needs a narrow dense table whose group values span a compact
- * range and 16-byte probe tuples; otherwise PG_ERR_UNSUPPORTED, and the caller
- * probes (materialised) and groups in two steps.                          */
+ * Output rows as pg_groupby: (group, agg), order unspecified; dec sums exact
+ * as pg_groupby's. Needs a narrow dense table whose group values span a
+ * compact range and 16-byte probe tuples, and a summed dec column free of
+ * infinities and NaNs; otherwise PG_ERR_UNSUPPORTED, and the caller probes
+ * (materialised) and groups in two steps.                                 */
 int pg_hashjoin_groupby(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht, const pg_rel* S,
 		uint32_t val_off, int val_type, int agg, void* out, uint64_t out_capacity, uint64_t* ngroups);
 

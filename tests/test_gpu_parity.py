@@ -597,7 +597,7 @@ def _gb_dec_check(ctx, rows, hint=0, has_key=True):
 
 
 @pytest.mark.parametrize("groups", [1, 300, 100_000])
-def test_groupby_dec_compensated(gbctx, groups):
+def test_groupby_dec_exact(gbctx, groups):
     ctx = gbctx
     rows = dg.groupby_rows(1_000_000, groups, 1e4, dg.seed_for(53))
     _gb_dec_check(ctx, rows)
