@@ -1,6 +1,8 @@
 """Serving loop: results are the same alone and in the mix, a host-side
 failure in one query leaves the others served, and a sample of results matches
-the oracle (join -> exactly rounded per-group sums, 1e-12 relative)."""
+the oracle (join -> exactly rounded per-group sums). The dec sums are exact
+fixed-point sums, so "the same" is bit for bit; the contract's 1e-12 relative
+bound is checked too."""
 import numpy as np
 import pytest
 
@@ -29,6 +31,7 @@ def _same(a, b):
     kb, vb = serving.canonical(b)
     assert np.array_equal(ka, kb)
     assert np.all(np.abs(va - vb) <= RTOL * np.abs(vb))
+    assert np.array_equal(va.view(np.int64), vb.view(np.int64))
 
 
 def test_results_identical_alone_and_mixed(ctx, catalog):
@@ -77,11 +80,12 @@ def test_results_match_oracle(ctx, catalog):
         assert np.array_equal(keys, exact[:, 0])
         ev = exact[:, 1].view(np.float64)
         assert np.all(np.abs(sums - ev) <= RTOL * np.abs(ev))
+        assert np.array_equal(np.ascontiguousarray(sums).view(np.int64), exact[:, 1])
 
 
 def test_one_pass_plan_matches_two_step_plan(ctx, catalog):
     # The fused join+group-by and the materialised probe + group-by give the
-    # same groups and sums (within the dec tolerance).
+    # same groups and the same sums, bit for bit.
     stream = ctx.stream
     for table in range(len(catalog.tables)):
         for z in (0.0, 0.8):
