@@ -2545,14 +2545,43 @@ static int hj_readback(pg_ctx* ctx, cudaStream_t s, unsigned long long* acc, con
 
 // pg_hashjoin_probe; with `pred`, the probe tuples failing it take no part
 // (only for the dense 16-byte layouts the register-loading kernels handle).
+// Stream-ordered scratch freed when it goes out of scope (after the kernels
+// queued on the stream that use it).
+struct HjScratch {
+	pg_ctx* ctx;
+	cudaStream_t s;
+	void* p = nullptr;
+	HjScratch(pg_ctx* c, cudaStream_t st) : ctx(c), s(st) { }
+	~HjScratch() { if (p) pg_free_async(ctx, s, p); }
+	HjScratch(const HjScratch&) = delete;
+	HjScratch& operator=(const HjScratch&) = delete;
+};
+
+// A hashed table far larger than L2, probed by at least as many tuples as it
+// has slots: the probe side is first partitioned on the top bits of its keys'
+// hash (PG_FN_MIXRADIX), the same bits that place a key's home slot, into a
+// scratch copy. Each stretch of the partitioned probe side then looks up one
+// slice of the table (16 MB) that stays in L2, instead of fetching a DRAM line
+// per lookup from all of it. Rows come out in partition order (join output
+// order is unspecified). Returns the number of partition bits, 0 for none.
+static uint32_t hj_probe_partition_bits(const pg_ctx* ctx, const pg_hashtable* ht, uint64_t n)
+{
+	const int64_t knob = ctx->tune[PG_TUNE_HASH_PARTITION];
+	if (knob == 1 || ht->dense || ht->dense32 || !ht->slots || ht->log2cap < 12) return 0;
+	const bool big = ht->log2cap > 22 && n >= ht->capacity;
+	if (knob != 2 && !big) return 0;
+	const uint32_t lp = ht->log2cap > 20 ? ht->log2cap - 20 : 1;
+	return std::min<uint32_t>(std::max<uint32_t>(lp, 1), 8);
+}
+
 static int hj_probe_run(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
-		const pg_rel* S, const pg_col* proj, int nproj,
+		const pg_rel* S_in, const pg_col* proj, int nproj,
 		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res, const PgPred16* pred)
 {
 	if (!ctx || !ht || !res) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe: null argument");
 	int rc;
-	if ((rc = hj_validate_rel(ctx, S, "pg_hashjoin_probe"))) return rc;
-	if ((rc = hj_validate_proj(ctx, proj, nproj, ht->wR, S->width))) return rc;
+	if ((rc = hj_validate_rel(ctx, S_in, "pg_hashjoin_probe"))) return rc;
+	if ((rc = hj_validate_proj(ctx, proj, nproj, ht->wR, S_in->width))) return rc;
 	HjCols pc;
 	if ((rc = hj_make_cols(ctx, ht, proj, nproj, &pc))) return rc;
 	const bool materialize = (flags & PG_JOIN_MATERIALIZE) != 0;
@@ -2561,7 +2590,18 @@ static int hj_probe_run(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 	if (materialize && out_capacity && !out) return pg_fail(ctx, PG_ERR_ARG, "pg_hashjoin_probe: null output");
 	cudaStream_t s = (cudaStream_t) stream;
 	res->n_out = 0; res->sum = 0;
-	if (S->n == 0) return PG_OK;
+	if (S_in->n == 0) return PG_OK;
+	pg_rel Sloc = *S_in;
+	const pg_rel* S = &Sloc;
+	HjScratch part_buf(ctx, s);
+	if (const uint32_t lp = hj_probe_partition_bits(ctx, ht, S_in->n)) {
+		if ((rc = pg_alloc_async(ctx, s, &part_buf.p, S_in->n * S_in->width))) return rc;
+		pg_hashfn f;
+		f.fn = PG_FN_MIXRADIX; f.k = 0; f.min = 0; f.max = 0; f.bucketrange = 0;
+		f.skipbits = 64 - lp; f.nbuckets = 1u << lp;
+		if ((rc = pg_partition_fn(ctx, s, S_in, f, part_buf.p, nullptr))) return rc;
+		Sloc.data = part_buf.p;
+	}
 	unsigned long long* acc = nullptr;   // [cursor, count, sum, spare]
 	if ((rc = pg_alloc_async(ctx, s, (void**) &acc, 64))) return rc;
 	PG_CUDA(ctx, cudaMemsetAsync(acc, 0, 64, s));

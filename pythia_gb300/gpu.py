@@ -73,7 +73,8 @@ SYMBOLS = ["pg_init", "pg_shutdown", "pg_last_error", "pg_device_status", "pg_st
 TUNE = {"probe_ctas_per_sm": 0, "probe_variant": 1, "dense": 2, "partition_tile": 3,
         "groupby_smem_groups": 4, "radix_bits": 5, "probe_items": 6, "probe_cache": 7, "probe_passes": 8, "groupby_path": 9,
         "probe_wide": 10, "build_spec": 11, "spin_limit": 12,
-        "l2_fetch": 13, "sort_path": 14, "groupby_ilp": 15}
+        "l2_fetch": 13, "sort_path": 14, "groupby_ilp": 15,
+        "hash_partition": 16}
 
 
 def lib_path():

@@ -138,6 +138,17 @@ def test_join_sparse_unique_keys(ctx):
     S[::777, 0] = -1
     _join_check(ctx, R, S)
     _join_check(ctx, R, S, proj=(("B", 8, 8), ("P", 0, 8)))
+    # The probe side partitioned on the keys' hash first (large hashed tables
+    # take this path; forced here): the same rows, in another order.
+    try:
+        ctx.tune(hash_partition=2)
+        _join_check(ctx, R, S)
+        _join_check(ctx, R, S, proj=(("B", 8, 8), ("P", 0, 8)))
+        _, n, sm = ctx.hashjoin(R, S, flags=gpu.JOIN_COUNT | gpu.JOIN_SUM, sum_col=1)
+        _, wn, ws = orc.hashjoin(R, S, sum_col=1, materialise=False, hash=orc.hashcfg("modulo", 1 << 12))
+        assert (n, sm) == (wn, ws)
+    finally:
+        ctx.tune(hash_partition=0)
 
 
 def test_join_dense_keys_wide_values(ctx):
@@ -267,6 +278,11 @@ def test_join_many_to_many(ctx):
     R = dg.uniform_keys(5000, 700, dg.seed_for(5))
     S = dg.uniform_keys(9000, 900, dg.seed_for(6))
     _join_check(ctx, R, S)
+    try:
+        ctx.tune(hash_partition=2, dense=2)          # hashed table, probe side partitioned first
+        _join_check(ctx, R, S)
+    finally:
+        ctx.tune(hash_partition=0, dense=0)
 
 
 def test_join_projection_orders(ctx):
