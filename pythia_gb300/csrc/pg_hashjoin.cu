@@ -1969,6 +1969,35 @@ static bool hj_vec16(const pg_rel* R, const HjBuildCols& bc)
 	return v;
 }
 
+// Stream-ordered scratch freed when it goes out of scope (after the kernels
+// queued on the stream that use it).
+struct HjScratch {
+	pg_ctx* ctx;
+	cudaStream_t s;
+	void* p = nullptr;
+	HjScratch(pg_ctx* c, cudaStream_t st) : ctx(c), s(st) { }
+	~HjScratch() { if (p) pg_free_async(ctx, s, p); }
+	HjScratch(const HjScratch&) = delete;
+	HjScratch& operator=(const HjScratch&) = delete;
+};
+
+// A hashed table far larger than L2, probed by at least as many tuples as it
+// has slots: the probe side is first partitioned on the top bits of its keys'
+// hash (PG_FN_MIXRADIX), the same bits that place a key's home slot, into a
+// scratch copy. Each stretch of the partitioned probe side then looks up one
+// slice of the table (16 MB) that stays in L2, instead of fetching a DRAM line
+// per lookup from all of it. Rows come out in partition order (join output
+// order is unspecified). Returns the number of partition bits, 0 for none.
+static uint32_t hj_probe_partition_bits(const pg_ctx* ctx, const pg_hashtable* ht, uint64_t n)
+{
+	const int64_t knob = ctx->tune[PG_TUNE_HASH_PARTITION];
+	if (knob == 1 || ht->dense || ht->dense32 || !ht->slots || ht->log2cap < 12) return 0;
+	const bool big = ht->log2cap > 22 && n >= ht->capacity;
+	if (knob != 2 && !big) return 0;
+	const uint32_t lp = ht->log2cap > 20 ? ht->log2cap - 20 : 1;
+	return std::min<uint32_t>(std::max<uint32_t>(lp, 1), 8);
+}
+
 // The table of R with host round trips: exact key and value ranges read back
 // first, then a dense layout (duplicates counted and read back) or the hashed
 // table. Fills the layout fields of `ht`.
@@ -2060,12 +2089,28 @@ static int hj_build_exact(pg_ctx* ctx, cudaStream_t s, const pg_rel* R, pg_hasht
 	// side buffer tail: [side_count u32][flags i32]
 	unsigned int* side_count = reinterpret_cast<unsigned int*>(ht->side + ht->side_cap);
 	int* flags = reinterpret_cast<int*>(side_count + 1);
+	// A table far larger than L2 whose slots hold the packed values (not row
+	// indices into R): the inserts run over a copy of R partitioned on the
+	// keys' hash, as the probe side is (hj_probe_partition_bits), so that they
+	// fill one 16 MB slice of the table at a time in L2.
+	HjScratch part_buf(ctx, s);
+	const char* Rb = (const char*) R->data;
+	if (ht->inline_val && R->n >= (1ull << 20)) {
+		if (const uint32_t lp = hj_probe_partition_bits(ctx, ht, ht->capacity)) {
+			if ((rc = pg_alloc_async(ctx, s, &part_buf.p, R->n * R->width))) return rc;
+			pg_hashfn f;
+			f.fn = PG_FN_MIXRADIX; f.k = 0; f.min = 0; f.max = 0; f.bucketrange = 0;
+			f.skipbits = 64 - lp; f.nbuckets = 1u << lp;
+			if ((rc = pg_partition_fn(ctx, s, R, f, part_buf.p, nullptr))) return rc;
+			Rb = (const char*) part_buf.p;
+		}
+	}
 	for (int attempt = 0; attempt < 2; ++attempt) {
 		PG_CUDA(ctx, cudaMemsetAsync(ht->slots, 0xFF, ht->capacity * 16, s));
 		PG_CUDA(ctx, cudaMemsetAsync(side_count, 0, 8, s));
 		if (R->n) {
 			int blocks = (int) std::min<uint64_t>(pg_div_up(R->n, 256 * HT_ILP), (uint64_t) ctx->sm_count * 16);
-			k_ht_build<<<blocks, 256, 0, s>>>((const char*) R->data, R->n, R->width, R->key_off, R->key_bytes,
+			k_ht_build<<<blocks, 256, 0, s>>>(Rb, R->n, R->width, R->key_off, R->key_bytes,
 					hj_pack_code(ht->bcols), ht->inline_val, ht->slots, ht->log2cap, ht->side, ht->side_cap,
 					side_count, flags, ctx->d_status);
 			PG_LAUNCHED(ctx);
@@ -2545,35 +2590,6 @@ static int hj_readback(pg_ctx* ctx, cudaStream_t s, unsigned long long* acc, con
 
 // pg_hashjoin_probe; with `pred`, the probe tuples failing it take no part
 // (only for the dense 16-byte layouts the register-loading kernels handle).
-// Stream-ordered scratch freed when it goes out of scope (after the kernels
-// queued on the stream that use it).
-struct HjScratch {
-	pg_ctx* ctx;
-	cudaStream_t s;
-	void* p = nullptr;
-	HjScratch(pg_ctx* c, cudaStream_t st) : ctx(c), s(st) { }
-	~HjScratch() { if (p) pg_free_async(ctx, s, p); }
-	HjScratch(const HjScratch&) = delete;
-	HjScratch& operator=(const HjScratch&) = delete;
-};
-
-// A hashed table far larger than L2, probed by at least as many tuples as it
-// has slots: the probe side is first partitioned on the top bits of its keys'
-// hash (PG_FN_MIXRADIX), the same bits that place a key's home slot, into a
-// scratch copy. Each stretch of the partitioned probe side then looks up one
-// slice of the table (16 MB) that stays in L2, instead of fetching a DRAM line
-// per lookup from all of it. Rows come out in partition order (join output
-// order is unspecified). Returns the number of partition bits, 0 for none.
-static uint32_t hj_probe_partition_bits(const pg_ctx* ctx, const pg_hashtable* ht, uint64_t n)
-{
-	const int64_t knob = ctx->tune[PG_TUNE_HASH_PARTITION];
-	if (knob == 1 || ht->dense || ht->dense32 || !ht->slots || ht->log2cap < 12) return 0;
-	const bool big = ht->log2cap > 22 && n >= ht->capacity;
-	if (knob != 2 && !big) return 0;
-	const uint32_t lp = ht->log2cap > 20 ? ht->log2cap - 20 : 1;
-	return std::min<uint32_t>(std::max<uint32_t>(lp, 1), 8);
-}
-
 static int hj_probe_run(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht,
 		const pg_rel* S_in, const pg_col* proj, int nproj,
 		void* out, uint64_t out_capacity, int flags, int sum_col, pg_join_result* res, const PgPred16* pred)
