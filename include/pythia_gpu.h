@@ -183,10 +183,10 @@ enum {
 	                                    whenever the span fits 63 bits, 2 bitonic tiles and merges always */
 	PG_TUNE_GROUPBY_ILP = 15,        /* rows in flight per thread of the dense group-by over a global table: 8
 	                                    (0: built-in) or 4 */
-	PG_TUNE_HASH_PARTITION = 16,     /* probe of a hashed table: 0 partitions the probe side on the keys' hash
-	                                    first when the table exceeds 64 MB and the probe side has as many tuples
-	                                    as the table has slots (each partition then looks up a 16 MB slice of
-	                                    the table), 1 never, 2 always */
+	PG_TUNE_HASH_PARTITION = 16,     /* hashed tables: 2 partitions the probe side (and R, for packed values) on
+	                                    the keys' hash first, so that each partition uses a 16 MB slice of the
+	                                    table; 0 (built-in) or 1: not (measured slower on the 16M x 256M
+	                                    sparse-key join) */
 	PG_TUNE_COUNT = 17
 };
 int pg_tune_set(pg_ctx* ctx, int knob, int64_t value);

@@ -32,6 +32,7 @@ __device__ __forceinline__ uint32_t part_bucket(const pg_hashfn& f, const char* 
 		const int64_t v = pg_load_key(p, kbytes);
 		return (uint32_t) (((v - f.min) & f.k) >> f.skipbits);
 	}
+	if (FN == PG_FN_MIXRADIX) return (uint32_t) (pg_mix64((uint64_t) pg_load_key(p, kbytes)) >> f.skipbits);
 	return pg_hash_field(f, p, kbytes);
 }
 
@@ -325,9 +326,12 @@ int pg_partition_fn(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, const pg_hash
 	int rc;
 	uint64_t* counts = nullptr;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &counts, (size_t) B * G * 8 + 8))) return rc;
-	const bool radix = f.fn == PG_FN_PARAMMODULO;
+	const bool radix = f.fn == PG_FN_PARAMMODULO, mix = f.fn == PG_FN_MIXRADIX;
 	if (radix)
 		k_part_hist<PG_FN_PARAMMODULO><<<(unsigned) G, 512, B * sizeof(uint32_t), s>>>((const char*) in->data, n, W,
+				in->key_off, in->key_bytes, f, tile, tpc, counts, (uint32_t) G, ctx->d_status);
+	else if (mix)
+		k_part_hist<PG_FN_MIXRADIX><<<(unsigned) G, 512, B * sizeof(uint32_t), s>>>((const char*) in->data, n, W,
 				in->key_off, in->key_bytes, f, tile, tpc, counts, (uint32_t) G, ctx->d_status);
 	else
 		k_part_hist<PART_FN_ANY><<<(unsigned) G, 512, B * sizeof(uint32_t), s>>>((const char*) in->data, n, W,
@@ -339,10 +343,15 @@ int pg_partition_fn(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, const pg_hash
 		PG_CUDA(ctx, cudaFuncSetAttribute(k_part_scatter<NWv, FNv, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)); \
 		k_part_scatter<NWv, FNv, NB><<<(unsigned) G, NWv * 32, smem, s>>>((const char*) in->data, n, W, in->key_off, \
 				in->key_bytes, f, tile, tpc, counts, (uint32_t) G, (char*) out, bulk_ok, ctx->d_status); } while (0)
-	// Radix passes (parammodulo) of 256 or 64 buckets take the specialised
-	// kernel; everything else the general one.
+	// Radix passes (parammodulo) of 256 or 64 buckets and partitions on the
+	// top bits of the key hash (mixradix, 32 to 256 buckets) take specialised
+	// kernels; everything else the general one.
 	if (NW == 8 && radix && B == 256) PS_LAUNCH(8, PG_FN_PARAMMODULO, 8);
 	else if (NW == 8 && radix && B == 64) PS_LAUNCH(8, PG_FN_PARAMMODULO, 6);
+	else if (NW == 8 && mix && B == 256) PS_LAUNCH(8, PG_FN_MIXRADIX, 8);
+	else if (NW == 8 && mix && B == 128) PS_LAUNCH(8, PG_FN_MIXRADIX, 7);
+	else if (NW == 8 && mix && B == 64) PS_LAUNCH(8, PG_FN_MIXRADIX, 6);
+	else if (NW == 8 && mix && B == 32) PS_LAUNCH(8, PG_FN_MIXRADIX, 5);
 	else if (NW == 8) PS_LAUNCH(8, PART_FN_ANY, 0);
 	else PS_LAUNCH(4, PART_FN_ANY, 0);
 #undef PS_LAUNCH
