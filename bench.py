@@ -1577,10 +1577,10 @@ def suite(args, ws, rank, local):
                           max(sub.steps, 10), sub.warmup, cpu_sample=None, want_cpu=not args.no_cpu)),
         ("cfg2a_join_16Mx256M_zipf1.0",
          lambda: run_join(sub, ws, rank, local, join_spec(1 << 24, 1 << 28, "zipf", 1.0), sub.steps, sub.warmup,
-                          e2e_steps=1, cpu_sample=1 << 23, want_cpu=not args.no_cpu)),
+                          e2e_steps=3, cpu_sample=1 << 23, want_cpu=not args.no_cpu)),
         ("cfg2a_join_16Mx256M_sparse_keys",
          lambda: run_join(sub, ws, rank, local, join_spec(1 << 24, 1 << 28, key_domain="sparse"), sub.steps,
-                          sub.warmup, e2e_steps=1, cpu_sample=1 << 23, want_cpu=not args.no_cpu)),
+                          sub.warmup, e2e_steps=3, cpu_sample=1 << 23, want_cpu=not args.no_cpu)),
         ("cfg2b_groupby_256M_1M_groups", lambda: _captured(run_op, sub, ws, rank, local, "groupby")),
         ("cfg3_mpsm_64Mx64M_count_sum", lambda: _captured(run_op, sub, ws, rank, local, "mpsm")),
         ("cfg3_mpsm_64Mx64M_materialised", lambda: _captured(run_op, sub, ws, rank, local, "mpsmmat")),
