@@ -1696,71 +1696,6 @@ k_probe16_deep(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjPr
 	if (lane == 0) atomicAdd(&agg[0], cnt_acc);
 }
 
-// Count and sum form of the deep pipeline (no rows written): the table
-// lookups of chunk c + W and the tuple loads of chunk c + 2W are in flight
-// while chunk c is folded into the warp's count and the sum of the projected
-// column sum_col (its words picked through wsel as the rows would be). One
-// pair of global atomics per CTA.
-__global__ void __launch_bounds__(PW_WARPS * 32, 3)
-k_probe16_deep_agg(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb0, uint32_t wsel,
-		uint32_t sum_w0, uint32_t sum_words, int sum_col, unsigned long long* __restrict__ agg)
-{
-	HjProbeTable tb = tb0;
-	if (!hj_spec_resolve(tb)) return;
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	const uint64_t nchunks = pg_div_up(n, PW_CHUNK);
-	const uint64_t W = (uint64_t) gridDim.x * PW_WARPS;
-	const uint64_t first = (uint64_t) blockIdx.x * PW_WARPS + warp;
-	const uint64_t keep = pg_policy_keep((tb.cache >> 4) & 7);
-	const uint64_t stream = pg_policy_evict_first();
-	const uint32_t s0 = (wsel >> (4 * sum_w0)) & 15, s1 = (wsel >> (4 * sum_w0 + 4)) & 15;
-	unsigned long long cnt_acc = 0, sum_acc = 0;
-	auto rows_of = [&](uint64_t c) -> uint32_t { return c < nchunks ? (uint32_t) pg_min64(PW_CHUNK, n - c * PW_CHUNK) : 0; };
-	auto load = [&](uint64_t c, uint4 (&t)[4]) {
-		const uint32_t rows = rows_of(c);
-		#pragma unroll
-		for (int j = 0; j < 4; ++j) {
-			const uint32_t p = j * 32 + lane;
-			t[j] = p < rows ? hj_ld_stream(S + (c * PW_CHUNK + p) * 16, stream) : make_uint4(0, 0, 0, 0);
-		}
-	};
-	uint4 cur[4], nxt[4], nx2[4];
-	uint32_t ecur[4], enxt[4];
-	load(first, cur);
-	load(first + W, nxt);
-	hj_lookup4<false>(tb, cur, rows_of(first), lane, koff, keep, ecur, PgPred16());
-	for (uint64_t c = first; c < nchunks; c += W) {
-		const uint64_t c1 = c + W, c2 = c + 2 * W;
-		if (c1 < nchunks) hj_lookup4<false>(tb, nxt, rows_of(c1), lane, koff, keep, enxt, PgPred16());
-		load(c2, nx2);
-		#pragma unroll
-		for (int j = 0; j < 4; ++j) {
-			const bool h = ecur[j] != 0xFFFFFFFFu;
-			cnt_acc += __popc(__ballot_sync(0xffffffffu, h));
-			if (h && sum_col >= 0) {
-				const uint64_t v = tb.vmin + ecur[j];
-				const uint32_t lo = hj_pick(cur[j], v, s0);
-				if (sum_words == 2) sum_acc += ((unsigned long long) hj_pick(cur[j], v, s1) << 32) | lo;
-				else sum_acc += (unsigned long long) (long long) (int32_t) lo;
-			}
-		}
-		#pragma unroll
-		for (int j = 0; j < 4; ++j) { cur[j] = nxt[j]; nxt[j] = nx2[j]; ecur[j] = enxt[j]; }
-	}
-	#pragma unroll
-	for (int o = 16; o > 0; o >>= 1) sum_acc += __shfl_down_sync(0xffffffffu, sum_acc, o);
-	__shared__ unsigned long long red[2][PW_WARPS];
-	if (lane == 0) { red[0][warp] = cnt_acc; red[1][warp] = sum_acc; }
-	__syncthreads();
-	if (threadIdx.x == 0) {
-		unsigned long long c = 0, t = 0;
-		#pragma unroll
-		for (int w = 0; w < PW_WARPS; ++w) { c += red[0][w]; t += red[1][w]; }
-		if (c) atomicAdd(&agg[0], c);
-		if (t) atomicAdd(&agg[1], t);
-	}
-}
-
 // Compacting form of the deep pipeline, for probes where a fraction of the
 // probe tuples yields rows (a Filter fused into the probe): each warp appends
 // its rows to a 512-row stage in shared memory and, before a chunk could
@@ -2517,14 +2452,6 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 									wsel, sum_w0, sum_words, nullptr, nullptr, acc + 1, sum_col, dlo, dhi, run, pr);
 					} else if (materialize && mode == 2 && (var == 0 || var == 5) && wsel == 0x5432u && passes == 1) {
 						k_probe16_deep<false><<<g5, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, out, counts, acc, PgPred16());
-					} else if (!materialize && mode == 2 && (var == 0 || var == 5) && passes == 1) {
-						// Count and sum on the deep pipeline; about eight chunks per
-						// warp, so that the pipeline fills on short probe sides too.
-						const uint64_t nch = pg_div_up(n, PW_CHUNK);
-						const int ga = (int) std::max<uint64_t>(1, std::min<uint64_t>((uint64_t) g5,
-								pg_div_up(nch, (uint64_t) PW_WARPS * 8)));
-						k_probe16_deep_agg<<<ga, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, wsel, sum_w0, sum_words, sum_col,
-								acc + 1);
 					} else if (materialize && mode == 2 && pf && wsel == 0x5432u) {
 						k_probe16_direct<true, 2, true, true><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, wsel, sum_w0,
 								sum_words, out, counts, acc, -1, dlo, dhi, run);
