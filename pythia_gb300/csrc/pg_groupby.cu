@@ -309,24 +309,27 @@ k_gb_insert_ilp(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t ko
 // groups out. A partition whose groups overflow the shared table sends the
 // excess keys to the global table (emitted afterwards).
 // ---------------------------------------------------------------------------
-#define GBP_LOG2 12
-#define GBP_SLOTS (1u << GBP_LOG2)
 #define GBP_THREADS 512
+// Slots of a partition's shared-memory table: 4096, or 2048 for dec sums
+// (key and three count words per slot), so that a CTA's table takes 64 KB and
+// three CTAs share an SM; a partition holds about 1K groups either way.
+#define GBP_SLOTS (GB_DEC ? 2048u : 4096u)
 
 // Slot of key k in a per-partition table: low bits of the mix (the top bits
 // are the partition number).
+template <uint32_t SLOTS>
 __device__ __forceinline__ uint32_t gbp_slot(unsigned long long* keys, int64_t k, int* sentinel)
 {
-	if (k == PG_EMPTY_KEY) { if (!*sentinel) atomicExch(sentinel, 1); return GBP_SLOTS; }
-	uint32_t s = (uint32_t) (pg_mix64((uint64_t) k) & (GBP_SLOTS - 1));
-	for (uint32_t probe = 0; probe < GBP_SLOTS; ++probe) {
+	if (k == PG_EMPTY_KEY) { if (!*sentinel) atomicExch(sentinel, 1); return SLOTS; }
+	uint32_t s = (uint32_t) (pg_mix64((uint64_t) k) & (SLOTS - 1));
+	for (uint32_t probe = 0; probe < SLOTS; ++probe) {
 		const unsigned long long cur = keys[s];
 		if (cur == (unsigned long long) k) return s;
 		if (cur == (unsigned long long) PG_EMPTY_KEY) {
 			const unsigned long long old = atomicCAS(&keys[s], (unsigned long long) PG_EMPTY_KEY, (unsigned long long) k);
 			if (old == (unsigned long long) PG_EMPTY_KEY || old == (unsigned long long) k) return s;
 		}
-		s = (s + 1) & (GBP_SLOTS - 1);
+		s = (s + 1) & (SLOTS - 1);
 	}
 	return UINT32_MAX;
 }
@@ -398,7 +401,7 @@ k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, 
 			} else if (!valid) {
 				continue;
 			}
-			const uint32_t s = gbp_slot(skeys, k, &s_sent);
+			const uint32_t s = gbp_slot<GBP_SLOTS>(skeys, k, &s_sent);
 			if (s != UINT32_MAX) { fold_slot<VT, AGG>(sacc, smid, stop, s, v); continue; }
 			// Shared table full: this key lives in the global table.
 			const uint64_t g = gb_slot(t.keys, t.log2cap, k, t.sentinel_used);
@@ -998,7 +1001,7 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 			fn.skipbits = 64 - lp; fn.nbuckets = P;
 			if ((rc = pg_partition_fn(ctx, s, in, fn, prow, poffs))) return rc;
 			const size_t psm = (size_t) (GBP_SLOTS + 1) * (GB_DEC ? 32 : 16);
-			const int pblocks = (int) std::min<uint64_t>(P, (uint64_t) ctx->sm_count * 2);
+			const int pblocks = (int) std::min<uint64_t>(P, (uint64_t) ctx->sm_count * 3);   // 64 KB tables: 3 per SM
 			if (path == 4) {
 				PG_CUDA(ctx, cudaFuncSetAttribute(k_gb_part_agg<VT, AGG, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) psm));
 				k_gb_part_agg<VT, AGG, false><<<pblocks, GBP_THREADS, psm, s>>>(prow, poffs, P, in->width, in->key_off,
