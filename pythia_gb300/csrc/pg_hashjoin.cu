@@ -1642,7 +1642,7 @@ __device__ __forceinline__ void hj_lookup4(const HjProbeTable& tb, const uint4 (
 }
 
 template <bool PRED>
-__global__ void __launch_bounds__(PW_WARPS * 32, 3)
+__global__ void __launch_bounds__(PW_WARPS * 32, 4)
 k_probe16_deep(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb0, char* __restrict__ out,
 		uint64_t* __restrict__ chunk_counts, unsigned long long* __restrict__ agg, const PgPred16 pr)
 {
