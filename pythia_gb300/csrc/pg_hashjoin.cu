@@ -2415,9 +2415,9 @@ static int hj_launch_unique(pg_ctx* ctx, cudaStream_t s, const pg_hashtable* ht,
 #define PD_LAUNCH(M, D, P) k_probe16_direct<M, D, P><<<dgrid, PW_WARPS * 32, 0, s>>>(S, n, koff, tb, wsel, sum_w0, \
 						sum_words, M ? out : nullptr, M ? counts : nullptr, M ? acc : acc + 1, M ? -1 : sum_col, dlo, dhi, run)
 					// The standard (P$1, B$1) rows of a narrow dense table take the
-					// deeper pipeline by default (72 CTAs per SM, 3 resident:
-					// measured best on the 16M x 256M join); variant 3 selects
-					// the one-chunk-prefetch kernel.
+					// deeper pipeline by default (72 CTAs per SM in waves, 4 resident
+					// at 64 registers: measured best on the 16M x 256M join);
+					// variant 3 selects the one-chunk-prefetch kernel.
 					const int g5 = (int) std::min<uint64_t>(wchunks, (uint64_t) ctx->sm_count *
 							(ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] > 0 ? ctx->tune[PG_TUNE_PROBE_CTAS_PER_SM] : 72));
 					if (pred) {
