@@ -181,8 +181,8 @@ enum {
 	                                    fits 63 bits (bitonic tiles and merge-path merges for wider spans and for
 	                                    inputs of at most 2^18 tuples whose span needs over 32 bits), 1 radix
 	                                    whenever the span fits 63 bits, 2 bitonic tiles and merges always */
-	PG_TUNE_GROUPBY_ILP = 15,        /* rows in flight per thread of the dense group-by over a global table: 8
-	                                    (0: built-in) or 4 */
+	PG_TUNE_GROUPBY_ILP = 15,        /* rows in flight per thread of the dense group-by over a global table: 4
+	                                    or 8 (0: built-in, 4 for dec sums, 8 otherwise) */
 	PG_TUNE_HASH_PARTITION = 16,     /* hashed tables: 2 partitions the probe side (and R, for packed values) on
 	                                    the keys' hash first, so that each partition uses a 16 MB slice of the
 	                                    table; 0 (built-in) or 1: not (measured slower on the 16M x 256M

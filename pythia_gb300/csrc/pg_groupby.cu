@@ -9,19 +9,20 @@
 // Here one open-addressing table per operator holds every group: the key word
 // is claimed with atomicCAS, accumulators are updated with atomics. Integer
 // sums and counts are exact (wrapping like the reference's CtInt/CtLong +=).
-// Dec (double) sums are exact 128-bit fixed-point integers (pg_fixsum.h): a
-// value becomes a count of units 2^s, counts add with two integer atomics
-// (low word returning its old value for the carry, then the high word), and
-// the sum is rounded to a double once at emission. Integer adds do not depend
-// on the order in which threads arrive, so every run gives the same bits; when
-// all values are within about 2^45 of the largest, the result is the
-// correctly rounded exact sum. The unit comes from the largest exponent of the
-// column (sampled, with a margin, on large inputs; a value above the bound
-// makes the operator redo the sum with the exact bound). Infinities and NaNs
-// are summed on the side and patch their groups' results. Lanes of a warp
-// that carry the same key are combined first (warp match), which cuts atomics
-// on skewed keys; with few groups each CTA aggregates into a shared-memory
-// table and merges once.
+// Dec (double) sums are exact fixed-point integers (pg_fixsum.h): a value
+// becomes a count of units 2^s, counts add into seven words per group with
+// integer atomics (a value near the column's largest: one returning add, its
+// old word giving the rare overflow into another word), and the sum is
+// rounded to a double once at emission. Integer adds do not depend on the
+// order in which threads arrive, so every run gives the same bits; when all
+// values are within 2^135 of the largest, the result is the correctly rounded
+// exact sum. The unit comes from the largest exponent of the column (sampled,
+// with a margin, on large inputs; a value above the bound makes the operator
+// redo the sum with the exact bound). Infinities and NaNs are summed on the
+// side and patch their groups' results. Lanes of a warp that carry the same
+// key are combined first (warp match), which cuts atomics on skewed keys;
+// with few groups each CTA aggregates into a shared-memory table and merges
+// once.
 #include "pg_internal.cuh"
 #include <algorithm>
 
@@ -31,42 +32,48 @@
 
 // An open-addressing group table. A group's aggregate is one word of acc (a
 // count, a long sum, an int sum in its low 4 bytes) or, for a dec sum, the
-// three words acc, mid and top of its count of units (pg_fixsum.h).
+// table words of its count of units (pg_fixsum.h) at acc[slot + k * (cap +
+// 1)], k < PG_FX_WORDS.
 struct GbTable {
 	unsigned long long* keys;   // [cap + 1]; slot cap is the group whose key is the empty marker
-	unsigned long long* acc;    // [cap + 1]
-	unsigned long long* mid;    // [cap + 1]
-	unsigned long long* top;    // [cap + 1]
+	unsigned long long* acc;    // [PG_FX_WORDS (cap + 1)]
 	int* sentinel_used;
 	uint32_t log2cap;
+	__device__ __forceinline__ uint64_t wstride() const { return (1ull << log2cap) + 1; }
 };
 
 // One row's (or a combined run's) value: an integer, or a dec sum's count.
 struct GbVal {
 	unsigned long long i;
-	pg_fx3 f;
+	pg_fx4 f;
 };
 
-// Adds v into the aggregate of slot `slot` (words acc/mid/top).
+// Adds v into the aggregate of slot `slot` (a dec sum's word k at acc[slot +
+// k * wstride]).
 template <int VT, int AGG>
-__device__ __forceinline__ void fold_slot(unsigned long long* acc, unsigned long long* mid, unsigned long long* top,
-		uint64_t slot, const GbVal& v)
+__device__ __forceinline__ void fold_slot(unsigned long long* acc, uint64_t wstride, uint64_t slot, const GbVal& v)
 {
 	if (AGG == PG_AGG_COUNT) atomicAdd(&acc[slot], v.i);
 	else if (VT == PG_VAL_LONG) atomicAdd(&acc[slot], v.i);
 	else if (VT == PG_VAL_INT) atomicAdd(reinterpret_cast<unsigned int*>(&acc[slot]), (unsigned int) v.i);
-	else pg_fx_atomic_add(&acc[slot], &mid[slot], &top[slot], v.f);
+	else pg_fx_atomic_add(&acc[slot], wstride, v.f);
+}
+
+// A dec sum's count from table words acc[slot + k * wstride].
+__device__ __forceinline__ pg_fx4 gb_table_count(const unsigned long long* acc, uint64_t wstride, uint64_t slot)
+{
+	return pg_fx_from_table(reinterpret_cast<const uint64_t*>(acc + slot), wstride);
 }
 
 // Loads one row's value (a dec value quantised for unit 2^fs, bound fb).
 template <int VT, int AGG>
 __device__ __forceinline__ GbVal gb_load_val(const char* r, uint32_t voff, int fs, int fb, uint32_t& fl)
 {
-	GbVal v = {0, {0, 0, 0}};
+	GbVal v = {0, {0, 0, 0, 0}};
 	if (AGG == PG_AGG_COUNT) v.i = 1;
 	else if (VT == PG_VAL_INT) v.i = (unsigned long long) (long long) *reinterpret_cast<const int32_t*>(r + voff);
 	else if (VT == PG_VAL_LONG) v.i = (unsigned long long) pg_load_key(r + voff, 8);
-	else v.f = pg_fx_take((uint64_t) pg_load_key(r + voff, 8), fs, fb, fl);
+	else v.f = pg_fx_widen(pg_fx_take((uint64_t) pg_load_key(r + voff, 8), fs, fb, fl));
 	return v;
 }
 
@@ -91,18 +98,18 @@ __device__ __forceinline__ uint64_t gb_slot(unsigned long long* keys, uint32_t l
 }
 
 // Combines the values of lanes in `peers` (same key) at the leader lane:
-// integer adds (192-bit for dec sums' counts of units), exact in any order.
+// integer adds (256-bit for dec sums' counts of units), exact in any order.
 template <int VT, int AGG>
 __device__ __forceinline__ void warp_combine(uint32_t peers, GbVal& v)
 {
-	GbVal t = {0, {0, 0, 0}};
+	GbVal t = {0, {0, 0, 0, 0}};
 	uint32_t m = peers;
 	while (m) {
 		const int src = __ffs(m) - 1; m &= m - 1;
 		if (GB_DEC) {
-			const pg_fx3 x = {__shfl_sync(peers, v.f.w0, src), __shfl_sync(peers, v.f.w1, src),
-			                  __shfl_sync(peers, v.f.w2, src)};
-			pg_fx_add(t.f, x);
+			const pg_fx4 x = {__shfl_sync(peers, v.f.w0, src), __shfl_sync(peers, v.f.w1, src),
+			                  __shfl_sync(peers, v.f.w2, src), __shfl_sync(peers, v.f.w3, src)};
+			pg_fx_add4(t.f, x);
 		} else {
 			t.i += __shfl_sync(peers, v.i, src);
 		}
@@ -118,14 +125,11 @@ k_gb_insert(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, 
 	extern __shared__ __align__(16) unsigned char sm[];
 	const uint32_t sc1 = SMEM ? (1u << smem_log2) + 1 : 0;
 	unsigned long long* skeys = reinterpret_cast<unsigned long long*>(sm);
-	unsigned long long* sacc = skeys + sc1;
-	unsigned long long* smid = sacc + sc1;
-	unsigned long long* stop = smid + sc1;
+	unsigned long long* sacc = skeys + sc1;                 // [PG_FX_WORDS sc1]: a dec sum's words sc1 apart
 	__shared__ int s_sentinel;
 	if (SMEM) {
-		for (uint32_t i = threadIdx.x; i < sc1; i += blockDim.x) {
-			skeys[i] = (unsigned long long) PG_EMPTY_KEY; sacc[i] = 0; smid[i] = 0; stop[i] = 0;
-		}
+		for (uint32_t i = threadIdx.x; i < sc1; i += blockDim.x) skeys[i] = (unsigned long long) PG_EMPTY_KEY;
+		for (uint32_t i = threadIdx.x; i < PG_FX_WORDS * sc1; i += blockDim.x) sacc[i] = 0;
 		if (threadIdx.x == 0) s_sentinel = 0;
 		__syncthreads();
 	}
@@ -138,7 +142,7 @@ k_gb_insert(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, 
 	for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n_round; i += stride) {
 		bool valid = i < n;
 		int64_t k = 0;
-		GbVal v = {0, {0, 0, 0}};
+		GbVal v = {0, {0, 0, 0, 0}};
 		if (valid) {
 			const char* r = in + i * W;
 			if (HASKEY) k = pg_load_key(r + koff, kbytes);
@@ -153,11 +157,11 @@ k_gb_insert(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, 
 		if (SMEM) {
 			uint64_t s = HASKEY ? gb_slot(skeys, smem_log2, k, &s_sentinel) : 0;
 			if (s == UINT64_MAX) { full = true; continue; }
-			fold_slot<VT, AGG>(sacc, smid, stop, s, v);
+			fold_slot<VT, AGG>(sacc, sc1, s, v);
 		} else {
 			uint64_t s = HASKEY ? gb_slot(t.keys, t.log2cap, k, t.sentinel_used) : 0;
 			if (s == UINT64_MAX) { full = true; continue; }
-			fold_slot<VT, AGG>(t.acc, t.mid, t.top, s, v);
+			fold_slot<VT, AGG>(t.acc, t.wstride(), s, v);
 		}
 	}
 	if (full) pg_set_status(status, PG_ERR_TABLE_FULL);
@@ -173,46 +177,10 @@ k_gb_insert(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, 
 			int64_t k = (i < sc) ? (int64_t) skeys[i] : PG_EMPTY_KEY;
 			uint64_t s = HASKEY ? gb_slot(t.keys, t.log2cap, k, t.sentinel_used) : 0;
 			if (s == UINT64_MAX) { pg_set_status(status, PG_ERR_TABLE_FULL); continue; }
-			const GbVal v = {sacc[i], {sacc[i], smid[i], stop[i]}};
-			fold_slot<VT, AGG>(t.acc, t.mid, t.top, s, v);
+			GbVal v = {sacc[i], {0, 0, 0, 0}};
+			if (GB_DEC) v.f = gb_table_count(sacc, sc1, i);
+			fold_slot<VT, AGG>(t.acc, t.wstride(), s, v);
 		}
-	}
-}
-
-// Adds dec counts v[j] of the lead rows into their slots' words, all rows'
-// adds of one word before the next word's: the low words (rarely non-zero)
-// return their old value for the carry, then the middle words (likewise),
-// then the top words without a return. With `present`, a row marks its slot
-// present when its middle-word add returned the initial 0 (the slot's first
-// such add) or it made none: one byte store per group, not per row, since
-// stores of every row onto a small present array contend on its L2 lines.
-template <int ILP>
-__device__ __forceinline__ void gb_fx_add_rows(unsigned long long* acc, unsigned long long* mid, unsigned long long* top,
-		const uint64_t (&slot)[ILP], const bool (&lead)[ILP], const pg_fx3 (&v)[ILP], uint64_t stride = 1,
-		unsigned char* present = nullptr)
-{
-	uint64_t c[ILP], x1[ILP];
-	unsigned long long o[ILP];
-	#pragma unroll
-	for (int j = 0; j < ILP; ++j) {
-		c[j] = 0;
-		if (lead[j] && v[j].w0) {
-			const unsigned long long old = atomicAdd(&acc[slot[j] * stride], (unsigned long long) v[j].w0);
-			c[j] = (uint64_t) (old + v[j].w0) < (uint64_t) old;
-		}
-	}
-	#pragma unroll
-	for (int j = 0; j < ILP; ++j) {
-		x1[j] = v[j].w1 + c[j];
-		c[j] = x1[j] < c[j];
-		o[j] = lead[j] && x1[j] ? atomicAdd(&mid[slot[j] * stride], (unsigned long long) x1[j]) : 0;
-	}
-	#pragma unroll
-	for (int j = 0; j < ILP; ++j) {
-		if (!lead[j]) continue;
-		const uint64_t x2 = v[j].w2 + c[j] + ((uint64_t) (o[j] + x1[j]) < (uint64_t) o[j]);
-		if (x2) atomicAdd(&top[slot[j] * stride], (unsigned long long) x2);
-		if (present && (x1[j] == 0 || o[j] == 0)) present[slot[j]] = 1;
 	}
 }
 
@@ -241,7 +209,7 @@ k_gb_insert_ilp(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t ko
 		for (int j = 0; j < GB_ILP; ++j) {
 			const uint64_t i = base + j * stride;
 			const bool valid = i < n;
-			k[j] = 0; v[j] = GbVal{0, {0, 0, 0}}; lead[j] = false;
+			k[j] = 0; v[j] = GbVal{0, {0, 0, 0, 0}}; lead[j] = false;
 			if (valid) {
 				const char* r = in + i * W;
 				k[j] = pg_load_key(r + koff, kbytes);
@@ -287,14 +255,14 @@ k_gb_insert_ilp(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t ko
 			if (probe == cap) { full = true; lead[j] = false; }
 		}
 		if (GB_DEC) {
-			pg_fx3 f[GB_ILP];
+			pg_fx4 f[GB_ILP];
 			#pragma unroll
 			for (int j = 0; j < GB_ILP; ++j) f[j] = v[j].f;
-			gb_fx_add_rows<GB_ILP>(t.acc, t.mid, t.top, slot, lead, f);
+			pg_fx_atomic_add_rows<GB_ILP>(t.acc, t.wstride(), slot, 1, lead, f, nullptr);
 		} else {
 			#pragma unroll
 			for (int j = 0; j < GB_ILP; ++j)
-				if (lead[j]) fold_slot<VT, AGG>(t.acc, t.mid, t.top, slot[j], v[j]);
+				if (lead[j]) fold_slot<VT, AGG>(t.acc, 1, slot[j], v[j]);
 		}
 	}
 	if (full) pg_set_status(status, PG_ERR_TABLE_FULL);
@@ -310,10 +278,11 @@ k_gb_insert_ilp(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t ko
 // excess keys to the global table (emitted afterwards).
 // ---------------------------------------------------------------------------
 #define GBP_THREADS 512
-// Slots of a partition's shared-memory table: 4096, or 2048 for dec sums
-// (key and three count words per slot), so that a CTA's table takes 64 KB and
-// three CTAs share an SM; a partition holds about 1K groups either way.
-#define GBP_SLOTS (GB_DEC ? 2048u : 4096u)
+// Slots of a partition's shared-memory table: 4096 (64 KB), or 1024 for dec
+// sums (key and seven count words per slot: 64 KB), so that three CTAs share
+// an SM; a partition holds about 1K groups, or 512 for dec sums.
+#define GBP_SLOTS (GB_DEC ? 1024u : 4096u)
+#define GBP_GROUPS (GB_DEC ? 512u : 1024u)
 
 // Slot of key k in a per-partition table: low bits of the mix (the top bits
 // are the partition number).
@@ -335,11 +304,10 @@ __device__ __forceinline__ uint32_t gbp_slot(unsigned long long* keys, int64_t k
 }
 
 // Writes one group's row: kbytes of key (none for 0), then its aggregate:
-// word a, or for a dec sum the count (a, mid, top) of units 2^fx_s rounded to
-// a double.
+// word a, or for a dec sum the count c of units 2^fx_s rounded to a double.
 template <int VT, int AGG>
 __device__ __forceinline__ void gb_write_agg(char* o, uint32_t kbytes, int64_t k, unsigned long long a,
-		unsigned long long mid, unsigned long long top, int fx_s)
+		const pg_fx4& c, int fx_s)
 {
 	if (kbytes == 4) *reinterpret_cast<int32_t*>(o) = (int32_t) k;
 	else if (kbytes == 8) {
@@ -348,10 +316,7 @@ __device__ __forceinline__ void gb_write_agg(char* o, uint32_t kbytes, int64_t k
 	}
 	o += kbytes;
 	if (AGG == PG_AGG_SUM && VT == PG_VAL_INT) { *reinterpret_cast<uint32_t*>(o) = (uint32_t) a; return; }
-	if (GB_DEC) {
-		const pg_fx3 c = {a, mid, top};
-		a = (unsigned long long) __double_as_longlong(pg_fx_double(c, fx_s));
-	}
+	if (GB_DEC) a = (unsigned long long) __double_as_longlong(pg_fx_double4(c, fx_s));
 	reinterpret_cast<uint32_t*>(o)[0] = (uint32_t) a;
 	reinterpret_cast<uint32_t*>(o)[1] = (uint32_t) (a >> 32);
 }
@@ -363,10 +328,9 @@ k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, 
 		unsigned long long* __restrict__ cursor, int* __restrict__ overflow, int* __restrict__ status)
 {
 	extern __shared__ __align__(16) unsigned char sm[];
+	constexpr uint32_t SW = GBP_SLOTS + 1;                                         // a dec sum's word stride
 	unsigned long long* skeys = reinterpret_cast<unsigned long long*>(sm);        // [SLOTS + 1]
-	unsigned long long* sacc = skeys + GBP_SLOTS + 1;                              // [SLOTS + 1]
-	unsigned long long* smid = sacc + GBP_SLOTS + 1;                               // [SLOTS + 1], dec sums only
-	unsigned long long* stop = smid + GBP_SLOTS + 1;                               // [SLOTS + 1], dec sums only
+	unsigned long long* sacc = skeys + SW;                                         // [SLOTS + 1], PG_FX_WORDS [SLOTS + 1] for dec
 	__shared__ int s_sent;
 	__shared__ uint32_t wtot[GBP_THREADS / 32];
 	__shared__ unsigned long long s_base;
@@ -377,7 +341,8 @@ k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, 
 	for (uint32_t part = blockIdx.x; part < P; part += gridDim.x) {
 		for (uint32_t i = tid; i <= GBP_SLOTS; i += blockDim.x) {
 			skeys[i] = (unsigned long long) PG_EMPTY_KEY; sacc[i] = 0;
-			if (GB_DEC) { smid[i] = 0; stop[i] = 0; }
+			if (GB_DEC)
+				for (int w = 1; w < PG_FX_WORDS; ++w) sacc[i + w * SW] = 0;
 		}
 		if (tid == 0) s_sent = 0;
 		__syncthreads();
@@ -386,7 +351,7 @@ k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, 
 		for (uint64_t i = lo + tid; i < lo + pg_div_up(hi - lo, 32) * 32; i += blockDim.x) {
 			const bool valid = i < hi;
 			int64_t k = 0;
-			GbVal v = {0, {0, 0, 0}};
+			GbVal v = {0, {0, 0, 0, 0}};
 			if (valid) {
 				const char* r = rows + i * W;
 				k = pg_load_key(r + koff, kbytes);
@@ -402,11 +367,11 @@ k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, 
 				continue;
 			}
 			const uint32_t s = gbp_slot<GBP_SLOTS>(skeys, k, &s_sent);
-			if (s != UINT32_MAX) { fold_slot<VT, AGG>(sacc, smid, stop, s, v); continue; }
+			if (s != UINT32_MAX) { fold_slot<VT, AGG>(sacc, SW, s, v); continue; }
 			// Shared table full: this key lives in the global table.
 			const uint64_t g = gb_slot(t.keys, t.log2cap, k, t.sentinel_used);
 			if (g == UINT64_MAX) { pg_set_status(status, PG_ERR_TABLE_FULL); continue; }
-			fold_slot<VT, AGG>(t.acc, t.mid, t.top, g, v);
+			fold_slot<VT, AGG>(t.acc, t.wstride(), g, v);
 			spilled = true;
 		}
 		if (spilled) atomicExch(overflow, 1);
@@ -433,7 +398,7 @@ k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, 
 			if (!used) continue;
 			if (pos < out_cap)
 				gb_write_agg<VT, AGG>(out + pos * ow, kbytes, i < GBP_SLOTS ? (int64_t) skeys[i] : PG_EMPTY_KEY,
-						sacc[i], GB_DEC ? smid[i] : 0, GB_DEC ? stop[i] : 0, fs);
+						sacc[i], GB_DEC ? gb_table_count(sacc, SW, i) : pg_fx4{0, 0, 0, 0}, fs);
 			++pos;
 		}
 		__syncthreads();
@@ -468,8 +433,8 @@ __global__ void k_gb_emit(GbTable t, uint32_t kbytes, char* __restrict__ out, ui
 		uint64_t pos = base + __popc(ball & ((1u << lane) - 1));
 		if (pos >= cap_rows) continue;
 		const int64_t k = HASKEY ? (i < cap ? (int64_t) t.keys[i] : PG_EMPTY_KEY) : 0;
-		gb_write_agg<VT, AGG>(out + pos * ow, HASKEY ? kbytes : 0, k, t.acc[i], GB_DEC ? t.mid[i] : 0,
-				GB_DEC ? t.top[i] : 0, fx_s);
+		gb_write_agg<VT, AGG>(out + pos * ow, HASKEY ? kbytes : 0, k, t.acc[i],
+				GB_DEC ? gb_table_count(t.acc, t.wstride(), i) : pg_fx4{0, 0, 0, 0}, fx_s);
 	}
 }
 
@@ -477,8 +442,11 @@ __global__ void k_gb_emit(GbTable t, uint32_t kbytes, char* __restrict__ out, ui
 // Dense key domain (keys span at most a few times the group count, e.g.
 // group numbers 0..G-1 or surrogate keys): a min/max pass, then the slot of a
 // row is key - kmin. No probing and no key words: a row costs its atomics
-// (two for a typical dec value, one otherwise) and, for sums, a byte store
-// marking the group present. A dec sum's slot is PG_FX_SLOT words.
+// (one for a typical dec value, as for the integer aggregates) and, for
+// sums, a byte store marking the group present. A dec sum's table keeps
+// each of its PG_FX_WORDS words in an array of its own (word k of slot i at
+// acc[i + k * range]), so the word every row adds into takes 8 bytes a group
+// of L2.
 // ---------------------------------------------------------------------------
 // Min and max key over rows 0, step, 2 step, ... (step 1: every row).
 template <bool VEC16>
@@ -563,7 +531,7 @@ k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, u
 			else iv[j] = vbits;
 		}
 		if (GB_DEC) {
-			gb_fx_add_rows<ILP>(acc, acc + 1, acc + 2, d, ok, f, PG_FX_SLOT, present);
+			pg_fx_atomic_add_rows<ILP>(acc, range, d, 1, ok, f, present);
 		} else {
 			#pragma unroll
 			for (int j = 0; j < ILP; ++j) {
@@ -580,18 +548,19 @@ k_gb_dense(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, u
 }
 
 // Dense group-by over a window of at most GBS_MAX_SLOTS keys: each CTA sums
-// its rows into a copy of the table in shared memory (dec sums' three count
+// its rows into a copy of the table in shared memory (dec sums' seven table
 // words, int sums in the low 4 bytes, counts and long sums in 8), then adds
 // each slot it saw into the global table once. Few groups otherwise put every
 // row's atomic on a handful of L2 lines.
 #define GBS_MAX_SLOTS 4096
+#define GBS_MAX_SLOTS_DEC 1536                     // 57 bytes a slot: two CTAs per SM
 template <int VT, int AGG, bool VEC16>
 __global__ void __launch_bounds__(GB_THREADS)
 k_gb_dense_smem(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t koff, uint32_t kbytes, uint32_t voff,
 		long long kmin, uint32_t range, unsigned long long* __restrict__ acc, PgFx fx,
 		unsigned char* __restrict__ present, unsigned int* __restrict__ overflow)
 {
-	constexpr uint32_t SW = GB_DEC ? 3 : 1;                                           // shared words per slot
+	constexpr uint32_t SW = GB_DEC ? PG_FX_WORDS : 1;                                 // shared words per slot
 	extern __shared__ __align__(16) unsigned char gsm[];
 	unsigned long long* const sacc = reinterpret_cast<unsigned long long*>(gsm);
 	unsigned char* const spres = gsm + (size_t) range * SW * 8;
@@ -626,7 +595,7 @@ k_gb_dense_smem(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t ko
 		#pragma unroll
 		for (int j = 0; j < GBD_ILP; ++j) {
 			if (!ok[j]) continue;
-			if (GB_DEC) pg_fx_atomic_add(&sacc[3 * d[j]], &sacc[3 * d[j] + 1], &sacc[3 * d[j] + 2], f[j]);
+			if (GB_DEC) pg_fx_atomic_add(&sacc[d[j]], range, pg_fx_widen(f[j]));
 			else if (VT == PG_VAL_INT && AGG == PG_AGG_SUM)
 				atomicAdd(reinterpret_cast<unsigned int*>(&sacc[d[j]]), (unsigned int) iv[j]);
 			else atomicAdd(&sacc[d[j]], iv[j]);
@@ -642,10 +611,7 @@ k_gb_dense_smem(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t ko
 			continue;
 		}
 		if (!spres[i]) continue;
-		if (GB_DEC) {
-			const pg_fx3 c = {sacc[3 * i], sacc[3 * i + 1], sacc[3 * i + 2]};
-			pg_fx_atomic_add(&acc[PG_FX_SLOT * i], &acc[PG_FX_SLOT * i + 1], &acc[PG_FX_SLOT * i + 2], c);
-		}
+		if (GB_DEC) pg_fx_atomic_add(&acc[i], range, gb_table_count(sacc, range, i));
 		else if (VT == PG_VAL_INT) atomicAdd(reinterpret_cast<unsigned int*>(&acc[i]), (unsigned int) sacc[i]);
 		else atomicAdd(&acc[i], sacc[i]);
 		present[i] = 1;
@@ -674,9 +640,8 @@ __global__ void k_gb_dense_emit(const unsigned long long* __restrict__ acc, PgFx
 		if (pos >= cap_rows) continue;
 		const int64_t k = (int64_t) ((uint64_t) kmin + i);
 		if (GB_DEC)
-			gb_write_agg<VT, AGG>(out + pos * ow, kbytes, k, acc[PG_FX_SLOT * i], acc[PG_FX_SLOT * i + 1],
-					acc[PG_FX_SLOT * i + 2], fx_s);
-		else gb_write_agg<VT, AGG>(out + pos * ow, kbytes, k, acc[i], 0, 0, 0);
+			gb_write_agg<VT, AGG>(out + pos * ow, kbytes, k, 0, gb_table_count(acc, range, i), fx_s);
+		else gb_write_agg<VT, AGG>(out + pos * ow, kbytes, k, acc[i], pg_fx4{0, 0, 0, 0}, 0);
 	}
 }
 
@@ -700,10 +665,10 @@ __global__ void k_fx_max_field(const char* __restrict__ in, uint64_t n, uint32_t
 }
 
 // p[0] unit exponent, p[1] bound, p[2] flags cleared, from the field in p[3].
-__global__ void k_fx_finish(int* __restrict__ p, uint64_t n, int margin)
+__global__ void k_fx_finish(int* __restrict__ p, int margin)
 {
 	const int bound = min(p[3] + margin, PG_FX_EXP_SPECIAL - 1);
-	p[0] = pg_fx_unit(bound, n);
+	p[0] = pg_fx_unit(bound);
 	p[1] = bound;
 	p[2] = 0;
 }
@@ -718,7 +683,7 @@ int pg_fx_prepare(pg_ctx* ctx, cudaStream_t s, const char* data, uint64_t n, uin
 		k_fx_max_field<<<blocks, 256, 0, s>>>(data, n, W, voff, step, fx.p);
 		PG_LAUNCHED(ctx);
 	}
-	k_fx_finish<<<1, 1, 0, s>>>(fx.p, n, step > 1 ? margin : 0);
+	k_fx_finish<<<1, 1, 0, s>>>(fx.p, step > 1 ? margin : 0);
 	PG_LAUNCHED(ctx);
 	return PG_OK;
 }
@@ -825,17 +790,17 @@ static int gb_dense_window(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32
 {
 	int rc;
 	char* mem = nullptr;
-	const uint64_t words = range * (GB_DEC ? PG_FX_SLOT : 1);
+	const uint64_t words = range * (GB_DEC ? PG_FX_WORDS : 1);
 	const size_t bytes = words * 8 + range + 128;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &mem, bytes))) return rc;
-	unsigned long long* acc = reinterpret_cast<unsigned long long*>(mem);      // PG_FX_SLOT words per slot for a dec sum
+	unsigned long long* acc = reinterpret_cast<unsigned long long*>(mem);      // a dec sum: word k of slot i at acc[i + k range]
 	unsigned long long* cursor = acc + words;
 	unsigned char* present = reinterpret_cast<unsigned char*>(cursor + 1);
 	unsigned int* oflag = reinterpret_cast<unsigned int*>((reinterpret_cast<uintptr_t>(present + range) + 15) & ~uintptr_t(15));
 	PG_CUDA(ctx, cudaMemsetAsync(mem, 0, bytes, s));
-	if (range <= GBS_MAX_SLOTS && ctx->tune[PG_TUNE_GROUPBY_PATH] != 7) {
+	if (range <= (GB_DEC ? GBS_MAX_SLOTS_DEC : GBS_MAX_SLOTS) && ctx->tune[PG_TUNE_GROUPBY_PATH] != 7) {
 		// Few groups: per-CTA tables in shared memory, one flush each.
-		const int sbytes = (int) (range * (GB_DEC ? 25 : 9));
+		const int sbytes = (int) (range * (GB_DEC ? 8 * PG_FX_WORDS + 1 : 9));
 		int per_sm = 0;
 		if (vec16) {
 			PG_CUDA(ctx, cudaFuncSetAttribute(k_gb_dense_smem<VT, AGG, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sbytes));
@@ -852,10 +817,11 @@ static int gb_dense_window(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32
 				in->width, in->key_off, in->key_bytes, voff, kmin, (uint32_t) range, acc, fx, present, oflag);
 		PG_LAUNCHED(ctx);
 	} else {
-		// Eight rows in flight per thread by default (measured: 3.74 against
-		// 3.87 ms for 256M rows in 1M groups); the kernel waits on the returning
-		// atomic of each row's count.
-		const int ilp = ctx->tune[PG_TUNE_GROUPBY_ILP] == 4 ? GBD_ILP : 8;
+		// Rows in flight per thread: eight for counts and integer sums, four for
+		// dec sums, whose kernel holds more registers a row (85 at eight rows:
+		// 3.60 against 2.74 ms at four for 256M rows in 1M groups).
+		const int64_t knob = ctx->tune[PG_TUNE_GROUPBY_ILP];
+		const int ilp = knob == 4 ? GBD_ILP : knob == 8 ? 8 : GB_DEC ? GBD_ILP : 8;
 		const int gblocks = (int) std::min<uint64_t>(pg_div_up(in->n, (uint64_t) GB_THREADS * ilp),
 				(uint64_t) ctx->sm_count * 8);
 #define GBD_LAUNCH(V, I) k_gb_dense<VT, AGG, V, I><<<gblocks, GB_THREADS, 0, s>>>((const char*) in->data, in->n, \
@@ -970,17 +936,15 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 		t.log2cap = lg;
 		char* mem = nullptr;
 		int rc;
-		size_t bytes = (cap + 1) * 32 + 64;
+		size_t bytes = (cap + 1) * 8 * (1 + PG_FX_WORDS) + 64;
 		if ((rc = pg_alloc_async(ctx, s, (void**) &mem, bytes))) return rc;
 		t.keys = reinterpret_cast<unsigned long long*>(mem);
 		t.acc = t.keys + cap + 1;
-		t.mid = t.acc + cap + 1;
-		t.top = t.mid + cap + 1;
-		t.sentinel_used = reinterpret_cast<int*>(t.top + cap + 1);
+		t.sentinel_used = reinterpret_cast<int*>(t.acc + PG_FX_WORDS * (cap + 1));
 		unsigned long long* cursor = reinterpret_cast<unsigned long long*>(t.sentinel_used + 2);
 		PG_CUDA(ctx, cudaMemsetAsync(t.keys, 0xFF, (cap + 1) * 8, s));
-		PG_CUDA(ctx, cudaMemsetAsync(t.acc, 0, (cap + 1) * 24 + 64, s));
-		const bool smem = groups <= GB_SMEM_SLOTS / 2;
+		PG_CUDA(ctx, cudaMemsetAsync(t.acc, 0, (cap + 1) * 8 * PG_FX_WORDS + 64, s));
+		const bool smem = groups <= GB_SMEM_SLOTS / (GB_DEC ? 8 : 2);       // tables up to 66 KB
 		// Path knob: 0 by size, 1 global table (warp-combined), 2 partitioned,
 		// 3 global table without the warp combine.
 		const int64_t path = ctx->tune[PG_TUNE_GROUPBY_PATH];
@@ -989,7 +953,7 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 		if (part_ok && (path == 2 || path == 4 || (path == 0 && in->n >= 4 * groups))) {
 			// High cardinality: partition by key hash, aggregate per partition.
 			uint32_t lp = 1;
-			while ((1ull << lp) < groups / 1024 && lp < 12) ++lp;
+			while ((1ull << lp) < groups / GBP_GROUPS && lp < 12) ++lp;
 			const uint32_t P = 1u << lp;
 			char* prow = nullptr;
 			uint64_t* poffs = nullptr;
@@ -1000,7 +964,7 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 			fn.fn = PG_FN_MIXRADIX; fn.k = 0; fn.min = 0; fn.max = 0; fn.bucketrange = 0;
 			fn.skipbits = 64 - lp; fn.nbuckets = P;
 			if ((rc = pg_partition_fn(ctx, s, in, fn, prow, poffs))) return rc;
-			const size_t psm = (size_t) (GBP_SLOTS + 1) * (GB_DEC ? 32 : 16);
+			const size_t psm = (size_t) (GBP_SLOTS + 1) * (GB_DEC ? 8 * (1 + PG_FX_WORDS) : 16);
 			const int pblocks = (int) std::min<uint64_t>(P, (uint64_t) ctx->sm_count * 3);   // 64 KB tables: 3 per SM
 			if (path == 4) {
 				PG_CUDA(ctx, cudaFuncSetAttribute(k_gb_part_agg<VT, AGG, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) psm));
@@ -1037,7 +1001,7 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 		uint32_t slg = 1;
 		while ((1u << slg) < 2 * groups) ++slg;
 		if (!haskey) slg = 0;
-		const size_t smem_bytes = smem ? ((size_t) (1u << slg) + 1) * 32 : 0;
+		const size_t smem_bytes = smem ? ((size_t) (1u << slg) + 1) * 8 * (1 + PG_FX_WORDS) : 0;
 		int blocks = (int) std::min<uint64_t>(pg_div_up(std::max<uint64_t>(in->n, 1), GB_THREADS),
 				(uint64_t) ctx->sm_count * (smem ? 4 : 8));
 		if (in->n) {

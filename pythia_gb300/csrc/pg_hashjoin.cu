@@ -2976,14 +2976,14 @@ extern "C" int pg_hashjoin_host(pg_ctx* ctx, const pg_rel* Rh, const pg_rel* Sh,
 // group key is the table's value (the one projected build column); a narrow
 // dense table stores value - vmin, which is the row's group slot directly. The
 // probe-side value is folded into a dense group table with the atomics of the
-// group-by (a dec value as an exact count of units 2^s in three words: for a
-// value near the column's largest, one returning atomic and one plain), so
-// the join rows are never written.
+// group-by (a dec value as an exact count of units 2^s in four words: for a
+// value near the column's largest, one returning atomic), so the join rows
+// are never written.
 // ---------------------------------------------------------------------------
 template <int VT, int AGG>
 __global__ void __launch_bounds__(PW_WARPS * 32, 4)
 k_probe16_groupby(const char* __restrict__ S, uint64_t n, uint32_t koff, const HjProbeTable tb, uint32_t voff,
-		uint32_t goff, unsigned long long* __restrict__ acc, PgFx fx, unsigned char* __restrict__ present)
+		uint32_t goff, unsigned long long* __restrict__ acc, uint64_t wst, PgFx fx, unsigned char* __restrict__ present)
 {
 	constexpr bool DEC = AGG == PG_AGG_SUM && VT == PG_VAL_DEC;
 	constexpr int ITEMS = PW_CHUNK / 32;
@@ -3022,38 +3022,23 @@ k_probe16_groupby(const char* __restrict__ S, uint64_t n, uint32_t koff, const H
 			if (e[j] != 0xFFFFFFFFu) e[j] -= goff;      // group slot: value - smallest value
 		}
 		if (DEC) {
-			// PG_FX_SLOT words per group; each word's adds for all items before
-			// the next word's, carries from the returned old words.
+			// PG_FX_WORDS words per group, word k at acc[group + k * wst]
+			// (pg_fx_atomic_add_rows): a value near the column's largest is one
+			// returning add; the first add into a group returns the initial 0
+			// and marks it present once.
 			pg_fx3 f[ITEMS];
-			uint64_t c[ITEMS], x1[ITEMS];
-			unsigned long long o[ITEMS];
+			uint64_t slot[ITEMS];
+			bool ok[ITEMS];
 			#pragma unroll
 			for (int j = 0; j < ITEMS; ++j) {
 				const uint4 t = cur[j];
-				f[j] = pg_fx3{0, 0, 0}; c[j] = 0;
-				if (e[j] == 0xFFFFFFFFu) continue;
-				f[j] = pg_fx_take(voff == 0 ? (((uint64_t) t.y << 32) | t.x) : (((uint64_t) t.w << 32) | t.z), fs, fb, fl);
-				if (f[j].w0) {
-					const unsigned long long old = atomicAdd(&acc[PG_FX_SLOT * (uint64_t) e[j]], (unsigned long long) f[j].w0);
-					c[j] = (uint64_t) (old + f[j].w0) < (uint64_t) old;
-				}
+				ok[j] = e[j] != 0xFFFFFFFFu;
+				slot[j] = ok[j] ? e[j] : 0;
+				f[j] = ok[j] ? pg_fx_take(voff == 0 ? (((uint64_t) t.y << 32) | t.x) : (((uint64_t) t.w << 32) | t.z),
+				                          fs, fb, fl)
+				             : pg_fx3{0, 0, 0};
 			}
-			#pragma unroll
-			for (int j = 0; j < ITEMS; ++j) {
-				x1[j] = f[j].w1 + c[j];
-				c[j] = x1[j] < c[j];
-				o[j] = e[j] != 0xFFFFFFFFu && x1[j] ? atomicAdd(&acc[PG_FX_SLOT * (uint64_t) e[j] + 1], (unsigned long long) x1[j]) : 0;
-			}
-			#pragma unroll
-			for (int j = 0; j < ITEMS; ++j) {
-				if (e[j] == 0xFFFFFFFFu) continue;
-				const uint64_t x2 = f[j].w2 + c[j] + ((uint64_t) (o[j] + x1[j]) < (uint64_t) o[j]);
-				if (x2) atomicAdd(&acc[PG_FX_SLOT * (uint64_t) e[j] + 2], (unsigned long long) x2);
-				// Present once per group: the first middle-word add returns the
-				// initial 0 (a row without one marks it itself). Every row storing
-				// onto the small present array would contend on its L2 lines.
-				if (x1[j] == 0 || o[j] == 0) present[e[j]] = 1;
-			}
+			pg_fx_atomic_add_rows<ITEMS>(acc, wst, slot, 1, ok, f, present);
 		} else {
 			#pragma unroll
 			for (int j = 0; j < ITEMS; ++j) {
@@ -3097,11 +3082,11 @@ extern "C" int pg_hashjoin_groupby(pg_ctx* ctx, pg_stream stream, pg_hashtable* 
 	cudaStream_t s = (cudaStream_t) stream;
 	const bool dec = agg == PG_AGG_SUM && val_type == PG_VAL_DEC;
 	char* mem = nullptr;
-	const uint64_t words = vrange * (dec ? PG_FX_SLOT : 1);
+	const uint64_t words = vrange * (dec ? PG_FX_WORDS : 1);
 	const size_t pres_end = (words + 1) * 8 + ((vrange + 15) & ~15ull);
 	const size_t bytes = pres_end + 16;
 	if ((rc = pg_alloc_async(ctx, s, (void**) &mem, bytes))) return rc;
-	unsigned long long* acc = reinterpret_cast<unsigned long long*>(mem);   // PG_FX_SLOT words per group for a dec sum
+	unsigned long long* acc = reinterpret_cast<unsigned long long*>(mem);   // a dec sum: word k of group g at acc[g + k vrange]
 	unsigned long long* cursor = acc + words;
 	unsigned char* present = reinterpret_cast<unsigned char*>(cursor + 1);
 	PgFx fx = {reinterpret_cast<int*>(mem + pres_end)};
@@ -3117,7 +3102,7 @@ extern "C" int pg_hashjoin_groupby(pg_ctx* ctx, pg_stream stream, pg_hashtable* 
 			tb.dense32 = ht->dense32; tb.vmin = ht->vmin; tb.dmin = ht->dmin; tb.drange = ht->drange;
 			const int grid = (int) std::min<uint64_t>(pg_div_up(pg_div_up(S->n, PW_CHUNK), PW_WARPS), (uint64_t) ctx->sm_count * 24);
 #define PG_LAUNCH(VT, AGG) k_probe16_groupby<VT, AGG><<<grid, PW_WARPS * 32, 0, s>>>((const char*) S->data, S->n, \
-					S->key_off, tb, val_off, (uint32_t) (ht->vlo - ht->vmin), acc, fx, present)
+					S->key_off, tb, val_off, (uint32_t) (ht->vlo - ht->vmin), acc, vrange, fx, present)
 			if (agg == PG_AGG_COUNT) PG_LAUNCH(PG_VAL_LONG, PG_AGG_COUNT);
 			else if (val_type == PG_VAL_INT) PG_LAUNCH(PG_VAL_INT, PG_AGG_SUM);
 			else if (val_type == PG_VAL_LONG) PG_LAUNCH(PG_VAL_LONG, PG_AGG_SUM);

@@ -362,8 +362,8 @@ __host__ __device__ __forceinline__ uint32_t pg_min32(uint32_t a, uint32_t b) { 
 // Exclusive scan of n uint64 values in place on the device (multi-block).
 int pg_scan_u64(pg_ctx* ctx, cudaStream_t s, uint64_t* data, uint64_t n, uint64_t* total_dev);
 
-// Dec sums as exact 128-bit fixed-point integers (pg_fixsum.h): order-
-// independent, so a group's sum is the same on every run.
+// Dec sums as exact fixed-point integers (pg_fixsum.h): order-independent,
+// so a group's sum is the same on every run.
 #include "pg_fixsum.h"
 
 // The unit of one dec sum, in four device words made by pg_fx_prepare:
@@ -377,9 +377,6 @@ struct PgFx {
 	int* p;
 };
 #define PG_FX_RANGE 2u
-// Words per group of a dense dec-sum table: the count's three and a spare,
-// so that a row's atomics fall in one 32-byte sector.
-#define PG_FX_SLOT 4
 #define PG_FX_SPECIALS 4u
 
 // Quantises the dec value with bit pattern b for unit 2^s and bound `bound`.
@@ -391,26 +388,58 @@ __device__ __forceinline__ pg_fx3 pg_fx_take(uint64_t b, int s, int bound, uint3
 	return pg_fx_quant(b, s);
 }
 
-// Adds the count a into table words (*w0, *w1, *w2): an add that can carry
-// returns the old word, whose overflow is the carry into the next word. A
-// value near the column's largest has w0 = 0, so this is one returning add
-// and one plain add.
-__device__ __forceinline__ void pg_fx_atomic_add(unsigned long long* w0, unsigned long long* w1, unsigned long long* w2,
-		const pg_fx3& a)
+// The upper word of a value's count (sign extension) or of a sum's.
+__device__ __forceinline__ uint64_t pg_fx_hi(const pg_fx3& a) { return (uint64_t) ((int64_t) a.w2 >> 63); }
+__device__ __forceinline__ uint64_t pg_fx_hi(const pg_fx4& a) { return a.w3; }
+
+// Adds count a into one group's table words (word k at t[k * stride]) with
+// atomics (pg_fx_table_add). Returns whether the group's present marker is
+// to be set (an add returned 0, or none was made).
+__device__ __forceinline__ bool pg_fx_atomic_add(unsigned long long* t, uint64_t stride, const pg_fx4& a)
 {
-	uint64_t c = 0;
-	if (a.w0) {
-		const unsigned long long old = atomicAdd(w0, (unsigned long long) a.w0);
-		c = (uint64_t) (old + a.w0) < (uint64_t) old;
+	return pg_fx_table_add(reinterpret_cast<uint64_t*>(t), stride, a, [](uint64_t* p, uint64_t v) {
+		return (uint64_t) atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long) v);
+	});
+}
+
+// The same for ILP rows at once: word k of row j's group at base[slot[j] *
+// sstride + k * wstride]. The low bits' chunks of the rows (values far below
+// the column's largest) go to the lazy words first, with adds that return
+// nothing; then the returning t2 adds of all rows are issued together, and
+// each row reads its old t2 for the rare overflow into t3. So a row waits
+// for one L2 round trip, with only its t2 part, old word and slot live across
+// it. Rows with ok[j] false are skipped. With `present`, a row whose t2 add
+// returned the initial 0 (or that made none) marks its slot present: a byte
+// store per group rather than per row.
+template <int ILP, class V>
+__device__ __forceinline__ void pg_fx_atomic_add_rows(unsigned long long* base, uint64_t wstride,
+		const uint64_t (&slot)[ILP], uint64_t sstride, const bool (&ok)[ILP], const V (&a)[ILP],
+		unsigned char* present)
+{
+	#pragma unroll
+	for (int j = 0; j < ILP; ++j) {
+		if (!ok[j] || !(a[j].w0 | a[j].w1)) continue;
+		#pragma unroll
+		for (int k = 0; k < PG_FX_LAZY; ++k) {
+			const uint64_t c = pg_fx_chunk(a[j].w0, a[j].w1, k);
+			if (c) atomicAdd(&base[slot[j] * sstride + (PG_FX_L0 + k) * wstride], (unsigned long long) c);
+		}
 	}
-	const uint64_t x1 = a.w1 + c;
-	c = x1 < c;
-	if (x1) {
-		const unsigned long long old = atomicAdd(w1, (unsigned long long) x1);
-		c += (uint64_t) (old + x1) < (uint64_t) old;
+	unsigned long long o[ILP];                              // old t2; 1 where no add was made
+	#pragma unroll
+	for (int j = 0; j < ILP; ++j)
+		o[j] = ok[j] && a[j].w2 ? atomicAdd(&base[slot[j] * sstride + PG_FX_T2 * wstride], (unsigned long long) a[j].w2)
+		                        : 1;
+	#pragma unroll
+	for (int j = 0; j < ILP; ++j) {
+		if (!ok[j]) continue;
+		int64_t r;
+		uint64_t q;
+		pg_fx_split_top(a[j].w2, pg_fx_hi(a[j]), r, q);
+		if (r) q += pg_fx_overflow(o[j], r);
+		if (q) atomicAdd(&base[slot[j] * sstride + PG_FX_T3 * wstride], (unsigned long long) q);
+		if (present && (o[j] == 0 || !a[j].w2)) present[slot[j]] = 1;
 	}
-	const uint64_t x2 = a.w2 + c;
-	if (x2) atomicAdd(w2, (unsigned long long) x2);
 }
 
 // Fills fx->p (16 bytes of device memory, allocated by the caller) for a dec
@@ -426,7 +455,8 @@ int pg_fx_prepare(pg_ctx* ctx, cudaStream_t s, const char* data, uint64_t n, uin
 int pg_fx_patch_specials(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, char* out, uint64_t ngroups);
 
 // Dense group table emission (pg_groupby.cu): acc holds a word per slot, or
-// for a dec sum four words per slot, the first three its count of units (fx).
+// for a dec sum the PG_FX_WORDS table words of its count of units (fx), word
+// k of slot i at acc[i + k * range].
 int pg_dense_groups_emit(pg_ctx* ctx, cudaStream_t s, const unsigned long long* acc, PgFx fx,
 		const unsigned char* present, uint64_t range, long long kmin, uint32_t kbytes, int val_type, int agg,
 		void* out, uint64_t out_cap, unsigned long long* cursor);

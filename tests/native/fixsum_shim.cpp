@@ -1,9 +1,20 @@
 // Host entry points over pythia_gb300/csrc/pg_fixsum.h for the Python test:
-// quantisation of doubles to counts of units 2^s and the rounding of a
-// 192-bit count back to a double, checked there against exact fractions.
+// quantisation of doubles to counts of units 2^s, the table adds of the GPU
+// kernels (run here one at a time, with plain adds in place of atomics) and
+// the rounding of a count back to a double, checked there against exact
+// fractions.
 #include "pg_fixsum.h"
 
-extern "C" int fx_unit(int field, uint64_t n) { return pg_fx_unit(field, n); }
+static uint64_t plain_add(uint64_t* p, uint64_t v)
+{
+	const uint64_t old = *p;
+	*p = old + v;
+	return old;
+}
+
+extern "C" int fx_unit(int field) { return pg_fx_unit(field); }
+
+extern "C" int fx_words() { return PG_FX_WORDS; }
 
 extern "C" int fx_field(double x)
 {
@@ -12,18 +23,18 @@ extern "C" int fx_field(double x)
 	return pg_fx_field(b);
 }
 
-// Sums xs[0..n) (all finite, fields <= the bound s was made from) as the GPU
-// kernels do, in the given order; returns the double, the count in w[0..3).
-extern "C" double fx_sum(const double* xs, uint64_t n, int s, uint64_t* w)
+// Sums xs[0..n) (all finite, fields <= the bound s was made from) into table
+// words t[0..PG_FX_WORDS) as the GPU kernels do, in the given order; returns
+// the double.
+extern "C" double fx_sum(const double* xs, uint64_t n, int s, uint64_t* t)
 {
-	pg_fx3 a = {0, 0, 0};
+	for (int k = 0; k < PG_FX_WORDS; ++k) t[k] = 0;
 	for (uint64_t i = 0; i < n; ++i) {
 		uint64_t b;
 		memcpy(&b, &xs[i], 8);
-		pg_fx_add(a, pg_fx_quant(b, s));
+		pg_fx_table_add(t, 1, pg_fx_widen(pg_fx_quant(b, s)), plain_add);
 	}
-	w[0] = a.w0; w[1] = a.w1; w[2] = a.w2;
-	return pg_fx_double(a, s);
+	return pg_fx_table_double(t, 1, s);
 }
 
 extern "C" void fx_quant(double x, int s, uint64_t* w)
@@ -34,10 +45,25 @@ extern "C" void fx_quant(double x, int s, uint64_t* w)
 	w[0] = a.w0; w[1] = a.w1; w[2] = a.w2;
 }
 
+// Adds the 256-bit count w[0..4) into table words t[0..PG_FX_WORDS); returns
+// whether the add marks the group present.
+extern "C" int fx_table_add(uint64_t* t, const uint64_t* w)
+{
+	const pg_fx4 a = {w[0], w[1], w[2], w[3]};
+	return pg_fx_table_add(t, 1, a, plain_add);
+}
+
+// The 256-bit count held by table words t[0..PG_FX_WORDS).
+extern "C" void fx_table_count(const uint64_t* t, uint64_t* w)
+{
+	const pg_fx4 a = pg_fx_from_table(t, 1);
+	w[0] = a.w0; w[1] = a.w1; w[2] = a.w2; w[3] = a.w3;
+}
+
 extern "C" double fx_double(const uint64_t* w, int s)
 {
-	const pg_fx3 a = {w[0], w[1], w[2]};
-	return pg_fx_double(a, s);
+	const pg_fx4 a = {w[0], w[1], w[2], w[3]};
+	return pg_fx_double4(a, s);
 }
 
 extern "C" uint64_t fx_special_bits(uint32_t flags) { return pg_fx_special_bits(flags); }

@@ -668,7 +668,7 @@ def test_groupby_dec_independent_of_row_order(gbctx):
     assert np.array_equal(canon(ctx.groupby(rows, val=(8, "dec"), agg="sum")), first)
     assert np.array_equal(canon(ctx.groupby(rows[::-1], val=(8, "dec"), agg="sum", groups_hint=2000)), first)
     try:
-        ctx.tune(groupby_ilp=4)                     # four rows in flight per thread: same bits
+        ctx.tune(groupby_ilp=8)                     # eight rows in flight per thread: same bits
         assert np.array_equal(canon(ctx.groupby(rows[perm], val=(8, "dec"), agg="sum")), first)
     finally:
         ctx.tune(groupby_ilp=0)
