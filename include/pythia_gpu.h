@@ -344,9 +344,9 @@ int pg_hashjoin_probe_where(pg_ctx* ctx, pg_stream stream, pg_hashtable* ht, con
  * (the "alwayszero" plan). Output rows: (key, agg) packed; agg is int32 for
  * an int sum (wrapping, as the reference's CtInt +=), int64 for a long sum or
  * a count, double for a dec sum. Integer results are exact; dec sums are exact
- * 192-bit fixed-point sums rounded once (the correctly rounded sum whenever the
- * values lie within about 2^109 of the column's largest; the same bits in any
- * row order); infinities and NaNs give IEEE's result for their groups.
+ * fixed-point sums rounded once (the correctly rounded sum whenever the values
+ * lie within 2^133 of the column's largest; the same bits in any row order);
+ * infinities and NaNs give IEEE's result for their groups.
  * groups_hint sizes the table (0: n).                                      */
 /* ---------------------------------------------------------------------- */
 enum { PG_VAL_INT = 0, PG_VAL_LONG = 1, PG_VAL_DEC = 2 };
