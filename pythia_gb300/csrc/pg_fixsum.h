@@ -230,6 +230,38 @@ PG_FX_HD bool pg_fx_table_add(uint64_t* t, uint64_t stride, const pg_fx4& a, ADD
 	return mark;
 }
 
+// A compact four-word form for tables in shared memory, where returning
+// adds are cheap: t[0], t[1] unsigned, t[2] signed, t[3] its overflows, the
+// sum being t3 2^192 + t2 2^128 + t1 2^64 + t0. Each add returns the old word,
+// whose overflow is the carry into the next word.
+template <class ADD>
+PG_FX_HD void pg_fx_chain_add(uint64_t* t, uint64_t stride, const pg_fx4& a, ADD add)
+{
+	uint64_t c = 0;
+	if (a.w0) {
+		const uint64_t old = add(t, a.w0);
+		c = old + a.w0 < old;
+	}
+	const uint64_t x1 = a.w1 + c;
+	c = x1 < c;
+	if (x1) {
+		const uint64_t old = add(t + stride, x1);
+		c += old + x1 < old;
+	}
+	const uint64_t l = a.w2 + c;                           // the rest: (a3 + carry) 2^192 + l 2^128
+	uint64_t q = a.w3 + (l < c) + (l >> 63);
+	const int64_t r = (int64_t) l;
+	if (r) q += pg_fx_overflow(add(t + 2 * stride, (uint64_t) r), r);
+	if (q) add(t + 3 * stride, q);
+}
+
+// The count held by a four-word chained table t[k * stride].
+PG_FX_HD pg_fx4 pg_fx_from_chain(const uint64_t* t, uint64_t stride)
+{
+	const uint64_t t2 = t[2 * stride];
+	return pg_fx4{t[0], t[stride], t2, t[3 * stride] - (t2 >> 63)};
+}
+
 PG_FX_HD void pg_fx_neg4(pg_fx4& a)
 {
 	a.w0 = ~a.w0; a.w1 = ~a.w1; a.w2 = ~a.w2; a.w3 = ~a.w3;

@@ -278,11 +278,12 @@ k_gb_insert_ilp(const char* __restrict__ in, uint64_t n, uint32_t W, uint32_t ko
 // excess keys to the global table (emitted afterwards).
 // ---------------------------------------------------------------------------
 #define GBP_THREADS 512
-// Slots of a partition's shared-memory table: 4096 (64 KB), or 1024 for dec
-// sums (key and seven count words per slot: 64 KB), so that three CTAs share
-// an SM; a partition holds about 1K groups, or 512 for dec sums.
-#define GBP_SLOTS (GB_DEC ? 1024u : 4096u)
-#define GBP_GROUPS (GB_DEC ? 512u : 1024u)
+// Slots of a partition's shared-memory table: 4096 (64 KB, three CTAs per
+// SM), or 2048 for dec sums (key and the four words of the chained form,
+// pg_fx_chain_add: 80 KB, two CTAs per SM); a partition holds about 1K groups
+// either way.
+#define GBP_SLOTS (GB_DEC ? 2048u : 4096u)
+#define GBP_GROUPS 1024u
 
 // Slot of key k in a per-partition table: low bits of the mix (the top bits
 // are the partition number).
@@ -330,7 +331,7 @@ k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, 
 	extern __shared__ __align__(16) unsigned char sm[];
 	constexpr uint32_t SW = GBP_SLOTS + 1;                                         // a dec sum's word stride
 	unsigned long long* skeys = reinterpret_cast<unsigned long long*>(sm);        // [SLOTS + 1]
-	unsigned long long* sacc = skeys + SW;                                         // [SLOTS + 1], PG_FX_WORDS [SLOTS + 1] for dec
+	unsigned long long* sacc = skeys + SW;                                         // [SLOTS + 1], 4 [SLOTS + 1] for dec
 	__shared__ int s_sent;
 	__shared__ uint32_t wtot[GBP_THREADS / 32];
 	__shared__ unsigned long long s_base;
@@ -341,8 +342,7 @@ k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, 
 	for (uint32_t part = blockIdx.x; part < P; part += gridDim.x) {
 		for (uint32_t i = tid; i <= GBP_SLOTS; i += blockDim.x) {
 			skeys[i] = (unsigned long long) PG_EMPTY_KEY; sacc[i] = 0;
-			if (GB_DEC)
-				for (int w = 1; w < PG_FX_WORDS; ++w) sacc[i + w * SW] = 0;
+			if (GB_DEC) { sacc[i + SW] = 0; sacc[i + 2 * SW] = 0; sacc[i + 3 * SW] = 0; }
 		}
 		if (tid == 0) s_sent = 0;
 		__syncthreads();
@@ -367,7 +367,11 @@ k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, 
 				continue;
 			}
 			const uint32_t s = gbp_slot<GBP_SLOTS>(skeys, k, &s_sent);
-			if (s != UINT32_MAX) { fold_slot<VT, AGG>(sacc, SW, s, v); continue; }
+			if (s != UINT32_MAX) {
+				if (GB_DEC) pg_fx_atomic_chain_add(&sacc[s], SW, v.f);
+				else fold_slot<VT, AGG>(sacc, SW, s, v);
+				continue;
+			}
 			// Shared table full: this key lives in the global table.
 			const uint64_t g = gb_slot(t.keys, t.log2cap, k, t.sentinel_used);
 			if (g == UINT64_MAX) { pg_set_status(status, PG_ERR_TABLE_FULL); continue; }
@@ -398,7 +402,8 @@ k_gb_part_agg(const char* __restrict__ rows, const uint64_t* __restrict__ offs, 
 			if (!used) continue;
 			if (pos < out_cap)
 				gb_write_agg<VT, AGG>(out + pos * ow, kbytes, i < GBP_SLOTS ? (int64_t) skeys[i] : PG_EMPTY_KEY,
-						sacc[i], GB_DEC ? gb_table_count(sacc, SW, i) : pg_fx4{0, 0, 0, 0}, fs);
+						sacc[i], GB_DEC ? pg_fx_from_chain(reinterpret_cast<const uint64_t*>(sacc + i), SW)
+						                : pg_fx4{0, 0, 0, 0}, fs);
 			++pos;
 		}
 		__syncthreads();
@@ -964,8 +969,8 @@ static int gb_run(pg_ctx* ctx, cudaStream_t s, const pg_rel* in, uint32_t voff, 
 			fn.fn = PG_FN_MIXRADIX; fn.k = 0; fn.min = 0; fn.max = 0; fn.bucketrange = 0;
 			fn.skipbits = 64 - lp; fn.nbuckets = P;
 			if ((rc = pg_partition_fn(ctx, s, in, fn, prow, poffs))) return rc;
-			const size_t psm = (size_t) (GBP_SLOTS + 1) * (GB_DEC ? 8 * (1 + PG_FX_WORDS) : 16);
-			const int pblocks = (int) std::min<uint64_t>(P, (uint64_t) ctx->sm_count * 3);   // 64 KB tables: 3 per SM
+			const size_t psm = (size_t) (GBP_SLOTS + 1) * (GB_DEC ? 40 : 16);
+			const int pblocks = (int) std::min<uint64_t>(P, (uint64_t) ctx->sm_count * (GB_DEC ? 2 : 3));   // CTAs per SM
 			if (path == 4) {
 				PG_CUDA(ctx, cudaFuncSetAttribute(k_gb_part_agg<VT, AGG, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) psm));
 				k_gb_part_agg<VT, AGG, false><<<pblocks, GBP_THREADS, psm, s>>>(prow, poffs, P, in->width, in->key_off,

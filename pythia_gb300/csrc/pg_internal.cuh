@@ -402,6 +402,15 @@ __device__ __forceinline__ bool pg_fx_atomic_add(unsigned long long* t, uint64_t
 	});
 }
 
+// Adds count a into a four-word chained table (pg_fx_chain_add) with atomics:
+// for tables in shared memory.
+__device__ __forceinline__ void pg_fx_atomic_chain_add(unsigned long long* t, uint64_t stride, const pg_fx4& a)
+{
+	pg_fx_chain_add(reinterpret_cast<uint64_t*>(t), stride, a, [](uint64_t* p, uint64_t v) {
+		return (uint64_t) atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long) v);
+	});
+}
+
 // The same for ILP rows at once: word k of row j's group at base[slot[j] *
 // sstride + k * wstride]. The low bits' chunks of the rows (values far below
 // the column's largest) go to the lazy words first, with adds that return

@@ -60,6 +60,19 @@ extern "C" void fx_table_count(const uint64_t* t, uint64_t* w)
 	w[0] = a.w0; w[1] = a.w1; w[2] = a.w2; w[3] = a.w3;
 }
 
+// The same for the four-word chained form of shared-memory tables.
+extern "C" void fx_chain_add(uint64_t* t, const uint64_t* w)
+{
+	const pg_fx4 a = {w[0], w[1], w[2], w[3]};
+	pg_fx_chain_add(t, 1, a, plain_add);
+}
+
+extern "C" void fx_chain_count(const uint64_t* t, uint64_t* w)
+{
+	const pg_fx4 a = pg_fx_from_chain(t, 1);
+	w[0] = a.w0; w[1] = a.w1; w[2] = a.w2; w[3] = a.w3;
+}
+
 extern "C" double fx_double(const uint64_t* w, int s)
 {
 	const pg_fx4 a = {w[0], w[1], w[2], w[3]};

@@ -39,6 +39,8 @@ def fx(tmp_path_factory):
     L.fx_table_add.argtypes, L.fx_table_add.restype = [ctypes.POINTER(U64), ctypes.POINTER(U64)], ctypes.c_int
     L.fx_table_count.argtypes = [ctypes.POINTER(U64), ctypes.POINTER(U64)]
     L.fx_words.restype = ctypes.c_int
+    L.fx_chain_add.argtypes = [ctypes.POINTER(U64), ctypes.POINTER(U64)]
+    L.fx_chain_count.argtypes = [ctypes.POINTER(U64), ctypes.POINTER(U64)]
     L.fx_special_bits.argtypes, L.fx_special_bits.restype = [ctypes.c_uint32], U64
     return L
 
@@ -164,7 +166,8 @@ def test_table_adds_hold_the_exact_sum(fx):
     # Values at the top of the bound's binade overflow the signed word t2
     # every few adds (one add into t3); values far below the largest add
     # 28-bit chunks into the lazy words; runs of one sign, cancellation and
-    # wide sums (warp-combined counts) end on the exact total in any order.
+    # wide sums (warp-combined counts) end on the exact total in any order, in
+    # the global tables' form and in the chained form of shared-memory tables.
     rng = np.random.default_rng(8)
     top = 1 << 188
     for trial in range(40):
@@ -187,6 +190,11 @@ def test_table_adds_hold_the_exact_sum(fx):
             marks = [fx.fx_table_add(t, words(v)) for v in seq]
             assert table_total(fx, t) == want, (trial, order)
             assert marks[0] == 1                          # the first add returns the initial 0 (or makes none)
+            c, w = (U64 * 4)(), (U64 * 4)()               # the chained form of shared-memory tables
+            for v in seq:
+                fx.fx_chain_add(c, words(v))
+            fx.fx_chain_count(c, w)
+            assert signed256(w) == want, (trial, order)
 
 
 def test_special_results(fx):
