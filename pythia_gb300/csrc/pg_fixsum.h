@@ -127,19 +127,6 @@ PG_FX_HD pg_fx3 pg_fx_quant(uint64_t b, int s)
 	return r;
 }
 
-// a += b, modulo 2^192.
-PG_FX_HD void pg_fx_add(pg_fx3& a, const pg_fx3& b)
-{
-	const uint64_t l = a.w0 + b.w0;
-	uint64_t c = l < a.w0;
-	a.w0 = l;
-	const uint64_t m = a.w1 + b.w1;
-	const uint64_t c1 = m < a.w1;
-	a.w1 = m + c;
-	c = c1 + (a.w1 < c);
-	a.w2 += b.w2 + c;
-}
-
 // The 256-bit count of a value's 192-bit one (sign-extended).
 PG_FX_HD pg_fx4 pg_fx_widen(const pg_fx3& a)
 {
