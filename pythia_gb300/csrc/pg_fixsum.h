@@ -30,8 +30,11 @@
 // value near the column's largest, whose low bits are zero, costs one
 // returning atomic, t2 overflows only about once per 2^(64 - PG_FX_TOP) such
 // values, and values far below the largest add fire-and-forget chunks.
-// Host and device: the host test checks quantisation, the table adds and the
-// rounding against exact rational arithmetic.
+// Tables in shared memory, where returning adds are cheap, use a compact
+// four-word chained form instead (pg_fx_chain_add).
+//
+// Host and device: the host test checks quantisation, both table forms' adds
+// and the rounding against exact rational arithmetic.
 #ifndef PG_FIXSUM_H
 #define PG_FIXSUM_H
 
